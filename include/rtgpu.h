@@ -1,0 +1,288 @@
+/*
+ * rtgpu.h -- C ABI of the GB300 light-transport core (librtgpu.so).
+ *
+ * The library replaces the per-sample render loop of Iscandel/Raytracer for
+ * its two path-tracing integrators (PathTracingMIS, VolPathTracing).  A host
+ * plugin flattens an initialised reference Scene into the plain structs below
+ * and calls these entry points; nothing here uses C++ types, exceptions or
+ * torch types.  Every entry point returns an rt_status; rt_last_error()
+ * returns a thread-local description of the last failure.
+ *
+ * Reference interfaces each entry point stands in for (paths relative to
+ * RaytracerNew2/src):
+ *   rt_scene_create  Scene::initialize              core/Scene.cpp:115-138
+ *                    (Bvh build Bvh.cpp:51-79, light init
+ *                     EnvironmentLight.cpp:256-262, Integrator::initialize
+ *                     integrator/Integrator.cpp:24-38, Mesh CDF Mesh.cpp:8-32,
+ *                     Heterogeneous::setOwnerBBox Heterogeneous.cpp:281-369)
+ *   rt_render        Scene::compute render step     core/Scene.cpp:83-101
+ *                    + SampleJob::run               core/SampleJob.cpp:28-72
+ *                    + Integrator::li (PathTracingMIS.cpp:27-262,
+ *                      VolPathTracing.cpp:25-367)
+ *                    + Screen::addSample/merge      core/Screen.cpp:44-97,136-157
+ *   rt_trace         Scene::computeIntersection     core/Scene.cpp:106-113
+ *                    (Bvh::intersection Bvh.cpp:392-481)
+ *   rt_bsdf_query    BSDF::eval/sample/pdf          bsdf/BSDF.h
+ *   rt_light_query   Light::sample/pdf/le           light/Light.h
+ *   rt_medium_query  Medium::sampleDistance/transmittance  medium/Medium.h
+ */
+#ifndef RTGPU_H
+#define RTGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RTGPU_ABI_VERSION 1
+
+typedef int32_t rt_status;
+enum {
+    RT_OK = 0,
+    RT_ERR_INVALID = 1,     /* bad argument or malformed scene            */
+    RT_ERR_CUDA = 2,        /* a CUDA runtime call failed                 */
+    RT_ERR_LIMIT = 3,       /* a device loop hit its iteration cap        */
+    RT_ERR_NOMEM = 4,       /* device or host allocation failed           */
+    RT_ERR_UNSUPPORTED = 5  /* feature not provided by this build         */
+};
+
+/* ------------------------------------------------------------------ */
+/* Scene description (host memory, caller-owned, read during create)  */
+/* All matrices are 4x4 row-major float[16], applied to column        */
+/* vectors exactly as core/Transform.h:90-99 applies them.            */
+/* ------------------------------------------------------------------ */
+
+enum { RT_BSDF_DIFFUSE = 0, RT_BSDF_ROUGH_CONDUCTOR = 1,
+       RT_BSDF_ROUGH_DIELECTRIC = 2, RT_BSDF_SMOOTH_LAYERED = 3 };
+/* bsdf/MicrofacetDistribution.h:9-13 name order */
+enum { RT_DIST_BECKMANN = 0, RT_DIST_PHONG = 1, RT_DIST_GGX = 2 };
+
+typedef struct rt_bsdf_desc {
+    int32_t type;            /* RT_BSDF_*                                        */
+    int32_t distribution;    /* RT_DIST_* (rough conductor / dielectric)         */
+    float albedo[3];         /* Diffuse albedo; SmoothLayered: base Diffuse albedo */
+    float reflectance[3];    /* "reflectanceTexture" (constant), default 1       */
+    float transmittance[3];  /* "transmittedTexture" (constant), default 1       */
+    float eta[3];            /* RoughConductor eta                               */
+    float k[3];              /* RoughConductor absorption                        */
+    float alpha;             /* "alpha" (constant texture), default 0.2          */
+    float eta_int;           /* default 1.5046                                   */
+    float eta_ext;           /* default 1.000277                                 */
+    float thickness;         /* SmoothLayered, default 1.2                       */
+    float absorbance[3];     /* SmoothLayered, default 0                         */
+} rt_bsdf_desc;
+
+/* One reference Mesh (factory/MeshFactory.h:39-139): a contiguous range of
+ * triangles with one BSDF, an optional area light and its media. */
+typedef struct rt_mesh_desc {
+    int32_t first_tri;
+    int32_t n_tris;
+    int32_t bsdf;            /* index into bsdfs, -1 = no BSDF (null boundary)   */
+    int32_t light;           /* index into lights, -1 = not emissive             */
+    int32_t interior;        /* index into media, -1 = none                      */
+    int32_t exterior;        /* index into media, -1 = none                      */
+} rt_mesh_desc;
+
+/* Analytic sphere (geometricShape/Sphere.cpp), object space centred at 0. */
+typedef struct rt_sphere_desc {
+    float radius;
+    float to_world[16];
+    float to_object[16];     /* inverse of to_world                              */
+    int32_t bsdf, light, interior, exterior;
+} rt_sphere_desc;
+
+enum { RT_LIGHT_AREA = 0,    /* AreaLight / MeshLight bound to a shape           */
+       RT_LIGHT_ENV = 1 };   /* EnvironmentLight (lat-long map)                  */
+enum { RT_SHAPE_MESH = 0, RT_SHAPE_SPHERE = 1 };
+
+typedef struct rt_light_desc {
+    int32_t type;            /* RT_LIGHT_*                                       */
+    int32_t mesh_light;      /* 1: MeshLight::sample (light/MeshLight.cpp:32-64),
+                                0: AreaLight::sample (light/AreaLight.cpp:31-55) */
+    int32_t shape_kind;      /* RT_SHAPE_*                                       */
+    int32_t shape;           /* mesh or sphere index                             */
+    float radiance[3];
+    /* environment map: width*height RGB floats, row-major (y*W+x)              */
+    int32_t env_width, env_height;
+    const float *env_rgb;
+    float env_scale;         /* "scale"                                          */
+    float env_to_world[16];  /* "toWorld"                                        */
+    float env_to_light[16];  /* inverse of env_to_world                          */
+} rt_light_desc;
+
+enum { RT_MEDIUM_HOMOGENEOUS = 0, RT_MEDIUM_HETEROGENEOUS = 1 };
+enum { RT_PHASE_ISOTROPIC = 0, RT_PHASE_HG = 1 };
+
+typedef struct rt_medium_desc {
+    int32_t type;            /* RT_MEDIUM_*                                      */
+    int32_t phase;           /* RT_PHASE_*                                       */
+    float g;                 /* HG asymmetry                                     */
+    float sigma_a[3];        /* Homogeneous                                      */
+    float sigma_s[3];        /* Homogeneous                                      */
+    float scale;             /* both types                                       */
+    float albedo[3];         /* Heterogeneous                                    */
+    int32_t res[3];          /* GridVolume resolution                            */
+    const float *density;    /* res[0]*res[1]*res[2] floats, x fastest           */
+    float grid_min[3];       /* GridVolume bounding box from the .vol header     */
+    float grid_max[3];
+    float to_world[16];      /* Heterogeneous "toWorld"                          */
+    int32_t centered;        /* Heterogeneous "centered" (default 1)             */
+} rt_medium_desc;
+
+typedef struct rt_camera_desc {
+    int32_t width, height;
+    float sample_to_camera[16];  /* NoriPerspective.cpp:32-34                    */
+    float camera_to_world[16];   /* Camera world transform                       */
+    float near_clip, far_clip;
+    float aperture_radius;       /* 0 = pinhole                                  */
+    float focal_plane;
+    int32_t medium;              /* camera medium or -1                          */
+} rt_camera_desc;
+
+typedef struct rt_scene_desc {
+    int32_t n_vertices;
+    const float *vertices;       /* 3 floats per vertex, world space             */
+    const float *normals;        /* 3 floats per vertex or NULL (face normals)   */
+    int32_t n_triangles;
+    const int32_t *indices;      /* 3 vertex indices per triangle                */
+    int32_t n_meshes;
+    const rt_mesh_desc *meshes;
+    int32_t n_spheres;
+    const rt_sphere_desc *spheres;
+    int32_t n_bsdfs;
+    const rt_bsdf_desc *bsdfs;
+    int32_t n_lights;
+    const rt_light_desc *lights; /* scene light order (Scene::getLights)          */
+    int32_t env_light;           /* index of the environment light or -1         */
+    int32_t n_media;
+    const rt_medium_desc *media;
+    rt_camera_desc camera;
+} rt_scene_desc;
+
+/* ------------------------------------------------------------------ */
+/* Render description                                                  */
+/* ------------------------------------------------------------------ */
+enum { RT_INTEGRATOR_PATH_MIS = 0, RT_INTEGRATOR_VOLPATH = 1 };
+/* integrator/Integrator.h:11-15 strategy names */
+enum { RT_STRATEGY_ALL_LIGHTS = 0, RT_STRATEGY_ONE_LIGHT_UNIFORM = 1,
+       RT_STRATEGY_ONE_LIGHT_WEIGHTED = 2 };
+
+typedef struct rt_render_desc {
+    int32_t integrator;      /* RT_INTEGRATOR_*                                  */
+    int32_t max_depth;       /* "maxDepth" (default 1000)                        */
+    int32_t min_depth;       /* "minDepth" (default 3)                           */
+    int32_t strategy;        /* RT_STRATEGY_*                                    */
+    int32_t spp;             /* samples per pixel rendered by this call          */
+    int32_t sample_begin;    /* first sample index (progressive rendering)       */
+    uint64_t seed;           /* path-stream sampler seed                         */
+    int32_t block_x, block_y;/* tile size of the reference job grid (default 32) */
+    int32_t flags;           /* reserved, 0                                      */
+} rt_render_desc;
+
+/* Per-path sample stream ("PathStreamSampler"): path (pixel p, sample s)
+ * draws from a PCG32 (tools/Rng.h:81-141) seeded with
+ *   initstate = rt_mix64((seed << 32) ^ p), initseq = s
+ * where p = y*width + x and rt_mix64 is the splitmix64 finaliser.  The
+ * draw order per path follows SampleJob.cpp:49-58 and the integrators. */
+
+typedef struct rt_ray {
+    float o[3]; float mint;
+    float d[3]; float maxt;
+} rt_ray;
+
+typedef struct rt_hit {
+    float t;
+    float u, v;              /* barycentrics of the hit (Triangle.cpp:73,78)     */
+    int32_t prim;            /* triangle index, or -(sphere index)-2, -1 = miss  */
+} rt_hit;
+
+/* BSDF point queries in the local shading frame (test hook). */
+enum { RT_BSDF_OP_EVAL = 0, RT_BSDF_OP_PDF = 1, RT_BSDF_OP_SAMPLE = 2 };
+typedef struct rt_bsdf_q {
+    float wi[3];
+    float wo[3];             /* eval / pdf                                       */
+    float u[2];              /* sample                                           */
+} rt_bsdf_q;
+typedef struct rt_bsdf_r {
+    float value[3];          /* eval value, or sample weight                     */
+    float pdf;
+    float wo[3];             /* sampled direction                                */
+    float relative_eta;
+    int32_t sampled_type;    /* BSDF::BSDFType bits (bsdf/BSDF.h)                */
+    int32_t pad;
+} rt_bsdf_r;
+
+/* Light queries (test hook): sample light `light` from point p with u. */
+typedef struct rt_light_q {
+    float p[3];
+    float u[2];
+} rt_light_q;
+typedef struct rt_light_r {
+    float intensity[3];
+    float pdf;
+    float to_light[3];
+    float distance;
+    float point[3];
+    float normal[3];
+    float pdf_eval;          /* Light::pdf(p, infos) for the sampled point       */
+    float pad;
+} rt_light_r;
+
+typedef struct rt_render_stats {
+    double kernel_ms;        /* summed device time of the last render (events)   */
+    double trace_ms;         /* of which closest/any-hit traversal               */
+    int64_t paths;           /* path samples rendered                            */
+    int64_t closest_rays;    /* closest-hit rays traced                          */
+    int64_t shadow_rays;     /* any-hit rays traced                              */
+    int64_t launches;        /* kernels launched by the last render              */
+    int64_t limit_hits;      /* device loops that hit their cap                  */
+    int64_t nan_samples;     /* samples dropped as NaN (Screen.cpp:46-50)        */
+} rt_render_stats;
+
+typedef struct rt_ctx rt_ctx;
+typedef struct rt_scene rt_scene;
+
+/* Library ------------------------------------------------------------ */
+int32_t rt_abi_version(void);
+const char *rt_last_error(void);
+uint64_t rt_mix64(uint64_t x);
+
+/* Context: one device, one CUDA stream.  Not thread-safe. */
+rt_status rt_ctx_create(int32_t device, rt_ctx **out);
+rt_status rt_ctx_destroy(rt_ctx *ctx);
+/* Optional stream override (cudaStream_t passed as an opaque pointer). */
+rt_status rt_ctx_set_stream(rt_ctx *ctx, void *stream);
+
+/* Scene: flatten + BVH build on the host, upload to device memory. */
+rt_status rt_scene_create(rt_ctx *ctx, const rt_scene_desc *desc, rt_scene **out);
+rt_status rt_scene_destroy(rt_scene *scene);
+/* Scene axis-aligned bounds (min xyz, max xyz) and device bytes held. */
+rt_status rt_scene_info(const rt_scene *scene, float bounds[6], int64_t *device_bytes,
+                        int32_t *bvh_nodes);
+
+/* Render spp samples per pixel starting at sample_begin; film_rgbw receives
+ * width*height*4 floats (rgb sum, weight), accumulated in sample order, in
+ * host memory (on_device = 0) or device memory (on_device = 1).  The film is
+ * overwritten, not accumulated into. */
+rt_status rt_render(rt_ctx *ctx, rt_scene *scene, const rt_render_desc *rd,
+                    float *film_rgbw, int32_t on_device);
+rt_status rt_render_stats_get(const rt_ctx *ctx, rt_render_stats *out);
+
+/* Trace n rays (closest hit, or any hit when anyhit != 0). */
+rt_status rt_trace(rt_ctx *ctx, rt_scene *scene, const rt_ray *rays, int32_t n,
+                   int32_t anyhit, rt_hit *hits, int32_t on_device);
+
+/* Evaluate BSDF `bsdf` of the scene for n queries (host arrays). */
+rt_status rt_bsdf_query(rt_ctx *ctx, rt_scene *scene, int32_t bsdf, int32_t op,
+                        const rt_bsdf_q *q, int32_t n, rt_bsdf_r *r);
+
+/* Sample light `light` (Light::sample + Light::pdf) for n queries. */
+rt_status rt_light_query(rt_ctx *ctx, rt_scene *scene, int32_t light,
+                         const rt_light_q *q, int32_t n, rt_light_r *r);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RTGPU_H */

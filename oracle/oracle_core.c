@@ -1,0 +1,1082 @@
+/*
+ * CPU oracle, part 1: math, sampler, BSDFs, lights, camera, media.
+ * TEST INFRASTRUCTURE ONLY -- see oracle.h.  Reference paths are relative to
+ * RaytracerNew2/src of Iscandel/Raytracer.
+ */
+#include "oracle.h"
+
+#include <stdlib.h>
+#include <string.h>
+
+/* ===================== transforms ===================== */
+/* core/Transform.h:90-99: explicit row sums, then divide by w if w != 0,1 */
+v3 xf_point(const float *m, v3 p)
+{
+    v3 o;
+    o.x = m[0] * p.x + m[1] * p.y + m[2] * p.z + m[3];
+    o.y = m[4] * p.x + m[5] * p.y + m[6] * p.z + m[7];
+    o.z = m[8] * p.x + m[9] * p.y + m[10] * p.z + m[11];
+    float w = m[12] * p.x + m[13] * p.y + m[14] * p.z + m[15];
+    if (w != 1.f && w != 0.f) o = v3_divs(o, w);
+    return o;
+}
+
+/* core/Transform.h:118-125: topLeftCorner<3,3>() * v */
+v3 xf_vector(const float *m, v3 v)
+{
+    return mk3(m[0] * v.x + m[1] * v.y + m[2] * v.z,
+               m[4] * v.x + m[5] * v.y + m[6] * v.z,
+               m[8] * v.x + m[9] * v.y + m[10] * v.z);
+}
+
+/* core/Transform.h:181-189: inverse.topLeftCorner<3,3>().transpose() * n */
+v3 xf_normal(const float *inv, v3 n)
+{
+    return mk3(inv[0] * n.x + inv[4] * n.y + inv[8] * n.z,
+               inv[1] * n.x + inv[5] * n.y + inv[9] * n.z,
+               inv[2] * n.x + inv[6] * n.y + inv[10] * n.z);
+}
+
+/* ===================== PCG32 (tools/Rng.h:57-141) ===================== */
+#define O_PCG_MULT 0x5851f42d4c957f2dULL
+
+uint32_t o_pcg_next(o_pcg32 *r)
+{
+    uint64_t old = r->state;
+    r->state = old * O_PCG_MULT + r->inc;
+    uint32_t xs = (uint32_t)(((old >> 18u) ^ old) >> 27u);
+    uint32_t rot = (uint32_t)(old >> 59u);
+    return (xs >> rot) | (xs << ((~rot + 1u) & 31));
+}
+
+void o_pcg_seed(o_pcg32 *r, uint64_t initstate, uint64_t initseq)
+{
+    r->state = 0u;
+    r->inc = (initseq << 1u) | 1u;
+    o_pcg_next(r);
+    r->state += initstate;
+    o_pcg_next(r);
+}
+
+/* Rng.h:132-141: mantissa trick, [1,2) - 1 */
+float o_pcg_float(o_pcg32 *r)
+{
+    union { uint32_t u; float f; } x;
+    x.u = (o_pcg_next(r) >> 9) | 0x3f800000u;
+    return x.f - 1.0f;
+}
+
+/* splitmix64 finaliser used to derive per-path initial states */
+uint64_t o_mix64(uint64_t x)
+{
+    x ^= x >> 30; x *= 0xbf58476d1ce4e5b9ULL;
+    x ^= x >> 27; x *= 0x94d049bb133111ebULL;
+    x ^= x >> 31;
+    return x;
+}
+
+/* Path-stream sampler: one PCG32 stream per (pixel, sample); the draw
+ * interface matches sampler/RandomSampler.cpp:28-38 with x drawn first. */
+void o_sampler_seed_path(o_sampler *s, uint64_t seed, uint32_t pixel, uint32_t sample)
+{
+    o_pcg_seed(&s->rng, o_mix64((seed << 32) ^ (uint64_t)pixel), (uint64_t)sample);
+}
+float o_next1d(o_sampler *s) { return o_pcg_float(&s->rng); }
+v2 o_next2d(o_sampler *s)
+{
+    float a = o_pcg_float(&s->rng);
+    float b = o_pcg_float(&s->rng);
+    return mk2(a, b);
+}
+
+/* ===================== CDF (core/CDF.h:14-81) ===================== */
+void o_cdf_init(o_cdf *c)
+{
+    c->cap = 16;
+    c->cdf = (float *)malloc(sizeof(float) * c->cap);
+    c->cdf[0] = 0.f;
+    c->n = 1;
+    c->sum = 0.f;
+    c->normalized = 0;
+}
+void o_cdf_free(o_cdf *c) { free(c->cdf); c->cdf = NULL; c->n = 0; }
+
+void o_cdf_add(o_cdf *c, float pdf)
+{
+    c->sum += pdf;
+    if (c->n == c->cap) { c->cap *= 2; c->cdf = (float *)realloc(c->cdf, sizeof(float) * c->cap); }
+    c->cdf[c->n++] = c->sum;
+}
+
+void o_cdf_normalize(o_cdf *c)
+{
+    if (c->sum != 0.f) {
+        float factor = 1.f / c->sum;
+        for (int i = 1; i < c->n; i++) c->cdf[i] *= factor;
+        c->cdf[c->n - 1] = 1.f;
+        c->normalized = 1;
+    }
+}
+
+/* lower_bound, then clamp to [0, size-2] (CDF.h:44-50) */
+int o_cdf_sample(const o_cdf *c, float u)
+{
+    int lo = 0, hi = c->n;
+    while (lo < hi) {
+        int mid = lo + (hi - lo) / 2;
+        if (c->cdf[mid] < u) lo = mid + 1; else hi = mid;
+    }
+    int index = imax(0, lo - 1);
+    return imin(index, c->n - 2);
+}
+int o_cdf_sample_pdf(const o_cdf *c, float u, float *pdf)
+{
+    int i = o_cdf_sample(c, u);
+    *pdf = c->cdf[i + 1] - c->cdf[i];
+    return i;
+}
+int o_cdf_sample_reuse(const o_cdf *c, float *u)
+{
+    int i = o_cdf_sample(c, *u);
+    *u = (*u - c->cdf[i]) / (c->cdf[i + 1] - c->cdf[i]);
+    return i;
+}
+int o_cdf_sample_reuse_pdf(const o_cdf *c, float *u, float *pdf)
+{
+    int i = o_cdf_sample_reuse(c, u);
+    *pdf = c->cdf[i + 1] - c->cdf[i];
+    return i;
+}
+
+/* ===================== warps (core/Mapping.h) ===================== */
+/* Mapping.h:110-140 */
+static v2 o_square_to_concentric_disk(v2 s)
+{
+    const float r1 = 2 * s.x - 1.f;
+    const float r2 = 2 * s.y - 1.f;
+    float rx, ry;
+    if (r1 > -r2 && r1 > r2) { rx = r1; ry = (O_PI * r2) / (4 * r1); }
+    else if (r1 < r2 && r1 > -r2) { rx = r2; ry = (O_PI / 4.f) * (2 - r1 / r2); }
+    else if (r1 < -r2 && r1 < r2) { rx = -r1; ry = (O_PI / 4.f) * (4 + r2 / r1); }
+    else { rx = -r2; ry = (O_PI / 4.f) * (6 - r1 / r2); }
+    return mk2(rx * cosf(ry), rx * sinf(ry));
+}
+/* Mapping.h:62-67 */
+static v3 o_square_to_cosine_hemisphere(v2 s)
+{
+    v2 t = o_square_to_concentric_disk(s);
+    float z = sqrtf(smax(0.f, 1.f - t.x * t.x - t.y * t.y));
+    return mk3(t.x, t.y, z);
+}
+/* Mapping.h:94-105 */
+static v3 o_square_to_triangle(v2 s)
+{
+    float sq = sqrtf(s.x);
+    return mk3(1 - sq, (1 - s.y) * sq, s.y * sq);
+}
+/* Mapping.h:145-164 */
+static v3 o_square_to_uniform_sphere(v2 s)
+{
+    float phi = 2.f * O_PI * s.x;
+    float u = 2 * s.y - 1.f;
+    float st = sqrtf(1.f - u * u);
+    return v3_normalized(mk3(st * cosf(phi), st * sinf(phi), u));
+}
+/* Mapping.h:199-202 */
+static float o_uniform_cone_pdf(float cos_theta) { return 1.f / (2 * O_PI * (1.f - cos_theta)); }
+
+/* core/Geometry.h:163-190 */
+static float o_spherical_phi(v3 v)
+{
+    float r = atan2f(v.x, -v.z);
+    return r < 0.f ? r + 2 * (float)3.14159265358979323846 : r;
+}
+static float o_spherical_theta(v3 v) { return acosf(v.y); }
+static v3 o_cartesian_from_spherical(float theta, float phi)
+{
+    float st = sinf(theta), ct = cosf(theta), cp = cosf(phi), sp = sinf(phi);
+    return mk3(sp * st, ct, -cp * st);
+}
+
+/* ===================== Fresnel (core/Fresnel.h) ===================== */
+/* Fresnel.h:30-49 (per channel) */
+static float o_fresnel_conductor1(float eta, float k, float cosI)
+{
+    float epa = eta * eta + k * k;
+    float cos2 = cosI * cosI;
+    float epac2 = epa * cos2;
+    float two = 2 * eta * cosI;
+    float rpar = (epac2 - two + 1) / (epac2 + two + 1);
+    float rperp = (epa - two + cos2) / (epa + two + cos2);
+    return (rpar * rpar + rperp * rperp) * 0.5f;
+}
+/* Fresnel.h:51-63 */
+static float o_fresnel_dielectric(float etaI, float etaT, float cosI, float cosT)
+{
+    float tcI = etaT * cosI, icT = etaI * cosT, icI = etaI * cosI, tcT = etaT * cosT;
+    float rpar = (tcI - icT) / (tcI + icT);
+    float rperp = (icI - tcT) / (icI + tcT);
+    return (rpar * rpar + rperp * rperp) * 0.5f;
+}
+/* Fresnel.h:83-114: returns the (grey) reflectance; all channels equal */
+static float o_estimate_dielectric(float etaExt, float etaInt, float cosI,
+                                   float *etaI, float *etaT, float *relEta, float *cosT)
+{
+    *etaI = etaExt; *etaT = etaInt;
+    int entering = 1;
+    float fr;
+    if (cosI <= 0.f) { entering = 0; float t = *etaI; *etaI = *etaT; *etaT = t; }
+    *relEta = *etaI / *etaT;
+    float sinT = *relEta * sqrtf(smax(0.f, 1 - cosI * cosI));
+    *cosT = sqrtf(smax(0.f, 1 - sinT * sinT));
+    if (sinT >= 1.f) { *cosT = 0.f; fr = 1.f; }
+    else {
+        fr = o_fresnel_dielectric(*etaI, *etaT, fabsf(cosI), *cosT);
+        if (entering) *cosT = -*cosT;
+    }
+    return fr;
+}
+/* .average() of the grey Color returned by estimateDielectric */
+static float o_fr_avg(float f) { return c3_avg(cfill(f)); }
+
+/* ===================== microfacet (bsdf/MicrofacetDistribution.cpp) ===================== */
+static float o_cos2(v3 v) { return v.z * v.z; }
+static float o_sin2(v3 v) { return 1.f - v.z * v.z; }
+static float o_sin(v3 v) { float s2 = o_sin2(v); if (s2 < 0.f) return 0.f; return sqrtf(s2); }
+static float o_tan2(v3 v) { float s2 = 1.f - v.z * v.z; if (s2 <= 0.f) return 0.f; return s2 / (v.z * v.z); }
+
+/* MicrofacetDistribution.cpp:29-52 */
+static v3 o_mf_sample_normal(int type, v2 s, float alpha)
+{
+    float theta;
+    if (type == RT_DIST_BECKMANN) theta = atanf(sqrtf(-alpha * alpha * logf(1 - s.x)));
+    else if (type == RT_DIST_GGX) theta = atanf(alpha * sqrtf(s.x) / sqrtf(1.f - s.x));
+    else theta = acosf(powf(s.x, 1.f / (alpha + 2)));
+    float phi = 2 * O_PI * s.y;
+    return mk3(sinf(theta) * cosf(phi), sinf(theta) * sinf(phi), cosf(theta));
+}
+/* MicrofacetDistribution.cpp:54-87 */
+static float o_mf_D(int type, v3 wh, float alpha)
+{
+    if (wh.z <= 0.f) return 0.f;
+    if (type == RT_DIST_BECKMANN) {
+        float c2 = wh.z * wh.z;
+        float t2 = o_sin2(wh) / c2;
+        float a2 = alpha * alpha;
+        return expf(-t2 / a2) / (O_PI * a2 * c2 * c2);
+    } else if (type == RT_DIST_GGX) {
+        float a2 = alpha * alpha;
+        float c2 = o_cos2(wh);
+        float t2 = o_tan2(wh);
+        float ss = a2 + t2;
+        return a2 / (O_PI * c2 * c2 * ss * ss);
+    }
+    return ((alpha + 2.f) / (2 * O_PI)) * powf(wh.z, alpha);
+}
+/* MicrofacetDistribution.cpp:105-159 */
+static float o_mf_G1(int type, v3 v, v3 m, float alpha)
+{
+    if (v3_dot(v, m) / v.z <= 0) return 0.f;
+    if (type == RT_DIST_BECKMANN) {
+        float tanv = o_sin(v) / v.z;
+        if (tanv == 0.f) return 1.f;
+        float b = fabsf(1.f / (alpha * tanv));
+        if (b < 1.6f) return (3.535f * b + 2.181f * b * b) / (1 + 2.276f * b + 2.577f * b * b);
+        return 1.f;
+    } else if (type == RT_DIST_GGX) {
+        float a2 = alpha * alpha;
+        float t2 = o_tan2(v);
+        return 2.f / (1 + sqrtf(1 + a2 * t2));
+    }
+    float tanv = o_sin(v) / v.z;
+    float b = sqrtf(0.5f * alpha + 1) / tanv;
+    if (b < 1.6f) return (3.535f * b + 2.181f * b * b) / (1 + 2.276f * b + 2.577f * b * b);
+    return 1.f;
+}
+static float o_mf_G(int type, v3 wi, v3 wo, v3 wh, float alpha)
+{
+    return o_mf_G1(type, wi, wh, alpha) * o_mf_G1(type, wo, wh, alpha);
+}
+/* MicrofacetDistribution.h:43-46 */
+static float o_adjusted_alpha(float alpha, float cosI)
+{
+    return (1.2f - 0.2f * sqrtf(fabsf(cosI))) * alpha;
+}
+static float o_sign(float v) { return v >= 0.f ? 1.f : -1.f; }
+
+/* bsdf/BSDF.h reflect/refract helpers */
+static v3 o_reflect_local(v3 v) { return mk3(-v.x, -v.y, v.z); }
+static v3 o_reflect_n(v3 v, v3 n) { float d = 2 * v3_dot(v, n); return v3_sub(v3_smul(d, n), v); }
+static v3 o_refract_local(v3 v, float cosT, float rel) { return mk3(rel * -v.x, rel * -v.y, cosT); }
+static v3 o_refract_n(v3 v, v3 n, float rel, float cosT)
+{
+    float s = v3_dot(v, n) * rel + cosT;
+    return v3_sub(v3_muls(n, s), v3_muls(v, rel));
+}
+/* RoughDielectric.h:32-35 (both branches negate) */
+static v3 o_half_dir_transmitted(v3 wi, v3 wo, float etaI, float etaT)
+{
+    v3 s = v3_add(v3_smul(etaI, wi), v3_smul(etaT, wo));
+    return v3_normalized(v3_smul(-1.f, s));
+}
+
+/* ===================== Diffuse (bsdf/Diffuse.cpp:28-106) ===================== */
+static c3 o_diffuse_eval(const float *albedo, v3 wi, v3 wo)
+{
+    if (wi.z <= 0.f || wo.z <= 0.f) return cfill(0.f);
+    return c3_muls(c3_from(albedo), O_INV_PI);
+}
+static float o_diffuse_pdf(v3 wi, v3 wo)
+{
+    if (wi.z <= 0.f || wo.z <= 0.f) return 0.f;
+    return O_INV_PI * wo.z;
+}
+static c3 o_diffuse_sample(const float *albedo, o_bsdf_rec *r, v2 s)
+{
+    if (r->wi.z <= 0.f) return cfill(0.f);
+    r->sampled_type = O_BSDF_DIFFUSE;
+    r->wo = o_square_to_cosine_hemisphere(s);
+    r->pdf = o_diffuse_pdf(r->wi, r->wo);
+    return c3_from(albedo);
+}
+
+/* ===================== RoughConductor (bsdf/RoughConductor.cpp:77-145) ===================== */
+static c3 o_rc_eval(const rt_bsdf_desc *b, v3 wi, v3 wo)
+{
+    float ci = wi.z, co = wo.z;
+    if (ci <= 0.f || co <= 0.f) return cfill(0.f);
+    v3 wh = v3_normalized(v3_add(wi, wo));
+    float a = c3_avg(cfill(b->alpha));
+    float D = o_mf_D(b->distribution, wh, a);
+    float G = o_mf_G(b->distribution, wi, wo, wh, a);
+    c3 F = mkc(o_fresnel_conductor1(b->eta[0], b->k[0], ci),
+               o_fresnel_conductor1(b->eta[1], b->k[1], ci),
+               o_fresnel_conductor1(b->eta[2], b->k[2], ci));
+    float den = 4 * ci * co;
+    c3 r = c3_muls(c3_from(b->reflectance), D);
+    r = c3_mul(r, F);
+    r = c3_muls(r, G);
+    return c3_divs(r, den);
+}
+static float o_rc_pdf(const rt_bsdf_desc *b, v3 wi, v3 wo)
+{
+    float ci = wi.z, co = wo.z;
+    if (ci <= 0.f || co <= 0.f) return 0.f;
+    v3 wh = v3_normalized(v3_add(wi, wo));
+    float ch = wh.z;
+    float Jh = 1.f / (4 * fabsf(v3_dot(wh, wo)));
+    float D = o_mf_D(b->distribution, wh, c3_avg(cfill(b->alpha)));
+    return D * ch * Jh;
+}
+static c3 o_rc_sample(const rt_bsdf_desc *b, o_bsdf_rec *r, v2 s)
+{
+    if (r->wi.z <= 0.f) return cfill(0.f);
+    r->sampled_type = O_BSDF_GLOSSY_REFLECTION;
+    float alpha = o_adjusted_alpha(c3_avg(cfill(b->alpha)), r->wi.z);
+    v3 n = o_mf_sample_normal(b->distribution, s, alpha);
+    r->wo = o_reflect_n(r->wi, n);
+    float co = r->wo.z;
+    if (co <= 0.f) return cfill(0.f);
+    r->pdf = o_rc_pdf(b, r->wi, r->wo);
+    if (r->pdf <= 0) return cfill(0.f);
+    c3 e = o_rc_eval(b, r->wi, r->wo);
+    return c3_divs(c3_muls(e, fabsf(co)), r->pdf);
+}
+
+/* ===================== RoughDielectric (bsdf/RoughDielectric.cpp:83-329) ===================== */
+static c3 o_rd_eval_reflection(const rt_bsdf_desc *b, v3 wi, v3 wo)
+{
+    float ci = wi.z, co = wo.z;
+    v3 wh = v3_normalized(v3_add(wi, wo));
+    wh = v3_smul(o_sign(ci), wh);
+    float alpha = c3_avg(cfill(b->alpha));
+    float D = o_mf_D(b->distribution, wh, alpha);
+    float eI, eT, rel, cT;
+    float fr = o_estimate_dielectric(b->eta_ext, b->eta_int, v3_dot(wi, wh), &eI, &eT, &rel, &cT);
+    float G = o_mf_G(b->distribution, wi, wo, wh, alpha);
+    float den = 4 * ci * co;
+    c3 r = c3_muls(c3_from(b->reflectance), D);
+    r = c3_muls(r, fr);
+    r = c3_muls(r, G);
+    return c3_divs(r, den);
+}
+static c3 o_rd_eval_refraction(const rt_bsdf_desc *b, v3 wi, v3 wo)
+{
+    float ci = wi.z, co = wo.z;
+    float eI, eT, rel, cT;
+    float fr = o_estimate_dielectric(b->eta_ext, b->eta_int, ci, &eI, &eT, &rel, &cT);
+    v3 wt = o_half_dir_transmitted(wi, wo, eI, eT);
+    float alpha = c3_avg(cfill(b->alpha));
+    float left = v3_dot(wi, wt) * v3_dot(wo, wt) / (ci * co);
+    float G = o_mf_G(b->distribution, wi, wo, wt, alpha);
+    float D = o_mf_D(b->distribution, wt, alpha);
+    float one_m_fr = (-1.f * fr) + 1.f;
+    c3 term = c3_muls(c3_from(b->transmittance), left);
+    term = c3_muls(term, eT);
+    term = c3_muls(term, eT);
+    term = c3_muls(term, one_m_fr);
+    term = c3_muls(term, G);
+    term = c3_muls(term, D);
+    term = c3_muls(term, rel);
+    term = c3_muls(term, rel);
+    float denom = eI * v3_dot(wi, wt) + eT * v3_dot(wo, wt);
+    return c3_divs(term, denom * denom);
+}
+static float o_rd_pdf_reflection(const rt_bsdf_desc *b, v3 wi, v3 wo)
+{
+    float ci = wi.z;
+    float alpha = (1.2f - 0.2f * sqrtf(fabsf(ci))) * c3_avg(cfill(b->alpha));
+    v3 wh = v3_normalized(v3_add(wi, wo));
+    wh = v3_smul(o_sign(ci), wh);
+    float ch = wh.z;
+    float Jh = 1.f / (4 * v3_dot(wh, wo));
+    return fabsf(o_mf_D(b->distribution, wh, alpha) * ch * Jh);
+}
+static float o_rd_pdf_refraction(const rt_bsdf_desc *b, v3 wi, v3 wo)
+{
+    float ci = wi.z;
+    float eI, eT, rel, cT;
+    o_estimate_dielectric(b->eta_ext, b->eta_int, ci, &eI, &eT, &rel, &cT);
+    v3 wt = o_half_dir_transmitted(wi, wo, eI, eT);
+    float cwt = wt.z;
+    float alpha = (1.2f - 0.2f * sqrtf(fabsf(ci))) * c3_avg(cfill(b->alpha));
+    float hd = eI * v3_dot(wi, wt) + eT * v3_dot(wo, wt);
+    float Jh = (eT * eT * v3_dot(wo, wt)) / (hd * hd);
+    return fabsf(o_mf_D(b->distribution, wt, alpha) * cwt * Jh);
+}
+static c3 o_rd_eval(const rt_bsdf_desc *b, v3 wi, v3 wo)
+{
+    if (wi.z * wo.z > 0) return o_rd_eval_reflection(b, wi, wo);
+    return o_rd_eval_refraction(b, wi, wo);
+}
+static float o_rd_pdf(const rt_bsdf_desc *b, v3 wi, v3 wo)
+{
+    float ci = wi.z, co = wo.z;
+    float eI, eT, rel, cT;
+    if (ci * co > 0) {
+        v3 wh = v3_normalized(v3_add(wi, wo));
+        wh = v3_smul(o_sign(ci), wh);
+        float fr = o_fr_avg(o_estimate_dielectric(b->eta_ext, b->eta_int, v3_dot(wi, wh), &eI, &eT, &rel, &cT));
+        return o_rd_pdf_reflection(b, wi, wo) * fr;
+    }
+    float etaI = b->eta_ext, etaT = b->eta_int;
+    if (ci < 0) { float t = etaI; etaI = etaT; etaT = t; }
+    v3 wt = o_half_dir_transmitted(wi, wo, etaI, etaT);
+    float fr = o_fr_avg(o_estimate_dielectric(b->eta_ext, b->eta_int, v3_dot(wi, wt), &eI, &eT, &rel, &cT));
+    return o_rd_pdf_refraction(b, wi, wo) * (1.f - fr);
+}
+static c3 o_rd_sample(const rt_bsdf_desc *b, o_bsdf_rec *r, v2 s)
+{
+    float ci = r->wi.z;
+    float alpha = o_adjusted_alpha(c3_avg(cfill(b->alpha)), ci);
+    v3 n = o_mf_sample_normal(b->distribution, s, alpha);
+    float eI, eT, rel, cT;
+    float fr = o_fr_avg(o_estimate_dielectric(b->eta_ext, b->eta_int, v3_dot(r->wi, n), &eI, &eT, &rel, &cT));
+    if (s.x <= fr) {
+        r->sampled_type = O_BSDF_GLOSSY_REFLECTION;
+        r->wo = o_reflect_n(r->wi, n);
+        if (r->wi.z * r->wo.z <= 0) return cfill(0.f);
+        r->pdf = o_rd_pdf_reflection(b, r->wi, r->wo) * fr;
+        if (r->pdf <= 0) return cfill(0.f);
+        v3 wh = v3_normalized(v3_add(r->wi, r->wo));
+        wh = v3_smul(o_sign(ci), wh);
+        float G = o_mf_G(b->distribution, r->wi, r->wo, wh, alpha);
+        float v = 1.f * v3_dot(r->wi, n);
+        v = v * G;
+        return cfill(v / (ci * n.z));
+    }
+    r->sampled_type = O_BSDF_GLOSSY_TRANSMISSION;
+    r->wo = v3_normalized(o_refract_n(r->wi, n, rel, cT));
+    r->relative_eta = rel;
+    float co = v3_dot(r->wo, n);
+    if (r->wi.z * r->wo.z >= 0) return cfill(0.f);
+    r->pdf = o_rd_pdf_refraction(b, r->wi, r->wo) * (1.f - fr);
+    if (r->pdf <= 0) return cfill(0.f);
+    c3 e = o_rd_eval_refraction(b, r->wi, r->wo);
+    return c3_divs(c3_muls(e, fabsf(co)), r->pdf);
+}
+
+/* ===================== SmoothLayered (bsdf/SmoothLayeredBSDF.cpp:139-403) ===================== */
+static c3 o_absorb(const rt_bsdf_desc *b, float wip, float wop)
+{
+    float s = 1.f / fabsf(wip) + 1.f / fabsf(wop);
+    return mkc(expf((-b->absorbance[0] * b->thickness) * s),
+               expf((-b->absorbance[1] * b->thickness) * s),
+               expf((-b->absorbance[2] * b->thickness) * s));
+}
+static c3 o_sl_eval(const rt_bsdf_desc *b, v3 wi, v3 wo)
+{
+    if (wi.z <= 0.f || wo.z <= 0.f) return cfill(0.f);
+    float ci = wi.z;
+    float eI, eT, rel, cT;
+    float fr1 = o_fr_avg(o_estimate_dielectric(b->eta_ext, b->eta_int, ci, &eI, &eT, &rel, &cT));
+    float T12 = 1.f - fr1;
+    if (fr1 == 1.f) return cfill(0.f);
+    v3 rwi = v3_normalized(o_refract_local(wi, cT, rel));
+    v3 rwo = v3_normalized(o_refract_local(wo, cT, rel));
+    rwi = v3_neg(rwi);
+    rwo = v3_neg(rwo);
+    ci = v3_neg(rwo).z;
+    float fr2 = o_fr_avg(o_estimate_dielectric(b->eta_ext, b->eta_int, ci, &eI, &eT, &rel, &cT));
+    if (fr2 == 1.f) return cfill(0.f);
+    float T21 = 1.f - fr2;
+    c3 f2 = o_diffuse_eval(b->albedo, rwi, rwo);
+    c3 a = o_absorb(b, rwi.z, rwo.z);
+    float G = 1.f;
+    float t = (1.f - G) + T21 * G;
+    float m = b->eta_ext / b->eta_int;
+    c3 r = mkc(T12 * f2.r, T12 * f2.g, T12 * f2.b);
+    r = c3_mul(r, a);
+    r = c3_muls(r, t);
+    r = c3_muls(r, m);
+    r = c3_muls(r, m);
+    r = c3_muls(r, wo.z);
+    r = c3_divs(r, rwo.z);
+    return c3_add(cfill(0.f), r);
+}
+static float o_sl_pdf(const rt_bsdf_desc *b, v3 wi, v3 wo)
+{
+    float ci = wi.z;
+    float eI, eT, rel, cT;
+    float fr1 = o_fr_avg(o_estimate_dielectric(b->eta_ext, b->eta_int, ci, &eI, &eT, &rel, &cT));
+    if (fr1 == 1.f) return 0.f;
+    v3 rwi = v3_normalized(o_refract_local(wi, cT, rel));
+    v3 rwo = v3_normalized(o_refract_local(wo, cT, rel));
+    rwi = v3_neg(rwi);
+    rwo = v3_neg(rwo);
+    float pbase = o_diffuse_pdf(rwi, rwo);
+    float m = b->eta_ext / b->eta_int;
+    return 0.f + pbase * (1.f - fr1) * m * m * wo.z / rwo.z;
+}
+static c3 o_sl_sample(const rt_bsdf_desc *b, o_bsdf_rec *r, v2 s)
+{
+    if (r->wi.z <= 0.f) return cfill(0.f);
+    float ci = r->wi.z;
+    r->sampled_type = O_BSDF_GLOSSY_REFLECTION;
+    float eI, eT, rel, cT;
+    float fr1 = o_fr_avg(o_estimate_dielectric(b->eta_ext, b->eta_int, ci, &eI, &eT, &rel, &cT));
+    if (fr1 == 1.f) return cfill(0.f);
+    if (s.x <= fr1) {
+        r->wo = o_reflect_local(r->wi);
+        r->pdf = fr1;
+        r->sampled_type = O_BSDF_DELTA_REFLECTION;
+        return cfill(1.f);
+    }
+    v3 rwi = v3_normalized(v3_neg(o_refract_local(r->wi, cT, rel)));
+    r->sampled_type = O_BSDF_UNKNOWN;
+    float T12 = 1.f - fr1;
+    o_bsdf_rec base;
+    base.wi = rwi; base.wo = mk3(0, 0, 0); base.sampled_type = O_BSDF_ALL;
+    base.relative_eta = 1.f; base.pdf = -1.f;
+    c3 f2 = o_diffuse_sample(b->albedo, &base, s);
+    if (c3_iszero(f2)) return cfill(0.f);
+    r->pdf = (1.f - fr1);
+    if (r->pdf <= 0.f) return cfill(0.f);
+    r->wo = v3_neg(base.wo);
+    float wip = rwi.z;
+    float wop = v3_neg(base.wo).z;
+    c3 a = o_absorb(b, wip, wop);
+    ci = r->wo.z;
+    float fr2 = o_fr_avg(o_estimate_dielectric(b->eta_ext, b->eta_int, ci, &eI, &eT, &rel, &cT));
+    if (fr2 == 1.f) return cfill(0.f);
+    float T21 = 1.f - fr2;
+    r->wo = v3_normalized(o_refract_local(r->wo, cT, rel));
+    float co = r->wo.z;
+    c3 res = mkc(T12 * f2.r, T12 * f2.g, T12 * f2.b);
+    res = c3_mul(res, a);
+    res = c3_muls(res, T21);
+    res = c3_add(cfill(0.f), res);
+    res = c3_muls(res, fabsf(co));
+    res = c3_divs(res, r->pdf);
+    float m = b->eta_ext / b->eta_int;
+    r->pdf *= base.pdf * m * m * r->wo.z / wop;
+    return res;
+}
+
+/* ===================== BSDF dispatch ===================== */
+c3 o_bsdf_eval(const rt_bsdf_desc *b, const o_bsdf_rec *r)
+{
+    switch (b->type) {
+    case RT_BSDF_DIFFUSE: return o_diffuse_eval(b->albedo, r->wi, r->wo);
+    case RT_BSDF_ROUGH_CONDUCTOR: return o_rc_eval(b, r->wi, r->wo);
+    case RT_BSDF_ROUGH_DIELECTRIC: return o_rd_eval(b, r->wi, r->wo);
+    case RT_BSDF_SMOOTH_LAYERED: return o_sl_eval(b, r->wi, r->wo);
+    }
+    return cfill(0.f);
+}
+float o_bsdf_pdf(const rt_bsdf_desc *b, const o_bsdf_rec *r)
+{
+    switch (b->type) {
+    case RT_BSDF_DIFFUSE: return o_diffuse_pdf(r->wi, r->wo);
+    case RT_BSDF_ROUGH_CONDUCTOR: return o_rc_pdf(b, r->wi, r->wo);
+    case RT_BSDF_ROUGH_DIELECTRIC: return o_rd_pdf(b, r->wi, r->wo);
+    case RT_BSDF_SMOOTH_LAYERED: return o_sl_pdf(b, r->wi, r->wo);
+    }
+    return 0.f;
+}
+c3 o_bsdf_sample(const rt_bsdf_desc *b, o_bsdf_rec *r, v2 s)
+{
+    switch (b->type) {
+    case RT_BSDF_DIFFUSE: return o_diffuse_sample(b->albedo, r, s);
+    case RT_BSDF_ROUGH_CONDUCTOR: return o_rc_sample(b, r, s);
+    case RT_BSDF_ROUGH_DIELECTRIC: return o_rd_sample(b, r, s);
+    case RT_BSDF_SMOOTH_LAYERED: return o_sl_sample(b, r, s);
+    }
+    return cfill(0.f);
+}
+
+/* ===================== shapes used by lights ===================== */
+static void o_tri_verts(const rt_scene_desc *d, int tri, v3 *p0, v3 *p1, v3 *p2)
+{
+    const int32_t *ix = d->indices + 3 * (size_t)tri;
+    *p0 = v3_from(d->vertices + 3 * (size_t)ix[0]);
+    *p1 = v3_from(d->vertices + 3 * (size_t)ix[1]);
+    *p2 = v3_from(d->vertices + 3 * (size_t)ix[2]);
+}
+
+/* Mesh::sample (geometricShape/Mesh.cpp:38-68) + Triangle::sample (Triangle.cpp:251-273) */
+static void o_mesh_sample(const o_scene *sc, int mesh, v2 s, v3 *pt, v3 *n)
+{
+    const rt_scene_desc *d = sc->d;
+    float ux = s.x;
+    int index = o_cdf_sample_reuse(&sc->mesh[mesh].cdf, &ux);
+    v2 s2 = mk2(ux, s.y);
+    int tri = d->meshes[mesh].first_tri + index;
+    v3 p0, p1, p2;
+    o_tri_verts(d, tri, &p0, &p1, &p2);
+    v3 b = o_square_to_triangle(s2);
+    *pt = v3_add(v3_add(v3_muls(p0, b.x), v3_muls(p1, b.y)), v3_muls(p2, b.z));
+    if (d->normals) {
+        const int32_t *ix = d->indices + 3 * (size_t)tri;
+        v3 n0 = v3_from(d->normals + 3 * (size_t)ix[0]);
+        v3 n1 = v3_from(d->normals + 3 * (size_t)ix[1]);
+        v3 n2 = v3_from(d->normals + 3 * (size_t)ix[2]);
+        *n = v3_normalized(v3_add(v3_add(v3_smul(b.x, n0), v3_smul(b.y, n1)), v3_smul(b.z, n2)));
+    } else {
+        *n = v3_normalized(v3_cross(v3_sub(p1, p0), v3_sub(p2, p0)));
+        *n = v3_normalized(*n);
+    }
+}
+/* Mesh::pdf (Mesh.cpp:70-93) */
+static float o_mesh_pdf(const o_scene *sc, int mesh, v3 p, v3 sampled, v3 n)
+{
+    v3 l = v3_sub(p, sampled);
+    float dist = v3_norm(l);
+    l = v3_normalized(l);
+    float c = v3_dot(n, l);
+    if (c > 0) return dist * dist / (sc->mesh[mesh].area * c);
+    return 0.f;
+}
+/* Sphere::normal (Sphere.cpp:27-34) */
+static v3 o_sphere_normal(const rt_sphere_desc *s, v3 p)
+{
+    v3 lp = xf_point(s->to_object, p);
+    return v3_normalized(v3_sub(lp, mk3(0, 0, 0)));
+}
+static float o_sphere_area(const rt_sphere_desc *s) { return 4.f * O_PI * s->radius * s->radius * s->radius; }
+/* Sphere::sample (Sphere.cpp:146-173) */
+static void o_sphere_sample(const rt_sphere_desc *s, v2 u, v3 *pt, v3 *n)
+{
+    float theta = 2.f * O_PI * u.x;
+    float phi = acosf(2 * u.y - 1.f);
+    float c = cosf(phi);
+    float sq = sqrtf(1 - c * c);
+    v3 p = mk3(sq * cosf(theta), sq * sinf(theta), c);
+    p = v3_muls(p, s->radius);
+    v3 nn = xf_normal(s->to_object, o_sphere_normal(s, p));
+    *n = v3_normalized(nn);
+    *pt = xf_point(s->to_world, p);
+}
+/* Sphere::pdf (Sphere.cpp:183-201) with the ISampledShape::pdf fallback (ISampledShape.cpp:17-40) */
+float o_sphere_light_pdf(const rt_sphere_desc *s, v3 p, v3 sampled, v3 n)
+{
+    v3 center = xf_point(s->to_world, mk3(0.f, 0.f, 0.f));
+    v3 itc = v3_sub(p, center);
+    float sqd = v3_sqnorm(itc);
+    if (v3_dot(n, itc) < 0.f) return 0.f;
+    if (sqd - s->radius * s->radius < O_EPSILON) {
+        v3 l = v3_sub(p, sampled);
+        float dist = v3_norm(l);
+        l = v3_normalized(l);
+        float c = v3_dot(n, l);
+        if (c >= 0) return dist * dist / (o_sphere_area(s) * c);
+        return 0.f;
+    }
+    float st2 = s->radius * s->radius / sqd;
+    float ct = sqrtf(smax(0.f, 1 - st2));
+    return o_uniform_cone_pdf(ct);
+}
+
+/* ===================== environment light (light/EnvironmentLight.cpp) ===================== */
+static c3 o_env_texel(const rt_light_desc *L, int x, int y)
+{
+    const float *p = L->env_rgb + 3 * ((size_t)y * L->env_width + x);
+    return c3_muls(c3_from(p), L->env_scale);
+}
+/* EnvironmentLight.cpp:265-275 */
+static void o_env_checkxy(const rt_light_desc *L, float *x, float *y)
+{
+    unsigned W = (unsigned)L->env_width, H = (unsigned)L->env_height;
+    if (*x >= (float)W) *x = (float)((unsigned)(int)*x % W) + (*x - (float)(int)*x);
+    else if (*x < 0) *x = (float)(W - (unsigned)abs((int)*x) % W) + (*x - (float)(int)*x);
+    if (*y >= (float)H) *y = (float)((unsigned)(int)*y % H) + (*y - (float)(int)*y);
+    else if (*y < 0) *y = (float)(H - (unsigned)abs((int)*y) % H) + (*y - (float)(int)*y);
+}
+static int o_clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+/* core/BasicMath.h:74-90 interp2 */
+static c3 o_env_interp(const rt_light_desc *L, float x, float y)
+{
+    int W = L->env_width, H = L->env_height;
+    float ax = x - (float)(int)x;
+    float ay = y - (float)(int)y;
+    int x0 = o_clampi((int)x, 0, W - 2);
+    int y0 = o_clampi((int)y, 0, H - 2);
+    int x1 = x0 + 1 < W ? x0 + 1 : x0; x1 = o_clampi(x1, 0, W - 1);
+    int y1 = y0 + 1 < H ? y0 + 1 : y0; y1 = o_clampi(y1, 0, H - 1);
+    const float *a00 = L->env_rgb + 3 * ((size_t)y0 * W + x0);
+    const float *a01 = L->env_rgb + 3 * ((size_t)y1 * W + x0);
+    const float *a10 = L->env_rgb + 3 * ((size_t)y0 * W + x1);
+    const float *a11 = L->env_rgb + 3 * ((size_t)y1 * W + x1);
+    float w00 = (1 - ax) * (1 - ay), w01 = (1 - ax) * ay, w10 = ax * (1 - ay), w11 = ax * ay;
+    c3 r;
+    r.r = ((w00 * a00[0] + w01 * a01[0]) + w10 * a10[0]) + w11 * a11[0];
+    r.g = ((w00 * a00[1] + w01 * a01[1]) + w10 * a10[1]) + w11 * a11[1];
+    r.b = ((w00 * a00[2] + w01 * a01[2]) + w10 * a10[2]) + w11 * a11[2];
+    return r;
+}
+static void o_env_dir_to_xy(const rt_light_desc *L, v3 dir, float *fx, float *fy)
+{
+    *fx = (o_spherical_phi(dir) / (2 * O_PI)) * (float)L->env_width;
+    *fy = (o_spherical_theta(dir) / O_PI) * (float)L->env_height;
+    /* offsetU/offsetV are 0 for every scene this core accepts */
+    *fx += 0.f * (float)L->env_width;
+    *fy += 0.f * (float)L->env_height;
+    o_env_checkxy(L, fx, fy);
+}
+/* EnvironmentLight.cpp:193-237 */
+c3 o_env_le(const o_scene *sc, int light, v3 direction)
+{
+    const rt_light_desc *L = &sc->d->lights[light];
+    v3 dir = v3_normalized(xf_vector(L->env_to_light, direction));
+    float fx, fy;
+    o_env_dir_to_xy(L, dir, &fx, &fy);
+    return c3_muls(o_env_interp(L, fx, fy), L->env_scale);
+}
+static float o_env_norm(const o_scene *sc, int light, int row)
+{
+    const rt_light_desc *L = &sc->d->lights[light];
+    const o_env_rt *E = &sc->env[light];
+    float den = E->marginal.sum * (2 * O_PI / (float)L->env_width);
+    den = den * (O_PI / (float)L->env_height);
+    return E->weight[row] / den;
+}
+/* EnvironmentLight.cpp:85-146 */
+static void o_env_sample(const o_scene *sc, int light, v3 p, v2 s, o_light_rec *out)
+{
+    const rt_light_desc *L = &sc->d->lights[light];
+    const o_env_rt *E = &sc->env[light];
+    float pr, pc;
+    int row = o_cdf_sample_pdf(&E->marginal, s.x, &pr);
+    int col = o_cdf_sample_pdf(&E->row[row], s.y, &pc);
+    float rcol = (float)col + 0.f * (float)L->env_width;
+    float rrow = (float)row + 0.f * (float)L->env_height;
+    o_env_checkxy(L, &rcol, &rrow);
+    row = (int)rrow;
+    col = (int)rcol;
+    float theta = O_PI * (float)row / (float)L->env_height;
+    float phi = 2 * O_PI * (float)col / (float)L->env_width;
+    float st = sinf(theta);
+    v3 dir = o_cartesian_from_spherical(theta, phi);
+    dir = xf_vector(L->env_to_world, dir);
+    out->distance = E->sphere_radius;
+    dir = v3_normalized(dir);
+    out->to_light = dir;
+    out->point = v3_add(p, v3_smul(E->sphere_radius, dir));
+    out->normal = mk3(0, 0, 0);
+    out->intensity = o_env_texel(L, o_clampi(col, 0, L->env_width - 1), o_clampi(row, 0, L->env_height - 1));
+    float pdf = c3_lum(out->intensity) * E->weight[row];
+    float den = E->marginal.sum * (2 * O_PI / (float)L->env_width);
+    den = den * (O_PI / (float)L->env_height);
+    pdf = pdf / den;
+    pdf /= smax(fabsf(st), O_EPSILON);
+    out->pdf = pdf;
+}
+/* EnvironmentLight.cpp:148-191 (sin of the pixel coordinate, as the reference does) */
+static float o_env_pdf(const o_scene *sc, int light, v3 to_light)
+{
+    const rt_light_desc *L = &sc->d->lights[light];
+    v3 dir = v3_normalized(xf_vector(L->env_to_light, to_light));
+    float fx, fy;
+    o_env_dir_to_xy(L, dir, &fx, &fy);
+    float st = sinf(fy);
+    float nf = o_env_norm(sc, light, (int)fy);
+    float lum = c3_lum(c3_muls(o_env_interp(L, fx, fy), L->env_scale));
+    float pdf = lum * nf;
+    pdf /= smax(fabsf(st), O_EPSILON);
+    return pdf;
+}
+
+/* ===================== light dispatch ===================== */
+void o_light_sample(const o_scene *sc, int light, v3 p, v2 s, o_light_rec *out)
+{
+    const rt_light_desc *L = &sc->d->lights[light];
+    out->light = light;
+    out->pdf = 0.f;
+    out->distance = 0.f;
+    out->intensity = cfill(0.f);
+    if (L->type == RT_LIGHT_ENV) { o_env_sample(sc, light, p, s, out); return; }
+    v3 pt, n;
+    if (L->shape_kind == RT_SHAPE_MESH) o_mesh_sample(sc, L->shape, s, &pt, &n);
+    else o_sphere_sample(&sc->d->spheres[L->shape], s, &pt, &n);
+    out->point = pt;
+    out->normal = n;
+    out->to_light = v3_sub(pt, p);
+    out->distance = v3_norm(out->to_light);
+    out->to_light = v3_divs(out->to_light, out->distance);
+    float c = v3_dot(n, v3_neg(out->to_light));
+    if (L->mesh_light && L->shape_kind == RT_SHAPE_MESH) {
+        /* MeshLight.cpp:42-61 */
+        if (c <= 0) { out->intensity = cfill(0.f); out->pdf = 0.f; }
+        else {
+            out->intensity = c3_from(L->radiance);
+            out->pdf = out->distance * out->distance / (sc->mesh[L->shape].area * c);
+        }
+    } else {
+        /* AreaLight.cpp:41-52 */
+        if (c < 0) { out->intensity = cfill(0.f); out->pdf = 0.f; }
+        else {
+            out->intensity = c3_from(L->radiance);
+            out->pdf = o_light_pdf(sc, light, p, out);
+        }
+    }
+}
+
+float o_light_pdf(const o_scene *sc, int light, v3 p, const o_light_rec *rec)
+{
+    const rt_light_desc *L = &sc->d->lights[light];
+    if (L->type == RT_LIGHT_ENV) return o_env_pdf(sc, light, rec->to_light);
+    if (L->shape_kind == RT_SHAPE_MESH) return o_mesh_pdf(sc, L->shape, p, rec->point, rec->normal);
+    return o_sphere_light_pdf(&sc->d->spheres[L->shape], p, rec->point, rec->normal);
+}
+
+/* ===================== camera (camera/NoriPerspective.cpp:80-118) ===================== */
+o_ray o_ray_make(v3 o, v3 d, float mint, float maxt)
+{
+    o_ray r;
+    r.o = o; r.d = d; r.mint = mint; r.maxt = maxt;
+    r.inv = mk3(1.f / d.x, 1.f / d.y, 1.f / d.z);
+    return r;
+}
+
+o_ray o_camera_ray(const rt_camera_desc *c, float px, float py, v2 lens)
+{
+    float invw = 1.f / (float)c->width, invh = 1.f / (float)c->height;
+    v3 nearP = xf_point(c->sample_to_camera, mk3(px * invw, py * invh, 0.0f));
+    v3 d = v3_normalized(nearP);
+    float invZ = 1.0f / d.z;
+    v3 o = mk3(0.f, 0.f, 0.f);
+    if (c->aperture_radius > 0.f) {
+        v2 s = o_square_to_concentric_disk(lens);
+        s.x *= c->aperture_radius; s.y *= c->aperture_radius;
+        o = mk3(s.x, s.y, 0.f);
+        float tdist = c->focal_plane * invZ;
+        v3 fp = v3_smul(tdist, d);
+        d = v3_normalized(v3_sub(fp, o));
+    }
+    v3 wo = xf_point(c->camera_to_world, o);
+    v3 wd = xf_vector(c->camera_to_world, d);
+    return o_ray_make(wo, wd, c->near_clip * invZ, c->far_clip * invZ);
+}
+
+/* ===================== phase functions ===================== */
+/* HGPhaseFunction.cpp:53-57 / IsotropicPhaseFunction */
+float o_phase_eval(const rt_medium_desc *m, v3 wi, v3 wo)
+{
+    if (m->phase == RT_PHASE_ISOTROPIC) return O_INV_FOUR_PI;
+    float g = m->g;
+    float c = v3_dot(v3_neg(wi), wo);
+    return O_INV_FOUR_PI * (1 - g * g) / powf(1 + g * g - 2 * g * c, 1.5f);
+}
+/* HGPhaseFunction.cpp:27-42 (world-frame direction, as the reference does) */
+float o_phase_sample(const rt_medium_desc *m, v3 wi, v2 u, v3 *wo, float *pdf)
+{
+    if (m->phase == RT_PHASE_ISOTROPIC) {
+        *wo = o_square_to_uniform_sphere(u);
+        *pdf = O_INV_FOUR_PI;
+        return 1.f;
+    }
+    float g = m->g;
+    float ct;
+    if (g < O_EPSILON) ct = 1.f - 2.f * u.x;
+    else ct = (1 + g * g - ((1 - g * g) * (1 - g * g) / (1 - g + 2 * g * u.x))) / (2 * g);
+    float theta = acosf(ct);
+    float phi = 2 * O_PI * u.y;
+    *wo = o_cartesian_from_spherical(theta, phi);
+    *pdf = o_phase_eval(m, wi, *wo);
+    return 1.f;
+}
+
+/* ===================== media ===================== */
+/* Homogeneous (medium/Homogeneous.cpp:6-78) */
+static c3 o_homog_sigma_t(const rt_medium_desc *m)
+{
+    c3 sa = c3_from(m->sigma_a), ss = c3_from(m->sigma_s);
+    if (m->scale != 1.f) { sa = c3_muls(sa, m->scale); ss = c3_muls(ss, m->scale); }
+    return c3_add(sa, ss);
+}
+static c3 o_homog_sigma_s(const rt_medium_desc *m)
+{
+    c3 ss = c3_from(m->sigma_s);
+    if (m->scale != 1.f) ss = c3_muls(ss, m->scale);
+    return ss;
+}
+static c3 o_homog_tr(const rt_medium_desc *m, float mint, float maxt)
+{
+    float t = maxt - mint;
+    c3 st = o_homog_sigma_t(m);
+    return mkc(expf(-st.r * t), expf(-st.g * t), expf(-st.b * t));
+}
+
+/* GridVolume::lookupSigmaT (volume/GridVolume.cpp:118-149) * scale */
+static float o_grid_lookup(const rt_medium_desc *m, v3 pa)
+{
+    float px = pa.x * (float)m->res[0], py = pa.y * (float)m->res[1], pz = pa.z * (float)m->res[2];
+    float fx = floorf(px), fy = floorf(py), fz = floorf(pz);
+    int ix = (int)fx, iy = (int)fy, iz = (int)fz;
+    if (ix < 0 || iy < 0 || iz < 0) return 0.0f * m->scale;
+    if (ix >= m->res[0] - 1 || iy >= m->res[1] - 1 || iz >= m->res[2] - 1) return 0.0f * m->scale;
+    size_t row = (size_t)m->res[0], slab = row * (size_t)m->res[1];
+    size_t off = (size_t)iz * slab + (size_t)iy * row + (size_t)ix;
+    const float *D = m->density;
+    float d000 = D[off], d001 = D[off + 1], d010 = D[off + row], d011 = D[off + row + 1];
+    float d100 = D[off + slab], d101 = D[off + slab + 1], d110 = D[off + slab + row], d111 = D[off + slab + row + 1];
+    float w1x = px - fx, w1y = py - fy, w1z = pz - fz;
+    float w0x = 1 - w1x, w0y = 1 - w1y, w0z = 1 - w1z;
+    float v = ((d000 * w0x + d001 * w1x) * w0y + (d010 * w0x + d011 * w1x) * w1y) * w0z +
+              ((d100 * w0x + d101 * w1x) * w0y + (d110 * w0x + d111 * w1x) * w1y) * w1z;
+    return v * m->scale;
+}
+
+/* BoundingBox::intersection (core/BoundingBox.h:154-183) */
+static int o_box_hit(const float *bmin, const float *bmax, const o_ray *r, float *nearT, float *farT)
+{
+    *nearT = -O_MAX_REAL;
+    *farT = O_MAX_REAL;
+    for (int i = 0; i < 3; i++) {
+        float o = v3_get(r->o, i), dd = v3_get(r->d, i), inv = v3_get(r->inv, i);
+        float mn = bmin[i], mx = bmax[i];
+        if (dd == 0) {
+            if (o < mn || o > mx) return 0;
+        } else {
+            float t1 = (mn - o) * inv;
+            float t2 = (mx - o) * inv;
+            if (t1 > t2) { float t = t1; t1 = t2; t2 = t; }
+            *nearT = smax(t1, *nearT);
+            *farT = smin(t2, *farT);
+            if (!(*nearT <= *farT)) return 0;
+        }
+    }
+    return (r->mint <= *farT && r->maxt >= *nearT);
+}
+
+static o_ray o_ray_xf(const float *m, const o_ray *r)
+{
+    return o_ray_make(xf_point(m, r->o), xf_vector(m, r->d), r->mint, r->maxt);
+}
+
+/* Heterogeneous::transmittance (medium/Heterogeneous.cpp:419-489) */
+static c3 o_hetero_tr(const o_scene *sc, int mi, const o_ray *wr, o_sampler *s)
+{
+    const rt_medium_desc *m = &sc->d->media[mi];
+    const o_medium_rt *M = &sc->med[mi];
+    o_ray ray = o_ray_xf(M->world_to_array, wr);
+    float tmax = ray.maxt - ray.mint;
+    float tr = 1.f;
+    float st = 0.f;
+    int breaker = 0;
+    float nearT, farT;
+    static const float bmin[3] = {0.f, 0.f, 0.f}, bmax[3] = {1.f, 1.f, 1.f};
+    if (!o_box_hit(bmin, bmax, &ray, &nearT, &farT)) return cfill(1.f);
+    tmax = smin(tmax, farT);
+    st = smax(nearT, ray.mint);
+    for (;;) {
+        st += -logf(1.f - o_next1d(s)) / M->max_sigma_t;
+        v3 pa = v3_add(ray.o, v3_smul(st, ray.d));
+        float proba = o_grid_lookup(m, pa);
+        if (st >= tmax) return cfill(tr);
+        tr *= 1 - smax(0.f, proba / M->max_sigma_t);
+        const float threshold = .1f;
+        if (tr < threshold) {
+            float q = smax(.05f, 1 - tr);
+            if (o_next1d(s) < q) return cfill(0.f);
+            tr /= 1 - q;
+        }
+        if (breaker > 1024) return cfill(0.f);
+        breaker++;
+    }
+}
+
+/* Heterogeneous::sampleDistance (medium/Heterogeneous.cpp:491-546) */
+static int o_hetero_sample(const o_scene *sc, int mi, const o_ray *wr, o_sampler *s,
+                           float *t, c3 *weight, c3 *emission)
+{
+    const rt_medium_desc *m = &sc->d->media[mi];
+    const o_medium_rt *M = &sc->med[mi];
+    o_ray ray = o_ray_xf(M->world_to_array, wr);
+    *t = ray.mint;
+    float cur = 0.f;
+    float nearT, farT;
+    if (!o_box_hit(M->wbox_min, M->wbox_max, wr, &nearT, &farT)) {
+        *weight = cfill(1.f); *emission = cfill(0.f); *t = ray.maxt;
+        return 0;
+    }
+    float tmax = smin(ray.maxt, farT);
+    for (;;) {
+        *t += -logf(1.f - o_next1d(s)) / M->max_sigma_t;
+        if (*t > tmax) {
+            *weight = cfill(1.f); *emission = cfill(0.f); *t = tmax;
+            return 0;
+        }
+        v3 pw = v3_add(wr->o, v3_smul(*t, wr->d));
+        cur = o_grid_lookup(m, xf_point(M->world_to_array, pw));
+        float proba = cur / M->max_sigma_t;
+        if (o_next1d(s) < proba) break;
+    }
+    if (cur != 0.f) { *weight = c3_from(m->albedo); *emission = cfill(0.f); }
+    else { *weight = cfill(0.f); *emission = cfill(0.f); }
+    return 1;
+}
+
+int o_medium_sample_distance(const o_scene *sc, int mi, const o_ray *ray, o_sampler *s,
+                             float *t, c3 *weight, c3 *emission)
+{
+    const rt_medium_desc *m = &sc->d->media[mi];
+    if (m->type == RT_MEDIUM_HETEROGENEOUS) return o_hetero_sample(sc, mi, ray, s, t, weight, emission);
+    /* Homogeneous::sampleDistance (Homogeneous.cpp:37-78) */
+    c3 st = o_homog_sigma_t(m);
+    int channel = (int)(o_next1d(s) * 3);
+    float ext = channel == 0 ? st.r : (channel == 1 ? st.g : st.b);
+    ext += O_EPSILON;
+    *t = -logf(1.f - o_next1d(s)) / ext;
+    if (*t > ray->maxt) {
+        *t = ray->maxt;
+        c3 e = mkc(expf(-st.r * *t), expf(-st.g * *t), expf(-st.b * *t));
+        float pdf = c3_avg(e);
+        *weight = c3_divs(o_homog_tr(m, ray->mint, ray->maxt), pdf);
+        *emission = cfill(0.f);
+        return 0;
+    }
+    c3 e = mkc(st.r * expf(-st.r * *t), st.g * expf(-st.g * *t), st.b * expf(-st.b * *t));
+    float pdf = c3_avg(e);
+    *t += ray->mint;
+    *weight = c3_divs(c3_mul(o_homog_sigma_s(m), o_homog_tr(m, ray->mint, *t)), pdf);
+    *emission = c3_div(cfill(0.f), st);
+    return 1;
+}
+
+c3 o_medium_transmittance(const o_scene *sc, int mi, const o_ray *ray, o_sampler *s)
+{
+    const rt_medium_desc *m = &sc->d->media[mi];
+    if (m->type == RT_MEDIUM_HETEROGENEOUS) return o_hetero_tr(sc, mi, ray, s);
+    return o_homog_tr(m, ray->mint, ray->maxt);
+}
