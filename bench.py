@@ -1,0 +1,329 @@
+"""Benchmark: path samples/s of the GB300 path tracer on the 1.31M-triangle
+displaced-icosphere scene (1024x1024, 64 spp, max depth 16, procedural sky),
+plus the reference CPU path (the oracle restatement) timed on the host.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
+
+A step is one full render of the scene: 1024*1024*64 = 67,108,864 path
+samples through PathTracingMIS.  `value` is measured with the scene and the
+film resident in device memory; `e2e` is the same render through the C ABI
+into a host film buffer (device->host film copy and the per-call host->device
+uploads inside the timed region).  Multi-GPU runs are weak-scaled replicas:
+rank r renders the same image with its own sample indices [r*spp, (r+1)*spp),
+no collective in the timed region.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CONFIG = dict(level=8, width=1024, height=1024, spp=64, max_depth=16, env=(1024, 512), seed=0)
+WORKLOAD = "displaced_icosphere_1310720tri_1024x1024_64spp_depth16_sky1024x512"
+METRIC = "path samples/s"
+UNIT = "samples/s"
+S_NODE = 64        # bytes per BVH2 node fetch (two child boxes + links)
+S_TRI = 36         # bytes per triangle test (three float3 vertices)
+S_RAY_IN = 32      # origin, direction, tmin, tmax
+S_HIT_OUT = 16     # t, u, v, triangle id
+
+
+def _peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+                for k, n in enumerate(names):
+                    if r[5 + k].lower() == "active":
+                        reasons.add(n)
+            except Exception:
+                continue
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_scene():
+    from raytracer_gb300 import scenes
+    return scenes.displaced_icosphere(level=CONFIG["level"], width=CONFIG["width"], height=CONFIG["height"],
+                                      seed=CONFIG["seed"], env_size=CONFIG["env"], max_depth=CONFIG["max_depth"])
+
+
+def cpu_oracle_rate(scene, target_s=15.0, threads=None):
+    """Time the CPU oracle (the reference path restated in C) on a bounded
+    sample: whole 32x32 tiles at the full spp, sized for about target_s."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib as O
+    threads = threads or os.cpu_count() or 1
+    t0 = time.time()
+    o = O.OracleScene(scene)
+    build_s = time.time() - t0
+    W, H = scene.camera["width"], scene.camera["height"]
+    tiles_x = (W + 31) // 32
+    ntiles = tiles_x * ((H + 31) // 32)
+    # calibration: one tile row of the image middle
+    mid = (ntiles // 2) - tiles_x // 2
+    cal = max(1, min(threads, 8))
+    t0 = time.time()
+    o.render_tiles(CONFIG["spp"], mid, mid + cal, seed=1, threads=threads)
+    dt = max(time.time() - t0, 1e-3)
+    per_tile = dt / cal * min(threads, cal) / threads
+    n = int(max(threads, min(ntiles, target_s / max(per_tile, 1e-4))))
+    n = max(1, min(n, ntiles))
+    start = max(0, ntiles // 2 - n // 2)
+    return o, start, n, build_s
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    scene = make_scene()
+    threads = os.cpu_count() or 1
+    o, start, n, build_s = cpu_oracle_rate(scene, target_s=args.cpu_seconds)
+    spp = CONFIG["spp"]
+    for _ in range(max(0, min(args.warmup, 1))):
+        o.render_tiles(spp, start, start + max(1, n // 8), seed=3, threads=threads)
+    times = []
+    for k in range(args.steps):
+        t0 = time.time()
+        o.render_tiles(spp, start, start + n, seed=4 + k, threads=threads)
+        times.append(time.time() - t0)
+    samples = n * 32 * 32 * spp
+    value = samples * len(times) / sum(times)
+    sample_desc = "%d of %d 32x32 tiles (%d path samples) per step, full 64 spp, %d threads" % (
+        n, (1024 // 32) ** 2, samples, threads)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * float(np.mean(times)),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded displaced icosphere + procedural sky)",
+            "config": {"workload": WORKLOAD, "integrator": "PathTracingMIS", "sample": sample_desc},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample_desc},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "notes": "reference CPU path = the oracle's C restatement of PathTracingMIS with the reference's "
+                     "two-level SAH BVH (the reference itself needs Eigen/SFML/OpenEXR/OpenVDB, absent here); "
+                     "oracle scene build %.1f s not timed" % build_s}
+    print(json.dumps(line))
+
+
+def run_gpu(args):
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from raytracer_gb300 import build as B
+    B.build()
+    import raytracer_gb300 as R
+    t0 = time.time()
+    data = make_scene()
+    gen_s = time.time() - t0
+    ctx = R.Context(local)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    t0 = time.time()
+    scene = R.Scene(ctx, data)
+    upload_s = time.time() - t0
+    info = scene.info()
+    W, H, spp = CONFIG["width"], CONFIG["height"], CONFIG["spp"]
+    film = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+    samples_per_step = W * H * spp
+    sbase = rank * spp
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # counting pass (traversal statistics for the roofline; not timed)
+    ctx.set_profiling(2)
+    scene.render(8, seed=99, film=film.data_ptr())
+    cstats = ctx.stats()
+    ctx.set_profiling(1)
+    for _ in range(args.warmup):
+        scene.render(spp, seed=7, sample_begin=sbase, film=film.data_ptr())
+    barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    agg = {}
+    launches = 0
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    barrier()
+    e0.record(stream)
+    for k in range(args.steps):
+        scene.render(spp, seed=1000 + k, sample_begin=sbase, film=film.data_ptr())
+        st = ctx.stats()
+        launches += st["launches"]
+        for key in ("trace_closest_ms", "trace_any_ms", "shade_ms", "camera_ms", "film_ms", "closest_rays",
+                    "shadow_rays", "trace_closest_launches", "trace_any_launches", "paths", "nan_samples"):
+            agg[key] = agg.get(key, 0) + st[key]
+    e1.record(stream)
+    barrier()
+    clk = clocks.stop()
+    dev_ms = e0.elapsed_time(e1)
+    t_local = dev_ms / 1000.0
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([t_local], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_local = float(t.item())
+    value = samples_per_step * args.steps * world / t_local
+    # end to end through the C ABI with a host film
+    ctx.set_profiling(0)
+    host_film = None
+    barrier()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        host_film = scene.render(spp, seed=2000 + k, sample_begin=sbase)
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    e2e_value = samples_per_step * args.steps * world / e2e_s
+    d2h = W * H * 16
+    h2d = 64 + 4 * (len(data.lights) + 1)
+    # roofline of the dominant kernel
+    kern = {"trace_closest": agg["trace_closest_ms"], "trace_any": agg["trace_any_ms"], "shade": agg["shade_ms"]}
+    dom = max(kern, key=kern.get)
+    peaks, src = _peaks()
+    rays_c, rays_a = agg["closest_rays"], agg["shadow_rays"]
+    nodes_pr_c = cstats["nodes_closest"] / max(cstats["closest_rays"], 1)
+    tris_pr_c = cstats["tris_closest"] / max(cstats["closest_rays"], 1)
+    nodes_pr_a = cstats["nodes_any"] / max(cstats["shadow_rays"], 1)
+    tris_pr_a = cstats["tris_any"] / max(cstats["shadow_rays"], 1)
+    if dom == "trace_closest":
+        per_ray = S_RAY_IN + S_HIT_OUT + nodes_pr_c * S_NODE + tris_pr_c * S_TRI
+        algo_bytes = rays_c * per_ray
+        nl = agg["trace_closest_launches"]
+    elif dom == "trace_any":
+        per_ray = S_RAY_IN + 4 + nodes_pr_a * S_NODE + tris_pr_a * S_TRI
+        algo_bytes = rays_a * per_ray
+        nl = agg["trace_any_launches"]
+    else:
+        per_ray = 2 * 128 + 2 * 32 + 64
+        algo_bytes = rays_c * per_ray
+        nl = max(agg["trace_closest_launches"], 1)
+    per_launch_bytes = algo_bytes / max(nl, 1)
+    avg_launch_s = kern[dom] / 1000.0 / max(nl, 1)
+    achieved = per_launch_bytes / max(avg_launch_s, 1e-12) / 1e9
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "trace_closest_traffic.json")
+    if dom == "trace_closest" and os.path.exists(tf):
+        try:
+            tj = json.load(open(tf))
+            traffic = tj.get("bytes_per_ray", 0) * rays_c / max(nl, 1)
+        except Exception:
+            traffic = None
+    rays_per_s = (rays_c + rays_a) * world / t_local
+    res = {}
+    if rank == 0:
+        try:
+            cpu_o, start, n, _ = cpu_oracle_rate(data, target_s=args.cpu_seconds)
+            threads = os.cpu_count() or 1
+            t0 = time.time()
+            cpu_o.render_tiles(spp, start, start + n, seed=5, threads=threads)
+            cdt = time.time() - t0
+            cpu_samples = n * 32 * 32 * spp
+            res["cpu_baseline"] = {"value": cpu_samples / cdt, "unit": UNIT, "cores": threads, "kind": "port",
+                                   "sample": "%d of 1024 32x32 tiles at 64 spp (%d path samples), %.1f s" %
+                                             (n, cpu_samples, cdt)}
+        except Exception as ex:  # the baseline never blocks the GPU line
+            res["cpu_baseline"] = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                                   "sample": "failed: %s" % ex}
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded displaced icosphere + procedural sky; no dataset)",
+                "config": {"workload": WORKLOAD, "integrator": "PathTracingMIS", "triangles": data.n_triangles,
+                           "resolution": [W, H], "spp": spp, "max_depth": CONFIG["max_depth"],
+                           "samples_per_step": samples_per_step, "parallelism": "replicas" if world > 1 else "single",
+                           "l2": "inputs larger than L2 (BVH+triangles %.0f MB, path state ~1 GB per batch)" %
+                                 (info["device_bytes"] / 1e6),
+                           "scene_gen_s": round(gen_s, 2), "scene_build_upload_s": round(upload_s, 2)},
+                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                             "frac": achieved / peaks.get("hbm_gbs", 1), "traffic": traffic,
+                             "kernel": dom, "peak_source": src,
+                             "algorithmic_bytes_per_ray": per_ray, "launches": nl,
+                             "avg_launch_ms": avg_launch_s * 1000},
+                "mrays_per_s": rays_per_s / 1e6,
+                "kernel_ms": {k: round(v / args.steps, 3) for k, v in kern.items()},
+                "traversal": {"nodes_per_closest_ray": nodes_pr_c, "tris_per_closest_ray": tris_pr_c,
+                              "nodes_per_shadow_ray": nodes_pr_a, "tris_per_shadow_ray": tris_pr_a},
+                "gpu_launches": launches, "clocks": clk}
+        line.update(res)
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

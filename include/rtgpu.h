@@ -230,12 +230,23 @@ typedef struct rt_light_r {
 } rt_light_r;
 
 typedef struct rt_render_stats {
-    double kernel_ms;        /* summed device time of the last render (events)   */
-    double trace_ms;         /* of which closest/any-hit traversal               */
+    double kernel_ms;        /* device time of the last render (events)          */
+    double camera_ms;        /* per-kernel device time, summed over launches;    */
+    double trace_closest_ms; /* filled when profiling is enabled                 */
+    double trace_any_ms;
+    double shade_ms;
+    double volpath_ms;
+    double film_ms;
     int64_t paths;           /* path samples rendered                            */
     int64_t closest_rays;    /* closest-hit rays traced                          */
     int64_t shadow_rays;     /* any-hit rays traced                              */
     int64_t launches;        /* kernels launched by the last render              */
+    int64_t trace_closest_launches;
+    int64_t trace_any_launches;
+    int64_t nodes_closest;   /* BVH nodes fetched by closest-hit rays (level 2)  */
+    int64_t tris_closest;    /* triangle slots tested by closest-hit rays        */
+    int64_t nodes_any;       /* ... by any-hit rays                              */
+    int64_t tris_any;
     int64_t limit_hits;      /* device loops that hit their cap                  */
     int64_t nan_samples;     /* samples dropped as NaN (Screen.cpp:46-50)        */
 } rt_render_stats;
@@ -268,6 +279,9 @@ rt_status rt_scene_info(const rt_scene *scene, float bounds[6], int64_t *device_
 rt_status rt_render(rt_ctx *ctx, rt_scene *scene, const rt_render_desc *rd,
                     float *film_rgbw, int32_t on_device);
 rt_status rt_render_stats_get(const rt_ctx *ctx, rt_render_stats *out);
+/* Profiling level of later renders: 0 off, 1 per-kernel CUDA-event timing,
+ * 2 timing plus BVH traversal counters (slower; for roofline accounting). */
+rt_status rt_ctx_set_profiling(rt_ctx *ctx, int32_t level);
 
 /* Trace n rays (closest hit, or any hit when anyhit != 0). */
 rt_status rt_trace(rt_ctx *ctx, rt_scene *scene, const rt_ray *rays, int32_t n,

@@ -809,7 +809,8 @@ static float o_env_pdf(const o_scene *sc, int light, v3 to_light)
     float fx, fy;
     o_env_dir_to_xy(L, dir, &fx, &fy);
     float st = sinf(fy);
-    float nf = o_env_norm(sc, light, (int)fy);
+    /* a NaN direction (degenerate sample) must not index outside the table */
+    float nf = o_env_norm(sc, light, isnan(fy) ? 0 : (int)fy);
     float lum = c3_lum(c3_muls(o_env_interp(L, fx, fy), L->env_scale));
     float pdf = lum * nf;
     pdf /= smax(fabsf(st), O_EPSILON);

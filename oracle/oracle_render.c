@@ -599,7 +599,7 @@ typedef struct {
     const rt_render_desc *rd;
     float *film;
     int ntx, nty;
-    int next;
+    int next, end;
     pthread_mutex_t mu;
     int64_t nan_count;
 } o_job;
@@ -633,7 +633,7 @@ static void *job_worker(void *arg)
         pthread_mutex_lock(&J->mu);
         int t = J->next++;
         pthread_mutex_unlock(&J->mu);
-        if (t >= J->ntx * J->nty) break;
+        if (t >= J->end) break;
         int ox = (t % J->ntx) * bx, oy = (t / J->ntx) * by;
         int ex = imin(cam->width, ox + bx), ey = imin(cam->height, oy + by);
         int tw = ex - ox, th = ey - oy;
@@ -660,7 +660,10 @@ static void *job_worker(void *arg)
     return NULL;
 }
 
-int32_t oracle_render(o_scene *sc, const rt_render_desc *rd, float *film, int32_t nthreads)
+/* Render tiles [tile0, tile1) of the job grid (all tiles when tile1 < 0);
+ * pixels outside those tiles are left zero. */
+int32_t oracle_render_tiles(o_scene *sc, const rt_render_desc *rd, int32_t tile0, int32_t tile1,
+                            float *film, int32_t nthreads)
 {
     if (!sc || !rd || !film) return RT_ERR_INVALID;
     if (sc->strategy != rd->strategy || !sc->light_cdf.cdf) build_light_cdf(sc, rd->strategy);
@@ -670,7 +673,9 @@ int32_t oracle_render(o_scene *sc, const rt_render_desc *rd, float *film, int32_
     J.sc = sc; J.rd = rd; J.film = film;
     J.ntx = (cam->width + bx - 1) / bx;
     J.nty = (cam->height + by - 1) / by;
-    J.next = 0; J.nan_count = 0;
+    J.next = tile0 < 0 ? 0 : tile0;
+    J.end = (tile1 < 0 || tile1 > J.ntx * J.nty) ? J.ntx * J.nty : tile1;
+    J.nan_count = 0;
     pthread_mutex_init(&J.mu, NULL);
     memset(film, 0, sizeof(float) * 4 * (size_t)cam->width * cam->height);
     if (nthreads < 1) nthreads = 1;
@@ -680,6 +685,11 @@ int32_t oracle_render(o_scene *sc, const rt_render_desc *rd, float *film, int32_
     free(th);
     pthread_mutex_destroy(&J.mu);
     return RT_OK;
+}
+
+int32_t oracle_render(o_scene *sc, const rt_render_desc *rd, float *film, int32_t nthreads)
+{
+    return oracle_render_tiles(sc, rd, 0, -1, film, nthreads);
 }
 
 /* Radiance of individual path samples (pixel index, sample index) */

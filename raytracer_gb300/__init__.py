@@ -1,0 +1,12 @@
+"""GB300-native light-transport core for Iscandel/Raytracer's PathTracingMIS
+and VolPathTracing integrators.
+
+The compute path is librtgpu.so (hand-written CUDA for sm_103a behind the C
+ABI declared in include/rtgpu.h); this package holds the Python host binding
+(`core`), the ctypes mirror of the scene description (`desc`), the seeded
+synthetic scenes (`scenes`) and the in-tree build (`build`).
+"""
+from . import desc  # noqa: F401
+from .core import Context, Scene, RtError, post_process, lib, LIB_PATH  # noqa: F401
+
+__all__ = ["Context", "Scene", "RtError", "post_process", "lib", "desc", "LIB_PATH"]

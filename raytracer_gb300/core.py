@@ -1,0 +1,184 @@
+"""Python host binding over librtgpu.so (the C ABI in include/rtgpu.h).
+
+This mirrors the reference's render entry points for the two path-tracing
+integrators: a `Scene` is the flattened, initialised reference scene
+(Scene::initialize, core/Scene.cpp:115-138) resident on the GPU, and
+`Scene.render` is the render step of Scene::compute (core/Scene.cpp:83-101)
+running PathTracingMIS::li or VolPathTracing::li for every path sample.
+There is no CPU fallback: if the CUDA library is missing or no GPU is
+present, construction raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import desc as D
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "librtgpu.so")
+
+RT_OK = 0
+_STATUS = {1: "RT_ERR_INVALID", 2: "RT_ERR_CUDA", 3: "RT_ERR_LIMIT", 4: "RT_ERR_NOMEM", 5: "RT_ERR_UNSUPPORTED"}
+
+
+class RtError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s: %s" % (_STATUS.get(status, status), msg))
+        self.status = status
+
+
+_lib = None
+
+
+def lib():
+    """Load librtgpu.so (built in-tree by raytracer_gb300.build)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RtError(5, "librtgpu.so not built (run raytracer_gb300.build.build())")
+    L = C.CDLL(LIB_PATH)
+    vp = C.c_void_p
+    L.rt_abi_version.restype = C.c_int32
+    L.rt_last_error.restype = C.c_char_p
+    L.rt_mix64.restype = C.c_uint64
+    L.rt_mix64.argtypes = [C.c_uint64]
+    L.rt_ctx_create.argtypes = [C.c_int32, C.POINTER(vp)]
+    L.rt_ctx_destroy.argtypes = [vp]
+    L.rt_ctx_set_stream.argtypes = [vp, vp]
+    L.rt_scene_create.argtypes = [vp, C.POINTER(D.SceneDesc), C.POINTER(vp)]
+    L.rt_scene_destroy.argtypes = [vp]
+    L.rt_scene_info.argtypes = [vp, vp, C.POINTER(C.c_int64), C.POINTER(C.c_int32)]
+    L.rt_render.argtypes = [vp, vp, C.POINTER(D.RenderDesc), vp, C.c_int32]
+    L.rt_render_stats_get.argtypes = [vp, C.POINTER(D.RenderStats)]
+    L.rt_ctx_set_profiling.argtypes = [vp, C.c_int32]
+    L.rt_trace.argtypes = [vp, vp, vp, C.c_int32, C.c_int32, vp, C.c_int32]
+    L.rt_bsdf_query.argtypes = [vp, vp, C.c_int32, C.c_int32, vp, C.c_int32, vp]
+    L.rt_light_query.argtypes = [vp, vp, C.c_int32, vp, C.c_int32, vp]
+    for name in ("rt_ctx_create", "rt_ctx_destroy", "rt_ctx_set_stream", "rt_scene_create", "rt_scene_destroy",
+                 "rt_scene_info", "rt_render", "rt_render_stats_get", "rt_ctx_set_profiling", "rt_trace", "rt_bsdf_query", "rt_light_query"):
+        getattr(L, name).restype = C.c_int32
+    _lib = L
+    return L
+
+
+def _check(status):
+    if status != RT_OK:
+        raise RtError(status, lib().rt_last_error().decode())
+
+
+def _p(a):
+    return C.c_void_p(a.ctypes.data)
+
+
+class Context:
+    """One GPU and one CUDA stream (rt_ctx)."""
+
+    def __init__(self, device=0):
+        self.h = C.c_void_p()
+        _check(lib().rt_ctx_create(device, C.byref(self.h)))
+        self.device = device
+
+    def close(self):
+        if self.h:
+            lib().rt_ctx_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_ptr):
+        _check(lib().rt_ctx_set_stream(self.h, C.c_void_p(stream_ptr)))
+
+    def set_profiling(self, level):
+        """0 off, 1 per-kernel event timing, 2 timing + traversal counters."""
+        _check(lib().rt_ctx_set_profiling(self.h, int(level)))
+
+    def stats(self):
+        s = D.RenderStats()
+        _check(lib().rt_render_stats_get(self.h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in D.RenderStats._fields_}
+
+
+class Scene:
+    """A SceneData flattened and uploaded to the device (rt_scene)."""
+
+    def __init__(self, ctx, scene):
+        self.ctx = ctx
+        self.data = scene
+        self._desc = scene.desc()
+        self.h = C.c_void_p()
+        _check(lib().rt_scene_create(ctx.h, C.byref(self._desc), C.byref(self.h)))
+        self.width = scene.camera["width"]
+        self.height = scene.camera["height"]
+
+    def close(self):
+        if self.h:
+            lib().rt_scene_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self):
+        b = np.zeros(6, np.float32)
+        nbytes = C.c_int64()
+        nodes = C.c_int32()
+        _check(lib().rt_scene_info(self.h, _p(b), C.byref(nbytes), C.byref(nodes)))
+        return dict(bounds=b, device_bytes=nbytes.value, bvh_nodes=nodes.value)
+
+    def render(self, spp, seed=0, sample_begin=0, film=None, block=32, **over):
+        """Render `spp` samples per pixel; returns the (H, W, 4) film of
+        (rgb sum, weight) in host memory, or writes a device pointer
+        (`film` as an int address) when given."""
+        rd = self.data.render_desc(spp, seed=seed, sample_begin=sample_begin, block=block, **over)
+        if film is None:
+            out = np.zeros((self.height, self.width, 4), np.float32)
+            _check(lib().rt_render(self.ctx.h, self.h, C.byref(rd), _p(out), 0))
+            return out
+        _check(lib().rt_render(self.ctx.h, self.h, C.byref(rd), C.c_void_p(int(film)), 1))
+        return None
+
+    def trace(self, rays, anyhit=False):
+        rays = np.ascontiguousarray(rays, D.RAY_DTYPE)
+        hits = np.zeros(len(rays), D.HIT_DTYPE)
+        _check(lib().rt_trace(self.ctx.h, self.h, _p(rays), len(rays), int(anyhit), _p(hits), 0))
+        return hits
+
+    def bsdf_query(self, bsdf, op, q):
+        q = np.ascontiguousarray(q, BSDF_Q)
+        r = np.zeros(len(q), BSDF_R)
+        _check(lib().rt_bsdf_query(self.ctx.h, self.h, bsdf, op, _p(q), len(q), _p(r)))
+        return r
+
+    def light_query(self, light, p, u):
+        q = np.zeros(len(p), LIGHT_Q)
+        q["p"], q["u"] = p, u
+        r = np.zeros(len(p), LIGHT_R)
+        _check(lib().rt_light_query(self.ctx.h, self.h, light, _p(q), len(q), _p(r)))
+        return r
+
+
+BSDF_Q = np.dtype([("wi", np.float32, 3), ("wo", np.float32, 3), ("u", np.float32, 2)])
+BSDF_R = np.dtype([("value", np.float32, 3), ("pdf", np.float32), ("wo", np.float32, 3),
+                   ("relative_eta", np.float32), ("sampled_type", np.int32), ("pad", np.int32)])
+LIGHT_Q = np.dtype([("p", np.float32, 3), ("u", np.float32, 2)])
+LIGHT_R = np.dtype([("intensity", np.float32, 3), ("pdf", np.float32), ("to_light", np.float32, 3),
+                    ("distance", np.float32), ("point", np.float32, 3), ("normal", np.float32, 3),
+                    ("pdf_eval", np.float32), ("pad", np.float32)])
+assert BSDF_Q.itemsize == C.sizeof(D.BsdfQ) and BSDF_R.itemsize == C.sizeof(D.BsdfR)
+assert LIGHT_Q.itemsize == C.sizeof(D.LightQ) and LIGHT_R.itemsize == C.sizeof(D.LightR)
+
+
+def post_process(film):
+    """Screen::postProcessColor (core/Screen.cpp:113-122): colour / weight."""
+    w = film[..., 3:4]
+    with np.errstate(invalid="ignore", divide="ignore"):
+        return np.where(w > 0, film[..., :3] / w, 0.0).astype(np.float32)

@@ -1,0 +1,1529 @@
+// rt_api.cu -- kernels of the GB300 light-transport core and its C ABI.
+//
+// Render structure (one rt_render call):
+//   for each batch of whole reference tiles (all samples of their pixels):
+//     k_camera          camera rays of every path (SampleJob.cpp:46-59)
+//     repeat per path vertex (PathTracingMIS):
+//       k_trace<closest> BSDF-sampled / primary rays      (Bvh.cpp:392-481)
+//       k_trace<any>     light-sample shadow rays         (Integrator.cpp:228-232)
+//       k_pt_shade       resolve the previous vertex, shade the new one
+//                        (PathTracingMIS.cpp:54-259), compact survivors
+//     or, for VolPathTracing, k_volpath: one persistent kernel that takes
+//     paths from a work counter and runs VolPathTracing::li to completion
+//     k_film            per-pixel reduction in the reference's sample order
+//                       (Screen::addSample with the box filter, Screen::merge)
+#include "rt_kernels.cuh"
+#include "rt_bvh.h"
+#include "../../include/rtgpu.h"
+
+#include <cuda_runtime.h>
+#include <cstdio>
+#include <cstring>
+#include <cmath>
+#include <string>
+#include <vector>
+#include <algorithm>
+
+using namespace rtgpu;
+
+// =====================================================================
+// error handling
+// =====================================================================
+static thread_local std::string g_err;
+static rt_status fail(rt_status st, const std::string &msg)
+{
+    g_err = msg;
+    return st;
+}
+#define CK(call)                                                                       \
+    do {                                                                               \
+        cudaError_t e_ = (call);                                                       \
+        if (e_ != cudaSuccess)                                                         \
+            return fail(RT_ERR_CUDA, std::string(#call " -> ") + cudaGetErrorString(e_)); \
+    } while (0)
+
+// =====================================================================
+// kernels
+// =====================================================================
+__device__ __forceinline__ float4 f4(V3 v, float w) { return make_float4(v.x, v.y, v.z, w); }
+__device__ __forceinline__ float4 f4c(C3 c, float w) { return make_float4(c.r, c.g, c.b, w); }
+__device__ __forceinline__ V3 xyz(float4 a) { return v3(a.x, a.y, a.z); }
+__device__ __forceinline__ C3 rgb(float4 a) { return c3(a.x, a.y, a.z); }
+
+// warp-aggregated append to a queue
+__device__ __forceinline__ void q_push(int *queue, int *count, int value, bool pred)
+{
+    unsigned mask = __ballot_sync(__activemask(), pred);
+    if (!pred) return;
+    int lane = threadIdx.x & 31;
+    int leader = __ffs(mask) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(count, __popc(mask));
+    base = __shfl_sync(mask, base, leader);
+    queue[base + __popc(mask & ((1u << lane) - 1))] = value;
+}
+
+// Film footprint of a sample inside its tile: Screen::addSample with the
+// box filter of radius 0.5 (Screen.cpp:52-66).  Returns the code
+// (sx - lx + 1) | (ex - lx + 1) << 2 | (sy - ly + 1) << 4 | (ey - ly + 1) << 6,
+// 0x55 being the usual "own pixel only".
+__device__ __forceinline__ uint8_t splat_code(float xx, float yy, int ox, int oy, int lx, int ly, int tw, int th)
+{
+    float fx = xx - 0.5f - (float)(ox - 0);
+    float fy = yy - 0.5f - (float)(oy - 0);
+    int sx = (int)ceilf(fx - 0.5f), ex = (int)floorf(fx + 0.5f);
+    int sy = (int)ceilf(fy - 0.5f), ey = (int)floorf(fy + 0.5f);
+    sx = imax(0, sx); ex = imin(tw - 1, ex);
+    sy = imax(0, sy); ey = imin(th - 1, ey);
+    // ranges are within [lx-1, lx+1]; an empty range encodes as start > end
+    int a = imin(imax(sx - lx + 1, 0), 3), b = imin(imax(ex - lx + 1, -1), 2);
+    int c = imin(imax(sy - ly + 1, 0), 3), d = imin(imax(ey - ly + 1, -1), 2);
+    if (b < 0 || d < 0 || a > b || c > d) return 0xFF;  // contributes nowhere
+    return (uint8_t)(a | (b << 2) | (c << 4) | (d << 6));
+}
+__device__ __forceinline__ bool splat_covers(uint8_t code, int dx, int dy)
+{
+    // dx, dy: target offset from the source pixel, in [-1, 1]
+    if (code == 0xFF) return false;
+    int a = (code & 3) - 1, b = ((code >> 2) & 3) - 1, c = ((code >> 4) & 3) - 1, d = ((code >> 6) & 3) - 1;
+    return dx >= a && dx <= b && dy >= c && dy <= d;
+}
+
+struct RenderParams {
+    DevScene S;
+    Wave W;
+    int4 *tileorder;   // g -> (x, y, lx | ly << 16, tw | th << 16)
+    int g0;            // first tile-order index of the batch
+    int npix, spp, sample_begin, n_paths;
+    uint64_t seed;
+    int max_depth, min_depth;
+    int *limit_flag;
+    unsigned long long *stats;  // [0] closest rays, [1] shadow rays, [2] nan samples
+};
+
+// ---------------------------------------------------------------- camera
+__global__ void k_camera(RenderParams P)
+{
+    const DevCamera &cam = P.S.cam;
+    for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < P.n_paths; slot += gridDim.x * blockDim.x) {
+        int q = slot % P.npix;
+        int s = slot / P.npix;
+        int4 to = P.tileorder[P.g0 + q];
+        int x = to.x, y = to.y;
+        int lx = to.z & 0xffff, ly = to.z >> 16, tw = to.w & 0xffff, th = to.w >> 16;
+        Pcg32 rng;
+        path_stream_seed(rng, P.seed, (uint32_t)(y * cam.width + x), (uint32_t)(P.sample_begin + s));
+        V2 j = next2d(rng);
+        float xx = (float)x + j.x, yy = (float)y + j.y;
+        V2 lens = v2(0.f, 0.f);
+        if (cam.aperture_radius > 0.f) lens = next2d(rng);
+        Ray r = camera_ray(cam, xx, yy, lens);
+        uint8_t code = splat_code(xx, yy, x - lx, y - ly, lx, ly, tw, th);
+        P.W.splat[slot] = code;
+        if (code != 0x55) P.W.pix_irregular[q] = 1;
+        P.W.rng[slot] = rng;
+        P.W.ray_o[slot] = f4(r.o, r.mint);
+        P.W.ray_d[slot] = f4(r.d, r.maxt);
+        P.W.tp[slot] = make_float4(1.f, 1.f, 1.f, 1.f);
+        P.W.rad[slot] = make_float4(0.f, 0.f, 0.f, __int_as_float(0));
+        P.W.flags[slot] = F_FIRST;
+        P.W.q_closest[slot] = slot;
+        P.W.q_active[0][slot] = slot;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        P.W.cnt[0].active = P.n_paths;
+        P.W.cnt[0].closest = P.n_paths;
+        P.W.cnt[0].shadow = 0;
+    }
+}
+
+// ---------------------------------------------------------------- traversal
+// Persistent kernel: warps fetch 32 queue entries at a time.  COUNT adds
+// BVH node / triangle-slot fetch counts to stats[3..6].
+template <bool ANY, bool COUNT>
+__global__ void __launch_bounds__(128) k_trace(RenderParams P, int round)
+{
+    RoundCounters *C = &P.W.cnt[round];
+    const int n = ANY ? C->shadow : C->closest;
+    int *wc = ANY ? &C->wc_shadow : &C->wc_closest;
+    const int *queue = ANY ? P.W.q_shadow : P.W.q_closest;
+    const int lane = threadIdx.x & 31;
+    int cnt[2] = {0, 0};
+    for (;;) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(wc, 32);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) break;
+        int i = base + lane;
+        if (i < n) {
+            int slot = queue[i];
+            float4 o = ANY ? P.W.sh_o[slot] : P.W.ray_o[slot];
+            float4 d = ANY ? P.W.sh_d[slot] : P.W.ray_d[slot];
+            Hit h;
+            bool hit = trace_ray<ANY, COUNT>(P.S, xyz(o), xyz(d), o.w, d.w, h, cnt);
+            if (ANY) P.W.occl[slot] = hit ? 1 : 0;
+            else P.W.hit[slot] = make_float4(h.t, h.u, h.v, __int_as_float(hit ? h.prim : -1));
+        }
+    }
+    if (COUNT) {
+        for (int off = 16; off > 0; off >>= 1) {
+            cnt[0] += __shfl_down_sync(0xffffffffu, cnt[0], off);
+            cnt[1] += __shfl_down_sync(0xffffffffu, cnt[1], off);
+        }
+        if (lane == 0) {
+            atomicAdd(&P.stats[ANY ? 5 : 3], (unsigned long long)cnt[0]);
+            atomicAdd(&P.stats[ANY ? 6 : 4], (unsigned long long)cnt[1]);
+        }
+    }
+    if (threadIdx.x == 0 && blockIdx.x == 0) atomicAdd(&P.stats[ANY ? 1 : 0], (unsigned long long)n);
+}
+
+// ---------------------------------------------------------------- PathTracingMIS vertex
+__global__ void __launch_bounds__(128) k_pt_shade(RenderParams P, int round)
+{
+    const DevScene &S = P.S;
+    RoundCounters *Cin = &P.W.cnt[round];
+    RoundCounters *Cout = &P.W.cnt[round + 1];
+    const int n = Cin->active;
+    const int *qin = P.W.q_active[round & 1];
+    int *qout = P.W.q_active[(round + 1) & 1];
+    const int env = S.env_light;
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    int stride = gridDim.x * blockDim.x;
+    int iters = (n + stride - 1) / stride;
+    for (int it = 0; it < iters; it++, idx += stride) {
+        bool valid = idx < n;
+        int slot = valid ? qin[idx] : 0;
+        bool push_active = false, push_closest = false, push_shadow = false;
+        if (valid) {
+            Pcg32 rng = P.W.rng[slot];
+            float4 tpv = P.W.tp[slot];
+            float4 radv = P.W.rad[slot];
+            C3 T = rgb(tpv);
+            float eta = tpv.w;
+            C3 L = rgb(radv);
+            int depth = __float_as_int(radv.w);
+            int flags = P.W.flags[slot];
+            float4 ro = P.W.ray_o[slot], rd = P.W.ray_d[slot];
+            Ray ray = make_ray(xyz(ro), xyz(rd), ro.w, rd.w);
+            float4 hv = P.W.hit[slot];
+            Hit h; h.t = hv.x; h.u = hv.y; h.v = hv.z; h.prim = __float_as_int(hv.w);
+            bool done = false;
+            bool have_frame = false;
+            Frame fr;
+            if (flags & F_FIRST) {
+                flags &= ~F_FIRST;
+                if (h.prim == -1) {
+                    if (env >= 0) L = L + env_le(S.lights[env], ray.d);
+                    done = true;
+                } else if (depth >= P.max_depth) {
+                    done = true;
+                }
+            } else {
+                // ---- resolve the previous vertex
+                if ((flags & F_NEE) && !P.W.occl[slot]) L = L + rgb(P.W.nee[slot]);
+                flags &= ~F_NEE;
+                if (flags & F_END) {
+                    done = true;
+                } else {
+                    float4 bsv = P.W.bs[slot];
+                    C3 f = rgb(bsv);
+                    float bpdf = bsv.w;
+                    int caught = -1;
+                    bool isenv = false;
+                    C3 Le = cfill(0.f);
+                    if (h.prim != -1) {
+                        fr = hit_frame(S, h, ray.o, ray.d);
+                        have_frame = true;
+                        int nl = prim_light(S, h.prim);
+                        if (nl >= 0) { caught = nl; Le = area_le(S, nl, -ray.d, fr.n); }
+                    } else {
+                        if (env < 0) done = true;
+                        else { caught = env; isenv = true; Le = env_le(S.lights[env], ray.d); }
+                    }
+                    if (!done && caught >= 0) {
+                        V3 pt = have_frame ? fr.p : v3(0, 0, 0), nn = have_frame ? fr.n : v3(0, 0, 0);
+                        float pl = (flags & F_DELTA) ? 0.f : light_pdf(S, caught, ray.o, pt, nn, ray.d);
+                        float w = power_heuristic(bpdf, pl);
+                        L = L + ((T * Le) * f) * w;
+                        if (isenv) done = true;
+                    }
+                    if (!done) {
+                        T = T * f;
+                        eta *= P.W.rel_eta[slot];
+                        if (depth >= P.min_depth) {
+                            float stop = smin(0.95f, lum(T) * eta * eta);
+                            if (next1d(rng) < stop) T = T / stop;
+                            else done = true;
+                        }
+                    }
+                    if (!done) {
+                        depth++;
+                        if (depth >= P.max_depth) done = true;
+                    }
+                }
+            }
+            if (!done) {
+                // ---- shade the vertex at h
+                if (!have_frame) fr = hit_frame(S, h, ray.o, ray.d);
+                int b = prim_bsdf(S, h.prim);
+                if (b < 0) {
+                    done = true;
+                } else {
+                    const DevBsdf &B = S.bsdfs[b];
+                    int hl = prim_light(S, h.prim);
+                    if (depth == 0 && hl >= 0) L = L + T * area_le(S, hl, -ray.d, fr.n);
+                    // light sampling (Integrator::sampleLightDirect)
+                    V2 s = next2d(rng);
+                    if (S.n_lights > 0) {
+                        float lw;
+                        int li_idx = cdf_sample_reuse(S.light_cdf, S.n_lights + 1, s.x, lw);
+                        LightRec li;
+                        light_sample(S, li_idx, fr.p, s, li);
+                        if (li.pdf > 0 && lum(li.intensity) > 0) {
+                            C3 value = (li.intensity / li.pdf) / lw;
+                            li.pdf *= lw;
+                            if (!iszero(value)) {
+                                V3 wi = to_local(fr, li.to_light), wo = to_local(fr, -ray.d);
+                                float ct = fabsf(wi.z);
+                                float bp = bsdf_pdf(B, wi, wo);
+                                float w = power_heuristic(li.pdf, bp);
+                                C3 contrib = (((T * value) * bsdf_eval(B, wi, wo)) * ct) * w;
+                                P.W.nee[slot] = f4c(contrib, 0.f);
+                                P.W.sh_o[slot] = f4(fr.p, RT_EPSILON);
+                                P.W.sh_d[slot] = f4(li.to_light, li.distance - RT_EPSILON);
+                                flags |= F_NEE;
+                                push_shadow = true;
+                            }
+                        }
+                    }
+                    // BSDF sampling
+                    BsdfRec r;
+                    r.wi = to_local(fr, -ray.d); r.wo = v3(0, 0, 0);
+                    r.type = BT_ALL; r.rel_eta = 1.f; r.pdf = -1.f;
+                    V2 u = next2d(rng);
+                    C3 f = bsdf_sample(B, r, u);
+                    if (iszero(f)) {
+                        if (flags & F_NEE) { flags |= F_END; push_active = true; }
+                        else done = true;
+                    } else {
+                        V3 nd = to_world(fr, r.wo);
+                        P.W.ray_o[slot] = f4(fr.p, RT_EPSILON);
+                        P.W.ray_d[slot] = f4(nd, RT_MAX_REAL);
+                        P.W.bs[slot] = f4c(f, r.pdf);
+                        P.W.rel_eta[slot] = r.rel_eta;
+                        if (r.type & BT_DELTA) flags |= F_DELTA; else flags &= ~F_DELTA;
+                        push_closest = true;
+                        push_active = true;
+                    }
+                }
+            }
+            if (done) {
+                flags |= F_DONE;
+                P.W.out[slot] = f4c(L, 0.f);
+                push_active = push_closest = push_shadow = false;
+            }
+            P.W.rng[slot] = rng;
+            P.W.tp[slot] = f4c(T, eta);
+            P.W.rad[slot] = f4c(L, __int_as_float(depth));
+            P.W.flags[slot] = flags;
+        }
+        q_push(qout, &Cout->active, slot, push_active);
+        q_push(P.W.q_closest, &Cout->closest, slot, push_closest);
+        q_push(P.W.q_shadow, &Cout->shadow, slot, push_shadow);
+    }
+}
+
+// ---------------------------------------------------------------- VolPathTracing
+// Integrator::evalTransmittance (Integrator.cpp:81-133)
+__device__ C3 eval_transmittance(const DevScene &S, Ray ray, int medium, Pcg32 &rng, int &limit)
+{
+    Ray tr = ray;
+    C3 T = cfill(1.f);
+    float dist = ray.maxt;
+    bool first = true;
+    for (int guard = 0; guard < 4096; guard++) {
+        Hit h;
+        bool inter = trace_ray<false>(S, tr.o, tr.d, tr.mint, tr.maxt, h);
+        if (inter && prim_bsdf(S, h.prim) >= 0) return cfill(0.f);
+        if (inter) dist -= h.t;
+        if (medium >= 0)
+            T = T * medium_tr(S.media[medium], make_ray(tr.o, tr.d, first ? tr.mint : 0.f, inter ? h.t : dist), rng, limit);
+        first = false;
+        if (!inter || iszero(T)) return T;
+        V3 np = tr.o + h.t * tr.d;
+        Frame f = hit_frame(S, h, tr.o, tr.d);
+        tr = make_ray(np, tr.d, RT_EPSILON, dist);
+        if (prim_interior(S, h.prim) != prim_exterior(S, h.prim))
+            medium = dot(f.n, tr.d) < 0.f ? prim_interior(S, h.prim) : prim_exterior(S, h.prim);
+    }
+    limit = 1;
+    return cfill(0.f);
+}
+
+// VolPathTracing::evalTransmittanceFromSampledBSDF (VolPathTracing.cpp:369-424)
+__device__ C3 eval_tr_sampled(const DevScene &S, Ray ray, Pcg32 &rng, int medium, Hit &h, Frame &fr, bool &was,
+                              int &newm, int &limit)
+{
+    Ray tr = ray;
+    C3 T = cfill(1.f);
+    bool first = true;
+    was = false;
+    for (int guard = 0; guard < 4096; guard++) {
+        Hit nh;
+        was = trace_ray<false>(S, tr.o, tr.d, tr.mint, tr.maxt, nh);
+        if (was) { h = nh; fr = hit_frame(S, h, tr.o, tr.d); }
+        if (medium >= 0)
+            T = T * medium_tr(S.media[medium], make_ray(tr.o, tr.d, first ? tr.mint : 0.f, was ? h.t : tr.maxt), rng, limit);
+        if (was && prim_bsdf(S, h.prim) >= 0) return T;
+        first = false;
+        if (!was || iszero(T)) return T;
+        V3 np = tr.o + h.t * tr.d;
+        tr = make_ray(np, tr.d, RT_EPSILON, tr.maxt);
+        if (prim_interior(S, h.prim) != prim_exterior(S, h.prim)) {
+            medium = dot(fr.n, tr.d) < 0.f ? prim_interior(S, h.prim) : prim_exterior(S, h.prim);
+            newm = medium;
+        }
+    }
+    limit = 1;
+    return T;
+}
+
+// Integrator::sampleAttenuatedLightDirect (Integrator.cpp:137-172)
+__device__ C3 sample_attenuated_light(const DevScene &S, V3 p, Pcg32 &rng, LightRec &li, int medium, int &limit)
+{
+    C3 value = cfill(0.f);
+    if (S.n_lights == 0) return value;
+    V2 u = next2d(rng);
+    float lw;
+    int idx = cdf_sample_reuse(S.light_cdf, S.n_lights + 1, u.x, lw);
+    light_sample(S, idx, p, u, li);
+    if (li.pdf > 0 && lum(li.intensity) > 0) {
+        C3 tr = eval_transmittance(S, make_ray(p, li.to_light, RT_EPSILON, li.distance - RT_EPSILON), medium, rng, limit);
+        li.pdf *= lw;
+        value = (tr * li.intensity) / li.pdf;
+    }
+    return value;
+}
+
+// VolPathTracing::li (VolPathTracing.cpp:25-367)
+__device__ C3 li_volpath(const DevScene &S, Ray ray, Pcg32 &rng, int max_depth, int min_depth, int &limit)
+{
+    C3 L = cfill(0.f), T = cfill(1.f);
+    float eta = 1.f;
+    int depth = 0;
+    bool emission = true;
+    const int env = S.env_light;
+    Hit h; h.t = RT_MAX_REAL; h.u = h.v = 0.f; h.prim = -1;
+    Frame fr; fr.p = v3(0, 0, 0); fr.n = fr.s = fr.t = v3(0, 0, 0);
+    Hit nh;
+    bool was = trace_ray<false>(S, ray.o, ray.d, ray.mint, ray.maxt, nh);
+    if (was) { h = nh; fr = hit_frame(S, h, ray.o, ray.d); }
+    int medium = S.cam.medium;
+    int guard = 0;
+    while (depth < max_depth) {
+        if (++guard > (1 << 16)) { limit = 1; break; }
+        float t = 0.f;
+        C3 wm = cfill(0.f), em = cfill(0.f);
+        bool scattered = false;
+        if (medium >= 0) scattered = medium_sample(S.media[medium], make_ray(ray.o, ray.d, ray.mint, h.t), rng, t, wm, em, limit);
+        if (scattered) {
+            const DevMedium &M = S.media[medium];
+            L = L + T * em;
+            T = T * wm;
+            fr.p = ray.o + t * ray.d;
+            LightRec li;
+            li.point = li.to_light = li.normal = v3(0, 0, 0);
+            li.intensity = cfill(0.f); li.distance = 0.f; li.pdf = 0.f;
+            C3 value = sample_attenuated_light(S, fr.p, rng, li, medium, limit);
+            if (!iszero(value)) {
+                float pf = phase_eval(M, li.to_light, -ray.d);
+                float w = power_heuristic(li.pdf, pf);
+                float ev = phase_eval(M, li.to_light, -ray.d);
+                L = L + ((T * value) * ev) * w;
+            }
+            V3 wo; float pfpdf;
+            float pfw = phase_sample(M, -ray.d, next2d(rng), wo, pfpdf);
+            ray = make_ray(fr.p, wo, 0.f, ray.maxt);
+            int newm = -1;
+            C3 tr = eval_tr_sampled(S, ray, rng, medium, h, fr, was, newm, limit);
+            T = T * pfw;
+            if (was) {
+                int hl = prim_light(S, h.prim);
+                if (hl >= 0) {
+                    C3 Le = area_le(S, hl, -ray.d, fr.n);
+                    float pl = light_pdf(S, hl, fr.p, li.point, li.normal, li.to_light);
+                    float w = power_heuristic(pfpdf, pl);
+                    L = L + ((T * Le) * tr) * w;
+                }
+            }
+        } else {
+            if (medium >= 0) {
+                L = L + T * em;
+                T = T * wm;
+            }
+            if (!was) {
+                if (emission && env >= 0) L = L + T * env_le(S.lights[env], ray.d);
+                return L;
+            }
+            int b = prim_bsdf(S, h.prim);
+            if (b < 0) {
+                ray = make_ray(fr.p, ray.d, RT_EPSILON, RT_MAX_REAL);
+                if (prim_interior(S, h.prim) != prim_exterior(S, h.prim))
+                    medium = dot(fr.n, ray.d) < 0.f ? prim_interior(S, h.prim) : prim_exterior(S, h.prim);
+                was = trace_ray<false>(S, ray.o, ray.d, ray.mint, ray.maxt, nh);
+                if (was) { h = nh; fr = hit_frame(S, h, ray.o, ray.d); }
+                continue;
+            }
+            const DevBsdf &B = S.bsdfs[b];
+            int hl = prim_light(S, h.prim);
+            if (emission && hl >= 0) L = L + T * area_le(S, hl, -ray.d, fr.n);
+            LightRec li;
+            li.point = li.to_light = li.normal = v3(0, 0, 0);
+            li.intensity = cfill(0.f); li.distance = 0.f; li.pdf = 0.f;
+            C3 value = sample_attenuated_light(S, fr.p, rng, li, medium, limit);
+            if (!iszero(value)) {
+                V3 wi = to_local(fr, li.to_light), wo = to_local(fr, -ray.d);
+                float ct = fabsf(wi.z);
+                float bp = bsdf_pdf(B, wi, wo);
+                float w = power_heuristic(li.pdf, bp);
+                L = L + (((T * value) * bsdf_eval(B, wi, wo)) * ct) * w;
+            }
+            BsdfRec r;
+            r.wi = to_local(fr, -ray.d); r.wo = v3(0, 0, 0);
+            r.type = BT_ALL; r.rel_eta = 1.f; r.pdf = -1.f;
+            C3 f = bsdf_sample(B, r, next2d(rng));
+            if (iszero(f)) break;
+            V3 pfrom = fr.p;
+            ray = make_ray(fr.p, to_world(fr, r.wo), RT_EPSILON, RT_MAX_REAL);
+            if (prim_interior(S, h.prim) != prim_exterior(S, h.prim))
+                medium = dot(fr.n, ray.d) < 0.f ? prim_interior(S, h.prim) : prim_exterior(S, h.prim);
+            int caught = -1;
+            bool isenv = false;
+            C3 Le = cfill(0.f);
+            int newm = -1;
+            C3 tr = eval_tr_sampled(S, ray, rng, medium, h, fr, was, newm, limit);
+            if (was) {
+                int nl = prim_light(S, h.prim);
+                if (nl >= 0) { caught = nl; Le = area_le(S, nl, -ray.d, fr.n); }
+            } else if (newm < 0) {
+                if (env >= 0) { caught = env; isenv = true; Le = env_le(S.lights[env], ray.d); }
+            }
+            if (caught >= 0) {
+                float pl = (r.type & BT_DELTA) ? 0.f : light_pdf(S, caught, pfrom, fr.p, fr.n, ray.d);
+                float w = power_heuristic(r.pdf, pl);
+                L = L + (((T * Le) * f) * tr) * w;
+                if (isenv && medium < 0) return L;
+            }
+            T = T * f;
+            eta *= r.rel_eta;
+        }
+        if (depth >= min_depth) {
+            float stop = smin(0.95f, cmax(T) * eta * eta);
+            if (next1d(rng) < stop) T = T / stop;
+            else return L;
+        }
+        was = trace_ray<false>(S, ray.o, ray.d, ray.mint, ray.maxt, nh);
+        if (was) { h = nh; fr = hit_frame(S, h, ray.o, ray.d); }
+        emission = false;
+        depth++;
+    }
+    return L;
+}
+
+// persistent: warps take 32 paths at a time from the batch (path regeneration)
+__global__ void __launch_bounds__(128) k_volpath(RenderParams P, int *work)
+{
+    const int lane = threadIdx.x & 31;
+    int limit = 0;
+    for (;;) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(work, 32);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= P.n_paths) break;
+        int slot = base + lane;
+        if (slot < P.n_paths) {
+            Pcg32 rng = P.W.rng[slot];
+            float4 ro = P.W.ray_o[slot], rd = P.W.ray_d[slot];
+            C3 L = li_volpath(P.S, make_ray(xyz(ro), xyz(rd), ro.w, rd.w), rng, P.max_depth, P.min_depth, limit);
+            P.W.out[slot] = f4c(L, 0.f);
+        }
+    }
+    if (limit) atomicExch(P.limit_flag, 1);
+}
+
+// ---------------------------------------------------------------- film
+// One thread per batch pixel: contributions in the order the reference's
+// tile loop produces them (pixels row-major, samples in order), restricted
+// to the 3x3 neighbourhood a box-filter splat can reach.
+__global__ void k_film(RenderParams P, float4 *film, int width)
+{
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= P.npix) return;
+    int4 to = P.tileorder[P.g0 + q];
+    int lx = to.z & 0xffff, ly = to.z >> 16, tw = to.w & 0xffff, th = to.w >> 16;
+    float r = 0.f, g = 0.f, b = 0.f, w = 0.f;
+    int nan = 0;
+    for (int dy = -1; dy <= 1; dy++) {
+        for (int dx = -1; dx <= 1; dx++) {
+            int sx = lx + dx, sy = ly + dy;
+            if (sx < 0 || sy < 0 || sx >= tw || sy >= th) continue;
+            int qs = q + dy * tw + dx;
+            bool self = (dx == 0 && dy == 0);
+            if (!self && !P.W.pix_irregular[qs]) continue;
+            for (int s = 0; s < P.spp; s++) {
+                int slot = s * P.npix + qs;
+                uint8_t code = P.W.splat[slot];
+                if (!splat_covers(code, -dx, -dy)) continue;
+                float4 L = P.W.out[slot];
+                if (isnan(L.x) || isnan(L.y) || isnan(L.z)) { if (self) nan++; continue; }
+                r += L.x * 1.f; g += L.y * 1.f; b += L.z * 1.f; w += 1.f;
+            }
+        }
+    }
+    film[(size_t)to.y * width + to.x] = make_float4(0.f + r, 0.f + g, 0.f + b, 0.f + w);
+    if (nan) atomicAdd(&P.stats[2], (unsigned long long)nan);
+}
+
+// ---------------------------------------------------------------- standalone queries
+__global__ void k_trace_rays(DevScene S, const rt_ray *rays, int n, int any, rt_hit *hits)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    rt_ray r = rays[i];
+    Hit h;
+    bool hit = any ? trace_ray<true>(S, vload(r.o), vload(r.d), r.mint, r.maxt, h)
+                   : trace_ray<false>(S, vload(r.o), vload(r.d), r.mint, r.maxt, h);
+    rt_hit o;
+    o.t = hit && !any ? h.t : 0.f;
+    o.u = hit && !any ? h.u : 0.f;
+    o.v = hit && !any ? h.v : 0.f;
+    o.prim = hit ? (any ? 0 : h.prim) : -1;
+    hits[i] = o;
+}
+
+__global__ void k_bsdf_query(DevScene S, int bsdf, int op, const rt_bsdf_q *q, int n, rt_bsdf_r *out)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const DevBsdf &B = S.bsdfs[bsdf];
+    rt_bsdf_r r;
+    memset(&r, 0, sizeof(r));
+    V3 wi = vload(q[i].wi), wo = vload(q[i].wo);
+    if (op == RT_BSDF_OP_EVAL) {
+        C3 v = bsdf_eval(B, wi, wo);
+        r.value[0] = v.r; r.value[1] = v.g; r.value[2] = v.b;
+    } else if (op == RT_BSDF_OP_PDF) {
+        r.pdf = bsdf_pdf(B, wi, wo);
+    } else {
+        BsdfRec rec;
+        rec.wi = wi; rec.wo = v3(0, 0, 0); rec.type = BT_ALL; rec.rel_eta = 1.f; rec.pdf = -1.f;
+        C3 v = bsdf_sample(B, rec, v2(q[i].u[0], q[i].u[1]));
+        r.value[0] = v.r; r.value[1] = v.g; r.value[2] = v.b;
+        r.pdf = rec.pdf;
+        r.wo[0] = rec.wo.x; r.wo[1] = rec.wo.y; r.wo[2] = rec.wo.z;
+        r.relative_eta = rec.rel_eta;
+        r.sampled_type = rec.type;
+    }
+    out[i] = r;
+}
+
+__global__ void k_light_query(DevScene S, int light, const rt_light_q *q, int n, rt_light_r *out)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    LightRec li;
+    li.point = li.to_light = li.normal = v3(0, 0, 0);
+    li.intensity = cfill(0.f); li.distance = 0.f; li.pdf = 0.f;
+    V3 p = vload(q[i].p);
+    light_sample(S, light, p, v2(q[i].u[0], q[i].u[1]), li);
+    rt_light_r r;
+    r.intensity[0] = li.intensity.r; r.intensity[1] = li.intensity.g; r.intensity[2] = li.intensity.b;
+    r.pdf = li.pdf;
+    r.to_light[0] = li.to_light.x; r.to_light[1] = li.to_light.y; r.to_light[2] = li.to_light.z;
+    r.distance = li.distance;
+    r.point[0] = li.point.x; r.point[1] = li.point.y; r.point[2] = li.point.z;
+    r.normal[0] = li.normal.x; r.normal[1] = li.normal.y; r.normal[2] = li.normal.z;
+    r.pdf_eval = light_pdf(S, light, p, li.point, li.normal, li.to_light);
+    r.pad = 0.f;
+    out[i] = r;
+}
+
+// =====================================================================
+// host side
+// =====================================================================
+struct DevBuf {
+    void *p = nullptr;
+    size_t n = 0;
+};
+
+struct rt_ctx {
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    // wavefront buffers (grown on demand)
+    int capacity = 0;
+    std::vector<void *> wave_allocs;
+    Wave W;
+    int4 *tileorder = nullptr;
+    size_t tileorder_n = 0;
+    int *work = nullptr;
+    int *limit_flag = nullptr;
+    unsigned long long *stats = nullptr;
+    float *light_cdf = nullptr;
+    int light_cdf_n = 0;
+    float4 *film = nullptr;
+    size_t film_n = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    rt_render_stats last;
+    int profiling = 0;
+    std::vector<cudaEvent_t> ev_pool;
+    std::vector<int> ev_kind;   // kernel kind per recorded pair
+    size_t ev_used = 0;
+    int tile_key[4] = {-1, -1, -1, -1};
+    std::vector<int> tile_start;
+};
+
+// kinds for per-kernel timing
+enum { K_CAMERA = 0, K_TRACE_C = 1, K_TRACE_A = 2, K_SHADE = 3, K_VOLPATH = 4, K_FILM = 5, K_KINDS = 6 };
+
+static void prof_begin(rt_ctx *c, int kind)
+{
+    if (!c->profiling) return;
+    size_t need = 2 * (c->ev_used + 1);
+    while (c->ev_pool.size() < need) {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        c->ev_pool.push_back(e);
+    }
+    if (c->ev_kind.size() < c->ev_used + 1) c->ev_kind.resize(c->ev_used + 1);
+    c->ev_kind[c->ev_used] = kind;
+    cudaEventRecord(c->ev_pool[2 * c->ev_used], c->stream);
+}
+static void prof_end(rt_ctx *c)
+{
+    if (!c->profiling) return;
+    cudaEventRecord(c->ev_pool[2 * c->ev_used + 1], c->stream);
+    c->ev_used++;
+}
+
+struct rt_scene {
+    rt_ctx *ctx = nullptr;
+    DevScene S;
+    std::vector<void *> allocs;
+    int64_t bytes = 0;
+    float bounds[6];
+    int n_lights = 0;
+    int n_bsdfs = 0;
+    std::vector<float> light_power_lum;  // per light, for the weighted strategy
+    std::vector<DevLight> lights_host;
+    DevLight *lights_dev = nullptr;
+};
+
+template <typename T>
+static rt_status upload(rt_scene *sc, const T *host, size_t count, const T **dev)
+{
+    *dev = nullptr;
+    if (count == 0) return RT_OK;
+    void *p = nullptr;
+    cudaError_t e = cudaMalloc(&p, sizeof(T) * count);
+    if (e != cudaSuccess) return fail(RT_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    sc->allocs.push_back(p);
+    sc->bytes += (int64_t)(sizeof(T) * count);
+    e = cudaMemcpy(p, host, sizeof(T) * count, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return fail(RT_ERR_CUDA, std::string("cudaMemcpy: ") + cudaGetErrorString(e));
+    *dev = (const T *)p;
+    return RT_OK;
+}
+
+// ---------------------------------------------------------------- host math mirrors
+static float h_cavg1(float v) { float s = 0.f; s += v; s += v; s += v; return s / 3.f; }
+static float h_lum(float r, float g, float b) { return 0.2126f * r + 0.7152f * g + 0.0722f * b; }
+static float h_smin(float a, float b) { return (b < a) ? b : a; }
+static float h_smax(float a, float b) { return (a < b) ? b : a; }
+
+struct HCdf {
+    std::vector<float> c{0.f};
+    float sum = 0.f;
+    void add(float p) { sum += p; c.push_back(sum); }
+    void normalize()
+    {
+        if (sum != 0.f) {
+            float f = 1.f / sum;
+            for (size_t i = 1; i < c.size(); i++) c[i] *= f;
+            c.back() = 1.f;
+        }
+    }
+};
+
+static void mat_mul4(const double *a, const double *b, double *o)
+{
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) {
+            double s = 0;
+            for (int k = 0; k < 4; k++) s += a[i * 4 + k] * b[k * 4 + j];
+            o[i * 4 + j] = s;
+        }
+}
+static bool mat_inv4(const double *m, double *inv)
+{
+    double a[4][8];
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 8; j++) a[i][j] = j < 4 ? m[i * 4 + j] : (j - 4 == i ? 1.0 : 0.0);
+    for (int c = 0; c < 4; c++) {
+        int p = c;
+        for (int r = c + 1; r < 4; r++) if (std::fabs(a[r][c]) > std::fabs(a[p][c])) p = r;
+        if (a[p][c] == 0) return false;
+        if (p != c) for (int j = 0; j < 8; j++) std::swap(a[p][j], a[c][j]);
+        double d = a[c][c];
+        for (int j = 0; j < 8; j++) a[c][j] /= d;
+        for (int r = 0; r < 4; r++) {
+            if (r == c) continue;
+            double f = a[r][c];
+            for (int j = 0; j < 8; j++) a[r][j] -= f * a[c][j];
+        }
+    }
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) inv[i * 4 + j] = a[i][j + 4];
+    return true;
+}
+static V3 h_xf_point(const float *m, V3 p) { return xf_point(m, p); }
+
+// Heterogeneous::setOwnerBBox (medium/Heterogeneous.cpp:281-369), matrices in double
+static void setup_hetero(const rt_medium_desc &m, const float *bmin, const float *bmax, DevMedium &D)
+{
+    double gmn[3], gmx[3], bmn[3], bmx[3];
+    for (int i = 0; i < 3; i++) { gmn[i] = m.grid_min[i]; gmx[i] = m.grid_max[i]; bmn[i] = bmin[i]; bmx[i] = bmax[i]; }
+    double ratio = (bmx[0] - bmn[0]) / (gmx[0] - gmn[0]);
+    double ry = (bmx[1] - bmn[1]) / (gmx[1] - gmn[1]);
+    if (ry < ratio) ratio = ry;
+    double rz = (bmx[2] - bmn[2]) / (gmx[2] - gmn[2]);
+    if (rz < ratio) ratio = rz;
+    double S[16] = {0}, ext[3];
+    for (int i = 0; i < 3; i++) { ext[i] = (gmx[i] - gmn[i]) * ratio; S[i * 5] = 1.0 / ext[i]; }
+    S[15] = 1;
+    double T[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+    for (int i = 0; i < 3; i++) T[i * 4 + 3] = m.centered ? -(bmn[i] + ((bmx[i] - bmn[i]) / 2.0 - ext[i] / 2.0)) : -bmn[i];
+    double Wm[16], Winv[16];
+    for (int i = 0; i < 16; i++) Wm[i] = m.to_world[i];
+    if (!mat_inv4(Wm, Winv)) std::memcpy(Winv, Wm, sizeof(Wm));
+    double ST[16], A[16], Ainv[16];
+    mat_mul4(S, T, ST);
+    mat_mul4(ST, Winv, A);
+    mat_inv4(A, Ainv);
+    float a2w[16];
+    for (int i = 0; i < 16; i++) { D.world_to_array[i] = (float)A[i]; a2w[i] = (float)Ainv[i]; }
+    float mn[3] = {RT_MAX_REAL, RT_MAX_REAL, RT_MAX_REAL}, mx[3] = {-RT_MAX_REAL, -RT_MAX_REAL, -RT_MAX_REAL};
+    const float c[8][3] = {{0, 0, 0}, {0, 0, 1}, {0, 1, 1}, {1, 1, 1}, {1, 0, 0}, {1, 1, 0}, {1, 0, 1}, {0, 1, 0}};
+    for (int k = 0; k < 8; k++) {
+        V3 p = h_xf_point(a2w, v3(c[k][0], c[k][1], c[k][2]));
+        mn[0] = h_smin(mn[0], p.x); mn[1] = h_smin(mn[1], p.y); mn[2] = h_smin(mn[2], p.z);
+        mx[0] = h_smax(mx[0], p.x); mx[1] = h_smax(mx[1], p.y); mx[2] = h_smax(mx[2], p.z);
+    }
+    for (int i = 0; i < 3; i++) { D.wbox_min[i] = mn[i]; D.wbox_max[i] = mx[i]; }
+    size_t nv = (size_t)m.res[0] * m.res[1] * m.res[2];
+    float mxs = m.density[0];
+    for (size_t i = 1; i < nv; i++) if (m.density[i] > mxs) mxs = m.density[i];
+    D.max_sigma_t = mxs * m.scale;
+}
+
+// =====================================================================
+// C ABI
+// =====================================================================
+extern "C" {
+
+int32_t rt_abi_version(void) { return RTGPU_ABI_VERSION; }
+const char *rt_last_error(void) { return g_err.c_str(); }
+uint64_t rt_mix64(uint64_t x) { return mix64(x); }
+
+rt_status rt_ctx_create(int32_t device, rt_ctx **out)
+{
+    if (!out) return fail(RT_ERR_INVALID, "rt_ctx_create: null out");
+    *out = nullptr;
+    int n = 0;
+    CK(cudaGetDeviceCount(&n));
+    if (device < 0 || device >= n) return fail(RT_ERR_INVALID, "rt_ctx_create: bad device index");
+    CK(cudaSetDevice(device));
+    rt_ctx *c = new rt_ctx();
+    c->device = device;
+    cudaDeviceProp prop;
+    cudaError_t e = cudaGetDeviceProperties(&prop, device);
+    if (e != cudaSuccess) { delete c; return fail(RT_ERR_CUDA, cudaGetErrorString(e)); }
+    c->sm_count = prop.multiProcessorCount;
+    e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { delete c; return fail(RT_ERR_CUDA, cudaGetErrorString(e)); }
+    c->own_stream = true;
+    cudaMalloc(&c->work, sizeof(int) * 4);
+    cudaMalloc(&c->limit_flag, sizeof(int));
+    cudaMalloc(&c->stats, sizeof(unsigned long long) * 8);
+    cudaEventCreate(&c->ev0);
+    cudaEventCreate(&c->ev1);
+    std::memset(&c->last, 0, sizeof(c->last));
+    *out = c;
+    return RT_OK;
+}
+
+static void free_wave(rt_ctx *c)
+{
+    for (void *p : c->wave_allocs) cudaFree(p);
+    c->wave_allocs.clear();
+    c->capacity = 0;
+}
+
+rt_status rt_ctx_destroy(rt_ctx *c)
+{
+    if (!c) return RT_OK;
+    cudaSetDevice(c->device);
+    free_wave(c);
+    cudaFree(c->tileorder);
+    cudaFree(c->work);
+    cudaFree(c->limit_flag);
+    cudaFree(c->stats);
+    cudaFree(c->light_cdf);
+    cudaFree(c->film);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return RT_OK;
+}
+
+rt_status rt_ctx_set_profiling(rt_ctx *c, int32_t level)
+{
+    if (!c) return fail(RT_ERR_INVALID, "null ctx");
+    if (level < 0 || level > 2) return fail(RT_ERR_INVALID, "profiling level must be 0, 1 or 2");
+    c->profiling = level;
+    return RT_OK;
+}
+
+rt_status rt_ctx_set_stream(rt_ctx *c, void *stream)
+{
+    if (!c) return fail(RT_ERR_INVALID, "null ctx");
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    c->stream = (cudaStream_t)stream;
+    c->own_stream = false;
+    return RT_OK;
+}
+
+rt_status rt_scene_destroy(rt_scene *sc)
+{
+    if (!sc) return RT_OK;
+    for (void *p : sc->allocs) cudaFree(p);
+    delete sc;
+    return RT_OK;
+}
+
+static rt_status validate(const rt_scene_desc *d)
+{
+    if (!d) return fail(RT_ERR_INVALID, "null scene desc");
+    if (d->n_triangles < 0 || d->n_vertices < 0 || d->n_meshes < 0 || d->n_spheres < 0 || d->n_bsdfs < 0 ||
+        d->n_lights < 0 || d->n_media < 0)
+        return fail(RT_ERR_INVALID, "negative count in scene desc");
+    if (d->n_triangles > (1 << 27)) return fail(RT_ERR_LIMIT, "more than 2^27 triangles");
+    if (d->n_triangles > 0 && (!d->vertices || !d->indices)) return fail(RT_ERR_INVALID, "missing geometry arrays");
+    for (int i = 0; i < 3 * d->n_triangles; i++)
+        if (d->indices[i] < 0 || d->indices[i] >= d->n_vertices) return fail(RT_ERR_INVALID, "vertex index out of range");
+    int64_t covered = 0;
+    for (int m = 0; m < d->n_meshes; m++) {
+        const rt_mesh_desc &M = d->meshes[m];
+        if (M.first_tri < 0 || M.n_tris < 0 || (int64_t)M.first_tri + M.n_tris > d->n_triangles)
+            return fail(RT_ERR_INVALID, "mesh triangle range out of bounds");
+        if (M.bsdf >= d->n_bsdfs || M.light >= d->n_lights || M.interior >= d->n_media || M.exterior >= d->n_media)
+            return fail(RT_ERR_INVALID, "mesh references a missing component");
+        covered += M.n_tris;
+    }
+    if (covered != d->n_triangles) return fail(RT_ERR_INVALID, "meshes must cover every triangle exactly once");
+    for (int s = 0; s < d->n_spheres; s++) {
+        const rt_sphere_desc &S = d->spheres[s];
+        if (S.bsdf >= d->n_bsdfs || S.light >= d->n_lights || S.interior >= d->n_media || S.exterior >= d->n_media)
+            return fail(RT_ERR_INVALID, "sphere references a missing component");
+    }
+    for (int l = 0; l < d->n_lights; l++) {
+        const rt_light_desc &L = d->lights[l];
+        if (L.type == RT_LIGHT_ENV) {
+            if (L.env_width < 2 || L.env_height < 2 || !L.env_rgb) return fail(RT_ERR_INVALID, "bad environment map");
+        } else if (L.type == RT_LIGHT_AREA) {
+            if (L.shape_kind == RT_SHAPE_MESH ? (L.shape < 0 || L.shape >= d->n_meshes || d->meshes[L.shape].n_tris == 0)
+                                              : (L.shape < 0 || L.shape >= d->n_spheres))
+                return fail(RT_ERR_INVALID, "area light without a valid shape");
+        } else {
+            return fail(RT_ERR_UNSUPPORTED, "light type not supported");
+        }
+    }
+    for (int b = 0; b < d->n_bsdfs; b++)
+        if (d->bsdfs[b].type < 0 || d->bsdfs[b].type > 3) return fail(RT_ERR_UNSUPPORTED, "BSDF type not supported");
+    for (int m = 0; m < d->n_media; m++) {
+        const rt_medium_desc &M = d->media[m];
+        if (M.type == RT_MEDIUM_HETEROGENEOUS && (!M.density || M.res[0] < 2 || M.res[1] < 2 || M.res[2] < 2))
+            return fail(RT_ERR_INVALID, "heterogeneous medium without a grid");
+    }
+    if (d->env_light >= d->n_lights) return fail(RT_ERR_INVALID, "env_light index out of range");
+    if (d->camera.width <= 0 || d->camera.height <= 0 || d->camera.width > 32768 || d->camera.height > 32768)
+        return fail(RT_ERR_INVALID, "bad film size");
+    if (d->camera.medium >= d->n_media) return fail(RT_ERR_INVALID, "camera medium out of range");
+    return RT_OK;
+}
+
+rt_status rt_scene_create(rt_ctx *ctx, const rt_scene_desc *d, rt_scene **out)
+{
+    if (!ctx || !out) return fail(RT_ERR_INVALID, "rt_scene_create: null argument");
+    *out = nullptr;
+    rt_status st = validate(d);
+    if (st != RT_OK) return st;
+    CK(cudaSetDevice(ctx->device));
+    rt_scene *sc = new rt_scene();
+    sc->ctx = ctx;
+    DevScene &S = sc->S;
+    std::memset(&S, 0, sizeof(S));
+    const int nt = d->n_triangles;
+    // per-triangle original vertices / normals / mesh id
+    std::vector<float> tri_v(9 * (size_t)nt), tri_n;
+    std::vector<int> tri_mesh(nt, 0);
+    for (int t = 0; t < nt; t++)
+        for (int k = 0; k < 3; k++)
+            for (int a = 0; a < 3; a++) tri_v[9 * (size_t)t + 3 * k + a] = d->vertices[3 * (size_t)d->indices[3 * (size_t)t + k] + a];
+    if (d->normals) {
+        tri_n.resize(9 * (size_t)nt);
+        for (int t = 0; t < nt; t++)
+            for (int k = 0; k < 3; k++)
+                for (int a = 0; a < 3; a++) tri_n[9 * (size_t)t + 3 * k + a] = d->normals[3 * (size_t)d->indices[3 * (size_t)t + k] + a];
+    }
+    // meshes: area CDF (Mesh.cpp:19-31) and owner boxes
+    std::vector<DevMesh> meshes(d->n_meshes);
+    std::vector<float> mesh_cdf;
+    std::vector<float> mbox(6 * (size_t)std::max(1, d->n_meshes));
+    float bmin[3] = {RT_MAX_REAL, RT_MAX_REAL, RT_MAX_REAL}, bmax[3] = {-RT_MAX_REAL, -RT_MAX_REAL, -RT_MAX_REAL};
+    for (int m = 0; m < d->n_meshes; m++) {
+        const rt_mesh_desc &M = d->meshes[m];
+        DevMesh &D = meshes[m];
+        D.first_tri = M.first_tri; D.n_tris = M.n_tris; D.bsdf = M.bsdf; D.light = M.light;
+        D.interior = M.interior; D.exterior = M.exterior;
+        D.cdf_off = (int)mesh_cdf.size();
+        HCdf c;
+        float area = 0.f;
+        float *mb = &mbox[6 * (size_t)m];
+        for (int i = 0; i < 3; i++) { mb[i] = RT_MAX_REAL; mb[3 + i] = -RT_MAX_REAL; }
+        for (int i = 0; i < M.n_tris; i++) {
+            int t = M.first_tri + i;
+            tri_mesh[t] = m;
+            const float *P = &tri_v[9 * (size_t)t];
+            V3 p0 = vload(P), p1 = vload(P + 3), p2 = vload(P + 6);
+            float a = 0.5f * norm(cross(p1 - p0, p2 - p0));
+            c.add(a);
+            area += a;
+            for (int k = 0; k < 3; k++)
+                for (int ax = 0; ax < 3; ax++) {
+                    mb[ax] = h_smin(mb[ax], P[3 * k + ax]);
+                    mb[3 + ax] = h_smax(mb[3 + ax], P[3 * k + ax]);
+                }
+        }
+        c.normalize();
+        D.area = area;
+        mesh_cdf.insert(mesh_cdf.end(), c.c.begin(), c.c.end());
+        for (int ax = 0; ax < 3; ax++) { bmin[ax] = h_smin(bmin[ax], mb[ax]); bmax[ax] = h_smax(bmax[ax], mb[3 + ax]); }
+    }
+    // spheres
+    std::vector<DevSphere> spheres(d->n_spheres);
+    for (int s = 0; s < d->n_spheres; s++) {
+        const rt_sphere_desc &Sd = d->spheres[s];
+        DevSphere &D = spheres[s];
+        D.radius = Sd.radius;
+        std::memcpy(D.to_world, Sd.to_world, sizeof(D.to_world));
+        std::memcpy(D.to_object, Sd.to_object, sizeof(D.to_object));
+        D.bsdf = Sd.bsdf; D.light = Sd.light; D.interior = Sd.interior; D.exterior = Sd.exterior;
+        float r = Sd.radius;
+        float lo[3] = {-r, -r, -r}, hi[3] = {r, r, r};
+        const float cx[8][3] = {{lo[0], lo[1], lo[2]}, {lo[0], lo[1], hi[2]}, {lo[0], hi[1], hi[2]}, {hi[0], hi[1], hi[2]},
+                                {hi[0], lo[1], lo[2]}, {hi[0], hi[1], lo[2]}, {hi[0], lo[1], hi[2]}, {lo[0], hi[1], lo[2]}};
+        for (int k = 0; k < 8; k++) {
+            V3 p = h_xf_point(Sd.to_world, v3(cx[k][0], cx[k][1], cx[k][2]));
+            bmin[0] = h_smin(bmin[0], p.x); bmin[1] = h_smin(bmin[1], p.y); bmin[2] = h_smin(bmin[2], p.z);
+            bmax[0] = h_smax(bmax[0], p.x); bmax[1] = h_smax(bmax[1], p.y); bmax[2] = h_smax(bmax[2], p.z);
+        }
+    }
+    for (int i = 0; i < 3; i++) { sc->bounds[i] = bmin[i]; sc->bounds[3 + i] = bmax[i]; S.bmin[i] = bmin[i]; S.bmax[i] = bmax[i]; }
+    // BSDFs
+    std::vector<DevBsdf> bsdfs(d->n_bsdfs);
+    for (int b = 0; b < d->n_bsdfs; b++) {
+        const rt_bsdf_desc &B = d->bsdfs[b];
+        DevBsdf &D = bsdfs[b];
+        D.type = B.type; D.distribution = B.distribution;
+        for (int i = 0; i < 3; i++) {
+            D.albedo[i] = B.albedo[i]; D.reflectance[i] = B.reflectance[i]; D.transmittance[i] = B.transmittance[i];
+            D.eta[i] = B.eta[i]; D.k[i] = B.k[i]; D.absorbance[i] = B.absorbance[i];
+        }
+        D.alpha = B.alpha;
+        D.alpha_avg = h_cavg1(B.alpha);
+        D.eta_int = B.eta_int; D.eta_ext = B.eta_ext; D.thickness = B.thickness;
+    }
+    // media
+    std::vector<DevMedium> media(d->n_media);
+    for (int m = 0; m < d->n_media; m++) {
+        const rt_medium_desc &M = d->media[m];
+        DevMedium &D = media[m];
+        std::memset(&D, 0, sizeof(D));
+        D.type = M.type; D.phase = M.phase; D.g = M.g; D.scale = M.scale;
+        float sa[3], ss[3];
+        for (int i = 0; i < 3; i++) { sa[i] = M.sigma_a[i]; ss[i] = M.sigma_s[i]; D.albedo[i] = M.albedo[i]; }
+        if (M.scale != 1.f) for (int i = 0; i < 3; i++) { sa[i] *= M.scale; ss[i] *= M.scale; }
+        for (int i = 0; i < 3; i++) { D.sigma_t[i] = sa[i] + ss[i]; D.sigma_s[i] = ss[i]; D.res[i] = M.res[i]; }
+    }
+    // Heterogeneous owner boxes, in mesh order, interior then exterior (MeshFactory.h:133-136)
+    for (int m = 0; m < d->n_meshes; m++) {
+        const rt_mesh_desc &M = d->meshes[m];
+        if (M.n_tris == 0) continue;
+        const float *mb = &mbox[6 * (size_t)m];
+        if (M.interior >= 0 && d->media[M.interior].type == RT_MEDIUM_HETEROGENEOUS)
+            setup_hetero(d->media[M.interior], mb, mb + 3, media[M.interior]);
+        if (M.exterior >= 0 && d->media[M.exterior].type == RT_MEDIUM_HETEROGENEOUS)
+            setup_hetero(d->media[M.exterior], mb, mb + 3, media[M.exterior]);
+    }
+    // lights
+    std::vector<DevLight> lights(d->n_lights);
+    sc->light_power_lum.assign(d->n_lights, 0.f);
+    for (int l = 0; l < d->n_lights; l++) {
+        const rt_light_desc &L = d->lights[l];
+        DevLight &D = lights[l];
+        std::memset(&D, 0, sizeof(D));
+        D.type = L.type; D.mesh_light = L.mesh_light; D.shape_kind = L.shape_kind; D.shape = L.shape;
+        for (int i = 0; i < 3; i++) D.radiance[i] = L.radiance[i];
+        std::memcpy(D.env_to_world, L.env_to_world, sizeof(D.env_to_world));
+        std::memcpy(D.env_to_light, L.env_to_light, sizeof(D.env_to_light));
+        if (L.type == RT_LIGHT_ENV) {
+            int Wd = L.env_width, H = L.env_height;
+            D.env_w = Wd; D.env_h = H; D.env_scale = L.env_scale;
+            std::vector<float> rows((size_t)H * (Wd + 1)), weight(H);
+            HCdf marg;
+            for (int i = 0; i < H; i++) {
+                float w = sinf(RT_PI * ((float)i + 0.5f) / (float)H);
+                HCdf row;
+                for (int j = 0; j < Wd; j++) {
+                    const float *p = L.env_rgb + 3 * ((size_t)i * Wd + j);
+                    row.add(h_lum(p[0] * L.env_scale, p[1] * L.env_scale, p[2] * L.env_scale));
+                }
+                weight[i] = w;
+                marg.add(row.sum * w);
+                row.normalize();
+                std::copy(row.c.begin(), row.c.end(), rows.begin() + (size_t)i * (Wd + 1));
+            }
+            marg.normalize();
+            D.env_marginal_sum = marg.sum;
+            V3 bmn = vload(bmin), bmx = vload(bmax);
+            V3 c = 0.5f * (bmx + bmn);
+            D.env_radius = 2 * h_smax(norm(bmn - c), norm(bmx - c));
+            const float *dp;
+            if ((st = upload(sc, L.env_rgb, 3 * (size_t)Wd * H, &dp)) != RT_OK) { rt_scene_destroy(sc); return st; }
+            D.env_rgb = dp;
+            if ((st = upload(sc, rows.data(), rows.size(), &dp)) != RT_OK) { rt_scene_destroy(sc); return st; }
+            D.env_row_cdf = dp;
+            if ((st = upload(sc, marg.c.data(), marg.c.size(), &dp)) != RT_OK) { rt_scene_destroy(sc); return st; }
+            D.env_marginal = dp;
+            if ((st = upload(sc, weight.data(), weight.size(), &dp)) != RT_OK) { rt_scene_destroy(sc); return st; }
+            D.env_weight = dp;
+            float R = D.env_radius;
+            float pw = 4 * RT_PI * R * R;
+            sc->light_power_lum[l] = h_lum(1.f * pw, 1.f * pw, 1.f * pw);
+        } else {
+            float area;
+            if (L.shape_kind == RT_SHAPE_MESH) area = meshes[L.shape].area;
+            else { float r = d->spheres[L.shape].radius; area = 4.f * RT_PI * r * r * r; }
+            sc->light_power_lum[l] = h_lum(RT_PI * L.radiance[0] * area, RT_PI * L.radiance[1] * area,
+                                           RT_PI * L.radiance[2] * area);
+        }
+    }
+    // medium grids
+    for (int m = 0; m < d->n_media; m++) {
+        const rt_medium_desc &M = d->media[m];
+        if (M.type != RT_MEDIUM_HETEROGENEOUS) continue;
+        const float *dp;
+        if ((st = upload(sc, M.density, (size_t)M.res[0] * M.res[1] * M.res[2], &dp)) != RT_OK) { rt_scene_destroy(sc); return st; }
+        media[m].density = dp;
+    }
+    // BVH
+    BvhImage img;
+    build_bvh2(tri_v.data(), nt, img, 4, 32);
+    const float4 *np = nullptr, *tp = nullptr;
+    if ((st = upload(sc, reinterpret_cast<const float4 *>(img.nodes.data()), (size_t)img.n_nodes * 4, &np)) != RT_OK) { rt_scene_destroy(sc); return st; }
+    if ((st = upload(sc, reinterpret_cast<const float4 *>(img.tri_slots.data()), (size_t)img.n_slots * 3, &tp)) != RT_OK) { rt_scene_destroy(sc); return st; }
+    S.nodes = np; S.tri_slots = tp; S.n_nodes = img.n_nodes;
+    const float *fp;
+    const int *ip;
+    if ((st = upload(sc, tri_v.data(), tri_v.size(), &fp)) != RT_OK) { rt_scene_destroy(sc); return st; }
+    S.tri_v = fp;
+    if (!tri_n.empty()) { if ((st = upload(sc, tri_n.data(), tri_n.size(), &fp)) != RT_OK) { rt_scene_destroy(sc); return st; } S.tri_n = fp; }
+    if ((st = upload(sc, tri_mesh.data(), tri_mesh.size(), &ip)) != RT_OK) { rt_scene_destroy(sc); return st; }
+    S.tri_mesh = ip;
+    const DevMesh *mp;
+    if ((st = upload(sc, meshes.data(), meshes.size(), &mp)) != RT_OK) { rt_scene_destroy(sc); return st; }
+    S.meshes = mp; S.n_meshes = d->n_meshes;
+    if ((st = upload(sc, mesh_cdf.data(), mesh_cdf.size(), &fp)) != RT_OK) { rt_scene_destroy(sc); return st; }
+    S.mesh_cdf = fp;
+    const DevSphere *spp;
+    if ((st = upload(sc, spheres.data(), spheres.size(), &spp)) != RT_OK) { rt_scene_destroy(sc); return st; }
+    S.spheres = spp; S.n_spheres = d->n_spheres;
+    const DevBsdf *bp;
+    if ((st = upload(sc, bsdfs.data(), bsdfs.size(), &bp)) != RT_OK) { rt_scene_destroy(sc); return st; }
+    S.bsdfs = bp;
+    const DevLight *lp;
+    if ((st = upload(sc, lights.data(), lights.size(), &lp)) != RT_OK) { rt_scene_destroy(sc); return st; }
+    S.lights = lp; S.n_lights = d->n_lights; S.env_light = d->env_light;
+    const DevMedium *mdp;
+    if ((st = upload(sc, media.data(), media.size(), &mdp)) != RT_OK) { rt_scene_destroy(sc); return st; }
+    S.media = mdp;
+    // camera
+    const rt_camera_desc &cd = d->camera;
+    S.cam.width = cd.width; S.cam.height = cd.height;
+    std::memcpy(S.cam.sample_to_camera, cd.sample_to_camera, sizeof(S.cam.sample_to_camera));
+    std::memcpy(S.cam.camera_to_world, cd.camera_to_world, sizeof(S.cam.camera_to_world));
+    S.cam.near_clip = cd.near_clip; S.cam.far_clip = cd.far_clip;
+    S.cam.aperture_radius = cd.aperture_radius; S.cam.focal_plane = cd.focal_plane;
+    S.cam.inv_w = 1.f / (float)cd.width; S.cam.inv_h = 1.f / (float)cd.height;
+    S.cam.medium = cd.medium;
+    sc->n_lights = d->n_lights;
+    sc->n_bsdfs = d->n_bsdfs;
+    *out = sc;
+    return RT_OK;
+}
+
+rt_status rt_scene_info(const rt_scene *sc, float bounds[6], int64_t *device_bytes, int32_t *bvh_nodes)
+{
+    if (!sc) return fail(RT_ERR_INVALID, "null scene");
+    if (bounds) std::memcpy(bounds, sc->bounds, sizeof(sc->bounds));
+    if (device_bytes) *device_bytes = sc->bytes;
+    if (bvh_nodes) *bvh_nodes = sc->S.n_nodes;
+    return RT_OK;
+}
+
+// ---------------------------------------------------------------- wavefront buffers
+static rt_status ensure_wave(rt_ctx *c, int capacity, int max_rounds)
+{
+    if (c->capacity >= capacity && c->W.max_rounds >= max_rounds) return RT_OK;
+    free_wave(c);
+    Wave &W = c->W;
+    size_t P = (size_t)capacity;
+    auto alloc = [&](void **p, size_t bytes) -> bool {
+        cudaError_t e = cudaMalloc(p, bytes);
+        if (e != cudaSuccess) return false;
+        c->wave_allocs.push_back(*p);
+        return true;
+    };
+    bool ok = true;
+    ok &= alloc((void **)&W.rng, P * sizeof(Pcg32));
+    ok &= alloc((void **)&W.tp, P * sizeof(float4));
+    ok &= alloc((void **)&W.rad, P * sizeof(float4));
+    ok &= alloc((void **)&W.ray_o, P * sizeof(float4));
+    ok &= alloc((void **)&W.ray_d, P * sizeof(float4));
+    ok &= alloc((void **)&W.hit, P * sizeof(float4));
+    ok &= alloc((void **)&W.bs, P * sizeof(float4));
+    ok &= alloc((void **)&W.rel_eta, P * sizeof(float));
+    ok &= alloc((void **)&W.flags, P * sizeof(int));
+    ok &= alloc((void **)&W.nee, P * sizeof(float4));
+    ok &= alloc((void **)&W.sh_o, P * sizeof(float4));
+    ok &= alloc((void **)&W.sh_d, P * sizeof(float4));
+    ok &= alloc((void **)&W.occl, P * sizeof(int));
+    ok &= alloc((void **)&W.out, P * sizeof(float4));
+    ok &= alloc((void **)&W.splat, P);
+    ok &= alloc((void **)&W.pix_irregular, P);
+    ok &= alloc((void **)&W.q_active[0], P * sizeof(int));
+    ok &= alloc((void **)&W.q_active[1], P * sizeof(int));
+    ok &= alloc((void **)&W.q_closest, P * sizeof(int));
+    ok &= alloc((void **)&W.q_shadow, P * sizeof(int));
+    ok &= alloc((void **)&W.cnt, (size_t)(max_rounds + 2) * sizeof(RoundCounters));
+    if (!ok) { free_wave(c); return fail(RT_ERR_NOMEM, "wavefront buffer allocation failed"); }
+    W.capacity = capacity;
+    W.max_rounds = max_rounds;
+    c->capacity = capacity;
+    return RT_OK;
+}
+
+static rt_status launch_check(const char *what)
+{
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(RT_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    return RT_OK;
+}
+
+rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *film_rgbw, int32_t on_device)
+{
+    if (!ctx || !sc || !rd || !film_rgbw) return fail(RT_ERR_INVALID, "rt_render: null argument");
+    if (rd->spp <= 0 || rd->sample_begin < 0) return fail(RT_ERR_INVALID, "rt_render: bad sample range");
+    if (rd->integrator != RT_INTEGRATOR_PATH_MIS && rd->integrator != RT_INTEGRATOR_VOLPATH)
+        return fail(RT_ERR_UNSUPPORTED, "rt_render: unknown integrator");
+    if (rd->integrator == RT_INTEGRATOR_PATH_MIS && rd->strategy == RT_STRATEGY_ALL_LIGHTS)
+        return fail(RT_ERR_UNSUPPORTED, "rt_render: all_lights strategy is not provided by the device path");
+    if (rd->max_depth < 0 || rd->min_depth < 0) return fail(RT_ERR_INVALID, "rt_render: negative depth");
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    const DevCamera &cam = sc->S.cam;
+    const int Wd = cam.width, H = cam.height;
+    const int bx = rd->block_x > 0 ? rd->block_x : 32, by = rd->block_y > 0 ? rd->block_y : 32;
+    if (bx > 0xffff || by > 0xffff) return fail(RT_ERR_INVALID, "block size too large");
+    const int tiles_x = (Wd + bx - 1) / bx, tiles_y = (H + by - 1) / by;
+    const size_t npix_all = (size_t)Wd * H;
+    // tile-order table (Scene.cpp:83-95 job grid, SampleJob.cpp:40-44 pixel
+    // loops); uploaded once per film size / block size
+    bool same_tiles = ctx->tile_key[0] == Wd && ctx->tile_key[1] == H && ctx->tile_key[2] == bx && ctx->tile_key[3] == by;
+    if (!same_tiles) {
+        std::vector<int4> order(npix_all);
+        ctx->tile_start.assign(tiles_x * tiles_y + 1, 0);
+        size_t g = 0;
+        for (int ty = 0; ty < tiles_y; ty++)
+            for (int tx = 0; tx < tiles_x; tx++) {
+                ctx->tile_start[ty * tiles_x + tx] = (int)g;
+                int ox = tx * bx, oy = ty * by;
+                int tw = std::min(Wd, ox + bx) - ox, th = std::min(H, oy + by) - oy;
+                for (int y = 0; y < th; y++)
+                    for (int x = 0; x < tw; x++) order[g++] = make_int4(ox + x, oy + y, x | (y << 16), tw | (th << 16));
+            }
+        ctx->tile_start[tiles_x * tiles_y] = (int)g;
+        if (ctx->tileorder_n < npix_all) {
+            cudaFree(ctx->tileorder);
+            ctx->tileorder = nullptr;
+            CK(cudaMalloc(&ctx->tileorder, npix_all * sizeof(int4)));
+            ctx->tileorder_n = npix_all;
+        }
+        CK(cudaMemcpy(ctx->tileorder, order.data(), npix_all * sizeof(int4), cudaMemcpyHostToDevice));
+        ctx->tile_key[0] = Wd; ctx->tile_key[1] = H; ctx->tile_key[2] = bx; ctx->tile_key[3] = by;
+    }
+    const std::vector<int> &tile_start = ctx->tile_start;
+    // light selection CDF (Integrator::initialize, Integrator.cpp:24-38)
+    {
+        HCdf c;
+        int n = sc->n_lights;
+        float pu = (float)1. / (float)n;
+        for (int l = 0; l < n; l++) c.add(rd->strategy == RT_STRATEGY_ONE_LIGHT_WEIGHTED ? sc->light_power_lum[l] : pu);
+        c.normalize();
+        if (ctx->light_cdf_n < (int)c.c.size()) {
+            cudaFree(ctx->light_cdf);
+            ctx->light_cdf = nullptr;
+            CK(cudaMalloc(&ctx->light_cdf, c.c.size() * sizeof(float) + 64));
+            ctx->light_cdf_n = (int)c.c.size();
+        }
+        CK(cudaMemcpyAsync(ctx->light_cdf, c.c.data(), c.c.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+        CK(cudaStreamSynchronize(st));
+    }
+    // film target
+    float4 *film = nullptr;
+    if (on_device) film = reinterpret_cast<float4 *>(film_rgbw);
+    else {
+        if (ctx->film_n < npix_all) {
+            cudaFree(ctx->film);
+            ctx->film = nullptr;
+            CK(cudaMalloc(&ctx->film, npix_all * sizeof(float4)));
+            ctx->film_n = npix_all;
+        }
+        film = ctx->film;
+    }
+    // batch capacity: whole tiles, all samples of their pixels, about 4M paths
+    const int cap_target = 1 << 22;
+    const int ntiles = tiles_x * tiles_y;
+    int tile_pix = bx * by;
+    if ((int64_t)tile_pix * rd->spp > (1 << 26)) return fail(RT_ERR_LIMIT, "one tile's samples exceed the path capacity");
+    int tiles_per_batch = std::max(1, cap_target / std::max(1, tile_pix * rd->spp));
+    int capacity = std::min(tiles_per_batch, ntiles) * tile_pix * rd->spp;
+    if (rd->integrator == RT_INTEGRATOR_PATH_MIS && rd->max_depth > (1 << 16))
+        return fail(RT_ERR_LIMIT, "rt_render: max_depth above 65536 is not provided by the device path");
+    int max_rounds = rd->integrator == RT_INTEGRATOR_PATH_MIS ? rd->max_depth + 3 : 1;
+    int round_buf = max_rounds;
+    rt_status s = ensure_wave(ctx, capacity, round_buf);
+    if (s != RT_OK) return s;
+    CK(cudaMemsetAsync(ctx->stats, 0, sizeof(unsigned long long) * 8, st));
+    CK(cudaMemsetAsync(ctx->limit_flag, 0, sizeof(int), st));
+    RenderParams P;
+    P.S = sc->S;
+    P.S.light_cdf = ctx->light_cdf;
+    P.W = ctx->W;
+    P.tileorder = ctx->tileorder;
+    P.seed = rd->seed;
+    P.max_depth = rd->max_depth;
+    P.min_depth = rd->min_depth;
+    P.limit_flag = ctx->limit_flag;
+    P.stats = ctx->stats;
+    P.spp = rd->spp;
+    P.sample_begin = rd->sample_begin;
+    const int sm = ctx->sm_count > 0 ? ctx->sm_count : 1;
+    int64_t launches = 0, trace_c_launches = 0, trace_a_launches = 0;
+    int64_t total_paths = 0;
+    ctx->ev_used = 0;
+    CK(cudaEventRecord(ctx->ev0, st));
+    for (int t0 = 0; t0 < ntiles; t0 += tiles_per_batch) {
+        int t1 = std::min(ntiles, t0 + tiles_per_batch);
+        P.g0 = tile_start[t0];
+        P.npix = tile_start[t1] - tile_start[t0];
+        P.n_paths = P.npix * rd->spp;
+        total_paths += P.n_paths;
+        CK(cudaMemsetAsync(ctx->W.pix_irregular, 0, (size_t)P.npix, st));
+        CK(cudaMemsetAsync(ctx->W.cnt, 0, sizeof(RoundCounters) * (size_t)(round_buf + 2), st));
+        int cam_blocks = std::min((P.n_paths + 255) / 256, sm * 16);
+        prof_begin(ctx, K_CAMERA);
+        k_camera<<<cam_blocks, 256, 0, st>>>(P);
+        prof_end(ctx);
+        launches++;
+        if ((s = launch_check("k_camera")) != RT_OK) return s;
+        if (rd->integrator == RT_INTEGRATOR_VOLPATH) {
+            CK(cudaMemsetAsync(ctx->work, 0, sizeof(int), st));
+            prof_begin(ctx, K_VOLPATH);
+            k_volpath<<<sm * 8, 128, 0, st>>>(P, ctx->work);
+            prof_end(ctx);
+            launches++;
+            if ((s = launch_check("k_volpath")) != RT_OK) return s;
+        } else {
+            int trace_blocks = sm * 12;
+            int shade_blocks = sm * 8;
+            for (int r = 0; r < max_rounds; r++) {
+                int ri = r;
+                prof_begin(ctx, K_TRACE_C);
+                if (ctx->profiling >= 2) k_trace<false, true><<<trace_blocks, 128, 0, st>>>(P, ri);
+                else k_trace<false, false><<<trace_blocks, 128, 0, st>>>(P, ri);
+                prof_end(ctx);
+                prof_begin(ctx, K_TRACE_A);
+                if (ctx->profiling >= 2) k_trace<true, true><<<trace_blocks, 128, 0, st>>>(P, ri);
+                else k_trace<true, false><<<trace_blocks, 128, 0, st>>>(P, ri);
+                prof_end(ctx);
+                prof_begin(ctx, K_SHADE);
+                k_pt_shade<<<shade_blocks, 128, 0, st>>>(P, ri);
+                prof_end(ctx);
+                launches += 3;
+                trace_c_launches++;
+                trace_a_launches++;
+                if ((s = launch_check("pt round")) != RT_OK) return s;
+                // cheap early exit: peek at the survivor count every 4 rounds
+                if ((r & 3) == 3 && r + 1 < max_rounds) {
+                    int nact = 0;
+                    CK(cudaMemcpyAsync(&nact, &ctx->W.cnt[ri + 1].active, sizeof(int), cudaMemcpyDeviceToHost, st));
+                    CK(cudaStreamSynchronize(st));
+                    if (nact == 0) break;
+                }
+            }
+        }
+        int fb = (P.npix + 127) / 128;
+        prof_begin(ctx, K_FILM);
+        k_film<<<fb, 128, 0, st>>>(P, film, Wd);
+        prof_end(ctx);
+        launches++;
+        if ((s = launch_check("k_film")) != RT_OK) return s;
+    }
+    CK(cudaEventRecord(ctx->ev1, st));
+    if (!on_device)
+        CK(cudaMemcpyAsync(film_rgbw, film, npix_all * sizeof(float4), cudaMemcpyDeviceToHost, st));
+    unsigned long long stats[8];
+    int limit = 0;
+    CK(cudaMemcpyAsync(stats, ctx->stats, sizeof(stats), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&limit, ctx->limit_flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    std::memset(&ctx->last, 0, sizeof(ctx->last));
+    ctx->last.kernel_ms = ms;
+    double kt[K_KINDS] = {0, 0, 0, 0, 0, 0};
+    for (size_t i = 0; i < ctx->ev_used; i++) {
+        float e = 0.f;
+        cudaEventElapsedTime(&e, ctx->ev_pool[2 * i], ctx->ev_pool[2 * i + 1]);
+        kt[ctx->ev_kind[i]] += e;
+    }
+    ctx->last.camera_ms = kt[K_CAMERA];
+    ctx->last.trace_closest_ms = kt[K_TRACE_C];
+    ctx->last.trace_any_ms = kt[K_TRACE_A];
+    ctx->last.shade_ms = kt[K_SHADE];
+    ctx->last.volpath_ms = kt[K_VOLPATH];
+    ctx->last.film_ms = kt[K_FILM];
+    ctx->last.trace_closest_launches = trace_c_launches;
+    ctx->last.trace_any_launches = trace_a_launches;
+    ctx->last.nodes_closest = (int64_t)stats[3];
+    ctx->last.tris_closest = (int64_t)stats[4];
+    ctx->last.nodes_any = (int64_t)stats[5];
+    ctx->last.tris_any = (int64_t)stats[6];
+    ctx->last.paths = total_paths;
+    ctx->last.closest_rays = (int64_t)stats[0];
+    ctx->last.shadow_rays = (int64_t)stats[1];
+    ctx->last.nan_samples = (int64_t)stats[2];
+    ctx->last.launches = launches;
+    ctx->last.limit_hits = limit;
+    if (limit) return fail(RT_ERR_LIMIT, "a device loop reached its iteration cap");
+    return RT_OK;
+}
+
+rt_status rt_render_stats_get(const rt_ctx *ctx, rt_render_stats *out)
+{
+    if (!ctx || !out) return fail(RT_ERR_INVALID, "null argument");
+    *out = ctx->last;
+    return RT_OK;
+}
+
+rt_status rt_trace(rt_ctx *ctx, rt_scene *sc, const rt_ray *rays, int32_t n, int32_t anyhit, rt_hit *hits, int32_t on_device)
+{
+    if (!ctx || !sc || (!rays && n) || (!hits && n) || n < 0) return fail(RT_ERR_INVALID, "rt_trace: bad argument");
+    if (n == 0) return RT_OK;
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    const rt_ray *dr = rays;
+    rt_hit *dh = hits;
+    void *tmp_r = nullptr, *tmp_h = nullptr;
+    if (!on_device) {
+        CK(cudaMalloc(&tmp_r, sizeof(rt_ray) * (size_t)n));
+        CK(cudaMalloc(&tmp_h, sizeof(rt_hit) * (size_t)n));
+        CK(cudaMemcpyAsync(tmp_r, rays, sizeof(rt_ray) * (size_t)n, cudaMemcpyHostToDevice, st));
+        dr = (const rt_ray *)tmp_r;
+        dh = (rt_hit *)tmp_h;
+    }
+    k_trace_rays<<<(n + 127) / 128, 128, 0, st>>>(sc->S, dr, n, anyhit, dh);
+    rt_status s = launch_check("k_trace_rays");
+    if (s == RT_OK && !on_device) {
+        cudaError_t e = cudaMemcpyAsync(hits, tmp_h, sizeof(rt_hit) * (size_t)n, cudaMemcpyDeviceToHost, st);
+        if (e != cudaSuccess) s = fail(RT_ERR_CUDA, cudaGetErrorString(e));
+    }
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (s == RT_OK && e != cudaSuccess) s = fail(RT_ERR_CUDA, cudaGetErrorString(e));
+    if (tmp_r) cudaFree(tmp_r);
+    if (tmp_h) cudaFree(tmp_h);
+    return s;
+}
+
+rt_status rt_bsdf_query(rt_ctx *ctx, rt_scene *sc, int32_t bsdf, int32_t op, const rt_bsdf_q *q, int32_t n, rt_bsdf_r *r)
+{
+    if (!ctx || !sc || n < 0 || (n && (!q || !r))) return fail(RT_ERR_INVALID, "rt_bsdf_query: bad argument");
+    if (op < 0 || op > 2) return fail(RT_ERR_INVALID, "rt_bsdf_query: bad op");
+    if (bsdf < 0 || bsdf >= sc->n_bsdfs) return fail(RT_ERR_INVALID, "rt_bsdf_query: bad bsdf index");
+    if (n == 0) return RT_OK;
+    CK(cudaSetDevice(ctx->device));
+    void *dq = nullptr, *dr = nullptr;
+    CK(cudaMalloc(&dq, sizeof(rt_bsdf_q) * (size_t)n));
+    CK(cudaMalloc(&dr, sizeof(rt_bsdf_r) * (size_t)n));
+    CK(cudaMemcpy(dq, q, sizeof(rt_bsdf_q) * (size_t)n, cudaMemcpyHostToDevice));
+    k_bsdf_query<<<(n + 127) / 128, 128, 0, ctx->stream>>>(sc->S, bsdf, op, (const rt_bsdf_q *)dq, n, (rt_bsdf_r *)dr);
+    rt_status s = launch_check("k_bsdf_query");
+    cudaStreamSynchronize(ctx->stream);
+    if (s == RT_OK) {
+        cudaError_t e = cudaMemcpy(r, dr, sizeof(rt_bsdf_r) * (size_t)n, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) s = fail(RT_ERR_CUDA, cudaGetErrorString(e));
+    }
+    cudaFree(dq);
+    cudaFree(dr);
+    return s;
+}
+
+rt_status rt_light_query(rt_ctx *ctx, rt_scene *sc, int32_t light, const rt_light_q *q, int32_t n, rt_light_r *r)
+{
+    if (!ctx || !sc || n < 0 || (n && (!q || !r))) return fail(RT_ERR_INVALID, "rt_light_query: bad argument");
+    if (light < 0 || light >= sc->n_lights) return fail(RT_ERR_INVALID, "rt_light_query: bad light");
+    if (n == 0) return RT_OK;
+    CK(cudaSetDevice(ctx->device));
+    void *dq = nullptr, *dr = nullptr;
+    CK(cudaMalloc(&dq, sizeof(rt_light_q) * (size_t)n));
+    CK(cudaMalloc(&dr, sizeof(rt_light_r) * (size_t)n));
+    CK(cudaMemcpy(dq, q, sizeof(rt_light_q) * (size_t)n, cudaMemcpyHostToDevice));
+    k_light_query<<<(n + 127) / 128, 128, 0, ctx->stream>>>(sc->S, light, (const rt_light_q *)dq, n, (rt_light_r *)dr);
+    rt_status s = launch_check("k_light_query");
+    cudaStreamSynchronize(ctx->stream);
+    if (s == RT_OK) {
+        cudaError_t e = cudaMemcpy(r, dr, sizeof(rt_light_r) * (size_t)n, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) s = fail(RT_ERR_CUDA, cudaGetErrorString(e));
+    }
+    cudaFree(dq);
+    cudaFree(dr);
+    return s;
+}
+
+}  // extern "C"

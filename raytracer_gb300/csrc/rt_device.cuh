@@ -1,0 +1,1198 @@
+// rt_device.cuh -- device-resident scene layout and the per-vertex physics
+// of the reference renderer (BSDFs, lights, camera, media, ray casting).
+//
+// Reference paths are relative to RaytracerNew2/src of Iscandel/Raytracer.
+// Each routine keeps the reference's operation order so that, fed the same
+// sample stream, the device reproduces the CPU renderer's arithmetic
+// (transcendental functions excepted: CUDA's expf/logf/sinf/... differ from
+// the C library by at most a few ulp).
+#pragma once
+#include "rt_math.cuh"
+
+// ------------------------------------------------------------------ layout
+struct DevMesh {
+    int first_tri, n_tris, bsdf, light, interior, exterior;
+    int cdf_off;      // offset of this mesh's area CDF (n_tris + 1 floats)
+    float area;       // Mesh::mySurfaceArea
+};
+
+struct DevSphere {
+    float radius;
+    float to_world[16];
+    float to_object[16];
+    int bsdf, light, interior, exterior;
+};
+
+struct DevBsdf {
+    int type, distribution;
+    float albedo[3], reflectance[3], transmittance[3], eta[3], k[3];
+    float alpha;      // raw "alpha" texture value
+    float alpha_avg;  // Color(alpha).average() as the BSDFs read it
+    float eta_int, eta_ext, thickness;
+    float absorbance[3];
+};
+
+struct DevLight {
+    int type, mesh_light, shape_kind, shape;
+    float radiance[3];
+    // environment map
+    int env_w, env_h;
+    float env_scale;
+    const float *env_rgb;       // W*H*3
+    const float *env_row_cdf;   // H * (W + 1)
+    const float *env_marginal;  // H + 1
+    const float *env_weight;    // H
+    float env_marginal_sum;
+    float env_radius;           // bounding sphere radius (EnvironmentLight::initialize)
+    float env_to_world[16], env_to_light[16];
+};
+
+struct DevMedium {
+    int type, phase;
+    float g;
+    float sigma_t[3], sigma_s[3];  // Homogeneous, scale applied (Homogeneous.cpp:16-22)
+    float scale;
+    float albedo[3];
+    int res[3];
+    const float *density;
+    float world_to_array[16];
+    float wbox_min[3], wbox_max[3];
+    float max_sigma_t;
+};
+
+struct DevCamera {
+    int width, height;
+    float sample_to_camera[16], camera_to_world[16];
+    float near_clip, far_clip, aperture_radius, focal_plane;
+    float inv_w, inv_h;
+    int medium;
+};
+
+struct DevScene {
+    // BVH2 (two child boxes per node, 64 B): see rt_bvh.cpp for the layout
+    const float4 *nodes;
+    const float4 *tri_slots;    // 3 float4 per leaf slot: (p0, id), (e1, 0), (e2, 0)
+    int n_nodes;
+    // original geometry
+    const float *tri_v;         // 9 floats per triangle (p0, p1, p2)
+    const float *tri_n;         // 9 floats per triangle (n0, n1, n2) or null
+    const int *tri_mesh;
+    const DevMesh *meshes;
+    const float *mesh_cdf;
+    int n_meshes;
+    const DevSphere *spheres;
+    int n_spheres;
+    const DevBsdf *bsdfs;
+    const DevLight *lights;
+    int n_lights;
+    int env_light;
+    const float *light_cdf;     // n_lights + 1 (Integrator::myLightWeights)
+    const DevMedium *media;
+    DevCamera cam;
+    float bmin[3], bmax[3];
+};
+
+// ------------------------------------------------------------------ rays / hits
+struct Ray {
+    V3 o, d;
+    float mint, maxt;
+};
+__device__ __forceinline__ Ray make_ray(V3 o, V3 d, float mint, float maxt)
+{
+    Ray r; r.o = o; r.d = d; r.mint = mint; r.maxt = maxt; return r;
+}
+
+struct Hit {
+    float t, u, v;
+    int prim;   // triangle id, -(sphere)-2, -1 = none
+};
+
+struct Frame {
+    V3 p;       // hit point
+    V3 n, s, t; // shading frame
+};
+
+// BoundingBox::intersection (core/BoundingBox.h:154-183)
+__device__ __forceinline__ bool ref_box_hit(const float *bmin, const float *bmax, V3 o, V3 d, float mint,
+                                            float maxt, float &nearT, float &farT)
+{
+    nearT = -RT_MAX_REAL;
+    farT = RT_MAX_REAL;
+    V3 inv = v3(1.f / d.x, 1.f / d.y, 1.f / d.z);
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        float oo = vget(o, i), dd = vget(d, i), iv = vget(inv, i);
+        float mn = bmin[i], mx = bmax[i];
+        if (dd == 0) {
+            if (oo < mn || oo > mx) return false;
+        } else {
+            float t1 = (mn - oo) * iv;
+            float t2 = (mx - oo) * iv;
+            if (t1 > t2) { float q = t1; t1 = t2; t2 = q; }
+            nearT = smax(t1, nearT);
+            farT = smin(t2, farT);
+            if (!(nearT <= farT)) return false;
+        }
+    }
+    return (mint <= farT && maxt >= nearT);
+}
+
+// ------------------------------------------------------------------ traversal
+// |det| < 1e-8 (double compare in Triangle.cpp:66) <=> |det| <= float32(1e-8)
+#define RT_DET_EPS 9.99999993922529e-09f
+#define RT_STACK 64
+
+// Triangle::intersection (geometricShape/Triangle.cpp:46-88), exact order
+__device__ __forceinline__ bool mt_test(float4 a, float4 b, float4 c, V3 o, V3 d, float mint, float maxt,
+                                        float &t, float &u, float &v)
+{
+    V3 p0 = v3(a.x, a.y, a.z), e1 = v3(b.x, b.y, b.z), e2 = v3(c.x, c.y, c.z);
+    V3 s = o - p0;
+    V3 s1 = cross(d, e2), s2 = cross(s, e1);
+    float det = dot(s1, e1);
+    if (fabsf(det) <= RT_DET_EPS) return false;
+    float inv = 1 / det;
+    float b1 = inv * dot(s1, s);
+    if (b1 < 0.f || b1 > 1.f) return false;
+    float b2 = inv * dot(s2, d);
+    if (b2 < 0.f || b1 + b2 > 1.f) return false;
+    float tt = inv * dot(s2, e2);
+    if (tt < mint || tt > maxt) return false;
+    t = tt; u = b1; v = b2;
+    return true;
+}
+
+// Sphere::intersection (geometricShape/Sphere.cpp:38-111)
+__device__ __forceinline__ bool sphere_test(const DevSphere &sp, V3 o, V3 d, float mint, float maxt, float &t)
+{
+    V3 lo = xf_point(sp.to_object, o);
+    V3 ld = xf_vector(sp.to_object, d);
+    V3 sto = lo - v3(0.f, 0.f, 0.f);
+    float a = 1;
+    float b = 2 * dot(ld, sto);
+    float c = dot(sto, sto) - sp.radius * sp.radius;
+    float delta = b * b - 4 * a * c;
+    if (delta < 0) return false;
+    float t1 = (-b + sqrtf(delta)) / (2 * a);
+    float t2 = (-b - sqrtf(delta)) / (2 * a);
+    float tn = t1, tf = t2;
+    if (tn > tf) { float q = tn; tn = tf; tf = q; }
+    if (tn <= mint) {
+        if (tf > mint && tf < maxt) { t = tf; return true; }
+        return false;
+    } else if (tn > mint && tn < maxt) { t = tn; return true; }
+    return false;
+}
+
+// Adaptive epsilon of Bvh::intersection (accelStruct/Bvh.cpp:411-413)
+__device__ __forceinline__ float adapt_mint(V3 o, float mint)
+{
+    if (mint == RT_EPSILON) {
+        float m = smax(smax(fabsf(o.x), fabsf(o.y)), fabsf(o.z));
+        mint = smax(mint, mint * m);
+    }
+    return mint;
+}
+
+// Leaf encoding of BVH2 child links: c >= 0 internal node index; c < 0 leaf
+// with v = ~c, first slot = v >> 3, count = (v & 7) + 1.
+__device__ __forceinline__ float rt_min4(float a, float b, float c, float d) { return fminf(fminf(a, b), fminf(c, d)); }
+__device__ __forceinline__ float rt_max4(float a, float b, float c, float d) { return fmaxf(fmaxf(a, b), fmaxf(c, d)); }
+
+// Closest / any hit through the BVH2 plus the analytic spheres.  With
+// COUNT, nodes fetched and triangle slots tested are added to cnt[0], cnt[1]
+// (the roofline's algorithmic-bytes accounting).
+template <bool ANY, bool COUNT = false>
+__device__ __forceinline__ bool trace_ray(const DevScene &S, V3 o, V3 d, float mint0, float maxt, Hit &h,
+                                          int *cnt = nullptr)
+{
+    float mint = adapt_mint(o, mint0);
+    h.prim = -1;
+    if (maxt < mint) return false;
+    float hit_t = maxt;
+    bool found = false;
+    const float eps = 1e-20f;
+    float idx = 1.0f / (fabsf(d.x) > eps ? d.x : copysignf(eps, d.x));
+    float idy = 1.0f / (fabsf(d.y) > eps ? d.y : copysignf(eps, d.y));
+    float idz = 1.0f / (fabsf(d.z) > eps ? d.z : copysignf(eps, d.z));
+    float ox = o.x * idx, oy = o.y * idy, oz = o.z * idz;
+    if (S.n_nodes > 0) {
+        int stack[RT_STACK];
+        int sp = 0;
+        int node = 0;
+        for (;;) {
+            while (node >= 0) {
+                if (COUNT) cnt[0]++;
+                const float4 *N = S.nodes + 4 * (size_t)node;
+                float4 n0 = __ldg(N), n1 = __ldg(N + 1), n2 = __ldg(N + 2);
+                int4 cc = __ldg(reinterpret_cast<const int4 *>(N + 3));
+                float c0lox = __fmaf_rn(n0.x, idx, -ox), c0hix = __fmaf_rn(n0.y, idx, -ox);
+                float c0loy = __fmaf_rn(n0.z, idy, -oy), c0hiy = __fmaf_rn(n0.w, idy, -oy);
+                float c0loz = __fmaf_rn(n2.x, idz, -oz), c0hiz = __fmaf_rn(n2.y, idz, -oz);
+                float c1lox = __fmaf_rn(n1.x, idx, -ox), c1hix = __fmaf_rn(n1.y, idx, -ox);
+                float c1loy = __fmaf_rn(n1.z, idy, -oy), c1hiy = __fmaf_rn(n1.w, idy, -oy);
+                float c1loz = __fmaf_rn(n2.z, idz, -oz), c1hiz = __fmaf_rn(n2.w, idz, -oz);
+                float c0min = rt_max4(fminf(c0lox, c0hix), fminf(c0loy, c0hiy), fminf(c0loz, c0hiz), mint);
+                float c0max = rt_min4(fmaxf(c0lox, c0hix), fmaxf(c0loy, c0hiy), fmaxf(c0loz, c0hiz), hit_t);
+                float c1min = rt_max4(fminf(c1lox, c1hix), fminf(c1loy, c1hiy), fminf(c1loz, c1hiz), mint);
+                float c1max = rt_min4(fmaxf(c1lox, c1hix), fmaxf(c1loy, c1hiy), fmaxf(c1loz, c1hiz), hit_t);
+                bool t0 = c0min <= c0max, t1 = c1min <= c1max;
+                if (!t0 && !t1) {
+                    if (sp == 0) { node = 0x7fffffff; break; }
+                    node = stack[--sp];
+                    continue;
+                }
+                if (t0 && t1) {
+                    int nearc = cc.x, farc = cc.y;
+                    if (c1min < c0min) { nearc = cc.y; farc = cc.x; }
+                    if (sp < RT_STACK) stack[sp++] = farc;
+                    node = nearc;
+                } else {
+                    node = t0 ? cc.x : cc.y;
+                }
+            }
+            if (node == 0x7fffffff) break;
+            // leaf
+            int v = ~node;
+            int first = v >> 3, cnt_leaf = (v & 7) + 1;
+            for (int i = 0; i < cnt_leaf; i++) {
+                if (COUNT) cnt[1]++;
+                const float4 *T = S.tri_slots + 3 * (size_t)(first + i);
+                float4 a = __ldg(T), b = __ldg(T + 1), c = __ldg(T + 2);
+                float t, u, w;
+                if (mt_test(a, b, c, o, d, mint, hit_t, t, u, w)) {
+                    h.t = t; h.u = u; h.v = w; h.prim = __float_as_int(a.w);
+                    found = true;
+                    if (ANY) return true;
+                    hit_t = t;
+                }
+            }
+            if (sp == 0) break;
+            node = stack[--sp];
+        }
+    }
+    for (int s = 0; s < S.n_spheres; s++) {
+        float t;
+        if (sphere_test(S.spheres[s], o, d, mint, hit_t, t)) {
+            h.t = t; h.u = 0.f; h.v = 0.f; h.prim = -s - 2;
+            found = true;
+            if (ANY) return true;
+            hit_t = t;
+        }
+    }
+    return found;
+}
+
+// DifferentialGeometry::coordinateSystem (core/DifferentialGeometry.h:36-50)
+__device__ __forceinline__ void frame_from(V3 n, V3 &s, V3 &t)
+{
+    V3 c;
+    if (fabsf(n.x) > fabsf(n.y)) {
+        float il = 1.0f / sqrtf(n.x * n.x + n.z * n.z);
+        c = v3(n.z * il, 0.0f, -n.x * il);
+    } else {
+        float il = 1.0f / sqrtf(n.y * n.y + n.z * n.z);
+        c = v3(0.0f, n.z * il, -n.y * il);
+    }
+    t = c;
+    s = cross(c, n);
+}
+
+// Differential geometry of a hit: Triangle::getDifferentialGeometry
+// (Triangle.cpp:130-190) or Sphere::getDifferentialGeometry (Sphere.cpp:115-139)
+__device__ __forceinline__ Frame hit_frame(const DevScene &S, const Hit &h, V3 o, V3 d)
+{
+    Frame f;
+    if (h.prim >= 0) {
+        const float *P = S.tri_v + 9 * (size_t)h.prim;
+        V3 p0 = vload(P), p1 = vload(P + 3), p2 = vload(P + 6);
+        float sum = h.u + h.v;
+        float bx = 1 - sum;
+        f.p = (bx * p0 + h.u * p1) + h.v * p2;
+        V3 ng = normalized(cross(p1 - p0, p2 - p0));
+        V3 ns = ng;
+        if (S.tri_n) {
+            const float *Nn = S.tri_n + 9 * (size_t)h.prim;
+            ns = normalized((bx * vload(Nn) + h.u * vload(Nn + 3)) + h.v * vload(Nn + 6));
+        }
+        f.n = ns;
+    } else {
+        const DevSphere &sp = S.spheres[-h.prim - 2];
+        f.p = o + h.t * d;
+        V3 nl = normalized(xf_point(sp.to_object, f.p) - v3(0, 0, 0));
+        f.n = normalized(xf_normal(sp.to_object, nl));
+    }
+    frame_from(f.n, f.s, f.t);
+    return f;
+}
+__device__ __forceinline__ V3 to_local(const Frame &f, V3 v) { return v3(dot(v, f.s), dot(v, f.t), dot(v, f.n)); }
+__device__ __forceinline__ V3 to_world(const Frame &f, V3 v) { return (f.s * v.x + f.t * v.y) + f.n * v.z; }
+
+// primitive attributes
+__device__ __forceinline__ int prim_bsdf(const DevScene &S, int prim)
+{
+    return prim >= 0 ? S.meshes[S.tri_mesh[prim]].bsdf : S.spheres[-prim - 2].bsdf;
+}
+__device__ __forceinline__ int prim_light(const DevScene &S, int prim)
+{
+    return prim >= 0 ? S.meshes[S.tri_mesh[prim]].light : S.spheres[-prim - 2].light;
+}
+__device__ __forceinline__ int prim_interior(const DevScene &S, int prim)
+{
+    return prim >= 0 ? S.meshes[S.tri_mesh[prim]].interior : S.spheres[-prim - 2].interior;
+}
+__device__ __forceinline__ int prim_exterior(const DevScene &S, int prim)
+{
+    return prim >= 0 ? S.meshes[S.tri_mesh[prim]].exterior : S.spheres[-prim - 2].exterior;
+}
+
+// ------------------------------------------------------------------ CDF (core/CDF.h:44-81)
+__device__ __forceinline__ int cdf_sample(const float *cdf, int n /* entries incl. leading 0 */, float u)
+{
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        int mid = lo + ((hi - lo) >> 1);
+        if (cdf[mid] < u) lo = mid + 1; else hi = mid;
+    }
+    return imin(imax(0, lo - 1), n - 2);
+}
+__device__ __forceinline__ int cdf_sample_reuse(const float *cdf, int n, float &u, float &pdf)
+{
+    int i = cdf_sample(cdf, n, u);
+    u = (u - cdf[i]) / (cdf[i + 1] - cdf[i]);
+    pdf = cdf[i + 1] - cdf[i];
+    return i;
+}
+
+// ------------------------------------------------------------------ warps (core/Mapping.h)
+__device__ __forceinline__ V2 concentric_disk(V2 s)
+{
+    const float r1 = 2 * s.x - 1.f;
+    const float r2 = 2 * s.y - 1.f;
+    float rx, ry;
+    if (r1 > -r2 && r1 > r2) { rx = r1; ry = (RT_PI * r2) / (4 * r1); }
+    else if (r1 < r2 && r1 > -r2) { rx = r2; ry = (RT_PI / 4.f) * (2 - r1 / r2); }
+    else if (r1 < -r2 && r1 < r2) { rx = -r1; ry = (RT_PI / 4.f) * (4 + r2 / r1); }
+    else { rx = -r2; ry = (RT_PI / 4.f) * (6 - r1 / r2); }
+    return v2(rx * cosf(ry), rx * sinf(ry));
+}
+__device__ __forceinline__ V3 cosine_hemisphere(V2 s)
+{
+    V2 t = concentric_disk(s);
+    float z = sqrtf(smax(0.f, 1.f - t.x * t.x - t.y * t.y));
+    return v3(t.x, t.y, z);
+}
+__device__ __forceinline__ V3 square_to_triangle(V2 s)
+{
+    float sq = sqrtf(s.x);
+    return v3(1 - sq, (1 - s.y) * sq, s.y * sq);
+}
+__device__ __forceinline__ V3 uniform_sphere(V2 s)
+{
+    float phi = 2.f * RT_PI * s.x;
+    float u = 2 * s.y - 1.f;
+    float st = sqrtf(1.f - u * u);
+    return normalized(v3(st * cosf(phi), st * sinf(phi), u));
+}
+__device__ __forceinline__ float cone_pdf(float c) { return 1.f / (2 * RT_PI * (1.f - c)); }
+__device__ __forceinline__ float spherical_phi(V3 v)
+{
+    float r = atan2f(v.x, -v.z);
+    return r < 0.f ? r + 2 * (float)3.14159265358979323846 : r;
+}
+__device__ __forceinline__ float spherical_theta(V3 v) { return acosf(v.y); }
+__device__ __forceinline__ V3 cartesian_from_spherical(float theta, float phi)
+{
+    float st = sinf(theta), ct = cosf(theta), cp = cosf(phi), sp = sinf(phi);
+    return v3(sp * st, ct, -cp * st);
+}
+
+// ------------------------------------------------------------------ Fresnel (core/Fresnel.h)
+__device__ __forceinline__ float fresnel_conductor1(float eta, float k, float cosI)
+{
+    float epa = eta * eta + k * k;
+    float c2 = cosI * cosI;
+    float epac2 = epa * c2;
+    float two = 2 * eta * cosI;
+    float rpar = (epac2 - two + 1) / (epac2 + two + 1);
+    float rperp = (epa - two + c2) / (epa + two + c2);
+    return (rpar * rpar + rperp * rperp) * 0.5f;
+}
+__device__ __forceinline__ float fresnel_dielectric(float eI, float eT, float cI, float cT)
+{
+    float tcI = eT * cI, icT = eI * cT, icI = eI * cI, tcT = eT * cT;
+    float rpar = (tcI - icT) / (tcI + icT);
+    float rperp = (icI - tcT) / (icI + tcT);
+    return (rpar * rpar + rperp * rperp) * 0.5f;
+}
+// Fresnel.h:83-114 (grey reflectance)
+__device__ __forceinline__ float estimate_dielectric(float etaExt, float etaInt, float cosI, float &eI, float &eT,
+                                                     float &rel, float &cT)
+{
+    eI = etaExt; eT = etaInt;
+    bool entering = true;
+    float fr;
+    if (cosI <= 0.f) { entering = false; float q = eI; eI = eT; eT = q; }
+    rel = eI / eT;
+    float sinT = rel * sqrtf(smax(0.f, 1 - cosI * cosI));
+    cT = sqrtf(smax(0.f, 1 - sinT * sinT));
+    if (sinT >= 1.f) { cT = 0.f; fr = 1.f; }
+    else {
+        fr = fresnel_dielectric(eI, eT, fabsf(cosI), cT);
+        if (entering) cT = -cT;
+    }
+    return fr;
+}
+
+// ------------------------------------------------------------------ microfacets (MicrofacetDistribution.cpp)
+__device__ __forceinline__ float sin2t(V3 v) { return 1.f - v.z * v.z; }
+__device__ __forceinline__ float sint(V3 v) { float s2 = sin2t(v); if (s2 < 0.f) return 0.f; return sqrtf(s2); }
+__device__ __forceinline__ float tan2t(V3 v) { float s2 = 1.f - v.z * v.z; if (s2 <= 0.f) return 0.f; return s2 / (v.z * v.z); }
+
+__device__ __forceinline__ V3 mf_sample_normal(int type, V2 s, float alpha)
+{
+    float theta;
+    if (type == 0) theta = atanf(sqrtf(-alpha * alpha * logf(1 - s.x)));
+    else if (type == 2) theta = atanf(alpha * sqrtf(s.x) / sqrtf(1.f - s.x));
+    else theta = acosf(powf(s.x, 1.f / (alpha + 2)));
+    float phi = 2 * RT_PI * s.y;
+    return v3(sinf(theta) * cosf(phi), sinf(theta) * sinf(phi), cosf(theta));
+}
+__device__ __forceinline__ float mf_D(int type, V3 wh, float alpha)
+{
+    if (wh.z <= 0.f) return 0.f;
+    if (type == 0) {
+        float c2 = wh.z * wh.z;
+        float t2 = sin2t(wh) / c2;
+        float a2 = alpha * alpha;
+        return expf(-t2 / a2) / (RT_PI * a2 * c2 * c2);
+    } else if (type == 2) {
+        float a2 = alpha * alpha;
+        float c2 = wh.z * wh.z;
+        float t2 = tan2t(wh);
+        float ss = a2 + t2;
+        return a2 / (RT_PI * c2 * c2 * ss * ss);
+    }
+    return ((alpha + 2.f) / (2 * RT_PI)) * powf(wh.z, alpha);
+}
+__device__ __forceinline__ float mf_G1(int type, V3 v, V3 m, float alpha)
+{
+    if (dot(v, m) / v.z <= 0) return 0.f;
+    if (type == 0) {
+        float tv = sint(v) / v.z;
+        if (tv == 0.f) return 1.f;
+        float b = fabsf(1.f / (alpha * tv));
+        if (b < 1.6f) return (3.535f * b + 2.181f * b * b) / (1 + 2.276f * b + 2.577f * b * b);
+        return 1.f;
+    } else if (type == 2) {
+        float a2 = alpha * alpha;
+        float t2 = tan2t(v);
+        return 2.f / (1 + sqrtf(1 + a2 * t2));
+    }
+    float tv = sint(v) / v.z;
+    float b = sqrtf(0.5f * alpha + 1) / tv;
+    if (b < 1.6f) return (3.535f * b + 2.181f * b * b) / (1 + 2.276f * b + 2.577f * b * b);
+    return 1.f;
+}
+__device__ __forceinline__ float mf_G(int type, V3 wi, V3 wo, V3 wh, float alpha)
+{
+    return mf_G1(type, wi, wh, alpha) * mf_G1(type, wo, wh, alpha);
+}
+__device__ __forceinline__ float adjusted_alpha(float a, float cosI) { return (1.2f - 0.2f * sqrtf(fabsf(cosI))) * a; }
+__device__ __forceinline__ float fsign(float v) { return v >= 0.f ? 1.f : -1.f; }
+__device__ __forceinline__ V3 reflect_n(V3 v, V3 n) { float d = 2 * dot(v, n); return d * n - v; }
+__device__ __forceinline__ V3 refract_local(V3 v, float cT, float rel) { return v3(rel * -v.x, rel * -v.y, cT); }
+__device__ __forceinline__ V3 refract_n(V3 v, V3 n, float rel, float cT)
+{
+    float s = dot(v, n) * rel + cT;
+    return n * s - v * rel;
+}
+__device__ __forceinline__ V3 half_dir_transmitted(V3 wi, V3 wo, float eI, float eT)
+{
+    V3 s = eI * wi + eT * wo;
+    return normalized(-1.f * s);
+}
+
+// ------------------------------------------------------------------ BSDFs
+enum { BT_UNKNOWN = 0, BT_DIFFUSE_REFLECTION = 1, BT_DELTA_REFLECTION = 2, BT_GLOSSY_REFLECTION = 4,
+       BT_DELTA_TRANSMISSION = 8, BT_GLOSSY_TRANSMISSION = 0x10, BT_DIFFUSE = 0x200,
+       BT_DELTA = 2 | 8, BT_ALL = (1 | 2 | 4) | (8 | 4) };
+
+struct BsdfRec {
+    V3 wi, wo;
+    int type;
+    float rel_eta;
+    float pdf;
+};
+
+// Diffuse (bsdf/Diffuse.cpp:28-106)
+__device__ __forceinline__ C3 diffuse_eval(const float *alb, V3 wi, V3 wo)
+{
+    if (wi.z <= 0.f || wo.z <= 0.f) return cfill(0.f);
+    return cload(alb) * RT_INV_PI;
+}
+__device__ __forceinline__ float diffuse_pdf(V3 wi, V3 wo)
+{
+    if (wi.z <= 0.f || wo.z <= 0.f) return 0.f;
+    return RT_INV_PI * wo.z;
+}
+__device__ __forceinline__ C3 diffuse_sample(const float *alb, BsdfRec &r, V2 s)
+{
+    if (r.wi.z <= 0.f) return cfill(0.f);
+    r.type = BT_DIFFUSE;
+    r.wo = cosine_hemisphere(s);
+    r.pdf = diffuse_pdf(r.wi, r.wo);
+    return cload(alb);
+}
+
+// RoughConductor (bsdf/RoughConductor.cpp:77-145)
+__device__ __forceinline__ C3 rc_eval(const DevBsdf &b, V3 wi, V3 wo)
+{
+    float ci = wi.z, co = wo.z;
+    if (ci <= 0.f || co <= 0.f) return cfill(0.f);
+    V3 wh = normalized(wi + wo);
+    float D = mf_D(b.distribution, wh, b.alpha_avg);
+    float G = mf_G(b.distribution, wi, wo, wh, b.alpha_avg);
+    C3 F = c3(fresnel_conductor1(b.eta[0], b.k[0], ci), fresnel_conductor1(b.eta[1], b.k[1], ci),
+              fresnel_conductor1(b.eta[2], b.k[2], ci));
+    float den = 4 * ci * co;
+    C3 r = cload(b.reflectance) * D;
+    r = r * F;
+    r = r * G;
+    return r / den;
+}
+__device__ __forceinline__ float rc_pdf(const DevBsdf &b, V3 wi, V3 wo)
+{
+    float ci = wi.z, co = wo.z;
+    if (ci <= 0.f || co <= 0.f) return 0.f;
+    V3 wh = normalized(wi + wo);
+    float ch = wh.z;
+    float Jh = 1.f / (4 * fabsf(dot(wh, wo)));
+    float D = mf_D(b.distribution, wh, b.alpha_avg);
+    return D * ch * Jh;
+}
+__device__ __forceinline__ C3 rc_sample(const DevBsdf &b, BsdfRec &r, V2 s)
+{
+    if (r.wi.z <= 0.f) return cfill(0.f);
+    r.type = BT_GLOSSY_REFLECTION;
+    float alpha = adjusted_alpha(b.alpha_avg, r.wi.z);
+    V3 n = mf_sample_normal(b.distribution, s, alpha);
+    r.wo = reflect_n(r.wi, n);
+    float co = r.wo.z;
+    if (co <= 0.f) return cfill(0.f);
+    r.pdf = rc_pdf(b, r.wi, r.wo);
+    if (r.pdf <= 0) return cfill(0.f);
+    C3 e = rc_eval(b, r.wi, r.wo);
+    return (e * fabsf(co)) / r.pdf;
+}
+
+// RoughDielectric (bsdf/RoughDielectric.cpp:83-329)
+__device__ __forceinline__ C3 rd_eval_reflection(const DevBsdf &b, V3 wi, V3 wo)
+{
+    float ci = wi.z, co = wo.z;
+    V3 wh = normalized(wi + wo);
+    wh = fsign(ci) * wh;
+    float alpha = b.alpha_avg;
+    float D = mf_D(b.distribution, wh, alpha);
+    float eI, eT, rel, cT;
+    float fr = estimate_dielectric(b.eta_ext, b.eta_int, dot(wi, wh), eI, eT, rel, cT);
+    float G = mf_G(b.distribution, wi, wo, wh, alpha);
+    float den = 4 * ci * co;
+    C3 r = cload(b.reflectance) * D;
+    r = r * fr;
+    r = r * G;
+    return r / den;
+}
+__device__ __forceinline__ C3 rd_eval_refraction(const DevBsdf &b, V3 wi, V3 wo)
+{
+    float ci = wi.z, co = wo.z;
+    float eI, eT, rel, cT;
+    float fr = estimate_dielectric(b.eta_ext, b.eta_int, ci, eI, eT, rel, cT);
+    V3 wt = half_dir_transmitted(wi, wo, eI, eT);
+    float alpha = b.alpha_avg;
+    float left = dot(wi, wt) * dot(wo, wt) / (ci * co);
+    float G = mf_G(b.distribution, wi, wo, wt, alpha);
+    float D = mf_D(b.distribution, wt, alpha);
+    float omf = (-1.f * fr) + 1.f;
+    C3 term = cload(b.transmittance) * left;
+    term = term * eT;
+    term = term * eT;
+    term = term * omf;
+    term = term * G;
+    term = term * D;
+    term = term * rel;
+    term = term * rel;
+    float denom = eI * dot(wi, wt) + eT * dot(wo, wt);
+    return term / (denom * denom);
+}
+__device__ __forceinline__ float rd_pdf_reflection(const DevBsdf &b, V3 wi, V3 wo)
+{
+    float ci = wi.z;
+    float alpha = (1.2f - 0.2f * sqrtf(fabsf(ci))) * b.alpha_avg;
+    V3 wh = normalized(wi + wo);
+    wh = fsign(ci) * wh;
+    float ch = wh.z;
+    float Jh = 1.f / (4 * dot(wh, wo));
+    return fabsf(mf_D(b.distribution, wh, alpha) * ch * Jh);
+}
+__device__ __forceinline__ float rd_pdf_refraction(const DevBsdf &b, V3 wi, V3 wo)
+{
+    float ci = wi.z;
+    float eI, eT, rel, cT;
+    estimate_dielectric(b.eta_ext, b.eta_int, ci, eI, eT, rel, cT);
+    V3 wt = half_dir_transmitted(wi, wo, eI, eT);
+    float cwt = wt.z;
+    float alpha = (1.2f - 0.2f * sqrtf(fabsf(ci))) * b.alpha_avg;
+    float hd = eI * dot(wi, wt) + eT * dot(wo, wt);
+    float Jh = (eT * eT * dot(wo, wt)) / (hd * hd);
+    return fabsf(mf_D(b.distribution, wt, alpha) * cwt * Jh);
+}
+__device__ __forceinline__ C3 rd_eval(const DevBsdf &b, V3 wi, V3 wo)
+{
+    if (wi.z * wo.z > 0) return rd_eval_reflection(b, wi, wo);
+    return rd_eval_refraction(b, wi, wo);
+}
+__device__ __forceinline__ float rd_pdf(const DevBsdf &b, V3 wi, V3 wo)
+{
+    float ci = wi.z, co = wo.z;
+    float eI, eT, rel, cT;
+    if (ci * co > 0) {
+        V3 wh = normalized(wi + wo);
+        wh = fsign(ci) * wh;
+        float fr = cavg1(estimate_dielectric(b.eta_ext, b.eta_int, dot(wi, wh), eI, eT, rel, cT));
+        return rd_pdf_reflection(b, wi, wo) * fr;
+    }
+    float etaI = b.eta_ext, etaT = b.eta_int;
+    if (ci < 0) { float q = etaI; etaI = etaT; etaT = q; }
+    V3 wt = half_dir_transmitted(wi, wo, etaI, etaT);
+    float fr = cavg1(estimate_dielectric(b.eta_ext, b.eta_int, dot(wi, wt), eI, eT, rel, cT));
+    return rd_pdf_refraction(b, wi, wo) * (1.f - fr);
+}
+__device__ __forceinline__ C3 rd_sample(const DevBsdf &b, BsdfRec &r, V2 s)
+{
+    float ci = r.wi.z;
+    float alpha = adjusted_alpha(b.alpha_avg, ci);
+    V3 n = mf_sample_normal(b.distribution, s, alpha);
+    float eI, eT, rel, cT;
+    float fr = cavg1(estimate_dielectric(b.eta_ext, b.eta_int, dot(r.wi, n), eI, eT, rel, cT));
+    if (s.x <= fr) {
+        r.type = BT_GLOSSY_REFLECTION;
+        r.wo = reflect_n(r.wi, n);
+        if (r.wi.z * r.wo.z <= 0) return cfill(0.f);
+        r.pdf = rd_pdf_reflection(b, r.wi, r.wo) * fr;
+        if (r.pdf <= 0) return cfill(0.f);
+        V3 wh = normalized(r.wi + r.wo);
+        wh = fsign(ci) * wh;
+        float G = mf_G(b.distribution, r.wi, r.wo, wh, alpha);
+        float v = 1.f * dot(r.wi, n);
+        v = v * G;
+        return cfill(v / (ci * n.z));
+    }
+    r.type = BT_GLOSSY_TRANSMISSION;
+    r.wo = normalized(refract_n(r.wi, n, rel, cT));
+    r.rel_eta = rel;
+    float co = dot(r.wo, n);
+    if (r.wi.z * r.wo.z >= 0) return cfill(0.f);
+    r.pdf = rd_pdf_refraction(b, r.wi, r.wo) * (1.f - fr);
+    if (r.pdf <= 0) return cfill(0.f);
+    C3 e = rd_eval_refraction(b, r.wi, r.wo);
+    return (e * fabsf(co)) / r.pdf;
+}
+
+// SmoothLayeredBSDF over a Diffuse base (bsdf/SmoothLayeredBSDF.cpp:139-403)
+__device__ __forceinline__ C3 absorb(const DevBsdf &b, float wip, float wop)
+{
+    float s = 1.f / fabsf(wip) + 1.f / fabsf(wop);
+    return c3(expf((-b.absorbance[0] * b.thickness) * s), expf((-b.absorbance[1] * b.thickness) * s),
+              expf((-b.absorbance[2] * b.thickness) * s));
+}
+__device__ __forceinline__ C3 sl_eval(const DevBsdf &b, V3 wi, V3 wo)
+{
+    if (wi.z <= 0.f || wo.z <= 0.f) return cfill(0.f);
+    float ci = wi.z;
+    float eI, eT, rel, cT;
+    float fr1 = cavg1(estimate_dielectric(b.eta_ext, b.eta_int, ci, eI, eT, rel, cT));
+    float T12 = 1.f - fr1;
+    if (fr1 == 1.f) return cfill(0.f);
+    V3 rwi = normalized(refract_local(wi, cT, rel));
+    V3 rwo = normalized(refract_local(wo, cT, rel));
+    rwi = -rwi;
+    rwo = -rwo;
+    ci = (-rwo).z;
+    float fr2 = cavg1(estimate_dielectric(b.eta_ext, b.eta_int, ci, eI, eT, rel, cT));
+    if (fr2 == 1.f) return cfill(0.f);
+    float T21 = 1.f - fr2;
+    C3 f2 = diffuse_eval(b.albedo, rwi, rwo);
+    C3 a = absorb(b, rwi.z, rwo.z);
+    float G = 1.f;
+    float t = (1.f - G) + T21 * G;
+    float m = b.eta_ext / b.eta_int;
+    C3 r = T12 * f2;
+    r = r * a;
+    r = r * t;
+    r = r * m;
+    r = r * m;
+    r = r * wo.z;
+    r = r / rwo.z;
+    return cfill(0.f) + r;
+}
+__device__ __forceinline__ float sl_pdf(const DevBsdf &b, V3 wi, V3 wo)
+{
+    float ci = wi.z;
+    float eI, eT, rel, cT;
+    float fr1 = cavg1(estimate_dielectric(b.eta_ext, b.eta_int, ci, eI, eT, rel, cT));
+    if (fr1 == 1.f) return 0.f;
+    V3 rwi = normalized(refract_local(wi, cT, rel));
+    V3 rwo = normalized(refract_local(wo, cT, rel));
+    rwi = -rwi;
+    rwo = -rwo;
+    float pb = diffuse_pdf(rwi, rwo);
+    float m = b.eta_ext / b.eta_int;
+    return 0.f + pb * (1.f - fr1) * m * m * wo.z / rwo.z;
+}
+__device__ __forceinline__ C3 sl_sample(const DevBsdf &b, BsdfRec &r, V2 s)
+{
+    if (r.wi.z <= 0.f) return cfill(0.f);
+    float ci = r.wi.z;
+    r.type = BT_GLOSSY_REFLECTION;
+    float eI, eT, rel, cT;
+    float fr1 = cavg1(estimate_dielectric(b.eta_ext, b.eta_int, ci, eI, eT, rel, cT));
+    if (fr1 == 1.f) return cfill(0.f);
+    if (s.x <= fr1) {
+        r.wo = v3(-r.wi.x, -r.wi.y, r.wi.z);
+        r.pdf = fr1;
+        r.type = BT_DELTA_REFLECTION;
+        return cfill(1.f);
+    }
+    V3 rwi = normalized(-refract_local(r.wi, cT, rel));
+    r.type = BT_UNKNOWN;
+    float T12 = 1.f - fr1;
+    BsdfRec base;
+    base.wi = rwi; base.wo = v3(0, 0, 0); base.type = BT_ALL; base.rel_eta = 1.f; base.pdf = -1.f;
+    C3 f2 = diffuse_sample(b.albedo, base, s);
+    if (iszero(f2)) return cfill(0.f);
+    r.pdf = (1.f - fr1);
+    if (r.pdf <= 0.f) return cfill(0.f);
+    r.wo = -base.wo;
+    float wip = rwi.z;
+    float wop = (-base.wo).z;
+    C3 a = absorb(b, wip, wop);
+    ci = r.wo.z;
+    float fr2 = cavg1(estimate_dielectric(b.eta_ext, b.eta_int, ci, eI, eT, rel, cT));
+    if (fr2 == 1.f) return cfill(0.f);
+    float T21 = 1.f - fr2;
+    r.wo = normalized(refract_local(r.wo, cT, rel));
+    float co = r.wo.z;
+    C3 res = T12 * f2;
+    res = res * a;
+    res = res * T21;
+    res = cfill(0.f) + res;
+    res = res * fabsf(co);
+    res = res / r.pdf;
+    float m = b.eta_ext / b.eta_int;
+    r.pdf *= base.pdf * m * m * r.wo.z / wop;
+    return res;
+}
+
+__device__ __forceinline__ C3 bsdf_eval(const DevBsdf &b, V3 wi, V3 wo)
+{
+    switch (b.type) {
+    case 0: return diffuse_eval(b.albedo, wi, wo);
+    case 1: return rc_eval(b, wi, wo);
+    case 2: return rd_eval(b, wi, wo);
+    default: return sl_eval(b, wi, wo);
+    }
+}
+__device__ __forceinline__ float bsdf_pdf(const DevBsdf &b, V3 wi, V3 wo)
+{
+    switch (b.type) {
+    case 0: return diffuse_pdf(wi, wo);
+    case 1: return rc_pdf(b, wi, wo);
+    case 2: return rd_pdf(b, wi, wo);
+    default: return sl_pdf(b, wi, wo);
+    }
+}
+__device__ __forceinline__ C3 bsdf_sample(const DevBsdf &b, BsdfRec &r, V2 s)
+{
+    switch (b.type) {
+    case 0: return diffuse_sample(b.albedo, r, s);
+    case 1: return rc_sample(b, r, s);
+    case 2: return rd_sample(b, r, s);
+    default: return sl_sample(b, r, s);
+    }
+}
+
+// ------------------------------------------------------------------ lights
+struct LightRec {
+    V3 point, to_light, normal;
+    C3 intensity;
+    float distance, pdf;
+};
+
+__device__ __forceinline__ void tri_verts(const DevScene &S, int tri, V3 &p0, V3 &p1, V3 &p2)
+{
+    const float *P = S.tri_v + 9 * (size_t)tri;
+    p0 = vload(P); p1 = vload(P + 3); p2 = vload(P + 6);
+}
+
+// Mesh::sample (geometricShape/Mesh.cpp:38-68) + Triangle::sample (Triangle.cpp:251-273)
+__device__ __forceinline__ void mesh_sample(const DevScene &S, int mesh, V2 s, V3 &pt, V3 &n)
+{
+    const DevMesh &M = S.meshes[mesh];
+    float ux = s.x, pdf;
+    int index = cdf_sample_reuse(S.mesh_cdf + M.cdf_off, M.n_tris + 1, ux, pdf);
+    V2 s2 = v2(ux, s.y);
+    int tri = M.first_tri + index;
+    V3 p0, p1, p2;
+    tri_verts(S, tri, p0, p1, p2);
+    V3 b = square_to_triangle(s2);
+    pt = (p0 * b.x + p1 * b.y) + p2 * b.z;
+    if (S.tri_n) {
+        const float *N = S.tri_n + 9 * (size_t)tri;
+        n = normalized((b.x * vload(N) + b.y * vload(N + 3)) + b.z * vload(N + 6));
+    } else {
+        n = normalized(cross(p1 - p0, p2 - p0));
+        n = normalized(n);
+    }
+}
+// Mesh::pdf (Mesh.cpp:70-93)
+__device__ __forceinline__ float mesh_pdf(const DevScene &S, int mesh, V3 p, V3 sampled, V3 n)
+{
+    V3 l = p - sampled;
+    float dist = norm(l);
+    l = normalized(l);
+    float c = dot(n, l);
+    if (c > 0) return dist * dist / (S.meshes[mesh].area * c);
+    return 0.f;
+}
+__device__ __forceinline__ V3 sphere_normal(const DevSphere &s, V3 p)
+{
+    return normalized(xf_point(s.to_object, p) - v3(0, 0, 0));
+}
+// Sphere::sample (Sphere.cpp:146-173)
+__device__ __forceinline__ void sphere_sample(const DevSphere &s, V2 u, V3 &pt, V3 &n)
+{
+    float theta = 2.f * RT_PI * u.x;
+    float phi = acosf(2 * u.y - 1.f);
+    float c = cosf(phi);
+    float sq = sqrtf(1 - c * c);
+    V3 p = v3(sq * cosf(theta), sq * sinf(theta), c);
+    p = p * s.radius;
+    n = normalized(xf_normal(s.to_object, sphere_normal(s, p)));
+    pt = xf_point(s.to_world, p);
+}
+// Sphere::pdf (Sphere.cpp:183-201) with ISampledShape::pdf (ISampledShape.cpp:17-40)
+__device__ __forceinline__ float sphere_pdf(const DevSphere &s, V3 p, V3 sampled, V3 n)
+{
+    V3 center = xf_point(s.to_world, v3(0.f, 0.f, 0.f));
+    V3 itc = p - center;
+    float sqd = sqnorm(itc);
+    if (dot(n, itc) < 0.f) return 0.f;
+    if (sqd - s.radius * s.radius < RT_EPSILON) {
+        V3 l = p - sampled;
+        float dist = norm(l);
+        l = normalized(l);
+        float c = dot(n, l);
+        float area = 4.f * RT_PI * s.radius * s.radius * s.radius;
+        if (c >= 0) return dist * dist / (area * c);
+        return 0.f;
+    }
+    float st2 = s.radius * s.radius / sqd;
+    float ct = sqrtf(smax(0.f, 1 - st2));
+    return cone_pdf(ct);
+}
+
+// EnvironmentLight (light/EnvironmentLight.cpp)
+__device__ __forceinline__ void env_checkxy(const DevLight &L, float &x, float &y)
+{
+    unsigned W = (unsigned)L.env_w, H = (unsigned)L.env_h;
+    if (x >= (float)W) x = (float)((unsigned)(int)x % W) + (x - (float)(int)x);
+    else if (x < 0) x = (float)(W - (unsigned)abs((int)x) % W) + (x - (float)(int)x);
+    if (y >= (float)H) y = (float)((unsigned)(int)y % H) + (y - (float)(int)y);
+    else if (y < 0) y = (float)(H - (unsigned)abs((int)y) % H) + (y - (float)(int)y);
+}
+__device__ __forceinline__ int iclamp(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+// core/BasicMath.h:74-90 interp2
+__device__ __forceinline__ C3 env_interp(const DevLight &L, float x, float y)
+{
+    int W = L.env_w, H = L.env_h;
+    float ax = x - (float)(int)x, ay = y - (float)(int)y;
+    int x0 = iclamp((int)x, 0, W - 2), y0 = iclamp((int)y, 0, H - 2);
+    int x1 = x0 + 1 < W ? x0 + 1 : x0; x1 = iclamp(x1, 0, W - 1);
+    int y1 = y0 + 1 < H ? y0 + 1 : y0; y1 = iclamp(y1, 0, H - 1);
+    const float *a00 = L.env_rgb + 3 * ((size_t)y0 * W + x0);
+    const float *a01 = L.env_rgb + 3 * ((size_t)y1 * W + x0);
+    const float *a10 = L.env_rgb + 3 * ((size_t)y0 * W + x1);
+    const float *a11 = L.env_rgb + 3 * ((size_t)y1 * W + x1);
+    float w00 = (1 - ax) * (1 - ay), w01 = (1 - ax) * ay, w10 = ax * (1 - ay), w11 = ax * ay;
+    C3 r;
+    r.r = ((w00 * a00[0] + w01 * a01[0]) + w10 * a10[0]) + w11 * a11[0];
+    r.g = ((w00 * a00[1] + w01 * a01[1]) + w10 * a10[1]) + w11 * a11[1];
+    r.b = ((w00 * a00[2] + w01 * a01[2]) + w10 * a10[2]) + w11 * a11[2];
+    return r;
+}
+__device__ __forceinline__ void env_dir_xy(const DevLight &L, V3 dir, float &fx, float &fy)
+{
+    fx = (spherical_phi(dir) / (2 * RT_PI)) * (float)L.env_w;
+    fy = (spherical_theta(dir) / RT_PI) * (float)L.env_h;
+    fx += 0.f * (float)L.env_w;
+    fy += 0.f * (float)L.env_h;
+    env_checkxy(L, fx, fy);
+}
+__device__ __forceinline__ C3 env_le(const DevLight &L, V3 direction)
+{
+    V3 dir = normalized(xf_vector(L.env_to_light, direction));
+    float fx, fy;
+    env_dir_xy(L, dir, fx, fy);
+    return env_interp(L, fx, fy) * L.env_scale;
+}
+__device__ __forceinline__ void env_sample(const DevLight &L, V3 p, V2 s, LightRec &o)
+{
+    int W = L.env_w, H = L.env_h;
+    int row = cdf_sample(L.env_marginal, H + 1, s.x);
+    int col = cdf_sample(L.env_row_cdf + (size_t)row * (W + 1), W + 1, s.y);
+    float rcol = (float)col + 0.f * (float)W;
+    float rrow = (float)row + 0.f * (float)H;
+    env_checkxy(L, rcol, rrow);
+    row = (int)rrow;
+    col = (int)rcol;
+    float theta = RT_PI * (float)row / (float)H;
+    float phi = 2 * RT_PI * (float)col / (float)W;
+    float st = sinf(theta);
+    V3 dir = cartesian_from_spherical(theta, phi);
+    dir = xf_vector(L.env_to_world, dir);
+    o.distance = L.env_radius;
+    dir = normalized(dir);
+    o.to_light = dir;
+    o.point = p + L.env_radius * dir;
+    o.normal = v3(0, 0, 0);
+    int cx = iclamp(col, 0, W - 1), cy = iclamp(row, 0, H - 1);
+    o.intensity = cload(L.env_rgb + 3 * ((size_t)cy * W + cx)) * L.env_scale;
+    float pdf = lum(o.intensity) * L.env_weight[row];
+    float den = L.env_marginal_sum * (2 * RT_PI / (float)W);
+    den = den * (RT_PI / (float)H);
+    pdf = pdf / den;
+    pdf /= smax(fabsf(st), RT_EPSILON);
+    o.pdf = pdf;
+}
+__device__ __forceinline__ float env_pdf(const DevLight &L, V3 to_light)
+{
+    V3 dir = normalized(xf_vector(L.env_to_light, to_light));
+    float fx, fy;
+    env_dir_xy(L, dir, fx, fy);
+    float st = sinf(fy);
+    float den = L.env_marginal_sum * (2 * RT_PI / (float)L.env_w);
+    den = den * (RT_PI / (float)L.env_h);
+    float nf = L.env_weight[(int)fy] / den;
+    float lm = lum(env_interp(L, fx, fy) * L.env_scale);
+    float pdf = lm * nf;
+    pdf /= smax(fabsf(st), RT_EPSILON);
+    return pdf;
+}
+
+__device__ __forceinline__ float light_pdf(const DevScene &S, int light, V3 p, V3 point, V3 normal, V3 to_light)
+{
+    const DevLight &L = S.lights[light];
+    if (L.type == 1) return env_pdf(L, to_light);
+    if (L.shape_kind == 0) return mesh_pdf(S, L.shape, p, point, normal);
+    return sphere_pdf(S.spheres[L.shape], p, point, normal);
+}
+
+// Light::sample dispatch: MeshLight.cpp:32-64, AreaLight.cpp:31-55, EnvironmentLight.cpp:85-146
+__device__ __forceinline__ void light_sample(const DevScene &S, int light, V3 p, V2 s, LightRec &o)
+{
+    const DevLight &L = S.lights[light];
+    o.pdf = 0.f;
+    o.distance = 0.f;
+    o.intensity = cfill(0.f);
+    if (L.type == 1) { env_sample(L, p, s, o); return; }
+    V3 pt, n;
+    if (L.shape_kind == 0) mesh_sample(S, L.shape, s, pt, n);
+    else sphere_sample(S.spheres[L.shape], s, pt, n);
+    o.point = pt;
+    o.normal = n;
+    o.to_light = pt - p;
+    o.distance = norm(o.to_light);
+    o.to_light = o.to_light / o.distance;
+    float c = dot(n, -o.to_light);
+    if (L.mesh_light && L.shape_kind == 0) {
+        if (c <= 0) { o.intensity = cfill(0.f); o.pdf = 0.f; }
+        else { o.intensity = cload(L.radiance); o.pdf = o.distance * o.distance / (S.meshes[L.shape].area * c); }
+    } else {
+        if (c < 0) { o.intensity = cfill(0.f); o.pdf = 0.f; }
+        else { o.intensity = cload(L.radiance); o.pdf = light_pdf(S, light, p, o.point, o.normal, o.to_light); }
+    }
+}
+// AreaLight::le (light/AreaLight.h:27-32)
+__device__ __forceinline__ C3 area_le(const DevScene &S, int light, V3 dir, V3 n)
+{
+    if (dot(dir, n) > 0.f) return cload(S.lights[light].radiance);
+    return cfill(0.f);
+}
+__device__ __forceinline__ float power_heuristic(float a, float b)
+{
+    float l = a * a, r = b * b;
+    return l / (l + r);
+}
+
+// ------------------------------------------------------------------ camera (NoriPerspective.cpp:80-118)
+__device__ __forceinline__ Ray camera_ray(const DevCamera &c, float px, float py, V2 lens)
+{
+    V3 nearP = xf_point(c.sample_to_camera, v3(px * c.inv_w, py * c.inv_h, 0.0f));
+    V3 d = normalized(nearP);
+    float invZ = 1.0f / d.z;
+    V3 o = v3(0.f, 0.f, 0.f);
+    if (c.aperture_radius > 0.f) {
+        V2 s = concentric_disk(lens);
+        s.x *= c.aperture_radius; s.y *= c.aperture_radius;
+        o = v3(s.x, s.y, 0.f);
+        float tdist = c.focal_plane * invZ;
+        V3 fp = tdist * d;
+        d = normalized(fp - o);
+    }
+    return make_ray(xf_point(c.camera_to_world, o), xf_vector(c.camera_to_world, d), c.near_clip * invZ,
+                    c.far_clip * invZ);
+}
+
+// ------------------------------------------------------------------ phase functions
+__device__ __forceinline__ float phase_eval(const DevMedium &m, V3 wi, V3 wo)
+{
+    if (m.phase == 0) return RT_INV_FOUR_PI;
+    float g = m.g;
+    float c = dot(-wi, wo);
+    return RT_INV_FOUR_PI * (1 - g * g) / powf(1 + g * g - 2 * g * c, 1.5f);
+}
+// HGPhaseFunction::sample (HGPhaseFunction.cpp:27-42), world-frame direction
+__device__ __forceinline__ float phase_sample(const DevMedium &m, V3 wi, V2 u, V3 &wo, float &pdf)
+{
+    if (m.phase == 0) {
+        wo = uniform_sphere(u);
+        pdf = RT_INV_FOUR_PI;
+        return 1.f;
+    }
+    float g = m.g;
+    float ct;
+    if (g < RT_EPSILON) ct = 1.f - 2.f * u.x;
+    else ct = (1 + g * g - ((1 - g * g) * (1 - g * g) / (1 - g + 2 * g * u.x))) / (2 * g);
+    float theta = acosf(ct);
+    float phi = 2 * RT_PI * u.y;
+    wo = cartesian_from_spherical(theta, phi);
+    pdf = phase_eval(m, wi, wo);
+    return 1.f;
+}
+
+// ------------------------------------------------------------------ media
+__device__ __forceinline__ C3 homog_tr(const DevMedium &m, float mint, float maxt)
+{
+    float t = maxt - mint;
+    return c3(expf(-m.sigma_t[0] * t), expf(-m.sigma_t[1] * t), expf(-m.sigma_t[2] * t));
+}
+// GridVolume::lookupSigmaT (volume/GridVolume.cpp:118-149) * scale
+__device__ __forceinline__ float grid_lookup(const DevMedium &m, V3 pa)
+{
+    float px = pa.x * (float)m.res[0], py = pa.y * (float)m.res[1], pz = pa.z * (float)m.res[2];
+    float fx = floorf(px), fy = floorf(py), fz = floorf(pz);
+    int ix = (int)fx, iy = (int)fy, iz = (int)fz;
+    if (ix < 0 || iy < 0 || iz < 0) return 0.0f * m.scale;
+    if (ix >= m.res[0] - 1 || iy >= m.res[1] - 1 || iz >= m.res[2] - 1) return 0.0f * m.scale;
+    size_t row = (size_t)m.res[0], slab = row * (size_t)m.res[1];
+    size_t off = (size_t)iz * slab + (size_t)iy * row + (size_t)ix;
+    const float *D = m.density;
+    float d000 = __ldg(D + off), d001 = __ldg(D + off + 1), d010 = __ldg(D + off + row),
+          d011 = __ldg(D + off + row + 1);
+    float d100 = __ldg(D + off + slab), d101 = __ldg(D + off + slab + 1), d110 = __ldg(D + off + slab + row),
+          d111 = __ldg(D + off + slab + row + 1);
+    float w1x = px - fx, w1y = py - fy, w1z = pz - fz;
+    float w0x = 1 - w1x, w0y = 1 - w1y, w0z = 1 - w1z;
+    float v = ((d000 * w0x + d001 * w1x) * w0y + (d010 * w0x + d011 * w1x) * w1y) * w0z +
+              ((d100 * w0x + d101 * w1x) * w0y + (d110 * w0x + d111 * w1x) * w1y) * w1z;
+    return v * m.scale;
+}
+
+#define RT_TRACK_CAP (1 << 20)
+
+// Heterogeneous::transmittance (medium/Heterogeneous.cpp:419-489): ratio tracking + RR
+__device__ __forceinline__ C3 hetero_tr(const DevMedium &m, Ray wr, Pcg32 &rng, int &limit)
+{
+    V3 o = xf_point(m.world_to_array, wr.o), d = xf_vector(m.world_to_array, wr.d);
+    float tmax = wr.maxt - wr.mint;
+    float tr = 1.f, st;
+    int breaker = 0;
+    float nearT, farT;
+    const float bmin[3] = {0.f, 0.f, 0.f}, bmax[3] = {1.f, 1.f, 1.f};
+    if (!ref_box_hit(bmin, bmax, o, d, wr.mint, wr.maxt, nearT, farT)) return cfill(1.f);
+    tmax = smin(tmax, farT);
+    st = smax(nearT, wr.mint);
+    for (;;) {
+        st += -logf(1.f - next1d(rng)) / m.max_sigma_t;
+        float proba = grid_lookup(m, o + st * d);
+        if (st >= tmax) return cfill(tr);
+        tr *= 1 - smax(0.f, proba / m.max_sigma_t);
+        const float threshold = .1f;
+        if (tr < threshold) {
+            float q = smax(.05f, 1 - tr);
+            if (next1d(rng) < q) return cfill(0.f);
+            tr /= 1 - q;
+        }
+        if (breaker > 1024) return cfill(0.f);
+        breaker++;
+    }
+}
+
+// Heterogeneous::sampleDistance (Heterogeneous.cpp:491-546): delta tracking
+__device__ __forceinline__ bool hetero_sample(const DevMedium &m, Ray wr, Pcg32 &rng, float &t, C3 &w, C3 &em,
+                                              int &limit)
+{
+    t = wr.mint;
+    float cur = 0.f;
+    float nearT, farT;
+    if (!ref_box_hit(m.wbox_min, m.wbox_max, wr.o, wr.d, wr.mint, wr.maxt, nearT, farT)) {
+        w = cfill(1.f); em = cfill(0.f); t = wr.maxt;
+        return false;
+    }
+    float tmax = smin(wr.maxt, farT);
+    int steps = 0;
+    for (;;) {
+        t += -logf(1.f - next1d(rng)) / m.max_sigma_t;
+        if (t > tmax) { w = cfill(1.f); em = cfill(0.f); t = tmax; return false; }
+        V3 pw = wr.o + t * wr.d;
+        cur = grid_lookup(m, xf_point(m.world_to_array, pw));
+        float proba = cur / m.max_sigma_t;
+        if (next1d(rng) < proba) break;
+        if (++steps >= RT_TRACK_CAP) { limit = 1; w = cfill(0.f); em = cfill(0.f); return true; }
+    }
+    if (cur != 0.f) w = cload(m.albedo); else w = cfill(0.f);
+    em = cfill(0.f);
+    return true;
+}
+
+__device__ __forceinline__ bool medium_sample(const DevMedium &m, Ray r, Pcg32 &rng, float &t, C3 &w, C3 &em,
+                                              int &limit)
+{
+    if (m.type == 1) return hetero_sample(m, r, rng, t, w, em, limit);
+    // Homogeneous::sampleDistance (Homogeneous.cpp:37-78)
+    int ch = (int)(next1d(rng) * 3);
+    float ext = ch == 0 ? m.sigma_t[0] : (ch == 1 ? m.sigma_t[1] : m.sigma_t[2]);
+    ext += RT_EPSILON;
+    t = -logf(1.f - next1d(rng)) / ext;
+    if (t > r.maxt) {
+        t = r.maxt;
+        C3 e = c3(expf(-m.sigma_t[0] * t), expf(-m.sigma_t[1] * t), expf(-m.sigma_t[2] * t));
+        float pdf = cavg(e);
+        w = homog_tr(m, r.mint, r.maxt) / pdf;
+        em = cfill(0.f);
+        return false;
+    }
+    C3 e = c3(m.sigma_t[0] * expf(-m.sigma_t[0] * t), m.sigma_t[1] * expf(-m.sigma_t[1] * t),
+              m.sigma_t[2] * expf(-m.sigma_t[2] * t));
+    float pdf = cavg(e);
+    t += r.mint;
+    w = (cload(m.sigma_s) * homog_tr(m, r.mint, t)) / pdf;
+    em = cfill(0.f) / cload(m.sigma_t);
+    return true;
+}
+__device__ __forceinline__ C3 medium_tr(const DevMedium &m, Ray r, Pcg32 &rng, int &limit)
+{
+    if (m.type == 1) return hetero_tr(m, r, rng, limit);
+    return homog_tr(m, r.mint, r.maxt);
+}

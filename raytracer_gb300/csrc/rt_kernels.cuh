@@ -1,0 +1,54 @@
+// rt_kernels.cuh -- wavefront state, kernels and launch helpers shared by
+// rt_api.cu.  One batch renders complete reference tiles (block_x x block_y
+// pixels, all samples of each pixel), so the film can be reduced per pixel in
+// the reference's own summation order without atomics.
+#pragma once
+#include "rt_device.cuh"
+
+namespace rtgpu {
+
+// path flags
+enum { F_FIRST = 1, F_DELTA = 2, F_NEE = 4, F_END = 8, F_DONE = 16 };
+
+struct RoundCounters {   // one per wavefront round, zeroed per batch
+    int active, closest, shadow, wc_closest, wc_shadow, pad0, pad1, pad2;
+};
+
+struct Wave {
+    // per path slot
+    Pcg32 *rng;
+    float4 *tp;        // throughput rgb, eta
+    float4 *rad;       // radiance rgb, depth (int bits)
+    float4 *ray_o;     // origin, mint
+    float4 *ray_d;     // direction, maxt
+    float4 *hit;       // t, u, v, prim (int bits)
+    float4 *bs;        // pending BSDF sample value rgb, pdf
+    float *rel_eta;
+    int *flags;
+    float4 *nee;       // pending light-sample contribution rgb
+    float4 *sh_o, *sh_d;
+    int *occl;
+    float4 *out;       // final radiance rgb, nan flag
+    uint8_t *splat;    // film footprint code of the sample
+    uint8_t *pix_irregular;  // per batch pixel: some sample splats off its pixel
+    // queues (ping-pong by round parity)
+    int *q_active[2];
+    int *q_closest, *q_shadow;
+    RoundCounters *cnt;
+    int capacity;
+    int max_rounds;
+};
+
+// batch geometry: tiles [tile0, tile0 + ntiles) of the reference job grid
+struct Batch {
+    int tile0, ntiles;      // tiles in raster order of the job grid
+    int tiles_x;            // job grid width in tiles
+    int bx, by;             // block size
+    int npix;               // pixels in the batch
+    int spp, sample_begin;
+    int n_paths;            // npix * spp
+    int *pix_of;            // batch pixel -> image pixel (y * W + x)
+    int *tile_of;           // batch pixel -> (local x | local y << 16)
+};
+
+}  // namespace rtgpu

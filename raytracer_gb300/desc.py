@@ -114,9 +114,13 @@ class LightR(C.Structure):
 
 
 class RenderStats(C.Structure):
-    _fields_ = [("kernel_ms", C.c_double), ("trace_ms", C.c_double), ("paths", C.c_int64),
-                ("closest_rays", C.c_int64), ("shadow_rays", C.c_int64), ("launches", C.c_int64),
-                ("limit_hits", C.c_int64), ("nan_samples", C.c_int64)]
+    _fields_ = [("kernel_ms", C.c_double), ("camera_ms", C.c_double), ("trace_closest_ms", C.c_double),
+                ("trace_any_ms", C.c_double), ("shade_ms", C.c_double), ("volpath_ms", C.c_double),
+                ("film_ms", C.c_double), ("paths", C.c_int64), ("closest_rays", C.c_int64),
+                ("shadow_rays", C.c_int64), ("launches", C.c_int64), ("trace_closest_launches", C.c_int64),
+                ("trace_any_launches", C.c_int64), ("nodes_closest", C.c_int64), ("tris_closest", C.c_int64),
+                ("nodes_any", C.c_int64), ("tris_any", C.c_int64), ("limit_hits", C.c_int64),
+                ("nan_samples", C.c_int64)]
 
 
 RAY_DTYPE = np.dtype([("o", np.float32, 3), ("mint", np.float32), ("d", np.float32, 3),

@@ -1,0 +1,81 @@
+"""Generate the golden fixtures that pin the CPU oracle to the reference.
+
+The reference's own tools/Rng.h (PCG32) and core/CDF.{h,cpp} are compiled in
+place by oracle/build_oracle.py (libref_pin.so); this script runs them on
+seeded inputs and writes small JSON fixtures next to itself:
+
+* pcg32_ref.json  -- raw 32-bit outputs and mantissa floats of Rng streams
+* cdf_ref.json    -- CDF::sampleAndReuse / CDF::sample on seeded pdf lists
+
+Run from the repository root:  python tests/golden/make_golden.py
+"""
+import ctypes as C
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+import build_oracle  # noqa: E402
+
+
+def main():
+    path = build_oracle.build_ref_pin(force=True)
+    if path is None:
+        raise SystemExit("reference sources not present; fixtures cannot be regenerated here")
+    L = C.CDLL(path)
+    L.ref_pcg_stream.argtypes = [C.c_uint64, C.c_uint64, C.c_int, C.c_void_p]
+    L.ref_pcg_reals.argtypes = [C.c_uint64, C.c_uint64, C.c_int, C.c_void_p]
+    L.ref_cdf_sample_reuse.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
+                                       C.c_void_p, C.c_void_p]
+    L.ref_cdf_sample.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+    streams = []
+    seeds = [(42, 54), (0, 0), (1, 1), (0xdeadbeefcafebabe, 7), (2 ** 64 - 1, 2 ** 63 + 5), (12345, 0)]
+    # path-stream seeds: splitmix64((seed << 32) ^ pixel), sample index
+    def mix64(x):
+        x &= 2 ** 64 - 1
+        x ^= x >> 30; x = (x * 0xbf58476d1ce4e5b9) & (2 ** 64 - 1)
+        x ^= x >> 27; x = (x * 0x94d049bb133111eb) & (2 ** 64 - 1)
+        x ^= x >> 31
+        return x
+    for pix, s in [(0, 0), (1, 0), (65535, 15), (1048575, 63)]:
+        seeds.append((mix64((0 << 32) ^ pix), s))
+    for st, sq in seeds:
+        u = np.zeros(64, np.uint32)
+        f = np.zeros(64, np.float32)
+        L.ref_pcg_stream(st, sq, 64, u.ctypes.data)
+        L.ref_pcg_reals(st, sq, 64, f.ctypes.data)
+        streams.append(dict(initstate=str(st), initseq=str(sq), u32=[int(x) for x in u],
+                            real_bits=[int(x) for x in f.view(np.uint32)]))
+    json.dump(dict(source="RaytracerNew2/src/tools/Rng.h compiled in place", streams=streams),
+              open(os.path.join(HERE, "pcg32_ref.json"), "w"), indent=0)
+    rng = np.random.default_rng(7)
+    cases = []
+    for n in [1, 2, 3, 7, 32, 100, 1000]:
+        pdfs = rng.random(n).astype(np.float32)
+        if n > 4:
+            pdfs[rng.integers(0, n, 2)] = 0.0  # zero-weight entries (empty rows / black texels)
+        u = np.concatenate([rng.random(200), [0.0, 1e-9, 0.5, 0.999999, np.nextafter(np.float32(1), 0)]]).astype(np.float32)
+        idx = np.zeros(len(u), np.int32)
+        uo = np.zeros(len(u), np.float32)
+        po = np.zeros(len(u), np.float32)
+        sm = np.zeros(1, np.float32)
+        L.ref_cdf_sample_reuse(pdfs.ctypes.data, n, u.ctypes.data, len(u), idx.ctypes.data, uo.ctypes.data,
+                               po.ctypes.data, sm.ctypes.data)
+        idx2 = np.zeros(len(u), np.int32)
+        po2 = np.zeros(len(u), np.float32)
+        L.ref_cdf_sample(pdfs.ctypes.data, n, u.ctypes.data, len(u), idx2.ctypes.data, po2.ctypes.data)
+        cases.append(dict(pdf_bits=[int(x) for x in pdfs.view(np.uint32)], u_bits=[int(x) for x in u.view(np.uint32)],
+                          index=[int(x) for x in idx], u_out_bits=[int(x) for x in uo.view(np.uint32)],
+                          pdf_out_bits=[int(x) for x in po.view(np.uint32)], sum_bits=int(sm.view(np.uint32)[0]),
+                          sample_index=[int(x) for x in idx2], sample_pdf_bits=[int(x) for x in po2.view(np.uint32)]))
+    json.dump(dict(source="RaytracerNew2/src/core/CDF.h + CDF.cpp compiled in place", cases=cases),
+              open(os.path.join(HERE, "cdf_ref.json"), "w"))
+    print("wrote", os.path.join(HERE, "pcg32_ref.json"), os.path.join(HERE, "cdf_ref.json"))
+
+
+if __name__ == "__main__":
+    main()

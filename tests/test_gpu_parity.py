@@ -1,0 +1,274 @@
+"""GPU parity: the CUDA path (through the C ABI) against the CPU oracle on
+the same seeded inputs.
+
+Tolerances (stated per test):
+* ray casting: identical hit/miss and triangle index; hit distance and
+  barycentrics within 2 ulp (both sides evaluate Moller-Trumbore in the same
+  binary32 order; the only freedom is which of several triangles at exactly
+  the same distance wins, and such ties are accepted);
+* BSDF eval / pdf / sample: 1e-5 relative (the device's expf/logf/sinf/...
+  differ from the C library by a few ulp);
+* rendered films: per-path radiance through identical path streams; paths
+  whose branch decisions flip on a last-ulp difference are counted and held
+  to a small fraction.
+"""
+import numpy as np
+import pytest
+
+import oracle_lib as O
+from raytracer_gb300 import desc as D, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def _ulp_diff(a, b):
+    a = np.asarray(a, np.float32).view(np.int32).astype(np.int64)
+    b = np.asarray(b, np.float32).view(np.int32).astype(np.int64)
+    a = np.where(a < 0, np.int64(-2 ** 31) - a, a)
+    b = np.where(b < 0, np.int64(-2 ** 31) - b, b)
+    return np.abs(a - b)
+
+
+def _random_rays(scene, n, rng, mint=1e-4):
+    lo, hi = scene.bounds()
+    ext = hi - lo
+    o = lo + rng.random((n, 3)) * ext
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    r = np.zeros(n, D.RAY_DTYPE)
+    r["o"], r["d"], r["mint"], r["maxt"] = o, d, mint, 1e8
+    return r
+
+
+@pytest.fixture(scope="module")
+def cornell():
+    return scenes.cornell_box(64, 48)
+
+
+@pytest.fixture(scope="module")
+def ico():
+    return scenes.displaced_icosphere(level=5, width=48, height=48, env_size=(128, 64))
+
+
+@pytest.fixture(scope="module")
+def vol():
+    return scenes.volume_grid(40, 32, res=32)
+
+
+def _trace_parity(ctx, rtlib, scene, n=20000, seed=0):
+    rng = np.random.default_rng(seed)
+    rays = _random_rays(scene, n, rng)
+    o = O.OracleScene(scene)
+    cam = o.camera_rays(rng.random((n // 4, 2)) * [scene.camera["width"], scene.camera["height"]])
+    rays = np.concatenate([rays, cam])
+    g = rtlib.Scene(ctx, scene)
+    hg = g.trace(rays)
+    ho = o.trace(rays)
+    hit_g, hit_o = hg["prim"] != -1, ho["prim"] != -1
+    mism = np.count_nonzero(hit_g != hit_o)
+    both = hit_g & hit_o
+    same = both & (hg["prim"] == ho["prim"])
+    tied = both & (hg["prim"] != ho["prim"])
+    # a different triangle is acceptable only at exactly the same distance
+    assert np.all(hg["t"][tied] == ho["t"][tied]), "different triangle at a different distance"
+    ud = _ulp_diff(hg["t"][same], ho["t"][same])
+    uu = _ulp_diff(hg["u"][same], ho["u"][same])
+    print("rays %d hits %d miss-mismatch %d tied %d max-ulp t %d u %d" %
+          (len(rays), both.sum(), mism, tied.sum(), ud.max(initial=0), uu.max(initial=0)))
+    assert mism == 0
+    assert ud.max(initial=0) <= 2 and uu.max(initial=0) <= 2
+    ag = g.trace(rays, anyhit=True)
+    ao = o.trace(rays, anyhit=True)
+    assert np.array_equal(ag["prim"] == 0, ao["prim"] == 0)
+    g.close()
+    o.close()
+
+
+def test_trace_parity_cornell(ctx, rtlib, cornell):
+    _trace_parity(ctx, rtlib, cornell)
+
+
+def test_trace_parity_icosphere(ctx, rtlib, ico):
+    _trace_parity(ctx, rtlib, ico, n=40000, seed=1)
+
+
+def test_trace_parity_spheres_and_boxes(ctx, rtlib, vol):
+    _trace_parity(ctx, rtlib, vol, n=20000, seed=2)
+
+
+def test_trace_edge_cases(ctx, rtlib, cornell):
+    g = rtlib.Scene(ctx, cornell)
+    o = O.OracleScene(cornell)
+    r = np.zeros(6, D.RAY_DTYPE)
+    # axis-aligned directions (zero components), maxt < mint, grazing, outside
+    r["o"] = [(0.5, 0.5, 0.5), (0.5, 0.5, 0.5), (0.5, 0.5, 0.5), (0.0, 0.5, 0.5), (5, 5, 5), (0.5, 1e-7, 0.5)]
+    r["d"] = [(1, 0, 0), (0, 1, 0), (0, 0, -1), (0, 1, 0), (1, 0, 0), (1, 0, 0)]
+    r["mint"] = [1e-4, 1e-4, 1e-4, 1e-4, 1e-4, 1e-4]
+    r["maxt"] = [1e8, 1e8, 1e-5, 1e8, 1e8, 1e8]
+    hg, ho = g.trace(r), o.trace(r)
+    assert np.array_equal(hg["prim"] != -1, ho["prim"] != -1)
+    m = (hg["prim"] != -1)
+    assert np.array_equal(hg["t"][m], ho["t"][m])
+    assert len(g.trace(np.zeros(0, D.RAY_DTYPE))) == 0
+
+
+BSDFS = [
+    D.bsdf(D.BSDF_DIFFUSE, albedo=(0.2, 0.5, 0.8)),
+    D.bsdf(D.BSDF_ROUGH_CONDUCTOR, distribution=D.DIST_GGX, alpha=0.15, eta=scenes.AU_ETA, k=scenes.AU_K),
+    D.bsdf(D.BSDF_ROUGH_CONDUCTOR, distribution=D.DIST_BECKMANN, alpha=0.4, eta=scenes.AU_ETA, k=scenes.AU_K),
+    D.bsdf(D.BSDF_ROUGH_CONDUCTOR, distribution=D.DIST_PHONG, alpha=30.0, eta=scenes.AU_ETA, k=scenes.AU_K),
+    D.bsdf(D.BSDF_ROUGH_DIELECTRIC, distribution=D.DIST_GGX, alpha=0.1, eta_int=1.5),
+    D.bsdf(D.BSDF_ROUGH_DIELECTRIC, distribution=D.DIST_BECKMANN, alpha=0.3, eta_int=1.33),
+    D.bsdf(D.BSDF_SMOOTH_LAYERED, albedo=(0.7, 0.25, 0.2), eta_int=1.5, thickness=0.1, absorbance=(0.1, 0.2, 0.3)),
+]
+
+
+def _rel_close(a, b, rtol, atol):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    both_nan = np.isnan(a) & np.isnan(b)
+    err = np.abs(a - b) / np.maximum(np.abs(b), atol / rtol)
+    return both_nan | (err <= rtol)
+
+
+@pytest.mark.parametrize("bi", range(len(BSDFS)))
+def test_bsdf_parity(ctx, rtlib, bi):
+    rng = np.random.default_rng(10 + bi)
+    s = scenes.cornell_box(8, 8)
+    s.bsdfs = [BSDFS[bi]]
+    for m in s.meshes:
+        m["bsdf"] = 0
+    g = rtlib.Scene(ctx, s)
+    n = 20000
+    wi = rng.normal(size=(n, 3)); wi /= np.linalg.norm(wi, axis=1, keepdims=True)
+    wo = rng.normal(size=(n, 3)); wo /= np.linalg.norm(wo, axis=1, keepdims=True)
+    wi[: n // 2, 2] = np.abs(wi[: n // 2, 2])
+    wo[: n // 4, 2] = np.abs(wo[: n // 4, 2])
+    q = np.zeros(n, O.BSDF_Q)
+    q["wi"], q["wo"], q["u"] = wi, wo, rng.random((n, 2))
+    for op, fields in ((D.BSDF_OP_EVAL, ["value"]), (D.BSDF_OP_PDF, ["pdf"]),
+                       (D.BSDF_OP_SAMPLE, ["value", "pdf", "wo", "relative_eta"])):
+        rg = g.bsdf_query(0, op, q)
+        ro = O.bsdf_query(BSDFS[bi], op, q)
+        if op == D.BSDF_OP_SAMPLE:
+            assert np.mean(rg["sampled_type"] == ro["sampled_type"]) > 0.999
+        for f in fields:
+            ok = _rel_close(rg[f], ro[f], 1e-5, 1e-7)
+            ok = ok.reshape(n, -1).all(1)
+            frac = 1 - ok.mean()
+            print("bsdf %d op %d %s mismatch fraction %.2e" % (bi, op, f, frac))
+            # branch flips (s.x <= Fr, sign tests) on last-ulp differences only
+            assert frac <= 2e-3, (bi, op, f, frac)
+    g.close()
+
+
+def _light_parity(ctx, rtlib, scene, light, n=20000, seed=0):
+    rng = np.random.default_rng(seed)
+    lo, hi = scene.bounds()
+    p = (lo + rng.random((n, 3)) * (hi - lo)).astype(np.float32)
+    u = rng.random((n, 2)).astype(np.float32)
+    g = rtlib.Scene(ctx, scene)
+    o = O.OracleScene(scene)
+    rg, ro = g.light_query(light, p, u), o.light_query(light, p, u)
+    for f in ("intensity", "pdf", "to_light", "distance", "point", "pdf_eval"):
+        ok = _rel_close(rg[f], ro[f], 1e-5, 1e-6).reshape(n, -1).all(1)
+        frac = 1 - ok.mean()
+        print("light %d %s mismatch fraction %.2e" % (light, f, frac))
+        assert frac <= 1e-3, (f, frac)
+    g.close()
+    o.close()
+
+
+def test_mesh_light_parity(ctx, rtlib, cornell):
+    _light_parity(ctx, rtlib, cornell, 0)
+
+
+def test_env_light_parity(ctx, rtlib, ico):
+    _light_parity(ctx, rtlib, ico, ico.env_light, seed=1)
+
+
+def test_sphere_light_parity(ctx, rtlib, vol):
+    _light_parity(ctx, rtlib, vol, 0, seed=2)
+
+
+def _film_parity(ctx, rtlib, scene, spp, seed, max_bad, block=16, **over):
+    g = rtlib.Scene(ctx, scene)
+    o = O.OracleScene(scene)
+    fg = g.render(spp, seed=seed, block=block, **over)
+    fo = o.render(spp, seed=seed, block=block, **over)
+    assert np.array_equal(fg[..., 3], fo[..., 3]), "film weights differ (splat footprint)"
+    a, b = fg[..., :3].astype(np.float64), fo[..., :3].astype(np.float64)
+    err = np.abs(a - b) / np.maximum(np.abs(b), 1e-3)
+    pix_err = err.max(-1)
+    exact = np.mean(pix_err == 0)
+    bad = np.mean(pix_err > 1e-3)
+    print("%s spp %d: exact pixels %.4f, >1e-3 %.4f, median rel %.2e, mean ratio %.6f" %
+          (scene.name, spp, exact, bad, np.median(pix_err), a.sum() / max(b.sum(), 1e-30)))
+    assert bad <= max_bad
+    g.close()
+    o.close()
+    return fg, fo
+
+
+def test_film_parity_cornell(ctx, rtlib, cornell):
+    _film_parity(ctx, rtlib, cornell, 4, 11, max_bad=0.02)
+
+
+def test_film_parity_cornell_ragged_tiles_and_offset(ctx, rtlib):
+    s = scenes.cornell_box(37, 23)
+    _film_parity(ctx, rtlib, s, 3, 5, max_bad=0.03, block=8, sample_begin=7)
+
+
+def test_film_parity_icosphere_env(ctx, rtlib, ico):
+    _film_parity(ctx, rtlib, ico, 2, 3, max_bad=0.03)
+
+
+def test_film_parity_volume(ctx, rtlib, vol):
+    _film_parity(ctx, rtlib, vol, 2, 4, max_bad=0.08)
+
+
+def test_depth_limits(ctx, rtlib, cornell):
+    for md in (0, 1, 2):
+        _film_parity(ctx, rtlib, cornell, 1, 2, max_bad=0.02, max_depth=md, min_depth=0)
+
+
+def test_weighted_light_strategy(ctx, rtlib, cornell):
+    _film_parity(ctx, rtlib, cornell, 1, 9, max_bad=0.02, strategy=D.STRATEGY_ONE_LIGHT_WEIGHTED)
+
+
+def test_converged_image_matches_oracle(ctx, rtlib):
+    """Statistical parity: independent sample streams, same expectation."""
+    s = scenes.cornell_box(32, 32)
+    g = rtlib.Scene(ctx, s)
+    o = O.OracleScene(s)
+    from raytracer_gb300 import post_process
+    ig = post_process(g.render(256, seed=1))
+    io = post_process(o.render(256, seed=2))
+    mg, mo = ig.mean((0, 1)), io.mean((0, 1))
+    print("mean gpu", mg, "oracle", mo)
+    assert np.allclose(mg, mo, rtol=0.02)
+    g.close()
+
+
+def test_invalid_inputs_raise(ctx, rtlib, cornell):
+    import raytracer_gb300 as R
+    bad = scenes.cornell_box(8, 8)
+    bad.meshes[0]["bsdf"] = 99
+    with pytest.raises(R.RtError):
+        R.Scene(ctx, bad)
+    g = R.Scene(ctx, cornell)
+    with pytest.raises(R.RtError):
+        g.render(0)
+    with pytest.raises(R.RtError):
+        g.bsdf_query(42, 0, np.zeros(1, R.core.BSDF_Q))
+    g.close()
+
+
+def test_empty_scene_renders_background(ctx, rtlib):
+    s = scenes.displaced_icosphere(level=0, width=16, height=16, env_size=(32, 16))
+    s.meshes = []
+    s.indices = np.zeros((0, 3), np.int32)
+    s.vertices = np.zeros((0, 3), np.float32)
+    g = rtlib.Scene(ctx, s)
+    o = O.OracleScene(s)
+    fg, fo = g.render(2, seed=1), o.render(2, seed=1)
+    assert np.allclose(fg, fo, rtol=1e-5, atol=1e-6)

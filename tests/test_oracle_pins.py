@@ -1,0 +1,159 @@
+"""Pin the CPU oracle: PCG32 and CDF against the reference's own code
+(golden fixtures generated from tools/Rng.h and core/CDF.{h,cpp} compiled in
+place, tests/golden/make_golden.py) and the published PCG32 known answer;
+plus determinism and physical sanity checks of the restatement."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle_lib as O
+from raytracer_gb300 import desc as D, scenes
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _stream(st, sq, n):
+    out = np.zeros(n, np.uint32)
+    O.lib().oracle_pcg_stream(st, sq, n, O._p(out))
+    return out
+
+
+def test_pcg32_published_known_answer():
+    # pcg32 reference demo: seed(42, 54) -> first six outputs
+    assert [hex(x) for x in _stream(42, 54, 6)] == [
+        "0xa15c02b7", "0x7b47f409", "0xba1d3330", "0x83d2f293", "0xbfa4784b", "0xcbed606e"]
+
+
+def test_pcg32_matches_reference_rng_h():
+    g = json.load(open(os.path.join(GOLDEN, "pcg32_ref.json")))
+    assert len(g["streams"]) >= 10
+    for s in g["streams"]:
+        st, sq = int(s["initstate"]), int(s["initseq"])
+        assert list(_stream(st, sq, 64)) == s["u32"]
+        f = np.zeros(64, np.float32)
+        O.lib().oracle_pcg_reals(st, sq, 64, O._p(f))
+        assert list(f.view(np.uint32)) == s["real_bits"]
+
+
+def test_cdf_matches_reference_cdf_h():
+    g = json.load(open(os.path.join(GOLDEN, "cdf_ref.json")))
+    for c in g["cases"]:
+        pdfs = np.array(c["pdf_bits"], np.uint32).view(np.float32)
+        u = np.array(c["u_bits"], np.uint32).view(np.float32)
+        idx = np.zeros(len(u), np.int32)
+        uo = np.zeros(len(u), np.float32)
+        po = np.zeros(len(u), np.float32)
+        sm = np.zeros(1, np.float32)
+        O.lib().oracle_cdf_sample_reuse(O._p(pdfs), len(pdfs), O._p(u), len(u), O._p(idx), O._p(uo), O._p(po), O._p(sm))
+        assert list(idx) == c["index"]
+        assert list(uo.view(np.uint32)) == c["u_out_bits"]
+        assert list(po.view(np.uint32)) == c["pdf_out_bits"]
+        assert int(sm.view(np.uint32)[0]) == c["sum_bits"]
+        idx2 = np.zeros(len(u), np.int32)
+        po2 = np.zeros(len(u), np.float32)
+        O.lib().oracle_cdf_sample(O._p(pdfs), len(pdfs), O._p(u), len(u), O._p(idx2), O._p(po2))
+        assert list(idx2) == c["sample_index"]
+        assert list(po2.view(np.uint32)) == c["sample_pdf_bits"]
+
+
+def test_reference_pin_library_agrees_live():
+    """Where the reference tree is present, re-run its Rng.h / CDF.h live."""
+    import sys
+    sys.path.insert(0, os.path.join(O.ROOT, "oracle"))
+    import build_oracle
+    path = build_oracle.build_ref_pin()
+    if path is None:
+        pytest.skip("reference sources not present on this machine")
+    import ctypes as C
+    L = C.CDLL(path)
+    L.ref_pcg_stream.argtypes = [C.c_uint64, C.c_uint64, C.c_int, C.c_void_p]
+    rng = np.random.default_rng(3)
+    for _ in range(20):
+        st, sq = int(rng.integers(0, 2 ** 63)), int(rng.integers(0, 2 ** 63))
+        ref = np.zeros(100, np.uint32)
+        L.ref_pcg_stream(st, sq, 100, ref.ctypes.data)
+        assert np.array_equal(ref, _stream(st, sq, 100))
+
+
+def test_oracle_render_is_thread_count_independent():
+    s = scenes.cornell_box(40, 24)
+    o = O.OracleScene(s)
+    a = o.render(3, seed=5, threads=1, block=16)
+    b = o.render(3, seed=5, threads=7, block=16)
+    assert np.array_equal(a, b)
+    assert a[..., 3].min() >= 2 and a[..., 3].max() <= 4   # box-filter weights
+
+
+def _q(wi, wo=None, u=None):
+    q = np.zeros(len(wi), O.BSDF_Q)
+    q["wi"] = wi
+    if wo is not None:
+        q["wo"] = wo
+    if u is not None:
+        q["u"] = u
+    return q
+
+
+def _sphere_dirs(n, rng, upper=True):
+    v = rng.normal(size=(n, 3))
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    if upper:
+        v[:, 2] = np.abs(v[:, 2])
+    return v.astype(np.float32)
+
+
+def test_diffuse_furnace_and_pdf():
+    rng = np.random.default_rng(0)
+    b = D.bsdf(D.BSDF_DIFFUSE, albedo=(0.3, 0.6, 0.9))
+    wi = _sphere_dirs(4000, rng)
+    r = O.bsdf_query(b, D.BSDF_OP_SAMPLE, _q(wi, u=rng.random((4000, 2))))
+    assert np.allclose(r["value"], [0.3, 0.6, 0.9])
+    assert np.allclose(r["pdf"], r["wo"][:, 2] / np.pi, rtol=1e-6)
+    # eval * cos / pdf == albedo along sampled directions
+    e = O.bsdf_query(b, D.BSDF_OP_EVAL, _q(wi, r["wo"]))
+    ok = r["pdf"] > 1e-3
+    assert np.allclose(e["value"][ok] * r["wo"][ok, 2:3] / r["pdf"][ok, None], [0.3, 0.6, 0.9], rtol=1e-5)
+
+
+def test_rough_conductor_estimator_consistency():
+    """sample() weight == eval * |cos| / pdf for the reference's RoughConductor."""
+    rng = np.random.default_rng(1)
+    for dist in (D.DIST_BECKMANN, D.DIST_GGX, D.DIST_PHONG):
+        b = D.bsdf(D.BSDF_ROUGH_CONDUCTOR, distribution=dist, alpha=0.3 if dist != D.DIST_PHONG else 20.0,
+                   eta=scenes.AU_ETA, k=scenes.AU_K)
+        wi = _sphere_dirs(2000, rng)
+        r = O.bsdf_query(b, D.BSDF_OP_SAMPLE, _q(wi, u=rng.random((2000, 2))))
+        ok = (r["pdf"] > 1e-2) & (np.abs(r["value"]).sum(1) > 0)
+        assert ok.sum() > 200
+        e = O.bsdf_query(b, D.BSDF_OP_EVAL, _q(wi[ok], r["wo"][ok]))
+        p = O.bsdf_query(b, D.BSDF_OP_PDF, _q(wi[ok], r["wo"][ok]))
+        assert np.allclose(p["pdf"], r["pdf"][ok], rtol=1e-5)
+        est = e["value"] * np.abs(r["wo"][ok, 2:3]) / p["pdf"][:, None]
+        assert np.allclose(est, r["value"][ok], rtol=1e-4)
+
+
+def test_fresnel_normal_incidence_of_smooth_coat():
+    # SmoothLayered reflects with probability Fr(normal) = ((n-1)/(n+1))^2
+    b = D.bsdf(D.BSDF_SMOOTH_LAYERED, eta_int=1.5, eta_ext=1.0)
+    fr = ((1.5 - 1.0) / 2.5) ** 2
+    r = O.bsdf_query(b, D.BSDF_OP_SAMPLE, _q(np.array([[0, 0, 1]] * 2, np.float32),
+                                             u=np.array([[fr * 0.99, 0.3], [fr * 1.01, 0.3]], np.float32)))
+    assert r["sampled_type"][0] == 2 and np.isclose(r["pdf"][0], fr, rtol=1e-6)   # delta reflection
+    assert r["sampled_type"][1] == 0                                              # through the coat
+
+
+def test_triangle_hit_exactness_small_scene():
+    s = scenes.cornell_box(16, 16)
+    o = O.OracleScene(s)
+    rays = np.zeros(3, D.RAY_DTYPE)
+    rays["o"] = [(0.5, 0.5, 0.5), (0.8, 0.8, 0.5), (0.2, 0.9, 0.5)]
+    rays["d"] = [(0, -1, 0), (0, 0, -1), (0, 1, 0)]
+    rays["mint"] = 1e-4
+    rays["maxt"] = 1e8
+    h = o.trace(rays)
+    assert np.allclose(h["t"], [0.5, 0.5, 0.1], atol=1e-6)
+    assert (h["prim"] >= 0).all()
+    a = o.trace(rays, anyhit=True)
+    assert (a["prim"] == 0).all()
