@@ -26,6 +26,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 CONFIG = dict(level=8, width=1024, height=1024, spp=64, max_depth=16, env=(1024, 512), seed=0)
+# --small: the same scene at 512x512, 8 spp, for profiler captures only
+SMALL = dict(width=512, height=512, spp=8)
 WORKLOAD = "displaced_icosphere_1310720tri_1024x1024_64spp_depth16_sky1024x512"
 METRIC = "path samples/s"
 UNIT = "samples/s"
@@ -228,10 +230,10 @@ def run_gpu(args):
     host_film = None
     barrier()
     t0 = time.perf_counter()
-    for k in range(args.steps):
+    for k in range(0 if args.small else args.steps):
         host_film = scene.render(spp, seed=2000 + k, sample_begin=sbase)
     barrier()
-    e2e_s = time.perf_counter() - t0
+    e2e_s = max(time.perf_counter() - t0, 1e-9)
     e2e_value = samples_per_step * args.steps * world / e2e_s
     d2h = W * H * 16
     h2d = 64 + 4 * (len(data.lights) + 1)
@@ -269,7 +271,7 @@ def run_gpu(args):
             traffic = None
     rays_per_s = (rays_c + rays_a) * world / t_local
     res = {}
-    if rank == 0:
+    if rank == 0 and not args.small:
         try:
             cpu_o, start, n, _ = cpu_oracle_rate(data, target_s=args.cpu_seconds)
             threads = os.cpu_count() or 1
@@ -318,7 +320,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--small", action="store_true",
+                    help="profiler case: same scene at 512x512, 8 spp, no CPU baseline, no e2e")
     args = ap.parse_args()
+    if args.small:
+        CONFIG.update(SMALL)
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -179,15 +179,159 @@ __global__ void __launch_bounds__(128) k_trace(RenderParams P, int round)
 }
 
 // ---------------------------------------------------------------- PathTracingMIS vertex
+// The per-vertex loop body of PathTracingMIS::li (PathTracingMIS.cpp:54-259)
+// is split in two wavefront stages:
+//   k_pt_resolve  finishes vertex v once its rays are traced: adds the light
+//                 sample if unoccluded (:140), the MIS-weighted emission found
+//                 by the BSDF-sampled ray (:173-220), throughput / eta update
+//                 (:222-223), Russian roulette (:225-253); then sorts the
+//                 surviving path by the BSDF type of its next vertex;
+//   k_pt_shade<T> shades vertex v+1 for one BSDF type: emission at depth 0
+//                 (:73-74), light sample (:121-153), BSDF sample (:156-168),
+//                 emitting the shadow ray and the next closest-hit ray.
+__global__ void __launch_bounds__(128) k_pt_resolve(RenderParams P, int round)
+{
+    const DevScene &S = P.S;
+    RoundCounters *C = &P.W.cnt[round];
+    const int n = C->active;
+    const int *qin = P.W.q_active[round & 1];
+    const int env = S.env_light;
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    int stride = gridDim.x * blockDim.x;
+    int iters = (n + stride - 1) / stride;
+    for (int it = 0; it < iters; it++, idx += stride) {
+        bool valid = idx < n;
+        int slot = valid ? qin[idx] : 0;
+        int mtype = -1;
+        if (valid) {
+            int flags = P.W.flags[slot];
+            float4 radv = P.W.rad[slot];
+            C3 L = rgb(radv);
+            int depth = __float_as_int(radv.w);
+            float4 hv = P.W.hit[slot];
+            Hit h; h.t = hv.x; h.u = hv.y; h.v = hv.z; h.prim = __float_as_int(hv.w);
+            bool done = false;
+            bool state_dirty = false;
+            float4 tpv = make_float4(0, 0, 0, 0);
+            if (flags & F_FIRST) {
+                flags &= ~F_FIRST;
+                if (h.prim == -1) {
+                    if (env >= 0) {
+                        float4 rd = P.W.ray_d[slot];
+                        L = L + env_le(S.lights[env], xyz(rd));
+                    }
+                    done = true;
+                } else if (depth >= P.max_depth) {
+                    done = true;
+                }
+            } else {
+                if ((flags & F_NEE) && !P.W.occl[slot]) L = L + rgb(P.W.nee[slot]);
+                flags &= ~F_NEE;
+                if (flags & F_END) {
+                    done = true;
+                } else {
+                    tpv = P.W.tp[slot];
+                    C3 T = rgb(tpv);
+                    float eta = tpv.w;
+                    float4 bsv = P.W.bs[slot];
+                    C3 f = rgb(bsv);
+                    float bpdf = bsv.w;
+                    float4 ro = P.W.ray_o[slot], rd = P.W.ray_d[slot];
+                    V3 o = xyz(ro), d = xyz(rd);
+                    int caught = -1;
+                    bool isenv = false;
+                    C3 Le = cfill(0.f);
+                    V3 pt = v3(0, 0, 0), nn = v3(0, 0, 0);
+                    if (h.prim != -1) {
+                        int nl = prim_light(S, h.prim);
+                        if (nl >= 0) {
+                            Frame fr = hit_frame(S, h, o, d);
+                            pt = fr.p; nn = fr.n;
+                            caught = nl;
+                            Le = area_le(S, nl, -d, fr.n);
+                        }
+                    } else {
+                        if (env < 0) done = true;
+                        else { caught = env; isenv = true; Le = env_le(S.lights[env], d); }
+                    }
+                    if (!done && caught >= 0) {
+                        float pl = (flags & F_DELTA) ? 0.f : light_pdf(S, caught, o, pt, nn, d);
+                        float w = power_heuristic(bpdf, pl);
+                        L = L + ((T * Le) * f) * w;
+                        if (isenv) done = true;
+                    }
+                    if (!done) {
+                        T = T * f;
+                        eta *= P.W.rel_eta[slot];
+                        if (depth >= P.min_depth) {
+                            Pcg32 rng = P.W.rng[slot];
+                            float stop = smin(0.95f, lum(T) * eta * eta);
+                            if (next1d(rng) < stop) T = T / stop;
+                            else done = true;
+                            P.W.rng[slot] = rng;
+                        }
+                        tpv = f4c(T, eta);
+                        state_dirty = true;
+                    }
+                    if (!done) {
+                        depth++;
+                        if (depth >= P.max_depth) done = true;
+                    }
+                }
+            }
+            if (!done) {
+                int b = prim_bsdf(S, h.prim);
+                if (b < 0) done = true;
+                else mtype = S.bsdfs[b].type;
+            }
+            if (done) {
+                flags |= F_DONE;
+                P.W.out[slot] = f4c(L, 0.f);
+            } else {
+                P.W.rad[slot] = f4c(L, __int_as_float(depth));
+                if (state_dirty) P.W.tp[slot] = tpv;
+            }
+            P.W.flags[slot] = flags;
+        }
+#pragma unroll
+        for (int t = 0; t < 4; t++) q_push(P.W.q_mat[t], &C->mat[t], slot, mtype == t);
+    }
+}
+
+template <int BT>
+__device__ __forceinline__ C3 bsdf_eval_t(const DevBsdf &b, V3 wi, V3 wo)
+{
+    if (BT == 0) return diffuse_eval(b.albedo, wi, wo);
+    if (BT == 1) return rc_eval(b, wi, wo);
+    if (BT == 2) return rd_eval(b, wi, wo);
+    return sl_eval(b, wi, wo);
+}
+template <int BT>
+__device__ __forceinline__ float bsdf_pdf_t(const DevBsdf &b, V3 wi, V3 wo)
+{
+    if (BT == 0) return diffuse_pdf(wi, wo);
+    if (BT == 1) return rc_pdf(b, wi, wo);
+    if (BT == 2) return rd_pdf(b, wi, wo);
+    return sl_pdf(b, wi, wo);
+}
+template <int BT>
+__device__ __forceinline__ C3 bsdf_sample_t(const DevBsdf &b, BsdfRec &r, V2 s)
+{
+    if (BT == 0) return diffuse_sample(b.albedo, r, s);
+    if (BT == 1) return rc_sample(b, r, s);
+    if (BT == 2) return rd_sample(b, r, s);
+    return sl_sample(b, r, s);
+}
+
+template <int BT>
 __global__ void __launch_bounds__(128) k_pt_shade(RenderParams P, int round)
 {
     const DevScene &S = P.S;
-    RoundCounters *Cin = &P.W.cnt[round];
+    RoundCounters *C = &P.W.cnt[round];
     RoundCounters *Cout = &P.W.cnt[round + 1];
-    const int n = Cin->active;
-    const int *qin = P.W.q_active[round & 1];
+    const int n = C->mat[BT];
+    const int *qin = P.W.q_mat[BT];
     int *qout = P.W.q_active[(round + 1) & 1];
-    const int env = S.env_light;
     int idx = blockIdx.x * blockDim.x + threadIdx.x;
     int stride = gridDim.x * blockDim.x;
     int iters = (n + stride - 1) / stride;
@@ -198,134 +342,70 @@ __global__ void __launch_bounds__(128) k_pt_shade(RenderParams P, int round)
         if (valid) {
             Pcg32 rng = P.W.rng[slot];
             float4 tpv = P.W.tp[slot];
-            float4 radv = P.W.rad[slot];
             C3 T = rgb(tpv);
-            float eta = tpv.w;
-            C3 L = rgb(radv);
+            float4 radv = P.W.rad[slot];
             int depth = __float_as_int(radv.w);
             int flags = P.W.flags[slot];
             float4 ro = P.W.ray_o[slot], rd = P.W.ray_d[slot];
-            Ray ray = make_ray(xyz(ro), xyz(rd), ro.w, rd.w);
+            V3 o = xyz(ro), d = xyz(rd);
             float4 hv = P.W.hit[slot];
             Hit h; h.t = hv.x; h.u = hv.y; h.v = hv.z; h.prim = __float_as_int(hv.w);
-            bool done = false;
-            bool have_frame = false;
-            Frame fr;
-            if (flags & F_FIRST) {
-                flags &= ~F_FIRST;
-                if (h.prim == -1) {
-                    if (env >= 0) L = L + env_le(S.lights[env], ray.d);
-                    done = true;
-                } else if (depth >= P.max_depth) {
-                    done = true;
+            Frame fr = hit_frame(S, h, o, d);
+            const DevBsdf &B = S.bsdfs[prim_bsdf(S, h.prim)];
+            if (depth == 0) {
+                int hl = prim_light(S, h.prim);
+                if (hl >= 0) {
+                    C3 L = rgb(radv) + T * area_le(S, hl, -d, fr.n);
+                    P.W.rad[slot] = f4c(L, radv.w);
+                }
+            }
+            // light sampling (Integrator::sampleLightDirect, Integrator.cpp:176-218)
+            V2 s = next2d(rng);
+            if (S.n_lights > 0) {
+                float lw;
+                int li_idx = cdf_sample_reuse(S.light_cdf, S.n_lights + 1, s.x, lw);
+                LightRec li;
+                light_sample(S, li_idx, fr.p, s, li);
+                if (li.pdf > 0 && lum(li.intensity) > 0) {
+                    C3 value = (li.intensity / li.pdf) / lw;
+                    li.pdf *= lw;
+                    if (!iszero(value)) {
+                        V3 wi = to_local(fr, li.to_light), wo = to_local(fr, -d);
+                        float ct = fabsf(wi.z);
+                        float bp = bsdf_pdf_t<BT>(B, wi, wo);
+                        float w = power_heuristic(li.pdf, bp);
+                        C3 contrib = (((T * value) * bsdf_eval_t<BT>(B, wi, wo)) * ct) * w;
+                        P.W.nee[slot] = f4c(contrib, 0.f);
+                        P.W.sh_o[slot] = f4(fr.p, RT_EPSILON);
+                        P.W.sh_d[slot] = f4(li.to_light, li.distance - RT_EPSILON);
+                        flags |= F_NEE;
+                        push_shadow = true;
+                    }
+                }
+            }
+            // BSDF sampling
+            BsdfRec r;
+            r.wi = to_local(fr, -d); r.wo = v3(0, 0, 0);
+            r.type = BT_ALL; r.rel_eta = 1.f; r.pdf = -1.f;
+            V2 u = next2d(rng);
+            C3 f = bsdf_sample_t<BT>(B, r, u);
+            if (iszero(f)) {
+                if (flags & F_NEE) { flags |= F_END; push_active = true; }
+                else {
+                    flags |= F_DONE;
+                    float4 rv = P.W.rad[slot];
+                    P.W.out[slot] = make_float4(rv.x, rv.y, rv.z, 0.f);
                 }
             } else {
-                // ---- resolve the previous vertex
-                if ((flags & F_NEE) && !P.W.occl[slot]) L = L + rgb(P.W.nee[slot]);
-                flags &= ~F_NEE;
-                if (flags & F_END) {
-                    done = true;
-                } else {
-                    float4 bsv = P.W.bs[slot];
-                    C3 f = rgb(bsv);
-                    float bpdf = bsv.w;
-                    int caught = -1;
-                    bool isenv = false;
-                    C3 Le = cfill(0.f);
-                    if (h.prim != -1) {
-                        fr = hit_frame(S, h, ray.o, ray.d);
-                        have_frame = true;
-                        int nl = prim_light(S, h.prim);
-                        if (nl >= 0) { caught = nl; Le = area_le(S, nl, -ray.d, fr.n); }
-                    } else {
-                        if (env < 0) done = true;
-                        else { caught = env; isenv = true; Le = env_le(S.lights[env], ray.d); }
-                    }
-                    if (!done && caught >= 0) {
-                        V3 pt = have_frame ? fr.p : v3(0, 0, 0), nn = have_frame ? fr.n : v3(0, 0, 0);
-                        float pl = (flags & F_DELTA) ? 0.f : light_pdf(S, caught, ray.o, pt, nn, ray.d);
-                        float w = power_heuristic(bpdf, pl);
-                        L = L + ((T * Le) * f) * w;
-                        if (isenv) done = true;
-                    }
-                    if (!done) {
-                        T = T * f;
-                        eta *= P.W.rel_eta[slot];
-                        if (depth >= P.min_depth) {
-                            float stop = smin(0.95f, lum(T) * eta * eta);
-                            if (next1d(rng) < stop) T = T / stop;
-                            else done = true;
-                        }
-                    }
-                    if (!done) {
-                        depth++;
-                        if (depth >= P.max_depth) done = true;
-                    }
-                }
-            }
-            if (!done) {
-                // ---- shade the vertex at h
-                if (!have_frame) fr = hit_frame(S, h, ray.o, ray.d);
-                int b = prim_bsdf(S, h.prim);
-                if (b < 0) {
-                    done = true;
-                } else {
-                    const DevBsdf &B = S.bsdfs[b];
-                    int hl = prim_light(S, h.prim);
-                    if (depth == 0 && hl >= 0) L = L + T * area_le(S, hl, -ray.d, fr.n);
-                    // light sampling (Integrator::sampleLightDirect)
-                    V2 s = next2d(rng);
-                    if (S.n_lights > 0) {
-                        float lw;
-                        int li_idx = cdf_sample_reuse(S.light_cdf, S.n_lights + 1, s.x, lw);
-                        LightRec li;
-                        light_sample(S, li_idx, fr.p, s, li);
-                        if (li.pdf > 0 && lum(li.intensity) > 0) {
-                            C3 value = (li.intensity / li.pdf) / lw;
-                            li.pdf *= lw;
-                            if (!iszero(value)) {
-                                V3 wi = to_local(fr, li.to_light), wo = to_local(fr, -ray.d);
-                                float ct = fabsf(wi.z);
-                                float bp = bsdf_pdf(B, wi, wo);
-                                float w = power_heuristic(li.pdf, bp);
-                                C3 contrib = (((T * value) * bsdf_eval(B, wi, wo)) * ct) * w;
-                                P.W.nee[slot] = f4c(contrib, 0.f);
-                                P.W.sh_o[slot] = f4(fr.p, RT_EPSILON);
-                                P.W.sh_d[slot] = f4(li.to_light, li.distance - RT_EPSILON);
-                                flags |= F_NEE;
-                                push_shadow = true;
-                            }
-                        }
-                    }
-                    // BSDF sampling
-                    BsdfRec r;
-                    r.wi = to_local(fr, -ray.d); r.wo = v3(0, 0, 0);
-                    r.type = BT_ALL; r.rel_eta = 1.f; r.pdf = -1.f;
-                    V2 u = next2d(rng);
-                    C3 f = bsdf_sample(B, r, u);
-                    if (iszero(f)) {
-                        if (flags & F_NEE) { flags |= F_END; push_active = true; }
-                        else done = true;
-                    } else {
-                        V3 nd = to_world(fr, r.wo);
-                        P.W.ray_o[slot] = f4(fr.p, RT_EPSILON);
-                        P.W.ray_d[slot] = f4(nd, RT_MAX_REAL);
-                        P.W.bs[slot] = f4c(f, r.pdf);
-                        P.W.rel_eta[slot] = r.rel_eta;
-                        if (r.type & BT_DELTA) flags |= F_DELTA; else flags &= ~F_DELTA;
-                        push_closest = true;
-                        push_active = true;
-                    }
-                }
-            }
-            if (done) {
-                flags |= F_DONE;
-                P.W.out[slot] = f4c(L, 0.f);
-                push_active = push_closest = push_shadow = false;
+                P.W.ray_o[slot] = f4(fr.p, RT_EPSILON);
+                P.W.ray_d[slot] = f4(to_world(fr, r.wo), RT_MAX_REAL);
+                P.W.bs[slot] = f4c(f, r.pdf);
+                P.W.rel_eta[slot] = r.rel_eta;
+                if (r.type & BT_DELTA) flags |= F_DELTA; else flags &= ~F_DELTA;
+                push_closest = true;
+                push_active = true;
             }
             P.W.rng[slot] = rng;
-            P.W.tp[slot] = f4c(T, eta);
-            P.W.rad[slot] = f4c(L, __int_as_float(depth));
             P.W.flags[slot] = flags;
         }
         q_push(qout, &Cout->active, slot, push_active);
@@ -716,6 +796,7 @@ struct rt_scene {
     float bounds[6];
     int n_lights = 0;
     int n_bsdfs = 0;
+    int bsdf_types = 0;   // bit t set when some BSDF of type t exists
     std::vector<float> light_power_lum;  // per light, for the weighted strategy
     std::vector<DevLight> lights_host;
     DevLight *lights_dev = nullptr;
@@ -1183,6 +1264,7 @@ rt_status rt_scene_create(rt_ctx *ctx, const rt_scene_desc *d, rt_scene **out)
     S.cam.medium = cd.medium;
     sc->n_lights = d->n_lights;
     sc->n_bsdfs = d->n_bsdfs;
+    for (int b = 0; b < d->n_bsdfs; b++) sc->bsdf_types |= 1 << d->bsdfs[b].type;
     *out = sc;
     return RT_OK;
 }
@@ -1230,6 +1312,7 @@ static rt_status ensure_wave(rt_ctx *c, int capacity, int max_rounds)
     ok &= alloc((void **)&W.q_active[1], P * sizeof(int));
     ok &= alloc((void **)&W.q_closest, P * sizeof(int));
     ok &= alloc((void **)&W.q_shadow, P * sizeof(int));
+    for (int t = 0; t < 4; t++) ok &= alloc((void **)&W.q_mat[t], P * sizeof(int));
     ok &= alloc((void **)&W.cnt, (size_t)(max_rounds + 2) * sizeof(RoundCounters));
     if (!ok) { free_wave(c); return fail(RT_ERR_NOMEM, "wavefront buffer allocation failed"); }
     W.capacity = capacity;
@@ -1383,9 +1466,13 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
                 else k_trace<true, false><<<trace_blocks, 128, 0, st>>>(P, ri);
                 prof_end(ctx);
                 prof_begin(ctx, K_SHADE);
-                k_pt_shade<<<shade_blocks, 128, 0, st>>>(P, ri);
+                k_pt_resolve<<<shade_blocks, 128, 0, st>>>(P, ri);
+                if (sc->bsdf_types & 1) k_pt_shade<0><<<shade_blocks, 128, 0, st>>>(P, ri);
+                if (sc->bsdf_types & 2) k_pt_shade<1><<<shade_blocks, 128, 0, st>>>(P, ri);
+                if (sc->bsdf_types & 4) k_pt_shade<2><<<shade_blocks, 128, 0, st>>>(P, ri);
+                if (sc->bsdf_types & 8) k_pt_shade<3><<<shade_blocks, 128, 0, st>>>(P, ri);
                 prof_end(ctx);
-                launches += 3;
+                launches += 3 + __builtin_popcount(sc->bsdf_types);
                 trace_c_launches++;
                 trace_a_launches++;
                 if ((s = launch_check("pt round")) != RT_OK) return s;

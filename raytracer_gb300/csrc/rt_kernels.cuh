@@ -11,7 +11,9 @@ namespace rtgpu {
 enum { F_FIRST = 1, F_DELTA = 2, F_NEE = 4, F_END = 8, F_DONE = 16 };
 
 struct RoundCounters {   // one per wavefront round, zeroed per batch
-    int active, closest, shadow, wc_closest, wc_shadow, pad0, pad1, pad2;
+    int active, closest, shadow, wc_closest, wc_shadow;
+    int mat[4];          // paths to shade per BSDF type (material-sorted queues)
+    int pad[7];
 };
 
 struct Wave {
@@ -34,6 +36,7 @@ struct Wave {
     // queues (ping-pong by round parity)
     int *q_active[2];
     int *q_closest, *q_shadow;
+    int *q_mat[4];     // per-BSDF-type shading queues
     RoundCounters *cnt;
     int capacity;
     int max_rounds;
