@@ -195,9 +195,11 @@ def run_gpu(args):
     ctx.set_profiling(2)
     scene.render(8, seed=99, film=film.data_ptr())
     cstats = ctx.stats()
+    pre_launches = cstats["launches"]
     ctx.set_profiling(1)
     for _ in range(args.warmup):
         scene.render(spp, seed=7, sample_begin=sbase, film=film.data_ptr())
+        pre_launches += ctx.stats()["launches"]
     barrier()
     clocks = ClockSampler(local)
     clocks.start()
@@ -305,7 +307,9 @@ def run_gpu(args):
                 "kernel_ms": {k: round(v / args.steps, 3) for k, v in kern.items()},
                 "traversal": {"nodes_per_closest_ray": nodes_pr_c, "tris_per_closest_ray": tris_pr_c,
                               "nodes_per_shadow_ray": nodes_pr_a, "tris_per_shadow_ray": tris_pr_a},
-                "gpu_launches": launches, "clocks": clk}
+                "gpu_launches": launches, "launches_before_timed": pre_launches,
+                "rays_per_step": {"closest": rays_c / args.steps, "shadow": rays_a / args.steps},
+                "clocks": clk}
         line.update(res)
         print(json.dumps(line))
     if world > 1:

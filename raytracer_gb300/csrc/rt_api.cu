@@ -138,31 +138,136 @@ __global__ void k_camera(RenderParams P)
 }
 
 // ---------------------------------------------------------------- traversal
-// Persistent kernel: warps fetch 32 queue entries at a time.  COUNT adds
-// BVH node / triangle-slot fetch counts to stats[3..6].
+// Persistent while-while traversal with per-lane dynamic ray fetch.  Lanes
+// that finish a ray fetch a new one as soon as enough lanes of the warp are
+// idle; inner nodes and leaves are processed in separate loops, and each
+// lane postpones the first leaf it reaches until every lane of the warp has
+// one, which keeps the warp converged.  COUNT adds BVH node / triangle-slot
+// fetch counts to stats[3..6].
+#define RT_SENT 0x76543210
+#define RT_FETCH_THRESHOLD 20
+
 template <bool ANY, bool COUNT>
 __global__ void __launch_bounds__(128) k_trace(RenderParams P, int round)
 {
+    const DevScene S = P.S;
     RoundCounters *C = &P.W.cnt[round];
     const int n = ANY ? C->shadow : C->closest;
     int *wc = ANY ? &C->wc_shadow : &C->wc_closest;
     const int *queue = ANY ? P.W.q_shadow : P.W.q_closest;
     const int lane = threadIdx.x & 31;
     int cnt[2] = {0, 0};
+
+    int stack[RT_STACK];
+    int sp = 0;
+    int node = RT_SENT, leaf = 0;
+    int slot = -1;
+    bool has_ray = false;
+    float ox = 0, oy = 0, oz = 0, dx = 0, dy = 0, dz = 0, idx = 0, idy = 0, idz = 0, oox = 0, ooy = 0, ooz = 0;
+    float tmin = 0, hit_t = 0, hu = 0, hv = 0;
+    int hprim = -1;
+
     for (;;) {
+        // ---- fetch rays for lanes whose ray is finished
+        const bool terminated = (node == RT_SENT);
+        const unsigned mterm = __ballot_sync(0xffffffffu, terminated);
+        const int nterm = __popc(mterm);
         int base = 0;
-        if (lane == 0) base = atomicAdd(wc, 32);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= n) break;
-        int i = base + lane;
-        if (i < n) {
-            int slot = queue[i];
-            float4 o = ANY ? P.W.sh_o[slot] : P.W.ray_o[slot];
-            float4 d = ANY ? P.W.sh_d[slot] : P.W.ray_d[slot];
-            Hit h;
-            bool hit = trace_ray<ANY, COUNT>(P.S, xyz(o), xyz(d), o.w, d.w, h, cnt);
-            if (ANY) P.W.occl[slot] = hit ? 1 : 0;
-            else P.W.hit[slot] = make_float4(h.t, h.u, h.v, __int_as_float(hit ? h.prim : -1));
+        if (nterm) {
+            const int leader = __ffs(mterm) - 1;
+            if (lane == leader) base = atomicAdd(wc, nterm);
+            base = __shfl_sync(0xffffffffu, base, leader);
+        }
+        if (terminated) {
+            int q = base + __popc(mterm & ((1u << lane) - 1));
+            has_ray = q < n;
+            if (has_ray) {
+                slot = queue[q];
+                float4 o4 = ANY ? P.W.sh_o[slot] : P.W.ray_o[slot];
+                float4 d4 = ANY ? P.W.sh_d[slot] : P.W.ray_d[slot];
+                ox = o4.x; oy = o4.y; oz = o4.z; dx = d4.x; dy = d4.y; dz = d4.z;
+                tmin = adapt_mint(v3(ox, oy, oz), o4.w);
+                hit_t = d4.w;
+                hprim = -1;
+                const float eps = 1e-20f;
+                idx = 1.0f / (fabsf(dx) > eps ? dx : copysignf(eps, dx));
+                idy = 1.0f / (fabsf(dy) > eps ? dy : copysignf(eps, dy));
+                idz = 1.0f / (fabsf(dz) > eps ? dz : copysignf(eps, dz));
+                oox = ox * idx; ooy = oy * idy; ooz = oz * idz;
+                sp = 0;
+                stack[sp++] = RT_SENT;
+                leaf = 0;
+                node = (S.n_nodes > 0 && !(hit_t < tmin)) ? 0 : RT_SENT;
+            }
+        }
+        if (!__any_sync(0xffffffffu, has_ray)) break;
+
+        // ---- traversal
+        while (node != RT_SENT) {
+            while ((unsigned)node < (unsigned)RT_SENT) {
+                if (COUNT) cnt[0]++;
+                const float4 *N = S.nodes + 4 * (size_t)node;
+                float4 n0 = __ldg(N), n1 = __ldg(N + 1), n2 = __ldg(N + 2);
+                int4 cc = __ldg(reinterpret_cast<const int4 *>(N + 3));
+                float c0lox = __fmaf_rn(n0.x, idx, -oox), c0hix = __fmaf_rn(n0.y, idx, -oox);
+                float c0loy = __fmaf_rn(n0.z, idy, -ooy), c0hiy = __fmaf_rn(n0.w, idy, -ooy);
+                float c0loz = __fmaf_rn(n2.x, idz, -ooz), c0hiz = __fmaf_rn(n2.y, idz, -ooz);
+                float c1lox = __fmaf_rn(n1.x, idx, -oox), c1hix = __fmaf_rn(n1.y, idx, -oox);
+                float c1loy = __fmaf_rn(n1.z, idy, -ooy), c1hiy = __fmaf_rn(n1.w, idy, -ooy);
+                float c1loz = __fmaf_rn(n2.z, idz, -ooz), c1hiz = __fmaf_rn(n2.w, idz, -ooz);
+                float c0min = rt_max4(fminf(c0lox, c0hix), fminf(c0loy, c0hiy), fminf(c0loz, c0hiz), tmin);
+                float c0max = rt_min4(fmaxf(c0lox, c0hix), fmaxf(c0loy, c0hiy), fmaxf(c0loz, c0hiz), hit_t);
+                float c1min = rt_max4(fminf(c1lox, c1hix), fminf(c1loy, c1hiy), fminf(c1loz, c1hiz), tmin);
+                float c1max = rt_min4(fmaxf(c1lox, c1hix), fmaxf(c1loy, c1hiy), fmaxf(c1loz, c1hiz), hit_t);
+                bool t0 = c0min <= c0max, t1 = c1min <= c1max;
+                if (!t0 && !t1) {
+                    node = stack[--sp];
+                } else {
+                    node = t0 ? cc.x : cc.y;
+                    if (t0 && t1) {
+                        int far = cc.y;
+                        if (c1min < c0min) { far = node; node = cc.y; }
+                        if (sp < RT_STACK) stack[sp++] = far;
+                    }
+                }
+                // first leaf found: postpone it and keep traversing
+                if (node < 0 && leaf >= 0) { leaf = node; node = stack[--sp]; }
+                if (!__any_sync(__activemask(), leaf >= 0)) break;
+            }
+            // ---- postponed leaves
+            while (leaf < 0) {
+                int v = ~leaf;
+                int first = v >> 3, cl = (v & 7) + 1;
+                for (int i = 0; i < cl; i++) {
+                    if (COUNT) cnt[1]++;
+                    const float4 *T = S.tri_slots + 3 * (size_t)(first + i);
+                    float4 a = __ldg(T), b = __ldg(T + 1), c = __ldg(T + 2);
+                    float t, u, w;
+                    if (mt_test(a, b, c, v3(ox, oy, oz), v3(dx, dy, dz), tmin, hit_t, t, u, w)) {
+                        hit_t = t; hu = u; hv = w; hprim = __float_as_int(a.w);
+                        if (ANY) { node = RT_SENT; break; }
+                    }
+                }
+                if (ANY && node == RT_SENT && hprim >= 0) { leaf = 0; break; }
+                leaf = node;
+                if (node < 0) node = stack[--sp];
+            }
+            if (__popc(__activemask()) < RT_FETCH_THRESHOLD) break;
+        }
+        // ---- finished rays: analytic spheres, then store
+        if (node == RT_SENT && has_ray) {
+            if (!(ANY && hprim >= 0)) {
+                for (int si = 0; si < S.n_spheres; si++) {
+                    float t;
+                    if (sphere_test(S.spheres[si], v3(ox, oy, oz), v3(dx, dy, dz), tmin, hit_t, t)) {
+                        hit_t = t; hu = 0.f; hv = 0.f; hprim = -si - 2;
+                        if (ANY) break;
+                    }
+                }
+            }
+            if (ANY) P.W.occl[slot] = hprim != -1 ? 1 : 0;
+            else P.W.hit[slot] = make_float4(hit_t, hu, hv, __int_as_float(hprim));
+            has_ray = false;
         }
     }
     if (COUNT) {
