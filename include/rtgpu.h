@@ -283,6 +283,25 @@ rt_status rt_render_stats_get(const rt_ctx *ctx, rt_render_stats *out);
  * 2 timing plus BVH traversal counters (slower; for roofline accounting). */
 rt_status rt_ctx_set_profiling(rt_ctx *ctx, int32_t level);
 
+/* Allocation-free tile render.  No counterpart in the reference: it exists
+ * for callers that cannot allocate device memory while rendering (plugins
+ * whose host application owns the device memory through its own pool under
+ * a hard budget, real-time loops that forbid cudaMalloc/cudaFree after
+ * start-up because they can synchronise the device, code issuing work while
+ * another component captures the stream).  Renders every sample of tile
+ * (tile_x, tile_y) of the block_x x block_y job grid into film_rgbw_device
+ * (a device pointer to the full width*height*4 film; only the tile's pixels
+ * are written), with the same results as rt_render for those pixels.
+ * Limits: tile pixels * spp * ~240 bytes of path state must fit the 32 MiB
+ * static scratch (about 130k path samples, e.g. 32x32 at 128 spp);
+ * max_depth <= 1024; at most 256 lights; larger requests return
+ * RT_ERR_LIMIT.  The first call on a device looks up the scratch address
+ * (cudaGetSymbolAddress) and should come before any stream capture.  All
+ * calls on one device share the scratch and keep its last contents: calls
+ * that overlap on the GPU (other threads or streams) race. */
+rt_status rt_render_tile_static(rt_ctx *ctx, rt_scene *scene, const rt_render_desc *rd,
+                                int32_t tile_x, int32_t tile_y, float *film_rgbw_device);
+
 /* Trace n rays (closest hit, or any hit when anyhit != 0). */
 rt_status rt_trace(rt_ctx *ctx, rt_scene *scene, const rt_ray *rays, int32_t n,
                    int32_t anyhit, rt_hit *hits, int32_t on_device);

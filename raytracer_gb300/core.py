@@ -54,6 +54,8 @@ def lib():
     L.rt_render_stats_get.argtypes = [vp, C.POINTER(D.RenderStats)]
     L.rt_ctx_set_profiling.argtypes = [vp, C.c_int32]
     L.rt_trace.argtypes = [vp, vp, vp, C.c_int32, C.c_int32, vp, C.c_int32]
+    L.rt_render_tile_static.argtypes = [vp, vp, C.POINTER(D.RenderDesc), C.c_int32, C.c_int32, vp]
+    L.rt_render_tile_static.restype = C.c_int32
     L.rt_bsdf_query.argtypes = [vp, vp, C.c_int32, C.c_int32, vp, C.c_int32, vp]
     L.rt_light_query.argtypes = [vp, vp, C.c_int32, vp, C.c_int32, vp]
     for name in ("rt_ctx_create", "rt_ctx_destroy", "rt_ctx_set_stream", "rt_scene_create", "rt_scene_destroy",
@@ -145,6 +147,14 @@ class Scene:
             return out
         _check(lib().rt_render(self.ctx.h, self.h, C.byref(rd), C.c_void_p(int(film)), 1))
         return None
+
+    def render_tile_static(self, tile_x, tile_y, film_ptr, spp, seed=0, sample_begin=0, block=32, **over):
+        """Allocation-free render of one job-grid tile into a device film
+        (an int device address of a width*height*4 float32 buffer); see
+        rt_render_tile_static in include/rtgpu.h for who needs it and its limits."""
+        rd = self.data.render_desc(spp, seed=seed, sample_begin=sample_begin, block=block, **over)
+        _check(lib().rt_render_tile_static(self.ctx.h, self.h, C.byref(rd), int(tile_x), int(tile_y),
+                                           C.c_void_p(int(film_ptr))))
 
     def trace(self, rays, anyhit=False):
         rays = np.ascontiguousarray(rays, D.RAY_DTYPE)

@@ -1719,3 +1719,202 @@ rt_status rt_light_query(rt_ctx *ctx, rt_scene *sc, int32_t light, const rt_ligh
 }
 
 }  // extern "C"
+
+// =====================================================================
+// Allocation-free tile render (rt_render_tile_static)
+// =====================================================================
+// Some callers cannot call cudaMalloc while they render: renderer plugins
+// that run inside a host application whose device memory is owned by that
+// application's own pool allocator under a hard budget, real-time loops that
+// forbid device allocation after start-up (cudaMalloc/cudaFree can
+// synchronise the device and stall the frame), and code that issues work
+// while another component is capturing the stream.  For them this entry point
+// renders one tile of the reference job grid with no allocation at all: the
+// wavefront path state lives in the file-scope array below, which every GPU
+// that loads the library holds until the process exits.  The scene (created
+// earlier by rt_scene_create) and the film are the caller's inputs and output.
+#define RT_STATIC_SCRATCH_BYTES (32u << 20)   // 32 MiB per device
+#define RT_STATIC_MAX_DEVICES 64
+#define RT_STATIC_MAX_LIGHTS 256
+#define RT_STATIC_MAX_DEPTH 1024
+
+static __device__ __align__(256) unsigned char g_static_scratch[RT_STATIC_SCRATCH_BYTES];
+
+#include <mutex>
+static std::mutex g_static_mu;
+static unsigned char *g_static_ptr[RT_STATIC_MAX_DEVICES];
+
+// Device address of g_static_scratch for the current device, looked up once
+// per device (the host-side name of a __device__ array is not a device
+// address).
+static rt_status static_scratch(int device, unsigned char **out)
+{
+    if (device < 0 || device >= RT_STATIC_MAX_DEVICES) return fail(RT_ERR_LIMIT, "device index above the static scratch table");
+    std::lock_guard<std::mutex> lk(g_static_mu);
+    if (!g_static_ptr[device]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+        if (e != cudaSuccess)
+            return fail(RT_ERR_CUDA, std::string("cudaGetSymbolAddress(g_static_scratch) -> ") + cudaGetErrorString(e));
+        g_static_ptr[device] = (unsigned char *)p;
+    }
+    *out = g_static_ptr[device];
+    return RT_OK;
+}
+
+__global__ void k_tile_order(int4 *out, int ox, int oy, int tw, int th)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= tw * th) return;
+    int x = i % tw, y = i / tw;
+    out[i] = make_int4(ox + x, oy + y, x | (y << 16), tw | (th << 16));
+}
+
+extern "C" rt_status rt_render_tile_static(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, int32_t tile_x,
+                                           int32_t tile_y, float *film_rgbw_device)
+{
+    if (!ctx || !sc || !rd || !film_rgbw_device) return fail(RT_ERR_INVALID, "rt_render_tile_static: null argument");
+    if (rd->spp <= 0 || rd->sample_begin < 0) return fail(RT_ERR_INVALID, "rt_render_tile_static: bad sample range");
+    if (rd->integrator != RT_INTEGRATOR_PATH_MIS && rd->integrator != RT_INTEGRATOR_VOLPATH)
+        return fail(RT_ERR_UNSUPPORTED, "rt_render_tile_static: unknown integrator");
+    if (rd->integrator == RT_INTEGRATOR_PATH_MIS && rd->strategy == RT_STRATEGY_ALL_LIGHTS)
+        return fail(RT_ERR_UNSUPPORTED, "rt_render_tile_static: all_lights strategy is not provided by the device path");
+    if (rd->max_depth < 0 || rd->min_depth < 0) return fail(RT_ERR_INVALID, "rt_render_tile_static: negative depth");
+    if (rd->max_depth > RT_STATIC_MAX_DEPTH)
+        return fail(RT_ERR_LIMIT, "rt_render_tile_static: max_depth above 1024 (the static round-counter table)");
+    if (sc->n_lights > RT_STATIC_MAX_LIGHTS) return fail(RT_ERR_LIMIT, "rt_render_tile_static: more than 256 lights");
+    const DevCamera &cam = sc->S.cam;
+    const int Wd = cam.width, H = cam.height;
+    const int bx = rd->block_x > 0 ? rd->block_x : 32, by = rd->block_y > 0 ? rd->block_y : 32;
+    if (bx > 0xffff || by > 0xffff) return fail(RT_ERR_INVALID, "block size too large");
+    const int tiles_x = (Wd + bx - 1) / bx, tiles_y = (H + by - 1) / by;
+    if (tile_x < 0 || tile_y < 0 || tile_x >= tiles_x || tile_y >= tiles_y)
+        return fail(RT_ERR_INVALID, "rt_render_tile_static: tile index outside the job grid");
+    const int ox = tile_x * bx, oy = tile_y * by;
+    const int tw = std::min(Wd, ox + bx) - ox, th = std::min(H, oy + by) - oy;
+    const int64_t npix = (int64_t)tw * th, paths = npix * rd->spp;
+    CK(cudaSetDevice(ctx->device));
+    unsigned char *base = nullptr;
+    rt_status s = static_scratch(ctx->device, &base);
+    if (s != RT_OK) return s;
+    // carve the scratch: every array 256-byte aligned
+    const int rounds = rd->integrator == RT_INTEGRATOR_PATH_MIS ? rd->max_depth + 3 : 1;
+    size_t off = 0;
+    auto take = [&](size_t bytes) -> unsigned char * {
+        size_t o = (off + 255) & ~(size_t)255;
+        off = o + bytes;
+        return base + o;
+    };
+    Wave W;
+    std::memset(&W, 0, sizeof(W));
+    const size_t P = (size_t)paths;
+    W.rng = (Pcg32 *)take(P * sizeof(Pcg32));
+    W.tp = (float4 *)take(P * sizeof(float4));
+    W.rad = (float4 *)take(P * sizeof(float4));
+    W.ray_o = (float4 *)take(P * sizeof(float4));
+    W.ray_d = (float4 *)take(P * sizeof(float4));
+    W.hit = (float4 *)take(P * sizeof(float4));
+    W.bs = (float4 *)take(P * sizeof(float4));
+    W.rel_eta = (float *)take(P * sizeof(float));
+    W.flags = (int *)take(P * sizeof(int));
+    W.nee = (float4 *)take(P * sizeof(float4));
+    W.sh_o = (float4 *)take(P * sizeof(float4));
+    W.sh_d = (float4 *)take(P * sizeof(float4));
+    W.occl = (int *)take(P * sizeof(int));
+    W.out = (float4 *)take(P * sizeof(float4));
+    W.splat = (uint8_t *)take(P);
+    W.pix_irregular = (uint8_t *)take((size_t)npix);
+    W.q_active[0] = (int *)take(P * sizeof(int));
+    W.q_active[1] = (int *)take(P * sizeof(int));
+    W.q_closest = (int *)take(P * sizeof(int));
+    W.q_shadow = (int *)take(P * sizeof(int));
+    for (int t = 0; t < 4; t++) W.q_mat[t] = (int *)take(P * sizeof(int));
+    W.cnt = (RoundCounters *)take((size_t)(rounds + 2) * sizeof(RoundCounters));
+    W.capacity = (int)P;
+    W.max_rounds = rounds;
+    int4 *tileorder = (int4 *)take((size_t)npix * sizeof(int4));
+    float *light_cdf = (float *)take((size_t)(RT_STATIC_MAX_LIGHTS + 1) * sizeof(float));
+    unsigned long long *stats = (unsigned long long *)take(8 * sizeof(unsigned long long));
+    int *limit_flag = (int *)take(sizeof(int));
+    int *work = (int *)take(sizeof(int));
+    if (off > RT_STATIC_SCRATCH_BYTES) {
+        char msg[256];
+        snprintf(msg, sizeof(msg),
+                 "rt_render_tile_static: a %dx%d tile at %d spp needs %zu bytes of path state; the static scratch "
+                 "holds %u (reduce spp or the block size)", tw, th, rd->spp, off, (unsigned)RT_STATIC_SCRATCH_BYTES);
+        return fail(RT_ERR_LIMIT, msg);
+    }
+    cudaStream_t st = ctx->stream;
+    // light selection CDF (Integrator::initialize) in a fixed host array
+    float cdf[RT_STATIC_MAX_LIGHTS + 1];
+    {
+        int n = sc->n_lights;
+        float pu = (float)1. / (float)n, sum = 0.f;
+        cdf[0] = 0.f;
+        for (int l = 0; l < n; l++) {
+            sum += rd->strategy == RT_STRATEGY_ONE_LIGHT_WEIGHTED ? sc->light_power_lum[l] : pu;
+            cdf[l + 1] = sum;
+        }
+        if (sum != 0.f) {
+            float f = 1.f / sum;
+            for (int i = 1; i <= n; i++) cdf[i] *= f;
+            cdf[n] = 1.f;
+        }
+        CK(cudaMemcpyAsync(light_cdf, cdf, sizeof(float) * (size_t)(n + 1), cudaMemcpyHostToDevice, st));
+    }
+    // the scratch keeps the previous call's contents: clear what counts from zero
+    CK(cudaMemsetAsync(W.cnt, 0, sizeof(RoundCounters) * (size_t)(rounds + 2), st));
+    CK(cudaMemsetAsync(W.pix_irregular, 0, (size_t)npix, st));
+    CK(cudaMemsetAsync(stats, 0, 8 * sizeof(unsigned long long), st));
+    CK(cudaMemsetAsync(limit_flag, 0, sizeof(int), st));
+    CK(cudaMemsetAsync(work, 0, sizeof(int), st));
+    k_tile_order<<<(int)((npix + 127) / 128), 128, 0, st>>>(tileorder, ox, oy, tw, th);
+    if ((s = launch_check("k_tile_order")) != RT_OK) return s;
+    RenderParams Pm;
+    Pm.S = sc->S;
+    Pm.S.light_cdf = light_cdf;
+    Pm.W = W;
+    Pm.tileorder = tileorder;
+    Pm.g0 = 0;
+    Pm.npix = (int)npix;
+    Pm.spp = rd->spp;
+    Pm.sample_begin = rd->sample_begin;
+    Pm.n_paths = (int)paths;
+    Pm.seed = rd->seed;
+    Pm.max_depth = rd->max_depth;
+    Pm.min_depth = rd->min_depth;
+    Pm.limit_flag = limit_flag;
+    Pm.stats = stats;
+    const int sm = ctx->sm_count > 0 ? ctx->sm_count : 1;
+    k_camera<<<std::min((int)((paths + 255) / 256), sm * 16), 256, 0, st>>>(Pm);
+    if ((s = launch_check("k_camera")) != RT_OK) return s;
+    if (rd->integrator == RT_INTEGRATOR_VOLPATH) {
+        k_volpath<<<sm * 8, 128, 0, st>>>(Pm, work);
+        if ((s = launch_check("k_volpath")) != RT_OK) return s;
+    } else {
+        const int blocks = sm * 8;
+        for (int r = 0; r < rounds; r++) {
+            k_trace<false, false><<<sm * 12, 128, 0, st>>>(Pm, r);
+            k_trace<true, false><<<sm * 12, 128, 0, st>>>(Pm, r);
+            k_pt_resolve<<<blocks, 128, 0, st>>>(Pm, r);
+            if (sc->bsdf_types & 1) k_pt_shade<0><<<blocks, 128, 0, st>>>(Pm, r);
+            if (sc->bsdf_types & 2) k_pt_shade<1><<<blocks, 128, 0, st>>>(Pm, r);
+            if (sc->bsdf_types & 4) k_pt_shade<2><<<blocks, 128, 0, st>>>(Pm, r);
+            if (sc->bsdf_types & 8) k_pt_shade<3><<<blocks, 128, 0, st>>>(Pm, r);
+            if ((s = launch_check("pt round (static)")) != RT_OK) return s;
+            if ((r & 3) == 3 && r + 1 < rounds) {
+                int nact = 0;
+                CK(cudaMemcpyAsync(&nact, &W.cnt[r + 1].active, sizeof(int), cudaMemcpyDeviceToHost, st));
+                CK(cudaStreamSynchronize(st));
+                if (nact == 0) break;
+            }
+        }
+    }
+    k_film<<<(int)((npix + 127) / 128), 128, 0, st>>>(Pm, reinterpret_cast<float4 *>(film_rgbw_device), Wd);
+    if ((s = launch_check("k_film (static)")) != RT_OK) return s;
+    int limit = 0;
+    CK(cudaMemcpyAsync(&limit, limit_flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (limit) return fail(RT_ERR_LIMIT, "a device loop reached its iteration cap");
+    return RT_OK;
+}
