@@ -282,6 +282,10 @@ rt_status rt_render_stats_get(const rt_ctx *ctx, rt_render_stats *out);
 /* Profiling level of later renders: 0 off, 1 per-kernel CUDA-event timing,
  * 2 timing plus BVH traversal counters (slower; for roofline accounting). */
 rt_status rt_ctx_set_profiling(rt_ctx *ctx, int32_t level);
+/* Tree used by later renders and rt_trace: 2 (binary BVH, the default) or 8
+ * (compressed 8-wide BVH); both report the same closest hits (a tie at equal
+ * distance may name another triangle) and the same occlusion. */
+rt_status rt_ctx_set_bvh_width(rt_ctx *ctx, int32_t width);
 
 /* Allocation-free tile render.  No counterpart in the reference: it exists
  * for callers that cannot allocate device memory while rendering (plugins

@@ -54,6 +54,8 @@ def build(force=False, verbose=False, ptxas_info=False):
                    "-I", os.path.join(ROOT, "include"), "-c", src, "-o", obj]
             if ptxas_info:
                 cmd.insert(1, "-Xptxas=-v")
+            extra = os.environ.get("RTGPU_NVCC_FLAGS", "").split()
+            cmd[1:1] = extra
             jobs.append(cmd)
     for s in HOST_SOURCES:
         src = os.path.join(CSRC, s)

@@ -53,13 +53,14 @@ def lib():
     L.rt_render.argtypes = [vp, vp, C.POINTER(D.RenderDesc), vp, C.c_int32]
     L.rt_render_stats_get.argtypes = [vp, C.POINTER(D.RenderStats)]
     L.rt_ctx_set_profiling.argtypes = [vp, C.c_int32]
+    L.rt_ctx_set_bvh_width.argtypes = [vp, C.c_int32]
     L.rt_trace.argtypes = [vp, vp, vp, C.c_int32, C.c_int32, vp, C.c_int32]
     L.rt_render_tile_static.argtypes = [vp, vp, C.POINTER(D.RenderDesc), C.c_int32, C.c_int32, vp]
     L.rt_render_tile_static.restype = C.c_int32
     L.rt_bsdf_query.argtypes = [vp, vp, C.c_int32, C.c_int32, vp, C.c_int32, vp]
     L.rt_light_query.argtypes = [vp, vp, C.c_int32, vp, C.c_int32, vp]
     for name in ("rt_ctx_create", "rt_ctx_destroy", "rt_ctx_set_stream", "rt_scene_create", "rt_scene_destroy",
-                 "rt_scene_info", "rt_render", "rt_render_stats_get", "rt_ctx_set_profiling", "rt_trace", "rt_bsdf_query", "rt_light_query"):
+                 "rt_scene_info", "rt_render", "rt_render_stats_get", "rt_ctx_set_profiling", "rt_ctx_set_bvh_width", "rt_trace", "rt_bsdf_query", "rt_light_query"):
         getattr(L, name).restype = C.c_int32
     _lib = L
     return L
@@ -99,6 +100,10 @@ class Context:
     def set_profiling(self, level):
         """0 off, 1 per-kernel event timing, 2 timing + traversal counters."""
         _check(lib().rt_ctx_set_profiling(self.h, int(level)))
+
+    def set_bvh_width(self, width):
+        """Traversal tree for later renders and traces: 2 (default) or 8."""
+        _check(lib().rt_ctx_set_bvh_width(self.h, int(width)))
 
     def stats(self):
         s = D.RenderStats()

@@ -148,7 +148,7 @@ __global__ void k_camera(RenderParams P)
 #define RT_FETCH_THRESHOLD 20
 
 template <bool ANY, bool COUNT>
-__global__ void __launch_bounds__(128) k_trace(RenderParams P, int round)
+__global__ void __launch_bounds__(128, 10) k_trace(RenderParams P, int round)
 {
     const DevScene S = P.S;
     RoundCounters *C = &P.W.cnt[round];
@@ -165,6 +165,7 @@ __global__ void __launch_bounds__(128) k_trace(RenderParams P, int round)
     bool has_ray = false;
     float ox = 0, oy = 0, oz = 0, dx = 0, dy = 0, dz = 0, idx = 0, idy = 0, idz = 0, oox = 0, ooy = 0, ooz = 0;
     float tmin = 0, hit_t = 0, hu = 0, hv = 0;
+    float lx = 0, hx = 0, ly = 0, hy = 0, lz = 0, hz = 0;   // guarded plane offsets (slab_guard)
     int hprim = -1;
 
     for (;;) {
@@ -194,6 +195,9 @@ __global__ void __launch_bounds__(128) k_trace(RenderParams P, int round)
                 idy = 1.0f / (fabsf(dy) > eps ? dy : copysignf(eps, dy));
                 idz = 1.0f / (fabsf(dz) > eps ? dz : copysignf(eps, dz));
                 oox = ox * idx; ooy = oy * idy; ooz = oz * idz;
+                lx = -(oox + copysignf(slab_guard(oox), idx)); hx = -(oox - copysignf(slab_guard(oox), idx));
+                ly = -(ooy + copysignf(slab_guard(ooy), idy)); hy = -(ooy - copysignf(slab_guard(ooy), idy));
+                lz = -(ooz + copysignf(slab_guard(ooz), idz)); hz = -(ooz - copysignf(slab_guard(ooz), idz));
                 sp = 0;
                 stack[sp++] = RT_SENT;
                 leaf = 0;
@@ -209,12 +213,12 @@ __global__ void __launch_bounds__(128) k_trace(RenderParams P, int round)
                 const float4 *N = S.nodes + 4 * (size_t)node;
                 float4 n0 = __ldg(N), n1 = __ldg(N + 1), n2 = __ldg(N + 2);
                 int4 cc = __ldg(reinterpret_cast<const int4 *>(N + 3));
-                float c0lox = __fmaf_rn(n0.x, idx, -oox), c0hix = __fmaf_rn(n0.y, idx, -oox);
-                float c0loy = __fmaf_rn(n0.z, idy, -ooy), c0hiy = __fmaf_rn(n0.w, idy, -ooy);
-                float c0loz = __fmaf_rn(n2.x, idz, -ooz), c0hiz = __fmaf_rn(n2.y, idz, -ooz);
-                float c1lox = __fmaf_rn(n1.x, idx, -oox), c1hix = __fmaf_rn(n1.y, idx, -oox);
-                float c1loy = __fmaf_rn(n1.z, idy, -ooy), c1hiy = __fmaf_rn(n1.w, idy, -ooy);
-                float c1loz = __fmaf_rn(n2.z, idz, -ooz), c1hiz = __fmaf_rn(n2.w, idz, -ooz);
+                float c0lox = __fmaf_rn(n0.x, idx, lx), c0hix = __fmaf_rn(n0.y, idx, hx);
+                float c0loy = __fmaf_rn(n0.z, idy, ly), c0hiy = __fmaf_rn(n0.w, idy, hy);
+                float c0loz = __fmaf_rn(n2.x, idz, lz), c0hiz = __fmaf_rn(n2.y, idz, hz);
+                float c1lox = __fmaf_rn(n1.x, idx, lx), c1hix = __fmaf_rn(n1.y, idx, hx);
+                float c1loy = __fmaf_rn(n1.z, idy, ly), c1hiy = __fmaf_rn(n1.w, idy, hy);
+                float c1loz = __fmaf_rn(n2.z, idz, lz), c1hiz = __fmaf_rn(n2.w, idz, hz);
                 float c0min = rt_max4(fminf(c0lox, c0hix), fminf(c0loy, c0hiy), fminf(c0loz, c0hiz), tmin);
                 float c0max = rt_min4(fmaxf(c0lox, c0hix), fmaxf(c0loy, c0hiy), fmaxf(c0loz, c0hiz), hit_t);
                 float c1min = rt_max4(fminf(c1lox, c1hix), fminf(c1loy, c1hiy), fminf(c1loz, c1hiz), tmin);
@@ -281,6 +285,241 @@ __global__ void __launch_bounds__(128) k_trace(RenderParams P, int round)
         }
     }
     if (threadIdx.x == 0 && blockIdx.x == 0) atomicAdd(&P.stats[ANY ? 1 : 0], (unsigned long long)n);
+}
+
+// ---------------------------------------------------------------- 8-wide traversal
+// Persistent traversal of the compressed 8-wide BVH with node groups: one
+// node visit tests its (up to) eight quantised child boxes and keeps the hit
+// children as an 8-bit mask in the ray's octant order (bit k <-> slot
+// k ^ octant, the build places children so that this order is roughly front
+// to back).  The lane walks the group; when it descends into an internal
+// child, the rest of the group is pushed as one stack entry
+// (node << 8 | mask), so the stack grows by at most one entry per level.
+// Node phase and leaf phase alternate warp-wide (while-while), and lanes
+// whose ray finished take a new ray from the queue as in k_trace.
+#define RT_WSTACK 32
+
+// byte j of w as an exact float: the byte is placed in the mantissa of 2^23
+// (one byte permute) and 2^23 subtracted, avoiding an integer conversion
+__device__ __forceinline__ float byte_f(unsigned w, int j)
+{
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u | (unsigned)j)) - 8388608.0f;
+}
+
+__device__ __forceinline__ unsigned meta_byte(int4 w1, unsigned slot)
+{
+    unsigned w = slot < 4 ? (unsigned)w1.z : (unsigned)w1.w;
+    return (w >> (8 * (slot & 3))) & 0xffu;
+}
+
+template <bool ANY, bool COUNT>
+__global__ void __launch_bounds__(128, 8) k_trace8(RenderParams P, int round)
+{
+    const DevScene S = P.S;
+    RoundCounters *C = &P.W.cnt[round];
+    const int n = ANY ? C->shadow : C->closest;
+    int *wc = ANY ? &C->wc_shadow : &C->wc_closest;
+    const int *queue = ANY ? P.W.q_shadow : P.W.q_closest;
+    const int lane = threadIdx.x & 31;
+    int cnt[2] = {0, 0};
+
+    int stack[RT_WSTACK];
+    int sp = 0;
+    int gnode = 0, vnode = -1;      // current group's node; node to visit next (-1 none)
+    unsigned gmask = 0, oct = 0;    // remaining hit children (octant order); ray octant
+    int4 g1 = make_int4(0, 0, 0, 0);
+    bool trav = false;              // a ray is being traversed
+    int slot = -1;
+    float ox = 0, oy = 0, oz = 0, dx = 0, dy = 0, dz = 0, idx = 0, idy = 0, idz = 0;
+    float tmin = 0, hit_t = 0, hu = 0, hv = 0;
+    float nx_ = 0, fx_ = 0, ny_ = 0, fy_ = 0, nz_ = 0, fz_ = 0;   // near / far plane offsets (slab_guard)
+    int hprim = -1;
+    bool negx = false, negy = false, negz = false;
+
+    for (;;) {
+        // ---- fetch rays for lanes whose ray is finished
+        const bool idle = !trav;
+        const unsigned midle = __ballot_sync(0xffffffffu, idle);
+        const int nidle = __popc(midle);
+        int base = 0;
+        bool has_ray = trav;
+        if (nidle) {
+            const int leader = __ffs(midle) - 1;
+            if (lane == leader) base = atomicAdd(wc, nidle);
+            base = __shfl_sync(0xffffffffu, base, leader);
+        }
+        if (idle) {
+            int q = base + __popc(midle & ((1u << lane) - 1));
+            has_ray = q < n;
+            if (has_ray) {
+                slot = queue[q];
+                float4 o4 = ANY ? P.W.sh_o[slot] : P.W.ray_o[slot];
+                float4 d4 = ANY ? P.W.sh_d[slot] : P.W.ray_d[slot];
+                ox = o4.x; oy = o4.y; oz = o4.z; dx = d4.x; dy = d4.y; dz = d4.z;
+                tmin = adapt_mint(v3(ox, oy, oz), o4.w);
+                hit_t = d4.w;
+                hprim = -1;
+                const float eps = 1e-20f;
+                idx = 1.0f / (fabsf(dx) > eps ? dx : copysignf(eps, dx));
+                idy = 1.0f / (fabsf(dy) > eps ? dy : copysignf(eps, dy));
+                idz = 1.0f / (fabsf(dz) > eps ? dz : copysignf(eps, dz));
+                const float oox = ox * idx, ooy = oy * idy, ooz = oz * idz;
+                nx_ = -(oox + slab_guard(oox)); fx_ = -(oox - slab_guard(oox));
+                ny_ = -(ooy + slab_guard(ooy)); fy_ = -(ooy - slab_guard(ooy));
+                nz_ = -(ooz + slab_guard(ooz)); fz_ = -(ooz - slab_guard(ooz));
+                negx = idx < 0.f; negy = idy < 0.f; negz = idz < 0.f;
+                oct = (negx ? 1u : 0u) | (negy ? 2u : 0u) | (negz ? 4u : 0u);
+                sp = 0;
+                gmask = 0;
+                vnode = (S.n_wnodes > 0 && !(hit_t < tmin)) ? 0 : -1;
+                trav = true;
+            }
+        }
+        if (!__any_sync(0xffffffffu, has_ray)) break;
+
+        while (trav) {
+            // ---- node phase: visit internal nodes until the next item is a leaf
+            for (;;) {
+                if (vnode < 0) {
+                    if (gmask == 0) {
+                        if (sp == 0) { trav = false; break; }
+                        const int e = stack[--sp];
+                        gnode = e >> 8;
+                        gmask = (unsigned)e & 0xffu;
+                        g1 = __ldg(reinterpret_cast<const int4 *>(S.wnodes + 5 * (size_t)gnode + 1));
+                    }
+                    const unsigned m = meta_byte(g1, (unsigned)(__ffs(gmask) - 1) ^ oct);
+                    if ((m >> 5) != 7u) break;             // a leaf comes next
+                    gmask &= gmask - 1;
+                    if (gmask && sp < RT_WSTACK) stack[sp++] = (gnode << 8) | (int)gmask;
+                    vnode = g1.x + (int)(m & 31u);
+                }
+                if (COUNT) cnt[0]++;
+                const float4 *N = S.wnodes + 5 * (size_t)vnode;
+                float4 w0 = __ldg(N);
+                int4 w1 = __ldg(reinterpret_cast<const int4 *>(N + 1));
+                uint4 w2 = __ldg(reinterpret_cast<const uint4 *>(N + 2));
+                uint4 w3 = __ldg(reinterpret_cast<const uint4 *>(N + 3));
+                uint4 w4 = __ldg(reinterpret_cast<const uint4 *>(N + 4));
+                unsigned eb = __float_as_uint(w0.w);
+                float sx = __uint_as_float((eb & 0xffu) << 23);
+                float sy = __uint_as_float(((eb >> 8) & 0xffu) << 23);
+                float sz = __uint_as_float(((eb >> 16) & 0xffu) << 23);
+                float anx = __fmaf_rn(w0.x, idx, nx_), any_ = __fmaf_rn(w0.y, idy, ny_), anz = __fmaf_rn(w0.z, idz, nz_);
+                float afx = __fmaf_rn(w0.x, idx, fx_), afy = __fmaf_rn(w0.y, idy, fy_), afz = __fmaf_rn(w0.z, idz, fz_);
+                float kx = sx * idx, ky = sy * idy, kz = sz * idz;
+                // near/far planes per axis from the direction signs
+                uint2 qxn = negx ? make_uint2(w3.z, w3.w) : make_uint2(w2.x, w2.y);
+                uint2 qxf = negx ? make_uint2(w2.x, w2.y) : make_uint2(w3.z, w3.w);
+                uint2 qyn = negy ? make_uint2(w4.x, w4.y) : make_uint2(w2.z, w2.w);
+                uint2 qyf = negy ? make_uint2(w2.z, w2.w) : make_uint2(w4.x, w4.y);
+                uint2 qzn = negz ? make_uint2(w4.z, w4.w) : make_uint2(w3.x, w3.y);
+                uint2 qzf = negz ? make_uint2(w3.x, w3.y) : make_uint2(w4.z, w4.w);
+                unsigned hm = 0;
+#pragma unroll
+                for (int i = 0; i < 8; i++) {
+                    unsigned wxn = i < 4 ? qxn.x : qxn.y, wxf = i < 4 ? qxf.x : qxf.y;
+                    unsigned wyn = i < 4 ? qyn.x : qyn.y, wyf = i < 4 ? qyf.x : qyf.y;
+                    unsigned wzn = i < 4 ? qzn.x : qzn.y, wzf = i < 4 ? qzf.x : qzf.y;
+                    float tnx = __fmaf_rn(byte_f(wxn, i & 3), kx, anx), tfx = __fmaf_rn(byte_f(wxf, i & 3), kx, afx);
+                    float tny = __fmaf_rn(byte_f(wyn, i & 3), ky, any_), tfy = __fmaf_rn(byte_f(wyf, i & 3), ky, afy);
+                    float tnz = __fmaf_rn(byte_f(wzn, i & 3), kz, anz), tfz = __fmaf_rn(byte_f(wzf, i & 3), kz, afz);
+                    float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
+                    float tf = fminf(fminf(tfx, tfy), fminf(tfz, hit_t));
+                    if (tn <= tf) hm |= 1u << i;
+                }
+                // empty slots hold an inverted box (lo 255, hi 0) and meta 0, a
+                // leaf of no triangles, should a degenerate node still report them
+                // slot order -> octant order: bit k <- bit k ^ oct
+                if (oct & 1u) hm = ((hm & 0x55u) << 1) | ((hm >> 1) & 0x55u);
+                if (oct & 2u) hm = ((hm & 0x33u) << 2) | ((hm >> 2) & 0x33u);
+                if (oct & 4u) hm = ((hm & 0x0fu) << 4) | ((hm >> 4) & 0x0fu);
+                gnode = vnode;
+                gmask = hm;
+                g1 = w1;
+                vnode = -1;
+            }
+            // ---- leaf phase: test the leaves at the front of the group
+            while (trav && gmask) {
+                const unsigned m = meta_byte(g1, (unsigned)(__ffs(gmask) - 1) ^ oct);
+                if ((m >> 5) == 7u) break;
+                gmask &= gmask - 1;
+                const int first = g1.y + (int)(m & 31u), cl = (int)(m >> 5);
+                bool done = false;
+                for (int i = 0; i < cl; i++) {
+                    if (COUNT) cnt[1]++;
+                    const float4 *T = S.wtri + 3 * (size_t)(first + i);
+                    float4 a = __ldg(T), b = __ldg(T + 1), c = __ldg(T + 2);
+                    float t, u, w;
+                    if (mt_test(a, b, c, v3(ox, oy, oz), v3(dx, dy, dz), tmin, hit_t, t, u, w)) {
+                        hit_t = t; hu = u; hv = w; hprim = __float_as_int(a.w);
+                        if (ANY) { done = true; break; }
+                    }
+                }
+                if (done) { gmask = 0; sp = 0; vnode = -1; trav = false; }
+            }
+            if (__popc(__activemask()) < RT_FETCH_THRESHOLD) break;
+        }
+        if (!trav && has_ray) {
+            if (!(ANY && hprim >= 0)) {
+                for (int si = 0; si < S.n_spheres; si++) {
+                    float t;
+                    if (sphere_test(S.spheres[si], v3(ox, oy, oz), v3(dx, dy, dz), tmin, hit_t, t)) {
+                        hit_t = t; hu = 0.f; hv = 0.f; hprim = -si - 2;
+                        if (ANY) break;
+                    }
+                }
+            }
+            if (ANY) P.W.occl[slot] = hprim != -1 ? 1 : 0;
+            else P.W.hit[slot] = make_float4(hit_t, hu, hv, __int_as_float(hprim));
+            has_ray = false;
+        }
+    }
+    if (COUNT) {
+        for (int off = 16; off > 0; off >>= 1) {
+            cnt[0] += __shfl_down_sync(0xffffffffu, cnt[0], off);
+            cnt[1] += __shfl_down_sync(0xffffffffu, cnt[1], off);
+        }
+        if (lane == 0) {
+            atomicAdd(&P.stats[ANY ? 5 : 3], (unsigned long long)cnt[0]);
+            atomicAdd(&P.stats[ANY ? 6 : 4], (unsigned long long)cnt[1]);
+        }
+    }
+    if (threadIdx.x == 0 && blockIdx.x == 0) atomicAdd(&P.stats[ANY ? 1 : 0], (unsigned long long)n);
+}
+
+// rays of the rt_trace test hook into the wavefront buffers, and back
+__global__ void k_rays_in(const rt_ray *rays, int n, RenderParams P, int anyhit)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    rt_ray r = rays[i];
+    float4 o = make_float4(r.o[0], r.o[1], r.o[2], r.mint), d = make_float4(r.d[0], r.d[1], r.d[2], r.maxt);
+    if (anyhit) { P.W.sh_o[i] = o; P.W.sh_d[i] = d; P.W.q_shadow[i] = i; }
+    else { P.W.ray_o[i] = o; P.W.ray_d[i] = d; P.W.q_closest[i] = i; }
+    if (i == 0) {
+        P.W.cnt[0].closest = anyhit ? 0 : n;
+        P.W.cnt[0].shadow = anyhit ? n : 0;
+        P.W.cnt[0].wc_closest = 0;
+        P.W.cnt[0].wc_shadow = 0;
+    }
+}
+__global__ void k_hits_out(RenderParams P, int n, int anyhit, rt_hit *hits)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    rt_hit h;
+    if (anyhit) {
+        h.t = 0.f; h.u = 0.f; h.v = 0.f; h.prim = P.W.occl[i] ? 0 : -1;
+    } else {
+        float4 v = P.W.hit[i];
+        int prim = __float_as_int(v.w);
+        h.prim = prim;
+        h.t = prim != -1 ? v.x : 0.f;
+        h.u = prim != -1 ? v.y : 0.f;
+        h.v = prim != -1 ? v.z : 0.f;
+    }
+    hits[i] = h;
 }
 
 // ---------------------------------------------------------------- PathTracingMIS vertex
@@ -863,6 +1102,7 @@ struct rt_ctx {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     rt_render_stats last;
     int profiling = 0;
+    int bvh_width = 2;          // traversal used by renders and rt_trace: 2 or 8
     std::vector<cudaEvent_t> ev_pool;
     std::vector<int> ev_kind;   // kernel kind per recorded pair
     size_t ev_used = 0;
@@ -902,6 +1142,8 @@ struct rt_scene {
     int n_lights = 0;
     int n_bsdfs = 0;
     int bsdf_types = 0;   // bit t set when some BSDF of type t exists
+    int wide_depth = 0;
+    bool wide_ok = false;  // the 8-wide BVH is uploaded (or the scene has no triangles)
     std::vector<float> light_power_lum;  // per light, for the weighted strategy
     std::vector<DevLight> lights_host;
     DevLight *lights_dev = nullptr;
@@ -1081,6 +1323,14 @@ rt_status rt_ctx_set_profiling(rt_ctx *c, int32_t level)
     if (!c) return fail(RT_ERR_INVALID, "null ctx");
     if (level < 0 || level > 2) return fail(RT_ERR_INVALID, "profiling level must be 0, 1 or 2");
     c->profiling = level;
+    return RT_OK;
+}
+
+rt_status rt_ctx_set_bvh_width(rt_ctx *c, int32_t width)
+{
+    if (!c) return fail(RT_ERR_INVALID, "null ctx");
+    if (width != 2 && width != 8) return fail(RT_ERR_INVALID, "BVH width must be 2 or 8");
+    c->bvh_width = width;
     return RT_OK;
 }
 
@@ -1334,6 +1584,19 @@ rt_status rt_scene_create(rt_ctx *ctx, const rt_scene_desc *d, rt_scene **out)
     if ((st = upload(sc, reinterpret_cast<const float4 *>(img.nodes.data()), (size_t)img.n_nodes * 4, &np)) != RT_OK) { rt_scene_destroy(sc); return st; }
     if ((st = upload(sc, reinterpret_cast<const float4 *>(img.tri_slots.data()), (size_t)img.n_slots * 3, &tp)) != RT_OK) { rt_scene_destroy(sc); return st; }
     S.nodes = np; S.tri_slots = tp; S.n_nodes = img.n_nodes;
+    {
+        WideBvhImage wimg;
+        build_wbvh8(tri_v.data(), nt, wimg, 32);
+        // the group stack holds one entry per level and node indices < 2^23;
+        // a tree outside either limit is not uploaded and renders use the BVH2
+        if (nt > 0 && (wimg.max_depth + 1 > RT_WSTACK || wimg.n_nodes >= (1 << 23))) wimg = WideBvhImage();
+        const float4 *wn = nullptr, *wt = nullptr;
+        if ((st = upload(sc, reinterpret_cast<const float4 *>(wimg.nodes.data()), (size_t)(nt > 0 ? wimg.n_nodes : 0) * 5, &wn)) != RT_OK) { rt_scene_destroy(sc); return st; }
+        if ((st = upload(sc, reinterpret_cast<const float4 *>(wimg.tri_slots.data()), (size_t)wimg.n_slots * 3, &wt)) != RT_OK) { rt_scene_destroy(sc); return st; }
+        S.wnodes = wn; S.wtri = wt; S.n_wnodes = nt > 0 ? wimg.n_nodes : 0;
+        sc->wide_depth = wimg.max_depth;
+        sc->wide_ok = nt == 0 || wimg.n_nodes > 0;
+    }
     const float *fp;
     const int *ip;
     if ((st = upload(sc, tri_v.data(), tri_v.size(), &fp)) != RT_OK) { rt_scene_destroy(sc); return st; }
@@ -1562,13 +1825,24 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
             int shade_blocks = sm * 8;
             for (int r = 0; r < max_rounds; r++) {
                 int ri = r;
+                const bool cnt2 = ctx->profiling >= 2, w8 = ctx->bvh_width == 8 && sc->wide_ok;
                 prof_begin(ctx, K_TRACE_C);
-                if (ctx->profiling >= 2) k_trace<false, true><<<trace_blocks, 128, 0, st>>>(P, ri);
-                else k_trace<false, false><<<trace_blocks, 128, 0, st>>>(P, ri);
+                if (w8) {
+                    if (cnt2) k_trace8<false, true><<<trace_blocks, 128, 0, st>>>(P, ri);
+                    else k_trace8<false, false><<<trace_blocks, 128, 0, st>>>(P, ri);
+                } else {
+                    if (cnt2) k_trace<false, true><<<trace_blocks, 128, 0, st>>>(P, ri);
+                    else k_trace<false, false><<<trace_blocks, 128, 0, st>>>(P, ri);
+                }
                 prof_end(ctx);
                 prof_begin(ctx, K_TRACE_A);
-                if (ctx->profiling >= 2) k_trace<true, true><<<trace_blocks, 128, 0, st>>>(P, ri);
-                else k_trace<true, false><<<trace_blocks, 128, 0, st>>>(P, ri);
+                if (w8) {
+                    if (cnt2) k_trace8<true, true><<<trace_blocks, 128, 0, st>>>(P, ri);
+                    else k_trace8<true, false><<<trace_blocks, 128, 0, st>>>(P, ri);
+                } else {
+                    if (cnt2) k_trace<true, true><<<trace_blocks, 128, 0, st>>>(P, ri);
+                    else k_trace<true, false><<<trace_blocks, 128, 0, st>>>(P, ri);
+                }
                 prof_end(ctx);
                 prof_begin(ctx, K_SHADE);
                 k_pt_resolve<<<shade_blocks, 128, 0, st>>>(P, ri);
@@ -1650,6 +1924,9 @@ rt_status rt_trace(rt_ctx *ctx, rt_scene *sc, const rt_ray *rays, int32_t n, int
     if (n == 0) return RT_OK;
     CK(cudaSetDevice(ctx->device));
     cudaStream_t st = ctx->stream;
+    // the rays go through the same persistent traversal kernels a render uses
+    rt_status s = ensure_wave(ctx, n, std::max(1, ctx->W.max_rounds));
+    if (s != RT_OK) return s;
     const rt_ray *dr = rays;
     rt_hit *dh = hits;
     void *tmp_r = nullptr, *tmp_h = nullptr;
@@ -1660,8 +1937,23 @@ rt_status rt_trace(rt_ctx *ctx, rt_scene *sc, const rt_ray *rays, int32_t n, int
         dr = (const rt_ray *)tmp_r;
         dh = (rt_hit *)tmp_h;
     }
-    k_trace_rays<<<(n + 127) / 128, 128, 0, st>>>(sc->S, dr, n, anyhit, dh);
-    rt_status s = launch_check("k_trace_rays");
+    RenderParams P;
+    std::memset(&P, 0, sizeof(P));
+    P.S = sc->S;
+    P.W = ctx->W;
+    P.stats = ctx->stats;
+    P.limit_flag = ctx->limit_flag;
+    const int sm = ctx->sm_count > 0 ? ctx->sm_count : 1;
+    k_rays_in<<<(n + 127) / 128, 128, 0, st>>>(dr, n, P, anyhit ? 1 : 0);
+    if (ctx->bvh_width == 8 && sc->wide_ok) {
+        if (anyhit) k_trace8<true, false><<<sm * 12, 128, 0, st>>>(P, 0);
+        else k_trace8<false, false><<<sm * 12, 128, 0, st>>>(P, 0);
+    } else {
+        if (anyhit) k_trace<true, false><<<sm * 12, 128, 0, st>>>(P, 0);
+        else k_trace<false, false><<<sm * 12, 128, 0, st>>>(P, 0);
+    }
+    k_hits_out<<<(n + 127) / 128, 128, 0, st>>>(P, n, anyhit ? 1 : 0, dh);
+    s = launch_check("rt_trace kernels");
     if (s == RT_OK && !on_device) {
         cudaError_t e = cudaMemcpyAsync(hits, tmp_h, sizeof(rt_hit) * (size_t)n, cudaMemcpyDeviceToHost, st);
         if (e != cudaSuccess) s = fail(RT_ERR_CUDA, cudaGetErrorString(e));
@@ -1894,8 +2186,13 @@ extern "C" rt_status rt_render_tile_static(rt_ctx *ctx, rt_scene *sc, const rt_r
     } else {
         const int blocks = sm * 8;
         for (int r = 0; r < rounds; r++) {
-            k_trace<false, false><<<sm * 12, 128, 0, st>>>(Pm, r);
-            k_trace<true, false><<<sm * 12, 128, 0, st>>>(Pm, r);
+            if (ctx->bvh_width == 8 && sc->wide_ok) {
+                k_trace8<false, false><<<sm * 12, 128, 0, st>>>(Pm, r);
+                k_trace8<true, false><<<sm * 12, 128, 0, st>>>(Pm, r);
+            } else {
+                k_trace<false, false><<<sm * 12, 128, 0, st>>>(Pm, r);
+                k_trace<true, false><<<sm * 12, 128, 0, st>>>(Pm, r);
+            }
             k_pt_resolve<<<blocks, 128, 0, st>>>(Pm, r);
             if (sc->bsdf_types & 1) k_pt_shade<0><<<blocks, 128, 0, st>>>(Pm, r);
             if (sc->bsdf_types & 2) k_pt_shade<1><<<blocks, 128, 0, st>>>(Pm, r);

@@ -242,4 +242,207 @@ void build_bvh2(const float *tv, int n, BvhImage &img, int max_leaf, int n_bins)
     img.sah_cost = sah;
 }
 
+namespace {
+
+struct Collapse {
+    const std::vector<BuildNode> &bn;
+    const std::vector<int> &order;
+    const float *tv;
+    float seps;
+    WideBvhImage &img;
+    int maxd = 0;
+
+    Collapse(const std::vector<BuildNode> &b, const std::vector<int> &o, const float *t, float e, WideBvhImage &im)
+        : bn(b), order(o), tv(t), seps(e), img(im) {}
+
+    void push_tri(int t)
+    {
+        const float *p = tv + 9 * (size_t)t;
+        float o[12];
+        int32_t id = t;
+        o[0] = p[0]; o[1] = p[1]; o[2] = p[2]; std::memcpy(&o[3], &id, 4);
+        o[4] = p[3] - p[0]; o[5] = p[4] - p[1]; o[6] = p[5] - p[2]; o[7] = 0.f;
+        o[8] = p[6] - p[0]; o[9] = p[7] - p[1]; o[10] = p[8] - p[2]; o[11] = 0.f;
+        img.tri_slots.insert(img.tri_slots.end(), o, o + 12);
+        img.n_slots++;
+    }
+
+    // quantise [lo, hi] outward on a grid p + q * s, q in [0, 255]
+    static void quant(float p, float s, float lo, float hi, uint8_t &qlo, uint8_t &qhi)
+    {
+        int a = (int)std::floor(((double)lo - p) / s);
+        int b = (int)std::ceil(((double)hi - p) / s);
+        a = std::max(0, std::min(255, a));
+        b = std::max(0, std::min(255, b));
+        // decoded with binary32 arithmetic the box must still contain [lo, hi]
+        while (a > 0 && p + (float)a * s > lo) a--;
+        while (b < 255 && p + (float)b * s < hi) b++;
+        qlo = (uint8_t)a;
+        qhi = (uint8_t)b;
+    }
+
+    void emit(int wi, int bi, int depth)
+    {
+        maxd = std::max(maxd, depth);
+        std::vector<int> ch;
+        if (bn[bi].leaf) ch.push_back(bi);
+        else { ch.push_back(bn[bi].child[0]); ch.push_back(bn[bi].child[1]); }
+        while ((int)ch.size() < 8) {
+            int best = -1;
+            double ba = -1.0;
+            for (int k = 0; k < (int)ch.size(); k++) {
+                const BuildNode &c = bn[ch[k]];
+                if (c.leaf) continue;
+                double a = c.box.area();
+                if (a > ba) { ba = a; best = k; }
+            }
+            if (best < 0) break;
+            int b = ch[best];
+            ch[best] = bn[b].child[0];
+            ch.insert(ch.begin() + best + 1, bn[b].child[1]);
+        }
+        // widened child boxes and the node box
+        float cb[8][6];
+        Box nb; nb.reset();
+        for (int k = 0; k < (int)ch.size(); k++) {
+            widen(bn[ch[k]].box, seps, cb[k]);
+            Box w;
+            for (int a = 0; a < 3; a++) { w.mn[a] = cb[k][2 * a]; w.mx[a] = cb[k][2 * a + 1]; }
+            nb.grow(w);
+        }
+        // The device evaluates a plane as fma(q, 2^e * idir, p * idir - o * idir):
+        // besides the origin term (covered by the traversal's slab guard) it rounds
+        // values up to |p| + extent of this node, so pad every child by that.
+        for (int a = 0; a < 3; a++) {
+            float npad = 2.5e-7f * (2.f * std::fabs(nb.mn[a]) + std::fabs(nb.mx[a]) + (nb.mx[a] - nb.mn[a]));
+            for (int k = 0; k < (int)ch.size(); k++) { cb[k][2 * a] -= npad; cb[k][2 * a + 1] += npad; }
+            nb.mn[a] -= npad; nb.mx[a] += npad;
+        }
+        float p[3], sc[3];
+        uint8_t e[3];
+        for (int a = 0; a < 3; a++) {
+            p[a] = nb.mn[a];
+            double ext = (double)nb.mx[a] - nb.mn[a];
+            int ex = -126;
+            if (ext > 0) {
+                ex = (int)std::ceil(std::log2(ext / 255.0 * (1.0 + 1e-6)));
+                while (std::ldexp(255.0, ex) < ext) ex++;
+            }
+            ex = std::max(-126, std::min(127, ex));
+            // the top quantum must reach the node's max in binary32 too
+            while (ex < 127 && p[a] + (float)std::ldexp(255.0, ex) < nb.mx[a]) ex++;
+            sc[a] = (float)std::ldexp(1.0, ex);
+            e[a] = (uint8_t)(ex + 127);
+        }
+        // Octant slots: slot s holds the child met first by rays whose
+        // direction has sign bits s (bit a set: negative along axis a), i.e.
+        // the child with the smallest centroid offset along that direction.
+        // Rays visit slots in the order k ^ octant, k = 0..7.
+        const int nc = (int)ch.size();
+        int slot_of[8];
+        {
+            double cost[8][8];
+            for (int k = 0; k < nc; k++) {
+                double c[3];
+                for (int a = 0; a < 3; a++)
+                    c[a] = 0.5 * ((double)cb[k][2 * a] + cb[k][2 * a + 1]) - 0.5 * ((double)nb.mn[a] + nb.mx[a]);
+                for (int sl = 0; sl < 8; sl++)
+                    cost[k][sl] = (sl & 1 ? -c[0] : c[0]) + (sl & 2 ? -c[1] : c[1]) + (sl & 4 ? -c[2] : c[2]);
+            }
+            bool kused[8] = {false}, sused[8] = {false};
+            for (int it = 0; it < nc; it++) {
+                int bk = -1, bs = -1;
+                double bc = 0.0;
+                for (int k = 0; k < nc; k++) {
+                    if (kused[k]) continue;
+                    for (int sl = 0; sl < 8; sl++)
+                        if (!sused[sl] && (bk < 0 || cost[k][sl] < bc)) { bk = k; bs = sl; bc = cost[k][sl]; }
+                }
+                kused[bk] = true; sused[bs] = true;
+                slot_of[bk] = bs;
+            }
+        }
+        int n_int = 0;
+        for (int c : ch) if (!bn[c].leaf) n_int++;
+        int child_base = img.n_nodes;
+        img.n_nodes += n_int;
+        img.nodes.resize(20 * (size_t)img.n_nodes, 0.f);
+        int tri_base = img.n_slots;
+        // empty slots: inverted boxes (lo 255 > hi 0) that no ray enters
+        uint8_t meta[8] = {0, 0, 0, 0, 0, 0, 0, 0}, ql[3][8], qh[3][8];
+        std::memset(ql, 255, sizeof(ql));
+        std::memset(qh, 0, sizeof(qh));
+        std::vector<std::pair<int, int>> inner;   // (wide index, binary index)
+        int ki = 0;
+        for (int sl = 0; sl < 8; sl++) {
+            int k = -1;
+            for (int j = 0; j < nc; j++) if (slot_of[j] == sl) k = j;
+            if (k < 0) continue;
+            const BuildNode &c = bn[ch[k]];
+            for (int a = 0; a < 3; a++) quant(p[a], sc[a], cb[k][2 * a], cb[k][2 * a + 1], ql[a][sl], qh[a][sl]);
+            if (c.leaf) {
+                int off = img.n_slots - tri_base;
+                for (int t = 0; t < c.count; t++) push_tri(order[c.first + t]);
+                meta[sl] = (uint8_t)((std::max(1, c.count) << 5) | off);
+            } else {
+                meta[sl] = (uint8_t)(0xE0 | ki);
+                inner.push_back({child_base + ki, ch[k]});
+                ki++;
+            }
+        }
+        float *o = &img.nodes[20 * (size_t)wi];
+        uint32_t ebits = (uint32_t)e[0] | ((uint32_t)e[1] << 8) | ((uint32_t)e[2] << 16);
+        o[0] = p[0]; o[1] = p[1]; o[2] = p[2]; std::memcpy(&o[3], &ebits, 4);
+        int32_t cbv = child_base, tbv = tri_base;
+        std::memcpy(&o[4], &cbv, 4);
+        std::memcpy(&o[5], &tbv, 4);
+        std::memcpy(&o[6], meta, 4);
+        std::memcpy(&o[7], meta + 4, 4);
+        std::memcpy(&o[8], ql[0], 8);
+        std::memcpy(&o[10], ql[1], 8);
+        std::memcpy(&o[12], ql[2], 8);
+        std::memcpy(&o[14], qh[0], 8);
+        std::memcpy(&o[16], qh[1], 8);
+        std::memcpy(&o[18], qh[2], 8);
+        for (auto &pr : inner) emit(pr.first, pr.second, depth + 1);
+    }
+};
+
+}  // namespace
+
+void build_wbvh8(const float *tv, int n, WideBvhImage &img, int n_bins)
+{
+    img = WideBvhImage();
+    if (n <= 0) return;
+    Builder B;
+    B.tv = tv;
+    B.max_leaf = 3;
+    B.n_bins = n_bins;
+    B.tb.resize(n);
+    B.cen.resize(3 * (size_t)n);
+    B.order.resize(n);
+    Box scene; scene.reset();
+    for (int t = 0; t < n; t++) {
+        Box b; b.reset();
+        for (int k = 0; k < 3; k++) b.grow(tv + 9 * (size_t)t + 3 * k);
+        B.tb[t] = b;
+        scene.grow(b);
+        for (int a = 0; a < 3; a++) B.cen[3 * (size_t)t + a] = 0.5f * (b.mn[a] + b.mx[a]);
+        B.order[t] = t;
+    }
+    float sext = 0.f;
+    for (int a = 0; a < 3; a++) sext = std::max(sext, scene.mx[a] - scene.mn[a]);
+    float seps = std::max(sext * 1e-7f, 1e-30f);
+    std::vector<BuildNode> bn;
+    bn.reserve(2 * (size_t)n / 2 + 16);
+    int maxd = 0;
+    B.build(0, n, bn, 0, maxd);
+    img.tri_slots.reserve(12 * (size_t)n);
+    img.n_nodes = 1;
+    img.nodes.assign(20, 0.f);
+    Collapse cl(bn, B.order, tv, seps, img);
+    cl.emit(0, 0, 0);
+    img.max_depth = cl.maxd;
+}
+
 }  // namespace rtgpu

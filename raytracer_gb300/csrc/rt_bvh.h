@@ -24,9 +24,33 @@ struct BvhImage {
     double sah_cost = 0.0;
 };
 
+// Compressed 8-wide BVH.  Each node is 5 float4 (80 bytes):
+//   w0 = (px, py, pz, bits: ex | ey << 8 | ez << 16)      grid origin, exponents
+//   w1 = (child_base, tri_base, meta[0..3], meta[4..7])   as int32 / packed bytes
+//   w2 = (qlo.x[0..7], qlo.y[0..7])   w3 = (qlo.z[0..7], qhi.x[0..7])
+//   w4 = (qhi.y[0..7], qhi.z[0..7])   one byte per child slot
+// Child box = p + q * 2^(e-127) per axis, quantised outward.  meta[i]:
+//   0 empty; 0xE0 | k internal child node child_base + k;
+//   (c << 5) | k leaf of c in 1..3 triangles at slots tri_base + k.
+// Slot i holds the child reached first by rays whose direction signs are the
+// bits of i (bit a set: negative along axis a); a ray with sign bits o visits
+// the slots in the order k ^ o, k = 0..7.
+struct WideBvhImage {
+    std::vector<float> nodes;      // 20 floats per node
+    std::vector<float> tri_slots;  // 12 floats per slot, same layout as BvhImage
+    int n_nodes = 0;
+    int n_slots = 0;
+    int max_depth = 0;
+};
+
 // Build from triangle vertex positions (9 floats per triangle).  Boxes are
 // widened outward by a few ulps so the fused slab test never culls a node
 // that contains a hit the exact Moller-Trumbore test accepts.
 void build_bvh2(const float *tri_v, int n_tris, BvhImage &out, int max_leaf = 4, int n_bins = 32);
+
+// Binned-SAH binary tree (leaves of at most 3 triangles) collapsed into the
+// compressed 8-wide layout above, greedily opening the child of largest
+// surface area until a node has 8 children.
+void build_wbvh8(const float *tri_v, int n_tris, WideBvhImage &out, int n_bins = 32);
 
 }  // namespace rtgpu

@@ -73,6 +73,10 @@ struct DevScene {
     const float4 *nodes;
     const float4 *tri_slots;    // 3 float4 per leaf slot: (p0, id), (e1, 0), (e2, 0)
     int n_nodes;
+    // compressed 8-wide BVH (80-byte nodes, see rt_bvh.h) and its triangle slots
+    const float4 *wnodes;
+    const float4 *wtri;
+    int n_wnodes;
     // original geometry
     const float *tri_v;         // 9 floats per triangle (p0, p1, p2)
     const float *tri_n;         // 9 floats per triangle (n0, n1, n2) or null
@@ -194,6 +198,14 @@ __device__ __forceinline__ float adapt_mint(V3 o, float mint)
     return mint;
 }
 
+// Per-axis guard of the fused slab test.  A slab distance is evaluated as
+// fma(plane, 1/d, -o/d); besides the rounding relative to the plane (covered
+// by widening the boxes when they are built) it carries a few ulps of |o/d|.
+// Every near plane is moved earlier and every far plane later by
+// 2^-21 |o/d|, which in distance along the axis is 2^-21 |o|, however
+// parallel the ray runs to the slab.
+__device__ __forceinline__ float slab_guard(float oo) { return fabsf(oo) * 4.76837158203125e-7f; }
+
 // Leaf encoding of BVH2 child links: c >= 0 internal node index; c < 0 leaf
 // with v = ~c, first slot = v >> 3, count = (v & 7) + 1.
 __device__ __forceinline__ float rt_min4(float a, float b, float c, float d) { return fminf(fminf(a, b), fminf(c, d)); }
@@ -215,7 +227,11 @@ __device__ __forceinline__ bool trace_ray(const DevScene &S, V3 o, V3 d, float m
     float idx = 1.0f / (fabsf(d.x) > eps ? d.x : copysignf(eps, d.x));
     float idy = 1.0f / (fabsf(d.y) > eps ? d.y : copysignf(eps, d.y));
     float idz = 1.0f / (fabsf(d.z) > eps ? d.z : copysignf(eps, d.z));
-    float ox = o.x * idx, oy = o.y * idy, oz = o.z * idz;
+    const float oox = o.x * idx, ooy = o.y * idy, ooz = o.z * idz;
+    // offsets for the lo and hi planes of each axis, guard applied outward
+    const float lx = -(oox + copysignf(slab_guard(oox), idx)), hx = -(oox - copysignf(slab_guard(oox), idx));
+    const float ly = -(ooy + copysignf(slab_guard(ooy), idy)), hy = -(ooy - copysignf(slab_guard(ooy), idy));
+    const float lz = -(ooz + copysignf(slab_guard(ooz), idz)), hz = -(ooz - copysignf(slab_guard(ooz), idz));
     if (S.n_nodes > 0) {
         int stack[RT_STACK];
         int sp = 0;
@@ -226,12 +242,12 @@ __device__ __forceinline__ bool trace_ray(const DevScene &S, V3 o, V3 d, float m
                 const float4 *N = S.nodes + 4 * (size_t)node;
                 float4 n0 = __ldg(N), n1 = __ldg(N + 1), n2 = __ldg(N + 2);
                 int4 cc = __ldg(reinterpret_cast<const int4 *>(N + 3));
-                float c0lox = __fmaf_rn(n0.x, idx, -ox), c0hix = __fmaf_rn(n0.y, idx, -ox);
-                float c0loy = __fmaf_rn(n0.z, idy, -oy), c0hiy = __fmaf_rn(n0.w, idy, -oy);
-                float c0loz = __fmaf_rn(n2.x, idz, -oz), c0hiz = __fmaf_rn(n2.y, idz, -oz);
-                float c1lox = __fmaf_rn(n1.x, idx, -ox), c1hix = __fmaf_rn(n1.y, idx, -ox);
-                float c1loy = __fmaf_rn(n1.z, idy, -oy), c1hiy = __fmaf_rn(n1.w, idy, -oy);
-                float c1loz = __fmaf_rn(n2.z, idz, -oz), c1hiz = __fmaf_rn(n2.w, idz, -oz);
+                float c0lox = __fmaf_rn(n0.x, idx, lx), c0hix = __fmaf_rn(n0.y, idx, hx);
+                float c0loy = __fmaf_rn(n0.z, idy, ly), c0hiy = __fmaf_rn(n0.w, idy, hy);
+                float c0loz = __fmaf_rn(n2.x, idz, lz), c0hiz = __fmaf_rn(n2.y, idz, hz);
+                float c1lox = __fmaf_rn(n1.x, idx, lx), c1hix = __fmaf_rn(n1.y, idx, hx);
+                float c1loy = __fmaf_rn(n1.z, idy, ly), c1hiy = __fmaf_rn(n1.w, idy, hy);
+                float c1loz = __fmaf_rn(n2.z, idz, lz), c1hiz = __fmaf_rn(n2.w, idz, hz);
                 float c0min = rt_max4(fminf(c0lox, c0hix), fminf(c0loy, c0hiy), fminf(c0loz, c0hiz), mint);
                 float c0max = rt_min4(fmaxf(c0lox, c0hix), fmaxf(c0loy, c0hiy), fmaxf(c0loz, c0hiz), hit_t);
                 float c1min = rt_max4(fminf(c1lox, c1hix), fminf(c1loy, c1hiy), fminf(c1loz, c1hiz), mint);

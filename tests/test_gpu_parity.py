@@ -84,19 +84,27 @@ def _trace_parity(ctx, rtlib, scene, n=20000, seed=0):
     o.close()
 
 
-def test_trace_parity_cornell(ctx, rtlib, cornell):
+@pytest.fixture(params=[2, 8], ids=["bvh2", "bvh8"])
+def width(request, ctx):
+    """Runs a test once per traversal tree (binary and compressed 8-wide)."""
+    ctx.set_bvh_width(request.param)
+    yield request.param
+    ctx.set_bvh_width(2)
+
+
+def test_trace_parity_cornell(ctx, rtlib, cornell, width):
     _trace_parity(ctx, rtlib, cornell)
 
 
-def test_trace_parity_icosphere(ctx, rtlib, ico):
+def test_trace_parity_icosphere(ctx, rtlib, ico, width):
     _trace_parity(ctx, rtlib, ico, n=40000, seed=1)
 
 
-def test_trace_parity_spheres_and_boxes(ctx, rtlib, vol):
+def test_trace_parity_spheres_and_boxes(ctx, rtlib, vol, width):
     _trace_parity(ctx, rtlib, vol, n=20000, seed=2)
 
 
-def test_trace_edge_cases(ctx, rtlib, cornell):
+def test_trace_edge_cases(ctx, rtlib, cornell, width):
     g = rtlib.Scene(ctx, cornell)
     o = O.OracleScene(cornell)
     r = np.zeros(6, D.RAY_DTYPE)
@@ -245,7 +253,7 @@ def _film_parity(ctx, rtlib, scene, spp, seed, max_bad, block=16, **over):
     return fg, fo
 
 
-def test_film_parity_cornell(ctx, rtlib, cornell):
+def test_film_parity_cornell(ctx, rtlib, cornell, width):
     _film_parity(ctx, rtlib, cornell, 4, 11, max_bad=0.02)
 
 
@@ -254,7 +262,7 @@ def test_film_parity_cornell_ragged_tiles_and_offset(ctx, rtlib):
     _film_parity(ctx, rtlib, s, 3, 5, max_bad=0.03, block=8, sample_begin=7)
 
 
-def test_film_parity_icosphere_env(ctx, rtlib, ico):
+def test_film_parity_icosphere_env(ctx, rtlib, ico, width):
     _film_parity(ctx, rtlib, ico, 2, 3, max_bad=0.03)
 
 
