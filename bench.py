@@ -323,6 +323,105 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
+def _batch_jobs(n):
+    from raytracer_gb300 import scenes
+    env, _ = scenes.sky_env(1024, 512)
+    return [scenes.batch_job(k, env) for k in range(n)]
+
+
+def run_batch(args):
+    """64 independent scenes: plain (one rt_render per job, one after the
+    other) against rt_batch_render on several lanes; same films."""
+    import torch
+    import raytracer_gb300 as R
+    torch.cuda.init()
+    t0 = time.time()
+    jobs = _batch_jobs(args.batch_jobs)
+    gen_s = time.time() - t0
+    ctx = R.Context(0)
+    t0 = time.time()
+    scs = [R.Scene(ctx, s) for s, _ in jobs]
+    upload_s = time.time() - t0
+    work = [(g, spp, dict(seed=k)) for k, (g, (_, spp)) in enumerate(zip(scs, jobs))]
+    total = sum(g.width * g.height * spp for g, spp, _ in work)
+    # warm-up: every scene once at 1 spp (tile tables, wavefront buffers)
+    ctx.batch_render([(g, 1, dict(seed=0)) for g, _, _ in work])
+    for g, _, _ in work[:4]:
+        g.render(1)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(0)
+    clocks.start()
+    t0 = time.perf_counter()
+    plain = [g.render(spp, **o) for g, spp, o in work]
+    plain_s = time.perf_counter() - t0
+    res = {}
+    for lanes in [int(x) for x in args.lanes.split(",")]:
+        ctx.set_lanes(lanes)
+        t0 = time.perf_counter()
+        films = ctx.batch_render(work)
+        dt = time.perf_counter() - t0
+        same = all(np.array_equal(a, b) for a, b in zip(films, plain))
+        res[lanes] = (dt, same)
+    clk = clocks.stop()
+    best = min(res, key=lambda k: res[k][0])
+    line = {"metric": METRIC, "value": total / res[best][0], "unit": UNIT, "n_gpus": 1, "higher_is_better": True,
+            "workload": "batch%d" % len(jobs), "dtype": "f32", "data": "synthetic (seeded scenes)",
+            "config": {"jobs": len(jobs), "total_samples": total,
+                       "triangles": int(sum(s.n_triangles for s, _ in jobs)),
+                       "pixels": int(sum(g.width * g.height for g in scs)), "max_depth": 12,
+                       "scene_gen_s": round(gen_s, 2), "scene_build_upload_s": round(upload_s, 2)},
+            "plain": {"value": total / plain_s, "seconds": plain_s},
+            "batched": {str(k): {"value": total / v[0], "seconds": v[0], "films_equal_plain": v[1]}
+                        for k, v in res.items()},
+            "best_lanes": best, "speedup_vs_plain": plain_s / res[best][0], "clocks": clk}
+    print(json.dumps(line))
+
+
+def run_serve(args):
+    """Poisson job arrivals served by rt_server (several lanes) and by a
+    one-lane server (plain, one job after another), same arrival trace,
+    each job rendered progressively to a target RMSE."""
+    import torch
+    import raytracer_gb300 as R
+    from raytracer_gb300 import scenes
+    torch.cuda.init()
+    jobs = _batch_jobs(args.batch_jobs)
+    vols = [scenes.volume_grid(256, 256, res=128, seed=k) for k in range(2)]
+    ctx = R.Context(0)
+    pt = [R.Scene(ctx, s) for s, _ in jobs]
+    vo = [R.Scene(ctx, s) for s in vols]
+    ctx.batch_render([(g, 1, dict(seed=0)) for g in pt + vo])
+    out = {"metric": "job latency", "unit": "ms", "workload": "serve", "higher_is_better": False,
+           "target_rmse": args.target_rmse, "spp_cap": args.spp_cap, "jobs_per_rate": args.serve_jobs,
+           "rates": {}}
+    for lam in [float(x) for x in args.rates.split(",")]:
+        rng = np.random.default_rng(int(lam * 10))
+        arrivals = np.cumsum(rng.exponential(1.0 / lam, args.serve_jobs))
+        picks = [(vo[rng.integers(len(vo))], 64) if rng.random() < 0.2 else (pt[rng.integers(len(pt))], args.spp_cap)
+                 for _ in range(args.serve_jobs)]
+        rec = {}
+        for name, lanes in (("plain", 1), ("served", args.serve_lanes)):
+            srv = R.Server(ctx, lanes=lanes)
+            t0 = time.perf_counter()
+            ids = []
+            for (g, cap), ta in zip(picks, arrivals):
+                dt = ta - (time.perf_counter() - t0)
+                if dt > 0:
+                    time.sleep(dt)
+                ids.append(srv.submit(g, cap, target_rmse=args.target_rmse, seed=len(ids)))
+            lat, spp = [], []
+            for j in ids:
+                info, _ = srv.wait(j)
+                lat.append(info["queue_ms"] + info["run_ms"])
+                spp.append(info["spp_done"])
+            wall = time.perf_counter() - t0
+            srv.stop()
+            rec[name] = {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                         "jobs_per_s": len(ids) / wall, "mean_spp": float(np.mean(spp))}
+        out["rates"][str(lam)] = rec
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -334,7 +433,21 @@ def main():
                     help="profiler case: same scene at 512x512, 8 spp, no CPU baseline, no e2e")
     ap.add_argument("--bvh-width", type=int, default=2, choices=[2, 8],
                     help="traversal tree: binary BVH (default) or compressed 8-wide BVH")
+    ap.add_argument("--workload", default="icosphere", choices=["icosphere", "batch", "serve"],
+                    help="icosphere: the headline single-scene render; batch: 64 scenes, plain vs "
+                         "rt_batch_render; serve: Poisson arrivals through rt_server")
+    ap.add_argument("--batch-jobs", type=int, default=64)
+    ap.add_argument("--lanes", default="2,4,8", help="batch: lane counts to time")
+    ap.add_argument("--rates", default="5,20,100", help="serve: arrival rates (jobs/s)")
+    ap.add_argument("--serve-jobs", type=int, default=24, help="serve: jobs per arrival rate")
+    ap.add_argument("--serve-lanes", type=int, default=4)
+    ap.add_argument("--target-rmse", type=float, default=0.02)
+    ap.add_argument("--spp-cap", type=int, default=256)
     args = ap.parse_args()
+    if args.workload == "batch":
+        return run_batch(args)
+    if args.workload == "serve":
+        return run_serve(args)
     if args.small:
         CONFIG.update(SMALL)
     if args.impl == "reference":

@@ -177,8 +177,14 @@ typedef struct rt_render_desc {
     int32_t sample_begin;    /* first sample index (progressive rendering)       */
     uint64_t seed;           /* path-stream sampler seed                         */
     int32_t block_x, block_y;/* tile size of the reference job grid (default 32) */
-    int32_t flags;           /* reserved, 0                                      */
+    int32_t flags;           /* RT_RENDER_* bits, 0 for a plain render           */
 } rt_render_desc;
+
+/* rt_render_desc.flags: add this call's (rgb sum, weight) to the film instead
+ * of overwriting it, for progressive rendering over disjoint sample ranges.
+ * Not part of the reference: there Screen::addSample always accumulates
+ * into one film per render (core/Screen.cpp:44-80). */
+#define RT_RENDER_ACCUMULATE 1
 
 /* Per-path sample stream ("PathStreamSampler"): path (pixel p, sample s)
  * draws from a PCG32 (tools/Rng.h:81-141) seeded with
@@ -275,7 +281,7 @@ rt_status rt_scene_info(const rt_scene *scene, float bounds[6], int64_t *device_
 /* Render spp samples per pixel starting at sample_begin; film_rgbw receives
  * width*height*4 floats (rgb sum, weight), accumulated in sample order, in
  * host memory (on_device = 0) or device memory (on_device = 1).  The film is
- * overwritten, not accumulated into. */
+ * overwritten unless rd->flags has RT_RENDER_ACCUMULATE. */
 rt_status rt_render(rt_ctx *ctx, rt_scene *scene, const rt_render_desc *rd,
                     float *film_rgbw, int32_t on_device);
 rt_status rt_render_stats_get(const rt_ctx *ctx, rt_render_stats *out);
@@ -305,6 +311,56 @@ rt_status rt_ctx_set_bvh_width(rt_ctx *ctx, int32_t width);
  * that overlap on the GPU (other threads or streams) race. */
 rt_status rt_render_tile_static(rt_ctx *ctx, rt_scene *scene, const rt_render_desc *rd,
                                 int32_t tile_x, int32_t tile_y, float *film_rgbw_device);
+
+/* Batched rendering: n independent jobs (scenes[i] rendered with descs[i]
+ * into films[i], each width*height*4 floats on the host or, with
+ * on_device = 1, on the device), largest job first, on up to
+ * rt_ctx_set_lanes() worker lanes of the context's device (one stream,
+ * wavefront buffers and host thread each).  Each film equals what
+ * rt_render writes for that job alone.  Returns after every job has
+ * finished; on failures the other jobs still run and the first error is
+ * returned.  rt_render_stats_get then reports the sums over the jobs, with
+ * kernel_ms the wall time of the batch.  The reference renders one scene per
+ * process (core/main.cpp:439-447); this call replaces a loop of such runs. */
+rt_status rt_batch_render(rt_ctx *ctx, rt_scene *const *scenes, const rt_render_desc *descs,
+                          int32_t n, float *const *films, int32_t on_device);
+/* Worker lanes of rt_batch_render: 1..16, default 4. */
+rt_status rt_ctx_set_lanes(rt_ctx *ctx, int32_t lanes);
+
+/* Served rendering: a job queue drained by worker lanes (one stream,
+ * wavefront buffers and host thread each) on the context's device.  No
+ * counterpart in the reference, which renders one scene per process. */
+typedef struct rt_server rt_server;
+typedef int64_t rt_job_id;
+typedef struct rt_server_opts {
+    int32_t lanes;                /* concurrent jobs, 1..16 (0: 4)                  */
+    int32_t max_queue;            /* queued jobs before submit fails (0: 4096)      */
+    int64_t device_budget_bytes;  /* film memory of running jobs, 0 = unlimited    */
+} rt_server_opts;
+enum { RT_JOB_QUEUED = 0, RT_JOB_RUNNING = 1, RT_JOB_DONE = 2, RT_JOB_FAILED = 3 };
+typedef struct rt_job_info {
+    int32_t state;                /* RT_JOB_*                                       */
+    int32_t spp_done;             /* samples per pixel in the film                  */
+    float rmse_estimate;          /* progressive jobs: estimated RMSE, else -1     */
+    float queue_ms, run_ms;       /* time queued, time rendering                    */
+    char error[128];              /* RT_JOB_FAILED: rt_last_error of the job        */
+} rt_job_info;
+rt_status rt_server_start(rt_ctx *ctx, const rt_server_opts *opts, rt_server **out);
+/* Queue a render of `scene` (which must outlive the job).  target_rmse <= 0:
+ * render desc->spp samples, the film equals rt_render's.  target_rmse > 0:
+ * render progressively from desc->sample_begin, at most desc->spp samples,
+ * until the RMSE of the film's pixel means (rgb / weight, over pixels and
+ * channels) estimated from two half films falls to target_rmse. */
+rt_status rt_job_submit(rt_server *srv, rt_scene *scene, const rt_render_desc *desc,
+                        float target_rmse, rt_job_id *id);
+/* Job state; when the job has finished and film is not NULL, copy its
+ * width*height*4 floats to film (host memory) and release the job. */
+rt_status rt_job_poll(rt_server *srv, rt_job_id id, rt_job_info *info, float *film);
+/* As rt_job_poll after waiting up to timeout_ms (< 0: no limit) for the job. */
+rt_status rt_job_wait(rt_server *srv, rt_job_id id, int32_t timeout_ms, rt_job_info *info,
+                      float *film);
+/* Finish running jobs, drop queued ones, release the lanes. */
+rt_status rt_server_stop(rt_server *srv);
 
 /* Trace n rays (closest hit, or any hit when anyhit != 0). */
 rt_status rt_trace(rt_ctx *ctx, rt_scene *scene, const rt_ray *rays, int32_t n,

@@ -7,6 +7,7 @@ rounded operations, as in the reference's CPU build; the traversal kernels
 use explicit fused multiply-adds where rounding cannot change a result.
 """
 import os
+import shutil
 import subprocess
 import sys
 from concurrent.futures import ThreadPoolExecutor
@@ -21,8 +22,13 @@ ARCH = os.environ.get("RTGPU_ARCH", "-gencode=arch=compute_103a,code=sm_103a")
 NVCC = os.environ.get("NVCC", "nvcc")
 
 CUDA_SOURCES = ["rt_api.cu"]
-HOST_SOURCES = ["rt_bvh.cpp"]
-HEADERS = ["rt_math.cuh", "rt_device.cuh", "rt_kernels.cuh", "rt_bvh.h"]
+HOST_SOURCES = ["rt_bvh.cpp", "rt_serve.cpp"]
+HEADERS = ["rt_math.cuh", "rt_device.cuh", "rt_kernels.cuh", "rt_bvh.h", "rt_internal.h"]
+
+
+def _cuda_include():
+    nvcc = NVCC if os.path.isabs(NVCC) else (shutil.which(NVCC) or "/usr/local/cuda/bin/nvcc")
+    return os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc))), "include")
 
 
 def _run(cmd):
@@ -62,7 +68,8 @@ def build(force=False, verbose=False, ptxas_info=False):
         obj = os.path.join(BUILD, s + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + hdrs):
-            jobs.append(["g++", "-O3", "-std=c++17", "-fPIC", "-pthread", "-c", src, "-o", obj])
+            jobs.append(["g++", "-O3", "-std=c++17", "-fPIC", "-pthread", "-I", os.path.join(ROOT, "include"),
+                         "-I", _cuda_include(), "-c", src, "-o", obj])
     logs = []
     if jobs:
         with ThreadPoolExecutor(max_workers=len(jobs)) as ex:

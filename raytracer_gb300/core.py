@@ -22,6 +22,18 @@ RT_OK = 0
 _STATUS = {1: "RT_ERR_INVALID", 2: "RT_ERR_CUDA", 3: "RT_ERR_LIMIT", 4: "RT_ERR_NOMEM", 5: "RT_ERR_UNSUPPORTED"}
 
 
+class ServerOpts(C.Structure):
+    _fields_ = [("lanes", C.c_int32), ("max_queue", C.c_int32), ("device_budget_bytes", C.c_int64)]
+
+
+class JobInfo(C.Structure):
+    _fields_ = [("state", C.c_int32), ("spp_done", C.c_int32), ("rmse_estimate", C.c_float),
+                ("queue_ms", C.c_float), ("run_ms", C.c_float), ("error", C.c_char * 128)]
+
+
+JOB_QUEUED, JOB_RUNNING, JOB_DONE, JOB_FAILED = 0, 1, 2, 3
+
+
 class RtError(RuntimeError):
     def __init__(self, status, msg):
         super().__init__("%s: %s" % (_STATUS.get(status, status), msg))
@@ -59,8 +71,17 @@ def lib():
     L.rt_render_tile_static.restype = C.c_int32
     L.rt_bsdf_query.argtypes = [vp, vp, C.c_int32, C.c_int32, vp, C.c_int32, vp]
     L.rt_light_query.argtypes = [vp, vp, C.c_int32, vp, C.c_int32, vp]
+    L.rt_batch_render.argtypes = [vp, C.POINTER(vp), C.POINTER(D.RenderDesc), C.c_int32, C.POINTER(vp), C.c_int32]
+    L.rt_ctx_set_lanes.argtypes = [vp, C.c_int32]
+    L.rt_server_start.argtypes = [vp, C.POINTER(ServerOpts), C.POINTER(vp)]
+    L.rt_job_submit.argtypes = [vp, vp, C.POINTER(D.RenderDesc), C.c_float, C.POINTER(C.c_int64)]
+    L.rt_job_poll.argtypes = [vp, C.c_int64, C.POINTER(JobInfo), vp]
+    L.rt_job_wait.argtypes = [vp, C.c_int64, C.c_int32, C.POINTER(JobInfo), vp]
+    L.rt_server_stop.argtypes = [vp]
     for name in ("rt_ctx_create", "rt_ctx_destroy", "rt_ctx_set_stream", "rt_scene_create", "rt_scene_destroy",
-                 "rt_scene_info", "rt_render", "rt_render_stats_get", "rt_ctx_set_profiling", "rt_ctx_set_bvh_width", "rt_trace", "rt_bsdf_query", "rt_light_query"):
+                 "rt_scene_info", "rt_render", "rt_render_stats_get", "rt_ctx_set_profiling", "rt_ctx_set_bvh_width",
+                 "rt_trace", "rt_bsdf_query", "rt_light_query", "rt_batch_render", "rt_ctx_set_lanes",
+                 "rt_server_start", "rt_job_submit", "rt_job_poll", "rt_job_wait", "rt_server_stop"):
         getattr(L, name).restype = C.c_int32
     _lib = L
     return L
@@ -105,6 +126,31 @@ class Context:
         """Traversal tree for later renders and traces: 2 (default) or 8."""
         _check(lib().rt_ctx_set_bvh_width(self.h, int(width)))
 
+    def set_lanes(self, lanes):
+        """Concurrent worker lanes of batch_render (1..16, default 4)."""
+        _check(lib().rt_ctx_set_lanes(self.h, int(lanes)))
+
+    def batch_render(self, jobs):
+        """Render independent jobs in one call (rt_batch_render).  `jobs` is
+        a list of (Scene, spp, options) with the options of Scene.render
+        (seed, sample_begin, block, max_depth, ...); returns the list of
+        (H, W, 4) host films, each equal to that job's Scene.render film."""
+        n = len(jobs)
+        scenes = (C.c_void_p * n)()
+        descs = (D.RenderDesc * n)()
+        films = []
+        fptr = (C.c_void_p * n)()
+        for i, (sc, spp, opt) in enumerate(jobs):
+            opt = dict(opt)
+            seed, sb, block = opt.pop("seed", 0), opt.pop("sample_begin", 0), opt.pop("block", 32)
+            descs[i] = sc.data.render_desc(spp, seed=seed, sample_begin=sb, block=block, **opt)
+            scenes[i] = sc.h
+            f = np.zeros((sc.height, sc.width, 4), np.float32)
+            films.append(f)
+            fptr[i] = f.ctypes.data
+        _check(lib().rt_batch_render(self.h, scenes, descs, n, fptr, 0))
+        return films
+
     def stats(self):
         s = D.RenderStats()
         _check(lib().rt_render_stats_get(self.h, C.byref(s)))
@@ -141,13 +187,17 @@ class Scene:
         _check(lib().rt_scene_info(self.h, _p(b), C.byref(nbytes), C.byref(nodes)))
         return dict(bounds=b, device_bytes=nbytes.value, bvh_nodes=nodes.value)
 
-    def render(self, spp, seed=0, sample_begin=0, film=None, block=32, **over):
+    def render(self, spp, seed=0, sample_begin=0, film=None, block=32, accumulate=False, out=None, **over):
         """Render `spp` samples per pixel; returns the (H, W, 4) film of
-        (rgb sum, weight) in host memory, or writes a device pointer
-        (`film` as an int address) when given."""
-        rd = self.data.render_desc(spp, seed=seed, sample_begin=sample_begin, block=block, **over)
+        (rgb sum, weight) in host memory (`out` when given), or writes a
+        device pointer (`film` as an int address) when given.  With
+        `accumulate` the samples are added to the film's contents."""
+        flags = D.RENDER_ACCUMULATE if accumulate else 0
+        rd = self.data.render_desc(spp, seed=seed, sample_begin=sample_begin, block=block, flags=flags, **over)
         if film is None:
-            out = np.zeros((self.height, self.width, 4), np.float32)
+            if out is None:
+                out = np.zeros((self.height, self.width, 4), np.float32)
+            assert out.dtype == np.float32 and out.flags.c_contiguous and out.shape == (self.height, self.width, 4)
             _check(lib().rt_render(self.ctx.h, self.h, C.byref(rd), _p(out), 0))
             return out
         _check(lib().rt_render(self.ctx.h, self.h, C.byref(rd), C.c_void_p(int(film)), 1))
@@ -179,6 +229,70 @@ class Scene:
         r = np.zeros(len(p), LIGHT_R)
         _check(lib().rt_light_query(self.ctx.h, self.h, light, _p(q), len(q), _p(r)))
         return r
+
+
+class Server:
+    """A render job queue on one device (rt_server_start ... rt_server_stop)."""
+
+    def __init__(self, ctx, lanes=4, max_queue=0, device_budget_bytes=0):
+        self.ctx = ctx
+        self.h = C.c_void_p()
+        self._scenes = {}
+        o = ServerOpts(int(lanes), int(max_queue), int(device_budget_bytes))
+        _check(lib().rt_server_start(ctx.h, C.byref(o), C.byref(self.h)))
+
+    def submit(self, scene, spp, target_rmse=0.0, seed=0, sample_begin=0, block=32, **over):
+        """Queue a render of `scene`; with target_rmse > 0 it renders
+        progressively, at most `spp` samples.  Returns the job id."""
+        rd = scene.data.render_desc(spp, seed=seed, sample_begin=sample_begin, block=block, **over)
+        jid = C.c_int64()
+        _check(lib().rt_job_submit(self.h, scene.h, C.byref(rd), float(target_rmse), C.byref(jid)))
+        self._scenes[jid.value] = scene
+        return jid.value
+
+    @staticmethod
+    def _info(ji):
+        return dict(state=ji.state, spp_done=ji.spp_done, rmse_estimate=ji.rmse_estimate,
+                    queue_ms=ji.queue_ms, run_ms=ji.run_ms, error=ji.error.decode())
+
+    def poll(self, jid, fetch=False):
+        """(info, film): film is the (H, W, 4) result when `fetch` is set and
+        the job has finished (the job is then released), else None."""
+        ji = JobInfo()
+        sc = self._scenes.get(jid)
+        fetch = fetch and sc is not None
+        film = np.zeros((sc.height, sc.width, 4), np.float32) if fetch else None
+        _check(lib().rt_job_poll(self.h, jid, C.byref(ji), _p(film) if fetch else None))
+        info = self._info(ji)
+        if fetch and info["state"] in (JOB_DONE, JOB_FAILED):
+            self._scenes.pop(jid, None)
+            return info, (film if info["state"] == JOB_DONE else None)
+        return info, None
+
+    def wait(self, jid, timeout_ms=-1):
+        """Wait for a job, then (info, film) as poll(fetch=True)."""
+        ji = JobInfo()
+        sc = self._scenes.get(jid)
+        if sc is None:
+            raise RtError(1, "unknown job %d" % jid)
+        film = np.zeros((sc.height, sc.width, 4), np.float32)
+        _check(lib().rt_job_wait(self.h, jid, int(timeout_ms), C.byref(ji), _p(film)))
+        info = self._info(ji)
+        if info["state"] in (JOB_DONE, JOB_FAILED):
+            self._scenes.pop(jid, None)
+            return info, (film if info["state"] == JOB_DONE else None)
+        return info, None
+
+    def stop(self):
+        if self.h:
+            lib().rt_server_stop(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.stop()
+        except Exception:
+            pass
 
 
 BSDF_Q = np.dtype([("wi", np.float32, 3), ("wo", np.float32, 3), ("u", np.float32, 2)])

@@ -24,6 +24,8 @@
 #include <vector>
 #include <algorithm>
 
+#include "rt_internal.h"
+
 using namespace rtgpu;
 
 // =====================================================================
@@ -980,7 +982,7 @@ __global__ void __launch_bounds__(128) k_volpath(RenderParams P, int *work)
 // One thread per batch pixel: contributions in the order the reference's
 // tile loop produces them (pixels row-major, samples in order), restricted
 // to the 3x3 neighbourhood a box-filter splat can reach.
-__global__ void k_film(RenderParams P, float4 *film, int width)
+__global__ void k_film(RenderParams P, float4 *film, int width, int accumulate)
 {
     int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= P.npix) return;
@@ -1005,7 +1007,13 @@ __global__ void k_film(RenderParams P, float4 *film, int width)
             }
         }
     }
-    film[(size_t)to.y * width + to.x] = make_float4(0.f + r, 0.f + g, 0.f + b, 0.f + w);
+    float4 *px = &film[(size_t)to.y * width + to.x];
+    if (accumulate) {
+        float4 o = *px;
+        *px = make_float4(o.x + r, o.y + g, o.z + b, o.w + w);
+    } else {
+        *px = make_float4(0.f + r, 0.f + g, 0.f + b, 0.f + w);
+    }
     if (nan) atomicAdd(&P.stats[2], (unsigned long long)nan);
 }
 
@@ -1108,6 +1116,7 @@ struct rt_ctx {
     size_t ev_used = 0;
     int tile_key[4] = {-1, -1, -1, -1};
     std::vector<int> tile_start;
+    rt_lane_pool *pool = nullptr;   // worker lanes of rt_batch_render (rt_serve.cpp)
 };
 
 // kinds for per-kernel timing
@@ -1302,6 +1311,8 @@ static void free_wave(rt_ctx *c)
 rt_status rt_ctx_destroy(rt_ctx *c)
 {
     if (!c) return RT_OK;
+    if (c->pool) rt_lane_pool_destroy(c->pool);
+    c->pool = nullptr;
     cudaSetDevice(c->device);
     free_wave(c);
     cudaFree(c->tileorder);
@@ -1705,6 +1716,8 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
     if (rd->integrator == RT_INTEGRATOR_PATH_MIS && rd->strategy == RT_STRATEGY_ALL_LIGHTS)
         return fail(RT_ERR_UNSUPPORTED, "rt_render: all_lights strategy is not provided by the device path");
     if (rd->max_depth < 0 || rd->min_depth < 0) return fail(RT_ERR_INVALID, "rt_render: negative depth");
+    if (rd->flags & ~RT_RENDER_ACCUMULATE) return fail(RT_ERR_INVALID, "rt_render: unknown flags");
+    const int accumulate = (rd->flags & RT_RENDER_ACCUMULATE) ? 1 : 0;
     CK(cudaSetDevice(ctx->device));
     cudaStream_t st = ctx->stream;
     const DevCamera &cam = sc->S.cam;
@@ -1766,6 +1779,8 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
             ctx->film_n = npix_all;
         }
         film = ctx->film;
+        if (accumulate)
+            CK(cudaMemcpyAsync(film, film_rgbw, npix_all * sizeof(float4), cudaMemcpyHostToDevice, st));
     }
     // batch capacity: whole tiles, all samples of their pixels, about 4M paths
     const int cap_target = 1 << 22;
@@ -1866,7 +1881,7 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
         }
         int fb = (P.npix + 127) / 128;
         prof_begin(ctx, K_FILM);
-        k_film<<<fb, 128, 0, st>>>(P, film, Wd);
+        k_film<<<fb, 128, 0, st>>>(P, film, Wd, accumulate);
         prof_end(ctx);
         launches++;
         if ((s = launch_check("k_film")) != RT_OK) return s;
@@ -2207,11 +2222,84 @@ extern "C" rt_status rt_render_tile_static(rt_ctx *ctx, rt_scene *sc, const rt_r
             }
         }
     }
-    k_film<<<(int)((npix + 127) / 128), 128, 0, st>>>(Pm, reinterpret_cast<float4 *>(film_rgbw_device), Wd);
+    k_film<<<(int)((npix + 127) / 128), 128, 0, st>>>(Pm, reinterpret_cast<float4 *>(film_rgbw_device), Wd, 0);
     if ((s = launch_check("k_film (static)")) != RT_OK) return s;
     int limit = 0;
     CK(cudaMemcpyAsync(&limit, limit_flag, sizeof(int), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     if (limit) return fail(RT_ERR_LIMIT, "a device loop reached its iteration cap");
     return RT_OK;
+}
+
+// =====================================================================
+// internal hooks for the batch and server layer (rt_serve.cpp)
+// =====================================================================
+rt_status rt_internal_error(rt_status st, const char *msg) { return fail(st, msg ? msg : ""); }
+int rt_internal_device(const rt_ctx *c) { return c->device; }
+int rt_internal_bvh_width(const rt_ctx *c) { return c->bvh_width; }
+void *rt_internal_stream(const rt_ctx *c) { return (void *)c->stream; }
+rt_lane_pool *&rt_internal_pool(rt_ctx *c) { return c->pool; }
+void rt_internal_set_stats(rt_ctx *c, const rt_render_stats &s) { c->last = s; }
+void rt_internal_film_size(const rt_scene *sc, int *w, int *h)
+{
+    *w = sc->S.cam.width;
+    *h = sc->S.cam.height;
+}
+
+// partial sums of (a.rgb/a.w - b.rgb/b.w)^2 over pixels with weight in both
+__global__ void k_film_sqdiff(const float4 *a, const float4 *b, size_t npix, double *partial)
+{
+    __shared__ double sh[256];
+    double acc = 0.0;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < npix; i += (size_t)gridDim.x * blockDim.x) {
+        float4 x = a[i], y = b[i];
+        if (x.w > 0.f && y.w > 0.f) {
+            double dr = (double)x.x / x.w - (double)y.x / y.w;
+            double dg = (double)x.y / x.w - (double)y.y / y.w;
+            double db = (double)x.z / x.w - (double)y.z / y.w;
+            acc += dr * dr + dg * dg + db * db;
+        }
+    }
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
+}
+
+__global__ void k_film_add(float4 *dst, const float4 *src, size_t npix)
+{
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < npix; i += (size_t)gridDim.x * blockDim.x) {
+        float4 d = dst[i], s = src[i];
+        dst[i] = make_float4(d.x + s.x, d.y + s.y, d.z + s.z, d.w + s.w);
+    }
+}
+
+rt_status rt_internal_film_sqdiff(rt_ctx *c, const float *a, const float *b, size_t npix, double *mean_sq)
+{
+    CK(cudaSetDevice(c->device));
+    const int blocks = 256;
+    double *part = nullptr;
+    CK(cudaMalloc(&part, blocks * sizeof(double)));
+    k_film_sqdiff<<<blocks, 256, 0, c->stream>>>(reinterpret_cast<const float4 *>(a), reinterpret_cast<const float4 *>(b),
+                                                  npix, part);
+    double h[blocks];
+    cudaError_t e = cudaMemcpyAsync(h, part, sizeof(h), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(part);
+    if (e != cudaSuccess) return fail(RT_ERR_CUDA, std::string("film comparison: ") + cudaGetErrorString(e));
+    double s = 0.0;
+    for (int i = 0; i < blocks; i++) s += h[i];
+    *mean_sq = npix ? s / (3.0 * (double)npix) : 0.0;
+    return RT_OK;
+}
+
+rt_status rt_internal_film_add(rt_ctx *c, float *dst, const float *src, size_t npix)
+{
+    CK(cudaSetDevice(c->device));
+    k_film_add<<<std::max(1, std::min((int)((npix + 255) / 256), 1024)), 256, 0, c->stream>>>(
+        reinterpret_cast<float4 *>(dst), reinterpret_cast<const float4 *>(src), npix);
+    return launch_check("k_film_add");
 }

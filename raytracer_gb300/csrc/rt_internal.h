@@ -1,0 +1,28 @@
+// rt_internal.h -- hooks shared by the translation units of librtgpu.
+//
+// rt_api.cu owns contexts, scenes and kernels; rt_serve.cpp builds batched
+// and served rendering on top of the public C ABI and needs a few more
+// facts about a context.  Nothing here is exported.
+#pragma once
+#include <cstddef>
+
+#include "rtgpu.h"
+
+#define RT_HIDDEN __attribute__((visibility("hidden")))
+
+struct rt_lane_pool;   // worker lanes of rt_batch_render, owned by a context
+
+RT_HIDDEN rt_status rt_internal_error(rt_status st, const char *msg);   // sets rt_last_error()
+RT_HIDDEN int rt_internal_device(const rt_ctx *c);
+RT_HIDDEN int rt_internal_bvh_width(const rt_ctx *c);
+RT_HIDDEN void *rt_internal_stream(const rt_ctx *c);
+RT_HIDDEN rt_lane_pool *&rt_internal_pool(rt_ctx *c);
+RT_HIDDEN void rt_internal_set_stats(rt_ctx *c, const rt_render_stats &s);
+RT_HIDDEN void rt_internal_film_size(const rt_scene *sc, int *w, int *h);
+// mean over pixels and channels of (a.rgb / a.w - b.rgb / b.w)^2 for two
+// device films (pixels with zero weight in either are skipped); synchronous
+RT_HIDDEN rt_status rt_internal_film_sqdiff(rt_ctx *c, const float *a, const float *b, size_t npix, double *mean_sq);
+// dst += src for two device films, queued on the context's stream
+RT_HIDDEN rt_status rt_internal_film_add(rt_ctx *c, float *dst, const float *src, size_t npix);
+
+RT_HIDDEN void rt_lane_pool_destroy(rt_lane_pool *p);   // rt_serve.cpp

@@ -1,0 +1,438 @@
+// rt_serve.cpp -- batched and served rendering over the C ABI.
+//
+// The reference renders one scene per process: main() loads a scene file,
+// Scene::compute splits the film into tiles and a JobManager runs them on a
+// thread pool (core/main.cpp:439-447, core/Scene.cpp:83-101,
+// core/JobManager.cpp:41-58).  Many small jobs leave a 152-SM GPU mostly
+// idle when they run one after another: each render has a short wavefront
+// and a host round trip every few bounces.  Both entry points here keep
+// several renders in flight instead.
+//
+//   rt_batch_render  a list of (scene, render desc, film) jobs, largest
+//                    first, on `lanes` worker contexts: one CUDA stream,
+//                    wavefront buffers and host thread each.  Every film is
+//                    the one rt_render produces for that job alone.
+//   rt_server_*      a job queue served by the same kind of lanes.  A job
+//                    either renders its sample count in one call or, with a
+//                    target RMSE, renders progressively into two films of
+//                    interleaved sample ranges until the RMSE estimated
+//                    from their difference meets the target.
+#include <cuda_runtime_api.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "rt_internal.h"
+
+namespace {
+
+double now_ms()
+{
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+struct LaneSet {
+    int device = 0;
+    std::vector<rt_ctx *> lanes;
+
+    rt_status grow(int k, int bvh_width)
+    {
+        while ((int)lanes.size() < k) {
+            rt_ctx *c = nullptr;
+            rt_status s = rt_ctx_create(device, &c);
+            if (s != RT_OK) return s;
+            rt_ctx_set_bvh_width(c, bvh_width);
+            lanes.push_back(c);
+        }
+        for (rt_ctx *c : lanes) rt_ctx_set_bvh_width(c, bvh_width);
+        return RT_OK;
+    }
+    void clear()
+    {
+        for (rt_ctx *c : lanes) rt_ctx_destroy(c);
+        lanes.clear();
+    }
+};
+
+// first failure of a group of jobs run on several threads
+struct FirstError {
+    std::mutex mu;
+    rt_status status = RT_OK;
+    std::string msg;
+    void set(rt_status s)
+    {
+        std::lock_guard<std::mutex> g(mu);
+        if (status == RT_OK) {
+            status = s;
+            msg = rt_last_error();
+        }
+    }
+};
+
+void add_stats(rt_render_stats &a, const rt_render_stats &b)
+{
+    a.camera_ms += b.camera_ms;
+    a.trace_closest_ms += b.trace_closest_ms;
+    a.trace_any_ms += b.trace_any_ms;
+    a.shade_ms += b.shade_ms;
+    a.volpath_ms += b.volpath_ms;
+    a.film_ms += b.film_ms;
+    a.paths += b.paths;
+    a.closest_rays += b.closest_rays;
+    a.shadow_rays += b.shadow_rays;
+    a.launches += b.launches;
+    a.trace_closest_launches += b.trace_closest_launches;
+    a.trace_any_launches += b.trace_any_launches;
+    a.nodes_closest += b.nodes_closest;
+    a.tris_closest += b.tris_closest;
+    a.nodes_any += b.nodes_any;
+    a.tris_any += b.tris_any;
+    a.limit_hits += b.limit_hits;
+    a.nan_samples += b.nan_samples;
+}
+
+}  // namespace
+
+struct rt_lane_pool {
+    int want = 4;
+    LaneSet set;
+};
+
+void rt_lane_pool_destroy(rt_lane_pool *p)
+{
+    if (!p) return;
+    p->set.clear();
+    delete p;
+}
+
+static rt_lane_pool *pool_of(rt_ctx *ctx)
+{
+    rt_lane_pool *&p = rt_internal_pool(ctx);
+    if (!p) {
+        p = new rt_lane_pool();
+        p->set.device = rt_internal_device(ctx);
+    }
+    return p;
+}
+
+extern "C" rt_status rt_ctx_set_lanes(rt_ctx *ctx, int32_t lanes)
+{
+    if (!ctx) return rt_internal_error(RT_ERR_INVALID, "null ctx");
+    if (lanes < 1 || lanes > 16) return rt_internal_error(RT_ERR_INVALID, "lanes must be in 1..16");
+    pool_of(ctx)->want = lanes;
+    return RT_OK;
+}
+
+extern "C" rt_status rt_batch_render(rt_ctx *ctx, rt_scene *const *scenes, const rt_render_desc *descs, int32_t n,
+                                     float *const *films, int32_t on_device)
+{
+    if (!ctx || n < 0 || (n > 0 && (!scenes || !descs || !films)))
+        return rt_internal_error(RT_ERR_INVALID, "rt_batch_render: bad argument");
+    for (int i = 0; i < n; i++)
+        if (!scenes[i] || !films[i]) return rt_internal_error(RT_ERR_INVALID, "rt_batch_render: null scene or film");
+    if (n == 0) return RT_OK;
+    if (cudaSetDevice(rt_internal_device(ctx)) != cudaSuccess)
+        return rt_internal_error(RT_ERR_CUDA, "rt_batch_render: cudaSetDevice failed");
+    // work queued by the caller on the context's stream (e.g. clearing the
+    // films) completes before the lanes start on their own streams
+    if (cudaStreamSynchronize((cudaStream_t)rt_internal_stream(ctx)) != cudaSuccess)
+        return rt_internal_error(RT_ERR_CUDA, "rt_batch_render: stream synchronize failed");
+    rt_lane_pool *pool = pool_of(ctx);
+    const int k = std::min(pool->want, n);
+    rt_status s = pool->set.grow(k, rt_internal_bvh_width(ctx));
+    if (s != RT_OK) return s;
+    // largest job first, so that the long ones do not start last
+    std::vector<int> order(n);
+    std::vector<double> work(n);
+    for (int i = 0; i < n; i++) {
+        int w = 0, h = 0;
+        rt_internal_film_size(scenes[i], &w, &h);
+        work[i] = (double)w * h * std::max(1, descs[i].spp) * std::max(1, std::min(descs[i].max_depth, 64));
+        order[i] = i;
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return work[a] > work[b]; });
+    std::atomic<int> next(0);
+    FirstError err;
+    std::vector<rt_render_stats> lane_stats(k);
+    const double t0 = now_ms();
+    auto worker = [&](int li) {
+        rt_ctx *lane = pool->set.lanes[li];
+        std::memset(&lane_stats[li], 0, sizeof(rt_render_stats));
+        for (;;) {
+            int j = next.fetch_add(1);
+            if (j >= n) break;
+            int i = order[j];
+            rt_status st = rt_render(lane, scenes[i], &descs[i], films[i], on_device);
+            if (st != RT_OK) { err.set(st); continue; }
+            rt_render_stats one;
+            rt_render_stats_get(lane, &one);
+            add_stats(lane_stats[li], one);
+        }
+    };
+    if (k == 1) {
+        worker(0);
+    } else {
+        std::vector<std::thread> th;
+        for (int li = 0; li < k; li++) th.emplace_back(worker, li);
+        for (auto &t : th) t.join();
+    }
+    rt_render_stats tot;
+    std::memset(&tot, 0, sizeof(tot));
+    for (auto &ls : lane_stats) add_stats(tot, ls);
+    tot.kernel_ms = (float)(now_ms() - t0);   // wall time of the whole batch
+    rt_internal_set_stats(ctx, tot);
+    if (err.status != RT_OK) return rt_internal_error(err.status, err.msg.c_str());
+    return RT_OK;
+}
+
+// =====================================================================
+// server
+// =====================================================================
+namespace {
+
+struct Job {
+    rt_job_id id = 0;
+    rt_scene *scene = nullptr;
+    rt_render_desc desc;
+    float target = 0.f;
+    int w = 0, h = 0;
+    int64_t bytes = 0;
+    int state = RT_JOB_QUEUED;
+    int spp_done = 0;
+    float rmse = -1.f;
+    double t_submit = 0, t_start = 0, t_end = 0;
+    std::vector<float> film;
+    std::string error;
+};
+
+}  // namespace
+
+struct rt_server {
+    rt_ctx *parent = nullptr;
+    LaneSet set;
+    std::vector<std::thread> threads;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<Job *> queue;
+    std::unordered_map<rt_job_id, Job *> jobs;
+    bool stopping = false;
+    rt_job_id next_id = 1;
+    int max_queue = 4096;
+    int64_t budget = 0, in_flight = 0;
+};
+
+// One job on one lane.  Plain jobs are a single rt_render.  Progressive
+// jobs render chunks of k samples alternately into films A and B (A takes
+// samples [s, s+k), B [s+k, s+2k)), so A and B are independent estimates of
+// the same image; with equal counts the error of their average is
+// |A - B| / 2 per pixel in expectation, and the next chunk is sized from
+// the ratio of that estimate to the target.
+static rt_status run_job(rt_ctx *lane, Job *J)
+{
+    const size_t npix = (size_t)J->w * J->h;
+    J->film.assign(npix * 4, 0.f);
+    if (!(J->target > 0.f)) {
+        rt_status s = rt_render(lane, J->scene, &J->desc, J->film.data(), 0);
+        if (s == RT_OK) J->spp_done = J->desc.spp;
+        return s;
+    }
+    float *A = nullptr, *B = nullptr;
+    if (cudaMalloc((void **)&A, npix * 16) != cudaSuccess || cudaMalloc((void **)&B, npix * 16) != cudaSuccess) {
+        cudaFree(A);
+        return rt_internal_error(RT_ERR_NOMEM, "server: film allocation failed");
+    }
+    cudaStream_t st = (cudaStream_t)rt_internal_stream(lane);
+    rt_status s = RT_OK;
+    if (cudaMemsetAsync(A, 0, npix * 16, st) != cudaSuccess || cudaMemsetAsync(B, 0, npix * 16, st) != cudaSuccess)
+        s = rt_internal_error(RT_ERR_CUDA, "server: film clear failed");
+    const int cap = std::max(2, J->desc.spp);
+    int done = 0, k = std::max(1, std::min(cap / 2, 4));
+    double est = -1.0;
+    while (s == RT_OK) {
+        rt_render_desc d = J->desc;
+        d.flags |= RT_RENDER_ACCUMULATE;
+        d.spp = k;
+        d.sample_begin = J->desc.sample_begin + done;
+        if ((s = rt_render(lane, J->scene, &d, A, 1)) != RT_OK) break;
+        d.sample_begin += k;
+        if ((s = rt_render(lane, J->scene, &d, B, 1)) != RT_OK) break;
+        done += 2 * k;
+        double msq = 0.0;
+        if ((s = rt_internal_film_sqdiff(lane, A, B, npix, &msq)) != RT_OK) break;
+        est = std::sqrt(msq) * 0.5;
+        if (est <= J->target || cap - done < 2) break;
+        double need = done * (est / J->target) * (est / J->target) * 1.1;
+        int nk = (int)std::ceil((need - done) * 0.5);
+        k = std::max(1, std::min(nk, (cap - done) / 2));
+    }
+    if (s == RT_OK) s = rt_internal_film_add(lane, A, B, npix);
+    if (s == RT_OK && cudaMemcpyAsync(J->film.data(), A, npix * 16, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+        s = rt_internal_error(RT_ERR_CUDA, "server: film copy failed");
+    if (s == RT_OK && cudaStreamSynchronize(st) != cudaSuccess)
+        s = rt_internal_error(RT_ERR_CUDA, "server: stream synchronize failed");
+    cudaFree(A);
+    cudaFree(B);
+    J->spp_done = done;
+    J->rmse = (float)est;
+    return s;
+}
+
+static void serve(rt_server *S, int li)
+{
+    rt_ctx *lane = S->set.lanes[li];
+    cudaSetDevice(S->set.device);
+    for (;;) {
+        Job *J = nullptr;
+        {
+            std::unique_lock<std::mutex> g(S->mu);
+            S->cv_work.wait(g, [&] {
+                if (S->stopping) return true;
+                if (S->queue.empty()) return false;
+                Job *f = S->queue.front();
+                return S->budget <= 0 || S->in_flight == 0 || S->in_flight + f->bytes <= S->budget;
+            });
+            if (S->stopping) return;
+            J = S->queue.front();
+            S->queue.pop_front();
+            J->state = RT_JOB_RUNNING;
+            J->t_start = now_ms();
+            S->in_flight += J->bytes;
+        }
+        rt_status s = run_job(lane, J);
+        {
+            std::lock_guard<std::mutex> g(S->mu);
+            J->t_end = now_ms();
+            J->state = s == RT_OK ? RT_JOB_DONE : RT_JOB_FAILED;
+            if (s != RT_OK) J->error = rt_last_error();
+            S->in_flight -= J->bytes;
+        }
+        S->cv_done.notify_all();
+        S->cv_work.notify_all();
+    }
+}
+
+extern "C" rt_status rt_server_start(rt_ctx *ctx, const rt_server_opts *opts, rt_server **out)
+{
+    if (!ctx || !out) return rt_internal_error(RT_ERR_INVALID, "rt_server_start: null argument");
+    *out = nullptr;
+    int lanes = opts && opts->lanes > 0 ? opts->lanes : 4;
+    if (lanes > 16) return rt_internal_error(RT_ERR_INVALID, "rt_server_start: lanes must be in 1..16");
+    rt_server *S = new rt_server();
+    S->parent = ctx;
+    S->set.device = rt_internal_device(ctx);
+    S->max_queue = opts && opts->max_queue > 0 ? opts->max_queue : 4096;
+    S->budget = opts ? opts->device_budget_bytes : 0;
+    rt_status s = S->set.grow(lanes, rt_internal_bvh_width(ctx));
+    if (s != RT_OK) {
+        S->set.clear();
+        delete S;
+        return s;
+    }
+    for (int li = 0; li < lanes; li++) S->threads.emplace_back(serve, S, li);
+    *out = S;
+    return RT_OK;
+}
+
+extern "C" rt_status rt_job_submit(rt_server *S, rt_scene *scene, const rt_render_desc *desc, float target_rmse,
+                                   rt_job_id *id)
+{
+    if (!S || !scene || !desc || !id) return rt_internal_error(RT_ERR_INVALID, "rt_job_submit: null argument");
+    if (desc->spp <= 0) return rt_internal_error(RT_ERR_INVALID, "rt_job_submit: spp must be positive");
+    if (desc->flags & RT_RENDER_ACCUMULATE)
+        return rt_internal_error(RT_ERR_INVALID, "rt_job_submit: jobs render into their own film");
+    Job *J = new Job();
+    J->scene = scene;
+    J->desc = *desc;
+    J->target = target_rmse;
+    rt_internal_film_size(scene, &J->w, &J->h);
+    J->bytes = (int64_t)J->w * J->h * 16 * (target_rmse > 0.f ? 3 : 1);
+    std::lock_guard<std::mutex> g(S->mu);
+    if (S->stopping) { delete J; return rt_internal_error(RT_ERR_INVALID, "rt_job_submit: server is stopping"); }
+    if (S->budget > 0 && J->bytes > S->budget) {
+        delete J;
+        return rt_internal_error(RT_ERR_LIMIT, "rt_job_submit: job film exceeds the device budget");
+    }
+    if ((int)S->queue.size() >= S->max_queue) {
+        delete J;
+        return rt_internal_error(RT_ERR_LIMIT, "rt_job_submit: queue full");
+    }
+    J->id = S->next_id++;
+    J->t_submit = now_ms();
+    S->jobs[J->id] = J;
+    S->queue.push_back(J);
+    *id = J->id;
+    S->cv_work.notify_one();
+    return RT_OK;
+}
+
+// fills info; with a film pointer and a finished job, copies the film out
+// and forgets the job (caller holds S->mu)
+static rt_status report(rt_server *S, Job *J, rt_job_info *info, float *film)
+{
+    if (info) {
+        std::memset(info, 0, sizeof(*info));
+        info->state = J->state;
+        info->spp_done = J->spp_done;
+        info->rmse_estimate = J->rmse;
+        double t = now_ms();
+        double start = J->t_start > 0 ? J->t_start : t;
+        info->queue_ms = (float)(start - J->t_submit);
+        info->run_ms = J->t_start > 0 ? (float)((J->t_end > 0 ? J->t_end : t) - J->t_start) : 0.f;
+        std::strncpy(info->error, J->error.c_str(), sizeof(info->error) - 1);
+    }
+    if (film && (J->state == RT_JOB_DONE || J->state == RT_JOB_FAILED)) {
+        if (J->state == RT_JOB_DONE) std::memcpy(film, J->film.data(), J->film.size() * sizeof(float));
+        S->jobs.erase(J->id);
+        delete J;
+    }
+    return RT_OK;
+}
+
+extern "C" rt_status rt_job_poll(rt_server *S, rt_job_id id, rt_job_info *info, float *film)
+{
+    if (!S) return rt_internal_error(RT_ERR_INVALID, "rt_job_poll: null server");
+    std::lock_guard<std::mutex> g(S->mu);
+    auto it = S->jobs.find(id);
+    if (it == S->jobs.end()) return rt_internal_error(RT_ERR_INVALID, "rt_job_poll: unknown job");
+    return report(S, it->second, info, film);
+}
+
+extern "C" rt_status rt_job_wait(rt_server *S, rt_job_id id, int32_t timeout_ms, rt_job_info *info, float *film)
+{
+    if (!S) return rt_internal_error(RT_ERR_INVALID, "rt_job_wait: null server");
+    std::unique_lock<std::mutex> g(S->mu);
+    auto it = S->jobs.find(id);
+    if (it == S->jobs.end()) return rt_internal_error(RT_ERR_INVALID, "rt_job_wait: unknown job");
+    Job *J = it->second;
+    auto finished = [&] { return J->state == RT_JOB_DONE || J->state == RT_JOB_FAILED; };
+    if (timeout_ms < 0) S->cv_done.wait(g, finished);
+    else S->cv_done.wait_for(g, std::chrono::milliseconds(timeout_ms), finished);
+    return report(S, J, info, film);
+}
+
+extern "C" rt_status rt_server_stop(rt_server *S)
+{
+    if (!S) return RT_OK;
+    {
+        std::lock_guard<std::mutex> g(S->mu);
+        S->stopping = true;
+    }
+    S->cv_work.notify_all();
+    for (auto &t : S->threads) t.join();
+    // running jobs have finished; queued ones are dropped
+    for (auto &kv : S->jobs) delete kv.second;
+    S->jobs.clear();
+    S->set.clear();
+    delete S;
+    return RT_OK;
+}

@@ -330,16 +330,19 @@ class SceneData:
         self._keep = keep
         return D
 
-    def render_desc(self, spp, seed=0, sample_begin=0, block=32, **over):
+    def render_desc(self, spp, seed=0, sample_begin=0, block=32, flags=0, **over):
         it = dict(self.integrator)
         it.update(over)
         return RenderDesc(it["integrator"], it["max_depth"], it["min_depth"], it["strategy"],
-                          spp, sample_begin, seed, block, block, 0)
+                          spp, sample_begin, seed, block, block, flags)
 
     def bounds(self):
         lo = self.vertices.min(0) if len(self.vertices) else np.full(3, np.inf)
         hi = self.vertices.max(0) if len(self.vertices) else np.full(3, -np.inf)
         return lo, hi
+
+
+RENDER_ACCUMULATE = 1   # rt_render_desc.flags: add to the film instead of overwriting it
 
 
 # ---------------------------------------------------------------- cameras

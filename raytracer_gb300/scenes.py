@@ -189,8 +189,9 @@ def cornell_box(width=256, height=256):
 
 
 def displaced_icosphere(level=8, width=1024, height=1024, seed=0, alpha_bins=32,
-                        env_size=(1024, 512), max_depth=16):
-    """Config [1]: displaced icosphere on a ground quad under a sky."""
+                        env_size=(1024, 512), max_depth=16, env=None):
+    """Config [1]: displaced icosphere on a ground quad under a sky (`env`:
+    a precomputed sky_env image to share between scenes)."""
     s = SceneData()
     s.name = "displaced_icosphere_l%d_%d" % (level, width)
     v, f = icosphere(level)
@@ -224,7 +225,8 @@ def displaced_icosphere(level=8, width=1024, height=1024, seed=0, alpha_bins=32,
     ground = s.add_bsdf(bsdf(BSDF_DIFFUSE, albedo=(0.4, 0.4, 0.4)))
     gv, gf = _quad((-12, 0, -12), (-12, 0, 12), (12, 0, 12), (12, 0, -12))
     s.add_mesh(gv, gf, bsdf=ground)
-    env, _ = sky_env(*env_size)
+    if env is None:
+        env, _ = sky_env(*env_size)
     s.add_env_light(env)
     s.camera = camera(width, height, 40.0, look_at((0.0, 2.2, 5.2), (0.0, 1.0, 0.0), (0, 1, 0)))
     s.integrator = dict(integrator=INTEGRATOR_PATH_MIS, max_depth=max_depth, min_depth=3,
@@ -277,3 +279,22 @@ CONFIGS = {
     "displaced_icosphere_1024": lambda: displaced_icosphere(),
     "volume_grid_512": lambda: volume_grid(),
 }
+
+
+def batch_job(k, env=None):
+    """Job k of the 64-scene batch: triangles log-uniform in [1e3, 5e5]
+    (realised as the icosphere level nearest in log scale, 1,280 to 327,680
+    triangles), resolution uniform over {128, 256, 512, 1024} squared, spp
+    log-uniform in [4, 256], max depth 12, the displaced-icosphere material
+    mix under the sky.  Returns (SceneData, spp)."""
+    rng = np.random.default_rng(1000 + k)
+    tris = np.exp(rng.uniform(np.log(1e3), np.log(5e5)))
+    levels = np.arange(3, 8)
+    level = int(levels[np.argmin(np.abs(np.log(20.0 * 4.0 ** levels) - np.log(tris)))])
+    res = int(rng.choice([128, 256, 512, 1024]))
+    spp = int(round(np.exp(rng.uniform(np.log(4), np.log(256)))))
+    if env is None:
+        env, _ = sky_env(1024, 512)
+    s = displaced_icosphere(level=level, width=res, height=res, seed=k, max_depth=12, env=env)
+    s.name = "batch%02d_l%d_%d_%dspp" % (k, level, res, spp)
+    return s, spp

@@ -1,0 +1,119 @@
+"""Batched and served rendering (rt_batch_render, rt_server_*) against rt_render.
+
+The batch and server layers only schedule renders: every job runs the same
+kernels on the same per-path sample streams as a lone rt_render, so plain
+jobs must reproduce rt_render's film bit for bit.  Progressive jobs are
+checked statistically against a high-sample reference film.
+"""
+import numpy as np
+import pytest
+
+import raytracer_gb300 as R
+from raytracer_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def job_scenes(ctx, rtlib):
+    s = {
+        "cornell": rtlib.Scene(ctx, scenes.cornell_box(64, 48)),
+        "ragged": rtlib.Scene(ctx, scenes.cornell_box(37, 23)),
+        "ico": rtlib.Scene(ctx, scenes.displaced_icosphere(level=3, width=48, height=40, env_size=(64, 32))),
+        "vol": rtlib.Scene(ctx, scenes.volume_grid(40, 32, res=16)),
+    }
+    yield s
+    for g in s.values():
+        g.close()
+
+
+JOBS = [("cornell", 4, dict(seed=1)), ("ico", 2, dict(seed=2)), ("vol", 2, dict(seed=3)),
+        ("ragged", 3, dict(seed=4, block=8, sample_begin=5)), ("cornell", 2, dict(seed=9, max_depth=2)),
+        ("ico", 1, dict(seed=7))]
+
+
+def test_batch_matches_individual_renders(ctx, job_scenes):
+    ctx.set_lanes(3)
+    films = ctx.batch_render([(job_scenes[n], spp, opt) for n, spp, opt in JOBS])
+    st = ctx.stats()
+    paths = 0
+    for (n, spp, opt), f in zip(JOBS, films):
+        ref = job_scenes[n].render(spp, **opt)
+        assert np.array_equal(f, ref), n
+        paths += job_scenes[n].width * job_scenes[n].height * spp
+    assert st["paths"] == paths
+    ctx.set_lanes(1)   # one lane runs the jobs in order on the caller's thread
+    films1 = ctx.batch_render([(job_scenes[n], spp, opt) for n, spp, opt in JOBS[:2]])
+    for a, b in zip(films1, films[:2]):
+        assert np.array_equal(a, b)
+    ctx.set_lanes(4)
+
+
+def test_batch_reports_first_error_and_runs_the_rest(ctx, job_scenes):
+    jobs = [(job_scenes["cornell"], 2, dict(seed=1)), (job_scenes["ico"], 2, dict(seed=2, max_depth=-1))]
+    with pytest.raises(R.RtError) as e:
+        ctx.batch_render(jobs)
+    assert e.value.status == 1
+    with pytest.raises(R.RtError):
+        ctx.set_lanes(0)
+
+
+def test_accumulate_flag_adds_sample_ranges(job_scenes):
+    g = job_scenes["cornell"]
+    full = g.render(4, seed=5)
+    part = g.render(2, seed=5)
+    g.render(2, seed=5, sample_begin=2, accumulate=True, out=part)
+    assert np.array_equal(part[..., 3], full[..., 3])
+    np.testing.assert_allclose(part[..., :3], full[..., :3], rtol=1e-5, atol=1e-6)
+
+
+def test_server_plain_jobs_equal_rt_render(ctx, job_scenes):
+    srv = R.Server(ctx, lanes=3)
+    ids = [(srv.submit(job_scenes[n], spp, **opt), n, spp, opt) for n, spp, opt in JOBS]
+    for jid, n, spp, opt in ids:
+        info, film = srv.wait(jid)
+        assert info["state"] == R.JOB_DONE, info
+        assert info["spp_done"] == spp and info["rmse_estimate"] < 0
+        assert np.array_equal(film, job_scenes[n].render(spp, **opt)), n
+    with pytest.raises(R.RtError):
+        srv.poll(ids[0][0])          # released after its film was fetched
+    srv.stop()
+
+
+def test_server_progressive_meets_target(ctx, job_scenes):
+    g = job_scenes["cornell"]
+    ref = R.post_process(g.render(4096, seed=100))
+    srv = R.Server(ctx, lanes=2)
+    target = 0.04
+    jid = srv.submit(g, 2048, target_rmse=target, seed=11)
+    info, film = srv.wait(jid)
+    srv.stop()
+    assert info["state"] == R.JOB_DONE
+    true_rmse = float(np.sqrt(np.mean((R.post_process(film) - ref) ** 2)))
+    print("progressive: spp %d, estimated rmse %.4f, measured %.4f" % (info["spp_done"], info["rmse_estimate"], true_rmse))
+    assert info["rmse_estimate"] <= target or info["spp_done"] >= 2047
+    assert 4 <= info["spp_done"] < 2048
+    # the 4096-sample reference has its own error; the estimate is statistical
+    assert true_rmse < 2.0 * target
+    # the box filter's footprint quirk moves a few samples to a neighbour pixel
+    assert abs(film[..., 3].mean() - info["spp_done"]) <= 0.01 * info["spp_done"]
+
+
+def test_server_queue_states_and_stop(ctx, job_scenes):
+    srv = R.Server(ctx, lanes=1, max_queue=3)
+    g = job_scenes["ico"]
+    ids = [srv.submit(g, 8, seed=i) for i in range(3)]
+    with pytest.raises(R.RtError) as e:   # the queue holds at most 3 (one may already run)
+        for i in range(4):
+            ids.append(srv.submit(g, 8, seed=10 + i))
+    assert e.value.status == 3
+    states = [srv.poll(j)[0]["state"] for j in ids]
+    assert all(s in (R.JOB_QUEUED, R.JOB_RUNNING, R.JOB_DONE) for s in states)
+    info, film = srv.wait(ids[0])
+    assert info["state"] == R.JOB_DONE and film is not None
+    srv.stop()   # drops what is still queued without hanging
+    budget = R.Server(ctx, lanes=1, device_budget_bytes=1024)
+    with pytest.raises(R.RtError) as e:
+        budget.submit(g, 1)
+    assert e.value.status == 3
+    budget.stop()
