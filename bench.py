@@ -26,6 +26,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 CONFIG = dict(level=8, width=1024, height=1024, spp=64, max_depth=16, env=(1024, 512), seed=0)
+# --workload volume: 128^3 fBm grid medium + homogeneous slab + sphere light, VolPathTracing
+VOLUME = dict(volume=True, width=512, height=512, spp=128, max_depth=64, res=128, seed=0)
+VOLUME_WORKLOAD = "volume_grid_128cube_fbm_slab_spherelight_512x512_128spp_depth64"
 # --small: the same scene at 512x512, 8 spp, for profiler captures only
 SMALL = dict(width=512, height=512, spp=8)
 WORKLOAD = "displaced_icosphere_1310720tri_1024x1024_64spp_depth16_sky1024x512"
@@ -97,6 +100,9 @@ class ClockSampler:
 
 def make_scene():
     from raytracer_gb300 import scenes
+    if CONFIG.get("volume"):
+        return scenes.volume_grid(CONFIG["width"], CONFIG["height"], res=CONFIG["res"], seed=CONFIG["seed"],
+                                  max_depth=CONFIG["max_depth"])
     return scenes.displaced_icosphere(level=CONFIG["level"], width=CONFIG["width"], height=CONFIG["height"],
                                       seed=CONFIG["seed"], env_size=CONFIG["env"], max_depth=CONFIG["max_depth"])
 
@@ -143,16 +149,19 @@ def run_reference(args):
         times.append(time.time() - t0)
     samples = n * 32 * 32 * spp
     value = samples * len(times) / sum(times)
-    sample_desc = "%d of %d 32x32 tiles (%d path samples) per step, full 64 spp, %d threads" % (
-        n, (1024 // 32) ** 2, samples, threads)
+    W, H = CONFIG["width"], CONFIG["height"]
+    sample_desc = "%d of %d 32x32 tiles (%d path samples) per step, full %d spp, %d threads" % (
+        n, ((W + 31) // 32) * ((H + 31) // 32), samples, spp, threads)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * float(np.mean(times)),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded displaced icosphere + procedural sky)",
-            "config": {"workload": WORKLOAD, "integrator": "PathTracingMIS", "sample": sample_desc},
+            "data": "synthetic (seeded scene generator, no dataset)",
+            "config": {"workload": VOLUME_WORKLOAD if CONFIG.get("volume") else WORKLOAD,
+                       "integrator": "VolPathTracing" if CONFIG.get("volume") else "PathTracingMIS",
+                       "sample": sample_desc},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample_desc},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "notes": "reference CPU path = the oracle's C restatement of PathTracingMIS with the reference's "
+            "notes": "reference CPU path = the oracle's C restatement of the integrator with the reference's "
                      "two-level SAH BVH (the reference itself needs Eigen/SFML/OpenEXR/OpenVDB, absent here); "
                      "oracle scene build %.1f s not timed" % build_s}
     print(json.dumps(line))
@@ -216,7 +225,7 @@ def run_gpu(args):
         scene.render(spp, seed=1000 + k, sample_begin=sbase, film=film.data_ptr())
         st = ctx.stats()
         launches += st["launches"]
-        for key in ("trace_closest_ms", "trace_any_ms", "shade_ms", "camera_ms", "film_ms", "closest_rays",
+        for key in ("trace_closest_ms", "trace_any_ms", "shade_ms", "volpath_ms", "camera_ms", "film_ms", "closest_rays",
                     "shadow_rays", "trace_closest_launches", "trace_any_launches", "paths", "nan_samples"):
             agg[key] = agg.get(key, 0) + st[key]
     e1.record(stream)
@@ -245,6 +254,8 @@ def run_gpu(args):
     h2d = 64 + 4 * (len(data.lights) + 1)
     # roofline of the dominant kernel
     kern = {"trace_closest": agg["trace_closest_ms"], "trace_any": agg["trace_any_ms"], "shade": agg["shade_ms"]}
+    if CONFIG.get("volume"):
+        kern = {"volpath": agg["volpath_ms"]}
     dom = max(kern, key=kern.get)
     peaks, src = _peaks()
     rays_c, rays_a = agg["closest_rays"], agg["shadow_rays"]
@@ -260,19 +271,30 @@ def run_gpu(args):
         per_ray = S_RAY_IN + 4 + nodes_pr_a * S_NODE[args.bvh_width] + tris_pr_a * S_TRI
         algo_bytes = rays_a * per_ray
         nl = agg["trace_any_launches"]
-    else:
+    elif dom == "shade":
         per_ray = 2 * 128 + 2 * 32 + 64
         algo_bytes = rays_c * per_ray
         nl = max(agg["trace_closest_launches"], 1)
+    else:
+        # persistent VolPath megakernel: path state stays in registers; the
+        # streamed bytes are the camera ray and the film (the grid and the
+        # BVH of 36 triangles stay in L2), so an HBM roofline says little
+        per_ray = 32 + 16
+        algo_bytes = agg["paths"] * per_ray
+        nl = args.steps * max(1, int(round(agg["paths"] / max(args.steps, 1) / (1 << 22))))
     per_launch_bytes = algo_bytes / max(nl, 1)
     avg_launch_s = kern[dom] / 1000.0 / max(nl, 1)
     achieved = per_launch_bytes / max(avg_launch_s, 1e-12) / 1e9
+    # DRAM traffic per launch: bytes per ray measured by ncu on the small
+    # case of the same scene (profiles/trace_traffic.json) x rays per launch
     traffic = None
-    tf = os.path.join(ROOT, "profiles", "trace_closest_traffic.json")
-    if dom == "trace_closest" and os.path.exists(tf):
+    tf = os.path.join(ROOT, "profiles", "trace_traffic.json")
+    if dom in ("trace_closest", "trace_any") and args.bvh_width == 2 and not CONFIG.get("volume") \
+            and os.path.exists(tf):
         try:
             tj = json.load(open(tf))
-            traffic = tj.get("bytes_per_ray", 0) * rays_c / max(nl, 1)
+            key, rays = ("closest_bytes_per_ray", rays_c) if dom == "trace_closest" else ("any_bytes_per_ray", rays_a)
+            traffic = tj[key] * rays / max(nl, 1)
         except Exception:
             traffic = None
     rays_per_s = (rays_c + rays_a) * world / t_local
@@ -286,8 +308,8 @@ def run_gpu(args):
             cdt = time.time() - t0
             cpu_samples = n * 32 * 32 * spp
             res["cpu_baseline"] = {"value": cpu_samples / cdt, "unit": UNIT, "cores": threads, "kind": "port",
-                                   "sample": "%d of 1024 32x32 tiles at 64 spp (%d path samples), %.1f s" %
-                                             (n, cpu_samples, cdt)}
+                                   "sample": "%d of %d 32x32 tiles at %d spp (%d path samples), %.1f s" %
+                                             (n, ((W + 31) // 32) * ((H + 31) // 32), spp, cpu_samples, cdt)}
         except Exception as ex:  # the baseline never blocks the GPU line
             res["cpu_baseline"] = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                                    "sample": "failed: %s" % ex}
@@ -295,8 +317,11 @@ def run_gpu(args):
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-                "data": "synthetic (seeded displaced icosphere + procedural sky; no dataset)",
-                "config": {"workload": WORKLOAD, "integrator": "PathTracingMIS", "triangles": data.n_triangles,
+                "data": "synthetic (seeded scene generator: %s; no dataset)" % (
+                    "fBm grid medium" if CONFIG.get("volume") else "displaced icosphere + procedural sky"),
+                "config": {"workload": VOLUME_WORKLOAD if CONFIG.get("volume") else WORKLOAD,
+                           "integrator": "VolPathTracing" if CONFIG.get("volume") else "PathTracingMIS",
+                           "triangles": data.n_triangles,
                            "resolution": [W, H], "spp": spp, "bvh_width": args.bvh_width, "max_depth": CONFIG["max_depth"],
                            "samples_per_step": samples_per_step, "parallelism": "replicas" if world > 1 else "single",
                            "l2": "inputs larger than L2 (BVH+triangles %.0f MB, path state ~1 GB per batch)" %
@@ -433,7 +458,7 @@ def main():
                     help="profiler case: same scene at 512x512, 8 spp, no CPU baseline, no e2e")
     ap.add_argument("--bvh-width", type=int, default=2, choices=[2, 8],
                     help="traversal tree: binary BVH (default) or compressed 8-wide BVH")
-    ap.add_argument("--workload", default="icosphere", choices=["icosphere", "batch", "serve"],
+    ap.add_argument("--workload", default="icosphere", choices=["icosphere", "volume", "batch", "serve"],
                     help="icosphere: the headline single-scene render; batch: 64 scenes, plain vs "
                          "rt_batch_render; serve: Poisson arrivals through rt_server")
     ap.add_argument("--batch-jobs", type=int, default=64)
@@ -448,6 +473,9 @@ def main():
         return run_batch(args)
     if args.workload == "serve":
         return run_serve(args)
+    if args.workload == "volume":
+        CONFIG.clear()
+        CONFIG.update(VOLUME)
     if args.small:
         CONFIG.update(SMALL)
     if args.impl == "reference":

@@ -235,6 +235,24 @@ typedef struct rt_light_r {
     float pad;
 } rt_light_r;
 
+/* Medium queries (test hook): Medium::sampleDistance or
+ * Medium::transmittance (medium/Medium.h, Homogeneous.cpp:30-78,
+ * Heterogeneous.cpp:419-546) for a ray segment, drawing from the per-path
+ * sample stream of (seed, pixel, sample). */
+enum { RT_MEDIUM_OP_SAMPLE = 0, RT_MEDIUM_OP_TRANSMITTANCE = 1 };
+typedef struct rt_medium_q {
+    float o[3]; float mint;
+    float d[3]; float maxt;
+    uint64_t seed;
+    uint32_t pixel, sample;
+} rt_medium_q;
+typedef struct rt_medium_r {
+    float weight[3];         /* sample: MediumSamplingInfos weight; else Tr     */
+    float t;                 /* sample: distance reached (scatter point or maxT) */
+    int32_t scattered;       /* sample: 1 when the ray scattered in the medium  */
+    int32_t limit;           /* 1 when a tracking loop reached its cap          */
+} rt_medium_r;
+
 typedef struct rt_render_stats {
     double kernel_ms;        /* device time of the last render (events)          */
     double camera_ms;        /* per-kernel device time, summed over launches;    */
@@ -373,6 +391,10 @@ rt_status rt_bsdf_query(rt_ctx *ctx, rt_scene *scene, int32_t bsdf, int32_t op,
 /* Sample light `light` (Light::sample + Light::pdf) for n queries. */
 rt_status rt_light_query(rt_ctx *ctx, rt_scene *scene, int32_t light,
                          const rt_light_q *q, int32_t n, rt_light_r *r);
+
+/* Sample or evaluate medium `medium` of the scene for n queries. */
+rt_status rt_medium_query(rt_ctx *ctx, rt_scene *scene, int32_t medium, int32_t op,
+                          const rt_medium_q *q, int32_t n, rt_medium_r *r);
 
 #ifdef __cplusplus
 }

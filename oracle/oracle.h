@@ -228,6 +228,10 @@ int32_t oracle_bsdf_query(const rt_bsdf_desc *b, int32_t op, const rt_bsdf_q *q,
                           rt_bsdf_r *r);
 int32_t oracle_light_query(const o_scene *sc, int32_t light, const rt_light_q *q, int32_t n,
                            rt_light_r *r);
+/* Medium::sampleDistance / Medium::transmittance for n ray segments, each
+ * drawing from the path stream (seed, pixel, sample) (rt_medium_query). */
+int32_t oracle_medium_query(const o_scene *sc, int32_t medium, int32_t op, const rt_medium_q *q, int32_t n,
+                            rt_medium_r *r);
 void oracle_pcg_stream(uint64_t initstate, uint64_t initseq, int32_t n, uint32_t *out);
 void oracle_cdf_sample_reuse(const float *pdfs, int32_t n, const float *u, int32_t m,
                              int32_t *index, float *u_out, float *pdf_out, float *sum_out);

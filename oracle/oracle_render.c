@@ -775,6 +775,29 @@ int32_t oracle_light_query(const o_scene *sc, int32_t light, const rt_light_q *q
     return RT_OK;
 }
 
+int32_t oracle_medium_query(const o_scene *sc, int32_t medium, int32_t op, const rt_medium_q *q, int32_t n,
+                            rt_medium_r *r)
+{
+    if (medium < 0 || medium >= sc->d->n_media) return RT_ERR_INVALID;
+    for (int i = 0; i < n; i++) {
+        o_sampler s;
+        o_sampler_seed_path(&s, q[i].seed, q[i].pixel, q[i].sample);
+        o_ray ray = o_ray_make(v3_from(q[i].o), v3_from(q[i].d), q[i].mint, q[i].maxt);
+        memset(&r[i], 0, sizeof(r[i]));
+        c3 w;
+        if (op == RT_MEDIUM_OP_SAMPLE) {
+            float t = 0.f;
+            c3 em;
+            r[i].scattered = o_medium_sample_distance(sc, medium, &ray, &s, &t, &w, &em);
+            r[i].t = t;
+        } else {
+            w = o_medium_transmittance(sc, medium, &ray, &s);
+        }
+        r[i].weight[0] = w.r; r[i].weight[1] = w.g; r[i].weight[2] = w.b;
+    }
+    return RT_OK;
+}
+
 void oracle_pcg_stream(uint64_t initstate, uint64_t initseq, int32_t n, uint32_t *out)
 {
     o_pcg32 r;

@@ -71,6 +71,7 @@ def lib():
     L.rt_render_tile_static.restype = C.c_int32
     L.rt_bsdf_query.argtypes = [vp, vp, C.c_int32, C.c_int32, vp, C.c_int32, vp]
     L.rt_light_query.argtypes = [vp, vp, C.c_int32, vp, C.c_int32, vp]
+    L.rt_medium_query.argtypes = [vp, vp, C.c_int32, C.c_int32, vp, C.c_int32, vp]
     L.rt_batch_render.argtypes = [vp, C.POINTER(vp), C.POINTER(D.RenderDesc), C.c_int32, C.POINTER(vp), C.c_int32]
     L.rt_ctx_set_lanes.argtypes = [vp, C.c_int32]
     L.rt_server_start.argtypes = [vp, C.POINTER(ServerOpts), C.POINTER(vp)]
@@ -80,7 +81,7 @@ def lib():
     L.rt_server_stop.argtypes = [vp]
     for name in ("rt_ctx_create", "rt_ctx_destroy", "rt_ctx_set_stream", "rt_scene_create", "rt_scene_destroy",
                  "rt_scene_info", "rt_render", "rt_render_stats_get", "rt_ctx_set_profiling", "rt_ctx_set_bvh_width",
-                 "rt_trace", "rt_bsdf_query", "rt_light_query", "rt_batch_render", "rt_ctx_set_lanes",
+                 "rt_trace", "rt_bsdf_query", "rt_light_query", "rt_medium_query", "rt_batch_render", "rt_ctx_set_lanes",
                  "rt_server_start", "rt_job_submit", "rt_job_poll", "rt_job_wait", "rt_server_stop"):
         getattr(L, name).restype = C.c_int32
     _lib = L
@@ -230,6 +231,13 @@ class Scene:
         _check(lib().rt_light_query(self.ctx.h, self.h, light, _p(q), len(q), _p(r)))
         return r
 
+    def medium_query(self, medium, op, q):
+        """Medium::sampleDistance (op 0) or transmittance (op 1) for MEDIUM_Q records."""
+        q = np.ascontiguousarray(q, MEDIUM_Q)
+        r = np.zeros(len(q), MEDIUM_R)
+        _check(lib().rt_medium_query(self.ctx.h, self.h, medium, op, _p(q), len(q), _p(r)))
+        return r
+
 
 class Server:
     """A render job queue on one device (rt_server_start ... rt_server_stop)."""
@@ -302,6 +310,10 @@ LIGHT_Q = np.dtype([("p", np.float32, 3), ("u", np.float32, 2)])
 LIGHT_R = np.dtype([("intensity", np.float32, 3), ("pdf", np.float32), ("to_light", np.float32, 3),
                     ("distance", np.float32), ("point", np.float32, 3), ("normal", np.float32, 3),
                     ("pdf_eval", np.float32), ("pad", np.float32)])
+MEDIUM_Q = np.dtype([("o", np.float32, 3), ("mint", np.float32), ("d", np.float32, 3), ("maxt", np.float32),
+                     ("seed", np.uint64), ("pixel", np.uint32), ("sample", np.uint32)])
+MEDIUM_R = np.dtype([("weight", np.float32, 3), ("t", np.float32), ("scattered", np.int32), ("limit", np.int32)])
+MEDIUM_OP_SAMPLE, MEDIUM_OP_TRANSMITTANCE = 0, 1
 assert BSDF_Q.itemsize == C.sizeof(D.BsdfQ) and BSDF_R.itemsize == C.sizeof(D.BsdfR)
 assert LIGHT_Q.itemsize == C.sizeof(D.LightQ) and LIGHT_R.itemsize == C.sizeof(D.LightR)
 

@@ -762,7 +762,36 @@ __global__ void __launch_bounds__(128) k_pt_shade(RenderParams P, int round)
 
 // ---------------------------------------------------------------- VolPathTracing
 // Integrator::evalTransmittance (Integrator.cpp:81-133)
-__device__ C3 eval_transmittance(const DevScene &S, Ray ray, int medium, Pcg32 &rng, int &limit)
+// Out-of-line copies of the helpers the VolPath code calls from many sites.
+// Inlined, every call site carried its own BVH traversal, tracking loop and
+// BSDF switch; the resulting kernel missed the instruction cache on most
+// issues.  One out-of-line copy each keeps the hot code small.
+__device__ __noinline__ bool vp_trace(const DevScene &S, V3 o, V3 d, float mint, float maxt, Hit &h)
+{
+    return trace_ray<false>(S, o, d, mint, maxt, h);
+}
+__device__ __noinline__ Frame vp_frame(const DevScene &S, const Hit &h, V3 o, V3 d) { return hit_frame(S, h, o, d); }
+__device__ __noinline__ C3 vp_medium_tr(const DevMedium &m, Ray r, Pcg32 &rng, int &limit)
+{
+    return medium_tr(m, r, rng, limit);
+}
+__device__ __noinline__ bool vp_medium_sample(const DevMedium &m, Ray r, Pcg32 &rng, float &t, C3 &w, C3 &em, int &limit)
+{
+    return medium_sample(m, r, rng, t, w, em, limit);
+}
+__device__ __noinline__ C3 vp_bsdf_sample(const DevBsdf &b, BsdfRec &r, V2 u) { return bsdf_sample(b, r, u); }
+__device__ __noinline__ C3 vp_bsdf_eval(const DevBsdf &b, V3 wi, V3 wo) { return bsdf_eval(b, wi, wo); }
+__device__ __noinline__ float vp_bsdf_pdf(const DevBsdf &b, V3 wi, V3 wo) { return bsdf_pdf(b, wi, wo); }
+__device__ __noinline__ void vp_light_sample(const DevScene &S, int idx, V3 p, V2 u, LightRec &li)
+{
+    light_sample(S, idx, p, u, li);
+}
+__device__ __noinline__ float vp_light_pdf(const DevScene &S, int l, V3 p, V3 lp, V3 ln, V3 dir)
+{
+    return light_pdf(S, l, p, lp, ln, dir);
+}
+
+__device__ __noinline__ C3 eval_transmittance(const DevScene &S, Ray ray, int medium, Pcg32 &rng, int &limit)
 {
     Ray tr = ray;
     C3 T = cfill(1.f);
@@ -770,15 +799,15 @@ __device__ C3 eval_transmittance(const DevScene &S, Ray ray, int medium, Pcg32 &
     bool first = true;
     for (int guard = 0; guard < 4096; guard++) {
         Hit h;
-        bool inter = trace_ray<false>(S, tr.o, tr.d, tr.mint, tr.maxt, h);
+        bool inter = vp_trace(S, tr.o, tr.d, tr.mint, tr.maxt, h);
         if (inter && prim_bsdf(S, h.prim) >= 0) return cfill(0.f);
         if (inter) dist -= h.t;
         if (medium >= 0)
-            T = T * medium_tr(S.media[medium], make_ray(tr.o, tr.d, first ? tr.mint : 0.f, inter ? h.t : dist), rng, limit);
+            T = T * vp_medium_tr(S.media[medium], make_ray(tr.o, tr.d, first ? tr.mint : 0.f, inter ? h.t : dist), rng, limit);
         first = false;
         if (!inter || iszero(T)) return T;
         V3 np = tr.o + h.t * tr.d;
-        Frame f = hit_frame(S, h, tr.o, tr.d);
+        Frame f = vp_frame(S, h, tr.o, tr.d);
         tr = make_ray(np, tr.d, RT_EPSILON, dist);
         if (prim_interior(S, h.prim) != prim_exterior(S, h.prim))
             medium = dot(f.n, tr.d) < 0.f ? prim_interior(S, h.prim) : prim_exterior(S, h.prim);
@@ -788,7 +817,7 @@ __device__ C3 eval_transmittance(const DevScene &S, Ray ray, int medium, Pcg32 &
 }
 
 // VolPathTracing::evalTransmittanceFromSampledBSDF (VolPathTracing.cpp:369-424)
-__device__ C3 eval_tr_sampled(const DevScene &S, Ray ray, Pcg32 &rng, int medium, Hit &h, Frame &fr, bool &was,
+__device__ __noinline__ C3 eval_tr_sampled(const DevScene &S, Ray ray, Pcg32 &rng, int medium, Hit &h, Frame &fr, bool &was,
                               int &newm, int &limit)
 {
     Ray tr = ray;
@@ -797,10 +826,10 @@ __device__ C3 eval_tr_sampled(const DevScene &S, Ray ray, Pcg32 &rng, int medium
     was = false;
     for (int guard = 0; guard < 4096; guard++) {
         Hit nh;
-        was = trace_ray<false>(S, tr.o, tr.d, tr.mint, tr.maxt, nh);
-        if (was) { h = nh; fr = hit_frame(S, h, tr.o, tr.d); }
+        was = vp_trace(S, tr.o, tr.d, tr.mint, tr.maxt, nh);
+        if (was) { h = nh; fr = vp_frame(S, h, tr.o, tr.d); }
         if (medium >= 0)
-            T = T * medium_tr(S.media[medium], make_ray(tr.o, tr.d, first ? tr.mint : 0.f, was ? h.t : tr.maxt), rng, limit);
+            T = T * vp_medium_tr(S.media[medium], make_ray(tr.o, tr.d, first ? tr.mint : 0.f, was ? h.t : tr.maxt), rng, limit);
         if (was && prim_bsdf(S, h.prim) >= 0) return T;
         first = false;
         if (!was || iszero(T)) return T;
@@ -816,14 +845,14 @@ __device__ C3 eval_tr_sampled(const DevScene &S, Ray ray, Pcg32 &rng, int medium
 }
 
 // Integrator::sampleAttenuatedLightDirect (Integrator.cpp:137-172)
-__device__ C3 sample_attenuated_light(const DevScene &S, V3 p, Pcg32 &rng, LightRec &li, int medium, int &limit)
+__device__ __noinline__ C3 sample_attenuated_light(const DevScene &S, V3 p, Pcg32 &rng, LightRec &li, int medium, int &limit)
 {
     C3 value = cfill(0.f);
     if (S.n_lights == 0) return value;
     V2 u = next2d(rng);
     float lw;
     int idx = cdf_sample_reuse(S.light_cdf, S.n_lights + 1, u.x, lw);
-    light_sample(S, idx, p, u, li);
+    vp_light_sample(S, idx, p, u, li);
     if (li.pdf > 0 && lum(li.intensity) > 0) {
         C3 tr = eval_transmittance(S, make_ray(p, li.to_light, RT_EPSILON, li.distance - RT_EPSILON), medium, rng, limit);
         li.pdf *= lw;
@@ -833,146 +862,193 @@ __device__ C3 sample_attenuated_light(const DevScene &S, V3 p, Pcg32 &rng, Light
 }
 
 // VolPathTracing::li (VolPathTracing.cpp:25-367)
-__device__ C3 li_volpath(const DevScene &S, Ray ray, Pcg32 &rng, int max_depth, int min_depth, int &limit)
+// One VolPathTracing path as a resumable state: vol_start traces the camera
+// ray, each vol_step runs one pass of the bounce loop of
+// VolPathTracing::li (VolPathTracing.cpp:25-367) and returns false once the
+// path has finished (its radiance is then in L).  The draws from the path's
+// sample stream come in the same order as one uninterrupted loop.
+struct VolState {
+    C3 L, T;
+    float eta;
+    int depth, medium, guard;
+    bool emission, was;
+    Ray ray;
+    Hit h;
+    Frame fr;
+};
+
+__device__ __forceinline__ void vol_start(const DevScene &S, VolState &st, Ray ray)
 {
-    C3 L = cfill(0.f), T = cfill(1.f);
-    float eta = 1.f;
-    int depth = 0;
-    bool emission = true;
-    const int env = S.env_light;
-    Hit h; h.t = RT_MAX_REAL; h.u = h.v = 0.f; h.prim = -1;
-    Frame fr; fr.p = v3(0, 0, 0); fr.n = fr.s = fr.t = v3(0, 0, 0);
+    st.L = cfill(0.f); st.T = cfill(1.f);
+    st.eta = 1.f;
+    st.depth = 0;
+    st.emission = true;
+    st.h.t = RT_MAX_REAL; st.h.u = st.h.v = 0.f; st.h.prim = -1;
+    st.fr.p = v3(0, 0, 0); st.fr.n = st.fr.s = st.fr.t = v3(0, 0, 0);
+    st.ray = ray;
     Hit nh;
-    bool was = trace_ray<false>(S, ray.o, ray.d, ray.mint, ray.maxt, nh);
-    if (was) { h = nh; fr = hit_frame(S, h, ray.o, ray.d); }
-    int medium = S.cam.medium;
-    int guard = 0;
-    while (depth < max_depth) {
-        if (++guard > (1 << 16)) { limit = 1; break; }
-        float t = 0.f;
-        C3 wm = cfill(0.f), em = cfill(0.f);
-        bool scattered = false;
-        if (medium >= 0) scattered = medium_sample(S.media[medium], make_ray(ray.o, ray.d, ray.mint, h.t), rng, t, wm, em, limit);
-        if (scattered) {
-            const DevMedium &M = S.media[medium];
-            L = L + T * em;
-            T = T * wm;
-            fr.p = ray.o + t * ray.d;
-            LightRec li;
-            li.point = li.to_light = li.normal = v3(0, 0, 0);
-            li.intensity = cfill(0.f); li.distance = 0.f; li.pdf = 0.f;
-            C3 value = sample_attenuated_light(S, fr.p, rng, li, medium, limit);
-            if (!iszero(value)) {
-                float pf = phase_eval(M, li.to_light, -ray.d);
-                float w = power_heuristic(li.pdf, pf);
-                float ev = phase_eval(M, li.to_light, -ray.d);
-                L = L + ((T * value) * ev) * w;
-            }
-            V3 wo; float pfpdf;
-            float pfw = phase_sample(M, -ray.d, next2d(rng), wo, pfpdf);
-            ray = make_ray(fr.p, wo, 0.f, ray.maxt);
-            int newm = -1;
-            C3 tr = eval_tr_sampled(S, ray, rng, medium, h, fr, was, newm, limit);
-            T = T * pfw;
-            if (was) {
-                int hl = prim_light(S, h.prim);
-                if (hl >= 0) {
-                    C3 Le = area_le(S, hl, -ray.d, fr.n);
-                    float pl = light_pdf(S, hl, fr.p, li.point, li.normal, li.to_light);
-                    float w = power_heuristic(pfpdf, pl);
-                    L = L + ((T * Le) * tr) * w;
-                }
-            }
-        } else {
-            if (medium >= 0) {
-                L = L + T * em;
-                T = T * wm;
-            }
-            if (!was) {
-                if (emission && env >= 0) L = L + T * env_le(S.lights[env], ray.d);
-                return L;
-            }
-            int b = prim_bsdf(S, h.prim);
-            if (b < 0) {
-                ray = make_ray(fr.p, ray.d, RT_EPSILON, RT_MAX_REAL);
-                if (prim_interior(S, h.prim) != prim_exterior(S, h.prim))
-                    medium = dot(fr.n, ray.d) < 0.f ? prim_interior(S, h.prim) : prim_exterior(S, h.prim);
-                was = trace_ray<false>(S, ray.o, ray.d, ray.mint, ray.maxt, nh);
-                if (was) { h = nh; fr = hit_frame(S, h, ray.o, ray.d); }
-                continue;
-            }
-            const DevBsdf &B = S.bsdfs[b];
-            int hl = prim_light(S, h.prim);
-            if (emission && hl >= 0) L = L + T * area_le(S, hl, -ray.d, fr.n);
-            LightRec li;
-            li.point = li.to_light = li.normal = v3(0, 0, 0);
-            li.intensity = cfill(0.f); li.distance = 0.f; li.pdf = 0.f;
-            C3 value = sample_attenuated_light(S, fr.p, rng, li, medium, limit);
-            if (!iszero(value)) {
-                V3 wi = to_local(fr, li.to_light), wo = to_local(fr, -ray.d);
-                float ct = fabsf(wi.z);
-                float bp = bsdf_pdf(B, wi, wo);
-                float w = power_heuristic(li.pdf, bp);
-                L = L + (((T * value) * bsdf_eval(B, wi, wo)) * ct) * w;
-            }
-            BsdfRec r;
-            r.wi = to_local(fr, -ray.d); r.wo = v3(0, 0, 0);
-            r.type = BT_ALL; r.rel_eta = 1.f; r.pdf = -1.f;
-            C3 f = bsdf_sample(B, r, next2d(rng));
-            if (iszero(f)) break;
-            V3 pfrom = fr.p;
-            ray = make_ray(fr.p, to_world(fr, r.wo), RT_EPSILON, RT_MAX_REAL);
-            if (prim_interior(S, h.prim) != prim_exterior(S, h.prim))
-                medium = dot(fr.n, ray.d) < 0.f ? prim_interior(S, h.prim) : prim_exterior(S, h.prim);
-            int caught = -1;
-            bool isenv = false;
-            C3 Le = cfill(0.f);
-            int newm = -1;
-            C3 tr = eval_tr_sampled(S, ray, rng, medium, h, fr, was, newm, limit);
-            if (was) {
-                int nl = prim_light(S, h.prim);
-                if (nl >= 0) { caught = nl; Le = area_le(S, nl, -ray.d, fr.n); }
-            } else if (newm < 0) {
-                if (env >= 0) { caught = env; isenv = true; Le = env_le(S.lights[env], ray.d); }
-            }
-            if (caught >= 0) {
-                float pl = (r.type & BT_DELTA) ? 0.f : light_pdf(S, caught, pfrom, fr.p, fr.n, ray.d);
-                float w = power_heuristic(r.pdf, pl);
-                L = L + (((T * Le) * f) * tr) * w;
-                if (isenv && medium < 0) return L;
-            }
-            T = T * f;
-            eta *= r.rel_eta;
-        }
-        if (depth >= min_depth) {
-            float stop = smin(0.95f, cmax(T) * eta * eta);
-            if (next1d(rng) < stop) T = T / stop;
-            else return L;
-        }
-        was = trace_ray<false>(S, ray.o, ray.d, ray.mint, ray.maxt, nh);
-        if (was) { h = nh; fr = hit_frame(S, h, ray.o, ray.d); }
-        emission = false;
-        depth++;
-    }
-    return L;
+    st.was = vp_trace(S, ray.o, ray.d, ray.mint, ray.maxt, nh);
+    if (st.was) { st.h = nh; st.fr = vp_frame(S, nh, ray.o, ray.d); }
+    st.medium = S.cam.medium;
+    st.guard = 0;
 }
 
-// persistent: warps take 32 paths at a time from the batch (path regeneration)
+__device__ bool vol_step(const DevScene &S, VolState &st, Pcg32 &rng, int max_depth, int min_depth, int &limit)
+{
+    if (st.depth >= max_depth) return false;
+    if (++st.guard > (1 << 16)) { limit = 1; return false; }
+    const int env = S.env_light;
+    Ray &ray = st.ray;
+    Hit &h = st.h;
+    Frame &fr = st.fr;
+    C3 &L = st.L, &T = st.T;
+    bool &was = st.was;
+    int &medium = st.medium;
+    Hit nh;
+    float t = 0.f;
+    C3 wm = cfill(0.f), em = cfill(0.f);
+    bool scattered = false;
+    if (medium >= 0) scattered = vp_medium_sample(S.media[medium], make_ray(ray.o, ray.d, ray.mint, h.t), rng, t, wm, em, limit);
+    if (scattered) {
+        const DevMedium &M = S.media[medium];
+        L = L + T * em;
+        T = T * wm;
+        fr.p = ray.o + t * ray.d;
+        LightRec li;
+        li.point = li.to_light = li.normal = v3(0, 0, 0);
+        li.intensity = cfill(0.f); li.distance = 0.f; li.pdf = 0.f;
+        C3 value = sample_attenuated_light(S, fr.p, rng, li, medium, limit);
+        if (!iszero(value)) {
+            float pf = phase_eval(M, li.to_light, -ray.d);
+            float w = power_heuristic(li.pdf, pf);
+            float ev = phase_eval(M, li.to_light, -ray.d);
+            L = L + ((T * value) * ev) * w;
+        }
+        V3 wo; float pfpdf;
+        float pfw = phase_sample(M, -ray.d, next2d(rng), wo, pfpdf);
+        ray = make_ray(fr.p, wo, 0.f, ray.maxt);
+        int newm = -1;
+        C3 tr = eval_tr_sampled(S, ray, rng, medium, h, fr, was, newm, limit);
+        T = T * pfw;
+        if (was) {
+            int hl = prim_light(S, h.prim);
+            if (hl >= 0) {
+                C3 Le = area_le(S, hl, -ray.d, fr.n);
+                float pl = vp_light_pdf(S, hl, fr.p, li.point, li.normal, li.to_light);
+                float w = power_heuristic(pfpdf, pl);
+                L = L + ((T * Le) * tr) * w;
+            }
+        }
+    } else {
+        if (medium >= 0) {
+            L = L + T * em;
+            T = T * wm;
+        }
+        if (!was) {
+            if (st.emission && env >= 0) L = L + T * env_le(S.lights[env], ray.d);
+            return false;
+        }
+        int b = prim_bsdf(S, h.prim);
+        if (b < 0) {
+            // null boundary: pass through without a bounce (no depth, no RR)
+            ray = make_ray(fr.p, ray.d, RT_EPSILON, RT_MAX_REAL);
+            if (prim_interior(S, h.prim) != prim_exterior(S, h.prim))
+                medium = dot(fr.n, ray.d) < 0.f ? prim_interior(S, h.prim) : prim_exterior(S, h.prim);
+            was = vp_trace(S, ray.o, ray.d, ray.mint, ray.maxt, nh);
+            if (was) { h = nh; fr = vp_frame(S, h, ray.o, ray.d); }
+            return true;
+        }
+        const DevBsdf &B = S.bsdfs[b];
+        int hl = prim_light(S, h.prim);
+        if (st.emission && hl >= 0) L = L + T * area_le(S, hl, -ray.d, fr.n);
+        LightRec li;
+        li.point = li.to_light = li.normal = v3(0, 0, 0);
+        li.intensity = cfill(0.f); li.distance = 0.f; li.pdf = 0.f;
+        C3 value = sample_attenuated_light(S, fr.p, rng, li, medium, limit);
+        if (!iszero(value)) {
+            V3 wi = to_local(fr, li.to_light), wo = to_local(fr, -ray.d);
+            float ct = fabsf(wi.z);
+            float bp = vp_bsdf_pdf(B, wi, wo);
+            float w = power_heuristic(li.pdf, bp);
+            L = L + (((T * value) * vp_bsdf_eval(B, wi, wo)) * ct) * w;
+        }
+        BsdfRec r;
+        r.wi = to_local(fr, -ray.d); r.wo = v3(0, 0, 0);
+        r.type = BT_ALL; r.rel_eta = 1.f; r.pdf = -1.f;
+        C3 f = vp_bsdf_sample(B, r, next2d(rng));
+        if (iszero(f)) return false;
+        V3 pfrom = fr.p;
+        ray = make_ray(fr.p, to_world(fr, r.wo), RT_EPSILON, RT_MAX_REAL);
+        if (prim_interior(S, h.prim) != prim_exterior(S, h.prim))
+            medium = dot(fr.n, ray.d) < 0.f ? prim_interior(S, h.prim) : prim_exterior(S, h.prim);
+        int caught = -1;
+        bool isenv = false;
+        C3 Le = cfill(0.f);
+        int newm = -1;
+        C3 tr = eval_tr_sampled(S, ray, rng, medium, h, fr, was, newm, limit);
+        if (was) {
+            int nl = prim_light(S, h.prim);
+            if (nl >= 0) { caught = nl; Le = area_le(S, nl, -ray.d, fr.n); }
+        } else if (newm < 0) {
+            if (env >= 0) { caught = env; isenv = true; Le = env_le(S.lights[env], ray.d); }
+        }
+        if (caught >= 0) {
+            float pl = (r.type & BT_DELTA) ? 0.f : vp_light_pdf(S, caught, pfrom, fr.p, fr.n, ray.d);
+            float w = power_heuristic(r.pdf, pl);
+            L = L + (((T * Le) * f) * tr) * w;
+            if (isenv && medium < 0) return false;
+        }
+        T = T * f;
+        st.eta *= r.rel_eta;
+    }
+    if (st.depth >= min_depth) {
+        float stop = smin(0.95f, cmax(T) * st.eta * st.eta);
+        if (next1d(rng) < stop) T = T / stop;
+        else return false;
+    }
+    was = vp_trace(S, ray.o, ray.d, ray.mint, ray.maxt, nh);
+    if (was) { h = nh; fr = vp_frame(S, h, ray.o, ray.d); }
+    st.emission = false;
+    st.depth++;
+    return true;
+}
+
+// Persistent VolPath kernel with per-lane path regeneration: a lane whose
+// path finished takes the next path of the batch (warp-aggregated atomic),
+// so the lanes of a warp stay busy however long each path runs.
 __global__ void __launch_bounds__(128) k_volpath(RenderParams P, int *work)
 {
     const int lane = threadIdx.x & 31;
     int limit = 0;
+    VolState st;
+    Pcg32 rng;
+    rng.state = rng.inc = 0;
+    int slot = -1;
+    bool active = false, more = true;
     for (;;) {
-        int base = 0;
-        if (lane == 0) base = atomicAdd(work, 32);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= P.n_paths) break;
-        int slot = base + lane;
-        if (slot < P.n_paths) {
-            Pcg32 rng = P.W.rng[slot];
-            float4 ro = P.W.ray_o[slot], rd = P.W.ray_d[slot];
-            C3 L = li_volpath(P.S, make_ray(xyz(ro), xyz(rd), ro.w, rd.w), rng, P.max_depth, P.min_depth, limit);
-            P.W.out[slot] = f4c(L, 0.f);
+        const unsigned need = __ballot_sync(0xffffffffu, !active && more);
+        if (need) {
+            int base = 0;
+            const int leader = __ffs(need) - 1;
+            if (lane == leader) base = atomicAdd(work, __popc(need));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (!active && more) {
+                int q = base + __popc(need & ((1u << lane) - 1));
+                if (q < P.n_paths) {
+                    slot = q;
+                    rng = P.W.rng[slot];
+                    float4 ro = P.W.ray_o[slot], rd = P.W.ray_d[slot];
+                    vol_start(P.S, st, make_ray(xyz(ro), xyz(rd), ro.w, rd.w));
+                    active = true;
+                } else {
+                    more = false;
+                }
+            }
+        }
+        if (!__any_sync(0xffffffffu, active)) break;
+        if (active && !vol_step(P.S, st, rng, P.max_depth, P.min_depth, limit)) {
+            P.W.out[slot] = f4c(st.L, 0.f);
+            active = false;
         }
     }
     if (limit) atomicExch(P.limit_flag, 1);
@@ -1081,6 +1157,31 @@ __global__ void k_light_query(DevScene S, int light, const rt_light_q *q, int n,
     out[i] = r;
 }
 
+__global__ void k_medium_query(DevScene S, int medium, int op, const rt_medium_q *q, int n, rt_medium_r *out)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Pcg32 rng;
+    path_stream_seed(rng, q[i].seed, q[i].pixel, q[i].sample);
+    Ray r = make_ray(vload(q[i].o), vload(q[i].d), q[i].mint, q[i].maxt);
+    const DevMedium &m = S.media[medium];
+    int limit = 0;
+    rt_medium_r o;
+    memset(&o, 0, sizeof(o));
+    if (op == RT_MEDIUM_OP_SAMPLE) {
+        float t = 0.f;
+        C3 w, em;
+        o.scattered = medium_sample(m, r, rng, t, w, em, limit) ? 1 : 0;
+        o.weight[0] = w.r; o.weight[1] = w.g; o.weight[2] = w.b;
+        o.t = t;
+    } else {
+        C3 tr = medium_tr(m, r, rng, limit);
+        o.weight[0] = tr.r; o.weight[1] = tr.g; o.weight[2] = tr.b;
+    }
+    o.limit = limit;
+    out[i] = o;
+}
+
 // =====================================================================
 // host side
 // =====================================================================
@@ -1150,6 +1251,7 @@ struct rt_scene {
     float bounds[6];
     int n_lights = 0;
     int n_bsdfs = 0;
+    int n_media = 0;
     int bsdf_types = 0;   // bit t set when some BSDF of type t exists
     int wide_depth = 0;
     bool wide_ok = false;  // the 8-wide BVH is uploaded (or the scene has no triangles)
@@ -1643,6 +1745,7 @@ rt_status rt_scene_create(rt_ctx *ctx, const rt_scene_desc *d, rt_scene **out)
     S.cam.medium = cd.medium;
     sc->n_lights = d->n_lights;
     sc->n_bsdfs = d->n_bsdfs;
+    sc->n_media = d->n_media;
     for (int b = 0; b < d->n_bsdfs; b++) sc->bsdf_types |= 1 << d->bsdfs[b].type;
     *out = sc;
     return RT_OK;
@@ -2018,6 +2121,32 @@ rt_status rt_light_query(rt_ctx *ctx, rt_scene *sc, int32_t light, const rt_ligh
     cudaStreamSynchronize(ctx->stream);
     if (s == RT_OK) {
         cudaError_t e = cudaMemcpy(r, dr, sizeof(rt_light_r) * (size_t)n, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) s = fail(RT_ERR_CUDA, cudaGetErrorString(e));
+    }
+    cudaFree(dq);
+    cudaFree(dr);
+    return s;
+}
+
+rt_status rt_medium_query(rt_ctx *ctx, rt_scene *sc, int32_t medium, int32_t op, const rt_medium_q *q, int32_t n,
+                          rt_medium_r *r)
+{
+    if (!ctx || !sc || n < 0 || (n && (!q || !r))) return fail(RT_ERR_INVALID, "rt_medium_query: bad argument");
+    if (medium < 0 || medium >= sc->n_media) return fail(RT_ERR_INVALID, "rt_medium_query: bad medium");
+    if (op != RT_MEDIUM_OP_SAMPLE && op != RT_MEDIUM_OP_TRANSMITTANCE)
+        return fail(RT_ERR_INVALID, "rt_medium_query: bad op");
+    if (n == 0) return RT_OK;
+    CK(cudaSetDevice(ctx->device));
+    void *dq = nullptr, *dr = nullptr;
+    CK(cudaMalloc(&dq, sizeof(rt_medium_q) * (size_t)n));
+    CK(cudaMalloc(&dr, sizeof(rt_medium_r) * (size_t)n));
+    CK(cudaMemcpy(dq, q, sizeof(rt_medium_q) * (size_t)n, cudaMemcpyHostToDevice));
+    k_medium_query<<<(n + 127) / 128, 128, 0, ctx->stream>>>(sc->S, medium, op, (const rt_medium_q *)dq, n,
+                                                              (rt_medium_r *)dr);
+    rt_status s = launch_check("k_medium_query");
+    cudaStreamSynchronize(ctx->stream);
+    if (s == RT_OK) {
+        cudaError_t e = cudaMemcpy(r, dr, sizeof(rt_medium_r) * (size_t)n, cudaMemcpyDeviceToHost);
         if (e != cudaSuccess) s = fail(RT_ERR_CUDA, cudaGetErrorString(e));
     }
     cudaFree(dq);

@@ -36,6 +36,7 @@ def lib():
         L.oracle_trace.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_void_p]
         L.oracle_bsdf_query.argtypes = [C.POINTER(D.BsdfDesc), C.c_int32, C.c_void_p, C.c_int32, C.c_void_p]
         L.oracle_light_query.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p]
+        L.oracle_medium_query.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p]
         L.oracle_scene_info.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         L.oracle_pcg_stream.argtypes = [C.c_uint64, C.c_uint64, C.c_int32, C.c_void_p]
         L.oracle_pcg_reals.argtypes = [C.c_uint64, C.c_uint64, C.c_int32, C.c_void_p]
@@ -108,6 +109,14 @@ class OracleScene:
                                               ("point", np.float32, 3), ("normal", np.float32, 3),
                                               ("pdf_eval", np.float32), ("pad", np.float32)]))
         lib().oracle_light_query(self.h, light, _p(q), len(q), _p(r))
+        return r
+
+    def medium_query(self, medium, op, q):
+        from raytracer_gb300.core import MEDIUM_Q, MEDIUM_R
+        q = np.ascontiguousarray(q, MEDIUM_Q)
+        r = np.zeros(len(q), MEDIUM_R)
+        rc = lib().oracle_medium_query(self.h, medium, op, _p(q), len(q), _p(r))
+        assert rc == 0
         return r
 
     def info(self):

@@ -42,6 +42,11 @@ def test_struct_layout_matches_header(tmp_path):
     prog = ['#include <stdio.h>', '#include <stddef.h>', '#include "rtgpu.h"', "int main(void){"]
     for k in structs:
         prog.append('printf("%s %%zu\\n", sizeof(%s));' % (k, k))
+    from raytracer_gb300 import core
+    extra = {"rt_medium_q": core.MEDIUM_Q.itemsize, "rt_medium_r": core.MEDIUM_R.itemsize,
+             "rt_server_opts": C.sizeof(core.ServerOpts), "rt_job_info": C.sizeof(core.JobInfo)}
+    for k in extra:
+        prog.append('printf("%s %%zu\\n", sizeof(%s));' % (k, k))
     prog.append('printf("camera_off %zu\\n", offsetof(rt_scene_desc, camera));')
     prog.append("return 0;}")
     c = tmp_path / "sz.c"
@@ -51,6 +56,8 @@ def test_struct_layout_matches_header(tmp_path):
     out = dict(l.split() for l in subprocess.check_output([str(exe)]).decode().split("\n") if l)
     for k, cls in structs.items():
         assert int(out[k]) == C.sizeof(cls), (k, out[k], C.sizeof(cls))
+    for k, size in extra.items():
+        assert int(out[k]) == size, (k, out[k], size)
     assert int(out["camera_off"]) == D.SceneDesc.camera.offset
 
 

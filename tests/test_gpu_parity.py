@@ -234,6 +234,53 @@ def test_sphere_light_parity(ctx, rtlib, vol):
     _light_parity(ctx, rtlib, vol, 0, seed=2)
 
 
+def _medium_queries(n, rng, box_lo, box_hi):
+    from raytracer_gb300.core import MEDIUM_Q
+    q = np.zeros(n, MEDIUM_Q)
+    pad = 0.3 * (box_hi - box_lo)
+    q["o"] = box_lo - pad + rng.random((n, 3)) * (box_hi - box_lo + 2 * pad)
+    d = rng.normal(size=(n, 3))
+    q["d"] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    q["mint"] = np.where(rng.random(n) < 0.5, 0.0, 1e-4)
+    q["maxt"] = rng.uniform(0.05, 2.5, n)
+    q["seed"] = 7
+    q["pixel"] = np.arange(n)
+    q["sample"] = 3
+    return q
+
+
+@pytest.mark.parametrize("medium,box", [(0, ((-0.5, 0.25, -0.5), (0.5, 1.25, 0.5))),
+                                        (1, ((-1.5, -0.2, -1.5), (1.5, 0.2, 1.5)))],
+                         ids=["heterogeneous", "homogeneous"])
+def test_medium_parity(ctx, rtlib, vol, medium, box):
+    """Medium::sampleDistance and ::transmittance on the same sample streams.
+    Homogeneous: closed forms, all within 1e-4 relative (expf/logf ulps).
+    Heterogeneous: delta / ratio tracking takes data-dependent branches on
+    the sampled distances, so a 1-ulp difference in logf can change a path;
+    at least 99% of the queries must agree within 1e-4."""
+    g = rtlib.Scene(ctx, vol)
+    o = O.OracleScene(vol)
+    rng = np.random.default_rng(13 + medium)
+    q = _medium_queries(20000, rng, np.array(box[0]), np.array(box[1]))
+    for op in (0, 1):
+        rg, ro = g.medium_query(medium, op, q), o.medium_query(medium, op, q)
+        assert not rg["limit"].any()
+        same_branch = rg["scattered"] == ro["scattered"]
+        close = _rel_close(rg["weight"], ro["weight"], 1e-4, 1e-6).all(-1) & _rel_close(rg["t"], ro["t"], 1e-4, 1e-6)
+        ok = same_branch & close
+        print("medium %d op %d: scattered %d, agree %.5f" % (medium, op, int(ro["scattered"].sum()), ok.mean()))
+        if medium == 1:
+            assert ok.all()
+        else:
+            assert ok.mean() >= 0.99
+        if op == 0:
+            assert 0.05 < ro["scattered"].mean() < 0.95   # both branches exercised
+    with pytest.raises(Exception):
+        g.medium_query(5, 0, q[:4])
+    g.close()
+    o.close()
+
+
 def _film_parity(ctx, rtlib, scene, spp, seed, max_bad, block=16, **over):
     g = rtlib.Scene(ctx, scene)
     o = O.OracleScene(scene)
