@@ -193,6 +193,7 @@ def run_gpu(args):
     W, H, spp = CONFIG["width"], CONFIG["height"], CONFIG["spp"]
     film = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
     samples_per_step = W * H * spp
+    batch_paths = min(samples_per_step, args.wave_paths or (1 << 26))
     sbase = rank * spp
 
     def barrier():
@@ -202,6 +203,8 @@ def run_gpu(args):
         torch.cuda.synchronize()
 
     ctx.set_bvh_width(args.bvh_width)
+    if args.wave_paths:
+        ctx.set_wave_paths(args.wave_paths)
     # counting pass (traversal statistics for the roofline; not timed)
     ctx.set_profiling(2)
     scene.render(8, seed=99, film=film.data_ptr())
@@ -225,7 +228,8 @@ def run_gpu(args):
         scene.render(spp, seed=1000 + k, sample_begin=sbase, film=film.data_ptr())
         st = ctx.stats()
         launches += st["launches"]
-        for key in ("trace_closest_ms", "trace_any_ms", "shade_ms", "volpath_ms", "camera_ms", "film_ms", "closest_rays",
+        for key in ("trace_closest_ms", "trace_any_ms", "shade_ms", "resolve_ms", "volpath_ms", "camera_ms", "film_ms",
+                    "closest_rays",
                     "shadow_rays", "trace_closest_launches", "trace_any_launches", "paths", "nan_samples"):
             agg[key] = agg.get(key, 0) + st[key]
     e1.record(stream)
@@ -253,7 +257,9 @@ def run_gpu(args):
     d2h = W * H * 16
     h2d = 64 + 4 * (len(data.lights) + 1)
     # roofline of the dominant kernel
-    kern = {"trace_closest": agg["trace_closest_ms"], "trace_any": agg["trace_any_ms"], "shade": agg["shade_ms"]}
+    # single kernels (shade = the four per-BSDF shade kernels of a round)
+    kern = {"trace_closest": agg["trace_closest_ms"], "trace_any": agg["trace_any_ms"],
+            "resolve": agg["resolve_ms"], "shade": agg["shade_ms"] - agg["resolve_ms"]}
     if CONFIG.get("volume"):
         kern = {"volpath": agg["volpath_ms"]}
     dom = max(kern, key=kern.get)
@@ -271,8 +277,10 @@ def run_gpu(args):
         per_ray = S_RAY_IN + 4 + nodes_pr_a * S_NODE[args.bvh_width] + tris_pr_a * S_TRI
         algo_bytes = rays_a * per_ray
         nl = agg["trace_any_launches"]
-    elif dom == "shade":
-        per_ray = 2 * 128 + 2 * 32 + 64
+    elif dom in ("shade", "resolve"):
+        # per path vertex: path state read + write (2 x 64 B), ray queue
+        # write + read (2 x 32 B), material parameters (64 B)
+        per_ray = 2 * 64 + 2 * 32 + 64
         algo_bytes = rays_c * per_ray
         nl = max(agg["trace_closest_launches"], 1)
     else:
@@ -324,8 +332,9 @@ def run_gpu(args):
                            "triangles": data.n_triangles,
                            "resolution": [W, H], "spp": spp, "bvh_width": args.bvh_width, "max_depth": CONFIG["max_depth"],
                            "samples_per_step": samples_per_step, "parallelism": "replicas" if world > 1 else "single",
-                           "l2": "inputs larger than L2 (BVH+triangles %.0f MB, path state ~1 GB per batch)" %
-                                 (info["device_bytes"] / 1e6),
+                           "l2": "inputs larger than L2 (scene %.0f MB on the device, path state %.1f GB per "
+                                 "batch of %d paths)" % (info["device_bytes"] / 1e6, batch_paths * 205 / 1e9,
+                                                         batch_paths),
                            "scene_gen_s": round(gen_s, 2), "scene_build_upload_s": round(upload_s, 2)},
                 "e2e": None if args.small else {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                                                 "d2h_bytes_per_step": d2h},
@@ -461,6 +470,7 @@ def main():
     ap.add_argument("--workload", default="icosphere", choices=["icosphere", "volume", "batch", "serve"],
                     help="icosphere: the headline single-scene render; batch: 64 scenes, plain vs "
                          "rt_batch_render; serve: Poisson arrivals through rt_server")
+    ap.add_argument("--wave-paths", type=int, default=0, help="paths per wavefront batch (0: library default)")
     ap.add_argument("--batch-jobs", type=int, default=64)
     ap.add_argument("--lanes", default="2,4,8", help="batch: lane counts to time")
     ap.add_argument("--rates", default="5,20,100", help="serve: arrival rates (jobs/s)")

@@ -273,6 +273,7 @@ typedef struct rt_render_stats {
     int64_t tris_any;
     int64_t limit_hits;      /* device loops that hit their cap                  */
     int64_t nan_samples;     /* samples dropped as NaN (Screen.cpp:46-50)        */
+    double resolve_ms;       /* part of shade_ms spent in the resolve kernel     */
 } rt_render_stats;
 
 typedef struct rt_ctx rt_ctx;
@@ -310,6 +311,10 @@ rt_status rt_ctx_set_profiling(rt_ctx *ctx, int32_t level);
  * (compressed 8-wide BVH); both report the same closest hits (a tie at equal
  * distance may name another triangle) and the same occlusion. */
 rt_status rt_ctx_set_bvh_width(rt_ctx *ctx, int32_t width);
+/* Paths per wavefront batch of later renders (whole tiles x all samples are
+ * batched up to this count): 2^16..2^26.  Device memory for path state is
+ * about 240 bytes per path. */
+rt_status rt_ctx_set_wave_paths(rt_ctx *ctx, int32_t paths);
 
 /* Allocation-free tile render.  No counterpart in the reference: it exists
  * for callers that cannot allocate device memory while rendering (plugins

@@ -147,7 +147,9 @@ __global__ void k_camera(RenderParams P)
 // one, which keeps the warp converged.  COUNT adds BVH node / triangle-slot
 // fetch counts to stats[3..6].
 #define RT_SENT 0x76543210
-#define RT_FETCH_THRESHOLD 20
+#ifndef RT_FETCH_THRESHOLD
+#define RT_FETCH_THRESHOLD 28
+#endif
 
 template <bool ANY, bool COUNT>
 __global__ void __launch_bounds__(128, 10) k_trace(RenderParams P, int round)
@@ -1212,6 +1214,7 @@ struct rt_ctx {
     rt_render_stats last;
     int profiling = 0;
     int bvh_width = 2;          // traversal used by renders and rt_trace: 2 or 8
+    int wave_paths = 1 << 26;   // target paths per wavefront batch (about 14 GB of path state)
     std::vector<cudaEvent_t> ev_pool;
     std::vector<int> ev_kind;   // kernel kind per recorded pair
     size_t ev_used = 0;
@@ -1221,7 +1224,7 @@ struct rt_ctx {
 };
 
 // kinds for per-kernel timing
-enum { K_CAMERA = 0, K_TRACE_C = 1, K_TRACE_A = 2, K_SHADE = 3, K_VOLPATH = 4, K_FILM = 5, K_KINDS = 6 };
+enum { K_CAMERA = 0, K_TRACE_C = 1, K_TRACE_A = 2, K_SHADE = 3, K_VOLPATH = 4, K_FILM = 5, K_RESOLVE = 6, K_KINDS = 7 };
 
 static void prof_begin(rt_ctx *c, int kind)
 {
@@ -1295,6 +1298,23 @@ struct HCdf {
         }
     }
 };
+
+// guide[k] = first i with c[i] >= k / G, k = 0..G (cdf_sample_guided)
+static void cdf_guide(const float *c, int n, int G, int *g)
+{
+    int i = 0;
+    for (int k = 0; k <= G; k++) {
+        float t = (float)k / (float)G;
+        while (i < n && c[i] < t) i++;
+        g[k] = i;
+    }
+}
+static int pow2_at_least(int n)
+{
+    int g = 1;
+    while (g < n && g < (1 << 20)) g <<= 1;
+    return g;
+}
 
 static void mat_mul4(const double *a, const double *b, double *o)
 {
@@ -1444,6 +1464,14 @@ rt_status rt_ctx_set_bvh_width(rt_ctx *c, int32_t width)
     if (!c) return fail(RT_ERR_INVALID, "null ctx");
     if (width != 2 && width != 8) return fail(RT_ERR_INVALID, "BVH width must be 2 or 8");
     c->bvh_width = width;
+    return RT_OK;
+}
+
+rt_status rt_ctx_set_wave_paths(rt_ctx *c, int32_t paths)
+{
+    if (!c) return fail(RT_ERR_INVALID, "null ctx");
+    if (paths < (1 << 16) || paths > (1 << 26)) return fail(RT_ERR_INVALID, "wave paths must be in [2^16, 2^26]");
+    c->wave_paths = paths;
     return RT_OK;
 }
 
@@ -1671,6 +1699,18 @@ rt_status rt_scene_create(rt_ctx *ctx, const rt_scene_desc *d, rt_scene **out)
             D.env_marginal = dp;
             if ((st = upload(sc, weight.data(), weight.size(), &dp)) != RT_OK) { rt_scene_destroy(sc); return st; }
             D.env_weight = dp;
+            // guide tables for the marginal and row CDF searches
+            D.env_gm = pow2_at_least(H);
+            D.env_gr = pow2_at_least(Wd);
+            std::vector<int> gm(D.env_gm + 1), gr((size_t)H * (D.env_gr + 1));
+            cdf_guide(marg.c.data(), H + 1, D.env_gm, gm.data());
+            for (int i = 0; i < H; i++)
+                cdf_guide(rows.data() + (size_t)i * (Wd + 1), Wd + 1, D.env_gr, gr.data() + (size_t)i * (D.env_gr + 1));
+            const int *ip;
+            if ((st = upload(sc, gm.data(), gm.size(), &ip)) != RT_OK) { rt_scene_destroy(sc); return st; }
+            D.env_marg_guide = ip;
+            if ((st = upload(sc, gr.data(), gr.size(), &ip)) != RT_OK) { rt_scene_destroy(sc); return st; }
+            D.env_row_guide = ip;
             float R = D.env_radius;
             float pw = 4 * RT_PI * R * R;
             sc->light_power_lum[l] = h_lum(1.f * pw, 1.f * pw, 1.f * pw);
@@ -1885,8 +1925,10 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
         if (accumulate)
             CK(cudaMemcpyAsync(film, film_rgbw, npix_all * sizeof(float4), cudaMemcpyHostToDevice, st));
     }
-    // batch capacity: whole tiles, all samples of their pixels, about 4M paths
-    const int cap_target = 1 << 22;
+    // batch capacity: whole tiles, all samples of their pixels, up to
+    // ctx->wave_paths paths (fewer, longer-tailed batches cost more: the last
+    // rounds of a batch hold few paths and run at the traversal latency floor)
+    const int cap_target = ctx->wave_paths;
     const int ntiles = tiles_x * tiles_y;
     int tile_pix = bx * by;
     if ((int64_t)tile_pix * rd->spp > (1 << 26)) return fail(RT_ERR_LIMIT, "one tile's samples exceed the path capacity");
@@ -1962,8 +2004,10 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
                     else k_trace<true, false><<<trace_blocks, 128, 0, st>>>(P, ri);
                 }
                 prof_end(ctx);
-                prof_begin(ctx, K_SHADE);
+                prof_begin(ctx, K_RESOLVE);
                 k_pt_resolve<<<shade_blocks, 128, 0, st>>>(P, ri);
+                prof_end(ctx);
+                prof_begin(ctx, K_SHADE);
                 if (sc->bsdf_types & 1) k_pt_shade<0><<<shade_blocks, 128, 0, st>>>(P, ri);
                 if (sc->bsdf_types & 2) k_pt_shade<1><<<shade_blocks, 128, 0, st>>>(P, ri);
                 if (sc->bsdf_types & 4) k_pt_shade<2><<<shade_blocks, 128, 0, st>>>(P, ri);
@@ -2001,7 +2045,7 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
     cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
     std::memset(&ctx->last, 0, sizeof(ctx->last));
     ctx->last.kernel_ms = ms;
-    double kt[K_KINDS] = {0, 0, 0, 0, 0, 0};
+    double kt[K_KINDS] = {0, 0, 0, 0, 0, 0, 0};
     for (size_t i = 0; i < ctx->ev_used; i++) {
         float e = 0.f;
         cudaEventElapsedTime(&e, ctx->ev_pool[2 * i], ctx->ev_pool[2 * i + 1]);
@@ -2010,7 +2054,8 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
     ctx->last.camera_ms = kt[K_CAMERA];
     ctx->last.trace_closest_ms = kt[K_TRACE_C];
     ctx->last.trace_any_ms = kt[K_TRACE_A];
-    ctx->last.shade_ms = kt[K_SHADE];
+    ctx->last.shade_ms = kt[K_SHADE] + kt[K_RESOLVE];
+    ctx->last.resolve_ms = kt[K_RESOLVE];
     ctx->last.volpath_ms = kt[K_VOLPATH];
     ctx->last.film_ms = kt[K_FILM];
     ctx->last.trace_closest_launches = trace_c_launches;

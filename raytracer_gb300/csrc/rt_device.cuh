@@ -42,6 +42,9 @@ struct DevLight {
     const float *env_row_cdf;   // H * (W + 1)
     const float *env_marginal;  // H + 1
     const float *env_weight;    // H
+    const int *env_marg_guide;  // env_gm + 1 entries (cdf_guide of env_marginal)
+    const int *env_row_guide;   // H * (env_gr + 1) entries
+    int env_gm, env_gr;         // guide cells, powers of two
     float env_marginal_sum;
     float env_radius;           // bounding sphere radius (EnvironmentLight::initialize)
     float env_to_world[16], env_to_light[16];
@@ -369,6 +372,21 @@ __device__ __forceinline__ int cdf_sample(const float *cdf, int n /* entries inc
     while (lo < hi) {
         int mid = lo + ((hi - lo) >> 1);
         if (cdf[mid] < u) lo = mid + 1; else hi = mid;
+    }
+    return imin(imax(0, lo - 1), n - 2);
+}
+// The same index as cdf_sample, with the search narrowed by a guide table:
+// guide[k] = first i with cdf[i] >= k / G (G a power of two, so k = (int)(u*G)
+// is exact).  For u in [k/G, (k+1)/G) the answer lies in [guide[k],
+// guide[k+1]], so a binary search over that range returns exactly what the
+// full lower_bound returns, in a step or two instead of log2(n).
+__device__ __forceinline__ int cdf_sample_guided(const float *cdf, int n, float u, const int *guide, int G)
+{
+    int k = imin(imax((int)(u * (float)G), 0), G - 1);
+    int lo = __ldg(guide + k), hi = __ldg(guide + k + 1);
+    while (lo < hi) {
+        int mid = lo + ((hi - lo) >> 1);
+        if (__ldg(cdf + mid) < u) lo = mid + 1; else hi = mid;
     }
     return imin(imax(0, lo - 1), n - 2);
 }
@@ -965,8 +983,9 @@ __device__ __forceinline__ C3 env_le(const DevLight &L, V3 direction)
 __device__ __forceinline__ void env_sample(const DevLight &L, V3 p, V2 s, LightRec &o)
 {
     int W = L.env_w, H = L.env_h;
-    int row = cdf_sample(L.env_marginal, H + 1, s.x);
-    int col = cdf_sample(L.env_row_cdf + (size_t)row * (W + 1), W + 1, s.y);
+    int row = cdf_sample_guided(L.env_marginal, H + 1, s.x, L.env_marg_guide, L.env_gm);
+    int col = cdf_sample_guided(L.env_row_cdf + (size_t)row * (W + 1), W + 1, s.y,
+                                L.env_row_guide + (size_t)row * (L.env_gr + 1), L.env_gr);
     float rcol = (float)col + 0.f * (float)W;
     float rrow = (float)row + 0.f * (float)H;
     env_checkxy(L, rcol, rrow);

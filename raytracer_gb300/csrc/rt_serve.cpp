@@ -52,6 +52,8 @@ struct LaneSet {
             rt_status s = rt_ctx_create(device, &c);
             if (s != RT_OK) return s;
             rt_ctx_set_bvh_width(c, bvh_width);
+            // lanes overlap several renders; smaller batches bound their memory
+            rt_ctx_set_wave_paths(c, 1 << 24);
             lanes.push_back(c);
         }
         for (rt_ctx *c : lanes) rt_ctx_set_bvh_width(c, bvh_width);
@@ -99,6 +101,7 @@ void add_stats(rt_render_stats &a, const rt_render_stats &b)
     a.tris_any += b.tris_any;
     a.limit_hits += b.limit_hits;
     a.nan_samples += b.nan_samples;
+    a.resolve_ms += b.resolve_ms;
 }
 
 }  // namespace
