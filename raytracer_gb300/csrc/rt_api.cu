@@ -130,13 +130,22 @@ __global__ void k_camera(RenderParams P)
         P.W.rad[slot] = make_float4(0.f, 0.f, 0.f, __int_as_float(0));
         P.W.flags[slot] = F_FIRST;
         P.W.q_closest[slot] = slot;
-        P.W.q_active[0][slot] = slot;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
-        P.W.cnt[0].active = P.n_paths;
         P.W.cnt[0].closest = P.n_paths;
         P.W.cnt[0].shadow = 0;
     }
+}
+
+// Sort a traced path by what its ray hit: the shading queue of the hit
+// surface's BSDF type, or the finish queue for a miss or a surface without a
+// BSDF.  Called by the lanes that just finished a closest-hit ray.
+__device__ __forceinline__ void classify_hit(const RenderParams &P, RoundCounters *C, int slot, int prim)
+{
+    const int t = prim == -1 ? -1 : prim_type(P.S, prim);
+#pragma unroll
+    for (int k = 0; k < 4; k++) q_push(P.W.q_mat[k], &C->mat[k], slot, t == k);
+    q_push(P.W.q_fin, &C->fin, slot, t < 0);
 }
 
 // ---------------------------------------------------------------- traversal
@@ -274,7 +283,10 @@ __global__ void __launch_bounds__(128, 10) k_trace(RenderParams P, int round)
                 }
             }
             if (ANY) P.W.occl[slot] = hprim != -1 ? 1 : 0;
-            else P.W.hit[slot] = make_float4(hit_t, hu, hv, __int_as_float(hprim));
+            else {
+                P.W.hit[slot] = make_float4(hit_t, hu, hv, __int_as_float(hprim));
+                classify_hit(P, C, slot, hprim);
+            }
             has_ray = false;
         }
     }
@@ -475,7 +487,10 @@ __global__ void __launch_bounds__(128, 8) k_trace8(RenderParams P, int round)
                 }
             }
             if (ANY) P.W.occl[slot] = hprim != -1 ? 1 : 0;
-            else P.W.hit[slot] = make_float4(hit_t, hu, hv, __int_as_float(hprim));
+            else {
+                P.W.hit[slot] = make_float4(hit_t, hu, hv, __int_as_float(hprim));
+                classify_hit(P, C, slot, hprim);
+            }
             has_ray = false;
         }
     }
@@ -502,10 +517,11 @@ __global__ void k_rays_in(const rt_ray *rays, int n, RenderParams P, int anyhit)
     if (anyhit) { P.W.sh_o[i] = o; P.W.sh_d[i] = d; P.W.q_shadow[i] = i; }
     else { P.W.ray_o[i] = o; P.W.ray_d[i] = d; P.W.q_closest[i] = i; }
     if (i == 0) {
-        P.W.cnt[0].closest = anyhit ? 0 : n;
-        P.W.cnt[0].shadow = anyhit ? n : 0;
-        P.W.cnt[0].wc_closest = 0;
-        P.W.cnt[0].wc_shadow = 0;
+        RoundCounters c;
+        memset(&c, 0, sizeof(c));
+        c.closest = anyhit ? 0 : n;
+        c.shadow = anyhit ? n : 0;
+        P.W.cnt[0] = c;
     }
 }
 __global__ void k_hits_out(RenderParams P, int n, int anyhit, rt_hit *hits)
@@ -528,121 +544,67 @@ __global__ void k_hits_out(RenderParams P, int n, int anyhit, rt_hit *hits)
 
 // ---------------------------------------------------------------- PathTracingMIS vertex
 // The per-vertex loop body of PathTracingMIS::li (PathTracingMIS.cpp:54-259)
-// is split in two wavefront stages:
-//   k_pt_resolve  finishes vertex v once its rays are traced: adds the light
-//                 sample if unoccluded (:140), the MIS-weighted emission found
-//                 by the BSDF-sampled ray (:173-220), throughput / eta update
-//                 (:222-223), Russian roulette (:225-253); then sorts the
-//                 surviving path by the BSDF type of its next vertex;
-//   k_pt_shade<T> shades vertex v+1 for one BSDF type: emission at depth 0
-//                 (:73-74), light sample (:121-153), BSDF sample (:156-168),
-//                 emitting the shadow ray and the next closest-hit ray.
-__global__ void __launch_bounds__(128) k_pt_resolve(RenderParams P, int round)
+// runs as three wavefront stages after the traces of a round:
+//   k_trace<closest>  sorts each traced path by what its ray hit (classify_hit);
+//   k_pt_finish       ends the paths whose ray missed or hit a surface without
+//                     a BSDF, and those that ended in shading with a light
+//                     sample pending: light sample if unoccluded (:140), the
+//                     MIS-weighted emission the BSDF-sampled ray found
+//                     (:173-220);
+//   k_pt_shade<T>     for paths that hit a surface of BSDF type T: first
+//                     finishes the previous vertex as above, then throughput /
+//                     eta update (:222-223) and Russian roulette (:225-253),
+//                     then shades the new vertex: emission at depth 0
+//                     (:73-74), light sample (:121-153), BSDF sample (:156-168),
+//                     emitting the shadow ray and the next closest-hit ray.
+__global__ void __launch_bounds__(128) k_pt_finish(RenderParams P, int round)
 {
     const DevScene &S = P.S;
     RoundCounters *C = &P.W.cnt[round];
-    const int n = C->active;
-    const int *qin = P.W.q_active[round & 1];
+    const int nf = C->fin, n = nf + C->end;
     const int env = S.env_light;
-    int idx = blockIdx.x * blockDim.x + threadIdx.x;
-    int stride = gridDim.x * blockDim.x;
-    int iters = (n + stride - 1) / stride;
-    for (int it = 0; it < iters; it++, idx += stride) {
-        bool valid = idx < n;
-        int slot = valid ? qin[idx] : 0;
-        int mtype = -1;
-        if (valid) {
-            int flags = P.W.flags[slot];
-            float4 radv = P.W.rad[slot];
-            C3 L = rgb(radv);
-            int depth = __float_as_int(radv.w);
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+        const int slot = idx < nf ? P.W.q_fin[idx] : P.W.q_end[idx - nf];
+        int flags = P.W.flags[slot];
+        C3 L = rgb(P.W.rad[slot]);
+        if (flags & F_FIRST) {
+            // camera ray: the environment if it missed; a surface without a
+            // BSDF ends the path (PathTracingMIS.cpp:60-70)
             float4 hv = P.W.hit[slot];
-            Hit h; h.t = hv.x; h.u = hv.y; h.v = hv.z; h.prim = __float_as_int(hv.w);
-            bool done = false;
-            bool state_dirty = false;
-            float4 tpv = make_float4(0, 0, 0, 0);
-            if (flags & F_FIRST) {
-                flags &= ~F_FIRST;
-                if (h.prim == -1) {
-                    if (env >= 0) {
-                        float4 rd = P.W.ray_d[slot];
-                        L = L + env_le(S.lights[env], xyz(rd));
+            if (__float_as_int(hv.w) == -1 && env >= 0) L = L + env_le(S.lights[env], xyz(P.W.ray_d[slot]));
+        } else {
+            if ((flags & F_NEE) && !P.W.occl[slot]) L = L + rgb(P.W.nee[slot]);
+            if (!(flags & F_END)) {
+                float4 hv = P.W.hit[slot];
+                Hit h; h.t = hv.x; h.u = hv.y; h.v = hv.z; h.prim = __float_as_int(hv.w);
+                float4 ro = P.W.ray_o[slot], rd = P.W.ray_d[slot];
+                V3 o = xyz(ro), d = xyz(rd);
+                int caught = -1;
+                C3 Le = cfill(0.f);
+                V3 pt = v3(0, 0, 0), nn = v3(0, 0, 0);
+                if (h.prim != -1) {
+                    int nl = prim_light(S, h.prim);
+                    if (nl >= 0) {
+                        Frame fr = hit_frame(S, h, o, d);
+                        pt = fr.p; nn = fr.n;
+                        caught = nl;
+                        Le = area_le(S, nl, -d, fr.n);
                     }
-                    done = true;
-                } else if (depth >= P.max_depth) {
-                    done = true;
+                } else if (env >= 0) {
+                    caught = env;
+                    Le = env_le(S.lights[env], d);
                 }
-            } else {
-                if ((flags & F_NEE) && !P.W.occl[slot]) L = L + rgb(P.W.nee[slot]);
-                flags &= ~F_NEE;
-                if (flags & F_END) {
-                    done = true;
-                } else {
-                    tpv = P.W.tp[slot];
-                    C3 T = rgb(tpv);
-                    float eta = tpv.w;
+                if (caught >= 0) {
+                    C3 T = rgb(P.W.tp[slot]);
                     float4 bsv = P.W.bs[slot];
-                    C3 f = rgb(bsv);
-                    float bpdf = bsv.w;
-                    float4 ro = P.W.ray_o[slot], rd = P.W.ray_d[slot];
-                    V3 o = xyz(ro), d = xyz(rd);
-                    int caught = -1;
-                    bool isenv = false;
-                    C3 Le = cfill(0.f);
-                    V3 pt = v3(0, 0, 0), nn = v3(0, 0, 0);
-                    if (h.prim != -1) {
-                        int nl = prim_light(S, h.prim);
-                        if (nl >= 0) {
-                            Frame fr = hit_frame(S, h, o, d);
-                            pt = fr.p; nn = fr.n;
-                            caught = nl;
-                            Le = area_le(S, nl, -d, fr.n);
-                        }
-                    } else {
-                        if (env < 0) done = true;
-                        else { caught = env; isenv = true; Le = env_le(S.lights[env], d); }
-                    }
-                    if (!done && caught >= 0) {
-                        float pl = (flags & F_DELTA) ? 0.f : light_pdf(S, caught, o, pt, nn, d);
-                        float w = power_heuristic(bpdf, pl);
-                        L = L + ((T * Le) * f) * w;
-                        if (isenv) done = true;
-                    }
-                    if (!done) {
-                        T = T * f;
-                        eta *= P.W.rel_eta[slot];
-                        if (depth >= P.min_depth) {
-                            Pcg32 rng = P.W.rng[slot];
-                            float stop = smin(0.95f, lum(T) * eta * eta);
-                            if (next1d(rng) < stop) T = T / stop;
-                            else done = true;
-                            P.W.rng[slot] = rng;
-                        }
-                        tpv = f4c(T, eta);
-                        state_dirty = true;
-                    }
-                    if (!done) {
-                        depth++;
-                        if (depth >= P.max_depth) done = true;
-                    }
+                    float pl = (flags & F_DELTA) ? 0.f : light_pdf(S, caught, o, pt, nn, d);
+                    float w = power_heuristic(bsv.w, pl);
+                    L = L + ((T * Le) * rgb(bsv)) * w;
                 }
             }
-            if (!done) {
-                int b = prim_bsdf(S, h.prim);
-                if (b < 0) done = true;
-                else mtype = S.bsdfs[b].type;
-            }
-            if (done) {
-                flags |= F_DONE;
-                P.W.out[slot] = f4c(L, 0.f);
-            } else {
-                P.W.rad[slot] = f4c(L, __int_as_float(depth));
-                if (state_dirty) P.W.tp[slot] = tpv;
-            }
-            P.W.flags[slot] = flags;
         }
-#pragma unroll
-        for (int t = 0; t < 4; t++) q_push(P.W.q_mat[t], &C->mat[t], slot, mtype == t);
+        P.W.out[slot] = f4c(L, 0.f);
+        P.W.flags[slot] = (flags & ~(F_FIRST | F_NEE)) | F_DONE;
     }
 }
 
@@ -679,19 +641,20 @@ __global__ void __launch_bounds__(128) k_pt_shade(RenderParams P, int round)
     RoundCounters *Cout = &P.W.cnt[round + 1];
     const int n = C->mat[BT];
     const int *qin = P.W.q_mat[BT];
-    int *qout = P.W.q_active[(round + 1) & 1];
     int idx = blockIdx.x * blockDim.x + threadIdx.x;
     int stride = gridDim.x * blockDim.x;
     int iters = (n + stride - 1) / stride;
     for (int it = 0; it < iters; it++, idx += stride) {
         bool valid = idx < n;
         int slot = valid ? qin[idx] : 0;
-        bool push_active = false, push_closest = false, push_shadow = false;
+        bool push_end = false, push_closest = false, push_shadow = false;
         if (valid) {
             Pcg32 rng = P.W.rng[slot];
             float4 tpv = P.W.tp[slot];
             C3 T = rgb(tpv);
+            float eta = tpv.w;
             float4 radv = P.W.rad[slot];
+            C3 L = rgb(radv);
             int depth = __float_as_int(radv.w);
             int flags = P.W.flags[slot];
             float4 ro = P.W.ray_o[slot], rd = P.W.ray_d[slot];
@@ -700,12 +663,45 @@ __global__ void __launch_bounds__(128) k_pt_shade(RenderParams P, int round)
             Hit h; h.t = hv.x; h.u = hv.y; h.v = hv.z; h.prim = __float_as_int(hv.w);
             Frame fr = hit_frame(S, h, o, d);
             const DevBsdf &B = S.bsdfs[prim_bsdf(S, h.prim)];
+            bool done = false;
+            // finish the previous vertex (its light sample and the emission
+            // its BSDF-sampled ray found), update throughput, roulette
+            if (flags & F_FIRST) {
+                flags &= ~F_FIRST;
+                if (depth >= P.max_depth) done = true;
+            } else {
+                if ((flags & F_NEE) && !P.W.occl[slot]) L = L + rgb(P.W.nee[slot]);
+                flags &= ~F_NEE;
+                float4 bsv = P.W.bs[slot];
+                C3 f = rgb(bsv);
+                int nl = prim_light(S, h.prim);
+                if (nl >= 0) {
+                    C3 Le = area_le(S, nl, -d, fr.n);
+                    float pl = (flags & F_DELTA) ? 0.f : light_pdf(S, nl, o, fr.p, fr.n, d);
+                    float w = power_heuristic(bsv.w, pl);
+                    L = L + ((T * Le) * f) * w;
+                }
+                T = T * f;
+                eta *= P.W.rel_eta[slot];
+                if (depth >= P.min_depth) {
+                    float stop = smin(0.95f, lum(T) * eta * eta);
+                    if (next1d(rng) < stop) T = T / stop;
+                    else done = true;
+                }
+                if (!done) {
+                    depth++;
+                    if (depth >= P.max_depth) done = true;
+                }
+            }
+            if (done) {
+                P.W.out[slot] = f4c(L, 0.f);
+                P.W.flags[slot] = flags | F_DONE;
+                P.W.rng[slot] = rng;
+            } else {
+            // emission of a light hit by the camera ray (PathTracingMIS.cpp:73-74)
             if (depth == 0) {
                 int hl = prim_light(S, h.prim);
-                if (hl >= 0) {
-                    C3 L = rgb(radv) + T * area_le(S, hl, -d, fr.n);
-                    P.W.rad[slot] = f4c(L, radv.w);
-                }
+                if (hl >= 0) L = L + T * area_le(S, hl, -d, fr.n);
             }
             // light sampling (Integrator::sampleLightDirect, Integrator.cpp:176-218)
             V2 s = next2d(rng);
@@ -738,11 +734,12 @@ __global__ void __launch_bounds__(128) k_pt_shade(RenderParams P, int round)
             V2 u = next2d(rng);
             C3 f = bsdf_sample_t<BT>(B, r, u);
             if (iszero(f)) {
-                if (flags & F_NEE) { flags |= F_END; push_active = true; }
-                else {
+                if (flags & F_NEE) {
+                    flags |= F_END;   // the light sample still needs its shadow ray
+                    push_end = true;
+                } else {
                     flags |= F_DONE;
-                    float4 rv = P.W.rad[slot];
-                    P.W.out[slot] = make_float4(rv.x, rv.y, rv.z, 0.f);
+                    P.W.out[slot] = f4c(L, 0.f);
                 }
             } else {
                 P.W.ray_o[slot] = f4(fr.p, RT_EPSILON);
@@ -751,12 +748,14 @@ __global__ void __launch_bounds__(128) k_pt_shade(RenderParams P, int round)
                 P.W.rel_eta[slot] = r.rel_eta;
                 if (r.type & BT_DELTA) flags |= F_DELTA; else flags &= ~F_DELTA;
                 push_closest = true;
-                push_active = true;
             }
+            P.W.rad[slot] = f4c(L, __int_as_float(depth));
+            P.W.tp[slot] = f4c(T, eta);
             P.W.rng[slot] = rng;
             P.W.flags[slot] = flags;
+            }
         }
-        q_push(qout, &Cout->active, slot, push_active);
+        q_push(P.W.q_end, &Cout->end, slot, push_end);
         q_push(P.W.q_closest, &Cout->closest, slot, push_closest);
         q_push(P.W.q_shadow, &Cout->shadow, slot, push_shadow);
     }
@@ -1757,6 +1756,17 @@ rt_status rt_scene_create(rt_ctx *ctx, const rt_scene_desc *d, rt_scene **out)
     if (!tri_n.empty()) { if ((st = upload(sc, tri_n.data(), tri_n.size(), &fp)) != RT_OK) { rt_scene_destroy(sc); return st; } S.tri_n = fp; }
     if ((st = upload(sc, tri_mesh.data(), tri_mesh.size(), &ip)) != RT_OK) { rt_scene_destroy(sc); return st; }
     S.tri_mesh = ip;
+    {
+        // BSDF type per triangle: the closest-hit trace sorts hits by it
+        std::vector<uint8_t> tri_type(nt, 255);
+        for (int t = 0; t < nt; t++) {
+            int b = d->meshes[tri_mesh[t]].bsdf;
+            if (b >= 0) tri_type[t] = (uint8_t)d->bsdfs[b].type;
+        }
+        const uint8_t *tp8;
+        if ((st = upload(sc, tri_type.data(), tri_type.size(), &tp8)) != RT_OK) { rt_scene_destroy(sc); return st; }
+        S.tri_type = tp8;
+    }
     const DevMesh *mp;
     if ((st = upload(sc, meshes.data(), meshes.size(), &mp)) != RT_OK) { rt_scene_destroy(sc); return st; }
     S.meshes = mp; S.n_meshes = d->n_meshes;
@@ -1830,8 +1840,8 @@ static rt_status ensure_wave(rt_ctx *c, int capacity, int max_rounds)
     ok &= alloc((void **)&W.out, P * sizeof(float4));
     ok &= alloc((void **)&W.splat, P);
     ok &= alloc((void **)&W.pix_irregular, P);
-    ok &= alloc((void **)&W.q_active[0], P * sizeof(int));
-    ok &= alloc((void **)&W.q_active[1], P * sizeof(int));
+    ok &= alloc((void **)&W.q_fin, P * sizeof(int));
+    ok &= alloc((void **)&W.q_end, P * sizeof(int));
     ok &= alloc((void **)&W.q_closest, P * sizeof(int));
     ok &= alloc((void **)&W.q_shadow, P * sizeof(int));
     for (int t = 0; t < 4; t++) ok &= alloc((void **)&W.q_mat[t], P * sizeof(int));
@@ -2005,7 +2015,7 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
                 }
                 prof_end(ctx);
                 prof_begin(ctx, K_RESOLVE);
-                k_pt_resolve<<<shade_blocks, 128, 0, st>>>(P, ri);
+                k_pt_finish<<<shade_blocks, 128, 0, st>>>(P, ri);
                 prof_end(ctx);
                 prof_begin(ctx, K_SHADE);
                 if (sc->bsdf_types & 1) k_pt_shade<0><<<shade_blocks, 128, 0, st>>>(P, ri);
@@ -2017,12 +2027,12 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
                 trace_c_launches++;
                 trace_a_launches++;
                 if ((s = launch_check("pt round")) != RT_OK) return s;
-                // cheap early exit: peek at the survivor count every 4 rounds
+                // cheap early exit: peek at the survivor counts every 4 rounds
                 if ((r & 3) == 3 && r + 1 < max_rounds) {
-                    int nact = 0;
-                    CK(cudaMemcpyAsync(&nact, &ctx->W.cnt[ri + 1].active, sizeof(int), cudaMemcpyDeviceToHost, st));
+                    RoundCounters nc;
+                    CK(cudaMemcpyAsync(&nc, &ctx->W.cnt[ri + 1], sizeof(nc), cudaMemcpyDeviceToHost, st));
                     CK(cudaStreamSynchronize(st));
-                    if (nact == 0) break;
+                    if (nc.closest == 0 && nc.end == 0) break;
                 }
             }
         }
@@ -2305,8 +2315,8 @@ extern "C" rt_status rt_render_tile_static(rt_ctx *ctx, rt_scene *sc, const rt_r
     W.out = (float4 *)take(P * sizeof(float4));
     W.splat = (uint8_t *)take(P);
     W.pix_irregular = (uint8_t *)take((size_t)npix);
-    W.q_active[0] = (int *)take(P * sizeof(int));
-    W.q_active[1] = (int *)take(P * sizeof(int));
+    W.q_fin = (int *)take(P * sizeof(int));
+    W.q_end = (int *)take(P * sizeof(int));
     W.q_closest = (int *)take(P * sizeof(int));
     W.q_shadow = (int *)take(P * sizeof(int));
     for (int t = 0; t < 4; t++) W.q_mat[t] = (int *)take(P * sizeof(int));
@@ -2382,17 +2392,17 @@ extern "C" rt_status rt_render_tile_static(rt_ctx *ctx, rt_scene *sc, const rt_r
                 k_trace<false, false><<<sm * 12, 128, 0, st>>>(Pm, r);
                 k_trace<true, false><<<sm * 12, 128, 0, st>>>(Pm, r);
             }
-            k_pt_resolve<<<blocks, 128, 0, st>>>(Pm, r);
+            k_pt_finish<<<blocks, 128, 0, st>>>(Pm, r);
             if (sc->bsdf_types & 1) k_pt_shade<0><<<blocks, 128, 0, st>>>(Pm, r);
             if (sc->bsdf_types & 2) k_pt_shade<1><<<blocks, 128, 0, st>>>(Pm, r);
             if (sc->bsdf_types & 4) k_pt_shade<2><<<blocks, 128, 0, st>>>(Pm, r);
             if (sc->bsdf_types & 8) k_pt_shade<3><<<blocks, 128, 0, st>>>(Pm, r);
             if ((s = launch_check("pt round (static)")) != RT_OK) return s;
             if ((r & 3) == 3 && r + 1 < rounds) {
-                int nact = 0;
-                CK(cudaMemcpyAsync(&nact, &W.cnt[r + 1].active, sizeof(int), cudaMemcpyDeviceToHost, st));
+                RoundCounters nc;
+                CK(cudaMemcpyAsync(&nc, &W.cnt[r + 1], sizeof(nc), cudaMemcpyDeviceToHost, st));
                 CK(cudaStreamSynchronize(st));
-                if (nact == 0) break;
+                if (nc.closest == 0 && nc.end == 0) break;
             }
         }
     }

@@ -84,6 +84,7 @@ struct DevScene {
     const float *tri_v;         // 9 floats per triangle (p0, p1, p2)
     const float *tri_n;         // 9 floats per triangle (n0, n1, n2) or null
     const int *tri_mesh;
+    const uint8_t *tri_type;    // BSDF type of the triangle's mesh, 255 = no BSDF
     const DevMesh *meshes;
     const float *mesh_cdf;
     int n_meshes;
@@ -355,6 +356,16 @@ __device__ __forceinline__ int prim_bsdf(const DevScene &S, int prim)
 __device__ __forceinline__ int prim_light(const DevScene &S, int prim)
 {
     return prim >= 0 ? S.meshes[S.tri_mesh[prim]].light : S.spheres[-prim - 2].light;
+}
+// BSDF type of a hit primitive (triangle or sphere), or -1 without a BSDF
+__device__ __forceinline__ int prim_type(const DevScene &S, int prim)
+{
+    if (prim >= 0) {
+        int t = __ldg(S.tri_type + prim);
+        return t == 255 ? -1 : t;
+    }
+    int b = S.spheres[-prim - 2].bsdf;
+    return b < 0 ? -1 : S.bsdfs[b].type;
 }
 __device__ __forceinline__ int prim_interior(const DevScene &S, int prim)
 {

@@ -11,9 +11,11 @@ namespace rtgpu {
 enum { F_FIRST = 1, F_DELTA = 2, F_NEE = 4, F_END = 8, F_DONE = 16 };
 
 struct RoundCounters {   // one per wavefront round, zeroed per batch
-    int active, closest, shadow, wc_closest, wc_shadow;
+    int closest, shadow, wc_closest, wc_shadow;
     int mat[4];          // paths to shade per BSDF type (material-sorted queues)
-    int pad[7];
+    int fin;             // paths whose traced ray missed or hit a surface without a BSDF
+    int end;             // paths that ended in shading with a light sample pending
+    int pad[6];
 };
 
 struct Wave {
@@ -33,10 +35,11 @@ struct Wave {
     float4 *out;       // final radiance rgb, nan flag
     uint8_t *splat;    // film footprint code of the sample
     uint8_t *pix_irregular;  // per batch pixel: some sample splats off its pixel
-    // queues (ping-pong by round parity)
-    int *q_active[2];
+    // queues of the current round
     int *q_closest, *q_shadow;
-    int *q_mat[4];     // per-BSDF-type shading queues
+    int *q_mat[4];     // per-BSDF-type shading queues, filled by the closest-hit trace
+    int *q_fin;        // rays that missed or hit a surface without a BSDF (to finish)
+    int *q_end;        // paths whose BSDF sample was zero, light sample pending
     RoundCounters *cnt;
     int capacity;
     int max_rounds;
