@@ -719,11 +719,18 @@ __global__ void __launch_bounds__(128) k_pt_shade(RenderParams P, int round)
                         float bp = bsdf_pdf_t<BT>(B, wi, wo);
                         float w = power_heuristic(li.pdf, bp);
                         C3 contrib = (((T * value) * bsdf_eval_t<BT>(B, wi, wo)) * ct) * w;
-                        P.W.nee[slot] = f4c(contrib, 0.f);
-                        P.W.sh_o[slot] = f4(fr.p, RT_EPSILON);
-                        P.W.sh_d[slot] = f4(li.to_light, li.distance - RT_EPSILON);
-                        flags |= F_NEE;
-                        push_shadow = true;
+                        // The reference traces the shadow ray before it weighs the
+                        // sample by the BSDF (Integrator.cpp:176-218); the ray draws
+                        // no random numbers, so when the weighted contribution is
+                        // exactly zero (e.g. a light direction below an opaque
+                        // surface) its outcome cannot change L and it is not traced.
+                        if (contrib.r != 0.f || contrib.g != 0.f || contrib.b != 0.f) {
+                            P.W.nee[slot] = f4c(contrib, 0.f);
+                            P.W.sh_o[slot] = f4(fr.p, RT_EPSILON);
+                            P.W.sh_d[slot] = f4(li.to_light, li.distance - RT_EPSILON);
+                            flags |= F_NEE;
+                            push_shadow = true;
+                        }
                     }
                 }
             }
