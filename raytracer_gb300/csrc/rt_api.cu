@@ -160,8 +160,11 @@ __device__ __forceinline__ void classify_hit(const RenderParams &P, RoundCounter
 #define RT_FETCH_THRESHOLD 28
 #endif
 
+#ifndef RT_TRACE_MINB
+#define RT_TRACE_MINB 10
+#endif
 template <bool ANY, bool COUNT>
-__global__ void __launch_bounds__(128, 10) k_trace(RenderParams P, int round)
+__global__ void __launch_bounds__(128, RT_TRACE_MINB) k_trace(RenderParams P, int round)
 {
     const DevScene S = P.S;
     RoundCounters *C = &P.W.cnt[round];
@@ -633,8 +636,14 @@ __device__ __forceinline__ C3 bsdf_sample_t(const DevBsdf &b, BsdfRec &r, V2 s)
     return sl_sample(b, r, s);
 }
 
+#ifndef RT_SHADE_MINB
+#define RT_SHADE_MINB 8
+#endif
+#ifndef RT_SHADE_GRID
+#define RT_SHADE_GRID 16
+#endif
 template <int BT>
-__global__ void __launch_bounds__(128) k_pt_shade(RenderParams P, int round)
+__global__ void __launch_bounds__(128, RT_SHADE_MINB) k_pt_shade(RenderParams P, int round)
 {
     const DevScene &S = P.S;
     RoundCounters *C = &P.W.cnt[round];
@@ -1999,7 +2008,7 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
             if ((s = launch_check("k_volpath")) != RT_OK) return s;
         } else {
             int trace_blocks = sm * 12;
-            int shade_blocks = sm * 8;
+            int shade_blocks = sm * RT_SHADE_GRID;
             for (int r = 0; r < max_rounds; r++) {
                 int ri = r;
                 const bool cnt2 = ctx->profiling >= 2, w8 = ctx->bvh_width == 8 && sc->wide_ok;
