@@ -143,7 +143,8 @@ typedef struct rt_camera_desc {
 typedef struct rt_scene_desc {
     int32_t n_vertices;
     const float *vertices;       /* 3 floats per vertex, world space             */
-    const float *normals;        /* 3 floats per vertex or NULL (face normals)   */
+    const float *normals;        /* 3 floats per vertex or NULL (face normals);  
+                                    a NaN x marks a vertex of a mesh without normals */
     int32_t n_triangles;
     const int32_t *indices;      /* 3 vertex indices per triangle                */
     int32_t n_meshes;
@@ -396,6 +397,28 @@ rt_status rt_bsdf_query(rt_ctx *ctx, rt_scene *scene, int32_t bsdf, int32_t op,
 /* Sample light `light` (Light::sample + Light::pdf) for n queries. */
 rt_status rt_light_query(rt_ctx *ctx, rt_scene *scene, int32_t light,
                          const rt_light_q *q, int32_t n, rt_light_r *r);
+
+/* Scene ingestion: a Wavefront OBJ file as the reference's ObjLoader reads
+ * it (io/ObjLoader.cpp:97-290): positions and normals transformed by
+ * to_world (row-major 4x4, NULL = identity), corners de-duplicated by their
+ * (position, uv, normal) indices in order of first use, quads split into
+ * (a b c) (d a c).  Arrays are allocated by the library (normals / uvs NULL
+ * when the file has none); release them with rt_mesh_data_free. */
+typedef struct rt_mesh_data {
+    int32_t n_vertices;
+    float *vertices;             /* 3 per vertex, world space                  */
+    float *normals;              /* 3 per vertex or NULL                       */
+    float *uvs;                  /* 2 per vertex or NULL                       */
+    int32_t n_triangles;
+    int32_t *indices;            /* 3 per triangle                             */
+} rt_mesh_data;
+rt_status rt_obj_load(const char *path, const float *to_world, rt_mesh_data *out);
+void rt_mesh_data_free(rt_mesh_data *mesh);
+/* A Radiance RGBE (.hdr) environment map as the reference reads it
+ * (io/ImageLoader.cpp:78-99): width*height RGB floats, top row first, in a
+ * library allocation released with rt_host_free. */
+rt_status rt_hdr_load(const char *path, int32_t *width, int32_t *height, float **rgb);
+void rt_host_free(void *p);
 
 /* Sample or evaluate medium `medium` of the scene for n queries. */
 rt_status rt_medium_query(rt_ctx *ctx, rt_scene *scene, int32_t medium, int32_t op,

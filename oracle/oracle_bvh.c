@@ -10,6 +10,7 @@
  * (geometricShape/Sphere.cpp:38-139) and DifferentialGeometry::coordinateSystem
  * (core/DifferentialGeometry.h:36-50).
  */
+#include <math.h>
 #include "oracle.h"
 
 #include <stdlib.h>
@@ -513,7 +514,7 @@ int o_intersect(const o_scene *sc, const o_ray *ray, o_hit *hit, int shadow)
         v3 ng = v3_normalized(v3_cross(v3_sub(p1, p0), v3_sub(p2, p0)));
         hit->ng = ng;
         v3 ns = ng;
-        if (d->normals) {
+        if (d->normals && !isnan(d->normals[3 * (size_t)d->indices[3 * (size_t)tri]])) {
             const int32_t *ix = d->indices + 3 * (size_t)tri;
             v3 n0 = v3_from(d->normals + 3 * (size_t)ix[0]);
             v3 n1 = v3_from(d->normals + 3 * (size_t)ix[1]);

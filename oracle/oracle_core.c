@@ -3,6 +3,7 @@
  * TEST INFRASTRUCTURE ONLY -- see oracle.h.  Reference paths are relative to
  * RaytracerNew2/src of Iscandel/Raytracer.
  */
+#include <math.h>
 #include "oracle.h"
 
 #include <stdlib.h>
@@ -646,7 +647,7 @@ static void o_mesh_sample(const o_scene *sc, int mesh, v2 s, v3 *pt, v3 *n)
     o_tri_verts(d, tri, &p0, &p1, &p2);
     v3 b = o_square_to_triangle(s2);
     *pt = v3_add(v3_add(v3_muls(p0, b.x), v3_muls(p1, b.y)), v3_muls(p2, b.z));
-    if (d->normals) {
+    if (d->normals && !isnan(d->normals[3 * (size_t)d->indices[3 * (size_t)tri]])) {
         const int32_t *ix = d->indices + 3 * (size_t)tri;
         v3 n0 = v3_from(d->normals + 3 * (size_t)ix[0]);
         v3 n1 = v3_from(d->normals + 3 * (size_t)ix[1]);

@@ -22,7 +22,7 @@ ARCH = os.environ.get("RTGPU_ARCH", "-gencode=arch=compute_103a,code=sm_103a")
 NVCC = os.environ.get("NVCC", "nvcc")
 
 CUDA_SOURCES = ["rt_api.cu"]
-HOST_SOURCES = ["rt_bvh.cpp", "rt_serve.cpp"]
+HOST_SOURCES = ["rt_bvh.cpp", "rt_serve.cpp", "rt_io.cpp"]
 HEADERS = ["rt_math.cuh", "rt_device.cuh", "rt_kernels.cuh", "rt_bvh.h", "rt_internal.h"]
 
 
@@ -57,6 +57,7 @@ def build(force=False, verbose=False, ptxas_info=False):
         objs.append(obj)
         if force or _stale(obj, [src] + hdrs):
             cmd = [NVCC, ARCH, "-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC",
+                   "-Xcompiler", "-ffp-contract=off",
                    "-I", os.path.join(ROOT, "include"), "-c", src, "-o", obj]
             if ptxas_info:
                 cmd.insert(1, "-Xptxas=-v")
@@ -68,7 +69,8 @@ def build(force=False, verbose=False, ptxas_info=False):
         obj = os.path.join(BUILD, s + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + hdrs):
-            jobs.append(["g++", "-O3", "-std=c++17", "-fPIC", "-pthread", "-I", os.path.join(ROOT, "include"),
+            jobs.append(["g++", "-O3", "-std=c++17", "-fPIC", "-pthread", "-ffp-contract=off",
+                         "-I", os.path.join(ROOT, "include"),
                          "-I", _cuda_include(), "-c", src, "-o", obj])
     logs = []
     if jobs:

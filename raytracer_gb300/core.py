@@ -34,6 +34,11 @@ class JobInfo(C.Structure):
 JOB_QUEUED, JOB_RUNNING, JOB_DONE, JOB_FAILED = 0, 1, 2, 3
 
 
+class MeshData(C.Structure):
+    _fields_ = [("n_vertices", C.c_int32), ("vertices", C.POINTER(C.c_float)), ("normals", C.POINTER(C.c_float)),
+                ("uvs", C.POINTER(C.c_float)), ("n_triangles", C.c_int32), ("indices", C.POINTER(C.c_int32))]
+
+
 class RtError(RuntimeError):
     def __init__(self, status, msg):
         super().__init__("%s: %s" % (_STATUS.get(status, status), msg))
@@ -80,6 +85,14 @@ def lib():
     L.rt_job_poll.argtypes = [vp, C.c_int64, C.POINTER(JobInfo), vp]
     L.rt_job_wait.argtypes = [vp, C.c_int64, C.c_int32, C.POINTER(JobInfo), vp]
     L.rt_server_stop.argtypes = [vp]
+    L.rt_obj_load.argtypes = [C.c_char_p, vp, C.POINTER(MeshData)]
+    L.rt_obj_load.restype = C.c_int32
+    L.rt_mesh_data_free.argtypes = [C.POINTER(MeshData)]
+    L.rt_mesh_data_free.restype = None
+    L.rt_hdr_load.argtypes = [C.c_char_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.POINTER(C.c_float))]
+    L.rt_hdr_load.restype = C.c_int32
+    L.rt_host_free.argtypes = [vp]
+    L.rt_host_free.restype = None
     for name in ("rt_ctx_create", "rt_ctx_destroy", "rt_ctx_set_stream", "rt_scene_create", "rt_scene_destroy",
                  "rt_scene_info", "rt_render", "rt_render_stats_get", "rt_ctx_set_profiling", "rt_ctx_set_bvh_width", "rt_ctx_set_wave_paths",
                  "rt_trace", "rt_bsdf_query", "rt_light_query", "rt_medium_query", "rt_batch_render", "rt_ctx_set_lanes",
@@ -321,6 +334,39 @@ MEDIUM_R = np.dtype([("weight", np.float32, 3), ("t", np.float32), ("scattered",
 MEDIUM_OP_SAMPLE, MEDIUM_OP_TRANSMITTANCE = 0, 1
 assert BSDF_Q.itemsize == C.sizeof(D.BsdfQ) and BSDF_R.itemsize == C.sizeof(D.BsdfR)
 assert LIGHT_Q.itemsize == C.sizeof(D.LightQ) and LIGHT_R.itemsize == C.sizeof(D.LightR)
+
+
+def load_obj(path, to_world=None):
+    """Read a Wavefront OBJ as the reference's ObjLoader does (rt_obj_load):
+    returns (vertices (n, 3), normals (n, 3) or None, uvs (n, 2) or None,
+    triangles (m, 3)), positions and normals already in world space."""
+    m = MeshData()
+    tw = None if to_world is None else np.ascontiguousarray(to_world, np.float32).reshape(16)
+    _check(lib().rt_obj_load(os.fsencode(path), None if tw is None else _p(tw), C.byref(m)))
+    try:
+        def arr(ptr, n, k, dt):
+            if not ptr or n == 0:
+                return None
+            return np.ctypeslib.as_array(ptr, shape=(n * k,)).astype(dt).reshape(n, k)
+        v = arr(m.vertices, m.n_vertices, 3, np.float32)
+        v = v if v is not None else np.zeros((0, 3), np.float32)
+        t = arr(m.indices, m.n_triangles, 3, np.int32)
+        t = t if t is not None else np.zeros((0, 3), np.int32)
+        return v, arr(m.normals, m.n_vertices, 3, np.float32), arr(m.uvs, m.n_vertices, 2, np.float32), t
+    finally:
+        lib().rt_mesh_data_free(C.byref(m))
+
+
+def load_hdr(path):
+    """Read a Radiance RGBE (.hdr) image as the reference reads environment
+    maps (rt_hdr_load): (height, width, 3) float32, top row first."""
+    w, h = C.c_int32(), C.c_int32()
+    ptr = C.POINTER(C.c_float)()
+    _check(lib().rt_hdr_load(os.fsencode(path), C.byref(w), C.byref(h), C.byref(ptr)))
+    try:
+        return np.ctypeslib.as_array(ptr, shape=(h.value * w.value * 3,)).astype(np.float32).reshape(h.value, w.value, 3)
+    finally:
+        lib().rt_host_free(C.cast(ptr, C.c_void_p))
 
 
 def post_process(film):

@@ -331,7 +331,8 @@ __device__ __forceinline__ Frame hit_frame(const DevScene &S, const Hit &h, V3 o
         f.p = (bx * p0 + h.u * p1) + h.v * p2;
         V3 ng = normalized(cross(p1 - p0, p2 - p0));
         V3 ns = ng;
-        if (S.tri_n) {
+        // a triangle of a mesh without normals carries NaN normals
+        if (S.tri_n && !isnan(S.tri_n[9 * (size_t)h.prim])) {
             const float *Nn = S.tri_n + 9 * (size_t)h.prim;
             ns = normalized((bx * vload(Nn) + h.u * vload(Nn + 3)) + h.v * vload(Nn + 6));
         }
@@ -892,7 +893,7 @@ __device__ __forceinline__ void mesh_sample(const DevScene &S, int mesh, V2 s, V
     tri_verts(S, tri, p0, p1, p2);
     V3 b = square_to_triangle(s2);
     pt = (p0 * b.x + p1 * b.y) + p2 * b.z;
-    if (S.tri_n) {
+    if (S.tri_n && !isnan(S.tri_n[9 * (size_t)tri])) {
         const float *N = S.tri_n + 9 * (size_t)tri;
         n = normalized((b.x * vload(N) + b.y * vload(N + 3)) + b.z * vload(N + 6));
     } else {

@@ -198,12 +198,14 @@ class SceneData:
         first = len(self.indices)
         self.vertices = np.concatenate([self.vertices, verts]) if len(self.vertices) else verts.copy()
         self.indices = np.concatenate([self.indices, tris + base]) if len(self.indices) else (tris + base).astype(np.int32)
+        # one normal array for all vertices: the vertices of meshes without
+        # normals carry NaN, and their triangles shade with the geometric normal
         if normals is not None:
             if self.normals is None:
-                self.normals = np.zeros((base, 3), np.float32)
+                self.normals = np.full((base, 3), np.nan, np.float32)
             self.normals = np.concatenate([self.normals, np.asarray(normals, np.float32).reshape(-1, 3)])
         elif self.normals is not None:
-            raise ValueError("all meshes must carry normals once one does")
+            self.normals = np.concatenate([self.normals, np.full((len(verts), 3), np.nan, np.float32)])
         self.meshes.append(dict(first_tri=first, n_tris=len(tris), bsdf=bsdf, light=light,
                                 interior=interior, exterior=exterior))
         return len(self.meshes) - 1

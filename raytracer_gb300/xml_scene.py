@@ -1,0 +1,484 @@
+"""Reference scene files (XML) into a SceneData the device renders.
+
+Follows xml::XMLLoader (core/XMLLoader.cpp) element by element for the
+types the GPU path renders; anything else raises UnsupportedScene naming
+the element.  Paths in the file are resolved against the file's folder
+(XMLLoader.cpp:36 adds it to the search path).
+
+    integrator   PathTracingMIS | VolPathTracing: maxDepth, minDepth, strategy
+                 (PathTracingMIS.cpp:15-19, VolPathTracing.cpp:13-17)
+    camera       NoriPerspective: fov, nearClip, farClip (NoriPerspective.cpp:15-17),
+                 sizeX, sizeY, apertureRadius, focalPlane (Camera.cpp:11-14),
+                 <transform> = camera to world, <filter> BoxFilter of radius 0.5
+    sampler      RandomSampler: sampleNumber -> `spp` (RandomSampler.cpp:10)
+    parameters   blockSizeX, blockSizeY -> `block` (XMLLoader.cpp:217-259)
+    medium       (top level) the camera medium (XMLLoader.cpp:96-101; the later
+                 referable-medium branch of the reference is unreachable)
+    lights       EnvironmentLight: path (.hdr), toWorld, scale (EnvironmentLight.cpp:8-19)
+    objects      shape Mesh (path .obj, toWorld; MeshFactory.h:39-139), Cube
+                 (toWorld; Cube.cpp), Sphere (radius, toWorld; Sphere.cpp:14-15),
+                 each with <bsdf>, <light type="AreaLight|MeshLight"> (radiance),
+                 <medium name="interior|exterior">
+    bsdf         Diffuse, RoughConductor, RoughDielectric, SmoothLayeredBSDF
+                 (over Diffuse); top-level <bsdf id=..> and <transform id=..>
+                 can be referenced with ref=".."
+    media        Homogeneous (sigmaA, sigmaS, scale), Heterogeneous (albedo,
+                 <volume type="GridVolume"> path .vol, centered, toWorld, scale),
+                 <phase name="phaseFunction" type="HGPhaseFunction|IsotropicPhaseFunction">
+
+`load_scene(path)` returns the SceneData with `spp` and `block` attributes.
+"""
+import math
+import os
+import warnings
+import xml.etree.ElementTree as ET
+
+import numpy as np
+
+from . import desc as D
+
+F32 = np.float32
+
+
+class UnsupportedScene(ValueError):
+    """The scene uses a type or option the GPU path does not provide."""
+
+
+# --------------------------------------------------------------- values
+def _num(s, kind):
+    s = s.strip()
+    if kind == "bool":
+        return s == "1" or s.lower() == "true"   # tools/Tools.h:119-126
+    if kind == "int":
+        return int(float(s)) if s else 0
+    return float(s)
+
+
+def _triple(s):
+    v = [float(x) for x in s.replace(",", " ").split()]
+    v = (v + [0.0, 0.0, 0.0])[:3]
+    return tuple(v)
+
+
+def _color(s, where):
+    """tools::stringToColor(.., 1): exactly three rgb values, blank or comma
+    separated; anything else is an error that yields black in the reference."""
+    parts = [p for p in s.replace(",", " ").split() if p]
+    if len(parts) != 3 or any(":" in p for p in parts):
+        warnings.warn("%s: RGB string %r is of wrong size; black, as in the reference" % (where, s))
+        return (0.0, 0.0, 0.0)
+    return tuple(float(p) for p in parts)
+
+
+# ------------------------------------------------------------ transforms
+def _deg2rad(a):
+    return F32(a) * F32(math.pi) / F32(180.0)
+
+
+def _rot(axis, deg):
+    r = _deg2rad(deg)
+    c, s = F32(math.cos(r)), F32(math.sin(r))
+    m = np.eye(4, dtype=F32)
+    i, j = {"x": (1, 2), "y": (2, 0), "z": (0, 1)}[axis]
+    m[i, i], m[i, j], m[j, i], m[j, j] = c, -s, s, c
+    return m
+
+
+def _xyz(el, default):
+    v = list(default)
+    for c in el:
+        if c.tag in ("x", "y", "z"):
+            v["xyz".index(c.tag)] = float(c.text)
+        else:
+            warnings.warn("unknown parameter %s" % c.tag)
+    return v
+
+
+def _transform(el):
+    """XMLLoader::handleTransform (XMLLoader.cpp:857-905): each child is
+    multiplied on the left of what came before."""
+    T = np.eye(4, dtype=F32)
+    for c in el:
+        if c.tag == "rotation":
+            r = _xyz(c, (0.0, 0.0, 0.0))
+            M = _rot("x", r[0]) @ _rot("y", r[1]) @ _rot("z", r[2])
+        elif c.tag == "translation":
+            t = _xyz(c, (0.0, 0.0, 0.0))
+            M = np.eye(4, dtype=F32)
+            M[:3, 3] = t
+        elif c.tag == "scale":
+            M = np.diag(list(_xyz(c, (1.0, 1.0, 1.0))) + [1.0]).astype(F32)
+        elif c.tag == "matrix":
+            M = np.array([float(x) for x in c.get("value").split()], F32).reshape(4, 4)
+        elif c.tag == "lookAt":
+            o = t = u = (0.0, 0.0, 0.0)
+            for k in c:
+                if k.tag == "origin":
+                    o = _triple(k.text)
+                elif k.tag == "lookAt":
+                    t = _triple(k.text)
+                elif k.tag == "up":
+                    u = _triple(k.text)
+            M = np.asarray(D.look_at(o, t, u), F32)
+        else:
+            warnings.warn("unknown transform element %s" % c.tag)
+            continue
+        T = (M.astype(F32) @ T).astype(F32)
+    return T
+
+
+# ------------------------------------------------------------- the loader
+class _Loader:
+    def __init__(self, path, materials):
+        self.path = os.path.abspath(path)
+        self.dir = os.path.dirname(self.path)
+        self.materials = dict(materials or {})
+        self.s = D.SceneData()
+        self.s.name = os.path.splitext(os.path.basename(path))[0]
+        self.ref_bsdf = {}
+        self.ref_transform = {}
+        self.ref_medium = {}
+        self.camera_params = None
+        self.camera_transform = np.eye(4, dtype=F32)
+        self.camera_medium = -1
+        self.spp = 1
+        self.block = (32, 32)
+
+    def resolve(self, p):
+        return p if os.path.isabs(p) else os.path.normpath(os.path.join(self.dir, p))
+
+    # XMLLoader::handleProperty (XMLLoader.cpp:714-830)
+    def props(self, el):
+        params = {}
+        for c in el:
+            name = c.get("name")
+            val = c.get("value")
+            tag = c.tag
+            if name is None and c.get("ref") is None:
+                warnings.warn("no name attribute for %s property" % tag)
+                continue
+            if tag == "bool":
+                params[name] = _num(val, "bool")
+            elif tag == "integer":
+                params[name] = _num(val, "int")
+            elif tag in ("double", "real"):
+                params[name] = _num(val, "float")
+            elif tag == "string":
+                params[name] = val
+            elif tag in ("point", "vector"):
+                params[name] = _triple(val)
+            elif tag == "color":
+                params[name] = _color(val, name)
+            elif tag == "spectrum":
+                raise UnsupportedScene("spectrum values (%s) are not provided" % name)
+            elif tag == "transform":
+                if c.get("ref"):
+                    params[name or "toWorld"] = self.ref_transform[c.get("ref")]
+                else:
+                    params[name] = _transform(c)
+            elif tag == "texture":
+                if c.get("type") != "ConstantTexture":
+                    raise UnsupportedScene("texture type %s is not provided" % c.get("type"))
+                tp = self.props(c)
+                params[name] = ("texture", tp.get("albedo", (0.5, 0.5, 0.5)))   # ConstantTexture.cpp:6-10
+            elif tag == "bsdf":
+                params[name] = self.ref_bsdf[c.get("ref")] if c.get("ref") else self.bsdf(c)
+            elif tag == "medium":
+                params[name] = self.ref_medium[c.get("ref")] if c.get("ref") else self.medium(c)
+            elif tag == "phase":
+                params[name] = ("phase", c.get("type"), self.props(c))
+            elif tag == "volume":
+                params[name] = ("volume", c.get("type"), self.props(c))
+            else:
+                warnings.warn("unknown property %s" % name)
+        return params
+
+    @staticmethod
+    def _tex_or(params, name, default):
+        v = params.get(name, default)
+        if isinstance(v, tuple) and len(v) == 2 and v[0] == "texture":
+            return tuple(v[1])
+        return v
+
+    # BSDFs: returns the index in the scene's BSDF table
+    def bsdf(self, el, params=None):
+        kind = el.get("type")
+        p = self.props(el) if params is None else params
+        if kind == "Diffuse":   # Diffuse.cpp:11-18
+            b = D.bsdf(D.BSDF_DIFFUSE, albedo=self._tex_or(p, "albedo", (0.5, 0.5, 0.5)))
+        elif kind == "RoughConductor":   # RoughConductor.cpp:13-30, tools/Common.cpp:56-81
+            mat = p.get("material", "")
+            if mat:
+                if mat not in self.materials:
+                    raise UnsupportedScene("conductor material %r needs its eta/k: pass materials={%r: (eta, k)}"
+                                           % (mat, mat))
+                eta, k = self.materials[mat]
+            else:
+                eta, k = p.get("eta", (0.0, 0.0, 0.0)), p.get("absorption", (0.0, 0.0, 0.0))
+            alpha = self._tex_or(p, "alpha", 0.2)
+            if isinstance(alpha, tuple):
+                alpha = (alpha[0] + alpha[0] + alpha[0]) / 3.0
+            b = D.bsdf(D.BSDF_ROUGH_CONDUCTOR, distribution=_dist(p.get("distribution", "beckmann")),
+                       alpha=alpha, eta=eta, k=k, reflectance=self._tex_or(p, "reflectanceTexture", (1.0, 1.0, 1.0)))
+        elif kind == "RoughDielectric":   # RoughDielectric.cpp:13-32
+            alpha = self._tex_or(p, "alpha", 0.2)
+            if isinstance(alpha, tuple):
+                alpha = (alpha[0] + alpha[0] + alpha[0]) / 3.0
+            b = D.bsdf(D.BSDF_ROUGH_DIELECTRIC, distribution=_dist(p.get("distribution", "beckmann")),
+                       alpha=alpha, eta_int=p.get("etaInt", 1.5046), eta_ext=p.get("etaExt", 1.000277),
+                       reflectance=self._tex_or(p, "reflectanceTexture", (1.0, 1.0, 1.0)),
+                       transmittance=self._tex_or(p, "transmittedTexture", (1.0, 1.0, 1.0)))
+        elif kind == "SmoothLayeredBSDF":   # SmoothLayeredBSDF.cpp:12-28
+            base = p.get("baseBSDF")
+            albedo = (0.5, 0.5, 0.5)
+            if base is not None:
+                bd = self.s.bsdfs[base]
+                if bd["type"] != D.BSDF_DIFFUSE:
+                    raise UnsupportedScene("SmoothLayeredBSDF over a non-Diffuse base is not provided")
+                albedo = bd["albedo"]
+            b = D.bsdf(D.BSDF_SMOOTH_LAYERED, albedo=albedo, eta_int=p.get("etaInt", 1.5046),
+                       eta_ext=p.get("etaExt", 1.000277), thickness=p.get("thickness", 1.2),
+                       absorbance=p.get("absorbance", (0.0, 0.0, 0.0)))
+        else:
+            raise UnsupportedScene("BSDF type %s is not provided" % kind)
+        return self.s.add_bsdf(b)
+
+    def phase(self, p):
+        ph = p.get("phaseFunction")
+        if ph is None:
+            return dict(phase=D.PHASE_ISOTROPIC)   # Medium.cpp:9
+        _, kind, pp = ph
+        if kind == "HGPhaseFunction":
+            return dict(phase=D.PHASE_HG, g=pp.get("g", -0.8))   # HGPhaseFunction.cpp:8
+        if kind == "IsotropicPhaseFunction":
+            return dict(phase=D.PHASE_ISOTROPIC)
+        raise UnsupportedScene("phase function %s is not provided" % kind)
+
+    def medium(self, el):
+        kind = el.get("type")
+        p = self.props(el)
+        if p.get("temperature", 0.0) or p.get("scaleEmissivity", 1.0) != 1.0:
+            raise UnsupportedScene("emissive media are not provided")
+        if kind == "Homogeneous":   # Homogeneous.cpp:9-14
+            m = dict(type=D.MEDIUM_HOMOGENEOUS, sigma_a=p.get("sigmaA", (0.15, 0.15, 0.15)),
+                     sigma_s=p.get("sigmaS", (0.15, 0.15, 0.15)), scale=p.get("scale", 1.0))
+        elif kind == "Heterogeneous":   # Heterogeneous.cpp:21-37
+            vol = p.get("volume")
+            if vol is None or vol[1] != "GridVolume":
+                raise UnsupportedScene("Heterogeneous media need a GridVolume")
+            dens, lo, hi = load_vol(self.resolve(vol[2].get("path", "")))
+            m = dict(type=D.MEDIUM_HETEROGENEOUS, albedo=p.get("albedo", (0.0, 0.0, 0.0)), density=dens,
+                     grid_min=lo, grid_max=hi, centered=int(p.get("centered", True)),
+                     to_world=np.asarray(p.get("toWorld", np.eye(4)), np.float64), scale=p.get("scale", 1.0))
+        else:
+            raise UnsupportedScene("medium type %s is not provided" % kind)
+        m.update(self.phase(p))
+        return self.s.add_medium(m)
+
+    # XMLLoader::handleObject (XMLLoader.cpp:293-398)
+    def shape(self, el):
+        kind = el.get("type")
+        bsdf, light = -1, None
+        rest = []
+        for c in el:
+            if c.tag == "bsdf":
+                if bsdf >= 0:
+                    warnings.warn("only 1 BSDF allowed for %s" % kind)
+                    continue
+                bsdf = self.ref_bsdf[c.get("ref")] if c.get("ref") else self.bsdf(c)
+            elif c.tag == "light":
+                if light is not None:
+                    warnings.warn("only 1 light allowed for %s" % kind)
+                    continue
+                light = (c.get("type"), self.props(c))
+            elif c.tag == "bssrdf":
+                raise UnsupportedScene("BSSRDFs are not provided")
+            else:
+                rest.append(c)
+        holder = ET.Element("shape")
+        holder.extend(rest)
+        p = self.props(holder)
+        interior = p.get("interior", -1)
+        exterior = p.get("exterior", -1)
+        to_world = np.asarray(p.get("toWorld", np.eye(4, dtype=F32)), F32)
+        if light is not None and light[0] not in ("AreaLight", "MeshLight"):
+            raise UnsupportedScene("shape light type %s is not provided" % light[0])
+        if kind in ("Mesh", "Cube"):
+            if kind == "Mesh":
+                if p.get("useMtl", False):
+                    raise UnsupportedScene("useMtl (OBJ materials) is not provided")
+                from .core import load_obj
+                v, n, _, t = load_obj(self.resolve(p.get("path", "")), to_world)
+            else:
+                v, n, t = cube_mesh(to_world)
+            mi = self.s.add_mesh(v, t, bsdf=bsdf, interior=interior, exterior=exterior, normals=n)
+            if light is not None:   # MeshFactory.h:88-114
+                li = self.s.add_area_light(light[1].get("radiance", (0.0, 0.0, 0.0)), D.SHAPE_MESH, mi,
+                                           mesh_light=light[0] == "MeshLight")
+                self.s.meshes[mi]["light"] = li
+        elif kind == "Sphere":
+            si = self.s.add_sphere(p.get("radius", 1.0), np.asarray(to_world, np.float64), bsdf=bsdf,
+                                   interior=interior, exterior=exterior)
+            if light is not None:
+                li = self.s.add_area_light(light[1].get("radiance", (0.0, 0.0, 0.0)), D.SHAPE_SPHERE, si,
+                                           mesh_light=light[0] == "MeshLight")
+                self.s.spheres[si]["light"] = li
+        else:
+            raise UnsupportedScene("shape type %s is not provided" % kind)
+
+    def camera(self, el):
+        kind = el.get("type")
+        if kind != "NoriPerspective":
+            raise UnsupportedScene("camera type %s is not provided" % kind)
+        rest = []
+        for c in el:
+            if c.tag == "transform":
+                self.camera_transform = _transform(c)
+            elif c.tag == "filter":
+                fp = self.props(c)
+                rx, ry = fp.get("radiusX", 0.5), fp.get("radiusY", 0.5)
+                if c.get("type") != "BoxFilter" or rx != 0.5 or ry != 0.5:
+                    raise UnsupportedScene("filter %s (radius %g x %g) is not provided; the device film "
+                                           "implements the box filter of radius 0.5" % (c.get("type"), rx, ry))
+            else:
+                rest.append(c)
+        holder = ET.Element("camera")
+        holder.extend(rest)
+        self.camera_params = self.props(holder)
+
+    def lights(self, el):
+        for c in el:
+            kind = c.get("type")
+            p = self.props(c)
+            if kind != "EnvironmentLight":
+                raise UnsupportedScene("light type %s is not provided" % kind)
+            if p.get("isProbe", False) or p.get("gamma", 0.0) not in (0.0, 1.0) or p.get("offsetU", 0.0) \
+                    or p.get("offsetV", 0.0):
+                raise UnsupportedScene("EnvironmentLight isProbe / gamma / offsets are not provided")
+            from .core import load_hdr
+            path = self.resolve(p.get("path", ""))
+            if not path.lower().endswith(".hdr"):
+                raise UnsupportedScene("environment maps other than Radiance .hdr are not provided")
+            rgb = load_hdr(path)
+            self.s.add_env_light(rgb, scale=p.get("scale", 1.0),
+                                 to_world=np.asarray(p.get("toWorld", np.eye(4)), np.float64))
+
+    def load(self):
+        root = ET.parse(self.path).getroot()
+        for el in root:   # XMLLoader.cpp:56-133
+            key = el.tag
+            if key == "camera":
+                self.camera(el)
+            elif key == "lights":
+                self.lights(el)
+            elif key == "parameters":
+                bx, by = 32, 32
+                for c in el:
+                    if c.tag == "blockSizeX":
+                        bx = int(c.text)
+                    elif c.tag == "blockSizeY":
+                        by = int(c.text)
+                self.block = (bx, by)
+            elif key == "sampler":
+                if el.get("type") != "RandomSampler":
+                    raise UnsupportedScene("sampler %s is not provided" % el.get("type"))
+                self.spp = int(self.props(el).get("sampleNumber", 1))
+            elif key == "integrator":
+                kind = el.get("type")
+                p = self.props(el)
+                ig = {"PathTracingMIS": D.INTEGRATOR_PATH_MIS, "VolPathTracing": D.INTEGRATOR_VOLPATH}.get(kind)
+                if ig is None:
+                    raise UnsupportedScene("integrator %s is not provided" % kind)
+                strat = {"all_lights": D.STRATEGY_ALL_LIGHTS, "one_light_uniform": D.STRATEGY_ONE_LIGHT_UNIFORM,
+                         "one_light_weighted": D.STRATEGY_ONE_LIGHT_WEIGHTED}[p.get("strategy", "one_light_uniform")]
+                self.s.integrator = dict(integrator=ig, max_depth=p.get("maxDepth", 1000),
+                                         min_depth=p.get("minDepth", 3), strategy=strat)
+            elif key == "medium":
+                self.camera_medium = self.medium(el)
+                if el.get("id"):
+                    self.ref_medium[el.get("id")] = self.camera_medium
+            elif key == "objects":
+                for c in el:
+                    self.shape(c)
+            elif key == "bsdf":
+                self.ref_bsdf[el.get("id")] = self.bsdf(el)
+            elif key == "transform":
+                self.ref_transform[el.get("id")] = _transform(el)
+        if self.camera_params is None:
+            raise UnsupportedScene("the scene has no camera")
+        cp = self.camera_params
+        cam = D.camera(int(cp.get("sizeX", 768)), int(cp.get("sizeY", 768)), cp.get("fov", 30.0),
+                       np.asarray(self.camera_transform, np.float64), near=cp.get("nearClip", 1e-4),
+                       far=cp.get("farClip", 1e4), medium=self.camera_medium)
+        cam["aperture_radius"] = cp.get("apertureRadius", 0.0)
+        cam["focal_plane"] = cp.get("focalPlane", 3.4028234663852886e38)
+        self.s.camera = cam
+        self.s.spp = self.spp
+        self.s.block = self.block
+        return self.s
+
+
+def _dist(name):
+    # MicrofacetDistribution names (bsdf/MicrofacetDistribution.h:9-13)
+    d = {"beckmann": D.DIST_BECKMANN, "phong": D.DIST_PHONG, "ggx": D.DIST_GGX}.get(name)
+    if d is None:
+        raise UnsupportedScene("microfacet distribution %s is not provided" % name)
+    return d
+
+
+def cube_mesh(to_world):
+    """The Cube shape's mesh (geometricShape/Cube.cpp): the [-1, 1]^3 cube as
+    six faces of four vertices with face normals, two triangles per face,
+    in the reference's face and vertex order, transformed to world."""
+    faces = [  # (normal axis, sign, four corners)
+        ((0, -1, 0), [(1, -1, -1), (1, -1, 1), (-1, -1, 1), (-1, -1, -1)]),
+        ((0, 1, 0), [(1, 1, -1), (-1, 1, -1), (-1, 1, 1), (1, 1, 1)]),
+        ((1, 0, 0), [(1, -1, -1), (1, 1, -1), (1, 1, 1), (1, -1, 1)]),
+        ((0, 0, 1), [(1, -1, 1), (1, 1, 1), (-1, 1, 1), (-1, -1, 1)]),
+        ((-1, 0, 0), [(-1, -1, 1), (-1, 1, 1), (-1, 1, -1), (-1, -1, -1)]),
+        ((0, 0, -1), [(1, 1, -1), (1, -1, -1), (-1, -1, -1), (-1, 1, -1)]),
+    ]
+    M = np.asarray(to_world, F32)
+    NI = np.linalg.inv(M[:3, :3].astype(np.float64)).T.astype(F32)
+    v, n, t = [], [], []
+    for f, (nrm, quad) in enumerate(faces):
+        for q in quad:
+            p = np.asarray(q, F32)
+            x = ((M[0, 0] * p[0] + M[0, 1] * p[1]) + M[0, 2] * p[2]) + M[0, 3]
+            y = ((M[1, 0] * p[0] + M[1, 1] * p[1]) + M[1, 2] * p[2]) + M[1, 3]
+            z = ((M[2, 0] * p[0] + M[2, 1] * p[1]) + M[2, 2] * p[2]) + M[2, 3]
+            w = ((M[3, 0] * p[0] + M[3, 1] * p[1]) + M[3, 2] * p[2]) + M[3, 3]
+            if w != 1 and w != 0:
+                x, y, z = x / w, y / w, z / w
+            v.append((x, y, z))
+            n.append(NI @ np.asarray(nrm, F32))
+        b = 4 * f
+        t += [(b, b + 1, b + 2), (b + 3, b, b + 2)]
+    return np.asarray(v, F32), np.asarray(n, F32), np.asarray(t, np.int32)
+
+
+def load_vol(path):
+    """GridVolume file (volume/GridVolume.cpp:7-59): "VOL", version 3, an
+    encoding id, x/y/z resolution, a channel count and the float bounding
+    box, then float data with x fastest.  The reference skips four bytes
+    after the header before it reads the data (GridVolume.cpp:52-54), so
+    voxel i holds the file's value i + 1 and the last voxel is left unread;
+    the same offset is applied here, with 0 in the last voxel."""
+    raw = open(path, "rb").read()
+    if raw[:3] != b"VOL" or raw[3] != 3:
+        raise ValueError("%s is not a valid volume data file" % path)
+    rx, ry, rz, _ch = np.frombuffer(raw, "<i4", 4, 8)
+    lo = tuple(float(x) for x in np.frombuffer(raw, "<f4", 3, 24))
+    hi = tuple(float(x) for x in np.frombuffer(raw, "<f4", 3, 36))
+    n = int(rx) * int(ry) * int(rz)
+    data = np.frombuffer(raw, "<f4", min(n, max(0, (len(raw) - 52) // 4)), 52).astype(np.float32)
+    dens = np.zeros(n, np.float32)
+    dens[:len(data)] = data
+    return dens.reshape(int(rz), int(ry), int(rx)), lo, hi
+
+
+def load_scene(path, materials=None):
+    """Read a reference scene file.  `materials` maps conductor material
+    names (material="gold") to (eta rgb, k rgb); the reference derives them
+    from spectral data files (tools/Common.cpp:56-81)."""
+    return _Loader(path, materials).load()

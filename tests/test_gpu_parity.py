@@ -317,6 +317,18 @@ def test_film_parity_volume(ctx, rtlib, vol):
     _film_parity(ctx, rtlib, vol, 2, 4, max_bad=0.08)
 
 
+def test_film_parity_mixed_normals(ctx, rtlib):
+    """One mesh with vertex normals (shading normals), the others without
+    (NaN-marked, geometric normals), in one scene."""
+    s = scenes.cornell_box(40, 32)
+    v, f = scenes.icosphere(2)
+    gold = s.add_bsdf(D.bsdf(D.BSDF_ROUGH_CONDUCTOR, distribution=D.DIST_GGX, alpha=0.3,
+                             eta=scenes.AU_ETA, k=scenes.AU_K))
+    s.add_mesh(v * 0.15 + np.array([0.5, 0.75, 0.5]), f, bsdf=gold, normals=v)
+    assert np.isnan(s.normals[0]).all() and not np.isnan(s.normals[-1]).any()
+    _film_parity(ctx, rtlib, s, 4, 21, max_bad=0.03)
+
+
 def test_depth_limits(ctx, rtlib, cornell):
     for md in (0, 1, 2):
         _film_parity(ctx, rtlib, cornell, 1, 2, max_bad=0.02, max_depth=md, min_depth=0)
