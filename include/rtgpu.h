@@ -54,7 +54,8 @@ enum {
 /* ------------------------------------------------------------------ */
 
 enum { RT_BSDF_DIFFUSE = 0, RT_BSDF_ROUGH_CONDUCTOR = 1,
-       RT_BSDF_ROUGH_DIELECTRIC = 2, RT_BSDF_SMOOTH_LAYERED = 3 };
+       RT_BSDF_ROUGH_DIELECTRIC = 2, RT_BSDF_SMOOTH_LAYERED = 3,
+       RT_BSDF_LAYERED = 4 };
 /* bsdf/MicrofacetDistribution.h:9-13 name order */
 enum { RT_DIST_BECKMANN = 0, RT_DIST_PHONG = 1, RT_DIST_GGX = 2 };
 
@@ -69,8 +70,13 @@ typedef struct rt_bsdf_desc {
     float alpha;             /* "alpha" (constant texture), default 0.2          */
     float eta_int;           /* default 1.5046                                   */
     float eta_ext;           /* default 1.000277                                 */
-    float thickness;         /* SmoothLayered, default 1.2                       */
-    float absorbance[3];     /* SmoothLayered, default 0                         */
+    float thickness;         /* SmoothLayered / Layered, default 1.2             */
+    float absorbance[3];     /* SmoothLayered / Layered, default 0               */
+    /* LayeredBSDF (bsdf/LayeredBSDF.cpp:17-36): `distribution` (default ggx) and
+     * `alpha` ("alphaTop", default 0.01) describe the coat; the base
+     * RoughConductor takes eta, k, reflectance and these two: */
+    int32_t distribution_base; /* default beckmann                               */
+    float alpha_base;          /* default 0.2                                    */
 } rt_bsdf_desc;
 
 /* One reference Mesh (factory/MeshFactory.h:39-139): a contiguous range of

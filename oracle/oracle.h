@@ -170,7 +170,8 @@ enum { O_BSDF_UNKNOWN = 0, O_BSDF_DIFFUSE_REFLECTION = 1, O_BSDF_DELTA_REFLECTIO
 
 c3 o_bsdf_eval(const rt_bsdf_desc *b, const o_bsdf_rec *r);
 float o_bsdf_pdf(const rt_bsdf_desc *b, const o_bsdf_rec *r);
-c3 o_bsdf_sample(const rt_bsdf_desc *b, o_bsdf_rec *r, v2 s);
+/* aux_key: the side-stream key of a LayeredBSDF sample (o_ly_sample) */
+c3 o_bsdf_sample(const rt_bsdf_desc *b, o_bsdf_rec *r, v2 s, uint64_t aux_key);
 
 /* light sample record (light/Light.h LightSamplingInfos) */
 typedef struct {

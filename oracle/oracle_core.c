@@ -594,6 +594,134 @@ static c3 o_sl_sample(const rt_bsdf_desc *b, o_bsdf_rec *r, v2 s)
     return res;
 }
 
+/* ===================== LayeredBSDF (bsdf/LayeredBSDF.cpp:17-310) =====================
+ * A rough dielectric coat (distribution / alpha = "alphaTop", read as a plain
+ * real) over a RoughConductor base (distribution_base, alpha_base, eta, k,
+ * reflectance).  sample() draws its coat normal from a member Rng of the BSDF
+ * in the reference (LayeredBSDF.cpp:165); here from a side stream keyed by
+ * aux_key, the path stream's state after the BSDF sample was drawn, so the
+ * path stream itself advances as in the reference. */
+static rt_bsdf_desc o_ly_base(const rt_bsdf_desc *b)
+{
+    rt_bsdf_desc c = *b;
+    c.type = RT_BSDF_ROUGH_CONDUCTOR;
+    c.distribution = b->distribution_base;
+    c.alpha = b->alpha_base;
+    return c;
+}
+/* LayeredBSDF::evalReflection (LayeredBSDF.cpp:150-163) */
+static c3 o_ly_eval_reflection(const rt_bsdf_desc *b, v3 wi, v3 wo, float fr, float alpha)
+{
+    float ci = wi.z, co = wo.z;
+    v3 wh = v3_normalized(v3_add(wi, wo));
+    wh = v3_smul(o_sign(ci), wh);
+    c3 term = c3_muls(cfill(fr), o_mf_D(b->distribution, wh, alpha));
+    term = c3_muls(term, o_mf_G(b->distribution, wi, wo, wh, alpha));
+    return c3_divs(term, 4 * ci * co);
+}
+/* LayeredBSDF::eval (LayeredBSDF.cpp:79-147) */
+static c3 o_ly_eval(const rt_bsdf_desc *b, v3 wi, v3 wo)
+{
+    if (wi.z <= 0.f || wo.z <= 0.f) return cfill(0.f);
+    v3 wh = v3_normalized(v3_add(wi, wo));
+    float eI, eT, rel, cT;
+    float fr1 = o_fr_avg(o_estimate_dielectric(b->eta_ext, b->eta_int, v3_dot(wi, wh), &eI, &eT, &rel, &cT));
+    float T12 = 1.f - fr1;
+    float G = o_mf_G(b->distribution, wi, wo, wh, b->alpha);
+    if (fr1 == 1.f) return cfill(0.f);
+    v3 rwi = v3_normalized(o_refract_n(wi, wh, rel, cT));
+    v3 rwo = v3_normalized(o_refract_n(wo, wh, rel, cT));
+    c3 f1 = o_ly_eval_reflection(b, wi, wo, fr1, b->alpha);
+    rwi = v3_smul(-1.f, rwi);
+    rwo = v3_smul(-1.f, rwo);
+    wh = v3_normalized(v3_add(rwi, rwo));
+    float fr2 = o_fr_avg(o_estimate_dielectric(b->eta_ext, b->eta_int, v3_dot(v3_smul(-1.f, rwo), wh),
+                                               &eI, &eT, &rel, &cT));
+    if (fr2 == 1.f) return cfill(0.f);
+    float T21 = 1.f - fr2;
+    rel = b->eta_ext / b->eta_int;
+    rt_bsdf_desc base = o_ly_base(b);
+    c3 f2 = c3_muls(o_rc_eval(&base, rwi, rwo), rel);
+    f2 = c3_muls(f2, rel);
+    f2 = c3_muls(f2, wo.z);
+    f2 = c3_divs(f2, rwo.z);
+    float sum = 1.f / fabsf(rwi.z) + 1.f / fabsf(rwo.z);
+    c3 ab = c3_muls(c3_muls(c3_from(b->absorbance), -1.f), b->thickness);
+    ab = c3_muls(ab, sum);
+    c3 a = mkc(expf(ab.r), expf(ab.g), expf(ab.b));
+    float t = (1.f - G) + T21 * G;
+    c3 r = c3_muls(f2, T12);
+    r = c3_mul(r, a);
+    r = c3_muls(r, t);
+    return c3_add(f1, r);
+}
+/* LayeredBSDF::pdf (LayeredBSDF.cpp:262-303) */
+static float o_ly_pdf(const rt_bsdf_desc *b, v3 wi, v3 wo)
+{
+    v3 wh = v3_normalized(v3_add(wi, wo));
+    float eI, eT, rel, cT;
+    float fr1 = o_fr_avg(o_estimate_dielectric(b->eta_ext, b->eta_int, v3_dot(wi, wh), &eI, &eT, &rel, &cT));
+    if (fr1 == 1.f) return 0.f;
+    v3 rwi = v3_normalized(o_refract_n(wi, wh, rel, cT));
+    v3 rwo = v3_normalized(o_refract_n(wo, wh, rel, cT));
+    float ch = wh.z;
+    float Jh = 1.f / (4 * fabsf(v3_dot(wh, wo)));
+    float D = o_mf_D(b->distribution, wh, b->alpha);
+    float pd = fabsf(D * ch * Jh);
+    rwi = v3_smul(-1.f, rwi);
+    rwo = v3_smul(-1.f, rwo);
+    rt_bsdf_desc base = o_ly_base(b);
+    float pc = o_rc_pdf(&base, rwi, rwo);
+    rel = b->eta_ext / b->eta_int;
+    float q = pc * (1.f - fr1);
+    q = q * rel;
+    q = q * rel;
+    q = q * wo.z;
+    q = q / rwo.z;
+    return pd * fr1 + q;
+}
+/* LayeredBSDF::sample (LayeredBSDF.cpp:165-260) */
+static c3 o_ly_sample(const rt_bsdf_desc *b, o_bsdf_rec *r, v2 s, uint64_t aux_key)
+{
+    if (r->wi.z <= 0.f) return cfill(0.f);
+    float ci = r->wi.z;
+    float alpha = (1.2f - 0.2f * sqrtf(fabsf(ci))) * b->alpha;
+    o_pcg32 aux;
+    o_pcg_seed(&aux, aux_key ^ 0x9E3779B97F4A7C15ull, 0x4C61796572656442ull);
+    float n1 = o_pcg_float(&aux);
+    float n2 = o_pcg_float(&aux);
+    v3 normal = o_mf_sample_normal(b->distribution, mk2(n1, n2), alpha);
+    float eI, eT, rel, cT;
+    float fr1 = o_fr_avg(o_estimate_dielectric(b->eta_ext, b->eta_int, v3_dot(r->wi, normal), &eI, &eT, &rel, &cT));
+    if (fr1 == 1.f) return cfill(0.f);
+    if (s.x <= fr1) {
+        r->wo = o_reflect_n(r->wi, normal);
+        r->pdf = o_ly_pdf(b, r->wi, r->wo);
+        r->sampled_type = O_BSDF_GLOSSY_REFLECTION;
+        c3 f1 = o_ly_eval_reflection(b, r->wi, r->wo, fr1, alpha);
+        if (c3_iszero(f1)) return cfill(0.f);
+    } else {
+        r->sampled_type = O_BSDF_GLOSSY_REFLECTION;
+        v3 rwi = v3_normalized(v3_smul(-1.f, o_refract_n(r->wi, normal, rel, cT)));
+        o_bsdf_rec rr;
+        memset(&rr, 0, sizeof(rr));
+        rr.wi = rwi;
+        rr.relative_eta = 1.f;
+        rt_bsdf_desc base = o_ly_base(b);
+        c3 f2 = o_rc_sample(&base, &rr, s);
+        if (c3_iszero(f2)) return cfill(0.f);
+        r->wo = v3_smul(-1.f, rr.wo);
+        float fr2 = o_fr_avg(o_estimate_dielectric(b->eta_ext, b->eta_int, r->wo.z, &eI, &eT, &rel, &cT));
+        if (fr2 == 1.f) return cfill(0.f);
+        r->wo = v3_normalized(o_refract_n(r->wo, normal, rel, cT));
+        r->pdf = o_ly_pdf(b, r->wi, r->wo);
+        if (r->pdf == 0.f) return cfill(0.f);
+    }
+    if (r->pdf == 0.f) return cfill(0.f);
+    float co = r->wo.z;
+    return c3_divs(c3_muls(o_ly_eval(b, r->wi, r->wo), fabsf(co)), r->pdf);
+}
+
 /* ===================== BSDF dispatch ===================== */
 c3 o_bsdf_eval(const rt_bsdf_desc *b, const o_bsdf_rec *r)
 {
@@ -602,6 +730,7 @@ c3 o_bsdf_eval(const rt_bsdf_desc *b, const o_bsdf_rec *r)
     case RT_BSDF_ROUGH_CONDUCTOR: return o_rc_eval(b, r->wi, r->wo);
     case RT_BSDF_ROUGH_DIELECTRIC: return o_rd_eval(b, r->wi, r->wo);
     case RT_BSDF_SMOOTH_LAYERED: return o_sl_eval(b, r->wi, r->wo);
+    case RT_BSDF_LAYERED: return o_ly_eval(b, r->wi, r->wo);
     }
     return cfill(0.f);
 }
@@ -612,16 +741,18 @@ float o_bsdf_pdf(const rt_bsdf_desc *b, const o_bsdf_rec *r)
     case RT_BSDF_ROUGH_CONDUCTOR: return o_rc_pdf(b, r->wi, r->wo);
     case RT_BSDF_ROUGH_DIELECTRIC: return o_rd_pdf(b, r->wi, r->wo);
     case RT_BSDF_SMOOTH_LAYERED: return o_sl_pdf(b, r->wi, r->wo);
+    case RT_BSDF_LAYERED: return o_ly_pdf(b, r->wi, r->wo);
     }
     return 0.f;
 }
-c3 o_bsdf_sample(const rt_bsdf_desc *b, o_bsdf_rec *r, v2 s)
+c3 o_bsdf_sample(const rt_bsdf_desc *b, o_bsdf_rec *r, v2 s, uint64_t aux_key)
 {
     switch (b->type) {
     case RT_BSDF_DIFFUSE: return o_diffuse_sample(b->albedo, r, s);
     case RT_BSDF_ROUGH_CONDUCTOR: return o_rc_sample(b, r, s);
     case RT_BSDF_ROUGH_DIELECTRIC: return o_rd_sample(b, r, s);
     case RT_BSDF_SMOOTH_LAYERED: return o_sl_sample(b, r, s);
+    case RT_BSDF_LAYERED: return o_ly_sample(b, r, s, aux_key);
     }
     return cfill(0.f);
 }

@@ -392,7 +392,7 @@ static c3 li_path_mis(const o_scene *sc, const rt_render_desc *rd, o_sampler *s,
         r.wi = to_local(&it, v3_neg(ray.d)); r.wo = mk3(0, 0, 0);
         r.sampled_type = O_BSDF_ALL; r.relative_eta = 1.f; r.pdf = -1.f;
         v2 u = o_next2d(s);
-        c3 f = o_bsdf_sample(B, &r, u);
+        c3 f = o_bsdf_sample(B, &r, u, s->rng.state);
         if (c3_iszero(f)) break;
         o_ray refl = o_ray_make(it.p, to_world(&it, r.wo), O_EPSILON, O_MAX_REAL);
         o_hit nx;
@@ -538,7 +538,8 @@ static c3 li_volpath(const o_scene *sc, const rt_render_desc *rd, o_sampler *s, 
             o_bsdf_rec r;
             r.wi = to_local(&it, v3_neg(ray.d)); r.wo = mk3(0, 0, 0);
             r.sampled_type = O_BSDF_ALL; r.relative_eta = 1.f; r.pdf = -1.f;
-            c3 f = o_bsdf_sample(B, &r, o_next2d(s));
+            v2 bu = o_next2d(s);
+            c3 f = o_bsdf_sample(B, &r, bu, s->rng.state);
             if (c3_iszero(f)) break;
             ray = o_ray_make(it.p, to_world(&it, r.wo), O_EPSILON, O_MAX_REAL);
             if (hit_transition(sc, &it)) medium = hit_medium(sc, &it, ray.d);
@@ -744,7 +745,10 @@ int32_t oracle_bsdf_query(const rt_bsdf_desc *b, int32_t op, const rt_bsdf_q *q,
             r[i].pdf = o_bsdf_pdf(b, &rec);
         } else {
             rec.wo = mk3(0, 0, 0);
-            c3 v = o_bsdf_sample(b, &rec, mk2(q[i].u[0], q[i].u[1]));
+            union { float f; uint32_t u; } ux, uy;
+            ux.f = q[i].u[0];
+            uy.f = q[i].u[1];
+            c3 v = o_bsdf_sample(b, &rec, mk2(q[i].u[0], q[i].u[1]), ((uint64_t)ux.u << 32) | uy.u);
             r[i].value[0] = v.r; r[i].value[1] = v.g; r[i].value[2] = v.b;
             r[i].pdf = rec.pdf;
             r[i].wo[0] = rec.wo.x; r[i].wo[1] = rec.wo.y; r[i].wo[2] = rec.wo.z;

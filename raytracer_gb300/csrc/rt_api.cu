@@ -144,7 +144,7 @@ __device__ __forceinline__ void classify_hit(const RenderParams &P, RoundCounter
 {
     const int t = prim == -1 ? -1 : prim_type(P.S, prim);
 #pragma unroll
-    for (int k = 0; k < 4; k++) q_push(P.W.q_mat[k], &C->mat[k], slot, t == k);
+    for (int k = 0; k < RT_NBSDF; k++) q_push(P.W.q_mat[k], &C->mat[k], slot, t == k);
     q_push(P.W.q_fin, &C->fin, slot, t < 0);
 }
 
@@ -617,7 +617,8 @@ __device__ __forceinline__ C3 bsdf_eval_t(const DevBsdf &b, V3 wi, V3 wo)
     if (BT == 0) return diffuse_eval(b.albedo, wi, wo);
     if (BT == 1) return rc_eval(b, wi, wo);
     if (BT == 2) return rd_eval(b, wi, wo);
-    return sl_eval(b, wi, wo);
+    if (BT == 3) return sl_eval(b, wi, wo);
+    return ly_eval(b, wi, wo);
 }
 template <int BT>
 __device__ __forceinline__ float bsdf_pdf_t(const DevBsdf &b, V3 wi, V3 wo)
@@ -625,15 +626,17 @@ __device__ __forceinline__ float bsdf_pdf_t(const DevBsdf &b, V3 wi, V3 wo)
     if (BT == 0) return diffuse_pdf(wi, wo);
     if (BT == 1) return rc_pdf(b, wi, wo);
     if (BT == 2) return rd_pdf(b, wi, wo);
-    return sl_pdf(b, wi, wo);
+    if (BT == 3) return sl_pdf(b, wi, wo);
+    return ly_pdf(b, wi, wo);
 }
 template <int BT>
-__device__ __forceinline__ C3 bsdf_sample_t(const DevBsdf &b, BsdfRec &r, V2 s)
+__device__ __forceinline__ C3 bsdf_sample_t(const DevBsdf &b, BsdfRec &r, V2 s, uint64_t aux_key)
 {
     if (BT == 0) return diffuse_sample(b.albedo, r, s);
     if (BT == 1) return rc_sample(b, r, s);
     if (BT == 2) return rd_sample(b, r, s);
-    return sl_sample(b, r, s);
+    if (BT == 3) return sl_sample(b, r, s);
+    return ly_sample(b, r, s, aux_key);
 }
 
 #ifndef RT_SHADE_MINB
@@ -748,7 +751,7 @@ __global__ void __launch_bounds__(128, RT_SHADE_MINB) k_pt_shade(RenderParams P,
             r.wi = to_local(fr, -d); r.wo = v3(0, 0, 0);
             r.type = BT_ALL; r.rel_eta = 1.f; r.pdf = -1.f;
             V2 u = next2d(rng);
-            C3 f = bsdf_sample_t<BT>(B, r, u);
+            C3 f = bsdf_sample_t<BT>(B, r, u, rng.state);
             if (iszero(f)) {
                 if (flags & F_NEE) {
                     flags |= F_END;   // the light sample still needs its shadow ray
@@ -796,7 +799,10 @@ __device__ __noinline__ bool vp_medium_sample(const DevMedium &m, Ray r, Pcg32 &
 {
     return medium_sample(m, r, rng, t, w, em, limit);
 }
-__device__ __noinline__ C3 vp_bsdf_sample(const DevBsdf &b, BsdfRec &r, V2 u) { return bsdf_sample(b, r, u); }
+__device__ __noinline__ C3 vp_bsdf_sample(const DevBsdf &b, BsdfRec &r, V2 u, uint64_t aux_key)
+{
+    return bsdf_sample(b, r, u, aux_key);
+}
 __device__ __noinline__ C3 vp_bsdf_eval(const DevBsdf &b, V3 wi, V3 wo) { return bsdf_eval(b, wi, wo); }
 __device__ __noinline__ float vp_bsdf_pdf(const DevBsdf &b, V3 wi, V3 wo) { return bsdf_pdf(b, wi, wo); }
 __device__ __noinline__ void vp_light_sample(const DevScene &S, int idx, V3 p, V2 u, LightRec &li)
@@ -992,7 +998,8 @@ __device__ bool vol_step(const DevScene &S, VolState &st, Pcg32 &rng, int max_de
         BsdfRec r;
         r.wi = to_local(fr, -ray.d); r.wo = v3(0, 0, 0);
         r.type = BT_ALL; r.rel_eta = 1.f; r.pdf = -1.f;
-        C3 f = vp_bsdf_sample(B, r, next2d(rng));
+        V2 bu = next2d(rng);
+        C3 f = vp_bsdf_sample(B, r, bu, rng.state);
         if (iszero(f)) return false;
         V3 pfrom = fr.p;
         ray = make_ray(fr.p, to_world(fr, r.wo), RT_EPSILON, RT_MAX_REAL);
@@ -1143,7 +1150,9 @@ __global__ void k_bsdf_query(DevScene S, int bsdf, int op, const rt_bsdf_q *q, i
     } else {
         BsdfRec rec;
         rec.wi = wi; rec.wo = v3(0, 0, 0); rec.type = BT_ALL; rec.rel_eta = 1.f; rec.pdf = -1.f;
-        C3 v = bsdf_sample(B, rec, v2(q[i].u[0], q[i].u[1]));
+        // a LayeredBSDF query keys its coat-normal side stream by the sample's bits
+        uint64_t key = ((uint64_t)__float_as_uint(q[i].u[0]) << 32) | __float_as_uint(q[i].u[1]);
+        C3 v = bsdf_sample(B, rec, v2(q[i].u[0], q[i].u[1]), key);
         r.value[0] = v.r; r.value[1] = v.g; r.value[2] = v.b;
         r.pdf = rec.pdf;
         r.wo[0] = rec.wo.x; r.wo[1] = rec.wo.y; r.wo[2] = rec.wo.z;
@@ -1545,7 +1554,7 @@ static rt_status validate(const rt_scene_desc *d)
         }
     }
     for (int b = 0; b < d->n_bsdfs; b++)
-        if (d->bsdfs[b].type < 0 || d->bsdfs[b].type > 3) return fail(RT_ERR_UNSUPPORTED, "BSDF type not supported");
+        if (d->bsdfs[b].type < 0 || d->bsdfs[b].type > 4) return fail(RT_ERR_UNSUPPORTED, "BSDF type not supported");
     for (int m = 0; m < d->n_media; m++) {
         const rt_medium_desc &M = d->media[m];
         if (M.type == RT_MEDIUM_HETEROGENEOUS && (!M.density || M.res[0] < 2 || M.res[1] < 2 || M.res[2] < 2))
@@ -1648,6 +1657,8 @@ rt_status rt_scene_create(rt_ctx *ctx, const rt_scene_desc *d, rt_scene **out)
         }
         D.alpha = B.alpha;
         D.alpha_avg = h_cavg1(B.alpha);
+        D.dist_base = B.distribution_base;
+        D.alpha_base_avg = h_cavg1(B.alpha_base);
         D.eta_int = B.eta_int; D.eta_ext = B.eta_ext; D.thickness = B.thickness;
     }
     // media
@@ -1860,7 +1871,7 @@ static rt_status ensure_wave(rt_ctx *c, int capacity, int max_rounds)
     ok &= alloc((void **)&W.q_end, P * sizeof(int));
     ok &= alloc((void **)&W.q_closest, P * sizeof(int));
     ok &= alloc((void **)&W.q_shadow, P * sizeof(int));
-    for (int t = 0; t < 4; t++) ok &= alloc((void **)&W.q_mat[t], P * sizeof(int));
+    for (int t = 0; t < RT_NBSDF; t++) ok &= alloc((void **)&W.q_mat[t], P * sizeof(int));
     ok &= alloc((void **)&W.cnt, (size_t)(max_rounds + 2) * sizeof(RoundCounters));
     if (!ok) { free_wave(c); return fail(RT_ERR_NOMEM, "wavefront buffer allocation failed"); }
     W.capacity = capacity;
@@ -2038,6 +2049,7 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
                 if (sc->bsdf_types & 2) k_pt_shade<1><<<shade_blocks, 128, 0, st>>>(P, ri);
                 if (sc->bsdf_types & 4) k_pt_shade<2><<<shade_blocks, 128, 0, st>>>(P, ri);
                 if (sc->bsdf_types & 8) k_pt_shade<3><<<shade_blocks, 128, 0, st>>>(P, ri);
+                if (sc->bsdf_types & 16) k_pt_shade<4><<<shade_blocks, 128, 0, st>>>(P, ri);
                 prof_end(ctx);
                 launches += 3 + __builtin_popcount(sc->bsdf_types);
                 trace_c_launches++;
@@ -2335,7 +2347,7 @@ extern "C" rt_status rt_render_tile_static(rt_ctx *ctx, rt_scene *sc, const rt_r
     W.q_end = (int *)take(P * sizeof(int));
     W.q_closest = (int *)take(P * sizeof(int));
     W.q_shadow = (int *)take(P * sizeof(int));
-    for (int t = 0; t < 4; t++) W.q_mat[t] = (int *)take(P * sizeof(int));
+    for (int t = 0; t < RT_NBSDF; t++) W.q_mat[t] = (int *)take(P * sizeof(int));
     W.cnt = (RoundCounters *)take((size_t)(rounds + 2) * sizeof(RoundCounters));
     W.capacity = (int)P;
     W.max_rounds = rounds;
@@ -2413,6 +2425,7 @@ extern "C" rt_status rt_render_tile_static(rt_ctx *ctx, rt_scene *sc, const rt_r
             if (sc->bsdf_types & 2) k_pt_shade<1><<<blocks, 128, 0, st>>>(Pm, r);
             if (sc->bsdf_types & 4) k_pt_shade<2><<<blocks, 128, 0, st>>>(Pm, r);
             if (sc->bsdf_types & 8) k_pt_shade<3><<<blocks, 128, 0, st>>>(Pm, r);
+            if (sc->bsdf_types & 16) k_pt_shade<4><<<blocks, 128, 0, st>>>(Pm, r);
             if ((s = launch_check("pt round (static)")) != RT_OK) return s;
             if ((r & 3) == 3 && r + 1 < rounds) {
                 RoundCounters nc;

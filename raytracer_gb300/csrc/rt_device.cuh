@@ -30,6 +30,10 @@ struct DevBsdf {
     float alpha_avg;  // Color(alpha).average() as the BSDFs read it
     float eta_int, eta_ext, thickness;
     float absorbance[3];
+    // LayeredBSDF: its base RoughConductor's distribution and alpha (the
+    // base's eta, k and reflectance use the fields above)
+    int dist_base;
+    float alpha_base_avg;
 };
 
 struct DevLight {
@@ -840,13 +844,146 @@ __device__ __forceinline__ C3 sl_sample(const DevBsdf &b, BsdfRec &r, V2 s)
     return res;
 }
 
+// LayeredBSDF (bsdf/LayeredBSDF.cpp:17-310): a rough dielectric coat (GGX
+// by default, alphaTop read as a plain real, so `alpha` here, not the
+// texture average) over a RoughConductor base.  The reference draws the
+// coat normal of sample() from a member Rng of the BSDF object (shared by
+// all threads, LayeredBSDF.cpp:165), not from the sampler.  Here those two
+// numbers come from a side stream keyed by the path's state after its BSDF
+// sample was drawn (layered_aux), so the path's own stream advances exactly
+// as in the reference and the result stays reproducible.
+__device__ __forceinline__ Pcg32 layered_aux(uint64_t key)
+{
+    Pcg32 a;
+    pcg_seed(a, key ^ 0x9E3779B97F4A7C15ull, 0x4C61796572656442ull);
+    return a;
+}
+__device__ __forceinline__ DevBsdf layered_base(const DevBsdf &b)
+{
+    DevBsdf c = b;
+    c.type = 1;
+    c.distribution = b.dist_base;
+    c.alpha_avg = b.alpha_base_avg;
+    return c;
+}
+// LayeredBSDF::evalReflection (LayeredBSDF.cpp:150-163)
+__device__ __forceinline__ C3 ly_eval_reflection(const DevBsdf &b, V3 wi, V3 wo, float fr, float alpha)
+{
+    float ci = wi.z, co = wo.z;
+    V3 wh = normalized(wi + wo);
+    wh = fsign(ci) * wh;
+    C3 term = mf_D(b.distribution, wh, alpha) * cfill(fr);
+    term = term * mf_G(b.distribution, wi, wo, wh, alpha);
+    return term / (4 * ci * co);
+}
+// LayeredBSDF::eval (LayeredBSDF.cpp:79-147)
+__device__ __forceinline__ C3 ly_eval(const DevBsdf &b, V3 wi, V3 wo)
+{
+    if (wi.z <= 0.f || wo.z <= 0.f) return cfill(0.f);
+    V3 wh = normalized(wi + wo);
+    float eI, eT, rel, cT;
+    float fr1 = cavg1(estimate_dielectric(b.eta_ext, b.eta_int, dot(wi, wh), eI, eT, rel, cT));
+    float T12 = 1.f - fr1;
+    float G = mf_G(b.distribution, wi, wo, wh, b.alpha);
+    if (fr1 == 1.f) return cfill(0.f);
+    V3 rwi = normalized(refract_n(wi, wh, rel, cT));
+    V3 rwo = normalized(refract_n(wo, wh, rel, cT));
+    C3 f1 = ly_eval_reflection(b, wi, wo, fr1, b.alpha);
+    rwi = -1.f * rwi;
+    rwo = -1.f * rwo;
+    wh = normalized(rwi + rwo);
+    float fr2 = cavg1(estimate_dielectric(b.eta_ext, b.eta_int, dot(-1.f * rwo, wh), eI, eT, rel, cT));
+    if (fr2 == 1.f) return cfill(0.f);
+    float T21 = 1.f - fr2;
+    rel = b.eta_ext / b.eta_int;
+    DevBsdf base = layered_base(b);
+    C3 f2 = rc_eval(base, rwi, rwo) * rel;
+    f2 = f2 * rel;
+    f2 = f2 * wo.z;
+    f2 = f2 / rwo.z;
+    float s = 1.f / fabsf(rwi.z) + 1.f / fabsf(rwo.z);
+    C3 ab = (cload(b.absorbance) * -1.f) * b.thickness;
+    ab = ab * s;
+    C3 a = c3(expf(ab.r), expf(ab.g), expf(ab.b));
+    float t = (1.f - G) + T21 * G;
+    C3 r = T12 * f2;
+    r = r * a;
+    r = r * t;
+    return f1 + r;
+}
+// LayeredBSDF::pdf (LayeredBSDF.cpp:262-303)
+__device__ __forceinline__ float ly_pdf(const DevBsdf &b, V3 wi, V3 wo)
+{
+    V3 wh = normalized(wi + wo);
+    float eI, eT, rel, cT;
+    float fr1 = cavg1(estimate_dielectric(b.eta_ext, b.eta_int, dot(wi, wh), eI, eT, rel, cT));
+    if (fr1 == 1.f) return 0.f;
+    V3 rwi = normalized(refract_n(wi, wh, rel, cT));
+    V3 rwo = normalized(refract_n(wo, wh, rel, cT));
+    float ch = wh.z;
+    float Jh = 1.f / (4 * fabsf(dot(wh, wo)));
+    float D = mf_D(b.distribution, wh, b.alpha);
+    float pd = fabsf(D * ch * Jh);
+    rwi = -1.f * rwi;
+    rwo = -1.f * rwo;
+    DevBsdf base = layered_base(b);
+    float pc = rc_pdf(base, rwi, rwo);
+    rel = b.eta_ext / b.eta_int;
+    float q = pc * (1.f - fr1);
+    q = q * rel;
+    q = q * rel;
+    q = q * wo.z;
+    q = q / rwo.z;
+    return pd * fr1 + q;
+}
+// LayeredBSDF::sample (LayeredBSDF.cpp:165-260)
+__device__ __forceinline__ C3 ly_sample(const DevBsdf &b, BsdfRec &r, V2 s, uint64_t aux_key)
+{
+    if (r.wi.z <= 0.f) return cfill(0.f);
+    float ci = r.wi.z;
+    float alpha = (1.2f - 0.2f * sqrtf(fabsf(ci))) * b.alpha;
+    Pcg32 aux = layered_aux(aux_key);
+    float n1 = next1d(aux);
+    float n2 = next1d(aux);
+    V3 normal = mf_sample_normal(b.distribution, v2(n1, n2), alpha);
+    float eI, eT, rel, cT;
+    float fr1 = cavg1(estimate_dielectric(b.eta_ext, b.eta_int, dot(r.wi, normal), eI, eT, rel, cT));
+    if (fr1 == 1.f) return cfill(0.f);
+    if (s.x <= fr1) {
+        r.wo = reflect_n(r.wi, normal);
+        r.pdf = ly_pdf(b, r.wi, r.wo);
+        r.type = BT_GLOSSY_REFLECTION;
+        C3 f1 = ly_eval_reflection(b, r.wi, r.wo, fr1, alpha);
+        if (iszero(f1)) return cfill(0.f);
+    } else {
+        r.type = BT_GLOSSY_REFLECTION;
+        V3 rwi = normalized(-1.f * refract_n(r.wi, normal, rel, cT));
+        BsdfRec rr;
+        rr.wi = rwi; rr.wo = v3(0.f, 0.f, 0.f);
+        rr.type = BT_ALL; rr.rel_eta = 1.f; rr.pdf = -1.f;
+        DevBsdf base = layered_base(b);
+        C3 f2 = rc_sample(base, rr, s);
+        if (iszero(f2)) return cfill(0.f);
+        r.wo = -1.f * rr.wo;
+        float fr2 = cavg1(estimate_dielectric(b.eta_ext, b.eta_int, r.wo.z, eI, eT, rel, cT));
+        if (fr2 == 1.f) return cfill(0.f);
+        r.wo = normalized(refract_n(r.wo, normal, rel, cT));
+        r.pdf = ly_pdf(b, r.wi, r.wo);
+        if (r.pdf == 0.f) return cfill(0.f);
+    }
+    if (r.pdf == 0.f) return cfill(0.f);
+    float co = r.wo.z;
+    return (ly_eval(b, r.wi, r.wo) * fabsf(co)) / r.pdf;
+}
+
 __device__ __forceinline__ C3 bsdf_eval(const DevBsdf &b, V3 wi, V3 wo)
 {
     switch (b.type) {
     case 0: return diffuse_eval(b.albedo, wi, wo);
     case 1: return rc_eval(b, wi, wo);
     case 2: return rd_eval(b, wi, wo);
-    default: return sl_eval(b, wi, wo);
+    case 3: return sl_eval(b, wi, wo);
+    default: return ly_eval(b, wi, wo);
     }
 }
 __device__ __forceinline__ float bsdf_pdf(const DevBsdf &b, V3 wi, V3 wo)
@@ -855,16 +992,19 @@ __device__ __forceinline__ float bsdf_pdf(const DevBsdf &b, V3 wi, V3 wo)
     case 0: return diffuse_pdf(wi, wo);
     case 1: return rc_pdf(b, wi, wo);
     case 2: return rd_pdf(b, wi, wo);
-    default: return sl_pdf(b, wi, wo);
+    case 3: return sl_pdf(b, wi, wo);
+    default: return ly_pdf(b, wi, wo);
     }
 }
-__device__ __forceinline__ C3 bsdf_sample(const DevBsdf &b, BsdfRec &r, V2 s)
+// aux_key: the side-stream key of a LayeredBSDF sample (ly_sample)
+__device__ __forceinline__ C3 bsdf_sample(const DevBsdf &b, BsdfRec &r, V2 s, uint64_t aux_key)
 {
     switch (b.type) {
     case 0: return diffuse_sample(b.albedo, r, s);
     case 1: return rc_sample(b, r, s);
     case 2: return rd_sample(b, r, s);
-    default: return sl_sample(b, r, s);
+    case 3: return sl_sample(b, r, s);
+    default: return ly_sample(b, r, s, aux_key);
     }
 }
 

@@ -10,12 +10,14 @@ namespace rtgpu {
 // path flags
 enum { F_FIRST = 1, F_DELTA = 2, F_NEE = 4, F_END = 8, F_DONE = 16 };
 
+#define RT_NBSDF 5        // BSDF types, one shading queue and kernel each
+
 struct RoundCounters {   // one per wavefront round, zeroed per batch
     int closest, shadow, wc_closest, wc_shadow;
-    int mat[4];          // paths to shade per BSDF type (material-sorted queues)
+    int mat[RT_NBSDF];   // paths to shade per BSDF type (material-sorted queues)
     int fin;             // paths whose traced ray missed or hit a surface without a BSDF
     int end;             // paths that ended in shading with a light sample pending
-    int pad[6];
+    int pad[5];
 };
 
 struct Wave {
@@ -37,7 +39,7 @@ struct Wave {
     uint8_t *pix_irregular;  // per batch pixel: some sample splats off its pixel
     // queues of the current round
     int *q_closest, *q_shadow;
-    int *q_mat[4];     // per-BSDF-type shading queues, filled by the closest-hit trace
+    int *q_mat[RT_NBSDF];  // per-BSDF-type shading queues, filled by the closest-hit trace
     int *q_fin;        // rays that missed or hit a surface without a BSDF (to finish)
     int *q_end;        // paths whose BSDF sample was zero, light sample pending
     RoundCounters *cnt;

@@ -13,7 +13,7 @@ f3 = C.c_float * 3
 f16 = C.c_float * 16
 i3 = C.c_int32 * 3
 
-BSDF_DIFFUSE, BSDF_ROUGH_CONDUCTOR, BSDF_ROUGH_DIELECTRIC, BSDF_SMOOTH_LAYERED = 0, 1, 2, 3
+BSDF_DIFFUSE, BSDF_ROUGH_CONDUCTOR, BSDF_ROUGH_DIELECTRIC, BSDF_SMOOTH_LAYERED, BSDF_LAYERED = 0, 1, 2, 3, 4
 DIST_BECKMANN, DIST_PHONG, DIST_GGX = 0, 1, 2
 LIGHT_AREA, LIGHT_ENV = 0, 1
 SHAPE_MESH, SHAPE_SPHERE = 0, 1
@@ -25,7 +25,8 @@ BSDF_OP_EVAL, BSDF_OP_PDF, BSDF_OP_SAMPLE = 0, 1, 2
 
 # reference name -> enum (XML "type" attributes, bsdf/*.cpp RT_REGISTER_TYPE)
 BSDF_TYPES = {"diffuse": BSDF_DIFFUSE, "roughconductor": BSDF_ROUGH_CONDUCTOR,
-              "roughdielectric": BSDF_ROUGH_DIELECTRIC, "smoothlayeredbsdf": BSDF_SMOOTH_LAYERED}
+              "roughdielectric": BSDF_ROUGH_DIELECTRIC, "smoothlayeredbsdf": BSDF_SMOOTH_LAYERED,
+              "layeredbsdf": BSDF_LAYERED}
 DIST_TYPES = {"beckmann": DIST_BECKMANN, "phong": DIST_PHONG, "ggx": DIST_GGX}
 
 
@@ -33,7 +34,8 @@ class BsdfDesc(C.Structure):
     _fields_ = [("type", C.c_int32), ("distribution", C.c_int32), ("albedo", f3),
                 ("reflectance", f3), ("transmittance", f3), ("eta", f3), ("k", f3),
                 ("alpha", C.c_float), ("eta_int", C.c_float), ("eta_ext", C.c_float),
-                ("thickness", C.c_float), ("absorbance", f3)]
+                ("thickness", C.c_float), ("absorbance", f3),
+                ("distribution_base", C.c_int32), ("alpha_base", C.c_float)]
 
 
 class MeshDesc(C.Structure):
@@ -155,15 +157,20 @@ IDENTITY = np.eye(4)
 def bsdf(kind, **kw):
     """BSDF parameters with the reference constructors' defaults
     (Diffuse.cpp:11-18, RoughConductor.cpp:13-30, RoughDielectric.cpp:13-32,
-    SmoothLayeredBSDF.cpp:12-28)."""
-    d = dict(type=kind, distribution=kw.get("distribution", DIST_BECKMANN),
+    SmoothLayeredBSDF.cpp:12-28, LayeredBSDF.cpp:17-36: coat distribution ggx,
+    alphaTop 0.01, over a default RoughConductor: beckmann, alpha 0.2,
+    eta = k = 0)."""
+    layered = kind == BSDF_LAYERED
+    d = dict(type=kind, distribution=kw.get("distribution", DIST_GGX if layered else DIST_BECKMANN),
              albedo=kw.get("albedo", (0.5, 0.5, 0.5)),
              reflectance=kw.get("reflectance", (1.0, 1.0, 1.0)),
              transmittance=kw.get("transmittance", (1.0, 1.0, 1.0)),
              eta=kw.get("eta", (0.0, 0.0, 0.0)), k=kw.get("k", (0.0, 0.0, 0.0)),
-             alpha=kw.get("alpha", 0.2), eta_int=kw.get("eta_int", 1.5046),
+             alpha=kw.get("alpha", 0.01 if layered else 0.2), eta_int=kw.get("eta_int", 1.5046),
              eta_ext=kw.get("eta_ext", 1.000277), thickness=kw.get("thickness", 1.2),
-             absorbance=kw.get("absorbance", (0.0, 0.0, 0.0)))
+             absorbance=kw.get("absorbance", (0.0, 0.0, 0.0)),
+             distribution_base=kw.get("distribution_base", DIST_BECKMANN),
+             alpha_base=kw.get("alpha_base", 0.2))
     return d
 
 
@@ -270,7 +277,8 @@ class SceneData:
         for i, b in enumerate(self.bsdfs):
             bs[i] = BsdfDesc(b["type"], b["distribution"], f3(*b["albedo"]), f3(*b["reflectance"]),
                              f3(*b["transmittance"]), f3(*b["eta"]), f3(*b["k"]), b["alpha"],
-                             b["eta_int"], b["eta_ext"], b["thickness"], f3(*b["absorbance"]))
+                             b["eta_int"], b["eta_ext"], b["thickness"], f3(*b["absorbance"]),
+                             b.get("distribution_base", DIST_BECKMANN), b.get("alpha_base", 0.2))
         D.n_bsdfs = len(self.bsdfs)
         D.bsdfs = C.cast(bs, C.POINTER(BsdfDesc))
 

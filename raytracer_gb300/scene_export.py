@@ -17,7 +17,8 @@ import numpy as np
 from . import desc as D
 
 _BSDF_NAMES = {D.BSDF_DIFFUSE: "Diffuse", D.BSDF_ROUGH_CONDUCTOR: "RoughConductor",
-               D.BSDF_ROUGH_DIELECTRIC: "RoughDielectric", D.BSDF_SMOOTH_LAYERED: "SmoothLayeredBSDF"}
+               D.BSDF_ROUGH_DIELECTRIC: "RoughDielectric", D.BSDF_SMOOTH_LAYERED: "SmoothLayeredBSDF",
+               D.BSDF_LAYERED: "LayeredBSDF"}
 _DIST_NAMES = {D.DIST_BECKMANN: "beckmann", D.DIST_PHONG: "phong", D.DIST_GGX: "ggx"}
 _STRATEGY_NAMES = {D.STRATEGY_ALL_LIGHTS: "all_lights", D.STRATEGY_ONE_LIGHT_UNIFORM: "one_light_uniform",
                    D.STRATEGY_ONE_LIGHT_WEIGHTED: "one_light_weighted"}
@@ -104,13 +105,24 @@ def _bsdf_xml(b, indent):
                   '%s  <double name="etaInt" value="%s"/>' % (pad, _f(b["eta_int"])),
                   '%s  <double name="etaExt" value="%s"/>' % (pad, _f(b["eta_ext"])),
                   '%s  <string name="distribution" value="%s"/>' % (pad, _DIST_NAMES[b["distribution"]])]
-    else:
+    elif b["type"] == D.BSDF_SMOOTH_LAYERED:
         lines += ['%s  <double name="etaInt" value="%s"/>' % (pad, _f(b["eta_int"])),
                   '%s  <double name="etaExt" value="%s"/>' % (pad, _f(b["eta_ext"])),
                   '%s  <double name="thickness" value="%s"/>' % (pad, _f(b["thickness"])),
                   '%s  <color name="absorbance" value="%s"/>' % (pad, _c(b["absorbance"])),
                   '%s  <bsdf name="baseBSDF" type="Diffuse"><color name="albedo" value="%s"/></bsdf>'
                   % (pad, _c(b["albedo"]))]
+    else:
+        base = dict(b, type=D.BSDF_ROUGH_CONDUCTOR, distribution=b.get("distribution_base", D.DIST_BECKMANN),
+                    alpha=b.get("alpha_base", 0.2))
+        inner = _bsdf_xml(base, indent + 2)
+        inner[0] = inner[0].replace('<bsdf type=', '<bsdf name="baseBSDF" type=')
+        lines += ['%s  <double name="etaInt" value="%s"/>' % (pad, _f(b["eta_int"])),
+                  '%s  <double name="etaExt" value="%s"/>' % (pad, _f(b["eta_ext"])),
+                  '%s  <double name="thickness" value="%s"/>' % (pad, _f(b["thickness"])),
+                  '%s  <color name="absorbance" value="%s"/>' % (pad, _c(b["absorbance"])),
+                  '%s  <double name="alphaTop" value="%s"/>' % (pad, _f(b["alpha"])),
+                  '%s  <string name="distribution" value="%s"/>' % (pad, _DIST_NAMES[b["distribution"]])] + inner
     lines.append("%s</bsdf>" % pad)
     return lines
 

@@ -20,7 +20,8 @@ the element.  Paths in the file are resolved against the file's folder
                  each with <bsdf>, <light type="AreaLight|MeshLight"> (radiance),
                  <medium name="interior|exterior">
     bsdf         Diffuse, RoughConductor, RoughDielectric, SmoothLayeredBSDF
-                 (over Diffuse); top-level <bsdf id=..> and <transform id=..>
+                 (over Diffuse), LayeredBSDF (over RoughConductor); top-level
+                 <bsdf id=..> and <transform id=..>
                  can be referenced with ref=".."
     media        Homogeneous (sigmaA, sigmaS, scale), Heterogeneous (albedo,
                  <volume type="GridVolume"> path .vol, centered, toWorld, scale),
@@ -239,6 +240,18 @@ class _Loader:
             b = D.bsdf(D.BSDF_SMOOTH_LAYERED, albedo=albedo, eta_int=p.get("etaInt", 1.5046),
                        eta_ext=p.get("etaExt", 1.000277), thickness=p.get("thickness", 1.2),
                        absorbance=p.get("absorbance", (0.0, 0.0, 0.0)))
+        elif kind == "LayeredBSDF":   # LayeredBSDF.cpp:17-36
+            base = p.get("baseBSDF")
+            bd = D.bsdf(D.BSDF_ROUGH_CONDUCTOR)   # RoughConductor(Parameters()): eta = k = 0
+            if base is not None:
+                bd = self.s.bsdfs[base]
+                if bd["type"] != D.BSDF_ROUGH_CONDUCTOR:
+                    raise UnsupportedScene("LayeredBSDF over a non-RoughConductor base is not provided")
+            b = D.bsdf(D.BSDF_LAYERED, distribution=_dist(p.get("distribution", "ggx")),
+                       alpha=p.get("alphaTop", 0.01), eta_int=p.get("etaInt", 1.5046),
+                       eta_ext=p.get("etaExt", 1.000277), thickness=p.get("thickness", 1.2),
+                       absorbance=p.get("absorbance", (0.0, 0.0, 0.0)), eta=bd["eta"], k=bd["k"],
+                       reflectance=bd["reflectance"], distribution_base=bd["distribution"], alpha_base=bd["alpha"])
         else:
             raise UnsupportedScene("BSDF type %s is not provided" % kind)
         return self.s.add_bsdf(b)

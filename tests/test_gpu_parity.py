@@ -128,6 +128,9 @@ BSDFS = [
     D.bsdf(D.BSDF_ROUGH_DIELECTRIC, distribution=D.DIST_GGX, alpha=0.1, eta_int=1.5),
     D.bsdf(D.BSDF_ROUGH_DIELECTRIC, distribution=D.DIST_BECKMANN, alpha=0.3, eta_int=1.33),
     D.bsdf(D.BSDF_SMOOTH_LAYERED, albedo=(0.7, 0.25, 0.2), eta_int=1.5, thickness=0.1, absorbance=(0.1, 0.2, 0.3)),
+    D.bsdf(D.BSDF_LAYERED, distribution=D.DIST_GGX, alpha=0.05, eta=scenes.AU_ETA, k=scenes.AU_K,
+           distribution_base=D.DIST_GGX, alpha_base=0.25, thickness=0.5, absorbance=(0.1, 0.2, 0.3)),
+    D.bsdf(D.BSDF_LAYERED, eta=(1.1, 0.9, 0.7), k=(3.0, 2.5, 2.0)),   # reference defaults: ggx 0.01 over beckmann 0.2
 ]
 
 
@@ -315,6 +318,16 @@ def test_film_parity_icosphere_env(ctx, rtlib, ico, width):
 
 def test_film_parity_volume(ctx, rtlib, vol):
     _film_parity(ctx, rtlib, vol, 2, 4, max_bad=0.08)
+
+
+def test_film_parity_layered(ctx, rtlib):
+    """LayeredBSDF (coat over a rough conductor) on the Cornell boxes; the
+    coat normal's side stream is keyed identically on both sides."""
+    s = scenes.cornell_box(40, 32)
+    ly = s.add_bsdf(BSDFS[-2])
+    for m in s.meshes[-3:-1]:
+        m["bsdf"] = ly
+    _film_parity(ctx, rtlib, s, 4, 23, max_bad=0.03)
 
 
 def test_film_parity_mixed_normals(ctx, rtlib):

@@ -198,6 +198,17 @@ def test_xml_roundtrip_cornell(built, tmp_path):
     assert np.array_equal(fa, fb)
 
 
+def test_xml_roundtrip_layered(built, tmp_path):
+    s = scenes.cornell_box(16, 12)
+    ly = s.add_bsdf(D.bsdf(D.BSDF_LAYERED, distribution=D.DIST_GGX, alpha=0.05, eta=scenes.AU_ETA, k=scenes.AU_K,
+                           distribution_base=D.DIST_GGX, alpha_base=0.25, thickness=0.5, absorbance=(0.1, 0.2, 0.3)))
+    s.meshes[3]["bsdf"] = ly
+    t = load_scene(write_scene(s, str(tmp_path)))
+    _same_scene(s, t)
+    fa, fb = _films_equal(s, t)
+    assert np.array_equal(fa, fb)
+
+
 def test_xml_roundtrip_volume(built, tmp_path):
     s = scenes.volume_grid(20, 16, res=12)
     xmlp = write_scene(s, str(tmp_path))
