@@ -174,6 +174,14 @@ def bsdf(kind, **kw):
     return d
 
 
+def bsdf_struct(b):
+    """rt_bsdf_desc of a bsdf() dict."""
+    return BsdfDesc(b["type"], b["distribution"], f3(*b["albedo"]), f3(*b["reflectance"]),
+                    f3(*b["transmittance"]), f3(*b["eta"]), f3(*b["k"]), b["alpha"],
+                    b["eta_int"], b["eta_ext"], b["thickness"], f3(*b["absorbance"]),
+                    b.get("distribution_base", DIST_BECKMANN), b.get("alpha_base", 0.2))
+
+
 class SceneData:
     """Flattened scene: numpy geometry plus lists of component dicts."""
 
@@ -275,10 +283,7 @@ class SceneData:
 
         bs = (BsdfDesc * max(1, len(self.bsdfs)))()
         for i, b in enumerate(self.bsdfs):
-            bs[i] = BsdfDesc(b["type"], b["distribution"], f3(*b["albedo"]), f3(*b["reflectance"]),
-                             f3(*b["transmittance"]), f3(*b["eta"]), f3(*b["k"]), b["alpha"],
-                             b["eta_int"], b["eta_ext"], b["thickness"], f3(*b["absorbance"]),
-                             b.get("distribution_base", DIST_BECKMANN), b.get("alpha_base", 0.2))
+            bs[i] = bsdf_struct(b)
         D.n_bsdfs = len(self.bsdfs)
         D.bsdfs = C.cast(bs, C.POINTER(BsdfDesc))
 

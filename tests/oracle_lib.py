@@ -139,11 +139,7 @@ BSDF_R = np.dtype([("value", np.float32, 3), ("pdf", np.float32), ("wo", np.floa
 
 
 def bsdf_query(bsdf_dict, op, q):
-    b = D.BsdfDesc(bsdf_dict["type"], bsdf_dict["distribution"], D.f3(*bsdf_dict["albedo"]),
-                   D.f3(*bsdf_dict["reflectance"]), D.f3(*bsdf_dict["transmittance"]),
-                   D.f3(*bsdf_dict["eta"]), D.f3(*bsdf_dict["k"]), bsdf_dict["alpha"],
-                   bsdf_dict["eta_int"], bsdf_dict["eta_ext"], bsdf_dict["thickness"],
-                   D.f3(*bsdf_dict["absorbance"]))
+    b = D.bsdf_struct(bsdf_dict)
     q = np.ascontiguousarray(q, BSDF_Q)
     r = np.zeros(len(q), BSDF_R)
     lib().oracle_bsdf_query(C.byref(b), op, _p(q), len(q), _p(r))
