@@ -144,7 +144,16 @@ typedef struct rt_camera_desc {
     float aperture_radius;       /* 0 = pinhole                                  */
     float focal_plane;
     int32_t medium;              /* camera medium or -1                          */
+    /* reconstruction filter of the camera's screen (filter/*.h): RT_FILTER_*,
+     * radii "radiusX"/"radiusY" (default 0.5) and two parameters: Gaussian
+     * "alpha", "omega" (GaussianFilter.cpp:16-17); Mitchell-Netravali "B", "C"
+     * (MitchellNetravaliFilter.cpp:17-18) */
+    int32_t filter;
+    float filter_radius[2];
+    float filter_param[2];
 } rt_camera_desc;
+
+enum { RT_FILTER_BOX = 0, RT_FILTER_GAUSSIAN = 1, RT_FILTER_MITCHELL = 2 };
 
 typedef struct rt_scene_desc {
     int32_t n_vertices;

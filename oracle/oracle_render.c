@@ -595,30 +595,72 @@ static c3 render_one(const o_scene *sc, const rt_render_desc *rd, int x, int y, 
 }
 
 /* ---------------- tile jobs ---------------- */
+/* ReconstructionFilter::precompute (ReconstructionFilter.cpp:27-40) with the
+ * Gaussian (GaussianFilter.cpp:28-36) and Mitchell-Netravali
+ * (MitchellNetravaliFilter.cpp:28-52) profiles; the box is 1 */
+static float o_gauss1(float a, float w, float v)
+{
+    float e1 = expf(-a * v * v), e2 = expf(-a * w * w);
+    float d = e1 - e2;
+    return d < 0.f ? 0.f : d;
+}
+static float o_mitchell1(float B, float C, float v)
+{
+    v = fabsf(2.f * v);
+    if (v > 1.f)
+        return ((((-B - 6 * C) * v * v * v + (6 * B + 30 * C) * v * v) + (-12 * B - 48 * C) * v + 8 * B) + 24 * C) *
+               (1.f / 6.f);
+    return ((12 - 9 * B - 6 * C) * v * v * v + (-18 + 12 * B + 6 * C) * v * v + (6 - 2 * B)) * (1.f / 6.f);
+}
+static void o_filter_table(const rt_camera_desc *c, float *t)
+{
+    float rx = c->filter_radius[0], ry = c->filter_radius[1];
+    for (int x = 0; x < 32; x++)
+        for (int y = 0; y < 32; y++) {
+            float fx = x * rx / 32, fy = y * ry / 32;
+            float v = 1.f;
+            if (c->filter == RT_FILTER_GAUSSIAN)
+                v = o_gauss1(c->filter_param[0], c->filter_param[1], fx) * o_gauss1(c->filter_param[0], c->filter_param[1], fy);
+            else if (c->filter == RT_FILTER_MITCHELL)
+                v = o_mitchell1(c->filter_param[0], c->filter_param[1], fx / rx) *
+                    o_mitchell1(c->filter_param[0], c->filter_param[1], fy / ry);
+            t[x + y * 32] = v;
+        }
+}
+
 typedef struct {
     o_scene *sc;
     const rt_render_desc *rd;
-    float *film;
-    int ntx, nty;
-    int next, end;
+    float *subs;          /* one tile screen per tile of the range, (bx + 2ovx) x (by + 2ovy) */
+    int ntx, nty, ovx, ovy, sw, sh;
+    int first, next, end;
+    float table[1024];
     pthread_mutex_t mu;
     int64_t nan_count;
 } o_job;
 
-/* Screen::addSample with the box filter (Screen.cpp:44-83) */
-static void film_add(float *sub, int tw, int th, int minx, int miny, float xx, float yy, c3 v, int64_t *nan)
+/* Screen::addSample (Screen.cpp:44-83) into a tile screen of sw x sh pixels
+ * whose pixel (0, 0) is image pixel (minx - ovx, miny - ovy) */
+static void film_add(const o_job *J, float *sub, int sw, int sh, int minx, int miny, float xx, float yy, c3 v,
+                     int64_t *nan)
 {
     if (c3_isnan(v)) { (*nan)++; return; }
-    xx = xx - 0.5f - (float)(minx - 0);
-    yy = yy - 0.5f - (float)(miny - 0);
-    int sx = (int)ceilf(xx - 0.5f), ex = (int)floorf(xx + 0.5f);
-    int sy = (int)ceilf(yy - 0.5f), ey = (int)floorf(yy + 0.5f);
-    sx = imax(0, sx); ex = imin(tw - 1, ex);
-    sy = imax(0, sy); ey = imin(th - 1, ey);
+    const rt_camera_desc *cam = &J->sc->d->camera;
+    float rx = cam->filter_radius[0], ry = cam->filter_radius[1];
+    xx = xx - 0.5f - (float)(minx - J->ovx);
+    yy = yy - 0.5f - (float)(miny - J->ovy);
+    int sx = (int)ceilf(xx - rx), ex = (int)floorf(xx + rx);
+    int sy = (int)ceilf(yy - ry), ey = (int)floorf(yy + ry);
+    sx = imax(0, sx); ex = imin(sw - 1, ex);
+    sy = imax(0, sy); ey = imin(sh - 1, ey);
     for (int x = sx; x <= ex; x++)
         for (int y = sy; y <= ey; y++) {
-            float *p = sub + 4 * ((size_t)y * tw + x);
-            p[0] += v.r * 1.f; p[1] += v.g * 1.f; p[2] += v.b * 1.f; p[3] += 1.f;
+            /* ReconstructionFilter::operator() (ReconstructionFilter.h:54-63) */
+            int ix = imin((int)((32 * fabsf((float)x - xx)) / rx), 31);
+            int iy = imin((int)((32 * fabsf((float)y - yy)) / ry), 31);
+            float w = J->table[ix + iy * 32];
+            float *p = sub + 4 * ((size_t)y * sw + x);
+            p[0] += v.r * w; p[1] += v.g * w; p[2] += v.b * w; p[3] += w;
         }
 }
 
@@ -628,7 +670,6 @@ static void *job_worker(void *arg)
     const rt_render_desc *rd = J->rd;
     const rt_camera_desc *cam = &J->sc->d->camera;
     int bx = rd->block_x > 0 ? rd->block_x : 32, by = rd->block_y > 0 ? rd->block_y : 32;
-    float *sub = (float *)malloc(sizeof(float) * 4 * (size_t)bx * by);
     int64_t nan = 0;
     for (;;) {
         pthread_mutex_lock(&J->mu);
@@ -638,31 +679,29 @@ static void *job_worker(void *arg)
         int ox = (t % J->ntx) * bx, oy = (t / J->ntx) * by;
         int ex = imin(cam->width, ox + bx), ey = imin(cam->height, oy + by);
         int tw = ex - ox, th = ey - oy;
-        memset(sub, 0, sizeof(float) * 4 * (size_t)tw * th);
+        int sw = tw + 2 * J->ovx, sh = th + 2 * J->ovy;
+        float *sub = J->subs + 4 * (size_t)J->sw * J->sh * (size_t)(t - J->first);
+        memset(sub, 0, sizeof(float) * 4 * (size_t)sw * sh);
         for (int y = oy; y < ey; y++)
             for (int x = ox; x < ex; x++)
                 for (int i = 0; i < rd->spp; i++) {
                     float xx, yy;
                     c3 L = render_one(J->sc, rd, x, y, rd->sample_begin + i, &xx, &yy);
-                    film_add(sub, tw, th, ox, oy, xx, yy, L, &nan);
+                    film_add(J, sub, sw, sh, ox, oy, xx, yy, L, &nan);
                 }
-        /* Screen::merge (Screen.cpp:136-157) into a zeroed film */
-        for (int y = 0; y < th; y++)
-            for (int x = 0; x < tw; x++) {
-                float *dst = J->film + 4 * ((size_t)(oy + y) * cam->width + (ox + x));
-                const float *src = sub + 4 * ((size_t)y * tw + x);
-                for (int k = 0; k < 4; k++) dst[k] = 0.f + src[k];
-            }
     }
-    free(sub);
     pthread_mutex_lock(&J->mu);
     J->nan_count += nan;
     pthread_mutex_unlock(&J->mu);
     return NULL;
 }
 
-/* Render tiles [tile0, tile1) of the job grid (all tiles when tile1 < 0);
- * pixels outside those tiles are left zero. */
+/* Render tiles [tile0, tile1) of the job grid (all tiles when tile1 < 0)
+ * and merge their screens in tile order (Screen::merge, Screen.cpp:136-157:
+ * the order of a single-threaded run) into the full screen, which has an
+ * overlap border of ceil(r - 0.5) pixels; `film` receives the full screen's
+ * top-left width x height block, as the reference reads it back
+ * (Screen.h:52, Screen.cpp:113-122).  Pixels no tile reaches stay zero. */
 int32_t oracle_render_tiles(o_scene *sc, const rt_render_desc *rd, int32_t tile0, int32_t tile1,
                             float *film, int32_t nthreads)
 {
@@ -671,20 +710,48 @@ int32_t oracle_render_tiles(o_scene *sc, const rt_render_desc *rd, int32_t tile0
     const rt_camera_desc *cam = &sc->d->camera;
     int bx = rd->block_x > 0 ? rd->block_x : 32, by = rd->block_y > 0 ? rd->block_y : 32;
     o_job J;
-    J.sc = sc; J.rd = rd; J.film = film;
+    J.sc = sc; J.rd = rd;
     J.ntx = (cam->width + bx - 1) / bx;
     J.nty = (cam->height + by - 1) / by;
-    J.next = tile0 < 0 ? 0 : tile0;
+    J.ovx = (int)ceilf(cam->filter_radius[0] - 0.5f);
+    J.ovy = (int)ceilf(cam->filter_radius[1] - 0.5f);
+    J.sw = bx + 2 * J.ovx;
+    J.sh = by + 2 * J.ovy;
+    J.first = J.next = tile0 < 0 ? 0 : tile0;
     J.end = (tile1 < 0 || tile1 > J.ntx * J.nty) ? J.ntx * J.nty : tile1;
     J.nan_count = 0;
+    o_filter_table(cam, J.table);
+    int nt = J.end - J.first;
+    if (nt < 0) nt = 0;
+    J.subs = (float *)malloc(sizeof(float) * 4 * (size_t)J.sw * J.sh * (size_t)(nt > 0 ? nt : 1));
+    if (!J.subs) return RT_ERR_NOMEM;
     pthread_mutex_init(&J.mu, NULL);
-    memset(film, 0, sizeof(float) * 4 * (size_t)cam->width * cam->height);
     if (nthreads < 1) nthreads = 1;
     pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * (size_t)nthreads);
     for (int i = 0; i < nthreads; i++) pthread_create(&th[i], NULL, job_worker, &J);
     for (int i = 0; i < nthreads; i++) pthread_join(th[i], NULL);
     free(th);
     pthread_mutex_destroy(&J.mu);
+    /* merge into the full screen (width + 2 ovx) x (height + 2 ovy) */
+    int FW = cam->width + 2 * J.ovx, FH = cam->height + 2 * J.ovy;
+    float *full = (float *)calloc(4 * (size_t)FW * FH, sizeof(float));
+    if (!full) { free(J.subs); return RT_ERR_NOMEM; }
+    for (int t = J.first; t < J.end; t++) {
+        int ox = (t % J.ntx) * bx, oy = (t / J.ntx) * by;
+        int tw = imin(cam->width, ox + bx) - ox, tht = imin(cam->height, oy + by) - oy;
+        int sw = tw + 2 * J.ovx, sh = tht + 2 * J.ovy;
+        const float *sub = J.subs + 4 * (size_t)J.sw * J.sh * (size_t)(t - J.first);
+        for (int x = 0; x < sw; x++)
+            for (int y = 0; y < sh; y++) {
+                float *dst = full + 4 * ((size_t)(oy + y) * FW + (ox + x));
+                const float *src = sub + 4 * ((size_t)y * sw + x);
+                for (int k = 0; k < 4; k++) dst[k] += src[k];
+            }
+    }
+    for (int y = 0; y < cam->height; y++)
+        memcpy(film + 4 * (size_t)y * cam->width, full + 4 * (size_t)y * FW, sizeof(float) * 4 * (size_t)cam->width);
+    free(full);
+    free(J.subs);
     return RT_OK;
 }
 

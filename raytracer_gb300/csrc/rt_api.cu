@@ -1117,6 +1117,70 @@ __global__ void k_film(RenderParams P, float4 *film, int width, int accumulate)
     if (nan) atomicAdd(&P.stats[2], (unsigned long long)nan);
 }
 
+// Film for reconstruction filters other than the box of radius 0.5
+// (Screen::addSample / merge / postProcessColor, Screen.cpp:44-157).  Each
+// tile's screen holds its pixels plus an overlap of ceil(r - 0.5) pixels on
+// every side; samples splat value * w and w into every pixel of that screen
+// within the filter radius, w read from the 32 x 32 table; screens are merged
+// into the full screen in tile order.  One thread per output pixel gathers,
+// tile by tile in raster order (the merge order of a single-threaded run), the
+// samples of the tile's pixels that reach it, in the tile loop's pixel and
+// sample order, re-deriving each sample's jitter from its path stream.  The
+// output is the full screen's top-left width x height block, which is what
+// the reference reads back (operator() and postProcessColor ignore the
+// overlap offset, Screen.h:52, Screen.cpp:113-122).
+__global__ void k_film_wide(RenderParams P, float4 *film, int t0, int t1, int tiles_x, int bx, int by)
+{
+    const DevCamera &cam = P.S.cam;
+    const int W = cam.width, H = cam.height;
+    const int ovx = cam.ov_x, ovy = cam.ov_y;
+    const float rx = cam.frx, ry = cam.fry;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= W * H) return;
+    const int ax = i % W, ay = i / W;   // full-screen (overlapped) coordinates
+    float4 acc = film[i];
+    const int ty_hi = imin((H + by - 1) / by - 1, ay / by), tx_hi = imin(tiles_x - 1, ax / bx);
+    const int ty_lo = imax(0, (ay - 2 * ovy) / by - 1), tx_lo = imax(0, (ax - 2 * ovx) / bx - 1);
+    const int reach_x = (int)ceilf(rx + 0.5f), reach_y = (int)ceilf(ry + 0.5f);
+    for (int ty = ty_lo; ty <= ty_hi; ty++) {
+        const int oy = ty * by, th = imin(by, H - oy);
+        for (int tx = tx_lo; tx <= tx_hi; tx++) {
+            const int t = ty * tiles_x + tx;
+            if (t < t0 || t >= t1) continue;
+            const int ox = tx * bx, tw = imin(bx, W - ox);
+            const int lx = ax - ox, ly = ay - oy;
+            if (lx < 0 || ly < 0 || lx >= tw + 2 * ovx || ly >= th + 2 * ovy) continue;
+            // first batch pixel of the tile: full tile rows above, then the tiles to the left
+            const int tile_first = oy * W + ox * th;
+            const int qx0 = imax(ox, ax - ovx - reach_x), qx1 = imin(ox + tw - 1, ax - ovx + reach_x);
+            const int qy0 = imax(oy, ay - ovy - reach_y), qy1 = imin(oy + th - 1, ay - ovy + reach_y);
+            float sr = 0.f, sg = 0.f, sb = 0.f, sw = 0.f;
+            for (int qy = qy0; qy <= qy1; qy++)
+                for (int qx = qx0; qx <= qx1; qx++) {
+                    const int q = tile_first - P.g0 + (qy - oy) * tw + (qx - ox);
+                    for (int sm = 0; sm < P.spp; sm++) {
+                        float4 L = P.W.out[(size_t)sm * P.npix + q];
+                        if (isnan(L.x) || isnan(L.y) || isnan(L.z)) continue;
+                        Pcg32 rng;
+                        path_stream_seed(rng, P.seed, (uint32_t)(qy * W + qx), (uint32_t)(P.sample_begin + sm));
+                        V2 j = next2d(rng);
+                        float xl = ((float)qx + j.x) - 0.5f - (float)(ox - ovx);
+                        float yl = ((float)qy + j.y) - 0.5f - (float)(oy - ovy);
+                        int sx = imax(0, (int)ceilf(xl - rx)), ex = imin(tw + 2 * ovx - 1, (int)floorf(xl + rx));
+                        int sy = imax(0, (int)ceilf(yl - ry)), ey = imin(th + 2 * ovy - 1, (int)floorf(yl + ry));
+                        if (lx < sx || lx > ex || ly < sy || ly > ey) continue;
+                        int ix = imin((int)((32 * fabsf((float)lx - xl)) / rx), 31);
+                        int iy = imin((int)((32 * fabsf((float)ly - yl)) / ry), 31);
+                        float w = __ldg(cam.filter_table + ix + iy * 32);
+                        sr += L.x * w; sg += L.y * w; sb += L.z * w; sw += w;
+                    }
+                }
+            acc = make_float4(acc.x + sr, acc.y + sg, acc.z + sb, acc.w + sw);
+        }
+    }
+    film[i] = acc;
+}
+
 // ---------------------------------------------------------------- standalone queries
 __global__ void k_trace_rays(DevScene S, const rt_ray *rays, int n, int any, rt_hit *hits)
 {
@@ -1322,6 +1386,41 @@ struct HCdf {
         }
     }
 };
+
+// ReconstructionFilter::precompute (ReconstructionFilter.cpp:27-40): the
+// filter at (x rX / 32, y rY / 32), x, y = 0..31, with the Gaussian
+// (GaussianFilter.cpp:28-36) and Mitchell-Netravali
+// (MitchellNetravaliFilter.cpp:28-52) one-dimensional profiles; binary32 in
+// the reference's operation order
+static float h_gauss1(float a, float w, float v)
+{
+    float e1 = expf(-a * v * v), e2 = expf(-a * w * w);
+    float d = e1 - e2;
+    return d < 0.f ? 0.f : d;
+}
+static float h_mitchell1(float B, float C, float v)
+{
+    v = fabsf(2.f * v);
+    if (v > 1.f)
+        return ((((-B - 6 * C) * v * v * v + (6 * B + 30 * C) * v * v) + (-12 * B - 48 * C) * v + 8 * B) + 24 * C) *
+               (1.f / 6.f);
+    return ((12 - 9 * B - 6 * C) * v * v * v + (-18 + 12 * B + 6 * C) * v * v + (6 - 2 * B)) * (1.f / 6.f);
+}
+static void filter_table(const rt_camera_desc &c, float *t)
+{
+    const float rx = c.filter_radius[0], ry = c.filter_radius[1];
+    for (int x = 0; x < 32; x++)
+        for (int y = 0; y < 32; y++) {
+            float fx = x * rx / 32, fy = y * ry / 32;
+            float v = 1.f;
+            if (c.filter == RT_FILTER_GAUSSIAN)
+                v = h_gauss1(c.filter_param[0], c.filter_param[1], fx) * h_gauss1(c.filter_param[0], c.filter_param[1], fy);
+            else if (c.filter == RT_FILTER_MITCHELL)
+                v = h_mitchell1(c.filter_param[0], c.filter_param[1], fx / rx) *
+                    h_mitchell1(c.filter_param[0], c.filter_param[1], fy / ry);
+            t[x + y * 32] = v;
+        }
+}
 
 // guide[k] = first i with c[i] >= k / G, k = 0..G (cdf_sample_guided)
 static void cdf_guide(const float *c, int n, int G, int *g)
@@ -1564,6 +1663,11 @@ static rt_status validate(const rt_scene_desc *d)
     if (d->camera.width <= 0 || d->camera.height <= 0 || d->camera.width > 32768 || d->camera.height > 32768)
         return fail(RT_ERR_INVALID, "bad film size");
     if (d->camera.medium >= d->n_media) return fail(RT_ERR_INVALID, "camera medium out of range");
+    if (d->camera.filter < RT_FILTER_BOX || d->camera.filter > RT_FILTER_MITCHELL)
+        return fail(RT_ERR_UNSUPPORTED, "reconstruction filter type not supported");
+    for (int k = 0; k < 2; k++)
+        if (!(d->camera.filter_radius[k] > 0.f) || d->camera.filter_radius[k] > 16.f)
+            return fail(RT_ERR_INVALID, "filter radius must be in (0, 16]");
     return RT_OK;
 }
 
@@ -1820,6 +1924,18 @@ rt_status rt_scene_create(rt_ctx *ctx, const rt_scene_desc *d, rt_scene **out)
     S.cam.aperture_radius = cd.aperture_radius; S.cam.focal_plane = cd.focal_plane;
     S.cam.inv_w = 1.f / (float)cd.width; S.cam.inv_h = 1.f / (float)cd.height;
     S.cam.medium = cd.medium;
+    {
+        S.cam.filter = cd.filter;
+        S.cam.frx = cd.filter_radius[0];
+        S.cam.fry = cd.filter_radius[1];
+        S.cam.ov_x = (int)ceilf(cd.filter_radius[0] - 0.5f);
+        S.cam.ov_y = (int)ceilf(cd.filter_radius[1] - 0.5f);
+        float tab[1024];
+        filter_table(cd, tab);
+        const float *tp;
+        if ((st = upload(sc, tab, 1024, &tp)) != RT_OK) { rt_scene_destroy(sc); return st; }
+        S.cam.filter_table = tp;
+    }
     sc->n_lights = d->n_lights;
     sc->n_bsdfs = d->n_bsdfs;
     sc->n_media = d->n_media;
@@ -1962,6 +2078,10 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
         if (accumulate)
             CK(cudaMemcpyAsync(film, film_rgbw, npix_all * sizeof(float4), cudaMemcpyHostToDevice, st));
     }
+    // the box filter of radius 0.5 reduces per batch pixel (k_film); any other
+    // filter gathers into a zeroed (or, accumulating, the given) film
+    const bool box_film = cam.filter == RT_FILTER_BOX && cam.frx == 0.5f && cam.fry == 0.5f;
+    if (!box_film && !accumulate) CK(cudaMemsetAsync(film, 0, npix_all * sizeof(float4), st));
     // batch capacity: whole tiles, all samples of their pixels, up to
     // ctx->wave_paths paths (fewer, longer-tailed batches cost more: the last
     // rounds of a batch hold few paths and run at the traversal latency floor)
@@ -2064,9 +2184,13 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
                 }
             }
         }
-        int fb = (P.npix + 127) / 128;
         prof_begin(ctx, K_FILM);
-        k_film<<<fb, 128, 0, st>>>(P, film, Wd, accumulate);
+        if (box_film) {
+            int fb = (P.npix + 127) / 128;
+            k_film<<<fb, 128, 0, st>>>(P, film, Wd, accumulate);
+        } else {
+            k_film_wide<<<(int)((npix_all + 127) / 128), 128, 0, st>>>(P, film, t0, t1, tiles_x, bx, by);
+        }
         prof_end(ctx);
         launches++;
         if ((s = launch_check("k_film")) != RT_OK) return s;
@@ -2303,6 +2427,8 @@ extern "C" rt_status rt_render_tile_static(rt_ctx *ctx, rt_scene *sc, const rt_r
         return fail(RT_ERR_LIMIT, "rt_render_tile_static: max_depth above 1024 (the static round-counter table)");
     if (sc->n_lights > RT_STATIC_MAX_LIGHTS) return fail(RT_ERR_LIMIT, "rt_render_tile_static: more than 256 lights");
     const DevCamera &cam = sc->S.cam;
+    if (!(cam.filter == RT_FILTER_BOX && cam.frx == 0.5f && cam.fry == 0.5f))
+        return fail(RT_ERR_UNSUPPORTED, "rt_render_tile_static: only the box filter of radius 0.5");
     const int Wd = cam.width, H = cam.height;
     const int bx = rd->block_x > 0 ? rd->block_x : 32, by = rd->block_y > 0 ? rd->block_y : 32;
     if (bx > 0xffff || by > 0xffff) return fail(RT_ERR_INVALID, "block size too large");

@@ -73,6 +73,12 @@ struct DevCamera {
     float near_clip, far_clip, aperture_radius, focal_plane;
     float inv_w, inv_h;
     int medium;
+    // reconstruction filter: type, radii, screen overlap (Screen::setFilter,
+    // Screen.cpp:98-108) and the 32 x 32 weight table of
+    // ReconstructionFilter::precompute (ReconstructionFilter.cpp:27-40)
+    int filter, ov_x, ov_y;
+    float frx, fry;
+    const float *filter_table;
 };
 
 struct DevScene {

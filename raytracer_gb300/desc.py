@@ -67,7 +67,8 @@ class CameraDesc(C.Structure):
     _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("sample_to_camera", f16),
                 ("camera_to_world", f16), ("near_clip", C.c_float), ("far_clip", C.c_float),
                 ("aperture_radius", C.c_float), ("focal_plane", C.c_float),
-                ("medium", C.c_int32)]
+                ("medium", C.c_int32), ("filter", C.c_int32), ("filter_radius", C.c_float * 2),
+                ("filter_param", C.c_float * 2)]
 
 
 class SceneDesc(C.Structure):
@@ -337,10 +338,12 @@ class SceneData:
         D.media = C.cast(ms, C.POINTER(MediumDesc))
 
         c = self.camera
+        flt = c.get("filter", box_filter())
         D.camera = CameraDesc(c["width"], c["height"], mat(c["sample_to_camera"]),
                               mat(c["camera_to_world"]), c["near_clip"], c["far_clip"],
                               c.get("aperture_radius", 0.0), c.get("focal_plane", 1e8),
-                              c.get("medium", -1))
+                              c.get("medium", -1), flt["type"], (C.c_float * 2)(*flt["radius"]),
+                              (C.c_float * 2)(*flt["param"]))
         keep += [meshes, spheres, bs, ls, ms]
         self._keep = keep
         return D
@@ -358,6 +361,25 @@ class SceneData:
 
 
 RENDER_ACCUMULATE = 1   # rt_render_desc.flags: add to the film instead of overwriting it
+
+FILTER_BOX, FILTER_GAUSSIAN, FILTER_MITCHELL = 0, 1, 2
+
+
+def box_filter(rx=0.5, ry=0.5):
+    """BoxFilter (filter/BoxFilter.h), radii default 0.5 (ReconstructionFilter.cpp:15-16)."""
+    return dict(type=FILTER_BOX, radius=(rx, ry), param=(0.0, 0.0))
+
+
+def gaussian_filter(rx=0.5, ry=0.5, alpha=None, omega=None):
+    """GaussianFilter: alpha default 1 / (2 * 0.5 * 0.5), omega default radiusX
+    (GaussianFilter.cpp:14-19)."""
+    return dict(type=FILTER_GAUSSIAN, radius=(rx, ry),
+                param=(1 / (2.0 * 0.5 * 0.5) if alpha is None else alpha, rx if omega is None else omega))
+
+
+def mitchell_filter(rx=0.5, ry=0.5, b=1.0 / 3, c=1.0 / 3):
+    """MitchellNetravaliFilter: B and C default 1/3 (MitchellNetravaliFilter.cpp:14-19)."""
+    return dict(type=FILTER_MITCHELL, radius=(rx, ry), param=(b, c))
 
 
 # ---------------------------------------------------------------- cameras

@@ -151,6 +151,19 @@ def _medium_xml(m, name, folder, stem, indent):
     return lines
 
 
+def _filter_xml(f):
+    name = {D.FILTER_BOX: "BoxFilter", D.FILTER_GAUSSIAN: "GaussianFilter",
+            D.FILTER_MITCHELL: "MitchellNetravaliFilter"}[f["type"]]
+    body = '<double name="radiusX" value="%s"/><double name="radiusY" value="%s"/>' % (
+        _f(f["radius"][0]), _f(f["radius"][1]))
+    if f["type"] == D.FILTER_GAUSSIAN:
+        body += '<double name="alpha" value="%s"/><double name="omega" value="%s"/>' % (
+            _f(f["param"][0]), _f(f["param"][1]))
+    elif f["type"] == D.FILTER_MITCHELL:
+        body += '<double name="B" value="%s"/><double name="C" value="%s"/>' % (_f(f["param"][0]), _f(f["param"][1]))
+    return '    <filter type="%s">%s</filter>' % (name, body)
+
+
 def write_scene(scene, folder, spp=1, name="scene"):
     """Write `scene` as folder/name.xml plus its mesh, map and grid files.
     Returns the XML path."""
@@ -172,7 +185,7 @@ def write_scene(scene, folder, spp=1, name="scene"):
             '    <double name="farClip" value="%s"/>' % _f(cam["far_clip"]),
             '    <integer name="sizeX" value="%d"/>' % cam["width"],
             '    <integer name="sizeY" value="%d"/>' % cam["height"],
-            '    <filter type="BoxFilter"/>',
+            _filter_xml(cam.get("filter", D.box_filter())),
             "  </camera>"]
     block = getattr(s, "block", (32, 32))
     out += ["  <parameters>", "    <blockSizeX>%d</blockSizeX>" % block[0],

@@ -9,7 +9,8 @@ the element.  Paths in the file are resolved against the file's folder
                  (PathTracingMIS.cpp:15-19, VolPathTracing.cpp:13-17)
     camera       NoriPerspective: fov, nearClip, farClip (NoriPerspective.cpp:15-17),
                  sizeX, sizeY, apertureRadius, focalPlane (Camera.cpp:11-14),
-                 <transform> = camera to world, <filter> BoxFilter of radius 0.5
+                 <transform> = camera to world, <filter> BoxFilter, GaussianFilter,
+                 MitchellNetravaliFilter (radiusX, radiusY, alpha/omega, B/C)
     sampler      RandomSampler: sampleNumber -> `spp` (RandomSampler.cpp:10)
     parameters   blockSizeX, blockSizeY -> `block` (XMLLoader.cpp:217-259)
     medium       (top level) the camera medium (XMLLoader.cpp:96-101; the later
@@ -144,6 +145,7 @@ class _Loader:
         self.camera_medium = -1
         self.spp = 1
         self.block = (32, 32)
+        self.filter = D.box_filter()
 
     def resolve(self, p):
         return p if os.path.isabs(p) else os.path.normpath(os.path.join(self.dir, p))
@@ -347,12 +349,18 @@ class _Loader:
         for c in el:
             if c.tag == "transform":
                 self.camera_transform = _transform(c)
-            elif c.tag == "filter":
+            elif c.tag == "filter":   # ReconstructionFilter.cpp:12-18 and the filters' constructors
                 fp = self.props(c)
                 rx, ry = fp.get("radiusX", 0.5), fp.get("radiusY", 0.5)
-                if c.get("type") != "BoxFilter" or rx != 0.5 or ry != 0.5:
-                    raise UnsupportedScene("filter %s (radius %g x %g) is not provided; the device film "
-                                           "implements the box filter of radius 0.5" % (c.get("type"), rx, ry))
+                kind = c.get("type")
+                if kind == "BoxFilter":
+                    self.filter = D.box_filter(rx, ry)
+                elif kind == "GaussianFilter":
+                    self.filter = D.gaussian_filter(rx, ry, fp.get("alpha"), fp.get("omega"))
+                elif kind == "MitchellNetravaliFilter":
+                    self.filter = D.mitchell_filter(rx, ry, fp.get("B", 1.0 / 3), fp.get("C", 1.0 / 3))
+                else:
+                    raise UnsupportedScene("filter %s is not provided" % kind)
             else:
                 rest.append(c)
         holder = ET.Element("camera")
@@ -424,6 +432,7 @@ class _Loader:
                        np.asarray(self.camera_transform, np.float64), near=cp.get("nearClip", 1e-4),
                        far=cp.get("farClip", 1e4), medium=self.camera_medium)
         cam["aperture_radius"] = cp.get("apertureRadius", 0.0)
+        cam["filter"] = self.filter
         cam["focal_plane"] = cp.get("focalPlane", 3.4028234663852886e38)
         self.s.camera = cam
         self.s.spp = self.spp

@@ -320,6 +320,21 @@ def test_film_parity_volume(ctx, rtlib, vol):
     _film_parity(ctx, rtlib, vol, 2, 4, max_bad=0.08)
 
 
+@pytest.mark.parametrize("flt", [D.gaussian_filter(1.5, 1.5), D.mitchell_filter(2.0, 1.0), D.box_filter(1.0, 0.5)],
+                         ids=["gauss1.5", "mitchell2x1", "box1x0.5"])
+def test_film_parity_filters(ctx, rtlib, flt):
+    """Wider reconstruction filters: tile screens with an overlap border
+    merged in tile order, across two wavefront batches (small wave size),
+    with ragged 8x8 tiles; the film is the full screen's top-left block."""
+    s = scenes.cornell_box(80, 60)   # 76,800 paths: two batches of 64 and 16 tiles
+    s.camera["filter"] = flt
+    ctx.set_wave_paths(1 << 16)
+    try:
+        _film_parity(ctx, rtlib, s, 16, 31, max_bad=0.03, block=8)
+    finally:
+        ctx.set_wave_paths(1 << 26)
+
+
 def test_film_parity_layered(ctx, rtlib):
     """LayeredBSDF (coat over a rough conductor) on the Cornell boxes; the
     coat normal's side stream is keyed identically on both sides."""

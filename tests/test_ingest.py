@@ -209,6 +209,17 @@ def test_xml_roundtrip_layered(built, tmp_path):
     assert np.array_equal(fa, fb)
 
 
+@pytest.mark.parametrize("flt", [D.gaussian_filter(1.5, 1.5), D.mitchell_filter(2.0, 1.0)], ids=["gauss", "mitchell"])
+def test_xml_roundtrip_filter(built, tmp_path, flt):
+    s = scenes.cornell_box(20, 14)
+    s.camera["filter"] = flt
+    t = load_scene(write_scene(s, str(tmp_path)))
+    assert t.camera["filter"]["type"] == flt["type"]
+    np.testing.assert_allclose(t.camera["filter"]["param"], flt["param"], rtol=1e-6)
+    fa, fb = _films_equal(s, t)
+    assert np.array_equal(fa, fb)
+
+
 def test_xml_roundtrip_volume(built, tmp_path):
     s = scenes.volume_grid(20, 16, res=12)
     xmlp = write_scene(s, str(tmp_path))
@@ -236,8 +247,7 @@ def test_xml_unsupported_and_quirks(built, tmp_path):
     s = scenes.cornell_box(8, 8)
     xmlp = write_scene(s, str(tmp_path))
     text = open(xmlp).read()
-    open(tmp_path / "f.xml", "w").write(text.replace('<filter type="BoxFilter"/>',
-                                                     '<filter type="MitchellNetravaliFilter"/>'))
+    open(tmp_path / "f.xml", "w").write(text.replace('<filter type="BoxFilter">', '<filter type="LanczosFilter">'))
     with pytest.raises(UnsupportedScene):
         load_scene(str(tmp_path / "f.xml"))
     open(tmp_path / "b.xml", "w").write(text.replace('type="Diffuse"', 'type="Phong"', 1))
