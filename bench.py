@@ -205,6 +205,7 @@ def run_gpu(args):
     ctx.set_bvh_width(args.bvh_width)
     if args.wave_paths:
         ctx.set_wave_paths(args.wave_paths)
+    ctx.set_ray_sort(args.ray_sort)
     # counting pass (traversal statistics for the roofline; not timed)
     ctx.set_profiling(2)
     scene.render(8, seed=99, film=film.data_ptr())
@@ -228,7 +229,8 @@ def run_gpu(args):
         scene.render(spp, seed=1000 + k, sample_begin=sbase, film=film.data_ptr())
         st = ctx.stats()
         launches += st["launches"]
-        for key in ("trace_closest_ms", "trace_any_ms", "shade_ms", "resolve_ms", "volpath_ms", "camera_ms", "film_ms",
+        for key in ("trace_closest_ms", "trace_any_ms", "shade_ms", "resolve_ms", "sort_ms", "volpath_ms", "camera_ms",
+                    "film_ms",
                     "closest_rays",
                     "shadow_rays", "trace_closest_launches", "trace_any_launches", "paths", "nan_samples"):
             agg[key] = agg.get(key, 0) + st[key]
@@ -259,7 +261,7 @@ def run_gpu(args):
     # roofline of the dominant kernel
     # single kernels (shade = the four per-BSDF shade kernels of a round)
     kern = {"trace_closest": agg["trace_closest_ms"], "trace_any": agg["trace_any_ms"],
-            "resolve": agg["resolve_ms"], "shade": agg["shade_ms"] - agg["resolve_ms"]}
+            "resolve": agg["resolve_ms"], "shade": agg["shade_ms"] - agg["resolve_ms"], "sort": agg["sort_ms"]}
     if CONFIG.get("volume"):
         kern = {"volpath": agg["volpath_ms"]}
     dom = max(kern, key=kern.get)
@@ -471,6 +473,7 @@ def main():
                     help="icosphere: the headline single-scene render; batch: 64 scenes, plain vs "
                          "rt_batch_render; serve: Poisson arrivals through rt_server")
     ap.add_argument("--wave-paths", type=int, default=0, help="paths per wavefront batch (0: library default)")
+    ap.add_argument("--ray-sort", type=int, default=0, choices=[0, 1], help="regroup rays before each trace")
     ap.add_argument("--batch-jobs", type=int, default=64)
     ap.add_argument("--lanes", default="2,4,8", help="batch: lane counts to time")
     ap.add_argument("--rates", default="5,20,100", help="serve: arrival rates (jobs/s)")

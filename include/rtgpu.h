@@ -290,6 +290,7 @@ typedef struct rt_render_stats {
     int64_t limit_hits;      /* device loops that hit their cap                  */
     int64_t nan_samples;     /* samples dropped as NaN (Screen.cpp:46-50)        */
     double resolve_ms;       /* part of shade_ms spent in the resolve kernel     */
+    double sort_ms;          /* ray reordering before the traces                 */
 } rt_render_stats;
 
 typedef struct rt_ctx rt_ctx;
@@ -331,6 +332,9 @@ rt_status rt_ctx_set_bvh_width(rt_ctx *ctx, int32_t width);
  * batched up to this count): 2^16..2^26.  Device memory for path state is
  * about 240 bytes per path. */
 rt_status rt_ctx_set_wave_paths(rt_ctx *ctx, int32_t paths);
+/* Regroup the rays of every bounce after the first by direction octant and
+ * origin cell before tracing them (0 off, 1 on); results are unchanged. */
+rt_status rt_ctx_set_ray_sort(rt_ctx *ctx, int32_t on);
 
 /* Allocation-free tile render.  No counterpart in the reference: it exists
  * for callers that cannot allocate device memory while rendering (plugins

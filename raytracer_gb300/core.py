@@ -72,6 +72,7 @@ def lib():
     L.rt_ctx_set_profiling.argtypes = [vp, C.c_int32]
     L.rt_ctx_set_bvh_width.argtypes = [vp, C.c_int32]
     L.rt_ctx_set_wave_paths.argtypes = [vp, C.c_int32]
+    L.rt_ctx_set_ray_sort.argtypes = [vp, C.c_int32]
     L.rt_trace.argtypes = [vp, vp, vp, C.c_int32, C.c_int32, vp, C.c_int32]
     L.rt_render_tile_static.argtypes = [vp, vp, C.POINTER(D.RenderDesc), C.c_int32, C.c_int32, vp]
     L.rt_render_tile_static.restype = C.c_int32
@@ -94,7 +95,7 @@ def lib():
     L.rt_host_free.argtypes = [vp]
     L.rt_host_free.restype = None
     for name in ("rt_ctx_create", "rt_ctx_destroy", "rt_ctx_set_stream", "rt_scene_create", "rt_scene_destroy",
-                 "rt_scene_info", "rt_render", "rt_render_stats_get", "rt_ctx_set_profiling", "rt_ctx_set_bvh_width", "rt_ctx_set_wave_paths",
+                 "rt_scene_info", "rt_render", "rt_render_stats_get", "rt_ctx_set_profiling", "rt_ctx_set_bvh_width", "rt_ctx_set_wave_paths", "rt_ctx_set_ray_sort",
                  "rt_trace", "rt_bsdf_query", "rt_light_query", "rt_medium_query", "rt_batch_render", "rt_ctx_set_lanes",
                  "rt_server_start", "rt_job_submit", "rt_job_poll", "rt_job_wait", "rt_server_stop"):
         getattr(L, name).restype = C.c_int32
@@ -144,6 +145,10 @@ class Context:
     def set_wave_paths(self, paths):
         """Paths per wavefront batch of later renders (2^16..2^26)."""
         _check(lib().rt_ctx_set_wave_paths(self.h, int(paths)))
+
+    def set_ray_sort(self, on):
+        """Regroup secondary and shadow rays by octant and origin cell before tracing."""
+        _check(lib().rt_ctx_set_ray_sort(self.h, int(bool(on))))
 
     def set_lanes(self, lanes):
         """Concurrent worker lanes of batch_render (1..16, default 4)."""

@@ -148,6 +148,95 @@ __device__ __forceinline__ void classify_hit(const RenderParams &P, RoundCounter
     q_push(P.W.q_fin, &C->fin, slot, t < 0);
 }
 
+// ---------------------------------------------------------------- ray reordering
+// Before a trace, the queued rays can be regrouped by a key made of the
+// direction octant and the Morton code of the origin on a 32^3 grid over the
+// scene bounds (a counting sort: key counts, exclusive scan, scatter), so
+// that a warp traces rays that start close together and head the same way.
+// Every ray still gets its own result; only the order in which rays are
+// taken from the queue changes.
+#define RT_SORT_GRID_BITS 5
+#define RT_SORT_BINS (8 << (3 * RT_SORT_GRID_BITS))
+
+__device__ __forceinline__ unsigned spread3(unsigned v)
+{
+    v &= 0x3ffu;
+    v = (v | (v << 16)) & 0x030000FFu;
+    v = (v | (v << 8)) & 0x0300F00Fu;
+    v = (v | (v << 4)) & 0x030C30C3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+__device__ __forceinline__ unsigned ray_sort_key(const DevScene &S, float4 o, float4 d)
+{
+    const float G = (float)(1 << RT_SORT_GRID_BITS);
+    unsigned c[3];
+    const float oo[3] = {o.x, o.y, o.z};
+    for (int a = 0; a < 3; a++) {
+        float ext = S.bmax[a] - S.bmin[a];
+        float f = ext > 0.f ? (oo[a] - S.bmin[a]) / ext * G : 0.f;
+        int q = (int)f;
+        c[a] = (unsigned)imin(imax(q, 0), (1 << RT_SORT_GRID_BITS) - 1);
+    }
+    unsigned oct = (d.x < 0.f ? 1u : 0u) | (d.y < 0.f ? 2u : 0u) | (d.z < 0.f ? 4u : 0u);
+    unsigned m = spread3(c[0]) | (spread3(c[1]) << 1) | (spread3(c[2]) << 2);
+    return (oct << (3 * RT_SORT_GRID_BITS)) | m;
+}
+__global__ void k_sort_count(RenderParams P, int round, int shadow)
+{
+    const RoundCounters *C = &P.W.cnt[round];
+    const int n = shadow ? C->shadow : C->closest;
+    const int *queue = shadow ? P.W.q_shadow : P.W.q_closest;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int slot = queue[i];
+        float4 o = shadow ? P.W.sh_o[slot] : P.W.ray_o[slot];
+        float4 d = shadow ? P.W.sh_d[slot] : P.W.ray_d[slot];
+        unsigned k = ray_sort_key(P.S, o, d);
+        P.W.sort_keys[i] = k;
+        atomicAdd(&P.W.sort_hist[k], 1u);
+    }
+}
+// exclusive scan of the key counts, one block of 1024 threads
+__global__ void __launch_bounds__(1024) k_sort_scan(RenderParams P)
+{
+    __shared__ unsigned part[1024];
+    const int per = RT_SORT_BINS / 1024;
+    unsigned *h = P.W.sort_hist + threadIdx.x * per;
+    unsigned s = 0;
+    for (int i = 0; i < per; i++) s += h[i];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+        unsigned v = threadIdx.x >= (unsigned)off ? part[threadIdx.x - off] : 0u;
+        __syncthreads();
+        part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    unsigned run = part[threadIdx.x] - s;
+    for (int i = 0; i < per; i++) {
+        unsigned c = h[i];
+        h[i] = run;
+        run += c;
+    }
+}
+__global__ void k_sort_scatter(RenderParams P, int round, int shadow)
+{
+    const RoundCounters *C = &P.W.cnt[round];
+    const int n = shadow ? C->shadow : C->closest;
+    const int *queue = shadow ? P.W.q_shadow : P.W.q_closest;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        unsigned pos = atomicAdd(&P.W.sort_hist[P.W.sort_keys[i]], 1u);
+        P.W.sort_tmp[pos] = queue[i];
+    }
+}
+__global__ void k_sort_copy(RenderParams P, int round, int shadow)
+{
+    const RoundCounters *C = &P.W.cnt[round];
+    const int n = shadow ? C->shadow : C->closest;
+    int *queue = shadow ? P.W.q_shadow : P.W.q_closest;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) queue[i] = P.W.sort_tmp[i];
+}
+
 // ---------------------------------------------------------------- traversal
 // Persistent while-while traversal with per-lane dynamic ray fetch.  Lanes
 // that finish a ray fetch a new one as soon as enough lanes of the warp are
@@ -1303,6 +1392,7 @@ struct rt_ctx {
     int profiling = 0;
     int bvh_width = 2;          // traversal used by renders and rt_trace: 2 or 8
     int wave_paths = 1 << 26;   // target paths per wavefront batch (about 14 GB of path state)
+    int ray_sort = 0;           // reorder secondary and shadow rays before tracing
     std::vector<cudaEvent_t> ev_pool;
     std::vector<int> ev_kind;   // kernel kind per recorded pair
     size_t ev_used = 0;
@@ -1312,7 +1402,8 @@ struct rt_ctx {
 };
 
 // kinds for per-kernel timing
-enum { K_CAMERA = 0, K_TRACE_C = 1, K_TRACE_A = 2, K_SHADE = 3, K_VOLPATH = 4, K_FILM = 5, K_RESOLVE = 6, K_KINDS = 7 };
+enum { K_CAMERA = 0, K_TRACE_C = 1, K_TRACE_A = 2, K_SHADE = 3, K_VOLPATH = 4, K_FILM = 5, K_RESOLVE = 6, K_SORT = 7,
+       K_KINDS = 8 };
 
 static void prof_begin(rt_ctx *c, int kind)
 {
@@ -1595,6 +1686,13 @@ rt_status rt_ctx_set_wave_paths(rt_ctx *c, int32_t paths)
     if (!c) return fail(RT_ERR_INVALID, "null ctx");
     if (paths < (1 << 16) || paths > (1 << 26)) return fail(RT_ERR_INVALID, "wave paths must be in [2^16, 2^26]");
     c->wave_paths = paths;
+    return RT_OK;
+}
+
+rt_status rt_ctx_set_ray_sort(rt_ctx *c, int32_t on)
+{
+    if (!c) return fail(RT_ERR_INVALID, "null ctx");
+    c->ray_sort = on ? 1 : 0;
     return RT_OK;
 }
 
@@ -1989,11 +2087,29 @@ static rt_status ensure_wave(rt_ctx *c, int capacity, int max_rounds)
     ok &= alloc((void **)&W.q_shadow, P * sizeof(int));
     for (int t = 0; t < RT_NBSDF; t++) ok &= alloc((void **)&W.q_mat[t], P * sizeof(int));
     ok &= alloc((void **)&W.cnt, (size_t)(max_rounds + 2) * sizeof(RoundCounters));
+    ok &= alloc((void **)&W.sort_keys, P * sizeof(unsigned));
+    ok &= alloc((void **)&W.sort_tmp, P * sizeof(int));
+    ok &= alloc((void **)&W.sort_hist, (size_t)RT_SORT_BINS * sizeof(unsigned));
     if (!ok) { free_wave(c); return fail(RT_ERR_NOMEM, "wavefront buffer allocation failed"); }
     W.capacity = capacity;
     W.max_rounds = max_rounds;
     c->capacity = capacity;
     return RT_OK;
+}
+
+static rt_status launch_check(const char *what);
+// reorder the round's closest-hit (shadow = 0) or shadow (shadow = 1) queue
+static rt_status sort_rays(rt_ctx *ctx, const RenderParams &P, int round, int shadow, int64_t &launches)
+{
+    cudaStream_t st = ctx->stream;
+    const int sm = ctx->sm_count > 0 ? ctx->sm_count : 1;
+    CK(cudaMemsetAsync(ctx->W.sort_hist, 0, (size_t)RT_SORT_BINS * sizeof(unsigned), st));
+    k_sort_count<<<sm * 8, 256, 0, st>>>(P, round, shadow);
+    k_sort_scan<<<1, 1024, 0, st>>>(P);
+    k_sort_scatter<<<sm * 8, 256, 0, st>>>(P, round, shadow);
+    k_sort_copy<<<sm * 8, 256, 0, st>>>(P, round, shadow);
+    launches += 4;
+    return launch_check("ray reordering");
 }
 
 static rt_status launch_check(const char *what)
@@ -2143,6 +2259,12 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
             for (int r = 0; r < max_rounds; r++) {
                 int ri = r;
                 const bool cnt2 = ctx->profiling >= 2, w8 = ctx->bvh_width == 8 && sc->wide_ok;
+                if (ctx->ray_sort && ri > 0) {
+                    prof_begin(ctx, K_SORT);
+                    if ((s = sort_rays(ctx, P, ri, 0, launches)) != RT_OK) return s;
+                    if ((s = sort_rays(ctx, P, ri, 1, launches)) != RT_OK) return s;
+                    prof_end(ctx);
+                }
                 prof_begin(ctx, K_TRACE_C);
                 if (w8) {
                     if (cnt2) k_trace8<false, true><<<trace_blocks, 128, 0, st>>>(P, ri);
@@ -2207,7 +2329,7 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
     cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
     std::memset(&ctx->last, 0, sizeof(ctx->last));
     ctx->last.kernel_ms = ms;
-    double kt[K_KINDS] = {0, 0, 0, 0, 0, 0, 0};
+    double kt[K_KINDS] = {0, 0, 0, 0, 0, 0, 0, 0};
     for (size_t i = 0; i < ctx->ev_used; i++) {
         float e = 0.f;
         cudaEventElapsedTime(&e, ctx->ev_pool[2 * i], ctx->ev_pool[2 * i + 1]);
@@ -2218,6 +2340,7 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
     ctx->last.trace_any_ms = kt[K_TRACE_A];
     ctx->last.shade_ms = kt[K_SHADE] + kt[K_RESOLVE];
     ctx->last.resolve_ms = kt[K_RESOLVE];
+    ctx->last.sort_ms = kt[K_SORT];
     ctx->last.volpath_ms = kt[K_VOLPATH];
     ctx->last.film_ms = kt[K_FILM];
     ctx->last.trace_closest_launches = trace_c_launches;

@@ -42,6 +42,10 @@ struct Wave {
     int *q_mat[RT_NBSDF];  // per-BSDF-type shading queues, filled by the closest-hit trace
     int *q_fin;        // rays that missed or hit a surface without a BSDF (to finish)
     int *q_end;        // paths whose BSDF sample was zero, light sample pending
+    // ray reordering (optional): per-ray keys, the reordered queue, key counts
+    unsigned *sort_keys;
+    int *sort_tmp;
+    unsigned *sort_hist;
     RoundCounters *cnt;
     int capacity;
     int max_rounds;

@@ -102,6 +102,7 @@ void add_stats(rt_render_stats &a, const rt_render_stats &b)
     a.limit_hits += b.limit_hits;
     a.nan_samples += b.nan_samples;
     a.resolve_ms += b.resolve_ms;
+    a.sort_ms += b.sort_ms;
 }
 
 }  // namespace

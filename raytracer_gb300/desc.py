@@ -123,7 +123,7 @@ class RenderStats(C.Structure):
                 ("shadow_rays", C.c_int64), ("launches", C.c_int64), ("trace_closest_launches", C.c_int64),
                 ("trace_any_launches", C.c_int64), ("nodes_closest", C.c_int64), ("tris_closest", C.c_int64),
                 ("nodes_any", C.c_int64), ("tris_any", C.c_int64), ("limit_hits", C.c_int64),
-                ("nan_samples", C.c_int64), ("resolve_ms", C.c_double)]
+                ("nan_samples", C.c_int64), ("resolve_ms", C.c_double), ("sort_ms", C.c_double)]
 
 
 RAY_DTYPE = np.dtype([("o", np.float32, 3), ("mint", np.float32), ("d", np.float32, 3),
