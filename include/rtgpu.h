@@ -55,7 +55,11 @@ enum {
 
 enum { RT_BSDF_DIFFUSE = 0, RT_BSDF_ROUGH_CONDUCTOR = 1,
        RT_BSDF_ROUGH_DIELECTRIC = 2, RT_BSDF_SMOOTH_LAYERED = 3,
-       RT_BSDF_LAYERED = 4 };
+       RT_BSDF_LAYERED = 4,
+       /* smooth (delta) BSDFs: bsdf/Dielectric.cpp, Conductor.cpp, Mirror.cpp.
+        * Dielectric reads reflectance, transmittance, eta_int and eta_ext;
+        * Conductor reads reflectance, eta and k; Mirror reads nothing. */
+       RT_BSDF_DIELECTRIC = 5, RT_BSDF_CONDUCTOR = 6, RT_BSDF_MIRROR = 7 };
 /* bsdf/MicrofacetDistribution.h:9-13 name order */
 enum { RT_DIST_BECKMANN = 0, RT_DIST_PHONG = 1, RT_DIST_GGX = 2 };
 
@@ -77,6 +81,9 @@ typedef struct rt_bsdf_desc {
      * RoughConductor takes eta, k, reflectance and these two: */
     int32_t distribution_base; /* default beckmann                               */
     float alpha_base;          /* default 0.2                                    */
+    /* 1: wrapped in a TwoSides (bsdf/TwoSides.cpp) with this BSDF on both
+     * sides (the one-child form, where "bsdf2" defaults to "bsdf") */
+    int32_t two_sided;
 } rt_bsdf_desc;
 
 /* One reference Mesh (factory/MeshFactory.h:39-139): a contiguous range of

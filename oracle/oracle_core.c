@@ -722,30 +722,88 @@ static c3 o_ly_sample(const rt_bsdf_desc *b, o_bsdf_rec *r, v2 s, uint64_t aux_k
     return c3_divs(c3_muls(o_ly_eval(b, r->wi, r->wo), fabsf(co)), r->pdf);
 }
 
-/* ===================== BSDF dispatch ===================== */
-c3 o_bsdf_eval(const rt_bsdf_desc *b, const o_bsdf_rec *r)
+/* ===================== smooth (delta) BSDFs ===================== */
+/* Their eval and pdf are zero away from the discrete measure the reference
+ * only attaches to sampled directions (Dielectric.cpp:23-26,85-91;
+ * Conductor.cpp:26-37,55-64; Mirror.cpp:22-29,43-49). */
+/* Dielectric::sample (Dielectric.cpp:28-82) */
+static c3 o_dl_sample(const rt_bsdf_desc *b, o_bsdf_rec *r, v2 s)
 {
-    switch (b->type) {
-    case RT_BSDF_DIFFUSE: return o_diffuse_eval(b->albedo, r->wi, r->wo);
-    case RT_BSDF_ROUGH_CONDUCTOR: return o_rc_eval(b, r->wi, r->wo);
-    case RT_BSDF_ROUGH_DIELECTRIC: return o_rd_eval(b, r->wi, r->wo);
-    case RT_BSDF_SMOOTH_LAYERED: return o_sl_eval(b, r->wi, r->wo);
-    case RT_BSDF_LAYERED: return o_ly_eval(b, r->wi, r->wo);
+    float cosThetaI = r->wi.z;
+    float etaI = b->eta_ext, etaT = b->eta_int;
+    int isEntering = 1;
+    float fr = 0.f;
+    if (cosThetaI <= 0.f) {
+        isEntering = 0;
+        float t = etaI; etaI = etaT; etaT = t;
     }
-    return cfill(0.f);
+    float relativeEta = etaI / etaT;
+    float sinThetaT = relativeEta * sqrtf(fmaxf(0.f, 1 - cosThetaI * cosThetaI));
+    float cosThetaT = sqrtf(fmaxf(0.f, 1 - sinThetaT * sinThetaT));
+    if (sinThetaT >= 1.f) {
+        fr = 1.f;
+    } else {
+        fr = o_fresnel_dielectric(etaI, etaT, fabsf(cosThetaI), cosThetaT);
+        if (isEntering) cosThetaT = -cosThetaT;
+    }
+    r->relative_eta = relativeEta;
+    if (s.x <= fr) {
+        r->sampled_type = O_BSDF_DELTA_REFLECTION;
+        r->wo = o_reflect_local(r->wi);
+        r->pdf = fr;
+        return c3_from(b->reflectance);
+    }
+    r->sampled_type = O_BSDF_DELTA_TRANSMISSION;
+    r->wo = o_refract_local(r->wi, cosThetaT, relativeEta);
+    r->pdf = 1 - fr;
+    return c3_muls(c3_muls(c3_from(b->transmittance), relativeEta), relativeEta);
 }
-float o_bsdf_pdf(const rt_bsdf_desc *b, const o_bsdf_rec *r)
+/* Conductor::sample (Conductor.cpp:39-53) */
+static c3 o_cd_sample(const rt_bsdf_desc *b, o_bsdf_rec *r)
+{
+    if (r->wi.z <= 0.f) return cfill(0.f);
+    r->sampled_type = O_BSDF_DELTA_REFLECTION;
+    r->wo = o_reflect_local(r->wi);
+    r->pdf = 1.f;
+    float cosI = r->wi.z;
+    c3 f = mkc(o_fresnel_conductor1(b->eta[0], b->k[0], cosI), o_fresnel_conductor1(b->eta[1], b->k[1], cosI),
+               o_fresnel_conductor1(b->eta[2], b->k[2], cosI));
+    return c3_mul(c3_from(b->reflectance), f);
+}
+/* Mirror::sample (Mirror.cpp:31-43) */
+static c3 o_mr_sample(o_bsdf_rec *r)
+{
+    if (r->wi.z <= 0.f) return cfill(0.f);
+    r->sampled_type = O_BSDF_DELTA_REFLECTION;
+    r->wo = o_reflect_local(r->wi);
+    r->pdf = 1.f;
+    return cfill(1.f);
+}
+
+/* ===================== BSDF dispatch ===================== */
+static c3 o_bsdf_eval1(const rt_bsdf_desc *b, v3 wi, v3 wo)
 {
     switch (b->type) {
-    case RT_BSDF_DIFFUSE: return o_diffuse_pdf(r->wi, r->wo);
-    case RT_BSDF_ROUGH_CONDUCTOR: return o_rc_pdf(b, r->wi, r->wo);
-    case RT_BSDF_ROUGH_DIELECTRIC: return o_rd_pdf(b, r->wi, r->wo);
-    case RT_BSDF_SMOOTH_LAYERED: return o_sl_pdf(b, r->wi, r->wo);
-    case RT_BSDF_LAYERED: return o_ly_pdf(b, r->wi, r->wo);
+    case RT_BSDF_DIFFUSE: return o_diffuse_eval(b->albedo, wi, wo);
+    case RT_BSDF_ROUGH_CONDUCTOR: return o_rc_eval(b, wi, wo);
+    case RT_BSDF_ROUGH_DIELECTRIC: return o_rd_eval(b, wi, wo);
+    case RT_BSDF_SMOOTH_LAYERED: return o_sl_eval(b, wi, wo);
+    case RT_BSDF_LAYERED: return o_ly_eval(b, wi, wo);
+    }
+    return cfill(0.f);   /* Dielectric, Conductor, Mirror */
+}
+static float o_bsdf_pdf1(const rt_bsdf_desc *b, v3 wi, v3 wo)
+{
+    switch (b->type) {
+    case RT_BSDF_DIFFUSE: return o_diffuse_pdf(wi, wo);
+    case RT_BSDF_ROUGH_CONDUCTOR: return o_rc_pdf(b, wi, wo);
+    case RT_BSDF_ROUGH_DIELECTRIC: return o_rd_pdf(b, wi, wo);
+    case RT_BSDF_SMOOTH_LAYERED: return o_sl_pdf(b, wi, wo);
+    case RT_BSDF_LAYERED: return o_ly_pdf(b, wi, wo);
     }
     return 0.f;
 }
-c3 o_bsdf_sample(const rt_bsdf_desc *b, o_bsdf_rec *r, v2 s, uint64_t aux_key)
+static c3 o_bsdf_sample1(const rt_bsdf_desc *b, o_bsdf_rec *r, v2 s, uint64_t aux_key)
 {
     switch (b->type) {
     case RT_BSDF_DIFFUSE: return o_diffuse_sample(b->albedo, r, s);
@@ -753,8 +811,37 @@ c3 o_bsdf_sample(const rt_bsdf_desc *b, o_bsdf_rec *r, v2 s, uint64_t aux_key)
     case RT_BSDF_ROUGH_DIELECTRIC: return o_rd_sample(b, r, s);
     case RT_BSDF_SMOOTH_LAYERED: return o_sl_sample(b, r, s);
     case RT_BSDF_LAYERED: return o_ly_sample(b, r, s, aux_key);
+    case RT_BSDF_DIELECTRIC: return o_dl_sample(b, r, s);
+    case RT_BSDF_CONDUCTOR: return o_cd_sample(b, r);
+    case RT_BSDF_MIRROR: return o_mr_sample(r);
     }
     return cfill(0.f);
+}
+/* TwoSides (TwoSides.cpp:22-70), both sides the same BSDF: a query with
+ * cosTheta(wi) <= 0 goes to the BSDF with wi.z and wo.z negated, and the
+ * direction it samples comes back with wo.z negated. */
+c3 o_bsdf_eval(const rt_bsdf_desc *b, const o_bsdf_rec *r)
+{
+    v3 wi = r->wi, wo = r->wo;
+    if (b->two_sided && !(wi.z > 0.f)) { wi.z = -r->wi.z; wo.z = -r->wo.z; }
+    return o_bsdf_eval1(b, wi, wo);
+}
+float o_bsdf_pdf(const rt_bsdf_desc *b, const o_bsdf_rec *r)
+{
+    v3 wi = r->wi, wo = r->wo;
+    if (b->two_sided && !(wi.z > 0.f)) { wi.z = -r->wi.z; wo.z = -r->wo.z; }
+    return o_bsdf_pdf1(b, wi, wo);
+}
+c3 o_bsdf_sample(const rt_bsdf_desc *b, o_bsdf_rec *r, v2 s, uint64_t aux_key)
+{
+    if (b->two_sided && !(r->wi.z > 0.f)) {
+        r->wi.z = -r->wi.z;
+        c3 res = o_bsdf_sample1(b, r, s, aux_key);
+        r->wi.z = -r->wi.z;
+        r->wo.z = -r->wo.z;
+        return res;
+    }
+    return o_bsdf_sample1(b, r, s, aux_key);
 }
 
 /* ===================== shapes used by lights ===================== */

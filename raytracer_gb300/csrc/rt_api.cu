@@ -700,9 +700,14 @@ __global__ void __launch_bounds__(128) k_pt_finish(RenderParams P, int round)
     }
 }
 
+// The BSDF functions of one shading queue (bsdf_queue), with the TwoSides
+// mirroring of bsdf_eval/bsdf_pdf/bsdf_sample.  Queue RT_QUEUE_DELTA holds
+// the smooth BSDFs, whose eval and pdf are zero.
 template <int BT>
 __device__ __forceinline__ C3 bsdf_eval_t(const DevBsdf &b, V3 wi, V3 wo)
 {
+    if (BT == RT_QUEUE_DELTA) return cfill(0.f);
+    if (b.two_sided && !(wi.z > 0.f)) { wi.z = -wi.z; wo.z = -wo.z; }
     if (BT == 0) return diffuse_eval(b.albedo, wi, wo);
     if (BT == 1) return rc_eval(b, wi, wo);
     if (BT == 2) return rd_eval(b, wi, wo);
@@ -712,6 +717,8 @@ __device__ __forceinline__ C3 bsdf_eval_t(const DevBsdf &b, V3 wi, V3 wo)
 template <int BT>
 __device__ __forceinline__ float bsdf_pdf_t(const DevBsdf &b, V3 wi, V3 wo)
 {
+    if (BT == RT_QUEUE_DELTA) return 0.f;
+    if (b.two_sided && !(wi.z > 0.f)) { wi.z = -wi.z; wo.z = -wo.z; }
     if (BT == 0) return diffuse_pdf(wi, wo);
     if (BT == 1) return rc_pdf(b, wi, wo);
     if (BT == 2) return rd_pdf(b, wi, wo);
@@ -719,13 +726,28 @@ __device__ __forceinline__ float bsdf_pdf_t(const DevBsdf &b, V3 wi, V3 wo)
     return ly_pdf(b, wi, wo);
 }
 template <int BT>
-__device__ __forceinline__ C3 bsdf_sample_t(const DevBsdf &b, BsdfRec &r, V2 s, uint64_t aux_key)
+__device__ __forceinline__ C3 bsdf_sample1_t(const DevBsdf &b, BsdfRec &r, V2 s, uint64_t aux_key)
 {
     if (BT == 0) return diffuse_sample(b.albedo, r, s);
     if (BT == 1) return rc_sample(b, r, s);
     if (BT == 2) return rd_sample(b, r, s);
     if (BT == 3) return sl_sample(b, r, s);
-    return ly_sample(b, r, s, aux_key);
+    if (BT == 4) return ly_sample(b, r, s, aux_key);
+    if (b.type == RT_BSDF_DIELECTRIC) return dl_sample(b, r, s);
+    if (b.type == RT_BSDF_CONDUCTOR) return cd_sample(b, r);
+    return mr_sample(r);
+}
+template <int BT>
+__device__ __forceinline__ C3 bsdf_sample_t(const DevBsdf &b, BsdfRec &r, V2 s, uint64_t aux_key)
+{
+    if (b.two_sided && !(r.wi.z > 0.f)) {
+        r.wi.z = -r.wi.z;
+        C3 res = bsdf_sample1_t<BT>(b, r, s, aux_key);
+        r.wi.z = -r.wi.z;
+        r.wo.z = -r.wo.z;
+        return res;
+    }
+    return bsdf_sample1_t<BT>(b, r, s, aux_key);
 }
 
 #ifndef RT_SHADE_MINB
@@ -1444,7 +1466,7 @@ struct rt_scene {
     int n_lights = 0;
     int n_bsdfs = 0;
     int n_media = 0;
-    int bsdf_types = 0;   // bit t set when some BSDF of type t exists
+    int bsdf_types = 0;   // bit q set when some BSDF uses shading queue q (bsdf_queue)
     int wide_depth = 0;
     bool wide_ok = false;  // the 8-wide BVH is uploaded (or the scene has no triangles)
     std::vector<float> light_power_lum;  // per light, for the weighted strategy
@@ -1761,7 +1783,7 @@ static rt_status validate(const rt_scene_desc *d)
         }
     }
     for (int b = 0; b < d->n_bsdfs; b++)
-        if (d->bsdfs[b].type < 0 || d->bsdfs[b].type > 4) return fail(RT_ERR_UNSUPPORTED, "BSDF type not supported");
+        if (d->bsdfs[b].type < 0 || d->bsdfs[b].type > RT_BSDF_MIRROR) return fail(RT_ERR_UNSUPPORTED, "BSDF type not supported");
     for (int m = 0; m < d->n_media; m++) {
         const rt_medium_desc &M = d->media[m];
         if (M.type == RT_MEDIUM_HETEROGENEOUS && (!M.density || M.res[0] < 2 || M.res[1] < 2 || M.res[2] < 2))
@@ -1872,6 +1894,7 @@ rt_status rt_scene_create(rt_ctx *ctx, const rt_scene_desc *d, rt_scene **out)
         D.dist_base = B.distribution_base;
         D.alpha_base_avg = h_cavg1(B.alpha_base);
         D.eta_int = B.eta_int; D.eta_ext = B.eta_ext; D.thickness = B.thickness;
+        D.two_sided = B.two_sided != 0;
     }
     // media
     std::vector<DevMedium> media(d->n_media);
@@ -2000,7 +2023,7 @@ rt_status rt_scene_create(rt_ctx *ctx, const rt_scene_desc *d, rt_scene **out)
         std::vector<uint8_t> tri_type(nt, 255);
         for (int t = 0; t < nt; t++) {
             int b = d->meshes[tri_mesh[t]].bsdf;
-            if (b >= 0) tri_type[t] = (uint8_t)d->bsdfs[b].type;
+            if (b >= 0) tri_type[t] = (uint8_t)bsdf_queue(d->bsdfs[b].type);
         }
         const uint8_t *tp8;
         if ((st = upload(sc, tri_type.data(), tri_type.size(), &tp8)) != RT_OK) { rt_scene_destroy(sc); return st; }
@@ -2047,7 +2070,7 @@ rt_status rt_scene_create(rt_ctx *ctx, const rt_scene_desc *d, rt_scene **out)
     sc->n_lights = d->n_lights;
     sc->n_bsdfs = d->n_bsdfs;
     sc->n_media = d->n_media;
-    for (int b = 0; b < d->n_bsdfs; b++) sc->bsdf_types |= 1 << d->bsdfs[b].type;
+    for (int b = 0; b < d->n_bsdfs; b++) sc->bsdf_types |= 1 << bsdf_queue(d->bsdfs[b].type);
     *out = sc;
     return RT_OK;
 }
@@ -2302,6 +2325,7 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
                 if (sc->bsdf_types & 4) k_pt_shade<2><<<shade_blocks, 128, 0, st>>>(P, ri);
                 if (sc->bsdf_types & 8) k_pt_shade<3><<<shade_blocks, 128, 0, st>>>(P, ri);
                 if (sc->bsdf_types & 16) k_pt_shade<4><<<shade_blocks, 128, 0, st>>>(P, ri);
+                if (sc->bsdf_types & 32) k_pt_shade<5><<<shade_blocks, 128, 0, st>>>(P, ri);
                 prof_end(ctx);
                 launches += 3 + __builtin_popcount(sc->bsdf_types);
                 trace_c_launches++;
@@ -2685,6 +2709,7 @@ extern "C" rt_status rt_render_tile_static(rt_ctx *ctx, rt_scene *sc, const rt_r
             if (sc->bsdf_types & 4) k_pt_shade<2><<<blocks, 128, 0, st>>>(Pm, r);
             if (sc->bsdf_types & 8) k_pt_shade<3><<<blocks, 128, 0, st>>>(Pm, r);
             if (sc->bsdf_types & 16) k_pt_shade<4><<<blocks, 128, 0, st>>>(Pm, r);
+            if (sc->bsdf_types & 32) k_pt_shade<5><<<blocks, 128, 0, st>>>(Pm, r);
             if ((s = launch_check("pt round (static)")) != RT_OK) return s;
             if ((r & 3) == 3 && r + 1 < rounds) {
                 RoundCounters nc;

@@ -34,7 +34,14 @@ struct DevBsdf {
     // base's eta, k and reflectance use the fields above)
     int dist_base;
     float alpha_base_avg;
+    int two_sided;    // wrapped in TwoSides (bsdf/TwoSides.cpp) with itself on both sides
 };
+
+// Shading queue of a BSDF type.  The heavy types (0-4) get a queue and a
+// shading kernel each; the smooth (delta) types Dielectric, Conductor and
+// Mirror (5-7) are cheap and share one.
+#define RT_QUEUE_DELTA 5
+__host__ __device__ __forceinline__ int bsdf_queue(int type) { return type < RT_QUEUE_DELTA ? type : RT_QUEUE_DELTA; }
 
 struct DevLight {
     int type, mesh_light, shape_kind, shape;
@@ -94,7 +101,7 @@ struct DevScene {
     const float *tri_v;         // 9 floats per triangle (p0, p1, p2)
     const float *tri_n;         // 9 floats per triangle (n0, n1, n2) or null
     const int *tri_mesh;
-    const uint8_t *tri_type;    // BSDF type of the triangle's mesh, 255 = no BSDF
+    const uint8_t *tri_type;    // shading queue (bsdf_queue) of the triangle's mesh BSDF, 255 = no BSDF
     const DevMesh *meshes;
     const float *mesh_cdf;
     int n_meshes;
@@ -368,7 +375,7 @@ __device__ __forceinline__ int prim_light(const DevScene &S, int prim)
 {
     return prim >= 0 ? S.meshes[S.tri_mesh[prim]].light : S.spheres[-prim - 2].light;
 }
-// BSDF type of a hit primitive (triangle or sphere), or -1 without a BSDF
+// shading queue (bsdf_queue) of a hit primitive's BSDF, or -1 without a BSDF
 __device__ __forceinline__ int prim_type(const DevScene &S, int prim)
 {
     if (prim >= 0) {
@@ -376,7 +383,7 @@ __device__ __forceinline__ int prim_type(const DevScene &S, int prim)
         return t == 255 ? -1 : t;
     }
     int b = S.spheres[-prim - 2].bsdf;
-    return b < 0 ? -1 : S.bsdfs[b].type;
+    return b < 0 ? -1 : bsdf_queue(S.bsdfs[b].type);
 }
 __device__ __forceinline__ int prim_interior(const DevScene &S, int prim)
 {
@@ -982,36 +989,122 @@ __device__ __forceinline__ C3 ly_sample(const DevBsdf &b, BsdfRec &r, V2 s, uint
     return (ly_eval(b, r.wi, r.wo) * fabsf(co)) / r.pdf;
 }
 
-__device__ __forceinline__ C3 bsdf_eval(const DevBsdf &b, V3 wi, V3 wo)
+// Smooth (delta) BSDFs.  Their eval and pdf are zero outside the discrete
+// measure the reference attaches only to sampled directions
+// (Dielectric.cpp:23-26,85-88; Conductor.cpp:26-37,55-64; Mirror.cpp:17-20,
+// 36-39), so only sample() contributes.
+// Dielectric::sample (bsdf/Dielectric.cpp:28-82): Fresnel-chosen delta
+// reflection or refraction; relativeEta is set on both branches
+__device__ __forceinline__ C3 dl_sample(const DevBsdf &b, BsdfRec &r, V2 s)
+{
+    float ci = r.wi.z;
+    float eI = b.eta_ext, eT = b.eta_int;
+    bool entering = true;
+    float fr = 0.f;
+    if (ci <= 0.f) { entering = false; float q = eI; eI = eT; eT = q; }
+    float rel = eI / eT;
+    float sinT = rel * sqrtf(smax(0.f, 1 - ci * ci));
+    float cT = sqrtf(smax(0.f, 1 - sinT * sinT));
+    if (sinT >= 1.f) fr = 1.f;
+    else {
+        fr = fresnel_dielectric(eI, eT, fabsf(ci), cT);
+        if (entering) cT = -cT;
+    }
+    r.rel_eta = rel;
+    if (s.x <= fr) {
+        r.type = BT_DELTA_REFLECTION;
+        r.wo = v3(-r.wi.x, -r.wi.y, r.wi.z);
+        r.pdf = fr;
+        return cload(b.reflectance);
+    }
+    r.type = BT_DELTA_TRANSMISSION;
+    r.wo = refract_local(r.wi, cT, rel);
+    r.pdf = 1 - fr;
+    C3 t = cload(b.transmittance) * rel;
+    return t * rel;
+}
+// Conductor::sample (bsdf/Conductor.cpp:39-53)
+__device__ __forceinline__ C3 cd_sample(const DevBsdf &b, BsdfRec &r)
+{
+    if (r.wi.z <= 0.f) return cfill(0.f);
+    r.type = BT_DELTA_REFLECTION;
+    r.wo = v3(-r.wi.x, -r.wi.y, r.wi.z);
+    r.pdf = 1.f;
+    float ci = r.wi.z;
+    C3 F = c3(fresnel_conductor1(b.eta[0], b.k[0], ci), fresnel_conductor1(b.eta[1], b.k[1], ci),
+              fresnel_conductor1(b.eta[2], b.k[2], ci));
+    return cload(b.reflectance) * F;
+}
+// Mirror::sample (bsdf/Mirror.cpp:22-34)
+__device__ __forceinline__ C3 mr_sample(BsdfRec &r)
+{
+    if (r.wi.z <= 0.f) return cfill(0.f);
+    r.type = BT_DELTA_REFLECTION;
+    r.wo = v3(-r.wi.x, -r.wi.y, r.wi.z);
+    r.pdf = 1.f;
+    return cfill(1.f);
+}
+
+// one BSDF type, no TwoSides wrapper
+__device__ __forceinline__ C3 bsdf_eval1(const DevBsdf &b, V3 wi, V3 wo)
 {
     switch (b.type) {
     case 0: return diffuse_eval(b.albedo, wi, wo);
     case 1: return rc_eval(b, wi, wo);
     case 2: return rd_eval(b, wi, wo);
     case 3: return sl_eval(b, wi, wo);
-    default: return ly_eval(b, wi, wo);
+    case 4: return ly_eval(b, wi, wo);
+    default: return cfill(0.f);
     }
 }
-__device__ __forceinline__ float bsdf_pdf(const DevBsdf &b, V3 wi, V3 wo)
+__device__ __forceinline__ float bsdf_pdf1(const DevBsdf &b, V3 wi, V3 wo)
 {
     switch (b.type) {
     case 0: return diffuse_pdf(wi, wo);
     case 1: return rc_pdf(b, wi, wo);
     case 2: return rd_pdf(b, wi, wo);
     case 3: return sl_pdf(b, wi, wo);
-    default: return ly_pdf(b, wi, wo);
+    case 4: return ly_pdf(b, wi, wo);
+    default: return 0.f;
     }
 }
-// aux_key: the side-stream key of a LayeredBSDF sample (ly_sample)
-__device__ __forceinline__ C3 bsdf_sample(const DevBsdf &b, BsdfRec &r, V2 s, uint64_t aux_key)
+__device__ __forceinline__ C3 bsdf_sample1(const DevBsdf &b, BsdfRec &r, V2 s, uint64_t aux_key)
 {
     switch (b.type) {
     case 0: return diffuse_sample(b.albedo, r, s);
     case 1: return rc_sample(b, r, s);
     case 2: return rd_sample(b, r, s);
     case 3: return sl_sample(b, r, s);
-    default: return ly_sample(b, r, s, aux_key);
+    case 4: return ly_sample(b, r, s, aux_key);
+    case 5: return dl_sample(b, r, s);
+    case 6: return cd_sample(b, r);
+    default: return mr_sample(r);
     }
+}
+// TwoSides (bsdf/TwoSides.cpp:24-70): seen from below, the directions are
+// mirrored to the upper side (z negated) before the wrapped BSDF and the
+// sampled direction mirrored back
+__device__ __forceinline__ C3 bsdf_eval(const DevBsdf &b, V3 wi, V3 wo)
+{
+    if (b.two_sided && !(wi.z > 0.f)) { wi.z = -wi.z; wo.z = -wo.z; }
+    return bsdf_eval1(b, wi, wo);
+}
+__device__ __forceinline__ float bsdf_pdf(const DevBsdf &b, V3 wi, V3 wo)
+{
+    if (b.two_sided && !(wi.z > 0.f)) { wi.z = -wi.z; wo.z = -wo.z; }
+    return bsdf_pdf1(b, wi, wo);
+}
+// aux_key: the side-stream key of a LayeredBSDF sample (ly_sample)
+__device__ __forceinline__ C3 bsdf_sample(const DevBsdf &b, BsdfRec &r, V2 s, uint64_t aux_key)
+{
+    if (b.two_sided && !(r.wi.z > 0.f)) {
+        r.wi.z = -r.wi.z;
+        C3 res = bsdf_sample1(b, r, s, aux_key);
+        r.wi.z = -r.wi.z;
+        r.wo.z = -r.wo.z;
+        return res;
+    }
+    return bsdf_sample1(b, r, s, aux_key);
 }
 
 // ------------------------------------------------------------------ lights

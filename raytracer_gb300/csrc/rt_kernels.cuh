@@ -10,14 +10,14 @@ namespace rtgpu {
 // path flags
 enum { F_FIRST = 1, F_DELTA = 2, F_NEE = 4, F_END = 8, F_DONE = 16 };
 
-#define RT_NBSDF 5        // BSDF types, one shading queue and kernel each
+#define RT_NBSDF 6        // shading queues (bsdf_queue): types 0-4, then the delta types
 
 struct RoundCounters {   // one per wavefront round, zeroed per batch
     int closest, shadow, wc_closest, wc_shadow;
-    int mat[RT_NBSDF];   // paths to shade per BSDF type (material-sorted queues)
+    int mat[RT_NBSDF];   // paths to shade per shading queue (material-sorted)
     int fin;             // paths whose traced ray missed or hit a surface without a BSDF
     int end;             // paths that ended in shading with a light sample pending
-    int pad[5];
+    int pad[4];
 };
 
 struct Wave {
@@ -39,7 +39,7 @@ struct Wave {
     uint8_t *pix_irregular;  // per batch pixel: some sample splats off its pixel
     // queues of the current round
     int *q_closest, *q_shadow;
-    int *q_mat[RT_NBSDF];  // per-BSDF-type shading queues, filled by the closest-hit trace
+    int *q_mat[RT_NBSDF];  // shading queues (bsdf_queue), filled by the closest-hit trace
     int *q_fin;        // rays that missed or hit a surface without a BSDF (to finish)
     int *q_end;        // paths whose BSDF sample was zero, light sample pending
     // ray reordering (optional): per-ray keys, the reordered queue, key counts

@@ -14,6 +14,7 @@ f16 = C.c_float * 16
 i3 = C.c_int32 * 3
 
 BSDF_DIFFUSE, BSDF_ROUGH_CONDUCTOR, BSDF_ROUGH_DIELECTRIC, BSDF_SMOOTH_LAYERED, BSDF_LAYERED = 0, 1, 2, 3, 4
+BSDF_DIELECTRIC, BSDF_CONDUCTOR, BSDF_MIRROR = 5, 6, 7
 DIST_BECKMANN, DIST_PHONG, DIST_GGX = 0, 1, 2
 LIGHT_AREA, LIGHT_ENV = 0, 1
 SHAPE_MESH, SHAPE_SPHERE = 0, 1
@@ -26,7 +27,8 @@ BSDF_OP_EVAL, BSDF_OP_PDF, BSDF_OP_SAMPLE = 0, 1, 2
 # reference name -> enum (XML "type" attributes, bsdf/*.cpp RT_REGISTER_TYPE)
 BSDF_TYPES = {"diffuse": BSDF_DIFFUSE, "roughconductor": BSDF_ROUGH_CONDUCTOR,
               "roughdielectric": BSDF_ROUGH_DIELECTRIC, "smoothlayeredbsdf": BSDF_SMOOTH_LAYERED,
-              "layeredbsdf": BSDF_LAYERED}
+              "layeredbsdf": BSDF_LAYERED, "dielectric": BSDF_DIELECTRIC,
+              "conductor": BSDF_CONDUCTOR, "mirror": BSDF_MIRROR}
 DIST_TYPES = {"beckmann": DIST_BECKMANN, "phong": DIST_PHONG, "ggx": DIST_GGX}
 
 
@@ -35,7 +37,8 @@ class BsdfDesc(C.Structure):
                 ("reflectance", f3), ("transmittance", f3), ("eta", f3), ("k", f3),
                 ("alpha", C.c_float), ("eta_int", C.c_float), ("eta_ext", C.c_float),
                 ("thickness", C.c_float), ("absorbance", f3),
-                ("distribution_base", C.c_int32), ("alpha_base", C.c_float)]
+                ("distribution_base", C.c_int32), ("alpha_base", C.c_float),
+                ("two_sided", C.c_int32)]
 
 
 class MeshDesc(C.Structure):
@@ -160,7 +163,9 @@ def bsdf(kind, **kw):
     (Diffuse.cpp:11-18, RoughConductor.cpp:13-30, RoughDielectric.cpp:13-32,
     SmoothLayeredBSDF.cpp:12-28, LayeredBSDF.cpp:17-36: coat distribution ggx,
     alphaTop 0.01, over a default RoughConductor: beckmann, alpha 0.2,
-    eta = k = 0)."""
+    eta = k = 0; Dielectric.cpp:10-17, Conductor.cpp:13-21, Mirror.cpp:7-15).
+    two_sided=True wraps it in a TwoSides (TwoSides.cpp:5-15) with the same
+    BSDF on both sides."""
     layered = kind == BSDF_LAYERED
     d = dict(type=kind, distribution=kw.get("distribution", DIST_GGX if layered else DIST_BECKMANN),
              albedo=kw.get("albedo", (0.5, 0.5, 0.5)),
@@ -171,7 +176,7 @@ def bsdf(kind, **kw):
              eta_ext=kw.get("eta_ext", 1.000277), thickness=kw.get("thickness", 1.2),
              absorbance=kw.get("absorbance", (0.0, 0.0, 0.0)),
              distribution_base=kw.get("distribution_base", DIST_BECKMANN),
-             alpha_base=kw.get("alpha_base", 0.2))
+             alpha_base=kw.get("alpha_base", 0.2), two_sided=bool(kw.get("two_sided", False)))
     return d
 
 
@@ -180,7 +185,8 @@ def bsdf_struct(b):
     return BsdfDesc(b["type"], b["distribution"], f3(*b["albedo"]), f3(*b["reflectance"]),
                     f3(*b["transmittance"]), f3(*b["eta"]), f3(*b["k"]), b["alpha"],
                     b["eta_int"], b["eta_ext"], b["thickness"], f3(*b["absorbance"]),
-                    b.get("distribution_base", DIST_BECKMANN), b.get("alpha_base", 0.2))
+                    b.get("distribution_base", DIST_BECKMANN), b.get("alpha_base", 0.2),
+                    int(bool(b.get("two_sided", False))))
 
 
 class SceneData:

@@ -18,7 +18,8 @@ from . import desc as D
 
 _BSDF_NAMES = {D.BSDF_DIFFUSE: "Diffuse", D.BSDF_ROUGH_CONDUCTOR: "RoughConductor",
                D.BSDF_ROUGH_DIELECTRIC: "RoughDielectric", D.BSDF_SMOOTH_LAYERED: "SmoothLayeredBSDF",
-               D.BSDF_LAYERED: "LayeredBSDF"}
+               D.BSDF_LAYERED: "LayeredBSDF", D.BSDF_DIELECTRIC: "Dielectric", D.BSDF_CONDUCTOR: "Conductor",
+               D.BSDF_MIRROR: "Mirror"}
 _DIST_NAMES = {D.DIST_BECKMANN: "beckmann", D.DIST_PHONG: "phong", D.DIST_GGX: "ggx"}
 _STRATEGY_NAMES = {D.STRATEGY_ALL_LIGHTS: "all_lights", D.STRATEGY_ONE_LIGHT_UNIFORM: "one_light_uniform",
                    D.STRATEGY_ONE_LIGHT_WEIGHTED: "one_light_weighted"}
@@ -86,9 +87,18 @@ def _write_obj(path, v, n, t):
                 f.write("f %d %d %d\n" % (a, b, c))
 
 
+def _tex_xml(pad, name, c):
+    return ('%s  <texture name="%s" type="ConstantTexture"><color name="albedo" value="%s"/></texture>'
+            % (pad, name, _c(c)))
+
+
 def _bsdf_xml(b, indent):
-    name = _BSDF_NAMES[b["type"]]
     pad = " " * indent
+    if b.get("two_sided"):
+        inner = _bsdf_xml(dict(b, two_sided=False), indent + 2)
+        inner[0] = inner[0].replace('<bsdf type=', '<bsdf name="bsdf" type=')
+        return ['%s<bsdf type="TwoSides">' % pad] + inner + ["%s</bsdf>" % pad]
+    name = _BSDF_NAMES[b["type"]]
     lines = ['%s<bsdf type="%s">' % (pad, name)]
     if b["type"] == D.BSDF_DIFFUSE:
         lines.append('%s  <color name="albedo" value="%s"/>' % (pad, _c(b["albedo"])))
@@ -98,13 +108,30 @@ def _bsdf_xml(b, indent):
                   '%s  <double name="alpha" value="%s"/>' % (pad, _f(b["alpha"])),
                   '%s  <string name="distribution" value="%s"/>' % (pad, _DIST_NAMES[b["distribution"]])]
         if tuple(b["reflectance"]) != (1.0, 1.0, 1.0):
-            lines.append('%s  <texture name="reflectanceTexture" type="ConstantTexture"><color name="albedo" '
-                         'value="%s"/></texture>' % (pad, _c(b["reflectance"])))
+            lines.append(_tex_xml(pad, "reflectanceTexture", b["reflectance"]))
     elif b["type"] == D.BSDF_ROUGH_DIELECTRIC:
         lines += ['%s  <double name="alpha" value="%s"/>' % (pad, _f(b["alpha"])),
                   '%s  <double name="etaInt" value="%s"/>' % (pad, _f(b["eta_int"])),
                   '%s  <double name="etaExt" value="%s"/>' % (pad, _f(b["eta_ext"])),
                   '%s  <string name="distribution" value="%s"/>' % (pad, _DIST_NAMES[b["distribution"]])]
+        if tuple(b["reflectance"]) != (1.0, 1.0, 1.0):
+            lines.append(_tex_xml(pad, "reflectanceTexture", b["reflectance"]))
+        if tuple(b["transmittance"]) != (1.0, 1.0, 1.0):
+            lines.append(_tex_xml(pad, "transmittedTexture", b["transmittance"]))
+    elif b["type"] == D.BSDF_DIELECTRIC:
+        lines += ['%s  <double name="etaInt" value="%s"/>' % (pad, _f(b["eta_int"])),
+                  '%s  <double name="etaExt" value="%s"/>' % (pad, _f(b["eta_ext"]))]
+        if tuple(b["reflectance"]) != (1.0, 1.0, 1.0):
+            lines.append(_tex_xml(pad, "reflectanceTexture", b["reflectance"]))
+        if tuple(b["transmittance"]) != (1.0, 1.0, 1.0):
+            lines.append(_tex_xml(pad, "transmittedTexture", b["transmittance"]))
+    elif b["type"] == D.BSDF_CONDUCTOR:
+        lines += ['%s  <color name="eta" value="%s"/>' % (pad, _c(b["eta"])),
+                  '%s  <color name="absorption" value="%s"/>' % (pad, _c(b["k"]))]
+        if tuple(b["reflectance"]) != (1.0, 1.0, 1.0):
+            lines.append(_tex_xml(pad, "reflectanceTexture", b["reflectance"]))
+    elif b["type"] == D.BSDF_MIRROR:
+        pass
     elif b["type"] == D.BSDF_SMOOTH_LAYERED:
         lines += ['%s  <double name="etaInt" value="%s"/>' % (pad, _f(b["eta_int"])),
                   '%s  <double name="etaExt" value="%s"/>' % (pad, _f(b["eta_ext"])),

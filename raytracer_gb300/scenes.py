@@ -188,6 +188,33 @@ def cornell_box(width=256, height=256):
     return s
 
 
+def cornell_smooth(width=128, height=128, max_depth=12):
+    """The Cornell-box room furnished with the smooth BSDFs: a gold Conductor
+    tall box, a glass (Dielectric) short box, a Mirror sphere, and two thin
+    panels seen from both sides, one a TwoSides Diffuse and one a TwoSides
+    RoughConductor."""
+    s = cornell_box(width, height)
+    s.name = "cornell_smooth_%d" % width
+    from .desc import BSDF_CONDUCTOR, BSDF_DIELECTRIC, BSDF_MIRROR
+    gold = s.add_bsdf(bsdf(BSDF_CONDUCTOR, eta=AU_ETA, k=AU_K))
+    glass = s.add_bsdf(bsdf(BSDF_DIELECTRIC, eta_int=1.5, transmittance=(0.95, 0.97, 1.0)))
+    mirror = s.add_bsdf(bsdf(BSDF_MIRROR))
+    pan_d = s.add_bsdf(bsdf(BSDF_DIFFUSE, albedo=(0.2, 0.3, 0.7), two_sided=True))
+    pan_c = s.add_bsdf(bsdf(BSDF_ROUGH_CONDUCTOR, distribution=DIST_GGX, alpha=0.25, eta=AU_ETA, k=AU_K,
+                            two_sided=True))
+    s.meshes[3]["bsdf"] = gold    # tall box
+    s.meshes[4]["bsdf"] = glass   # short box
+    T = np.eye(4)
+    T[:3, 3] = (0.22, 0.1, 0.78)
+    s.add_sphere(0.1, T, bsdf=mirror)
+    # panels facing +z (toward the camera) in the upper corners, tilted so
+    # that both of their sides see the light
+    s.add_mesh(*_quad((0.05, 0.62, 0.55), (0.3, 0.62, 0.45), (0.3, 0.85, 0.6), (0.05, 0.85, 0.7)), bsdf=pan_d)
+    s.add_mesh(*_quad((0.7, 0.62, 0.45), (0.95, 0.62, 0.55), (0.95, 0.85, 0.7), (0.7, 0.85, 0.6)), bsdf=pan_c)
+    s.integrator = dict(s.integrator, max_depth=max_depth)
+    return s
+
+
 def displaced_icosphere(level=8, width=1024, height=1024, seed=0, alpha_bins=32,
                         env_size=(1024, 512), max_depth=16, env=None):
     """Config [1]: displaced icosphere on a ground quad under a sky (`env`:

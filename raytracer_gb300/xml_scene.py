@@ -21,8 +21,9 @@ the element.  Paths in the file are resolved against the file's folder
                  each with <bsdf>, <light type="AreaLight|MeshLight"> (radiance),
                  <medium name="interior|exterior">
     bsdf         Diffuse, RoughConductor, RoughDielectric, SmoothLayeredBSDF
-                 (over Diffuse), LayeredBSDF (over RoughConductor); top-level
-                 <bsdf id=..> and <transform id=..>
+                 (over Diffuse), LayeredBSDF (over RoughConductor), Dielectric,
+                 Conductor, Mirror, TwoSides (one "bsdf" for both sides);
+                 top-level <bsdf id=..> and <transform id=..>
                  can be referenced with ref=".."
     media        Homogeneous (sigmaA, sigmaS, scale), Heterogeneous (albedo,
                  <volume type="GridVolume"> path .vol, centered, toWorld, scale),
@@ -138,6 +139,7 @@ class _Loader:
         self.s = D.SceneData()
         self.s.name = os.path.splitext(os.path.basename(path))[0]
         self.ref_bsdf = {}
+        self.ref_bsdf_name = {}   # id -> the element's name attribute (XMLLoader.cpp:108-114)
         self.ref_transform = {}
         self.ref_medium = {}
         self.camera_params = None
@@ -185,7 +187,12 @@ class _Loader:
                 tp = self.props(c)
                 params[name] = ("texture", tp.get("albedo", (0.5, 0.5, 0.5)))   # ConstantTexture.cpp:6-10
             elif tag == "bsdf":
-                params[name] = self.ref_bsdf[c.get("ref")] if c.get("ref") else self.bsdf(c)
+                # a referenced BSDF keeps the name its <bsdf id=..> element
+                # gave it (XMLLoader.cpp:762-775)
+                if c.get("ref"):
+                    params[self.ref_bsdf_name[c.get("ref")]] = self.ref_bsdf[c.get("ref")]
+                else:
+                    params[name] = self.bsdf(c)
             elif tag == "medium":
                 params[name] = self.ref_medium[c.get("ref")] if c.get("ref") else self.medium(c)
             elif tag == "phase":
@@ -210,14 +217,7 @@ class _Loader:
         if kind == "Diffuse":   # Diffuse.cpp:11-18
             b = D.bsdf(D.BSDF_DIFFUSE, albedo=self._tex_or(p, "albedo", (0.5, 0.5, 0.5)))
         elif kind == "RoughConductor":   # RoughConductor.cpp:13-30, tools/Common.cpp:56-81
-            mat = p.get("material", "")
-            if mat:
-                if mat not in self.materials:
-                    raise UnsupportedScene("conductor material %r needs its eta/k: pass materials={%r: (eta, k)}"
-                                           % (mat, mat))
-                eta, k = self.materials[mat]
-            else:
-                eta, k = p.get("eta", (0.0, 0.0, 0.0)), p.get("absorption", (0.0, 0.0, 0.0))
+            eta, k = self._conductor_ior(p)
             alpha = self._tex_or(p, "alpha", 0.2)
             if isinstance(alpha, tuple):
                 alpha = (alpha[0] + alpha[0] + alpha[0]) / 3.0
@@ -254,9 +254,38 @@ class _Loader:
                        eta_ext=p.get("etaExt", 1.000277), thickness=p.get("thickness", 1.2),
                        absorbance=p.get("absorbance", (0.0, 0.0, 0.0)), eta=bd["eta"], k=bd["k"],
                        reflectance=bd["reflectance"], distribution_base=bd["distribution"], alpha_base=bd["alpha"])
+        elif kind == "Dielectric":   # Dielectric.cpp:10-17
+            b = D.bsdf(D.BSDF_DIELECTRIC, eta_int=p.get("etaInt", 1.5046), eta_ext=p.get("etaExt", 1.000277),
+                       reflectance=self._tex_or(p, "reflectanceTexture", (1.0, 1.0, 1.0)),
+                       transmittance=self._tex_or(p, "transmittedTexture", (1.0, 1.0, 1.0)))
+        elif kind == "Conductor":   # Conductor.cpp:13-21, tools/Common.cpp:56-81
+            eta, k = self._conductor_ior(p)
+            b = D.bsdf(D.BSDF_CONDUCTOR, eta=eta, k=k,
+                       reflectance=self._tex_or(p, "reflectanceTexture", (1.0, 1.0, 1.0)))
+        elif kind == "Mirror":   # Mirror.cpp:7-15
+            b = D.bsdf(D.BSDF_MIRROR)
+        elif kind == "TwoSides":   # TwoSides.cpp:5-15
+            front = p.get("bsdf")
+            if front is None:
+                raise UnsupportedScene("TwoSides without a bsdf")
+            back = p.get("bsdf2", front)
+            if back != front:
+                raise UnsupportedScene("TwoSides with a different bsdf2 is not provided")
+            b = dict(self.s.bsdfs[front], two_sided=True)
         else:
             raise UnsupportedScene("BSDF type %s is not provided" % kind)
         return self.s.add_bsdf(b)
+
+    def _conductor_ior(self, p):
+        """IORHelper::evalConductorIOR (tools/Common.cpp:56-81): a named
+        material's spectra, else the eta and absorption colors."""
+        mat = p.get("material", "")
+        if mat:
+            if mat not in self.materials:
+                raise UnsupportedScene("conductor material %r needs its eta/k: pass materials={%r: (eta, k)}"
+                                       % (mat, mat))
+            return self.materials[mat]
+        return p.get("eta", (0.0, 0.0, 0.0)), p.get("absorption", (0.0, 0.0, 0.0))
 
     def phase(self, p):
         ph = p.get("phaseFunction")
@@ -423,6 +452,7 @@ class _Loader:
                     self.shape(c)
             elif key == "bsdf":
                 self.ref_bsdf[el.get("id")] = self.bsdf(el)
+                self.ref_bsdf_name[el.get("id")] = el.get("name") or ""
             elif key == "transform":
                 self.ref_transform[el.get("id")] = _transform(el)
         if self.camera_params is None:

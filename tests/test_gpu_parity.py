@@ -131,6 +131,15 @@ BSDFS = [
     D.bsdf(D.BSDF_LAYERED, distribution=D.DIST_GGX, alpha=0.05, eta=scenes.AU_ETA, k=scenes.AU_K,
            distribution_base=D.DIST_GGX, alpha_base=0.25, thickness=0.5, absorbance=(0.1, 0.2, 0.3)),
     D.bsdf(D.BSDF_LAYERED, eta=(1.1, 0.9, 0.7), k=(3.0, 2.5, 2.0)),   # reference defaults: ggx 0.01 over beckmann 0.2
+    D.bsdf(D.BSDF_DIELECTRIC, eta_int=1.5, transmittance=(0.9, 0.95, 1.0)),
+    D.bsdf(D.BSDF_DIELECTRIC, eta_int=1.33, eta_ext=1.1, reflectance=(0.8, 0.9, 1.0)),
+    D.bsdf(D.BSDF_CONDUCTOR, eta=scenes.AU_ETA, k=scenes.AU_K, reflectance=(1.0, 0.9, 0.8)),
+    D.bsdf(D.BSDF_MIRROR),
+    D.bsdf(D.BSDF_DIFFUSE, albedo=(0.2, 0.5, 0.8), two_sided=True),
+    D.bsdf(D.BSDF_ROUGH_CONDUCTOR, distribution=D.DIST_GGX, alpha=0.15, eta=scenes.AU_ETA, k=scenes.AU_K,
+           two_sided=True),
+    D.bsdf(D.BSDF_DIELECTRIC, eta_int=1.5, two_sided=True),
+    D.bsdf(D.BSDF_LAYERED, eta=(1.1, 0.9, 0.7), k=(3.0, 2.5, 2.0), two_sided=True),
 ]
 
 
@@ -357,6 +366,23 @@ def test_film_parity_layered(ctx, rtlib):
     for m in s.meshes[-3:-1]:
         m["bsdf"] = ly
     _film_parity(ctx, rtlib, s, 4, 23, max_bad=0.03)
+
+
+def test_film_parity_smooth_bsdfs(ctx, rtlib, width):
+    """Dielectric, Conductor and Mirror (one shared shading queue) and
+    TwoSides-wrapped Diffuse and RoughConductor panels, PathTracingMIS."""
+    _film_parity(ctx, rtlib, scenes.cornell_smooth(48, 40), 4, 29, max_bad=0.03)
+
+
+def test_film_parity_smooth_bsdfs_volpath(ctx, rtlib):
+    """The same room under VolPathTracing, with a homogeneous medium inside
+    the glass box."""
+    s = scenes.cornell_smooth(40, 32)
+    m = s.add_medium(dict(type=D.MEDIUM_HOMOGENEOUS, phase=D.PHASE_ISOTROPIC, sigma_a=(0.5, 1.0, 2.0),
+                          sigma_s=(1.0, 1.0, 1.0), scale=2.0))
+    s.meshes[4]["interior"] = m
+    s.integrator = dict(s.integrator, integrator=D.INTEGRATOR_VOLPATH)
+    _film_parity(ctx, rtlib, s, 4, 37, max_bad=0.05)
 
 
 def test_film_parity_mixed_normals(ctx, rtlib):

@@ -258,3 +258,43 @@ def test_xml_unsupported_and_quirks(built, tmp_path):
     with pytest.warns(UserWarning):
         t = load_scene(str(tmp_path / "c.xml"))
     assert tuple(t.bsdfs[0]["albedo"]) == (0.0, 0.0, 0.0)
+
+
+def test_xml_roundtrip_smooth_bsdfs(built, tmp_path):
+    """Dielectric, Conductor, Mirror and TwoSides-wrapped Diffuse and
+    RoughConductor survive the file round trip, film for film."""
+    s = scenes.cornell_smooth(16, 12)
+    t = load_scene(write_scene(s, str(tmp_path)))
+    _same_scene(s, t)
+    kinds = {b["type"] for b in t.bsdfs}
+    assert {D.BSDF_DIELECTRIC, D.BSDF_CONDUCTOR, D.BSDF_MIRROR} <= kinds
+    assert any(b.get("two_sided") for b in t.bsdfs)
+    fa, fb = _films_equal(s, t)
+    assert np.array_equal(fa, fb)
+
+
+def test_xml_two_sides_forms(built, tmp_path):
+    """TwoSides over a nested or referenced BSDF (a referenced BSDF keeps the
+    name of its top-level element, XMLLoader.cpp:762-775); a different bsdf2
+    is not provided."""
+    s = scenes.cornell_box(8, 8)
+    text = open(write_scene(s, str(tmp_path))).read()
+    first = text.index('<bsdf type="Diffuse">')
+    end = text.index("</bsdf>", first) + len("</bsdf>")
+    inner = text[first:end]
+    nested = '<bsdf type="TwoSides">' + inner.replace('<bsdf type=', '<bsdf name="bsdf" type=') + "</bsdf>"
+    open(tmp_path / "n.xml", "w").write(text[:first] + nested + text[end:])
+    t = load_scene(str(tmp_path / "n.xml"))
+    b = t.bsdfs[t.meshes[0]["bsdf"]]
+    assert b["two_sided"] and b["type"] == D.BSDF_DIFFUSE and np.allclose(b["albedo"], s.bsdfs[0]["albedo"])
+    top = inner.replace('<bsdf type=', '<bsdf id="wall" name="bsdf" type=')
+    ref = '<bsdf type="TwoSides"><bsdf ref="wall"/></bsdf>'
+    body = text[:first] + ref + text[end:]
+    body = body.replace("<objects>", top + "\n<objects>", 1)
+    open(tmp_path / "r.xml", "w").write(body)
+    t = load_scene(str(tmp_path / "r.xml"))
+    assert t.bsdfs[t.meshes[0]["bsdf"]]["two_sided"]
+    two = nested.replace("</bsdf></bsdf>", '</bsdf><bsdf name="bsdf2" type="Mirror"/></bsdf>')
+    open(tmp_path / "m.xml", "w").write(text[:first] + two + text[end:])
+    with pytest.raises(UnsupportedScene):
+        load_scene(str(tmp_path / "m.xml"))

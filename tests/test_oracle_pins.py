@@ -144,6 +144,84 @@ def test_fresnel_normal_incidence_of_smooth_coat():
     assert r["sampled_type"][1] == 0                                              # through the coat
 
 
+def test_smooth_dielectric_fresnel_and_snell():
+    """Dielectric.cpp:28-82: reflect with probability Fr, else refract by
+    Snell's law with weight transmittance * eta^2; total internal reflection
+    from inside past the critical angle."""
+    n = 1.5
+    b = D.bsdf(D.BSDF_DIELECTRIC, eta_int=n, eta_ext=1.0, transmittance=(0.9, 0.8, 0.7), reflectance=(0.5, 0.6, 0.7))
+    fr = ((n - 1.0) / (n + 1.0)) ** 2
+    up = np.array([[0, 0, 1]] * 2, np.float32)
+    r = O.bsdf_query(b, D.BSDF_OP_SAMPLE, _q(up, u=np.array([[fr * 0.99, 0.5], [fr * 1.01, 0.5]], np.float32)))
+    assert r["sampled_type"][0] == 2 and np.isclose(r["pdf"][0], fr, rtol=1e-5)
+    assert np.allclose(r["value"][0], [0.5, 0.6, 0.7]) and np.allclose(r["wo"][0], [0, 0, 1])
+    assert r["sampled_type"][1] == 8 and np.isclose(r["pdf"][1], 1 - fr, rtol=1e-5)
+    assert np.allclose(r["value"][1], np.array([0.9, 0.8, 0.7]) / n / n, rtol=1e-6)
+    assert np.allclose(r["wo"][1], [0, 0, -1]) and np.isclose(r["relative_eta"][1], 1 / n)
+    rng = np.random.default_rng(3)
+    wi = _sphere_dirs(4000, rng, upper=False)
+    r = O.bsdf_query(b, D.BSDF_OP_SAMPLE, _q(wi, u=np.full((4000, 2), 0.999, np.float32)))
+    inside = wi[:, 2] <= 0
+    rel = np.where(inside, n, 1 / n)
+    sin_t = rel * np.sqrt(np.maximum(0, 1 - wi[:, 2].astype(np.float64) ** 2))
+    tir = sin_t >= 1
+    assert np.all(r["sampled_type"][tir] == 2) and np.all(r["pdf"][tir] == 1)
+    t = ~tir & (r["sampled_type"] == 8)
+    assert t.sum() > 1000
+    # Snell: tangential components scale by eta_i / eta_t, the side flips
+    assert np.allclose(r["wo"][t, :2], -rel[t, None] * wi[t, :2], rtol=1e-5, atol=1e-6)
+    assert np.all(np.sign(r["wo"][t, 2]) == -np.sign(wi[t, 2]))
+    assert np.allclose(np.linalg.norm(r["wo"][t], axis=1), 1, atol=1e-5)
+    for op in (D.BSDF_OP_EVAL, D.BSDF_OP_PDF):
+        e = O.bsdf_query(b, op, _q(wi, -wi))
+        assert not np.any(e["value"]) and not np.any(e["pdf"])
+
+
+def test_smooth_conductor_and_mirror():
+    """Conductor.cpp:39-53 (reflectance * per-channel Fresnel), Mirror.cpp:31-43."""
+    rng = np.random.default_rng(4)
+    wi = _sphere_dirs(1000, rng, upper=False)
+    eta, k = np.array(scenes.AU_ETA), np.array(scenes.AU_K)
+    c = D.bsdf(D.BSDF_CONDUCTOR, eta=tuple(eta), k=tuple(k), reflectance=(0.9, 1.0, 0.8))
+    r = O.bsdf_query(c, D.BSDF_OP_SAMPLE, _q(wi, u=rng.random((1000, 2))))
+    up = wi[:, 2] > 0
+    ci = wi[up, 2:3].astype(np.float64)
+    epa = eta * eta + k * k
+    rpar = (epa * ci * ci - 2 * eta * ci + 1) / (epa * ci * ci + 2 * eta * ci + 1)
+    rperp = (epa - 2 * eta * ci + ci * ci) / (epa + 2 * eta * ci + ci * ci)
+    assert np.allclose(r["value"][up], np.array([0.9, 1.0, 0.8]) * (rpar ** 2 + rperp ** 2) / 2, rtol=1e-5)
+    assert np.all(r["value"][~up] == 0)
+    assert np.allclose(r["wo"][up], wi[up] * [-1, -1, 1]) and np.all(r["pdf"][up] == 1)
+    m = O.bsdf_query(D.bsdf(D.BSDF_MIRROR), D.BSDF_OP_SAMPLE, _q(wi, u=rng.random((1000, 2))))
+    assert np.all(m["value"][up] == 1) and np.all(m["value"][~up] == 0)
+    assert np.all(m["sampled_type"][up] == 2)
+
+
+@pytest.mark.parametrize("kind", [D.BSDF_DIFFUSE, D.BSDF_ROUGH_CONDUCTOR, D.BSDF_CONDUCTOR, D.BSDF_DIELECTRIC])
+def test_two_sides_mirrors_the_lower_side(kind):
+    """TwoSides.cpp:22-70: from below, the wrapped BSDF sees both directions
+    with z negated, and a sampled direction comes back with z negated."""
+    rng = np.random.default_rng(5 + kind)
+    one = D.bsdf(kind, eta=scenes.AU_ETA, k=scenes.AU_K, distribution=D.DIST_GGX, alpha=0.3)
+    two = dict(one, two_sided=True)
+    wi = _sphere_dirs(3000, rng, upper=True)
+    wo = _sphere_dirs(3000, rng, upper=False)
+    u = rng.random((3000, 2)).astype(np.float32)
+    flip = np.array([1, 1, -1], np.float32)
+    for op, f in ((D.BSDF_OP_EVAL, "value"), (D.BSDF_OP_PDF, "pdf")):
+        a = O.bsdf_query(two, op, _q(wi * flip, wo * flip, u))   # wi below
+        b = O.bsdf_query(one, op, _q(wi, wo, u))
+        assert np.array_equal(a[f], b[f])
+    below = wi * flip
+    a = O.bsdf_query(two, D.BSDF_OP_SAMPLE, _q(below, u=u))
+    b = O.bsdf_query(one, D.BSDF_OP_SAMPLE, _q(wi, u=u))
+    assert np.array_equal(a["value"], b["value"]) and np.array_equal(a["pdf"], b["pdf"])
+    assert np.array_equal(a["wo"], b["wo"] * flip)
+    # from above it is the wrapped BSDF itself
+    c = O.bsdf_query(two, D.BSDF_OP_SAMPLE, _q(wi, u=u))
+    assert np.array_equal(c["value"], b["value"]) and np.array_equal(c["wo"], b["wo"])
+
+
 def test_triangle_hit_exactness_small_scene():
     s = scenes.cornell_box(16, 16)
     o = O.OracleScene(s)
