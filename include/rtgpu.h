@@ -342,6 +342,44 @@ rt_status rt_ctx_set_wave_paths(rt_ctx *ctx, int32_t paths);
 /* Regroup the rays of every bounce after the first by direction octant and
  * origin cell before tracing them (0 off, 1 on); results are unchanged. */
 rt_status rt_ctx_set_ray_sort(rt_ctx *ctx, int32_t on);
+/* Launch each PathTracingMIS wavefront batch of later renders as one CUDA
+ * graph (0 off, 1 on): camera rays, the bounce rounds as a device-controlled
+ * conditional loop (it stops when no path is left, with no host round trip)
+ * and the film reduction.  Graphs are kept and reused for renders with
+ * identical parameters.  Renders with profiling or ray sorting on launch
+ * kernel by kernel.  Results are identical either way. */
+rt_status rt_ctx_set_graphs(rt_ctx *ctx, int32_t on);
+
+/* Launch shapes, queue capacities and scheduling choices of later renders.
+ * None of them changes a result: a film is the same bit for bit under any
+ * tuning.  (The tile size, blockSizeX/Y of the scene file, is not among
+ * them: it decides which neighbours a sample on a pixel edge reaches.) */
+typedef struct rt_tuning {
+    int32_t wave_paths;          /* paths per wavefront batch of this context's
+                                    renders (queue capacity), 2^16..2^26     */
+    int32_t lane_wave_paths;     /* the same for each lane of rt_batch_render
+                                    and of servers started from the context   */
+    int32_t trace_blocks_per_sm; /* traversal grid: 128-thread blocks per SM,
+                                    1..64                                      */
+    int32_t shade_blocks_per_sm; /* finish and shading grid, 1..64            */
+    int32_t sort_threshold;      /* bounces with fewer closest-hit rays than
+                                    this shade in one unsorted queue instead
+                                    of per-material queues (0: always sorted) */
+    int32_t lanes;               /* worker lanes of rt_batch_render, 1..16    */
+    int32_t graphs;              /* one CUDA graph per batch, 0 or 1          */
+} rt_tuning;
+rt_status rt_ctx_get_tuning(rt_ctx *ctx, rt_tuning *out);
+rt_status rt_ctx_set_tuning(rt_ctx *ctx, const rt_tuning *t);
+
+/* Autotuner.  Searches rt_tuning for the fastest rt_batch_render of the
+ * given jobs (a representative sample of a workload, e.g. a few of its jobs
+ * at reduced spp) by coordinate descent over a fixed candidate grid, with at
+ * most max_trials timed trials (each one untimed warm-up and the best of two
+ * timed runs).  The jobs render into scratch device films.  The best tuning
+ * is left set on the context and returned with its measured path samples
+ * per second (samples_per_s may be null). */
+rt_status rt_autotune(rt_ctx *ctx, rt_scene *const *scenes, const rt_render_desc *descs, int32_t n,
+                      int32_t max_trials, rt_tuning *best, double *samples_per_s);
 
 /* Allocation-free tile render.  No counterpart in the reference: it exists
  * for callers that cannot allocate device memory while rendering (plugins

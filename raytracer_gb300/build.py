@@ -22,7 +22,7 @@ ARCH = os.environ.get("RTGPU_ARCH", "-gencode=arch=compute_103a,code=sm_103a")
 NVCC = os.environ.get("NVCC", "nvcc")
 
 CUDA_SOURCES = ["rt_api.cu"]
-HOST_SOURCES = ["rt_bvh.cpp", "rt_serve.cpp", "rt_io.cpp"]
+HOST_SOURCES = ["rt_bvh.cpp", "rt_serve.cpp", "rt_io.cpp", "rt_tune.cpp"]
 HEADERS = ["rt_math.cuh", "rt_device.cuh", "rt_kernels.cuh", "rt_bvh.h", "rt_internal.h"]
 
 

@@ -34,6 +34,16 @@ class JobInfo(C.Structure):
 JOB_QUEUED, JOB_RUNNING, JOB_DONE, JOB_FAILED = 0, 1, 2, 3
 
 
+class Tuning(C.Structure):
+    """rt_tuning: launch shapes, queue capacities and scheduling choices."""
+    _fields_ = [("wave_paths", C.c_int32), ("lane_wave_paths", C.c_int32), ("trace_blocks_per_sm", C.c_int32),
+                ("shade_blocks_per_sm", C.c_int32), ("sort_threshold", C.c_int32), ("lanes", C.c_int32),
+                ("graphs", C.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class MeshData(C.Structure):
     _fields_ = [("n_vertices", C.c_int32), ("vertices", C.POINTER(C.c_float)), ("normals", C.POINTER(C.c_float)),
                 ("uvs", C.POINTER(C.c_float)), ("n_triangles", C.c_int32), ("indices", C.POINTER(C.c_int32))]
@@ -73,6 +83,11 @@ def lib():
     L.rt_ctx_set_bvh_width.argtypes = [vp, C.c_int32]
     L.rt_ctx_set_wave_paths.argtypes = [vp, C.c_int32]
     L.rt_ctx_set_ray_sort.argtypes = [vp, C.c_int32]
+    L.rt_ctx_set_graphs.argtypes = [vp, C.c_int32]
+    L.rt_ctx_get_tuning.argtypes = [vp, C.POINTER(Tuning)]
+    L.rt_ctx_set_tuning.argtypes = [vp, C.POINTER(Tuning)]
+    L.rt_autotune.argtypes = [vp, C.POINTER(C.c_void_p), C.POINTER(D.RenderDesc), C.c_int32, C.c_int32,
+                              C.POINTER(Tuning), C.POINTER(C.c_double)]
     L.rt_trace.argtypes = [vp, vp, vp, C.c_int32, C.c_int32, vp, C.c_int32]
     L.rt_render_tile_static.argtypes = [vp, vp, C.POINTER(D.RenderDesc), C.c_int32, C.c_int32, vp]
     L.rt_render_tile_static.restype = C.c_int32
@@ -95,7 +110,8 @@ def lib():
     L.rt_host_free.argtypes = [vp]
     L.rt_host_free.restype = None
     for name in ("rt_ctx_create", "rt_ctx_destroy", "rt_ctx_set_stream", "rt_scene_create", "rt_scene_destroy",
-                 "rt_scene_info", "rt_render", "rt_render_stats_get", "rt_ctx_set_profiling", "rt_ctx_set_bvh_width", "rt_ctx_set_wave_paths", "rt_ctx_set_ray_sort",
+                 "rt_scene_info", "rt_render", "rt_render_stats_get", "rt_ctx_set_profiling", "rt_ctx_set_bvh_width", "rt_ctx_set_wave_paths", "rt_ctx_set_ray_sort", "rt_ctx_set_graphs",
+                 "rt_ctx_get_tuning", "rt_ctx_set_tuning", "rt_autotune",
                  "rt_trace", "rt_bsdf_query", "rt_light_query", "rt_medium_query", "rt_batch_render", "rt_ctx_set_lanes",
                  "rt_server_start", "rt_job_submit", "rt_job_poll", "rt_job_wait", "rt_server_stop"):
         getattr(L, name).restype = C.c_int32
@@ -150,9 +166,26 @@ class Context:
         """Regroup secondary and shadow rays by octant and origin cell before tracing."""
         _check(lib().rt_ctx_set_ray_sort(self.h, int(bool(on))))
 
+    def set_graphs(self, on):
+        """Launch each PathTracingMIS batch of later renders as one CUDA graph
+        with a device-controlled bounce loop (results are identical)."""
+        _check(lib().rt_ctx_set_graphs(self.h, int(bool(on))))
+
     def set_lanes(self, lanes):
         """Concurrent worker lanes of batch_render (1..16, default 4)."""
         _check(lib().rt_ctx_set_lanes(self.h, int(lanes)))
+
+    @staticmethod
+    def _jobs(jobs):
+        n = len(jobs)
+        scenes = (C.c_void_p * n)()
+        descs = (D.RenderDesc * n)()
+        for i, (sc, spp, opt) in enumerate(jobs):
+            opt = dict(opt)
+            seed, sb, block = opt.pop("seed", 0), opt.pop("sample_begin", 0), opt.pop("block", 32)
+            descs[i] = sc.data.render_desc(spp, seed=seed, sample_begin=sb, block=block, **opt)
+            scenes[i] = sc.h
+        return scenes, descs
 
     def batch_render(self, jobs):
         """Render independent jobs in one call (rt_batch_render).  `jobs` is
@@ -160,20 +193,40 @@ class Context:
         (seed, sample_begin, block, max_depth, ...); returns the list of
         (H, W, 4) host films, each equal to that job's Scene.render film."""
         n = len(jobs)
-        scenes = (C.c_void_p * n)()
-        descs = (D.RenderDesc * n)()
+        scenes, descs = self._jobs(jobs)
         films = []
         fptr = (C.c_void_p * n)()
-        for i, (sc, spp, opt) in enumerate(jobs):
-            opt = dict(opt)
-            seed, sb, block = opt.pop("seed", 0), opt.pop("sample_begin", 0), opt.pop("block", 32)
-            descs[i] = sc.data.render_desc(spp, seed=seed, sample_begin=sb, block=block, **opt)
-            scenes[i] = sc.h
+        for i, (sc, _, _) in enumerate(jobs):
             f = np.zeros((sc.height, sc.width, 4), np.float32)
             films.append(f)
             fptr[i] = f.ctypes.data
         _check(lib().rt_batch_render(self.h, scenes, descs, n, fptr, 0))
         return films
+
+    def get_tuning(self):
+        t = Tuning()
+        _check(lib().rt_ctx_get_tuning(self.h, C.byref(t)))
+        return t.as_dict()
+
+    def set_tuning(self, **fields):
+        """Change some rt_tuning fields (the others keep their values)."""
+        t = Tuning()
+        _check(lib().rt_ctx_get_tuning(self.h, C.byref(t)))
+        for k, v in fields.items():
+            if k not in t.as_dict():
+                raise KeyError(k)
+            setattr(t, k, int(v))
+        _check(lib().rt_ctx_set_tuning(self.h, C.byref(t)))
+
+    def autotune(self, jobs, max_trials=32):
+        """Run the autotuner (rt_autotune) on a sample of jobs, as for
+        batch_render; the best tuning stays set.  Returns (tuning dict,
+        path samples per second of the sample under it)."""
+        scenes, descs = self._jobs(jobs)
+        t = Tuning()
+        sps = C.c_double()
+        _check(lib().rt_autotune(self.h, scenes, descs, len(jobs), int(max_trials), C.byref(t), C.byref(sps)))
+        return t.as_dict(), sps.value
 
     def stats(self):
         s = D.RenderStats()
@@ -375,7 +428,10 @@ def load_hdr(path):
 
 
 def post_process(film):
-    """Screen::postProcessColor (core/Screen.cpp:113-122): colour / weight."""
+    """Screen::postProcessColor (core/Screen.cpp:8-18,113-122): colour /
+    weight wherever the weight is not zero (a Mitchell-Netravali sum can be
+    negative), the colour as it is elsewhere."""
+    film = np.asarray(film, np.float32)
     w = film[..., 3:4]
     with np.errstate(invalid="ignore", divide="ignore"):
-        return np.where(w > 0, film[..., :3] / w, 0.0).astype(np.float32)
+        return np.where(w != 0, film[..., :3] / np.where(w != 0, w, 1), film[..., :3]).astype(np.float32)

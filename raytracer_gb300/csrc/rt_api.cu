@@ -101,7 +101,19 @@ struct RenderParams {
     int max_depth, min_depth;
     int *limit_flag;
     unsigned long long *stats;  // [0] closest rays, [1] shadow rays, [2] nan samples
+    // graph-launched rounds: the round index lives in device memory (the
+    // round loop is a conditional node; k_round_next advances it); null when
+    // the host passes the round as a kernel argument
+    int *round_dev;
+    // rounds with fewer closest-hit rays than this are not sorted by
+    // material: their hits go to one queue shaded by k_pt_shade<RT_QUEUE_MIXED>
+    int sort_threshold;
 };
+
+__device__ __forceinline__ int cur_round(const RenderParams &P, int round)
+{
+    return P.round_dev ? __ldcg(P.round_dev) : round;
+}
 
 // ---------------------------------------------------------------- camera
 __global__ void k_camera(RenderParams P)
@@ -140,11 +152,17 @@ __global__ void k_camera(RenderParams P)
 // Sort a traced path by what its ray hit: the shading queue of the hit
 // surface's BSDF type, or the finish queue for a miss or a surface without a
 // BSDF.  Called by the lanes that just finished a closest-hit ray.
-__device__ __forceinline__ void classify_hit(const RenderParams &P, RoundCounters *C, int slot, int prim)
+// `n` is the round's closest-hit ray count: below P.sort_threshold the hits
+// are not sorted by material (one queue, one generic shading kernel).
+__device__ __forceinline__ void classify_hit(const RenderParams &P, RoundCounters *C, int slot, int prim, int n)
 {
     const int t = prim == -1 ? -1 : prim_type(P.S, prim);
+    if (n < P.sort_threshold) {
+        q_push(P.W.q_mixed, &C->mixed, slot, t >= 0);
+    } else {
 #pragma unroll
-    for (int k = 0; k < RT_NBSDF; k++) q_push(P.W.q_mat[k], &C->mat[k], slot, t == k);
+        for (int k = 0; k < RT_NBSDF; k++) q_push(P.W.q_mat[k], &C->mat[k], slot, t == k);
+    }
     q_push(P.W.q_fin, &C->fin, slot, t < 0);
 }
 
@@ -255,6 +273,7 @@ __global__ void k_sort_copy(RenderParams P, int round, int shadow)
 template <bool ANY, bool COUNT>
 __global__ void __launch_bounds__(128, RT_TRACE_MINB) k_trace(RenderParams P, int round)
 {
+    round = cur_round(P, round);
     const DevScene S = P.S;
     RoundCounters *C = &P.W.cnt[round];
     const int n = ANY ? C->shadow : C->closest;
@@ -377,7 +396,7 @@ __global__ void __launch_bounds__(128, RT_TRACE_MINB) k_trace(RenderParams P, in
             if (ANY) P.W.occl[slot] = hprim != -1 ? 1 : 0;
             else {
                 P.W.hit[slot] = make_float4(hit_t, hu, hv, __int_as_float(hprim));
-                classify_hit(P, C, slot, hprim);
+                classify_hit(P, C, slot, hprim, n);
             }
             has_ray = false;
         }
@@ -423,6 +442,7 @@ __device__ __forceinline__ unsigned meta_byte(int4 w1, unsigned slot)
 template <bool ANY, bool COUNT>
 __global__ void __launch_bounds__(128, 8) k_trace8(RenderParams P, int round)
 {
+    round = cur_round(P, round);
     const DevScene S = P.S;
     RoundCounters *C = &P.W.cnt[round];
     const int n = ANY ? C->shadow : C->closest;
@@ -581,7 +601,7 @@ __global__ void __launch_bounds__(128, 8) k_trace8(RenderParams P, int round)
             if (ANY) P.W.occl[slot] = hprim != -1 ? 1 : 0;
             else {
                 P.W.hit[slot] = make_float4(hit_t, hu, hv, __int_as_float(hprim));
-                classify_hit(P, C, slot, hprim);
+                classify_hit(P, C, slot, hprim, n);
             }
             has_ray = false;
         }
@@ -651,6 +671,7 @@ __global__ void k_hits_out(RenderParams P, int n, int anyhit, rt_hit *hits)
 //                     emitting the shadow ray and the next closest-hit ray.
 __global__ void __launch_bounds__(128) k_pt_finish(RenderParams P, int round)
 {
+    round = cur_round(P, round);
     const DevScene &S = P.S;
     RoundCounters *C = &P.W.cnt[round];
     const int nf = C->fin, n = nf + C->end;
@@ -702,10 +723,12 @@ __global__ void __launch_bounds__(128) k_pt_finish(RenderParams P, int round)
 
 // The BSDF functions of one shading queue (bsdf_queue), with the TwoSides
 // mirroring of bsdf_eval/bsdf_pdf/bsdf_sample.  Queue RT_QUEUE_DELTA holds
-// the smooth BSDFs, whose eval and pdf are zero.
+// the smooth BSDFs, whose eval and pdf are zero; RT_QUEUE_MIXED holds every
+// type and dispatches at run time.
 template <int BT>
 __device__ __forceinline__ C3 bsdf_eval_t(const DevBsdf &b, V3 wi, V3 wo)
 {
+    if (BT == RT_QUEUE_MIXED) return bsdf_eval(b, wi, wo);
     if (BT == RT_QUEUE_DELTA) return cfill(0.f);
     if (b.two_sided && !(wi.z > 0.f)) { wi.z = -wi.z; wo.z = -wo.z; }
     if (BT == 0) return diffuse_eval(b.albedo, wi, wo);
@@ -717,6 +740,7 @@ __device__ __forceinline__ C3 bsdf_eval_t(const DevBsdf &b, V3 wi, V3 wo)
 template <int BT>
 __device__ __forceinline__ float bsdf_pdf_t(const DevBsdf &b, V3 wi, V3 wo)
 {
+    if (BT == RT_QUEUE_MIXED) return bsdf_pdf(b, wi, wo);
     if (BT == RT_QUEUE_DELTA) return 0.f;
     if (b.two_sided && !(wi.z > 0.f)) { wi.z = -wi.z; wo.z = -wo.z; }
     if (BT == 0) return diffuse_pdf(wi, wo);
@@ -740,6 +764,7 @@ __device__ __forceinline__ C3 bsdf_sample1_t(const DevBsdf &b, BsdfRec &r, V2 s,
 template <int BT>
 __device__ __forceinline__ C3 bsdf_sample_t(const DevBsdf &b, BsdfRec &r, V2 s, uint64_t aux_key)
 {
+    if (BT == RT_QUEUE_MIXED) return bsdf_sample(b, r, s, aux_key);
     if (b.two_sided && !(r.wi.z > 0.f)) {
         r.wi.z = -r.wi.z;
         C3 res = bsdf_sample1_t<BT>(b, r, s, aux_key);
@@ -759,11 +784,12 @@ __device__ __forceinline__ C3 bsdf_sample_t(const DevBsdf &b, BsdfRec &r, V2 s, 
 template <int BT>
 __global__ void __launch_bounds__(128, RT_SHADE_MINB) k_pt_shade(RenderParams P, int round)
 {
+    round = cur_round(P, round);
     const DevScene &S = P.S;
     RoundCounters *C = &P.W.cnt[round];
     RoundCounters *Cout = &P.W.cnt[round + 1];
-    const int n = C->mat[BT];
-    const int *qin = P.W.q_mat[BT];
+    const int n = BT == RT_QUEUE_MIXED ? C->mixed : C->mat[BT];
+    const int *qin = BT == RT_QUEUE_MIXED ? P.W.q_mixed : P.W.q_mat[BT];
     int idx = blockIdx.x * blockDim.x + threadIdx.x;
     int stride = gridDim.x * blockDim.x;
     int iters = (n + stride - 1) / stride;
@@ -889,6 +915,20 @@ __global__ void __launch_bounds__(128, RT_SHADE_MINB) k_pt_shade(RenderParams P,
         q_push(P.W.q_closest, &Cout->closest, slot, push_closest);
         q_push(P.W.q_shadow, &Cout->shadow, slot, push_shadow);
     }
+}
+
+// End of one graph-launched round: continue the round loop (the
+// conditional node's body) while the next round has paths to trace or to
+// finish, at most up to round max_rounds - 1, as the host-driven loop does.
+// The loop ends after at most max_rounds bodies whatever the counters say.
+__global__ void k_round_next(RenderParams P, cudaGraphConditionalHandle loop, int max_rounds)
+{
+    const int r = __ldcg(P.round_dev);
+    const RoundCounters &nc = P.W.cnt[r + 1];
+    const bool more = r + 1 < max_rounds && (__ldcg(&nc.closest) != 0 || __ldcg(&nc.end) != 0);
+    if (more) P.round_dev[0] = r + 1;
+    P.stats[7] += 1;   // rounds run, for the launch count
+    cudaGraphSetConditional(loop, more ? 1u : 0u);
 }
 
 // ---------------------------------------------------------------- VolPathTracing
@@ -1425,13 +1465,38 @@ struct rt_ctx {
     int bvh_width = 2;          // traversal used by renders and rt_trace: 2 or 8
     int wave_paths = 1 << 26;   // target paths per wavefront batch (about 14 GB of path state)
     int ray_sort = 0;           // reorder secondary and shadow rays before tracing
+    // launch shapes and the material-sort threshold (rt_ctx_set_tuning)
+    int trace_bpsm = 12;        // traversal kernels: blocks per SM
+    int shade_bpsm = RT_SHADE_GRID;   // finish and shading kernels: blocks per SM
+    int sort_threshold = 0;     // rounds with fewer closest-hit rays shade unsorted
     std::vector<cudaEvent_t> ev_pool;
     std::vector<int> ev_kind;   // kernel kind per recorded pair
     size_t ev_used = 0;
     int tile_key[4] = {-1, -1, -1, -1};
     std::vector<int> tile_start;
     rt_lane_pool *pool = nullptr;   // worker lanes of rt_batch_render (rt_serve.cpp)
+    // CUDA-graph batches (rt_ctx_set_graphs): instantiated graphs keyed by
+    // the exact bytes of their launch parameters, newest last
+    int graphs = 0;
+    int *round_dev = nullptr;
+    // graphs are captured on two streams of the context's own (the caller's
+    // stream may be the legacy default stream, which cannot capture) and
+    // launched on the context's stream
+    cudaStream_t cap_stream = nullptr;    // captures the batch
+    cudaStream_t body_stream = nullptr;   // captures the round loop's body
+    struct GraphEntry {
+        std::vector<unsigned char> key;
+        cudaGraphExec_t exec;
+    };
+    std::vector<GraphEntry> gcache;
+    int64_t graph_builds = 0, graph_hits = 0;
 };
+
+static void graph_cache_clear(rt_ctx *c)
+{
+    for (auto &e : c->gcache) cudaGraphExecDestroy(e.exec);
+    c->gcache.clear();
+}
 
 // kinds for per-kernel timing
 enum { K_CAMERA = 0, K_TRACE_C = 1, K_TRACE_A = 2, K_SHADE = 3, K_VOLPATH = 4, K_FILM = 5, K_RESOLVE = 6, K_SORT = 7,
@@ -1671,6 +1736,7 @@ rt_status rt_ctx_create(int32_t device, rt_ctx **out)
 
 static void free_wave(rt_ctx *c)
 {
+    graph_cache_clear(c);   // the graphs hold the freed buffers' addresses
     for (void *p : c->wave_allocs) cudaFree(p);
     c->wave_allocs.clear();
     c->capacity = 0;
@@ -1683,6 +1749,9 @@ rt_status rt_ctx_destroy(rt_ctx *c)
     c->pool = nullptr;
     cudaSetDevice(c->device);
     free_wave(c);
+    cudaFree(c->round_dev);
+    if (c->body_stream) cudaStreamDestroy(c->body_stream);
+    if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
     cudaFree(c->tileorder);
     cudaFree(c->work);
     cudaFree(c->limit_flag);
@@ -1725,6 +1794,17 @@ rt_status rt_ctx_set_ray_sort(rt_ctx *c, int32_t on)
 {
     if (!c) return fail(RT_ERR_INVALID, "null ctx");
     c->ray_sort = on ? 1 : 0;
+    return RT_OK;
+}
+
+rt_status rt_ctx_set_graphs(rt_ctx *c, int32_t on)
+{
+    if (!c) return fail(RT_ERR_INVALID, "null ctx");
+    c->graphs = on ? 1 : 0;
+    if (!c->graphs) {
+        cudaSetDevice(c->device);
+        graph_cache_clear(c);
+    }
     return RT_OK;
 }
 
@@ -2119,6 +2199,7 @@ static rt_status ensure_wave(rt_ctx *c, int capacity, int max_rounds)
     ok &= alloc((void **)&W.q_closest, P * sizeof(int));
     ok &= alloc((void **)&W.q_shadow, P * sizeof(int));
     for (int t = 0; t < RT_NBSDF; t++) ok &= alloc((void **)&W.q_mat[t], P * sizeof(int));
+    ok &= alloc((void **)&W.q_mixed, P * sizeof(int));
     ok &= alloc((void **)&W.cnt, (size_t)(max_rounds + 2) * sizeof(RoundCounters));
     ok &= alloc((void **)&W.sort_keys, P * sizeof(unsigned));
     ok &= alloc((void **)&W.sort_tmp, P * sizeof(int));
@@ -2149,6 +2230,127 @@ static rt_status launch_check(const char *what)
 {
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(RT_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    return RT_OK;
+}
+
+// One PathTracingMIS wavefront batch as a CUDA graph: reset the batch's
+// counters and the device round index, camera rays, then a conditional WHILE
+// node whose body is one round (closest-hit trace, shadow trace, finish,
+// shading, k_round_next), then the film reduction.  The graph is built once
+// per distinct set of launch parameters and kept; the conditional handle it
+// owns is only ever set by its own k_round_next.
+static rt_status pt_batch_graph(rt_ctx *ctx, rt_scene *sc, const RenderParams &P, float4 *film, bool box_film,
+                                int accumulate, int Wd, int t0, int t1, int tiles_x, int bx, int by, int max_rounds,
+                                int round_buf)
+{
+    cudaStream_t st = ctx->cap_stream;   // capture; the graph runs on ctx->stream
+    const int sm = ctx->sm_count > 0 ? ctx->sm_count : 1;
+    const int cam_blocks = std::min((P.n_paths + 255) / 256, sm * 16);
+    const int trace_blocks = sm * ctx->trace_bpsm, shade_blocks = sm * ctx->shade_bpsm;
+    const bool w8 = ctx->bvh_width == 8 && sc->wide_ok;
+    const int types = sc->bsdf_types | (P.sort_threshold > 0 ? 1 << RT_QUEUE_MIXED : 0);
+    const size_t npix_all = (size_t)Wd * sc->S.cam.height;
+    struct Tail {
+        const void *film;
+        int box, accumulate, wd, t0, t1, tiles_x, bx, by, max_rounds, round_buf, cam_blocks, trace_blocks,
+            shade_blocks, w8, types;
+    } tail;
+    std::memset(&tail, 0, sizeof(tail));
+    tail.film = film; tail.box = box_film; tail.accumulate = accumulate; tail.wd = Wd; tail.t0 = t0; tail.t1 = t1;
+    tail.tiles_x = tiles_x; tail.bx = bx; tail.by = by; tail.max_rounds = max_rounds; tail.round_buf = round_buf;
+    tail.cam_blocks = cam_blocks; tail.trace_blocks = trace_blocks; tail.shade_blocks = shade_blocks;
+    tail.w8 = w8; tail.types = types;
+    std::vector<unsigned char> key(sizeof(RenderParams) + sizeof(Tail));
+    std::memcpy(key.data(), &P, sizeof(RenderParams));
+    std::memcpy(key.data() + sizeof(RenderParams), &tail, sizeof(Tail));
+    cudaGraphExec_t exec = nullptr;
+    for (auto &e : ctx->gcache)
+        if (e.key == key) { exec = e.exec; break; }
+    if (exec) {
+        ctx->graph_hits++;
+    } else {
+        cudaGraph_t g = nullptr;
+        bool body_capturing = false;
+        const char *what = nullptr;
+        auto bad = [&](cudaError_t e, const char *w) {
+            if (e != cudaSuccess && !what) what = w;
+            return e != cudaSuccess;
+        };
+        CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        do {
+            if (bad(cudaMemsetAsync(P.W.pix_irregular, 0, (size_t)P.npix, st), "memset")) break;
+            if (bad(cudaMemsetAsync(P.W.cnt, 0, sizeof(RoundCounters) * (size_t)(round_buf + 2), st), "memset")) break;
+            if (bad(cudaMemsetAsync(P.round_dev, 0, sizeof(int), st), "memset")) break;
+            k_camera<<<cam_blocks, 256, 0, st>>>(P);
+            if (bad(cudaGetLastError(), "k_camera")) break;
+            cudaStreamCaptureStatus cst;
+            cudaGraph_t cg = nullptr;
+            const cudaGraphNode_t *deps = nullptr;
+            size_t nd = 0;
+            if (bad(cudaStreamGetCaptureInfo(st, &cst, nullptr, &cg, &deps, nullptr, &nd), "capture info")) break;
+            cudaGraphConditionalHandle loop;
+            if (bad(cudaGraphConditionalHandleCreate(&loop, cg, 1, cudaGraphCondAssignDefault), "conditional handle"))
+                break;
+            cudaGraphNodeParams cp = {};
+            cp.type = cudaGraphNodeTypeConditional;
+            cp.conditional.handle = loop;
+            cp.conditional.type = cudaGraphCondTypeWhile;
+            cp.conditional.size = 1;
+            cudaGraphNode_t cn;
+            if (bad(cudaGraphAddNode(&cn, cg, deps, nullptr, nd, &cp), "conditional node")) break;
+            cudaGraph_t body = cp.conditional.phGraph_out[0];
+            cudaStream_t bs = ctx->body_stream;
+            if (bad(cudaStreamBeginCaptureToGraph(bs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
+                    "body capture"))
+                break;
+            body_capturing = true;
+            if (w8) {
+                k_trace8<false, false><<<trace_blocks, 128, 0, bs>>>(P, 0);
+                k_trace8<true, false><<<trace_blocks, 128, 0, bs>>>(P, 0);
+            } else {
+                k_trace<false, false><<<trace_blocks, 128, 0, bs>>>(P, 0);
+                k_trace<true, false><<<trace_blocks, 128, 0, bs>>>(P, 0);
+            }
+            k_pt_finish<<<shade_blocks, 128, 0, bs>>>(P, 0);
+            if (types & 1) k_pt_shade<0><<<shade_blocks, 128, 0, bs>>>(P, 0);
+            if (types & 2) k_pt_shade<1><<<shade_blocks, 128, 0, bs>>>(P, 0);
+            if (types & 4) k_pt_shade<2><<<shade_blocks, 128, 0, bs>>>(P, 0);
+            if (types & 8) k_pt_shade<3><<<shade_blocks, 128, 0, bs>>>(P, 0);
+            if (types & 16) k_pt_shade<4><<<shade_blocks, 128, 0, bs>>>(P, 0);
+            if (types & 32) k_pt_shade<5><<<shade_blocks, 128, 0, bs>>>(P, 0);
+            if (types & 64) k_pt_shade<RT_QUEUE_MIXED><<<shade_blocks, 128, 0, bs>>>(P, 0);
+            k_round_next<<<1, 1, 0, bs>>>(P, loop, max_rounds);
+            if (bad(cudaGetLastError(), "round kernels")) break;
+            body_capturing = false;
+            if (bad(cudaStreamEndCapture(bs, &body), "body capture end")) break;
+            if (bad(cudaStreamUpdateCaptureDependencies(st, &cn, nullptr, 1, cudaStreamSetCaptureDependencies),
+                    "capture dependencies"))
+                break;
+            if (box_film) k_film<<<(P.npix + 127) / 128, 128, 0, st>>>(P, film, Wd, accumulate);
+            else k_film_wide<<<(int)((npix_all + 127) / 128), 128, 0, st>>>(P, film, t0, t1, tiles_x, bx, by);
+            if (bad(cudaGetLastError(), "film kernel")) break;
+        } while (0);
+        if (body_capturing) {
+            cudaGraph_t bg = nullptr;
+            cudaStreamEndCapture(ctx->body_stream, &bg);
+        }
+        cudaError_t ee = cudaStreamEndCapture(st, &g);
+        if (!what && ee != cudaSuccess) what = "capture end";
+        if (!what && cudaGraphInstantiate(&exec, g, 0) != cudaSuccess) what = "instantiate";
+        if (g) cudaGraphDestroy(g);
+        if (what) {
+            cudaGetLastError();
+            if (exec) cudaGraphExecDestroy(exec);
+            return fail(RT_ERR_CUDA, std::string("render graph: ") + what + " failed");
+        }
+        if (ctx->gcache.size() >= 8) {
+            cudaGraphExecDestroy(ctx->gcache.front().exec);
+            ctx->gcache.erase(ctx->gcache.begin());
+        }
+        ctx->gcache.push_back({std::move(key), exec});
+        ctx->graph_builds++;
+    }
+    CK(cudaGraphLaunch(exec, ctx->stream));
     return RT_OK;
 }
 
@@ -2249,6 +2451,7 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
     CK(cudaMemsetAsync(ctx->stats, 0, sizeof(unsigned long long) * 8, st));
     CK(cudaMemsetAsync(ctx->limit_flag, 0, sizeof(int), st));
     RenderParams P;
+    std::memset(&P, 0, sizeof(P));
     P.S = sc->S;
     P.S.light_cdf = ctx->light_cdf;
     P.W = ctx->W;
@@ -2260,9 +2463,20 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
     P.stats = ctx->stats;
     P.spp = rd->spp;
     P.sample_begin = rd->sample_begin;
+    P.sort_threshold = ctx->sort_threshold;
     const int sm = ctx->sm_count > 0 ? ctx->sm_count : 1;
     int64_t launches = 0, trace_c_launches = 0, trace_a_launches = 0;
     int64_t total_paths = 0;
+    // one CUDA graph per PathTracingMIS batch (rt_ctx_set_graphs)
+    const bool use_graph = ctx->graphs && !ctx->profiling && !ctx->ray_sort &&
+                           rd->integrator == RT_INTEGRATOR_PATH_MIS;
+    int graph_batches = 0;
+    if (use_graph) {
+        if (!ctx->round_dev) CK(cudaMalloc(&ctx->round_dev, sizeof(int)));
+        if (!ctx->body_stream) CK(cudaStreamCreateWithFlags(&ctx->body_stream, cudaStreamNonBlocking));
+        if (!ctx->cap_stream) CK(cudaStreamCreateWithFlags(&ctx->cap_stream, cudaStreamNonBlocking));
+        P.round_dev = ctx->round_dev;
+    }
     ctx->ev_used = 0;
     CK(cudaEventRecord(ctx->ev0, st));
     for (int t0 = 0; t0 < ntiles; t0 += tiles_per_batch) {
@@ -2271,6 +2485,13 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
         P.npix = tile_start[t1] - tile_start[t0];
         P.n_paths = P.npix * rd->spp;
         total_paths += P.n_paths;
+        if (use_graph) {
+            if ((s = pt_batch_graph(ctx, sc, P, film, box_film, accumulate, Wd, t0, t1, tiles_x, bx, by, max_rounds,
+                                    round_buf)) != RT_OK)
+                return s;
+            graph_batches++;
+            continue;
+        }
         CK(cudaMemsetAsync(ctx->W.pix_irregular, 0, (size_t)P.npix, st));
         CK(cudaMemsetAsync(ctx->W.cnt, 0, sizeof(RoundCounters) * (size_t)(round_buf + 2), st));
         int cam_blocks = std::min((P.n_paths + 255) / 256, sm * 16);
@@ -2287,8 +2508,8 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
             launches++;
             if ((s = launch_check("k_volpath")) != RT_OK) return s;
         } else {
-            int trace_blocks = sm * 12;
-            int shade_blocks = sm * RT_SHADE_GRID;
+            int trace_blocks = sm * ctx->trace_bpsm;
+            int shade_blocks = sm * ctx->shade_bpsm;
             for (int r = 0; r < max_rounds; r++) {
                 int ri = r;
                 const bool cnt2 = ctx->profiling >= 2, w8 = ctx->bvh_width == 8 && sc->wide_ok;
@@ -2326,8 +2547,9 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
                 if (sc->bsdf_types & 8) k_pt_shade<3><<<shade_blocks, 128, 0, st>>>(P, ri);
                 if (sc->bsdf_types & 16) k_pt_shade<4><<<shade_blocks, 128, 0, st>>>(P, ri);
                 if (sc->bsdf_types & 32) k_pt_shade<5><<<shade_blocks, 128, 0, st>>>(P, ri);
+                if (P.sort_threshold > 0) k_pt_shade<RT_QUEUE_MIXED><<<shade_blocks, 128, 0, st>>>(P, ri);
                 prof_end(ctx);
-                launches += 3 + __builtin_popcount(sc->bsdf_types);
+                launches += 3 + __builtin_popcount(sc->bsdf_types) + (P.sort_threshold > 0);
                 trace_c_launches++;
                 trace_a_launches++;
                 if ((s = launch_check("pt round")) != RT_OK) return s;
@@ -2387,6 +2609,14 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
     ctx->last.closest_rays = (int64_t)stats[0];
     ctx->last.shadow_rays = (int64_t)stats[1];
     ctx->last.nan_samples = (int64_t)stats[2];
+    if (graph_batches) {
+        // camera and film per batch, the rounds' kernels and k_round_next
+        const int64_t rounds = (int64_t)stats[7];
+        const int per_round = 3 + __builtin_popcount(sc->bsdf_types) + (P.sort_threshold > 0) + 1;
+        launches += 2 * (int64_t)graph_batches + rounds * per_round;
+        trace_c_launches += rounds;
+        trace_a_launches += rounds;
+    }
     ctx->last.launches = launches;
     ctx->last.limit_hits = limit;
     if (limit) return fail(RT_ERR_LIMIT, "a device loop reached its iteration cap");
@@ -2673,6 +2903,7 @@ extern "C" rt_status rt_render_tile_static(rt_ctx *ctx, rt_scene *sc, const rt_r
     k_tile_order<<<(int)((npix + 127) / 128), 128, 0, st>>>(tileorder, ox, oy, tw, th);
     if ((s = launch_check("k_tile_order")) != RT_OK) return s;
     RenderParams Pm;
+    std::memset(&Pm, 0, sizeof(Pm));
     Pm.S = sc->S;
     Pm.S.light_cdf = light_cdf;
     Pm.W = W;
@@ -2734,6 +2965,23 @@ extern "C" rt_status rt_render_tile_static(rt_ctx *ctx, rt_scene *sc, const rt_r
 rt_status rt_internal_error(rt_status st, const char *msg) { return fail(st, msg ? msg : ""); }
 int rt_internal_device(const rt_ctx *c) { return c->device; }
 int rt_internal_bvh_width(const rt_ctx *c) { return c->bvh_width; }
+int rt_internal_graphs(const rt_ctx *c) { return c->graphs; }
+void rt_internal_get_shape(const rt_ctx *c, int *wave_paths, int *trace_bpsm, int *shade_bpsm, int *sort_threshold)
+{
+    *wave_paths = c->wave_paths;
+    *trace_bpsm = c->trace_bpsm;
+    *shade_bpsm = c->shade_bpsm;
+    *sort_threshold = c->sort_threshold;
+}
+rt_status rt_internal_set_shape(rt_ctx *c, int trace_bpsm, int shade_bpsm, int sort_threshold)
+{
+    if (trace_bpsm < 1 || trace_bpsm > 64 || shade_bpsm < 1 || shade_bpsm > 64 || sort_threshold < 0)
+        return fail(RT_ERR_INVALID, "tuning: blocks per SM must be in 1..64 and the sort threshold >= 0");
+    c->trace_bpsm = trace_bpsm;
+    c->shade_bpsm = shade_bpsm;
+    c->sort_threshold = sort_threshold;
+    return RT_OK;
+}
 void *rt_internal_stream(const rt_ctx *c) { return (void *)c->stream; }
 rt_lane_pool *&rt_internal_pool(rt_ctx *c) { return c->pool; }
 void rt_internal_set_stats(rt_ctx *c, const rt_render_stats &s) { c->last = s; }

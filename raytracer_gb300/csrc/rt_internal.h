@@ -15,6 +15,11 @@ struct rt_lane_pool;   // worker lanes of rt_batch_render, owned by a context
 RT_HIDDEN rt_status rt_internal_error(rt_status st, const char *msg);   // sets rt_last_error()
 RT_HIDDEN int rt_internal_device(const rt_ctx *c);
 RT_HIDDEN int rt_internal_bvh_width(const rt_ctx *c);
+RT_HIDDEN int rt_internal_graphs(const rt_ctx *c);
+// launch shape and sort threshold of a context's renders (rt_tuning fields)
+RT_HIDDEN void rt_internal_get_shape(const rt_ctx *c, int *wave_paths, int *trace_bpsm, int *shade_bpsm,
+                                     int *sort_threshold);
+RT_HIDDEN rt_status rt_internal_set_shape(rt_ctx *c, int trace_bpsm, int shade_bpsm, int sort_threshold);
 RT_HIDDEN void *rt_internal_stream(const rt_ctx *c);
 RT_HIDDEN rt_lane_pool *&rt_internal_pool(rt_ctx *c);
 RT_HIDDEN void rt_internal_set_stats(rt_ctx *c, const rt_render_stats &s);

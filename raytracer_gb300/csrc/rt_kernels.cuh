@@ -11,13 +11,15 @@ namespace rtgpu {
 enum { F_FIRST = 1, F_DELTA = 2, F_NEE = 4, F_END = 8, F_DONE = 16 };
 
 #define RT_NBSDF 6        // shading queues (bsdf_queue): types 0-4, then the delta types
+#define RT_QUEUE_MIXED 6  // one more queue: every BSDF type, for rounds below the sort threshold
 
 struct RoundCounters {   // one per wavefront round, zeroed per batch
     int closest, shadow, wc_closest, wc_shadow;
     int mat[RT_NBSDF];   // paths to shade per shading queue (material-sorted)
     int fin;             // paths whose traced ray missed or hit a surface without a BSDF
     int end;             // paths that ended in shading with a light sample pending
-    int pad[4];
+    int mixed;           // paths to shade, not sorted by material (round below the sort threshold)
+    int pad[3];
 };
 
 struct Wave {
@@ -40,6 +42,7 @@ struct Wave {
     // queues of the current round
     int *q_closest, *q_shadow;
     int *q_mat[RT_NBSDF];  // shading queues (bsdf_queue), filled by the closest-hit trace
+    int *q_mixed;          // the unsorted shading queue (RT_QUEUE_MIXED)
     int *q_fin;        // rays that missed or hit a surface without a BSDF (to finish)
     int *q_end;        // paths whose BSDF sample was zero, light sample pending
     // ray reordering (optional): per-ray keys, the reordered queue, key counts

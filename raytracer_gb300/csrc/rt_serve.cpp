@@ -43,20 +43,30 @@ double now_ms()
 
 struct LaneSet {
     int device = 0;
+    // lanes overlap several renders; smaller batches than a lone render's
+    // bound their memory (about 240 bytes per path each)
+    int wave_paths = 1 << 24;
     std::vector<rt_ctx *> lanes;
 
-    rt_status grow(int k, int bvh_width)
+    // lanes take the owning context's traversal width, graph setting, launch
+    // shape and sort threshold
+    rt_status grow(int k, const rt_ctx *owner)
     {
         while ((int)lanes.size() < k) {
             rt_ctx *c = nullptr;
             rt_status s = rt_ctx_create(device, &c);
             if (s != RT_OK) return s;
-            rt_ctx_set_bvh_width(c, bvh_width);
-            // lanes overlap several renders; smaller batches bound their memory
-            rt_ctx_set_wave_paths(c, 1 << 24);
             lanes.push_back(c);
         }
-        for (rt_ctx *c : lanes) rt_ctx_set_bvh_width(c, bvh_width);
+        int wave, tb, sb, thr;
+        rt_internal_get_shape(owner, &wave, &tb, &sb, &thr);
+        for (rt_ctx *c : lanes) {
+            rt_ctx_set_bvh_width(c, rt_internal_bvh_width(owner));
+            rt_ctx_set_graphs(c, rt_internal_graphs(owner));
+            rt_ctx_set_wave_paths(c, wave_paths);
+            rt_status s = rt_internal_set_shape(c, tb, sb, thr);
+            if (s != RT_OK) return s;
+        }
         return RT_OK;
     }
     void clear()
@@ -137,6 +147,37 @@ extern "C" rt_status rt_ctx_set_lanes(rt_ctx *ctx, int32_t lanes)
     return RT_OK;
 }
 
+extern "C" rt_status rt_ctx_get_tuning(rt_ctx *ctx, rt_tuning *out)
+{
+    if (!ctx || !out) return rt_internal_error(RT_ERR_INVALID, "rt_ctx_get_tuning: null argument");
+    rt_lane_pool *pool = pool_of(ctx);
+    int wave, tb, sb, thr;
+    rt_internal_get_shape(ctx, &wave, &tb, &sb, &thr);
+    out->wave_paths = wave;
+    out->lane_wave_paths = pool->set.wave_paths;
+    out->trace_blocks_per_sm = tb;
+    out->shade_blocks_per_sm = sb;
+    out->sort_threshold = thr;
+    out->lanes = pool->want;
+    out->graphs = rt_internal_graphs(ctx);
+    return RT_OK;
+}
+
+extern "C" rt_status rt_ctx_set_tuning(rt_ctx *ctx, const rt_tuning *t)
+{
+    if (!ctx || !t) return rt_internal_error(RT_ERR_INVALID, "rt_ctx_set_tuning: null argument");
+    if (t->lane_wave_paths < (1 << 16) || t->lane_wave_paths > (1 << 26))
+        return rt_internal_error(RT_ERR_INVALID, "tuning: lane wave paths must be in [2^16, 2^26]");
+    if (t->graphs != 0 && t->graphs != 1) return rt_internal_error(RT_ERR_INVALID, "tuning: graphs must be 0 or 1");
+    rt_status s = rt_ctx_set_wave_paths(ctx, t->wave_paths);
+    if (s == RT_OK) s = rt_internal_set_shape(ctx, t->trace_blocks_per_sm, t->shade_blocks_per_sm, t->sort_threshold);
+    if (s == RT_OK) s = rt_ctx_set_lanes(ctx, t->lanes);
+    if (s != RT_OK) return s;
+    rt_ctx_set_graphs(ctx, t->graphs);
+    pool_of(ctx)->set.wave_paths = t->lane_wave_paths;
+    return RT_OK;
+}
+
 extern "C" rt_status rt_batch_render(rt_ctx *ctx, rt_scene *const *scenes, const rt_render_desc *descs, int32_t n,
                                      float *const *films, int32_t on_device)
 {
@@ -153,7 +194,7 @@ extern "C" rt_status rt_batch_render(rt_ctx *ctx, rt_scene *const *scenes, const
         return rt_internal_error(RT_ERR_CUDA, "rt_batch_render: stream synchronize failed");
     rt_lane_pool *pool = pool_of(ctx);
     const int k = std::min(pool->want, n);
-    rt_status s = pool->set.grow(k, rt_internal_bvh_width(ctx));
+    rt_status s = pool->set.grow(k, ctx);
     if (s != RT_OK) return s;
     // largest job first, so that the long ones do not start last
     std::vector<int> order(n);
@@ -336,7 +377,8 @@ extern "C" rt_status rt_server_start(rt_ctx *ctx, const rt_server_opts *opts, rt
     S->set.device = rt_internal_device(ctx);
     S->max_queue = opts && opts->max_queue > 0 ? opts->max_queue : 4096;
     S->budget = opts ? opts->device_budget_bytes : 0;
-    rt_status s = S->set.grow(lanes, rt_internal_bvh_width(ctx));
+    S->set.wave_paths = pool_of(ctx)->set.wave_paths;
+    rt_status s = S->set.grow(lanes, ctx);
     if (s != RT_OK) {
         S->set.clear();
         delete S;

@@ -355,10 +355,13 @@ class SceneData:
         return D
 
     def render_desc(self, spp, seed=0, sample_begin=0, block=32, flags=0, **over):
+        """`block`: the tile size (blockSizeX = blockSizeY), or a pair
+        (blockSizeX, blockSizeY)."""
         it = dict(self.integrator)
         it.update(over)
+        bx, by = (block, block) if np.isscalar(block) else block
         return RenderDesc(it["integrator"], it["max_depth"], it["min_depth"], it["strategy"],
-                          spp, sample_begin, seed, block, block, flags)
+                          spp, sample_begin, seed, int(bx), int(by), flags)
 
     def bounds(self):
         lo = self.vertices.min(0) if len(self.vertices) else np.full(3, np.inf)

@@ -215,8 +215,12 @@ def write_scene(scene, folder, spp=1, name="scene"):
             _filter_xml(cam.get("filter", D.box_filter())),
             "  </camera>"]
     block = getattr(s, "block", (32, 32))
+    fname = getattr(s, "file_name", "")
     out += ["  <parameters>", "    <blockSizeX>%d</blockSizeX>" % block[0],
-            "    <blockSizeY>%d</blockSizeY>" % block[1], "  </parameters>",
+            "    <blockSizeY>%d</blockSizeY>" % block[1]]
+    if fname:
+        out.append("    <fileName>%s</fileName>" % fname)
+    out += ["  </parameters>",
             '  <sampler type="RandomSampler"><integer name="sampleNumber" value="%d"/></sampler>' % spp]
     if cam.get("medium", -1) >= 0:
         out += _medium_xml(s.media[cam["medium"]], "camera", folder, "medium%d" % cam["medium"], 2)

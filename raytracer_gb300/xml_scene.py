@@ -12,7 +12,8 @@ the element.  Paths in the file are resolved against the file's folder
                  <transform> = camera to world, <filter> BoxFilter, GaussianFilter,
                  MitchellNetravaliFilter (radiusX, radiusY, alpha/omega, B/C)
     sampler      RandomSampler: sampleNumber -> `spp` (RandomSampler.cpp:10)
-    parameters   blockSizeX, blockSizeY -> `block` (XMLLoader.cpp:217-259)
+    parameters   blockSizeX, blockSizeY -> `block`, fileName -> `file_name`
+                 (XMLLoader.cpp:217-259)
     medium       (top level) the camera medium (XMLLoader.cpp:96-101; the later
                  referable-medium branch of the reference is unreachable)
     lights       EnvironmentLight: path (.hdr), toWorld, scale (EnvironmentLight.cpp:8-19)
@@ -147,6 +148,7 @@ class _Loader:
         self.camera_medium = -1
         self.spp = 1
         self.block = (32, 32)
+        self.file_name = ""
         self.filter = D.box_filter()
 
     def resolve(self, p):
@@ -428,6 +430,8 @@ class _Loader:
                         bx = int(c.text)
                     elif c.tag == "blockSizeY":
                         by = int(c.text)
+                    elif c.tag == "fileName":   # where main.cpp:560-563 saves the image
+                        self.file_name = (c.text or "").strip()
                 self.block = (bx, by)
             elif key == "sampler":
                 if el.get("type") != "RandomSampler":
@@ -467,6 +471,7 @@ class _Loader:
         self.s.camera = cam
         self.s.spp = self.spp
         self.s.block = self.block
+        self.s.file_name = self.file_name
         return self.s
 
 

@@ -44,7 +44,8 @@ def test_struct_layout_matches_header(tmp_path):
         prog.append('printf("%s %%zu\\n", sizeof(%s));' % (k, k))
     from raytracer_gb300 import core
     extra = {"rt_medium_q": core.MEDIUM_Q.itemsize, "rt_medium_r": core.MEDIUM_R.itemsize,
-             "rt_server_opts": C.sizeof(core.ServerOpts), "rt_job_info": C.sizeof(core.JobInfo)}
+             "rt_server_opts": C.sizeof(core.ServerOpts), "rt_job_info": C.sizeof(core.JobInfo),
+             "rt_tuning": C.sizeof(core.Tuning)}
     for k in extra:
         prog.append('printf("%s %%zu\\n", sizeof(%s));' % (k, k))
     prog.append('printf("camera_off %zu\\n", offsetof(rt_scene_desc, camera));')

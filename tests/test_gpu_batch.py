@@ -49,6 +49,23 @@ def test_batch_matches_individual_renders(ctx, job_scenes):
     ctx.set_lanes(4)
 
 
+def test_batch_with_graphs_matches_individual_renders(ctx, job_scenes):
+    """Lanes take the owning context's graph setting; graph-launched batches
+    reproduce the kernel-by-kernel films bit for bit."""
+    ref = [job_scenes[n].render(spp, **opt) for n, spp, opt in JOBS]
+    ctx.set_graphs(1)
+    try:
+        ctx.set_lanes(3)
+        films = ctx.batch_render([(job_scenes[n], spp, opt) for n, spp, opt in JOBS])
+        again = ctx.batch_render([(job_scenes[n], spp, opt) for n, spp, opt in JOBS])
+    finally:
+        ctx.set_graphs(0)
+        ctx.set_lanes(4)
+    for (n, _, _), a, b, r in zip(JOBS, films, again, ref):
+        assert np.array_equal(a, r), n
+        assert np.array_equal(b, r), n
+
+
 def test_batch_reports_first_error_and_runs_the_rest(ctx, job_scenes):
     jobs = [(job_scenes["cornell"], 2, dict(seed=1)), (job_scenes["ico"], 2, dict(seed=2, max_depth=-1))]
     with pytest.raises(R.RtError) as e:
@@ -117,3 +134,53 @@ def test_server_queue_states_and_stop(ctx, job_scenes):
         budget.submit(g, 1)
     assert e.value.status == 3
     budget.stop()
+
+
+TUNINGS = [dict(sort_threshold=1 << 30),                       # every bounce shaded from one unsorted queue
+           dict(sort_threshold=1 << 14, graphs=1),             # unsorted tail bounces, graph launches
+           dict(trace_blocks_per_sm=8, shade_blocks_per_sm=4, wave_paths=1 << 16),
+           dict(trace_blocks_per_sm=16, shade_blocks_per_sm=24, sort_threshold=1 << 12)]
+
+
+@pytest.mark.parametrize("ti", range(len(TUNINGS)))
+def test_tuning_keeps_the_film(ctx, job_scenes, ti):
+    """No rt_tuning field changes a result: queue capacity, grid sizes, the
+    material-sort threshold (one generic shading kernel below it) and graph
+    launches all give the default tuning's film bit for bit."""
+    smooth = R.Scene(ctx, scenes.cornell_smooth(40, 32))
+    cases = [(job_scenes["ico"], 2, dict(seed=2)), (job_scenes["cornell"], 4, dict(seed=1)),
+             (smooth, 3, dict(seed=5)), (job_scenes["vol"], 2, dict(seed=3))]
+    ref = [g.render(spp, **o) for g, spp, o in cases]
+    before = ctx.get_tuning()
+    try:
+        ctx.set_tuning(**TUNINGS[ti])
+        for (g, spp, o), r in zip(cases, ref):
+            assert np.array_equal(g.render(spp, **o), r)
+        films = ctx.batch_render(cases)
+        for f, r in zip(films, ref):
+            assert np.array_equal(f, r)
+    finally:
+        ctx.set_tuning(**before)
+        smooth.close()
+    assert ctx.get_tuning() == before
+
+
+def test_autotune_sets_a_valid_tuning(ctx, job_scenes):
+    """The autotuner times trials on the sample, leaves its choice set on the
+    context, and the films under it equal the default tuning's."""
+    sample = [(job_scenes["ico"], 2, dict(seed=2)), (job_scenes["cornell"], 2, dict(seed=1)),
+              (job_scenes["ragged"], 2, dict(seed=4, block=8))]
+    ref = [g.render(spp, **o) for g, spp, o in sample]
+    before = ctx.get_tuning()
+    try:
+        best, sps = ctx.autotune(sample, max_trials=10)
+        assert sps > 0
+        assert ctx.get_tuning() == best
+        assert best["lanes"] in (1, 2, 4, 8) and best["graphs"] in (0, 1)
+        assert best["sort_threshold"] in (0, 1 << 12, 1 << 14, 1 << 16, 1 << 18)
+        for f, r in zip(ctx.batch_render(sample), ref):
+            assert np.array_equal(f, r)
+        with pytest.raises(R.RtError):
+            ctx.autotune(sample, max_trials=0)
+    finally:
+        ctx.set_tuning(**before)

@@ -358,6 +358,64 @@ def test_ray_sort_keeps_the_film(ctx, rtlib, ico):
     g.close()
 
 
+@pytest.mark.parametrize("case", ["two_batches", "bvh8", "gaussian_smooth", "accumulate"])
+def test_graph_batches_keep_the_film(ctx, rtlib, ico, case):
+    """Each PathTracingMIS batch launched as one CUDA graph, with the bounce
+    loop a conditional node that the device ends, gives the kernel-by-kernel
+    film bit for bit; the repeated render reuses the instantiated graph."""
+    spp, over, scene = 4, {}, None
+    if case == "two_batches":
+        scene = rtlib.Scene(ctx, scenes.cornell_box(80, 60))   # 6 tiles x 16384 paths, 4 tiles per batch
+        spp = 16
+        ctx.set_wave_paths(1 << 16)
+    elif case == "bvh8":
+        scene = rtlib.Scene(ctx, ico)
+        spp = 2
+        ctx.set_bvh_width(8)
+    elif case == "gaussian_smooth":
+        s = scenes.cornell_smooth(48, 40)
+        s.camera["filter"] = D.gaussian_filter(1.5, 1.5)
+        scene = rtlib.Scene(ctx, s)
+    else:
+        scene = rtlib.Scene(ctx, scenes.cornell_box(40, 30))
+    try:
+        if case == "accumulate":
+            base = scene.render(2, seed=3)
+            ref = scene.render(2, seed=3, sample_begin=2, film=None, accumulate=True, out=base.copy())
+        else:
+            ref = scene.render(spp, seed=5, **over)
+        ctx.set_graphs(1)
+        for _ in range(2):
+            if case == "accumulate":
+                got = scene.render(2, seed=3, sample_begin=2, film=None, accumulate=True, out=base.copy())
+            else:
+                got = scene.render(spp, seed=5, **over)
+            assert np.array_equal(got, ref)
+        st = ctx.stats()
+        assert st["paths"] > 0 and st["launches"] > 0
+    finally:
+        ctx.set_graphs(0)
+        ctx.set_wave_paths(1 << 26)
+        ctx.set_bvh_width(2)
+        scene.close()
+
+
+def test_graphs_on_the_legacy_default_stream(rtlib):
+    """A context on the legacy default stream (stream 0, which cannot be
+    captured) still launches graph batches: they are captured on the
+    context's own streams and launched on the caller's."""
+    c = rtlib.Context(0)
+    try:
+        c.set_stream(0)
+        g = rtlib.Scene(c, scenes.cornell_box(40, 30))
+        ref = g.render(4, seed=2)
+        c.set_graphs(1)
+        assert np.array_equal(g.render(4, seed=2), ref)
+        g.close()
+    finally:
+        c.close()
+
+
 def test_film_parity_layered(ctx, rtlib):
     """LayeredBSDF (coat over a rough conductor) on the Cornell boxes; the
     coat normal's side stream is keyed identically on both sides."""
