@@ -84,7 +84,25 @@ typedef struct rt_bsdf_desc {
     /* 1: wrapped in a TwoSides (bsdf/TwoSides.cpp) with this BSDF on both
      * sides (the one-child form, where "bsdf2" defaults to "bsdf") */
     int32_t two_sided;
+    /* ImageTextures replacing the constants above at each hit's texture
+     * coordinates: index + 1 into rt_scene_desc.textures, 0 = the constant.
+     * albedo: Diffuse; reflectance: RoughConductor, RoughDielectric,
+     * Dielectric, Conductor; transmittance: RoughDielectric, Dielectric;
+     * alpha (the texel's channel average): RoughConductor, RoughDielectric. */
+    int32_t tex_albedo, tex_reflectance, tex_transmittance, tex_alpha;
 } rt_bsdf_desc;
+
+/* ImageTexture (texture/ImageTexture.cpp:8-70): a linear RGB image as
+ * ImageLoader::load leaves it (8-bit images decoded from sRGB, HDR images
+ * as stored), indexed (x, y) = rgb[3 * (x + y * width)], looked up with the
+ * reference's wrap and bilinear rules (math::interp2, core/BasicMath.h). */
+typedef struct rt_texture_desc {
+    int32_t width, height;
+    const float *rgb;
+    float scale;             /* "scale" (its absolute value), default 1          */
+    int32_t invert_x;        /* "invertX", default 0                             */
+    int32_t invert_y;        /* "invertY", default 0                             */
+} rt_texture_desc;
 
 /* One reference Mesh (factory/MeshFactory.h:39-139): a contiguous range of
  * triangles with one BSDF, an optional area light and its media. */
@@ -181,6 +199,12 @@ typedef struct rt_scene_desc {
     int32_t n_media;
     const rt_medium_desc *media;
     rt_camera_desc camera;
+    int32_t n_textures;
+    const rt_texture_desc *textures;
+    const float *uvs;            /* 2 floats per vertex or NULL; a NaN u marks a
+                                    vertex of a mesh without texture coordinates
+                                    (its hits use their barycentric (u, v),
+                                    Triangle.cpp:155-170) */
 } rt_scene_desc;
 
 /* ------------------------------------------------------------------ */

@@ -168,6 +168,12 @@ enum { O_BSDF_UNKNOWN = 0, O_BSDF_DIFFUSE_REFLECTION = 1, O_BSDF_DELTA_REFLECTIO
        O_BSDF_GLOSSY_TRANSMISSION = 0x10, O_BSDF_DIFFUSE = 0x200,
        O_BSDF_DELTA = 2 | 8, O_BSDF_ALL = (1 | 2 | 4) | (8 | 4) };
 
+/* ImageTextures (texture/ImageTexture.cpp): the BSDF at a hit, with its
+ * textured parameters replaced by their values at uv.  Returns b itself when
+ * it has no texture, else `tmp` filled in. */
+const rt_bsdf_desc *o_bsdf_at(const rt_scene_desc *d, const rt_bsdf_desc *b, v2 uv, rt_bsdf_desc *tmp);
+c3 o_tex_eval(const rt_texture_desc *t, v2 uv);
+
 c3 o_bsdf_eval(const rt_bsdf_desc *b, const o_bsdf_rec *r);
 float o_bsdf_pdf(const rt_bsdf_desc *b, const o_bsdf_rec *r);
 /* aux_key: the side-stream key of a LayeredBSDF sample (o_ly_sample) */
@@ -188,6 +194,9 @@ c3 o_env_le(const o_scene *sc, int light, v3 dir);
 /* ---------------- ray / intersection ---------------- */
 typedef struct { v3 o, d, inv; float mint, maxt; } o_ray;
 o_ray o_ray_make(v3 o, v3 d, float mint, float maxt);
+/* Sphere::intersection's uv (Sphere.cpp:98-104): spherical angles of the
+ * object-space hit point of ray r at t */
+v2 o_sphere_uv(const rt_sphere_desc *sp, const o_ray *r, float t);
 
 typedef struct {
     float t; float u, v;
@@ -195,6 +204,7 @@ typedef struct {
     v3 p;                   /* hit point                                    */
     v3 ng;                  /* true normal                                  */
     v3 n, s, tt;            /* shading frame (N, S, T)                      */
+    v2 uv;                  /* texture coordinates (Intersection::myUv)     */
 } o_hit;
 
 o_bvh *o_bvh_build_scene(const o_scene *sc);

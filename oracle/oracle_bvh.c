@@ -523,8 +523,17 @@ int o_intersect(const o_scene *sc, const o_ray *ray, o_hit *hit, int shadow)
         }
         hit->n = ns;
         frame_from(ns, &hit->s, &hit->tt);
+        /* texture coordinates (Triangle.cpp:155-170): the vertex uvs with the
+         * barycentrics, or the barycentrics themselves for a mesh without */
+        hit->uv = mk2(rec.u, rec.v);
+        if (d->uvs && !isnan(d->uvs[2 * (size_t)d->indices[3 * (size_t)tri]])) {
+            const int32_t *ix = d->indices + 3 * (size_t)tri;
+            const float *u0 = d->uvs + 2 * (size_t)ix[0], *u1 = d->uvs + 2 * (size_t)ix[1], *u2 = d->uvs + 2 * (size_t)ix[2];
+            hit->uv = mk2((bx * u0[0] + by * u1[0]) + bz * u2[0], (bx * u0[1] + by * u1[1]) + bz * u2[1]);
+        }
     } else {
         const rt_sphere_desc *sp = &d->spheres[-rec.prim - 2];
+        hit->uv = o_sphere_uv(sp, ray, rec.t);
         hit->p = rec.p;
         v3 nl = v3_normalized(v3_sub(xf_point(sp->to_object, rec.p), mk3(0, 0, 0)));
         v3 n = v3_normalized(xf_normal(sp->to_object, nl));

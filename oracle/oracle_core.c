@@ -199,6 +199,9 @@ static v3 o_cartesian_from_spherical(float theta, float phi)
     return mk3(sp * st, ct, -cp * st);
 }
 
+/* alpha as the rough BSDFs read it: myAlphaTexture->eval(uv).average() */
+static float o_alpha(const rt_bsdf_desc *b) { return b->tex_alpha == -1 ? b->alpha : c3_avg(cfill(b->alpha)); }
+
 /* ===================== Fresnel (core/Fresnel.h) ===================== */
 /* Fresnel.h:30-49 (per channel) */
 static float o_fresnel_conductor1(float eta, float k, float cosI)
@@ -347,7 +350,7 @@ static c3 o_rc_eval(const rt_bsdf_desc *b, v3 wi, v3 wo)
     float ci = wi.z, co = wo.z;
     if (ci <= 0.f || co <= 0.f) return cfill(0.f);
     v3 wh = v3_normalized(v3_add(wi, wo));
-    float a = c3_avg(cfill(b->alpha));
+    float a = o_alpha(b);
     float D = o_mf_D(b->distribution, wh, a);
     float G = o_mf_G(b->distribution, wi, wo, wh, a);
     c3 F = mkc(o_fresnel_conductor1(b->eta[0], b->k[0], ci),
@@ -366,14 +369,14 @@ static float o_rc_pdf(const rt_bsdf_desc *b, v3 wi, v3 wo)
     v3 wh = v3_normalized(v3_add(wi, wo));
     float ch = wh.z;
     float Jh = 1.f / (4 * fabsf(v3_dot(wh, wo)));
-    float D = o_mf_D(b->distribution, wh, c3_avg(cfill(b->alpha)));
+    float D = o_mf_D(b->distribution, wh, o_alpha(b));
     return D * ch * Jh;
 }
 static c3 o_rc_sample(const rt_bsdf_desc *b, o_bsdf_rec *r, v2 s)
 {
     if (r->wi.z <= 0.f) return cfill(0.f);
     r->sampled_type = O_BSDF_GLOSSY_REFLECTION;
-    float alpha = o_adjusted_alpha(c3_avg(cfill(b->alpha)), r->wi.z);
+    float alpha = o_adjusted_alpha(o_alpha(b), r->wi.z);
     v3 n = o_mf_sample_normal(b->distribution, s, alpha);
     r->wo = o_reflect_n(r->wi, n);
     float co = r->wo.z;
@@ -390,7 +393,7 @@ static c3 o_rd_eval_reflection(const rt_bsdf_desc *b, v3 wi, v3 wo)
     float ci = wi.z, co = wo.z;
     v3 wh = v3_normalized(v3_add(wi, wo));
     wh = v3_smul(o_sign(ci), wh);
-    float alpha = c3_avg(cfill(b->alpha));
+    float alpha = o_alpha(b);
     float D = o_mf_D(b->distribution, wh, alpha);
     float eI, eT, rel, cT;
     float fr = o_estimate_dielectric(b->eta_ext, b->eta_int, v3_dot(wi, wh), &eI, &eT, &rel, &cT);
@@ -407,7 +410,7 @@ static c3 o_rd_eval_refraction(const rt_bsdf_desc *b, v3 wi, v3 wo)
     float eI, eT, rel, cT;
     float fr = o_estimate_dielectric(b->eta_ext, b->eta_int, ci, &eI, &eT, &rel, &cT);
     v3 wt = o_half_dir_transmitted(wi, wo, eI, eT);
-    float alpha = c3_avg(cfill(b->alpha));
+    float alpha = o_alpha(b);
     float left = v3_dot(wi, wt) * v3_dot(wo, wt) / (ci * co);
     float G = o_mf_G(b->distribution, wi, wo, wt, alpha);
     float D = o_mf_D(b->distribution, wt, alpha);
@@ -426,7 +429,7 @@ static c3 o_rd_eval_refraction(const rt_bsdf_desc *b, v3 wi, v3 wo)
 static float o_rd_pdf_reflection(const rt_bsdf_desc *b, v3 wi, v3 wo)
 {
     float ci = wi.z;
-    float alpha = (1.2f - 0.2f * sqrtf(fabsf(ci))) * c3_avg(cfill(b->alpha));
+    float alpha = (1.2f - 0.2f * sqrtf(fabsf(ci))) * o_alpha(b);
     v3 wh = v3_normalized(v3_add(wi, wo));
     wh = v3_smul(o_sign(ci), wh);
     float ch = wh.z;
@@ -440,7 +443,7 @@ static float o_rd_pdf_refraction(const rt_bsdf_desc *b, v3 wi, v3 wo)
     o_estimate_dielectric(b->eta_ext, b->eta_int, ci, &eI, &eT, &rel, &cT);
     v3 wt = o_half_dir_transmitted(wi, wo, eI, eT);
     float cwt = wt.z;
-    float alpha = (1.2f - 0.2f * sqrtf(fabsf(ci))) * c3_avg(cfill(b->alpha));
+    float alpha = (1.2f - 0.2f * sqrtf(fabsf(ci))) * o_alpha(b);
     float hd = eI * v3_dot(wi, wt) + eT * v3_dot(wo, wt);
     float Jh = (eT * eT * v3_dot(wo, wt)) / (hd * hd);
     return fabsf(o_mf_D(b->distribution, wt, alpha) * cwt * Jh);
@@ -469,7 +472,7 @@ static float o_rd_pdf(const rt_bsdf_desc *b, v3 wi, v3 wo)
 static c3 o_rd_sample(const rt_bsdf_desc *b, o_bsdf_rec *r, v2 s)
 {
     float ci = r->wi.z;
-    float alpha = o_adjusted_alpha(c3_avg(cfill(b->alpha)), ci);
+    float alpha = o_adjusted_alpha(o_alpha(b), ci);
     v3 n = o_mf_sample_normal(b->distribution, s, alpha);
     float eI, eT, rel, cT;
     float fr = o_fr_avg(o_estimate_dielectric(b->eta_ext, b->eta_int, v3_dot(r->wi, n), &eI, &eT, &rel, &cT));
@@ -720,6 +723,79 @@ static c3 o_ly_sample(const rt_bsdf_desc *b, o_bsdf_rec *r, v2 s, uint64_t aux_k
     if (r->pdf == 0.f) return cfill(0.f);
     float co = r->wo.z;
     return c3_divs(c3_muls(o_ly_eval(b, r->wi, r->wo), fabsf(co)), r->pdf);
+}
+
+/* ===================== textures (texture/ImageTexture.cpp) ===================== */
+v2 o_sphere_uv(const rt_sphere_desc *sp, const o_ray *r, float t)
+{
+    v3 lo = xf_point(sp->to_object, r->o), ld = xf_vector(sp->to_object, r->d);
+    v3 n = v3_normalized(v3_add(lo, v3_smul(t, ld)));
+    return mk2(o_spherical_phi(n) / (2 * O_PI), o_spherical_theta(n) / O_PI);
+}
+static int o_tclamp(int v, int lo, int hi) { return v < lo ? lo : v > hi ? hi : v; }
+static c3 o_texel(const rt_texture_desc *t, int x, int y)
+{
+    const float *p = t->rgb + 3 * ((size_t)y * t->width + x);
+    return mkc(p[0], p[1], p[2]);
+}
+/* math::interp2 (core/BasicMath.h:73-90); a texture one texel wide (high)
+ * keeps index 0 where the reference's empty clamp range gives -1 */
+static c3 o_interp2(const rt_texture_desc *t, float x, float y)
+{
+    float advanceX = x - (float)(int)x, advanceY = y - (float)(int)y;
+    int xMin = t->width < 2 ? 0 : o_tclamp((int)x, 0, t->width - 2);
+    int yMin = t->height < 2 ? 0 : o_tclamp((int)y, 0, t->height - 2);
+    int xMax = xMin + 1 < t->width ? xMin + 1 : xMin;
+    xMax = o_tclamp(xMax, 0, t->width - 1);
+    int yMax = yMin + 1 < t->height ? yMin + 1 : yMin;
+    yMax = o_tclamp(yMax, 0, t->height - 1);
+    c3 r = c3_muls(o_texel(t, xMin, yMin), (1 - advanceX) * (1 - advanceY));
+    r = c3_add(r, c3_muls(o_texel(t, xMin, yMax), (1 - advanceX) * advanceY));
+    r = c3_add(r, c3_muls(o_texel(t, xMax, yMin), advanceX * (1 - advanceY)));
+    return c3_add(r, c3_muls(o_texel(t, xMax, yMax), advanceX * advanceY));
+}
+/* ImageTexture::eval (ImageTexture.cpp:28-70) */
+c3 o_tex_eval(const rt_texture_desc *t, v2 uv)
+{
+    unsigned W = (unsigned)t->width, H = (unsigned)t->height;
+    float x, y;
+    if (!t->invert_y) y = uv.y * (float)H;
+    else y = (float)(int)uv.y + ((uv.y >= 0.f ? 1 : -1) * 1.f - (uv.y - (float)(int)uv.y)) * (float)H;
+    if (!t->invert_x) x = uv.x * ((float)W - 1.f);
+    else x = (float)(int)uv.x + ((uv.x >= 0.f ? 1 : -1) * 1.f - (uv.x - (float)(int)uv.x)) * (float)W;
+    x *= t->scale;
+    y *= t->scale;
+    if (x >= (float)W) x = (float)((unsigned)(int)x % W) + (x - (float)(int)x);
+    else if (x < 0) x = (float)(W - (unsigned)abs((int)x) % W) + (x - (float)(int)x);
+    if (y >= (float)H) y = (float)((unsigned)(int)y % H) + (y - (float)(int)y);
+    else if (y < 0) y = (float)(H - (unsigned)abs((int)y) % H) + (y - (float)(int)y);
+    return o_interp2(t, x, y);
+}
+/* The BSDF at a hit with its textures applied.  An applied alpha texture is
+ * stored as its channel average with tex_alpha = -1 (a value the ABI does not
+ * use), which o_alpha reads as is; a constant alpha is averaged as a
+ * ConstantTexture's Color. */
+const rt_bsdf_desc *o_bsdf_at(const rt_scene_desc *d, const rt_bsdf_desc *b, v2 uv, rt_bsdf_desc *tmp)
+{
+    if (!(b->tex_albedo | b->tex_reflectance | b->tex_transmittance | b->tex_alpha)) return b;
+    *tmp = *b;
+    if (b->tex_albedo) {
+        c3 c = o_tex_eval(&d->textures[b->tex_albedo - 1], uv);
+        tmp->albedo[0] = c.r; tmp->albedo[1] = c.g; tmp->albedo[2] = c.b;
+    }
+    if (b->tex_reflectance) {
+        c3 c = o_tex_eval(&d->textures[b->tex_reflectance - 1], uv);
+        tmp->reflectance[0] = c.r; tmp->reflectance[1] = c.g; tmp->reflectance[2] = c.b;
+    }
+    if (b->tex_transmittance) {
+        c3 c = o_tex_eval(&d->textures[b->tex_transmittance - 1], uv);
+        tmp->transmittance[0] = c.r; tmp->transmittance[1] = c.g; tmp->transmittance[2] = c.b;
+    }
+    if (b->tex_alpha) {
+        tmp->alpha = c3_avg(o_tex_eval(&d->textures[b->tex_alpha - 1], uv));
+        tmp->tex_alpha = -1;
+    }
+    return tmp;
 }
 
 /* ===================== smooth (delta) BSDFs ===================== */

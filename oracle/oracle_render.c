@@ -358,7 +358,8 @@ static c3 li_path_mis(const o_scene *sc, const rt_render_desc *rd, o_sampler *s,
     while (depth < rd->max_depth) {
         int bsdf = prim_bsdf(sc, it.prim);
         if (bsdf < 0) return L;
-        const rt_bsdf_desc *B = &sc->d->bsdfs[bsdf];
+        rt_bsdf_desc Btex;
+        const rt_bsdf_desc *B = o_bsdf_at(sc->d, &sc->d->bsdfs[bsdf], it.uv, &Btex);
         int hl = prim_light(sc, it.prim);
         if (emission && hl >= 0) L = c3_add(L, c3_mul(T, area_le(sc, hl, v3_neg(ray.d), it.n)));
         /* light sampling */
@@ -521,7 +522,8 @@ static c3 li_volpath(const o_scene *sc, const rt_render_desc *rd, o_sampler *s, 
                 was = o_intersect(sc, &ray, &it, 0);
                 continue;
             }
-            const rt_bsdf_desc *B = &sc->d->bsdfs[bsdf];
+            rt_bsdf_desc Btex;
+        const rt_bsdf_desc *B = o_bsdf_at(sc->d, &sc->d->bsdfs[bsdf], it.uv, &Btex);
             int hl = prim_light(sc, it.prim);
             if (emission && hl >= 0) L = c3_add(L, c3_mul(T, area_le(sc, hl, v3_neg(ray.d), it.n)));
             o_light_rec li;
@@ -795,6 +797,16 @@ int32_t oracle_trace(const o_scene *sc, const rt_ray *rays, int32_t n, int32_t a
         if (hit && anyhit) { hits[i].prim = 0; hits[i].t = 0.f; hits[i].u = hits[i].v = 0.f; }
     }
     return RT_OK;
+}
+
+/* ImageTexture::eval of one texture at n texture coordinates (uv pairs);
+ * out: n rgb triples.  Test hook. */
+void oracle_tex_eval(const rt_texture_desc *t, const float *uv, int32_t n, float *out)
+{
+    for (int i = 0; i < n; i++) {
+        c3 c = o_tex_eval(t, mk2(uv[2 * i], uv[2 * i + 1]));
+        out[3 * i] = c.r; out[3 * i + 1] = c.g; out[3 * i + 2] = c.b;
+    }
 }
 
 int32_t oracle_bsdf_query(const rt_bsdf_desc *b, int32_t op, const rt_bsdf_q *q, int32_t n,

@@ -162,6 +162,7 @@ __device__ __forceinline__ void classify_hit(const RenderParams &P, RoundCounter
     } else {
 #pragma unroll
         for (int k = 0; k < RT_NBSDF; k++) q_push(P.W.q_mat[k], &C->mat[k], slot, t == k);
+        if (P.S.has_textured) q_push(P.W.q_mixed, &C->mixed, slot, t == RT_QUEUE_MIXED);
     }
     q_push(P.W.q_fin, &C->fin, slot, t < 0);
 }
@@ -811,7 +812,14 @@ __global__ void __launch_bounds__(128, RT_SHADE_MINB) k_pt_shade(RenderParams P,
             float4 hv = P.W.hit[slot];
             Hit h; h.t = hv.x; h.u = hv.y; h.v = hv.z; h.prim = __float_as_int(hv.w);
             Frame fr = hit_frame(S, h, o, d);
-            const DevBsdf &B = S.bsdfs[prim_bsdf(S, h.prim)];
+            // the mixed queue's BSDF is a copy with its textures applied at
+            // the hit; the sorted queues read the scene's (untextured) BSDF
+            DevBsdf Bl;
+            if (BT == RT_QUEUE_MIXED) {
+                Bl = S.bsdfs[prim_bsdf(S, h.prim)];
+                if (Bl.textured) tex_apply(S, Bl, hit_uv(S, h, o, d));
+            }
+            const DevBsdf &B = BT == RT_QUEUE_MIXED ? Bl : S.bsdfs[prim_bsdf(S, h.prim)];
             bool done = false;
             // finish the previous vertex (its light sample and the emission
             // its BSDF-sampled ray found), update throughput, roulette
@@ -942,6 +950,13 @@ __device__ __noinline__ bool vp_trace(const DevScene &S, V3 o, V3 d, float mint,
     return trace_ray<false>(S, o, d, mint, maxt, h);
 }
 __device__ __noinline__ Frame vp_frame(const DevScene &S, const Hit &h, V3 o, V3 d) { return hit_frame(S, h, o, d); }
+// the frame of a hit that may be shaded, with its texture coordinates when
+// the scene has textured BSDFs (a sphere's need the ray that found the hit)
+__device__ __noinline__ Frame vp_frame_uv(const DevScene &S, const Hit &h, V3 o, V3 d, V2 &uv)
+{
+    if (S.has_textured) uv = hit_uv(S, h, o, d);
+    return hit_frame(S, h, o, d);
+}
 __device__ __noinline__ C3 vp_medium_tr(const DevMedium &m, Ray r, Pcg32 &rng, int &limit)
 {
     return medium_tr(m, r, rng, limit);
@@ -991,8 +1006,8 @@ __device__ __noinline__ C3 eval_transmittance(const DevScene &S, Ray ray, int me
 }
 
 // VolPathTracing::evalTransmittanceFromSampledBSDF (VolPathTracing.cpp:369-424)
-__device__ __noinline__ C3 eval_tr_sampled(const DevScene &S, Ray ray, Pcg32 &rng, int medium, Hit &h, Frame &fr, bool &was,
-                              int &newm, int &limit)
+__device__ __noinline__ C3 eval_tr_sampled(const DevScene &S, Ray ray, Pcg32 &rng, int medium, Hit &h, Frame &fr, V2 &uv,
+                              bool &was, int &newm, int &limit)
 {
     Ray tr = ray;
     C3 T = cfill(1.f);
@@ -1001,7 +1016,7 @@ __device__ __noinline__ C3 eval_tr_sampled(const DevScene &S, Ray ray, Pcg32 &rn
     for (int guard = 0; guard < 4096; guard++) {
         Hit nh;
         was = vp_trace(S, tr.o, tr.d, tr.mint, tr.maxt, nh);
-        if (was) { h = nh; fr = vp_frame(S, h, tr.o, tr.d); }
+        if (was) { h = nh; fr = vp_frame_uv(S, h, tr.o, tr.d, uv); }
         if (medium >= 0)
             T = T * vp_medium_tr(S.media[medium], make_ray(tr.o, tr.d, first ? tr.mint : 0.f, was ? h.t : tr.maxt), rng, limit);
         if (was && prim_bsdf(S, h.prim) >= 0) return T;
@@ -1043,6 +1058,7 @@ __device__ __noinline__ C3 sample_attenuated_light(const DevScene &S, V3 p, Pcg3
 // sample stream come in the same order as one uninterrupted loop.
 struct VolState {
     C3 L, T;
+    V2 uv;            // texture coordinates of h (scenes with textured BSDFs)
     float eta;
     int depth, medium, guard;
     bool emission, was;
@@ -1062,7 +1078,8 @@ __device__ __forceinline__ void vol_start(const DevScene &S, VolState &st, Ray r
     st.ray = ray;
     Hit nh;
     st.was = vp_trace(S, ray.o, ray.d, ray.mint, ray.maxt, nh);
-    if (st.was) { st.h = nh; st.fr = vp_frame(S, nh, ray.o, ray.d); }
+    st.uv = v2(0.f, 0.f);
+    if (st.was) { st.h = nh; st.fr = vp_frame_uv(S, nh, ray.o, ray.d, st.uv); }
     st.medium = S.cam.medium;
     st.guard = 0;
 }
@@ -1102,7 +1119,7 @@ __device__ bool vol_step(const DevScene &S, VolState &st, Pcg32 &rng, int max_de
         float pfw = phase_sample(M, -ray.d, next2d(rng), wo, pfpdf);
         ray = make_ray(fr.p, wo, 0.f, ray.maxt);
         int newm = -1;
-        C3 tr = eval_tr_sampled(S, ray, rng, medium, h, fr, was, newm, limit);
+        C3 tr = eval_tr_sampled(S, ray, rng, medium, h, fr, st.uv, was, newm, limit);
         T = T * pfw;
         if (was) {
             int hl = prim_light(S, h.prim);
@@ -1129,10 +1146,18 @@ __device__ bool vol_step(const DevScene &S, VolState &st, Pcg32 &rng, int max_de
             if (prim_interior(S, h.prim) != prim_exterior(S, h.prim))
                 medium = dot(fr.n, ray.d) < 0.f ? prim_interior(S, h.prim) : prim_exterior(S, h.prim);
             was = vp_trace(S, ray.o, ray.d, ray.mint, ray.maxt, nh);
-            if (was) { h = nh; fr = vp_frame(S, h, ray.o, ray.d); }
+            if (was) { h = nh; fr = vp_frame_uv(S, h, ray.o, ray.d, st.uv); }
             return true;
         }
-        const DevBsdf &B = S.bsdfs[b];
+        // a textured BSDF: a copy with its textures applied at the hit
+        const DevBsdf *Bp = &S.bsdfs[b];
+        DevBsdf Bl;
+        if (Bp->textured) {
+            Bl = *Bp;
+            tex_apply(S, Bl, st.uv);
+            Bp = &Bl;
+        }
+        const DevBsdf &B = *Bp;
         int hl = prim_light(S, h.prim);
         if (st.emission && hl >= 0) L = L + T * area_le(S, hl, -ray.d, fr.n);
         LightRec li;
@@ -1160,7 +1185,7 @@ __device__ bool vol_step(const DevScene &S, VolState &st, Pcg32 &rng, int max_de
         bool isenv = false;
         C3 Le = cfill(0.f);
         int newm = -1;
-        C3 tr = eval_tr_sampled(S, ray, rng, medium, h, fr, was, newm, limit);
+        C3 tr = eval_tr_sampled(S, ray, rng, medium, h, fr, st.uv, was, newm, limit);
         if (was) {
             int nl = prim_light(S, h.prim);
             if (nl >= 0) { caught = nl; Le = area_le(S, nl, -ray.d, fr.n); }
@@ -1182,7 +1207,7 @@ __device__ bool vol_step(const DevScene &S, VolState &st, Pcg32 &rng, int max_de
         else return false;
     }
     was = vp_trace(S, ray.o, ray.d, ray.mint, ray.maxt, nh);
-    if (was) { h = nh; fr = vp_frame(S, h, ray.o, ray.d); }
+    if (was) { h = nh; fr = vp_frame_uv(S, h, ray.o, ray.d, st.uv); }
     st.emission = false;
     st.depth++;
     return true;
@@ -1862,8 +1887,28 @@ static rt_status validate(const rt_scene_desc *d)
             return fail(RT_ERR_UNSUPPORTED, "light type not supported");
         }
     }
-    for (int b = 0; b < d->n_bsdfs; b++)
-        if (d->bsdfs[b].type < 0 || d->bsdfs[b].type > RT_BSDF_MIRROR) return fail(RT_ERR_UNSUPPORTED, "BSDF type not supported");
+    if (d->n_textures < 0 || (d->n_textures > 0 && !d->textures)) return fail(RT_ERR_INVALID, "bad texture table");
+    for (int i = 0; i < d->n_textures; i++) {
+        const rt_texture_desc &T = d->textures[i];
+        if (T.width < 1 || T.height < 1 || !T.rgb || (int64_t)T.width * T.height > (1 << 28) || !(T.scale >= 0.f) ||
+            !(T.scale < 1e30f))
+            return fail(RT_ERR_INVALID, "texture without texels, too large, or with a bad scale");
+    }
+    for (int b = 0; b < d->n_bsdfs; b++) {
+        const rt_bsdf_desc &B = d->bsdfs[b];
+        if (B.type < 0 || B.type > RT_BSDF_MIRROR) return fail(RT_ERR_UNSUPPORTED, "BSDF type not supported");
+        const int32_t tx[4] = {B.tex_albedo, B.tex_reflectance, B.tex_transmittance, B.tex_alpha};
+        for (int k = 0; k < 4; k++)
+            if (tx[k] < 0 || tx[k] > d->n_textures) return fail(RT_ERR_INVALID, "BSDF texture index out of range");
+        // the parameters each BSDF reads through a texture in the reference
+        const int t = B.type;
+        const bool ok = (!B.tex_albedo || t == RT_BSDF_DIFFUSE) &&
+                        (!B.tex_reflectance || t == RT_BSDF_ROUGH_CONDUCTOR || t == RT_BSDF_ROUGH_DIELECTRIC ||
+                         t == RT_BSDF_DIELECTRIC || t == RT_BSDF_CONDUCTOR) &&
+                        (!B.tex_transmittance || t == RT_BSDF_ROUGH_DIELECTRIC || t == RT_BSDF_DIELECTRIC) &&
+                        (!B.tex_alpha || t == RT_BSDF_ROUGH_CONDUCTOR || t == RT_BSDF_ROUGH_DIELECTRIC);
+        if (!ok) return fail(RT_ERR_UNSUPPORTED, "a texture on a parameter this BSDF type does not texture");
+    }
     for (int m = 0; m < d->n_media; m++) {
         const rt_medium_desc &M = d->media[m];
         if (M.type == RT_MEDIUM_HETEROGENEOUS && (!M.density || M.res[0] < 2 || M.res[1] < 2 || M.res[2] < 2))
@@ -1904,6 +1949,13 @@ rt_status rt_scene_create(rt_ctx *ctx, const rt_scene_desc *d, rt_scene **out)
         for (int t = 0; t < nt; t++)
             for (int k = 0; k < 3; k++)
                 for (int a = 0; a < 3; a++) tri_n[9 * (size_t)t + 3 * k + a] = d->normals[3 * (size_t)d->indices[3 * (size_t)t + k] + a];
+    }
+    std::vector<float> tri_uv;   // 6 floats per triangle; NaN u: mesh without uvs
+    if (d->uvs) {
+        tri_uv.resize(6 * (size_t)nt);
+        for (int t = 0; t < nt; t++)
+            for (int k = 0; k < 3; k++)
+                for (int a = 0; a < 2; a++) tri_uv[6 * (size_t)t + 2 * k + a] = d->uvs[2 * (size_t)d->indices[3 * (size_t)t + k] + a];
     }
     // meshes: area CDF (Mesh.cpp:19-31) and owner boxes
     std::vector<DevMesh> meshes(d->n_meshes);
@@ -1975,6 +2027,11 @@ rt_status rt_scene_create(rt_ctx *ctx, const rt_scene_desc *d, rt_scene **out)
         D.alpha_base_avg = h_cavg1(B.alpha_base);
         D.eta_int = B.eta_int; D.eta_ext = B.eta_ext; D.thickness = B.thickness;
         D.two_sided = B.two_sided != 0;
+        D.tex[TEX_ALBEDO] = B.tex_albedo - 1;
+        D.tex[TEX_REFLECTANCE] = B.tex_reflectance - 1;
+        D.tex[TEX_TRANSMITTANCE] = B.tex_transmittance - 1;
+        D.tex[TEX_ALPHA] = B.tex_alpha - 1;
+        D.textured = (B.tex_albedo | B.tex_reflectance | B.tex_transmittance | B.tex_alpha) != 0;
     }
     // media
     std::vector<DevMedium> media(d->n_media);
@@ -2096,6 +2153,33 @@ rt_status rt_scene_create(rt_ctx *ctx, const rt_scene_desc *d, rt_scene **out)
     if ((st = upload(sc, tri_v.data(), tri_v.size(), &fp)) != RT_OK) { rt_scene_destroy(sc); return st; }
     S.tri_v = fp;
     if (!tri_n.empty()) { if ((st = upload(sc, tri_n.data(), tri_n.size(), &fp)) != RT_OK) { rt_scene_destroy(sc); return st; } S.tri_n = fp; }
+    if (!tri_uv.empty()) { if ((st = upload(sc, tri_uv.data(), tri_uv.size(), &fp)) != RT_OK) { rt_scene_destroy(sc); return st; } S.tri_uv = fp; }
+    // textures: all texels in one buffer, one DevTexture each
+    if (d->n_textures > 0) {
+        size_t total = 0;
+        for (int i = 0; i < d->n_textures; i++) total += 3 * (size_t)d->textures[i].width * d->textures[i].height;
+        std::vector<float> texels(total);
+        std::vector<size_t> off(d->n_textures);
+        size_t o = 0;
+        for (int i = 0; i < d->n_textures; i++) {
+            const rt_texture_desc &T = d->textures[i];
+            off[i] = o;
+            std::memcpy(texels.data() + o, T.rgb, sizeof(float) * 3 * (size_t)T.width * T.height);
+            o += 3 * (size_t)T.width * T.height;
+        }
+        if ((st = upload(sc, texels.data(), texels.size(), &fp)) != RT_OK) { rt_scene_destroy(sc); return st; }
+        std::vector<DevTexture> tex(d->n_textures);
+        for (int i = 0; i < d->n_textures; i++) {
+            const rt_texture_desc &T = d->textures[i];
+            tex[i].w = T.width; tex[i].h = T.height; tex[i].rgb = fp + off[i];
+            tex[i].scale = T.scale; tex[i].invert_x = T.invert_x != 0; tex[i].invert_y = T.invert_y != 0;
+        }
+        const DevTexture *tp;
+        if ((st = upload(sc, tex.data(), tex.size(), &tp)) != RT_OK) { rt_scene_destroy(sc); return st; }
+        S.textures = tp;
+        S.n_textures = d->n_textures;
+    }
+    for (const DevBsdf &b : bsdfs) S.has_textured |= b.textured;
     if ((st = upload(sc, tri_mesh.data(), tri_mesh.size(), &ip)) != RT_OK) { rt_scene_destroy(sc); return st; }
     S.tri_mesh = ip;
     {
@@ -2103,7 +2187,7 @@ rt_status rt_scene_create(rt_ctx *ctx, const rt_scene_desc *d, rt_scene **out)
         std::vector<uint8_t> tri_type(nt, 255);
         for (int t = 0; t < nt; t++) {
             int b = d->meshes[tri_mesh[t]].bsdf;
-            if (b >= 0) tri_type[t] = (uint8_t)bsdf_queue(d->bsdfs[b].type);
+            if (b >= 0) tri_type[t] = (uint8_t)bsdf_queue_of(bsdfs[b]);
         }
         const uint8_t *tp8;
         if ((st = upload(sc, tri_type.data(), tri_type.size(), &tp8)) != RT_OK) { rt_scene_destroy(sc); return st; }
@@ -2150,7 +2234,7 @@ rt_status rt_scene_create(rt_ctx *ctx, const rt_scene_desc *d, rt_scene **out)
     sc->n_lights = d->n_lights;
     sc->n_bsdfs = d->n_bsdfs;
     sc->n_media = d->n_media;
-    for (int b = 0; b < d->n_bsdfs; b++) sc->bsdf_types |= 1 << bsdf_queue(d->bsdfs[b].type);
+    for (int b = 0; b < d->n_bsdfs; b++) sc->bsdf_types |= 1 << bsdf_queue_of(bsdfs[b]);
     *out = sc;
     return RT_OK;
 }
@@ -2464,6 +2548,9 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
     P.spp = rd->spp;
     P.sample_begin = rd->sample_begin;
     P.sort_threshold = ctx->sort_threshold;
+    // shading queues in use: the scene's (textured BSDFs in the mixed one),
+    // and the mixed one for bounces below the sort threshold
+    const int types = sc->bsdf_types | (P.sort_threshold > 0 ? 1 << RT_QUEUE_MIXED : 0);
     const int sm = ctx->sm_count > 0 ? ctx->sm_count : 1;
     int64_t launches = 0, trace_c_launches = 0, trace_a_launches = 0;
     int64_t total_paths = 0;
@@ -2547,9 +2634,9 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
                 if (sc->bsdf_types & 8) k_pt_shade<3><<<shade_blocks, 128, 0, st>>>(P, ri);
                 if (sc->bsdf_types & 16) k_pt_shade<4><<<shade_blocks, 128, 0, st>>>(P, ri);
                 if (sc->bsdf_types & 32) k_pt_shade<5><<<shade_blocks, 128, 0, st>>>(P, ri);
-                if (P.sort_threshold > 0) k_pt_shade<RT_QUEUE_MIXED><<<shade_blocks, 128, 0, st>>>(P, ri);
+                if (types & (1 << RT_QUEUE_MIXED)) k_pt_shade<RT_QUEUE_MIXED><<<shade_blocks, 128, 0, st>>>(P, ri);
                 prof_end(ctx);
-                launches += 3 + __builtin_popcount(sc->bsdf_types) + (P.sort_threshold > 0);
+                launches += 3 + __builtin_popcount(types);
                 trace_c_launches++;
                 trace_a_launches++;
                 if ((s = launch_check("pt round")) != RT_OK) return s;
@@ -2612,7 +2699,7 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
     if (graph_batches) {
         // camera and film per batch, the rounds' kernels and k_round_next
         const int64_t rounds = (int64_t)stats[7];
-        const int per_round = 3 + __builtin_popcount(sc->bsdf_types) + (P.sort_threshold > 0) + 1;
+        const int per_round = 3 + __builtin_popcount(types) + 1;
         launches += 2 * (int64_t)graph_batches + rounds * per_round;
         trace_c_launches += rounds;
         trace_a_launches += rounds;
@@ -2816,6 +2903,8 @@ extern "C" rt_status rt_render_tile_static(rt_ctx *ctx, rt_scene *sc, const rt_r
     const DevCamera &cam = sc->S.cam;
     if (!(cam.filter == RT_FILTER_BOX && cam.frx == 0.5f && cam.fry == 0.5f))
         return fail(RT_ERR_UNSUPPORTED, "rt_render_tile_static: only the box filter of radius 0.5");
+    if (sc->S.has_textured)
+        return fail(RT_ERR_UNSUPPORTED, "rt_render_tile_static: textured BSDFs need rt_render");
     const int Wd = cam.width, H = cam.height;
     const int bx = rd->block_x > 0 ? rd->block_x : 32, by = rd->block_y > 0 ? rd->block_y : 32;
     if (bx > 0xffff || by > 0xffff) return fail(RT_ERR_INVALID, "block size too large");

@@ -35,13 +35,33 @@ struct DevBsdf {
     int dist_base;
     float alpha_base_avg;
     int two_sided;    // wrapped in TwoSides (bsdf/TwoSides.cpp) with itself on both sides
+    // ImageTextures (index into DevScene::textures, -1 = the constant) for
+    // albedo, reflectance, transmittance and alpha; textured = any of them
+    int tex[4];
+    int textured;
+};
+enum { TEX_ALBEDO = 0, TEX_REFLECTANCE = 1, TEX_TRANSMITTANCE = 2, TEX_ALPHA = 3 };
+
+// ImageTexture (texture/ImageTexture.cpp): linear RGB texels, (x, y) at
+// rgb[3 * (x + y * w)]
+struct DevTexture {
+    int w, h;
+    const float *rgb;
+    float scale;
+    int invert_x, invert_y;
 };
 
-// Shading queue of a BSDF type.  The heavy types (0-4) get a queue and a
-// shading kernel each; the smooth (delta) types Dielectric, Conductor and
-// Mirror (5-7) are cheap and share one.
+// Shading queue of a BSDF.  The heavy types (0-4) get a queue and a shading
+// kernel each; the smooth (delta) types Dielectric, Conductor and Mirror
+// (5-7) are cheap and share one; textured BSDFs of any type go to the mixed
+// queue, whose kernel dispatches at run time and applies the textures.
 #define RT_QUEUE_DELTA 5
+#define RT_QUEUE_MIXED 6
 __host__ __device__ __forceinline__ int bsdf_queue(int type) { return type < RT_QUEUE_DELTA ? type : RT_QUEUE_DELTA; }
+__host__ __device__ __forceinline__ int bsdf_queue_of(const DevBsdf &b)
+{
+    return b.textured ? RT_QUEUE_MIXED : bsdf_queue(b.type);
+}
 
 struct DevLight {
     int type, mesh_light, shape_kind, shape;
@@ -101,7 +121,11 @@ struct DevScene {
     const float *tri_v;         // 9 floats per triangle (p0, p1, p2)
     const float *tri_n;         // 9 floats per triangle (n0, n1, n2) or null
     const int *tri_mesh;
-    const uint8_t *tri_type;    // shading queue (bsdf_queue) of the triangle's mesh BSDF, 255 = no BSDF
+    const uint8_t *tri_type;    // shading queue (bsdf_queue_of) of the triangle's mesh BSDF, 255 = no BSDF
+    const float *tri_uv;        // 6 floats per triangle (uv0, uv1, uv2) or null; NaN: mesh without uvs
+    const DevTexture *textures;
+    int n_textures;
+    int has_textured;           // some BSDF is textured (the mixed shading queue is in use)
     const DevMesh *meshes;
     const float *mesh_cdf;
     int n_meshes;
@@ -383,8 +407,9 @@ __device__ __forceinline__ int prim_type(const DevScene &S, int prim)
         return t == 255 ? -1 : t;
     }
     int b = S.spheres[-prim - 2].bsdf;
-    return b < 0 ? -1 : bsdf_queue(S.bsdfs[b].type);
+    return b < 0 ? -1 : bsdf_queue_of(S.bsdfs[b]);
 }
+
 __device__ __forceinline__ int prim_interior(const DevScene &S, int prim)
 {
     return prim >= 0 ? S.meshes[S.tri_mesh[prim]].interior : S.spheres[-prim - 2].interior;
@@ -464,6 +489,95 @@ __device__ __forceinline__ float spherical_phi(V3 v)
     return r < 0.f ? r + 2 * (float)3.14159265358979323846 : r;
 }
 __device__ __forceinline__ float spherical_theta(V3 v) { return acosf(v.y); }
+
+// ------------------------------------------------------------------ textures
+// Texture coordinates of a hit (Intersection::myUv): a triangle's vertex uvs
+// interpolated with the barycentrics (Triangle.cpp:155-164), or the
+// barycentric (u, v) themselves for a mesh without uvs (Triangle::intersection
+// leaves them in myUv); a sphere's spherical angles of the object-space hit
+// point (Sphere.cpp:98-104).
+__device__ __forceinline__ V2 hit_uv(const DevScene &S, const Hit &h, V3 o, V3 d)
+{
+    if (h.prim >= 0) {
+        if (S.tri_uv) {
+            const float *q = S.tri_uv + 6 * (size_t)h.prim;
+            if (!isnan(q[0])) {
+                const float b0 = 1.f - (h.u + h.v);
+                return v2((b0 * q[0] + h.u * q[2]) + h.v * q[4], (b0 * q[1] + h.u * q[3]) + h.v * q[5]);
+            }
+        }
+        return v2(h.u, h.v);
+    }
+    const DevSphere &sp = S.spheres[-h.prim - 2];
+    V3 lo = xf_point(sp.to_object, o), ld = xf_vector(sp.to_object, d);
+    V3 n = normalized(lo + h.t * ld);
+    return v2(spherical_phi(n) / (2 * RT_PI), spherical_theta(n) / RT_PI);
+}
+
+__device__ __forceinline__ int tex_clamp(int v, int lo, int hi) { return v < lo ? lo : v > hi ? hi : v; }
+__device__ __forceinline__ C3 tex_texel(const DevTexture &T, int x, int y)
+{
+    const float *p = T.rgb + 3 * ((size_t)y * T.w + x);
+    return c3(__ldg(p), __ldg(p + 1), __ldg(p + 2));
+}
+// math::interp2 (core/BasicMath.h:73-90).  A texture one texel wide (high)
+// has an empty clamp range there, where the reference reads index -1; here
+// the index stays 0.
+__device__ __forceinline__ C3 tex_interp2(const DevTexture &T, float x, float y)
+{
+    const float ax = x - (float)(int)x, ay = y - (float)(int)y;
+    int x0 = T.w < 2 ? 0 : tex_clamp((int)x, 0, T.w - 2);
+    int y0 = T.h < 2 ? 0 : tex_clamp((int)y, 0, T.h - 2);
+    int x1 = tex_clamp(x0 + 1 < T.w ? x0 + 1 : x0, 0, T.w - 1);
+    int y1 = tex_clamp(y0 + 1 < T.h ? y0 + 1 : y0, 0, T.h - 1);
+    C3 r = ((1.f - ax) * (1.f - ay)) * tex_texel(T, x0, y0);
+    r = r + ((1.f - ax) * ay) * tex_texel(T, x0, y1);
+    r = r + (ax * (1.f - ay)) * tex_texel(T, x1, y0);
+    return r + (ax * ay) * tex_texel(T, x1, y1);
+}
+__device__ __forceinline__ float tex_sign(float v) { return v >= 0.f ? 1.f : -1.f; }
+// ImageTexture::eval (ImageTexture.cpp:28-70): x spans width - 1 and y spans
+// height; invertX / invertY flip within the unit tile; scale repeats; values
+// outside [0, size) wrap.
+__device__ __noinline__ C3 tex_eval(const DevTexture &T, V2 uv)
+{
+    const float W = (float)T.w, H = (float)T.h;
+    float x, y;
+    if (!T.invert_y) y = uv.y * H;
+    else y = (float)(int)uv.y + (tex_sign(uv.y) * 1.f - (uv.y - (float)(int)uv.y)) * H;
+    if (!T.invert_x) x = uv.x * (W - 1.f);
+    else x = (float)(int)uv.x + (tex_sign(uv.x) * 1.f - (uv.x - (float)(int)uv.x)) * W;
+    x *= T.scale;
+    y *= T.scale;
+    if (x >= W) x = (float)((unsigned)(int)x % (unsigned)T.w) + (x - (float)(int)x);
+    else if (x < 0.f) x = (float)((unsigned)T.w - (unsigned)abs((int)x) % (unsigned)T.w) + (x - (float)(int)x);
+    if (y >= H) y = (float)((unsigned)(int)y % (unsigned)T.h) + (y - (float)(int)y);
+    else if (y < 0.f) y = (float)((unsigned)T.h - (unsigned)abs((int)y) % (unsigned)T.h) + (y - (float)(int)y);
+    return tex_interp2(T, x, y);
+}
+// The BSDF parameters at a hit: textured ones replaced by their texture's
+// value at uv (an alpha texture by the average of its channels, as the
+// rough BSDFs read it).
+__device__ __noinline__ void tex_apply(const DevScene &S, DevBsdf &b, V2 uv)
+{
+    if (b.tex[TEX_ALBEDO] >= 0) {
+        C3 c = tex_eval(S.textures[b.tex[TEX_ALBEDO]], uv);
+        b.albedo[0] = c.r; b.albedo[1] = c.g; b.albedo[2] = c.b;
+    }
+    if (b.tex[TEX_REFLECTANCE] >= 0) {
+        C3 c = tex_eval(S.textures[b.tex[TEX_REFLECTANCE]], uv);
+        b.reflectance[0] = c.r; b.reflectance[1] = c.g; b.reflectance[2] = c.b;
+    }
+    if (b.tex[TEX_TRANSMITTANCE] >= 0) {
+        C3 c = tex_eval(S.textures[b.tex[TEX_TRANSMITTANCE]], uv);
+        b.transmittance[0] = c.r; b.transmittance[1] = c.g; b.transmittance[2] = c.b;
+    }
+    if (b.tex[TEX_ALPHA] >= 0) {
+        float a = cavg(tex_eval(S.textures[b.tex[TEX_ALPHA]], uv));
+        b.alpha = a;
+        b.alpha_avg = a;
+    }
+}
 __device__ __forceinline__ V3 cartesian_from_spherical(float theta, float phi)
 {
     float st = sinf(theta), ct = cosf(theta), cp = cosf(phi), sp = sinf(phi);

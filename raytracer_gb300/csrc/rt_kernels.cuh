@@ -10,8 +10,9 @@ namespace rtgpu {
 // path flags
 enum { F_FIRST = 1, F_DELTA = 2, F_NEE = 4, F_END = 8, F_DONE = 16 };
 
-#define RT_NBSDF 6        // shading queues (bsdf_queue): types 0-4, then the delta types
-#define RT_QUEUE_MIXED 6  // one more queue: every BSDF type, for rounds below the sort threshold
+#define RT_NBSDF 6        // sorted shading queues (bsdf_queue): types 0-4, then the delta types;
+                          // RT_QUEUE_MIXED (rt_device.cuh) is one more: textured BSDFs, and
+                          // every BSDF in bounces below the sort threshold
 
 struct RoundCounters {   // one per wavefront round, zeroed per batch
     int closest, shadow, wc_closest, wc_shadow;

@@ -38,7 +38,13 @@ class BsdfDesc(C.Structure):
                 ("alpha", C.c_float), ("eta_int", C.c_float), ("eta_ext", C.c_float),
                 ("thickness", C.c_float), ("absorbance", f3),
                 ("distribution_base", C.c_int32), ("alpha_base", C.c_float),
-                ("two_sided", C.c_int32)]
+                ("two_sided", C.c_int32), ("tex_albedo", C.c_int32), ("tex_reflectance", C.c_int32),
+                ("tex_transmittance", C.c_int32), ("tex_alpha", C.c_int32)]
+
+
+class TextureDesc(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("rgb", C.POINTER(C.c_float)),
+                ("scale", C.c_float), ("invert_x", C.c_int32), ("invert_y", C.c_int32)]
 
 
 class MeshDesc(C.Structure):
@@ -83,7 +89,8 @@ class SceneDesc(C.Structure):
                 ("bsdfs", C.POINTER(BsdfDesc)), ("n_lights", C.c_int32),
                 ("lights", C.POINTER(LightDesc)), ("env_light", C.c_int32),
                 ("n_media", C.c_int32), ("media", C.POINTER(MediumDesc)),
-                ("camera", CameraDesc)]
+                ("camera", CameraDesc), ("n_textures", C.c_int32), ("textures", C.POINTER(TextureDesc)),
+                ("uvs", C.POINTER(C.c_float))]
 
 
 class RenderDesc(C.Structure):
@@ -165,7 +172,9 @@ def bsdf(kind, **kw):
     alphaTop 0.01, over a default RoughConductor: beckmann, alpha 0.2,
     eta = k = 0; Dielectric.cpp:10-17, Conductor.cpp:13-21, Mirror.cpp:7-15).
     two_sided=True wraps it in a TwoSides (TwoSides.cpp:5-15) with the same
-    BSDF on both sides."""
+    BSDF on both sides.  tex_albedo, tex_reflectance, tex_transmittance and
+    tex_alpha name a texture of the scene (SceneData.add_texture) that
+    replaces that parameter (None: the constant)."""
     layered = kind == BSDF_LAYERED
     d = dict(type=kind, distribution=kw.get("distribution", DIST_GGX if layered else DIST_BECKMANN),
              albedo=kw.get("albedo", (0.5, 0.5, 0.5)),
@@ -177,7 +186,13 @@ def bsdf(kind, **kw):
              absorbance=kw.get("absorbance", (0.0, 0.0, 0.0)),
              distribution_base=kw.get("distribution_base", DIST_BECKMANN),
              alpha_base=kw.get("alpha_base", 0.2), two_sided=bool(kw.get("two_sided", False)))
+    for k in TEX_PARAMS:
+        if kw.get(k) is not None:
+            d[k] = int(kw[k])
     return d
+
+
+TEX_PARAMS = ("tex_albedo", "tex_reflectance", "tex_transmittance", "tex_alpha")
 
 
 def bsdf_struct(b):
@@ -186,7 +201,8 @@ def bsdf_struct(b):
                     f3(*b["transmittance"]), f3(*b["eta"]), f3(*b["k"]), b["alpha"],
                     b["eta_int"], b["eta_ext"], b["thickness"], f3(*b["absorbance"]),
                     b.get("distribution_base", DIST_BECKMANN), b.get("alpha_base", 0.2),
-                    int(bool(b.get("two_sided", False))))
+                    int(bool(b.get("two_sided", False))),
+                    *[0 if b.get(k) is None else int(b[k]) + 1 for k in TEX_PARAMS])
 
 
 class SceneData:
@@ -195,6 +211,8 @@ class SceneData:
     def __init__(self):
         self.vertices = np.zeros((0, 3), np.float32)
         self.normals = None
+        self.uvs = None      # per-vertex texture coordinates (NaN: mesh without)
+        self.textures = []   # dict(rgb (H, W, 3), scale, invert_x, invert_y)
         self.indices = np.zeros((0, 3), np.int32)
         self.meshes = []     # dict(first_tri, n_tris, bsdf, light, interior, exterior)
         self.spheres = []    # dict(radius, to_world, bsdf, light, interior, exterior)
@@ -213,7 +231,16 @@ class SceneData:
         self.bsdfs.append(d)
         return len(self.bsdfs) - 1
 
-    def add_mesh(self, verts, tris, bsdf=-1, light=-1, interior=-1, exterior=-1, normals=None):
+    def add_texture(self, rgb, scale=1.0, invert_x=False, invert_y=False):
+        """An ImageTexture: `rgb` an (H, W, 3) linear image; returns its index."""
+        rgb = np.ascontiguousarray(rgb, np.float32)
+        if rgb.ndim != 3 or rgb.shape[2] != 3 or rgb.shape[0] < 1 or rgb.shape[1] < 1:
+            raise ValueError("texture: expected an (H, W, 3) image")
+        self.textures.append(dict(rgb=rgb, scale=abs(float(scale)), invert_x=bool(invert_x),
+                                  invert_y=bool(invert_y)))
+        return len(self.textures) - 1
+
+    def add_mesh(self, verts, tris, bsdf=-1, light=-1, interior=-1, exterior=-1, normals=None, uvs=None):
         verts = np.asarray(verts, np.float32).reshape(-1, 3)
         tris = np.asarray(tris, np.int32).reshape(-1, 3)
         base = len(self.vertices)
@@ -228,6 +255,13 @@ class SceneData:
             self.normals = np.concatenate([self.normals, np.asarray(normals, np.float32).reshape(-1, 3)])
         elif self.normals is not None:
             self.normals = np.concatenate([self.normals, np.full((len(verts), 3), np.nan, np.float32)])
+        # texture coordinates likewise: NaN for the vertices of meshes without
+        if uvs is not None:
+            if self.uvs is None:
+                self.uvs = np.full((base, 2), np.nan, np.float32)
+            self.uvs = np.concatenate([self.uvs, np.asarray(uvs, np.float32).reshape(-1, 2)])
+        elif self.uvs is not None:
+            self.uvs = np.concatenate([self.uvs, np.full((len(verts), 2), np.nan, np.float32)])
         self.meshes.append(dict(first_tri=first, n_tris=len(tris), bsdf=bsdf, light=light,
                                 interior=interior, exterior=exterior))
         return len(self.meshes) - 1
@@ -350,7 +384,16 @@ class SceneData:
                               c.get("aperture_radius", 0.0), c.get("focal_plane", 1e8),
                               c.get("medium", -1), flt["type"], (C.c_float * 2)(*flt["radius"]),
                               (C.c_float * 2)(*flt["param"]))
-        keep += [meshes, spheres, bs, ls, ms]
+        tx = (TextureDesc * max(1, len(self.textures)))()
+        for i, t in enumerate(self.textures):
+            keep.append(t["rgb"])
+            tx[i] = TextureDesc(t["rgb"].shape[1], t["rgb"].shape[0], _fp(t["rgb"]), t.get("scale", 1.0),
+                                int(t.get("invert_x", False)), int(t.get("invert_y", False)))
+        D.n_textures = len(self.textures)
+        D.textures = C.cast(tx, C.POINTER(TextureDesc))
+        uv = None if self.uvs is None else np.ascontiguousarray(self.uvs, np.float32)
+        D.uvs = _fp(uv) if uv is not None else None
+        keep += [meshes, spheres, bs, ls, ms, tx, uv]
         self._keep = keep
         return D
 

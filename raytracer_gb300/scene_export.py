@@ -15,6 +15,7 @@ import struct
 import numpy as np
 
 from . import desc as D
+from .exr import write_exr
 
 _BSDF_NAMES = {D.BSDF_DIFFUSE: "Diffuse", D.BSDF_ROUGH_CONDUCTOR: "RoughConductor",
                D.BSDF_ROUGH_DIELECTRIC: "RoughDielectric", D.BSDF_SMOOTH_LAYERED: "SmoothLayeredBSDF",
@@ -73,17 +74,24 @@ def write_vol(path, density, lo=(0, 0, 0), hi=(1, 1, 1)):
         f.write(d.tobytes())
 
 
-def _write_obj(path, v, n, t):
+def _write_obj(path, v, n, t, uv=None):
     with open(path, "w") as f:
         for p in v:
             f.write("v %s\n" % _c(p))
+        if uv is not None:
+            for q in uv:
+                f.write("vt %s %s\n" % (_f(q[0]), _f(q[1])))
         if n is not None:
             for q in n:
                 f.write("vn %s\n" % _c(q))
-            for a, b, c in t + 1:
+        for a, b, c in t + 1:
+            if n is not None and uv is not None:
+                f.write("f %d/%d/%d %d/%d/%d %d/%d/%d\n" % (a, a, a, b, b, b, c, c, c))
+            elif n is not None:
                 f.write("f %d//%d %d//%d %d//%d\n" % (a, a, b, b, c, c))
-        else:
-            for a, b, c in t + 1:
+            elif uv is not None:
+                f.write("f %d/%d %d/%d %d/%d\n" % (a, a, b, b, c, c))
+            else:
                 f.write("f %d %d %d\n" % (a, b, c))
 
 
@@ -92,44 +100,60 @@ def _tex_xml(pad, name, c):
             % (pad, name, _c(c)))
 
 
-def _bsdf_xml(b, indent):
+def _bsdf_xml(b, indent, tex=()):
+    """`tex`: per scene texture, the inner XML of its ImageTexture element."""
     pad = " " * indent
+
+    def image(name, key):
+        return '%s  <texture name="%s" type="ImageTexture">%s</texture>' % (pad, name, tex[b[key]])
+
+    def refl_trans(names):
+        out = []
+        for name, key, tkey in names:
+            if b.get(tkey) is not None:
+                out.append(image(name, tkey))
+            elif tuple(b[key]) != (1.0, 1.0, 1.0):
+                out.append(_tex_xml(pad, name, b[key]))
+        return out
+
+    def alpha_line():
+        if b.get("tex_alpha") is not None:
+            return image("alpha", "tex_alpha")
+        return '%s  <double name="alpha" value="%s"/>' % (pad, _f(b["alpha"]))
+
     if b.get("two_sided"):
-        inner = _bsdf_xml(dict(b, two_sided=False), indent + 2)
+        inner = _bsdf_xml(dict(b, two_sided=False), indent + 2, tex)
         inner[0] = inner[0].replace('<bsdf type=', '<bsdf name="bsdf" type=')
         return ['%s<bsdf type="TwoSides">' % pad] + inner + ["%s</bsdf>" % pad]
     name = _BSDF_NAMES[b["type"]]
     lines = ['%s<bsdf type="%s">' % (pad, name)]
+    refl = ("reflectanceTexture", "reflectance", "tex_reflectance")
+    trans = ("transmittedTexture", "transmittance", "tex_transmittance")
     if b["type"] == D.BSDF_DIFFUSE:
-        lines.append('%s  <color name="albedo" value="%s"/>' % (pad, _c(b["albedo"])))
+        if b.get("tex_albedo") is not None:
+            lines.append(image("albedo", "tex_albedo"))
+        else:
+            lines.append('%s  <color name="albedo" value="%s"/>' % (pad, _c(b["albedo"])))
     elif b["type"] == D.BSDF_ROUGH_CONDUCTOR:
         lines += ['%s  <color name="eta" value="%s"/>' % (pad, _c(b["eta"])),
                   '%s  <color name="absorption" value="%s"/>' % (pad, _c(b["k"])),
-                  '%s  <double name="alpha" value="%s"/>' % (pad, _f(b["alpha"])),
+                  alpha_line(),
                   '%s  <string name="distribution" value="%s"/>' % (pad, _DIST_NAMES[b["distribution"]])]
-        if tuple(b["reflectance"]) != (1.0, 1.0, 1.0):
-            lines.append(_tex_xml(pad, "reflectanceTexture", b["reflectance"]))
+        lines += refl_trans([refl])
     elif b["type"] == D.BSDF_ROUGH_DIELECTRIC:
-        lines += ['%s  <double name="alpha" value="%s"/>' % (pad, _f(b["alpha"])),
+        lines += [alpha_line(),
                   '%s  <double name="etaInt" value="%s"/>' % (pad, _f(b["eta_int"])),
                   '%s  <double name="etaExt" value="%s"/>' % (pad, _f(b["eta_ext"])),
                   '%s  <string name="distribution" value="%s"/>' % (pad, _DIST_NAMES[b["distribution"]])]
-        if tuple(b["reflectance"]) != (1.0, 1.0, 1.0):
-            lines.append(_tex_xml(pad, "reflectanceTexture", b["reflectance"]))
-        if tuple(b["transmittance"]) != (1.0, 1.0, 1.0):
-            lines.append(_tex_xml(pad, "transmittedTexture", b["transmittance"]))
+        lines += refl_trans([refl, trans])
     elif b["type"] == D.BSDF_DIELECTRIC:
         lines += ['%s  <double name="etaInt" value="%s"/>' % (pad, _f(b["eta_int"])),
                   '%s  <double name="etaExt" value="%s"/>' % (pad, _f(b["eta_ext"]))]
-        if tuple(b["reflectance"]) != (1.0, 1.0, 1.0):
-            lines.append(_tex_xml(pad, "reflectanceTexture", b["reflectance"]))
-        if tuple(b["transmittance"]) != (1.0, 1.0, 1.0):
-            lines.append(_tex_xml(pad, "transmittedTexture", b["transmittance"]))
+        lines += refl_trans([refl, trans])
     elif b["type"] == D.BSDF_CONDUCTOR:
         lines += ['%s  <color name="eta" value="%s"/>' % (pad, _c(b["eta"])),
                   '%s  <color name="absorption" value="%s"/>' % (pad, _c(b["k"]))]
-        if tuple(b["reflectance"]) != (1.0, 1.0, 1.0):
-            lines.append(_tex_xml(pad, "reflectanceTexture", b["reflectance"]))
+        lines += refl_trans([refl])
     elif b["type"] == D.BSDF_MIRROR:
         pass
     elif b["type"] == D.BSDF_SMOOTH_LAYERED:
@@ -142,7 +166,7 @@ def _bsdf_xml(b, indent):
     else:
         base = dict(b, type=D.BSDF_ROUGH_CONDUCTOR, distribution=b.get("distribution_base", D.DIST_BECKMANN),
                     alpha=b.get("alpha_base", 0.2))
-        inner = _bsdf_xml(base, indent + 2)
+        inner = _bsdf_xml(base, indent + 2, tex)
         inner[0] = inner[0].replace('<bsdf type=', '<bsdf name="baseBSDF" type=')
         lines += ['%s  <double name="etaInt" value="%s"/>' % (pad, _f(b["eta_int"])),
                   '%s  <double name="etaExt" value="%s"/>' % (pad, _f(b["eta_ext"])),
@@ -240,6 +264,16 @@ def write_scene(scene, folder, spp=1, name="scene"):
     env_first = s.env_light == 0
     if env_first:
         out += env_lines
+    # textures: half-float OpenEXR files, which the reference reads linearly
+    # (ImageLoader.cpp:46-74), so their texels are quantised to half
+    tex = []
+    for ti, T in enumerate(getattr(s, "textures", [])):
+        name = "tex%d.exr" % ti
+        write_exr(os.path.join(folder, name), T["rgb"][::1])
+        tex.append('<string name="path" value="%s"/><double name="scale" value="%s"/>'
+                   '<bool name="invertX" value="%s"/><bool name="invertY" value="%s"/>'
+                   % (name, _f(T.get("scale", 1.0)), "true" if T.get("invert_x") else "false",
+                      "true" if T.get("invert_y") else "false"))
     out.append("  <objects>")
     for mi, m in enumerate(s.meshes):
         a, b = m["first_tri"], m["first_tri"] + m["n_tris"]
@@ -249,11 +283,15 @@ def write_scene(scene, folder, spp=1, name="scene"):
         n = None
         if s.normals is not None and not np.isnan(s.normals[used]).any():
             n = s.normals[used]
+        uv = None
+        uvs = getattr(s, "uvs", None)
+        if uvs is not None and not np.isnan(uvs[used]).any():
+            uv = uvs[used]
         obj = "mesh%d.obj" % mi
-        _write_obj(os.path.join(folder, obj), v, n, remap.reshape(-1, 3).astype(np.int64))
+        _write_obj(os.path.join(folder, obj), v, n, remap.reshape(-1, 3).astype(np.int64), uv)
         out += ['    <shape type="Mesh">', '      <string name="path" value="%s"/>' % obj]
         if m["bsdf"] >= 0:
-            out += _bsdf_xml(s.bsdfs[m["bsdf"]], 6)
+            out += _bsdf_xml(s.bsdfs[m["bsdf"]], 6, tex)
         if m["light"] >= 0:
             L = s.lights[m["light"]]
             out.append('      <light type="%s"><color name="radiance" value="%s"/></light>'
@@ -266,7 +304,7 @@ def write_scene(scene, folder, spp=1, name="scene"):
         out += ['    <shape type="Sphere">', '      <double name="radius" value="%s"/>' % _f(sp["radius"]),
                 '      <transform name="toWorld"><matrix value="%s"/></transform>' % _matrix(sp["to_world"])]
         if sp["bsdf"] >= 0:
-            out += _bsdf_xml(s.bsdfs[sp["bsdf"]], 6)
+            out += _bsdf_xml(s.bsdfs[sp["bsdf"]], 6, tex)
         if sp["light"] >= 0:
             L = s.lights[sp["light"]]
             out.append('      <light type="%s"><color name="radiance" value="%s"/></light>'

@@ -215,6 +215,78 @@ def cornell_smooth(width=128, height=128, max_depth=12):
     return s
 
 
+def texture_image(width, height, seed=0, kind="checker"):
+    """A seeded test image (H, W, 3) in [0, 1], rounded to half precision (so
+    that an OpenEXR copy of it is exact): "checker" squares with a colour
+    gradient, or "noise" (value noise)."""
+    y, x = np.mgrid[0:height, 0:width].astype(np.float64)
+    if kind == "checker":
+        sq = ((x // 4 + y // 4) % 2)[..., None]
+        grad = np.stack([x / max(1, width - 1), y / max(1, height - 1), 0.5 + 0 * x], axis=2)
+        img = 0.15 + 0.7 * (0.6 * sq + 0.4 * grad)
+    else:
+        p = np.stack([x / 8.0, y / 8.0, np.full_like(x, 0.37)], axis=-1).reshape(-1, 3)
+        v = value_noise(p, seed).reshape(height, width)
+        img = np.repeat((0.5 + 0.5 * v)[..., None], 3, axis=2) * np.array([1.0, 0.8, 0.6])
+    return np.clip(img, 0.0, 1.0).astype(np.float16).astype(np.float32)
+
+
+def textured_room(width=96, height=96, max_depth=10):
+    """The Cornell-box room with ImageTextures on every kind of parameter and
+    every kind of texture coordinates: uv-mapped walls (repeated albedo), a
+    left wall without uvs (barycentric coordinates, inverted texture), a
+    RoughConductor tall box with alpha and reflectance textures, a
+    RoughDielectric short box with a transmittance texture, a sphere with a
+    textured Diffuse albedo (spherical coordinates) and a one-texel and a
+    two-by-two texture."""
+    from .desc import BSDF_CONDUCTOR
+    s = SceneData()
+    s.name = "textured_room_%d" % width
+    checker = s.add_texture(texture_image(64, 48, 0, "checker"), scale=3.0)
+    noise = s.add_texture(texture_image(32, 32, 1, "noise"))
+    tiny = s.add_texture(np.array([[[0.8, 0.4, 0.2]]], np.float16).astype(np.float32))
+    two = s.add_texture(np.array([[[0.9, 0.1, 0.1], [0.1, 0.9, 0.1]], [[0.1, 0.1, 0.9], [0.9, 0.9, 0.1]]],
+                                 np.float16).astype(np.float32), invert_x=True, invert_y=True)
+    walls = s.add_bsdf(bsdf(BSDF_DIFFUSE, tex_albedo=checker))
+    left = s.add_bsdf(bsdf(BSDF_DIFFUSE, tex_albedo=two))
+    green = s.add_bsdf(bsdf(BSDF_DIFFUSE, albedo=(0.12, 0.45, 0.15)))
+    metal = s.add_bsdf(bsdf(BSDF_ROUGH_CONDUCTOR, distribution=DIST_GGX, eta=AU_ETA, k=AU_K, tex_alpha=noise,
+                            tex_reflectance=checker))
+    glass = s.add_bsdf(bsdf(BSDF_ROUGH_DIELECTRIC, distribution=DIST_GGX, alpha=0.15, eta_int=1.5,
+                            tex_transmittance=noise))
+    ball = s.add_bsdf(bsdf(BSDF_DIFFUSE, tex_albedo=checker))
+    mirror_ball = s.add_bsdf(bsdf(BSDF_CONDUCTOR, eta=AU_ETA, k=AU_K, tex_reflectance=tiny))
+    lightmat = s.add_bsdf(bsdf(BSDF_DIFFUSE, albedo=(0.78, 0.78, 0.78)))
+    quad_uv = np.array([(0, 0), (1, 0), (1, 1), (0, 1)], np.float32)
+    fl = _quad((0, 0, 0), (0, 0, 1), (1, 0, 1), (1, 0, 0))
+    ce = _quad((0, 1, 0), (1, 1, 0), (1, 1, 1), (0, 1, 1))
+    bk = _quad((0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0))
+    s.add_mesh(np.concatenate([fl[0], ce[0], bk[0]]), np.concatenate([fl[1], ce[1] + 4, bk[1] + 8]), bsdf=walls,
+               uvs=np.concatenate([quad_uv, quad_uv, quad_uv]))
+    s.add_mesh(*_quad((0, 0, 0), (0, 1, 0), (0, 1, 1), (0, 0, 1)), bsdf=left)
+    s.add_mesh(*_quad((1, 0, 0), (1, 0, 1), (1, 1, 1), (1, 1, 0)), bsdf=green)
+    tv, tf = _box((0.33, 0.3, 0.37), (0.3, 0.6, 0.3), 15.0)
+    s.add_mesh(tv, tf, bsdf=metal)
+    sv, sf = _box((0.66, 0.15, 0.65), (0.3, 0.3, 0.3), -18.0)
+    s.add_mesh(sv, sf, bsdf=glass)
+    T = np.eye(4)
+    T[:3, 3] = (0.22, 0.1, 0.78)
+    T[:3, :3] = np.array([[1, 0, 0], [0, 0, -1], [0, 1, 0]])   # a pole and the uv seam toward the camera
+    s.add_sphere(0.1, T, bsdf=ball)
+    T2 = np.eye(4)
+    T2[:3, 3] = (0.7, 0.42, 0.62)
+    s.add_sphere(0.08, T2, bsdf=mirror_ball)
+    h = 0.999
+    lv, lfc = _quad((0.375, h, 0.375), (0.625, h, 0.375), (0.625, h, 0.625), (0.375, h, 0.625))
+    lm = s.add_mesh(lv, lfc, bsdf=lightmat)
+    li = s.add_area_light((17.0, 12.0, 4.0), SHAPE_MESH, lm, mesh_light=True)
+    s.meshes[lm]["light"] = li
+    s.camera = camera(width, height, 40.0, look_at((0.5, 0.5, 2.4), (0.5, 0.5, 0.0), (0, 1, 0)))
+    s.integrator = dict(integrator=INTEGRATOR_PATH_MIS, max_depth=max_depth, min_depth=3,
+                        strategy=STRATEGY_ONE_LIGHT_UNIFORM)
+    return s
+
+
 def displaced_icosphere(level=8, width=1024, height=1024, seed=0, alpha_bins=32,
                         env_size=(1024, 512), max_depth=16, env=None):
     """Config [1]: displaced icosphere on a ground quad under a sky (`env`:

@@ -141,6 +141,7 @@ class _Loader:
         self.s.name = os.path.splitext(os.path.basename(path))[0]
         self.ref_bsdf = {}
         self.ref_bsdf_name = {}   # id -> the element's name attribute (XMLLoader.cpp:108-114)
+        self.tex_cache = {}
         self.ref_transform = {}
         self.ref_medium = {}
         self.camera_params = None
@@ -184,10 +185,14 @@ class _Loader:
                 else:
                     params[name] = _transform(c)
             elif tag == "texture":
-                if c.get("type") != "ConstantTexture":
-                    raise UnsupportedScene("texture type %s is not provided" % c.get("type"))
+                kind = c.get("type")
                 tp = self.props(c)
-                params[name] = ("texture", tp.get("albedo", (0.5, 0.5, 0.5)))   # ConstantTexture.cpp:6-10
+                if kind == "ConstantTexture":
+                    params[name] = ("texture", tp.get("albedo", (0.5, 0.5, 0.5)))   # ConstantTexture.cpp:6-10
+                elif kind == "ImageTexture":
+                    params[name] = ("image", self.image_texture(tp))
+                else:
+                    raise UnsupportedScene("texture type %s is not provided" % kind)
             elif tag == "bsdf":
                 # a referenced BSDF keeps the name its <bsdf id=..> element
                 # gave it (XMLLoader.cpp:762-775)
@@ -210,21 +215,54 @@ class _Loader:
         v = params.get(name, default)
         if isinstance(v, tuple) and len(v) == 2 and v[0] == "texture":
             return tuple(v[1])
+        if isinstance(v, tuple) and len(v) == 2 and v[0] == "image":
+            return default
         return v
+
+    @staticmethod
+    def _image(params, name):
+        """The scene texture index of an ImageTexture parameter, else None."""
+        v = params.get(name)
+        if isinstance(v, tuple) and len(v) == 2 and v[0] == "image":
+            return v[1]
+        return None
+
+    def image_texture(self, tp):
+        """ImageTexture (ImageTexture.cpp:8-21): path, invertX/Y, scale
+        (absolute value), gamma, channel; boundaryCondition is parsed by the
+        reference but not used by its eval."""
+        from .images import ImageError, load_image
+        path = tp.get("path", "")
+        gamma, channel = float(tp.get("gamma", 0.0)), str(tp.get("channel", "all")).lower()
+        scale = abs(float(tp.get("scale", 1.0)))
+        ix, iy = bool(tp.get("invertX", False)), bool(tp.get("invertY", False))
+        # one texture per distinct image and settings (ImageLoader caches the
+        # image array by path and channel, ImageLoader.cpp:36-41)
+        key = (self.resolve(path), gamma, channel, scale, ix, iy)
+        if key in self.tex_cache:
+            return self.tex_cache[key]
+        try:
+            rgb = load_image(key[0], gamma=gamma, channel=channel)
+        except (ImageError, OSError) as e:
+            raise UnsupportedScene("ImageTexture %s: %s" % (path, e))
+        self.tex_cache[key] = self.s.add_texture(rgb, scale=scale, invert_x=ix, invert_y=iy)
+        return self.tex_cache[key]
 
     # BSDFs: returns the index in the scene's BSDF table
     def bsdf(self, el, params=None):
         kind = el.get("type")
         p = self.props(el) if params is None else params
         if kind == "Diffuse":   # Diffuse.cpp:11-18
-            b = D.bsdf(D.BSDF_DIFFUSE, albedo=self._tex_or(p, "albedo", (0.5, 0.5, 0.5)))
+            b = D.bsdf(D.BSDF_DIFFUSE, albedo=self._tex_or(p, "albedo", (0.5, 0.5, 0.5)),
+                       tex_albedo=self._image(p, "albedo"))
         elif kind == "RoughConductor":   # RoughConductor.cpp:13-30, tools/Common.cpp:56-81
             eta, k = self._conductor_ior(p)
             alpha = self._tex_or(p, "alpha", 0.2)
             if isinstance(alpha, tuple):
                 alpha = (alpha[0] + alpha[0] + alpha[0]) / 3.0
             b = D.bsdf(D.BSDF_ROUGH_CONDUCTOR, distribution=_dist(p.get("distribution", "beckmann")),
-                       alpha=alpha, eta=eta, k=k, reflectance=self._tex_or(p, "reflectanceTexture", (1.0, 1.0, 1.0)))
+                       alpha=alpha, eta=eta, k=k, reflectance=self._tex_or(p, "reflectanceTexture", (1.0, 1.0, 1.0)),
+                       tex_reflectance=self._image(p, "reflectanceTexture"), tex_alpha=self._image(p, "alpha"))
         elif kind == "RoughDielectric":   # RoughDielectric.cpp:13-32
             alpha = self._tex_or(p, "alpha", 0.2)
             if isinstance(alpha, tuple):
@@ -232,7 +270,9 @@ class _Loader:
             b = D.bsdf(D.BSDF_ROUGH_DIELECTRIC, distribution=_dist(p.get("distribution", "beckmann")),
                        alpha=alpha, eta_int=p.get("etaInt", 1.5046), eta_ext=p.get("etaExt", 1.000277),
                        reflectance=self._tex_or(p, "reflectanceTexture", (1.0, 1.0, 1.0)),
-                       transmittance=self._tex_or(p, "transmittedTexture", (1.0, 1.0, 1.0)))
+                       transmittance=self._tex_or(p, "transmittedTexture", (1.0, 1.0, 1.0)),
+                       tex_reflectance=self._image(p, "reflectanceTexture"),
+                       tex_transmittance=self._image(p, "transmittedTexture"), tex_alpha=self._image(p, "alpha"))
         elif kind == "SmoothLayeredBSDF":   # SmoothLayeredBSDF.cpp:12-28
             base = p.get("baseBSDF")
             albedo = (0.5, 0.5, 0.5)
@@ -240,6 +280,8 @@ class _Loader:
                 bd = self.s.bsdfs[base]
                 if bd["type"] != D.BSDF_DIFFUSE:
                     raise UnsupportedScene("SmoothLayeredBSDF over a non-Diffuse base is not provided")
+                if any(bd.get(k) is not None for k in D.TEX_PARAMS):
+                    raise UnsupportedScene("SmoothLayeredBSDF over a textured base is not provided")
                 albedo = bd["albedo"]
             b = D.bsdf(D.BSDF_SMOOTH_LAYERED, albedo=albedo, eta_int=p.get("etaInt", 1.5046),
                        eta_ext=p.get("etaExt", 1.000277), thickness=p.get("thickness", 1.2),
@@ -251,6 +293,8 @@ class _Loader:
                 bd = self.s.bsdfs[base]
                 if bd["type"] != D.BSDF_ROUGH_CONDUCTOR:
                     raise UnsupportedScene("LayeredBSDF over a non-RoughConductor base is not provided")
+                if any(bd.get(k) is not None for k in D.TEX_PARAMS):
+                    raise UnsupportedScene("LayeredBSDF over a textured base is not provided")
             b = D.bsdf(D.BSDF_LAYERED, distribution=_dist(p.get("distribution", "ggx")),
                        alpha=p.get("alphaTop", 0.01), eta_int=p.get("etaInt", 1.5046),
                        eta_ext=p.get("etaExt", 1.000277), thickness=p.get("thickness", 1.2),
@@ -259,11 +303,14 @@ class _Loader:
         elif kind == "Dielectric":   # Dielectric.cpp:10-17
             b = D.bsdf(D.BSDF_DIELECTRIC, eta_int=p.get("etaInt", 1.5046), eta_ext=p.get("etaExt", 1.000277),
                        reflectance=self._tex_or(p, "reflectanceTexture", (1.0, 1.0, 1.0)),
-                       transmittance=self._tex_or(p, "transmittedTexture", (1.0, 1.0, 1.0)))
+                       transmittance=self._tex_or(p, "transmittedTexture", (1.0, 1.0, 1.0)),
+                       tex_reflectance=self._image(p, "reflectanceTexture"),
+                       tex_transmittance=self._image(p, "transmittedTexture"))
         elif kind == "Conductor":   # Conductor.cpp:13-21, tools/Common.cpp:56-81
             eta, k = self._conductor_ior(p)
             b = D.bsdf(D.BSDF_CONDUCTOR, eta=eta, k=k,
-                       reflectance=self._tex_or(p, "reflectanceTexture", (1.0, 1.0, 1.0)))
+                       reflectance=self._tex_or(p, "reflectanceTexture", (1.0, 1.0, 1.0)),
+                       tex_reflectance=self._image(p, "reflectanceTexture"))
         elif kind == "Mirror":   # Mirror.cpp:7-15
             b = D.bsdf(D.BSDF_MIRROR)
         elif kind == "TwoSides":   # TwoSides.cpp:5-15
@@ -354,10 +401,12 @@ class _Loader:
                 if p.get("useMtl", False):
                     raise UnsupportedScene("useMtl (OBJ materials) is not provided")
                 from .core import load_obj
-                v, n, _, t = load_obj(self.resolve(p.get("path", "")), to_world)
+                v, n, uv, t = load_obj(self.resolve(p.get("path", "")), to_world)
+                if uv is not None and len(uv) < 3:   # Triangle.cpp:155 uses uvs from three on
+                    uv = None
             else:
-                v, n, t = cube_mesh(to_world)
-            mi = self.s.add_mesh(v, t, bsdf=bsdf, interior=interior, exterior=exterior, normals=n)
+                v, n, uv, t = cube_mesh(to_world)
+            mi = self.s.add_mesh(v, t, bsdf=bsdf, interior=interior, exterior=exterior, normals=n, uvs=uv)
             if light is not None:   # MeshFactory.h:88-114
                 li = self.s.add_area_light(light[1].get("radiance", (0.0, 0.0, 0.0)), D.SHAPE_MESH, mi,
                                            mesh_light=light[0] == "MeshLight")
@@ -485,8 +534,9 @@ def _dist(name):
 
 def cube_mesh(to_world):
     """The Cube shape's mesh (geometricShape/Cube.cpp): the [-1, 1]^3 cube as
-    six faces of four vertices with face normals, two triangles per face,
-    in the reference's face and vertex order, transformed to world."""
+    six faces of four vertices with face normals and uvs (0,1) (1,1) (1,0)
+    (0,0), two triangles per face, in the reference's face and vertex order,
+    transformed to world.  Returns (vertices, normals, uvs, triangles)."""
     faces = [  # (normal axis, sign, four corners)
         ((0, -1, 0), [(1, -1, -1), (1, -1, 1), (-1, -1, 1), (-1, -1, -1)]),
         ((0, 1, 0), [(1, 1, -1), (-1, 1, -1), (-1, 1, 1), (1, 1, 1)]),
@@ -497,8 +547,9 @@ def cube_mesh(to_world):
     ]
     M = np.asarray(to_world, F32)
     NI = np.linalg.inv(M[:3, :3].astype(np.float64)).T.astype(F32)
-    v, n, t = [], [], []
+    v, n, uv, t = [], [], [], []
     for f, (nrm, quad) in enumerate(faces):
+        uv += [(0, 1), (1, 1), (1, 0), (0, 0)]
         for q in quad:
             p = np.asarray(q, F32)
             x = ((M[0, 0] * p[0] + M[0, 1] * p[1]) + M[0, 2] * p[2]) + M[0, 3]
@@ -511,7 +562,7 @@ def cube_mesh(to_world):
             n.append(NI @ np.asarray(nrm, F32))
         b = 4 * f
         t += [(b, b + 1, b + 2), (b + 3, b, b + 2)]
-    return np.asarray(v, F32), np.asarray(n, F32), np.asarray(t, np.int32)
+    return np.asarray(v, F32), np.asarray(n, F32), np.asarray(uv, F32), np.asarray(t, np.int32)
 
 
 def load_vol(path):

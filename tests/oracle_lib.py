@@ -44,6 +44,7 @@ def lib():
                                               C.c_void_p, C.c_void_p, C.c_void_p]
         L.oracle_cdf_sample.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]
         L.oracle_camera_rays.argtypes = [C.POINTER(D.SceneDesc), C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]
+        L.oracle_tex_eval.argtypes = [C.POINTER(D.TextureDesc), C.c_void_p, C.c_int32, C.c_void_p]
         _lib = L
     return _lib
 
@@ -131,6 +132,17 @@ class OracleScene:
         ln = None if lens is None else np.ascontiguousarray(lens, np.float32)
         lib().oracle_camera_rays(C.byref(self.desc), _p(pxy), None if ln is None else _p(ln), len(pxy), _p(out))
         return out
+
+
+def tex_eval(rgb, uv, scale=1.0, invert_x=False, invert_y=False):
+    """The oracle's ImageTexture::eval of an (H, W, 3) image at (n, 2) uvs."""
+    rgb = np.ascontiguousarray(rgb, np.float32)
+    uv = np.ascontiguousarray(uv, np.float32)
+    t = D.TextureDesc(rgb.shape[1], rgb.shape[0], rgb.ctypes.data_as(C.POINTER(C.c_float)), scale,
+                      int(invert_x), int(invert_y))
+    out = np.zeros((len(uv), 3), np.float32)
+    lib().oracle_tex_eval(C.byref(t), _p(uv), len(uv), _p(out))
+    return out
 
 
 BSDF_Q = np.dtype([("wi", np.float32, 3), ("wo", np.float32, 3), ("u", np.float32, 2)])

@@ -38,7 +38,7 @@ def test_struct_layout_matches_header(tmp_path):
                "rt_light_desc": D.LightDesc, "rt_medium_desc": D.MediumDesc, "rt_camera_desc": D.CameraDesc,
                "rt_scene_desc": D.SceneDesc, "rt_render_desc": D.RenderDesc, "rt_ray": D.Ray, "rt_hit": D.Hit,
                "rt_bsdf_q": D.BsdfQ, "rt_bsdf_r": D.BsdfR, "rt_light_q": D.LightQ, "rt_light_r": D.LightR,
-               "rt_render_stats": D.RenderStats}
+               "rt_render_stats": D.RenderStats, "rt_texture_desc": D.TextureDesc}
     prog = ['#include <stdio.h>', '#include <stddef.h>', '#include "rtgpu.h"', "int main(void){"]
     for k in structs:
         prog.append('printf("%s %%zu\\n", sizeof(%s));' % (k, k))

@@ -443,6 +443,52 @@ def test_film_parity_smooth_bsdfs_volpath(ctx, rtlib):
     _film_parity(ctx, rtlib, s, 4, 37, max_bad=0.05)
 
 
+def test_film_parity_textured(ctx, rtlib, width):
+    """ImageTextures on Diffuse albedo, RoughConductor alpha and reflectance,
+    RoughDielectric transmittance and Conductor reflectance, looked up at
+    uv-mapped, barycentric and spherical texture coordinates (textured BSDFs
+    shade from the mixed queue)."""
+    _film_parity(ctx, rtlib, scenes.textured_room(48, 40), 4, 41, max_bad=0.03)
+
+
+def test_film_parity_textured_volpath(ctx, rtlib):
+    s = scenes.textured_room(40, 32)
+    m = s.add_medium(dict(type=D.MEDIUM_HOMOGENEOUS, phase=D.PHASE_ISOTROPIC, sigma_a=(0.5, 1.0, 2.0),
+                          sigma_s=(1.0, 1.0, 1.0), scale=2.0))
+    s.meshes[4]["interior"] = m
+    s.integrator = dict(s.integrator, integrator=D.INTEGRATOR_VOLPATH)
+    _film_parity(ctx, rtlib, s, 4, 43, max_bad=0.05)
+
+
+def test_textured_film_with_graphs_and_threshold(ctx, rtlib):
+    """The mixed queue holds textured hits besides the below-threshold
+    bounces; graph launches and the sort threshold leave the film as is."""
+    g = rtlib.Scene(ctx, scenes.textured_room(40, 32))
+    ref = g.render(4, seed=9)
+    before = ctx.get_tuning()
+    try:
+        ctx.set_tuning(graphs=1, sort_threshold=1 << 12)
+        assert np.array_equal(g.render(4, seed=9), ref)
+    finally:
+        ctx.set_tuning(**before)
+        g.close()
+
+
+def test_texture_validation(ctx, rtlib):
+    import raytracer_gb300 as R
+    s = scenes.textured_room(8, 8)
+    s.bsdfs[0]["tex_albedo"] = 99
+    with pytest.raises(R.RtError) as e:
+        R.Scene(ctx, s)
+    assert e.value.status == 1
+    s = scenes.textured_room(8, 8)
+    s.bsdfs.append(D.bsdf(D.BSDF_LAYERED, tex_alpha=0))   # LayeredBSDF reads no texture
+    s.meshes[2]["bsdf"] = len(s.bsdfs) - 1
+    with pytest.raises(R.RtError) as e:
+        R.Scene(ctx, s)
+    assert e.value.status == 5
+
+
 def test_film_parity_mixed_normals(ctx, rtlib):
     """One mesh with vertex normals (shading normals), the others without
     (NaN-marked, geometric normals), in one scene."""

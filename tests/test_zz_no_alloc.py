@@ -72,3 +72,15 @@ def test_static_tile_render_rejects_oversize(ctx, rtlib):
     with pytest.raises(R.RtError):
         g.render_tile_static(5, 0, film.data_ptr(), 1, seed=0, block=32)     # outside the job grid
     g.close()
+
+
+def test_static_tile_render_refuses_textured_scenes(ctx, rtlib):
+    """Textured BSDFs shade from the mixed queue, which the static scratch
+    layout does not hold: the call fails with RT_ERR_UNSUPPORTED."""
+    torch = pytest.importorskip("torch")
+    g = rtlib.Scene(ctx, scenes.textured_room(32, 32))
+    film = torch.zeros((32, 32, 4), dtype=torch.float32, device="cuda")
+    with pytest.raises(rtlib.RtError) as e:
+        g.render_tile_static(0, 0, film.data_ptr(), 2, seed=1, block=32)
+    assert e.value.status == 5
+    g.close()
