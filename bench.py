@@ -231,6 +231,7 @@ def run_gpu(args):
     ctx.set_ray_sort(args.ray_sort)
     if args.sort_threshold:
         ctx.set_tuning(sort_threshold=args.sort_threshold)
+    ctx.set_tuning(volpath_wavefront=args.volpath_wavefront)
     # counting pass (traversal statistics for the roofline; not timed)
     ctx.set_profiling(2)
     scene.render(8, seed=99, film=film.data_ptr())
@@ -375,6 +376,7 @@ def run_gpu(args):
                            "triangles": data.n_triangles,
                            "resolution": [W, H], "spp": spp, "bvh_width": args.bvh_width, "max_depth": CONFIG["max_depth"],
                            "graphs": args.graphs, "sort_threshold": args.sort_threshold, "filter": args.filter,
+                           "volpath_wavefront": args.volpath_wavefront,
                            "samples_per_step": samples_per_step, "parallelism": "replicas" if world > 1 else "single",
                            "l2": "inputs larger than L2 (scene %.0f MB on the device, path state %.1f GB per "
                                  "batch of %d paths)" % (info["device_bytes"] / 1e6, batch_paths * 205 / 1e9,
@@ -553,6 +555,8 @@ def main():
                     help="launch each wavefront batch as a CUDA graph (render and serve workloads)")
     ap.add_argument("--sort-threshold", type=int, default=0,
                     help="bounces with fewer closest-hit rays shade unsorted (0: always sorted by material)")
+    ap.add_argument("--volpath-wavefront", type=int, default=1, choices=[0, 1],
+                    help="VolPathTracing as a wavefront of kernels (1) or one persistent kernel (0)")
     ap.add_argument("--filter", default="box", choices=["box", "gaussian", "mitchell"],
                     help="reconstruction filter of the rendered scene (box: radius 0.5)")
     ap.add_argument("--rates", default="5,20,100", help="serve: arrival rates (jobs/s)")

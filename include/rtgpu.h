@@ -391,6 +391,9 @@ typedef struct rt_tuning {
                                     of per-material queues (0: always sorted) */
     int32_t lanes;               /* worker lanes of rt_batch_render, 1..16    */
     int32_t graphs;              /* one CUDA graph per batch, 0 or 1          */
+    int32_t volpath_wavefront;   /* VolPathTracing as a wavefront of kernels
+                                    over queues (1, the default) or as one
+                                    persistent kernel per path (0)            */
 } rt_tuning;
 rt_status rt_ctx_get_tuning(rt_ctx *ctx, rt_tuning *out);
 rt_status rt_ctx_set_tuning(rt_ctx *ctx, const rt_tuning *t);

@@ -1264,6 +1264,461 @@ __global__ void __launch_bounds__(128, RT_VOLPATH_MINB) k_volpath(RenderParams P
     if (limit) atomicExch(P.limit_flag, 1);
 }
 
+// ---------------------------------------------------------------- VolPathTracing wavefront
+// The same bounce loop as vol_step, split at its loops into kernels, each
+// over a queue of paths in HBM.  One round runs one vol_step of every live
+// path (a bounce, or a null-boundary crossing, which the reference also
+// runs as one pass of its loop):
+//   k_vw_trace   [trace queue]   closest hit of the path's ray (the trace that
+//                                ends vol_step / vol_start / a null crossing)
+//   k_vw_step    [step queue]    depth and guard, delta tracking through the
+//                                medium, then either the scatter point or the
+//                                surface (emission, null boundary, env miss),
+//                                and the light pick and sample of
+//                                sampleAttenuatedLightDirect
+//   k_vw_shadow  [shadow queue]  the light sample's transmittance
+//                                (evalTransmittance: traces through null
+//                                boundaries, ratio tracking in media)
+//   k_vw_sample  [sample queue]  the light sample's MIS contribution, the
+//                                phase or BSDF sample and the new ray
+//   k_vw_trsamp  [trsamp queue]  evalTransmittanceFromSampledBSDF along it
+//   k_vw_finish  [finish queue]  emission MIS of what the sampled ray found,
+//                                throughput, Russian roulette
+// Each path's draws come in the order of one uninterrupted vol_step, so a
+// path's radiance is the megakernel's.  The hit frame is not stored: it is
+// rebuilt from the hit, the origin of the ray segment that found it and the
+// path's direction (hit_frame), which is what the megakernel holds.  Queue
+// counts live in the round's RoundCounters: trace = closest, step = mat[0],
+// shadow = shadow, sample = mat[1], trsamp = mat[2], finish = mat[3]; the
+// next round's trace queue is the next counters' closest.
+enum { VF_FIRST = F_FIRST, VF_EMISSION = 2, VF_WAS = 4, VF_SCAT = 8, VF_NULLX = 16, VF_DELTA = 32, VF_NEWM = 64,
+       VF_HASVAL = 128, VF_GUARD_SHIFT = 8 };
+
+// Integrator::sampleAttenuatedLightDirect (Integrator.cpp:137-172) up to its
+// shadow ray: the light pick and sample.  Returns whether the shadow ray's
+// transmittance is needed; li is zero without lights.
+__device__ __forceinline__ bool vw_light_pick(const DevScene &S, V3 p, Pcg32 &rng, LightRec &li, float &lw)
+{
+    li.point = li.to_light = li.normal = v3(0, 0, 0);
+    li.intensity = cfill(0.f); li.distance = 0.f; li.pdf = 0.f;
+    lw = 0.f;
+    if (S.n_lights == 0) return false;
+    V2 u = next2d(rng);
+    int idx = cdf_sample_reuse(S.light_cdf, S.n_lights + 1, u.x, lw);
+    vp_light_sample(S, idx, p, u, li);
+    return li.pdf > 0 && lum(li.intensity) > 0;
+}
+__device__ __forceinline__ void vw_store_light(const RenderParams &P, int slot, const LightRec &li, V3 p, float lw)
+{
+    P.W.v_p[slot] = f4(p, lw);
+    P.W.v_li0[slot] = f4(li.to_light, li.distance);
+    P.W.v_li1[slot] = f4(li.point, li.pdf);
+    P.W.v_li2[slot] = f4(li.normal, 0.f);
+    P.W.v_val[slot] = f4c(li.intensity, 0.f);
+}
+__device__ __forceinline__ void vw_done(const RenderParams &P, int slot, C3 L) { P.W.out[slot] = f4c(L, 0.f); }
+
+// evalTransmittanceFromSampledBSDF (VolPathTracing.cpp:369-424), as
+// eval_tr_sampled, reporting the segment origin of the hit instead of its frame
+__device__ __noinline__ C3 vw_tr_sampled(const DevScene &S, Ray ray, Pcg32 &rng, int medium, Hit &h, V3 &seg, bool &was,
+                                         int &newm, int &limit)
+{
+    Ray tr = ray;
+    C3 T = cfill(1.f);
+    bool first = true;
+    was = false;
+    for (int guard = 0; guard < 4096; guard++) {
+        Hit nh;
+        was = vp_trace(S, tr.o, tr.d, tr.mint, tr.maxt, nh);
+        if (was) { h = nh; seg = tr.o; }
+        if (medium >= 0)
+            T = T * vp_medium_tr(S.media[medium], make_ray(tr.o, tr.d, first ? tr.mint : 0.f, was ? h.t : tr.maxt), rng, limit);
+        if (was && prim_bsdf(S, h.prim) >= 0) return T;
+        first = false;
+        if (!was || iszero(T)) return T;
+        V3 np = tr.o + h.t * tr.d;
+        const V3 seg_o = tr.o;
+        tr = make_ray(np, tr.d, RT_EPSILON, tr.maxt);
+        if (prim_interior(S, h.prim) != prim_exterior(S, h.prim)) {
+            Frame f = vp_frame(S, h, seg_o, tr.d);
+            medium = dot(f.n, tr.d) < 0.f ? prim_interior(S, h.prim) : prim_exterior(S, h.prim);
+            newm = medium;
+        }
+    }
+    limit = 1;
+    return T;
+}
+
+#ifndef RT_VW_MINB
+#define RT_VW_MINB 8
+#endif
+#define VW_LOOP(COUNT, QUEUE)                                                                      \
+    const int n_ = (COUNT);                                                                        \
+    const int *qin_ = (QUEUE);                                                                     \
+    for (int i_ = blockIdx.x * blockDim.x + threadIdx.x; i_ < n_; i_ += gridDim.x * blockDim.x)
+
+__global__ void __launch_bounds__(128, RT_VW_MINB) k_vw_trace(RenderParams P, int round)
+{
+    round = cur_round(P, round);
+    const DevScene &S = P.S;
+    RoundCounters *C = &P.W.cnt[round];
+    VW_LOOP(C->closest, P.W.q_closest)
+    {
+        const int slot = qin_[i_];
+        int flags = P.W.flags[slot];
+        float4 ro = P.W.ray_o[slot], rd = P.W.ray_d[slot];
+        float4 seg;
+        Hit h;
+        if (flags & VF_FIRST) {
+            // vol_start: no hit yet, the camera medium
+            h.t = RT_MAX_REAL; h.u = h.v = 0.f; h.prim = -1;
+            seg = make_float4(0.f, 0.f, 0.f, __int_as_float(S.cam.medium));
+            flags = VF_EMISSION;
+        } else {
+            float4 hv = P.W.hit[slot];
+            h.t = hv.x; h.u = hv.y; h.v = hv.z; h.prim = __float_as_int(hv.w);
+            seg = P.W.v_seg[slot];
+            if (!(flags & VF_NULLX)) {   // the trace that ends a bounce
+                flags &= ~VF_EMISSION;
+                float4 rad = P.W.rad[slot];
+                rad.w = __int_as_float(__float_as_int(rad.w) + 1);
+                P.W.rad[slot] = rad;
+            }
+        }
+        Hit nh;
+        const bool was = vp_trace(S, xyz(ro), xyz(rd), ro.w, rd.w, nh);
+        if (was) {
+            h = nh;
+            seg = make_float4(ro.x, ro.y, ro.z, seg.w);
+        }
+        flags = (flags & ~(VF_NULLX | VF_WAS)) | (was ? VF_WAS : 0);
+        P.W.hit[slot] = make_float4(h.t, h.u, h.v, __int_as_float(h.prim));
+        P.W.v_seg[slot] = seg;
+        P.W.flags[slot] = flags;
+        q_push(P.W.q_mat[0], &C->mat[0], slot, true);
+    }
+}
+
+__global__ void __launch_bounds__(128, RT_VW_MINB) k_vw_step(RenderParams P, int round)
+{
+    round = cur_round(P, round);
+    const DevScene &S = P.S;
+    RoundCounters *C = &P.W.cnt[round];
+    RoundCounters *Cn = &P.W.cnt[round + 1];
+    int limit = 0;
+    VW_LOOP(C->mat[0], P.W.q_mat[0])
+    {
+        const int slot = qin_[i_];
+        int flags = P.W.flags[slot];
+        float4 radv = P.W.rad[slot], tpv = P.W.tp[slot];
+        C3 L = rgb(radv), T = rgb(tpv);
+        const int depth = __float_as_int(radv.w);
+        bool push_shadow = false, push_sample = false, push_trace = false;
+        int guard = (flags >> VF_GUARD_SHIFT) + 1;
+        if (depth >= P.max_depth) {
+            vw_done(P, slot, L);
+        } else if (guard > (1 << 16)) {
+            limit = 1;
+            vw_done(P, slot, L);
+        } else {
+            Pcg32 rng = P.W.rng[slot];
+            float4 ro = P.W.ray_o[slot], rd = P.W.ray_d[slot];
+            Ray ray = make_ray(xyz(ro), xyz(rd), ro.w, rd.w);
+            float4 hv = P.W.hit[slot];
+            Hit h; h.t = hv.x; h.u = hv.y; h.v = hv.z; h.prim = __float_as_int(hv.w);
+            float4 seg = P.W.v_seg[slot];
+            int medium = __float_as_int(seg.w);
+            float t = 0.f;
+            C3 wm = cfill(0.f), em = cfill(0.f);
+            bool scattered = false;
+            if (medium >= 0)
+                scattered = vp_medium_sample(S.media[medium], make_ray(ray.o, ray.d, ray.mint, h.t), rng, t, wm, em, limit);
+            bool done = false;
+            if (scattered) {
+                L = L + T * em;
+                T = T * wm;
+                V3 p = ray.o + t * ray.d;
+                LightRec li;
+                float lw;
+                const bool shadow = vw_light_pick(S, p, rng, li, lw);
+                vw_store_light(P, slot, li, p, lw);
+                flags |= VF_SCAT;
+                flags &= ~VF_HASVAL;
+                push_shadow = shadow;
+                push_sample = !shadow;
+            } else {
+                flags &= ~VF_SCAT;
+                if (medium >= 0) {
+                    L = L + T * em;
+                    T = T * wm;
+                }
+                if (!(flags & VF_WAS)) {
+                    if ((flags & VF_EMISSION) && S.env_light >= 0) L = L + T * env_le(S.lights[S.env_light], ray.d);
+                    done = true;
+                } else {
+                    Frame fr = vp_frame(S, h, xyz(seg), ray.d);
+                    if (prim_bsdf(S, h.prim) < 0) {
+                        // null boundary: through, without a bounce
+                        ray = make_ray(fr.p, ray.d, RT_EPSILON, RT_MAX_REAL);
+                        if (prim_interior(S, h.prim) != prim_exterior(S, h.prim))
+                            medium = dot(fr.n, ray.d) < 0.f ? prim_interior(S, h.prim) : prim_exterior(S, h.prim);
+                        P.W.ray_o[slot] = f4(ray.o, ray.mint);
+                        P.W.ray_d[slot] = f4(ray.d, ray.maxt);
+                        flags |= VF_NULLX;
+                        push_trace = true;
+                    } else {
+                        int hl = prim_light(S, h.prim);
+                        if ((flags & VF_EMISSION) && hl >= 0) L = L + T * area_le(S, hl, -ray.d, fr.n);
+                        LightRec li;
+                        float lw;
+                        const bool shadow = vw_light_pick(S, fr.p, rng, li, lw);
+                        vw_store_light(P, slot, li, fr.p, lw);
+                        flags &= ~VF_HASVAL;
+                        push_shadow = shadow;
+                        push_sample = !shadow;
+                    }
+                }
+            }
+            if (done) {
+                vw_done(P, slot, L);
+            } else {
+                P.W.rng[slot] = rng;
+                P.W.rad[slot] = f4c(L, __int_as_float(depth));
+                P.W.tp[slot] = f4c(T, tpv.w);
+                P.W.v_seg[slot] = make_float4(seg.x, seg.y, seg.z, __int_as_float(medium));
+                P.W.flags[slot] = (flags & ((1 << VF_GUARD_SHIFT) - 1)) | (guard << VF_GUARD_SHIFT);
+            }
+        }
+        q_push(P.W.q_shadow, &C->shadow, slot, push_shadow);
+        q_push(P.W.q_mat[1], &C->mat[1], slot, push_sample);
+        q_push(P.W.q_closest, &Cn->closest, slot, push_trace);
+    }
+    if (limit) atomicExch(P.limit_flag, 1);
+}
+
+__global__ void __launch_bounds__(128, RT_VW_MINB) k_vw_shadow(RenderParams P, int round)
+{
+    round = cur_round(P, round);
+    const DevScene &S = P.S;
+    RoundCounters *C = &P.W.cnt[round];
+    int limit = 0;
+    VW_LOOP(C->shadow, P.W.q_shadow)
+    {
+        const int slot = qin_[i_];
+        Pcg32 rng = P.W.rng[slot];
+        float4 pv = P.W.v_p[slot], l0 = P.W.v_li0[slot], l1 = P.W.v_li1[slot], iv = P.W.v_val[slot];
+        const int medium = __float_as_int(P.W.v_seg[slot].w);
+        C3 tr = eval_transmittance(S, make_ray(xyz(pv), xyz(l0), RT_EPSILON, l0.w - RT_EPSILON), medium, rng, limit);
+        float pdf = l1.w * pv.w;
+        C3 value = (tr * rgb(iv)) / pdf;
+        P.W.v_li1[slot] = make_float4(l1.x, l1.y, l1.z, pdf);
+        P.W.v_val[slot] = f4c(value, 0.f);
+        P.W.rng[slot] = rng;
+        P.W.flags[slot] |= VF_HASVAL;
+        q_push(P.W.q_mat[1], &C->mat[1], slot, true);
+    }
+    if (limit) atomicExch(P.limit_flag, 1);
+}
+
+__global__ void __launch_bounds__(128, RT_VW_MINB) k_vw_sample(RenderParams P, int round)
+{
+    round = cur_round(P, round);
+    const DevScene &S = P.S;
+    RoundCounters *C = &P.W.cnt[round];
+    VW_LOOP(C->mat[1], P.W.q_mat[1])
+    {
+        const int slot = qin_[i_];
+        int flags = P.W.flags[slot];
+        Pcg32 rng = P.W.rng[slot];
+        float4 radv = P.W.rad[slot], tpv = P.W.tp[slot];
+        C3 L = rgb(radv), T = rgb(tpv);
+        float4 ro = P.W.ray_o[slot], rd = P.W.ray_d[slot];
+        Ray ray = make_ray(xyz(ro), xyz(rd), ro.w, rd.w);
+        float4 seg = P.W.v_seg[slot];
+        int medium = __float_as_int(seg.w);
+        const bool hasval = flags & VF_HASVAL;
+        C3 value = hasval ? rgb(P.W.v_val[slot]) : cfill(0.f);
+        bool push = true;
+        if (flags & VF_SCAT) {
+            const DevMedium &M = S.media[medium];
+            if (!iszero(value)) {
+                V3 to_light = xyz(P.W.v_li0[slot]);
+                float lpdf = P.W.v_li1[slot].w;
+                float pf = phase_eval(M, to_light, -ray.d);
+                float w = power_heuristic(lpdf, pf);
+                float ev = phase_eval(M, to_light, -ray.d);
+                L = L + ((T * value) * ev) * w;
+            }
+            V3 wo;
+            float pfpdf;
+            float pfw = phase_sample(M, -ray.d, next2d(rng), wo, pfpdf);
+            V3 p = xyz(P.W.v_p[slot]);
+            ray = make_ray(p, wo, 0.f, ray.maxt);
+            P.W.bs[slot] = f4c(cfill(pfw), pfpdf);
+        } else {
+            float4 hv = P.W.hit[slot];
+            Hit h; h.t = hv.x; h.u = hv.y; h.v = hv.z; h.prim = __float_as_int(hv.w);
+            Frame fr = vp_frame(S, h, xyz(seg), ray.d);
+            const DevBsdf *Bp = &S.bsdfs[prim_bsdf(S, h.prim)];
+            DevBsdf Bl;
+            if (Bp->textured) {
+                Bl = *Bp;
+                tex_apply(S, Bl, hit_uv(S, h, xyz(seg), ray.d));
+                Bp = &Bl;
+            }
+            const DevBsdf &B = *Bp;
+            if (!iszero(value)) {
+                V3 to_light = xyz(P.W.v_li0[slot]);
+                float lpdf = P.W.v_li1[slot].w;
+                V3 wi = to_local(fr, to_light), wo = to_local(fr, -ray.d);
+                float ct = fabsf(wi.z);
+                float bp = vp_bsdf_pdf(B, wi, wo);
+                float w = power_heuristic(lpdf, bp);
+                L = L + (((T * value) * vp_bsdf_eval(B, wi, wo)) * ct) * w;
+            }
+            BsdfRec r;
+            r.wi = to_local(fr, -ray.d); r.wo = v3(0, 0, 0);
+            r.type = BT_ALL; r.rel_eta = 1.f; r.pdf = -1.f;
+            V2 bu = next2d(rng);
+            C3 f = vp_bsdf_sample(B, r, bu, rng.state);
+            if (iszero(f)) {
+                vw_done(P, slot, L);
+                push = false;
+            } else {
+                ray = make_ray(fr.p, to_world(fr, r.wo), RT_EPSILON, RT_MAX_REAL);
+                if (prim_interior(S, h.prim) != prim_exterior(S, h.prim))
+                    medium = dot(fr.n, ray.d) < 0.f ? prim_interior(S, h.prim) : prim_exterior(S, h.prim);
+                P.W.bs[slot] = f4c(f, r.pdf);
+                P.W.rel_eta[slot] = r.rel_eta;
+                flags = (r.type & BT_DELTA) ? (flags | VF_DELTA) : (flags & ~VF_DELTA);
+            }
+        }
+        if (push) {
+            P.W.rng[slot] = rng;
+            P.W.rad[slot] = f4c(L, radv.w);
+            P.W.ray_o[slot] = f4(ray.o, ray.mint);
+            P.W.ray_d[slot] = f4(ray.d, ray.maxt);
+            P.W.v_seg[slot] = make_float4(seg.x, seg.y, seg.z, __int_as_float(medium));
+            P.W.flags[slot] = flags;
+        }
+        q_push(P.W.q_mat[2], &C->mat[2], slot, push);
+    }
+}
+
+__global__ void __launch_bounds__(128, RT_VW_MINB) k_vw_trsamp(RenderParams P, int round)
+{
+    round = cur_round(P, round);
+    const DevScene &S = P.S;
+    RoundCounters *C = &P.W.cnt[round];
+    int limit = 0;
+    VW_LOOP(C->mat[2], P.W.q_mat[2])
+    {
+        const int slot = qin_[i_];
+        int flags = P.W.flags[slot];
+        Pcg32 rng = P.W.rng[slot];
+        float4 ro = P.W.ray_o[slot], rd = P.W.ray_d[slot];
+        float4 hv = P.W.hit[slot];
+        Hit h; h.t = hv.x; h.u = hv.y; h.v = hv.z; h.prim = __float_as_int(hv.w);
+        float4 seg = P.W.v_seg[slot];
+        V3 so = xyz(seg);
+        bool was;
+        int newm = -1;
+        C3 tr = vw_tr_sampled(S, make_ray(xyz(ro), xyz(rd), ro.w, rd.w), rng, __float_as_int(seg.w), h, so, was, newm,
+                              limit);
+        P.W.nee[slot] = f4c(tr, 0.f);
+        P.W.hit[slot] = make_float4(h.t, h.u, h.v, __int_as_float(h.prim));
+        P.W.v_seg[slot] = make_float4(so.x, so.y, so.z, seg.w);
+        P.W.rng[slot] = rng;
+        flags = (flags & ~(VF_WAS | VF_NEWM)) | (was ? VF_WAS : 0) | (newm >= 0 ? VF_NEWM : 0);
+        P.W.flags[slot] = flags;
+        q_push(P.W.q_mat[3], &C->mat[3], slot, true);
+    }
+    if (limit) atomicExch(P.limit_flag, 1);
+}
+
+__global__ void __launch_bounds__(128, RT_VW_MINB) k_vw_finish(RenderParams P, int round)
+{
+    round = cur_round(P, round);
+    const DevScene &S = P.S;
+    RoundCounters *C = &P.W.cnt[round];
+    RoundCounters *Cn = &P.W.cnt[round + 1];
+    VW_LOOP(C->mat[3], P.W.q_mat[3])
+    {
+        const int slot = qin_[i_];
+        const int flags = P.W.flags[slot];
+        float4 radv = P.W.rad[slot], tpv = P.W.tp[slot];
+        C3 L = rgb(radv), T = rgb(tpv);
+        float eta = tpv.w;
+        const int depth = __float_as_int(radv.w);
+        float4 rd = P.W.ray_d[slot];
+        const V3 d = xyz(rd);
+        float4 bsv = P.W.bs[slot];
+        C3 tr = rgb(P.W.nee[slot]);
+        const bool was = flags & VF_WAS;
+        float4 hv = P.W.hit[slot];
+        Hit h; h.t = hv.x; h.u = hv.y; h.v = hv.z; h.prim = __float_as_int(hv.w);
+        float4 seg = P.W.v_seg[slot];
+        const int medium = __float_as_int(seg.w);
+        bool done = false;
+        if (flags & VF_SCAT) {
+            T = T * rgb(bsv);
+            if (was) {
+                int hl = prim_light(S, h.prim);
+                if (hl >= 0) {
+                    Frame fr = vp_frame(S, h, xyz(seg), d);
+                    C3 Le = area_le(S, hl, -d, fr.n);
+                    float pl = vp_light_pdf(S, hl, fr.p, xyz(P.W.v_li1[slot]), xyz(P.W.v_li2[slot]),
+                                            xyz(P.W.v_li0[slot]));
+                    float w = power_heuristic(bsv.w, pl);
+                    L = L + ((T * Le) * tr) * w;
+                }
+            }
+        } else {
+            const C3 f = rgb(bsv);
+            int caught = -1;
+            bool isenv = false;
+            C3 Le = cfill(0.f);
+            Frame fr;
+            fr.p = fr.n = v3(0, 0, 0);
+            if (was) {
+                int nl = prim_light(S, h.prim);
+                if (nl >= 0) {
+                    caught = nl;
+                    fr = vp_frame(S, h, xyz(seg), d);
+                    Le = area_le(S, nl, -d, fr.n);
+                }
+            } else if (!(flags & VF_NEWM)) {
+                // a miss: the environment (its pdf depends on the direction only)
+                if (S.env_light >= 0) { caught = S.env_light; isenv = true; Le = env_le(S.lights[S.env_light], d); }
+            }
+            if (caught >= 0) {
+                float pl = (flags & VF_DELTA) ? 0.f : vp_light_pdf(S, caught, xyz(P.W.v_p[slot]), fr.p, fr.n, d);
+                float w = power_heuristic(bsv.w, pl);
+                L = L + (((T * Le) * f) * tr) * w;
+                if (isenv && medium < 0) done = true;
+            }
+            if (!done) {
+                T = T * f;
+                eta *= P.W.rel_eta[slot];
+            }
+        }
+        if (!done && depth >= P.min_depth) {
+            Pcg32 rng = P.W.rng[slot];
+            float stop = smin(0.95f, cmax(T) * eta * eta);
+            if (next1d(rng) < stop) T = T / stop;
+            else done = true;
+            P.W.rng[slot] = rng;
+        }
+        if (done) {
+            vw_done(P, slot, L);
+        } else {
+            P.W.rad[slot] = f4c(L, radv.w);
+            P.W.tp[slot] = f4c(T, eta);
+        }
+        q_push(P.W.q_closest, &Cn->closest, slot, !done);
+    }
+}
+
 // ---------------------------------------------------------------- film
 // One thread per batch pixel: contributions in the order the reference's
 // tile loop produces them (pixels row-major, samples in order), restricted
@@ -1494,6 +1949,7 @@ struct rt_ctx {
     int trace_bpsm = 12;        // traversal kernels: blocks per SM
     int shade_bpsm = RT_SHADE_GRID;   // finish and shading kernels: blocks per SM
     int sort_threshold = 0;     // rounds with fewer closest-hit rays shade unsorted
+    int volpath_wave = 1;       // VolPathTracing as the wavefront (0: the megakernel)
     std::vector<cudaEvent_t> ev_pool;
     std::vector<int> ev_kind;   // kernel kind per recorded pair
     size_t ev_used = 0;
@@ -1765,6 +2221,7 @@ static void free_wave(rt_ctx *c)
     for (void *p : c->wave_allocs) cudaFree(p);
     c->wave_allocs.clear();
     c->capacity = 0;
+    c->W.vw_capacity = 0;
 }
 
 rt_status rt_ctx_destroy(rt_ctx *c)
@@ -2249,6 +2706,28 @@ rt_status rt_scene_info(const rt_scene *sc, float bounds[6], int64_t *device_byt
 }
 
 // ---------------------------------------------------------------- wavefront buffers
+static rt_status ensure_wave(rt_ctx *c, int capacity, int max_rounds);
+// the VolPath wavefront's extra path state (after ensure_wave, which frees it
+// when it reallocates)
+static rt_status ensure_vw(rt_ctx *c, int capacity)
+{
+    if (c->W.vw_capacity >= capacity) return RT_OK;
+    Wave &W = c->W;
+    const size_t P = (size_t)capacity;
+    float4 **arr[6] = {&W.v_seg, &W.v_p, &W.v_li0, &W.v_li1, &W.v_li2, &W.v_val};
+    for (float4 **a : arr) {
+        void *p = nullptr;
+        if (cudaMalloc(&p, P * sizeof(float4)) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(RT_ERR_NOMEM, "VolPath wavefront buffer allocation failed");
+        }
+        c->wave_allocs.push_back(p);
+        *a = (float4 *)p;
+    }
+    W.vw_capacity = capacity;
+    return RT_OK;
+}
+
 static rt_status ensure_wave(rt_ctx *c, int capacity, int max_rounds)
 {
     if (c->capacity >= capacity && c->W.max_rounds >= max_rounds) return RT_OK;
@@ -2528,10 +3007,14 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
     int capacity = std::min(tiles_per_batch, ntiles) * tile_pix * rd->spp;
     if (rd->integrator == RT_INTEGRATOR_PATH_MIS && rd->max_depth > (1 << 16))
         return fail(RT_ERR_LIMIT, "rt_render: max_depth above 65536 is not provided by the device path");
-    int max_rounds = rd->integrator == RT_INTEGRATOR_PATH_MIS ? rd->max_depth + 3 : 1;
+    // rounds: PathTracingMIS, a bounce each; the VolPath wavefront, a
+    // vol_step each, capped like the megakernel's 2^16 steps per path
+    const bool vw = rd->integrator == RT_INTEGRATOR_VOLPATH && ctx->volpath_wave;
+    int max_rounds = rd->integrator == RT_INTEGRATOR_PATH_MIS ? rd->max_depth + 3 : vw ? (1 << 16) + 2 : 1;
     int round_buf = max_rounds;
     rt_status s = ensure_wave(ctx, capacity, round_buf);
     if (s != RT_OK) return s;
+    if (vw && (s = ensure_vw(ctx, capacity)) != RT_OK) return s;
     CK(cudaMemsetAsync(ctx->stats, 0, sizeof(unsigned long long) * 8, st));
     CK(cudaMemsetAsync(ctx->limit_flag, 0, sizeof(int), st));
     RenderParams P;
@@ -2587,7 +3070,28 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
         prof_end(ctx);
         launches++;
         if ((s = launch_check("k_camera")) != RT_OK) return s;
-        if (rd->integrator == RT_INTEGRATOR_VOLPATH) {
+        if (rd->integrator == RT_INTEGRATOR_VOLPATH && ctx->volpath_wave) {
+            // one round = one vol_step of every live path (six kernels)
+            const int vb = sm * 8;
+            prof_begin(ctx, K_VOLPATH);
+            for (int r = 0; r < max_rounds; r++) {
+                k_vw_trace<<<vb, 128, 0, st>>>(P, r);
+                k_vw_step<<<vb, 128, 0, st>>>(P, r);
+                k_vw_shadow<<<vb, 128, 0, st>>>(P, r);
+                k_vw_sample<<<vb, 128, 0, st>>>(P, r);
+                k_vw_trsamp<<<vb, 128, 0, st>>>(P, r);
+                k_vw_finish<<<vb, 128, 0, st>>>(P, r);
+                launches += 6;
+                if ((s = launch_check("VolPath round")) != RT_OK) return s;
+                if ((r & 3) == 3 && r + 1 < max_rounds) {
+                    int nq = 0;
+                    CK(cudaMemcpyAsync(&nq, &ctx->W.cnt[r + 1].closest, sizeof(int), cudaMemcpyDeviceToHost, st));
+                    CK(cudaStreamSynchronize(st));
+                    if (nq == 0) break;
+                }
+            }
+            prof_end(ctx);
+        } else if (rd->integrator == RT_INTEGRATOR_VOLPATH) {
             CK(cudaMemsetAsync(ctx->work, 0, sizeof(int), st));
             prof_begin(ctx, K_VOLPATH);
             k_volpath<<<sm * RT_VOLPATH_GRID, 128, 0, st>>>(P, ctx->work);
@@ -3055,6 +3559,8 @@ rt_status rt_internal_error(rt_status st, const char *msg) { return fail(st, msg
 int rt_internal_device(const rt_ctx *c) { return c->device; }
 int rt_internal_bvh_width(const rt_ctx *c) { return c->bvh_width; }
 int rt_internal_graphs(const rt_ctx *c) { return c->graphs; }
+int rt_internal_volpath_wave(const rt_ctx *c) { return c->volpath_wave; }
+void rt_internal_set_volpath_wave(rt_ctx *c, int on) { c->volpath_wave = on ? 1 : 0; }
 void rt_internal_get_shape(const rt_ctx *c, int *wave_paths, int *trace_bpsm, int *shade_bpsm, int *sort_threshold)
 {
     *wave_paths = c->wave_paths;

@@ -20,6 +20,8 @@ RT_HIDDEN int rt_internal_graphs(const rt_ctx *c);
 RT_HIDDEN void rt_internal_get_shape(const rt_ctx *c, int *wave_paths, int *trace_bpsm, int *shade_bpsm,
                                      int *sort_threshold);
 RT_HIDDEN rt_status rt_internal_set_shape(rt_ctx *c, int trace_bpsm, int shade_bpsm, int sort_threshold);
+RT_HIDDEN int rt_internal_volpath_wave(const rt_ctx *c);
+RT_HIDDEN void rt_internal_set_volpath_wave(rt_ctx *c, int on);
 RT_HIDDEN void *rt_internal_stream(const rt_ctx *c);
 RT_HIDDEN rt_lane_pool *&rt_internal_pool(rt_ctx *c);
 RT_HIDDEN void rt_internal_set_stats(rt_ctx *c, const rt_render_stats &s);

@@ -53,6 +53,14 @@ struct Wave {
     RoundCounters *cnt;
     int capacity;
     int max_rounds;
+    // VolPathTracing wavefront (allocated only for it, vw_capacity paths)
+    float4 *v_seg;     // origin of the ray segment that found `hit` (its direction is the path's), medium
+    float4 *v_p;       // vertex position (scatter point or surface point), light-selection weight
+    float4 *v_li0;     // light sample: direction to the light, distance
+    float4 *v_li1;     // light sample: point on the light, pdf
+    float4 *v_li2;     // light sample: normal at the point
+    float4 *v_val;     // light sample intensity, then the attenuated light-sample value
+    int vw_capacity;
 };
 
 // batch geometry: tiles [tile0, tile0 + ntiles) of the reference job grid

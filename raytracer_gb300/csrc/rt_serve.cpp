@@ -63,6 +63,7 @@ struct LaneSet {
         for (rt_ctx *c : lanes) {
             rt_ctx_set_bvh_width(c, rt_internal_bvh_width(owner));
             rt_ctx_set_graphs(c, rt_internal_graphs(owner));
+            rt_internal_set_volpath_wave(c, rt_internal_volpath_wave(owner));
             rt_ctx_set_wave_paths(c, wave_paths);
             rt_status s = rt_internal_set_shape(c, tb, sb, thr);
             if (s != RT_OK) return s;
@@ -160,6 +161,7 @@ extern "C" rt_status rt_ctx_get_tuning(rt_ctx *ctx, rt_tuning *out)
     out->sort_threshold = thr;
     out->lanes = pool->want;
     out->graphs = rt_internal_graphs(ctx);
+    out->volpath_wavefront = rt_internal_volpath_wave(ctx);
     return RT_OK;
 }
 
@@ -169,11 +171,14 @@ extern "C" rt_status rt_ctx_set_tuning(rt_ctx *ctx, const rt_tuning *t)
     if (t->lane_wave_paths < (1 << 16) || t->lane_wave_paths > (1 << 26))
         return rt_internal_error(RT_ERR_INVALID, "tuning: lane wave paths must be in [2^16, 2^26]");
     if (t->graphs != 0 && t->graphs != 1) return rt_internal_error(RT_ERR_INVALID, "tuning: graphs must be 0 or 1");
+    if (t->volpath_wavefront != 0 && t->volpath_wavefront != 1)
+        return rt_internal_error(RT_ERR_INVALID, "tuning: volpath_wavefront must be 0 or 1");
     rt_status s = rt_ctx_set_wave_paths(ctx, t->wave_paths);
     if (s == RT_OK) s = rt_internal_set_shape(ctx, t->trace_blocks_per_sm, t->shade_blocks_per_sm, t->sort_threshold);
     if (s == RT_OK) s = rt_ctx_set_lanes(ctx, t->lanes);
     if (s != RT_OK) return s;
     rt_ctx_set_graphs(ctx, t->graphs);
+    rt_internal_set_volpath_wave(ctx, t->volpath_wavefront);
     pool_of(ctx)->set.wave_paths = t->lane_wave_paths;
     return RT_OK;
 }

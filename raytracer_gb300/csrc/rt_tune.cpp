@@ -11,6 +11,7 @@
 //
 // The knobs and their candidates:
 //   graphs               0, 1
+//   volpath_wavefront    1, 0 (VolPath as a wavefront or one persistent kernel)
 //   lanes                1, 2, 4, 8 (batches of more than one job)
 //   sort_threshold       0, 2^12, 2^14, 2^16, 2^18 closest-hit rays
 //   shade blocks per SM  4, 8, 16, 24
@@ -84,6 +85,7 @@ extern "C" rt_status rt_autotune(rt_ctx *ctx, rt_scene *const *scenes, const rt_
     if (st == RT_OK) st = measure(cur, cur_s);
     std::vector<Knob> knobs;
     knobs.push_back({&rt_tuning::graphs, {0, 1}});
+    knobs.push_back({&rt_tuning::volpath_wavefront, {1, 0}});
     if (n > 1) knobs.push_back({&rt_tuning::lanes, {1, 2, 4, 8}});
     knobs.push_back({&rt_tuning::sort_threshold, {0, 1 << 12, 1 << 14, 1 << 16, 1 << 18}});
     knobs.push_back({&rt_tuning::shade_blocks_per_sm, {4, 8, 16, 24}});

@@ -489,6 +489,47 @@ def test_texture_validation(ctx, rtlib):
     assert e.value.status == 5
 
 
+def _volpath_cases():
+    smooth = scenes.cornell_smooth(40, 32)
+    m = smooth.add_medium(dict(type=D.MEDIUM_HOMOGENEOUS, phase=D.PHASE_HG, g=0.4, sigma_a=(0.5, 1.0, 2.0),
+                               sigma_s=(1.0, 1.0, 1.0), scale=2.0))
+    smooth.meshes[4]["interior"] = m
+    smooth.integrator = dict(smooth.integrator, integrator=D.INTEGRATOR_VOLPATH)
+    tex = scenes.textured_room(32, 24)
+    tex.integrator = dict(tex.integrator, integrator=D.INTEGRATOR_VOLPATH)
+    fog = scenes.cornell_box(32, 24)   # the camera inside a medium filling the room
+    fm = fog.add_medium(dict(type=D.MEDIUM_HOMOGENEOUS, phase=D.PHASE_ISOTROPIC, sigma_a=(0.05, 0.05, 0.05),
+                             sigma_s=(0.6, 0.6, 0.6), scale=1.0))
+    fog.camera["medium"] = fm
+    fog.integrator = dict(fog.integrator, integrator=D.INTEGRATOR_VOLPATH)
+    return {"grid": (scenes.volume_grid(48, 40, res=16), 3), "smooth": (smooth, 3), "textured": (tex, 2),
+            "fog": (fog, 3), "two_batches": (scenes.volume_grid(80, 60, res=16), 16)}
+
+
+@pytest.mark.parametrize("case", ["grid", "smooth", "textured", "fog", "two_batches"])
+def test_volpath_wavefront_equals_megakernel(ctx, rtlib, case):
+    """VolPathTracing as six kernels over queues (one vol_step per round)
+    gives the persistent megakernel's film bit for bit: each path draws its
+    numbers in the same order and ends with the same radiance."""
+    s, spp = _volpath_cases()[case]
+    g = rtlib.Scene(ctx, s)
+    before = ctx.get_tuning()
+    try:
+        if case == "two_batches":
+            ctx.set_wave_paths(1 << 16)
+        ctx.set_tuning(volpath_wavefront=0)
+        ref = g.render(spp, seed=13)
+        ctx.set_tuning(volpath_wavefront=1)
+        got = g.render(spp, seed=13)
+        st = ctx.stats()
+    finally:
+        ctx.set_tuning(**before)
+        ctx.set_wave_paths(1 << 26)
+        g.close()
+    assert np.array_equal(got, ref)
+    assert st["launches"] >= 6
+
+
 def test_film_parity_mixed_normals(ctx, rtlib):
     """One mesh with vertex normals (shading normals), the others without
     (NaN-marked, geometric normals), in one scene."""
