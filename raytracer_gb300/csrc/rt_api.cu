@@ -1349,15 +1349,35 @@ __device__ __noinline__ C3 vw_tr_sampled(const DevScene &S, Ray ray, Pcg32 &rng,
     return T;
 }
 
+// resident 128-thread blocks per SM of each wavefront kernel (its launch
+// bound and its grid); the tracking loops of shadow and trsamp wait on memory
 #ifndef RT_VW_MINB
 #define RT_VW_MINB 8
+#endif
+#ifndef RT_VW_MINB_TRACE
+#define RT_VW_MINB_TRACE RT_VW_MINB
+#endif
+#ifndef RT_VW_MINB_STEP
+#define RT_VW_MINB_STEP RT_VW_MINB
+#endif
+#ifndef RT_VW_MINB_SHADOW
+#define RT_VW_MINB_SHADOW RT_VW_MINB
+#endif
+#ifndef RT_VW_MINB_SAMPLE
+#define RT_VW_MINB_SAMPLE RT_VW_MINB
+#endif
+#ifndef RT_VW_MINB_TRSAMP
+#define RT_VW_MINB_TRSAMP RT_VW_MINB
+#endif
+#ifndef RT_VW_MINB_FINISH
+#define RT_VW_MINB_FINISH RT_VW_MINB
 #endif
 #define VW_LOOP(COUNT, QUEUE)                                                                      \
     const int n_ = (COUNT);                                                                        \
     const int *qin_ = (QUEUE);                                                                     \
     for (int i_ = blockIdx.x * blockDim.x + threadIdx.x; i_ < n_; i_ += gridDim.x * blockDim.x)
 
-__global__ void __launch_bounds__(128, RT_VW_MINB) k_vw_trace(RenderParams P, int round)
+__global__ void __launch_bounds__(128, RT_VW_MINB_TRACE) k_vw_trace(RenderParams P, int round)
 {
     round = cur_round(P, round);
     const DevScene &S = P.S;
@@ -1399,7 +1419,7 @@ __global__ void __launch_bounds__(128, RT_VW_MINB) k_vw_trace(RenderParams P, in
     }
 }
 
-__global__ void __launch_bounds__(128, RT_VW_MINB) k_vw_step(RenderParams P, int round)
+__global__ void __launch_bounds__(128, RT_VW_MINB_STEP) k_vw_step(RenderParams P, int round)
 {
     round = cur_round(P, round);
     const DevScene &S = P.S;
@@ -1496,7 +1516,7 @@ __global__ void __launch_bounds__(128, RT_VW_MINB) k_vw_step(RenderParams P, int
     if (limit) atomicExch(P.limit_flag, 1);
 }
 
-__global__ void __launch_bounds__(128, RT_VW_MINB) k_vw_shadow(RenderParams P, int round)
+__global__ void __launch_bounds__(128, RT_VW_MINB_SHADOW) k_vw_shadow(RenderParams P, int round)
 {
     round = cur_round(P, round);
     const DevScene &S = P.S;
@@ -1520,7 +1540,7 @@ __global__ void __launch_bounds__(128, RT_VW_MINB) k_vw_shadow(RenderParams P, i
     if (limit) atomicExch(P.limit_flag, 1);
 }
 
-__global__ void __launch_bounds__(128, RT_VW_MINB) k_vw_sample(RenderParams P, int round)
+__global__ void __launch_bounds__(128, RT_VW_MINB_SAMPLE) k_vw_sample(RenderParams P, int round)
 {
     round = cur_round(P, round);
     const DevScene &S = P.S;
@@ -1605,7 +1625,7 @@ __global__ void __launch_bounds__(128, RT_VW_MINB) k_vw_sample(RenderParams P, i
     }
 }
 
-__global__ void __launch_bounds__(128, RT_VW_MINB) k_vw_trsamp(RenderParams P, int round)
+__global__ void __launch_bounds__(128, RT_VW_MINB_TRSAMP) k_vw_trsamp(RenderParams P, int round)
 {
     round = cur_round(P, round);
     const DevScene &S = P.S;
@@ -1636,7 +1656,7 @@ __global__ void __launch_bounds__(128, RT_VW_MINB) k_vw_trsamp(RenderParams P, i
     if (limit) atomicExch(P.limit_flag, 1);
 }
 
-__global__ void __launch_bounds__(128, RT_VW_MINB) k_vw_finish(RenderParams P, int round)
+__global__ void __launch_bounds__(128, RT_VW_MINB_FINISH) k_vw_finish(RenderParams P, int round)
 {
     round = cur_round(P, round);
     const DevScene &S = P.S;
@@ -3072,15 +3092,14 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
         if ((s = launch_check("k_camera")) != RT_OK) return s;
         if (rd->integrator == RT_INTEGRATOR_VOLPATH && ctx->volpath_wave) {
             // one round = one vol_step of every live path (six kernels)
-            const int vb = sm * 8;
             prof_begin(ctx, K_VOLPATH);
             for (int r = 0; r < max_rounds; r++) {
-                k_vw_trace<<<vb, 128, 0, st>>>(P, r);
-                k_vw_step<<<vb, 128, 0, st>>>(P, r);
-                k_vw_shadow<<<vb, 128, 0, st>>>(P, r);
-                k_vw_sample<<<vb, 128, 0, st>>>(P, r);
-                k_vw_trsamp<<<vb, 128, 0, st>>>(P, r);
-                k_vw_finish<<<vb, 128, 0, st>>>(P, r);
+                k_vw_trace<<<sm * RT_VW_MINB_TRACE, 128, 0, st>>>(P, r);
+                k_vw_step<<<sm * RT_VW_MINB_STEP, 128, 0, st>>>(P, r);
+                k_vw_shadow<<<sm * RT_VW_MINB_SHADOW, 128, 0, st>>>(P, r);
+                k_vw_sample<<<sm * RT_VW_MINB_SAMPLE, 128, 0, st>>>(P, r);
+                k_vw_trsamp<<<sm * RT_VW_MINB_TRSAMP, 128, 0, st>>>(P, r);
+                k_vw_finish<<<sm * RT_VW_MINB_FINISH, 128, 0, st>>>(P, r);
                 launches += 6;
                 if ((s = launch_check("VolPath round")) != RT_OK) return s;
                 if ((r & 3) == 3 && r + 1 < max_rounds) {
