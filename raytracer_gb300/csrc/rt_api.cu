@@ -2816,15 +2816,16 @@ static rt_status launch_check(const char *what)
     return RT_OK;
 }
 
-// One PathTracingMIS wavefront batch as a CUDA graph: reset the batch's
-// counters and the device round index, camera rays, then a conditional WHILE
-// node whose body is one round (closest-hit trace, shadow trace, finish,
-// shading, k_round_next), then the film reduction.  The graph is built once
+// One wavefront batch as a CUDA graph: reset the batch's counters and the
+// device round index, camera rays, then a conditional WHILE node whose body
+// is one round (PathTracingMIS: closest-hit trace, shadow trace, finish,
+// shading; VolPath: its six kernels; then k_round_next), then the film
+// reduction.  The graph is built once
 // per distinct set of launch parameters and kept; the conditional handle it
 // owns is only ever set by its own k_round_next.
 static rt_status pt_batch_graph(rt_ctx *ctx, rt_scene *sc, const RenderParams &P, float4 *film, bool box_film,
                                 int accumulate, int Wd, int t0, int t1, int tiles_x, int bx, int by, int max_rounds,
-                                int round_buf)
+                                int round_buf, bool vw)
 {
     cudaStream_t st = ctx->cap_stream;   // capture; the graph runs on ctx->stream
     const int sm = ctx->sm_count > 0 ? ctx->sm_count : 1;
@@ -2836,13 +2837,13 @@ static rt_status pt_batch_graph(rt_ctx *ctx, rt_scene *sc, const RenderParams &P
     struct Tail {
         const void *film;
         int box, accumulate, wd, t0, t1, tiles_x, bx, by, max_rounds, round_buf, cam_blocks, trace_blocks,
-            shade_blocks, w8, types;
+            shade_blocks, w8, types, vw;
     } tail;
     std::memset(&tail, 0, sizeof(tail));
     tail.film = film; tail.box = box_film; tail.accumulate = accumulate; tail.wd = Wd; tail.t0 = t0; tail.t1 = t1;
     tail.tiles_x = tiles_x; tail.bx = bx; tail.by = by; tail.max_rounds = max_rounds; tail.round_buf = round_buf;
     tail.cam_blocks = cam_blocks; tail.trace_blocks = trace_blocks; tail.shade_blocks = shade_blocks;
-    tail.w8 = w8; tail.types = types;
+    tail.w8 = w8; tail.types = types; tail.vw = vw;
     std::vector<unsigned char> key(sizeof(RenderParams) + sizeof(Tail));
     std::memcpy(key.data(), &P, sizeof(RenderParams));
     std::memcpy(key.data() + sizeof(RenderParams), &tail, sizeof(Tail));
@@ -2887,21 +2888,32 @@ static rt_status pt_batch_graph(rt_ctx *ctx, rt_scene *sc, const RenderParams &P
                     "body capture"))
                 break;
             body_capturing = true;
-            if (w8) {
-                k_trace8<false, false><<<trace_blocks, 128, 0, bs>>>(P, 0);
-                k_trace8<true, false><<<trace_blocks, 128, 0, bs>>>(P, 0);
+            if (vw) {
+                // one VolPath round (the next round's trace queue is its
+                // counters' closest, which k_round_next tests)
+                k_vw_trace<<<sm * RT_VW_MINB_TRACE, 128, 0, bs>>>(P, 0);
+                k_vw_step<<<sm * RT_VW_MINB_STEP, 128, 0, bs>>>(P, 0);
+                k_vw_shadow<<<sm * RT_VW_MINB_SHADOW, 128, 0, bs>>>(P, 0);
+                k_vw_sample<<<sm * RT_VW_MINB_SAMPLE, 128, 0, bs>>>(P, 0);
+                k_vw_trsamp<<<sm * RT_VW_MINB_TRSAMP, 128, 0, bs>>>(P, 0);
+                k_vw_finish<<<sm * RT_VW_MINB_FINISH, 128, 0, bs>>>(P, 0);
             } else {
-                k_trace<false, false><<<trace_blocks, 128, 0, bs>>>(P, 0);
-                k_trace<true, false><<<trace_blocks, 128, 0, bs>>>(P, 0);
+                if (w8) {
+                    k_trace8<false, false><<<trace_blocks, 128, 0, bs>>>(P, 0);
+                    k_trace8<true, false><<<trace_blocks, 128, 0, bs>>>(P, 0);
+                } else {
+                    k_trace<false, false><<<trace_blocks, 128, 0, bs>>>(P, 0);
+                    k_trace<true, false><<<trace_blocks, 128, 0, bs>>>(P, 0);
+                }
+                k_pt_finish<<<shade_blocks, 128, 0, bs>>>(P, 0);
+                if (types & 1) k_pt_shade<0><<<shade_blocks, 128, 0, bs>>>(P, 0);
+                if (types & 2) k_pt_shade<1><<<shade_blocks, 128, 0, bs>>>(P, 0);
+                if (types & 4) k_pt_shade<2><<<shade_blocks, 128, 0, bs>>>(P, 0);
+                if (types & 8) k_pt_shade<3><<<shade_blocks, 128, 0, bs>>>(P, 0);
+                if (types & 16) k_pt_shade<4><<<shade_blocks, 128, 0, bs>>>(P, 0);
+                if (types & 32) k_pt_shade<5><<<shade_blocks, 128, 0, bs>>>(P, 0);
+                if (types & 64) k_pt_shade<RT_QUEUE_MIXED><<<shade_blocks, 128, 0, bs>>>(P, 0);
             }
-            k_pt_finish<<<shade_blocks, 128, 0, bs>>>(P, 0);
-            if (types & 1) k_pt_shade<0><<<shade_blocks, 128, 0, bs>>>(P, 0);
-            if (types & 2) k_pt_shade<1><<<shade_blocks, 128, 0, bs>>>(P, 0);
-            if (types & 4) k_pt_shade<2><<<shade_blocks, 128, 0, bs>>>(P, 0);
-            if (types & 8) k_pt_shade<3><<<shade_blocks, 128, 0, bs>>>(P, 0);
-            if (types & 16) k_pt_shade<4><<<shade_blocks, 128, 0, bs>>>(P, 0);
-            if (types & 32) k_pt_shade<5><<<shade_blocks, 128, 0, bs>>>(P, 0);
-            if (types & 64) k_pt_shade<RT_QUEUE_MIXED><<<shade_blocks, 128, 0, bs>>>(P, 0);
             k_round_next<<<1, 1, 0, bs>>>(P, loop, max_rounds);
             if (bad(cudaGetLastError(), "round kernels")) break;
             body_capturing = false;
@@ -3057,9 +3069,9 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
     const int sm = ctx->sm_count > 0 ? ctx->sm_count : 1;
     int64_t launches = 0, trace_c_launches = 0, trace_a_launches = 0;
     int64_t total_paths = 0;
-    // one CUDA graph per PathTracingMIS batch (rt_ctx_set_graphs)
+    // one CUDA graph per PathTracingMIS or VolPath-wavefront batch (rt_ctx_set_graphs)
     const bool use_graph = ctx->graphs && !ctx->profiling && !ctx->ray_sort &&
-                           rd->integrator == RT_INTEGRATOR_PATH_MIS;
+                           (rd->integrator == RT_INTEGRATOR_PATH_MIS || vw);
     int graph_batches = 0;
     if (use_graph) {
         if (!ctx->round_dev) CK(cudaMalloc(&ctx->round_dev, sizeof(int)));
@@ -3077,7 +3089,7 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
         total_paths += P.n_paths;
         if (use_graph) {
             if ((s = pt_batch_graph(ctx, sc, P, film, box_film, accumulate, Wd, t0, t1, tiles_x, bx, by, max_rounds,
-                                    round_buf)) != RT_OK)
+                                    round_buf, vw)) != RT_OK)
                 return s;
             graph_batches++;
             continue;
@@ -3222,7 +3234,7 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
     if (graph_batches) {
         // camera and film per batch, the rounds' kernels and k_round_next
         const int64_t rounds = (int64_t)stats[7];
-        const int per_round = 3 + __builtin_popcount(types) + 1;
+        const int per_round = vw ? 6 + 1 : 3 + __builtin_popcount(types) + 1;
         launches += 2 * (int64_t)graph_batches + rounds * per_round;
         trace_c_launches += rounds;
         trace_a_launches += rounds;

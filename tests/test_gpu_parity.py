@@ -508,9 +508,10 @@ def _volpath_cases():
 
 @pytest.mark.parametrize("case", ["grid", "smooth", "textured", "fog", "two_batches"])
 def test_volpath_wavefront_equals_megakernel(ctx, rtlib, case):
-    """VolPathTracing as six kernels over queues (one vol_step per round)
-    gives the persistent megakernel's film bit for bit: each path draws its
-    numbers in the same order and ends with the same radiance."""
+    """VolPathTracing as six kernels over queues (one vol_step per round),
+    launched kernel by kernel or as a graph, gives the persistent
+    megakernel's film bit for bit: each path draws its numbers in the same
+    order and ends with the same radiance."""
     s, spp = _volpath_cases()[case]
     g = rtlib.Scene(ctx, s)
     before = ctx.get_tuning()
@@ -522,12 +523,16 @@ def test_volpath_wavefront_equals_megakernel(ctx, rtlib, case):
         ctx.set_tuning(volpath_wavefront=1)
         got = g.render(spp, seed=13)
         st = ctx.stats()
+        ctx.set_tuning(graphs=1)   # the rounds as a graph with a device-ended loop
+        got_g = [g.render(spp, seed=13) for _ in range(2)]
     finally:
         ctx.set_tuning(**before)
         ctx.set_wave_paths(1 << 26)
         g.close()
     assert np.array_equal(got, ref)
     assert st["launches"] >= 6
+    for f in got_g:
+        assert np.array_equal(f, ref)
 
 
 def test_film_parity_mixed_normals(ctx, rtlib):
