@@ -271,6 +271,9 @@ __global__ void k_sort_copy(RenderParams P, int round, int shadow)
 #ifndef RT_TRACE_MINB
 #define RT_TRACE_MINB 10
 #endif
+#ifndef RT_TRACE_SSTACK
+#define RT_TRACE_SSTACK 0
+#endif
 template <bool ANY, bool COUNT>
 __global__ void __launch_bounds__(128, RT_TRACE_MINB) k_trace(RenderParams P, int round)
 {
@@ -283,7 +286,28 @@ __global__ void __launch_bounds__(128, RT_TRACE_MINB) k_trace(RenderParams P, in
     const int lane = threadIdx.x & 31;
     int cnt[2] = {0, 0};
 
+    // traversal stack: the bottom RT_TRACE_SSTACK entries in shared memory
+    // (entry i of thread t at [i * 128 + t], conflict-free), the rest in a
+    // local array
+#if RT_TRACE_SSTACK > 0
+    __shared__ int sstack[RT_TRACE_SSTACK * 128];
+    int lstack[RT_STACK - RT_TRACE_SSTACK];
+#define SPUSH(v)                                                                       \
+    do {                                                                               \
+        if (sp < RT_TRACE_SSTACK) sstack[sp * 128 + threadIdx.x] = (v);                \
+        else lstack[sp - RT_TRACE_SSTACK] = (v);                                       \
+        sp++;                                                                          \
+    } while (0)
+#define SPOP(dst)                                                                      \
+    do {                                                                               \
+        --sp;                                                                          \
+        (dst) = sp < RT_TRACE_SSTACK ? sstack[sp * 128 + threadIdx.x] : lstack[sp - RT_TRACE_SSTACK]; \
+    } while (0)
+#else
     int stack[RT_STACK];
+#define SPUSH(v) stack[sp++] = (v)
+#define SPOP(dst) (dst) = stack[--sp]
+#endif
     int sp = 0;
     int node = RT_SENT, leaf = 0;
     int slot = -1;
@@ -324,7 +348,7 @@ __global__ void __launch_bounds__(128, RT_TRACE_MINB) k_trace(RenderParams P, in
                 ly = -(ooy + copysignf(slab_guard(ooy), idy)); hy = -(ooy - copysignf(slab_guard(ooy), idy));
                 lz = -(ooz + copysignf(slab_guard(ooz), idz)); hz = -(ooz - copysignf(slab_guard(ooz), idz));
                 sp = 0;
-                stack[sp++] = RT_SENT;
+                SPUSH(RT_SENT);
                 leaf = 0;
                 node = (S.n_nodes > 0 && !(hit_t < tmin)) ? 0 : RT_SENT;
             }
@@ -350,17 +374,17 @@ __global__ void __launch_bounds__(128, RT_TRACE_MINB) k_trace(RenderParams P, in
                 float c1max = rt_min4(fmaxf(c1lox, c1hix), fmaxf(c1loy, c1hiy), fmaxf(c1loz, c1hiz), hit_t);
                 bool t0 = c0min <= c0max, t1 = c1min <= c1max;
                 if (!t0 && !t1) {
-                    node = stack[--sp];
+                    SPOP(node);
                 } else {
                     node = t0 ? cc.x : cc.y;
                     if (t0 && t1) {
                         int far = cc.y;
                         if (c1min < c0min) { far = node; node = cc.y; }
-                        if (sp < RT_STACK) stack[sp++] = far;
+                        if (sp < RT_STACK) SPUSH(far);
                     }
                 }
                 // first leaf found: postpone it and keep traversing
-                if (node < 0 && leaf >= 0) { leaf = node; node = stack[--sp]; }
+                if (node < 0 && leaf >= 0) { leaf = node; SPOP(node); }
                 if (!__any_sync(__activemask(), leaf >= 0)) break;
             }
             // ---- postponed leaves
@@ -379,7 +403,7 @@ __global__ void __launch_bounds__(128, RT_TRACE_MINB) k_trace(RenderParams P, in
                 }
                 if (ANY && node == RT_SENT && hprim >= 0) { leaf = 0; break; }
                 leaf = node;
-                if (node < 0) node = stack[--sp];
+                if (node < 0) SPOP(node);
             }
             if (__popc(__activemask()) < RT_FETCH_THRESHOLD) break;
         }
@@ -413,6 +437,8 @@ __global__ void __launch_bounds__(128, RT_TRACE_MINB) k_trace(RenderParams P, in
         }
     }
     if (threadIdx.x == 0 && blockIdx.x == 0) atomicAdd(&P.stats[ANY ? 1 : 0], (unsigned long long)n);
+#undef SPUSH
+#undef SPOP
 }
 
 // ---------------------------------------------------------------- 8-wide traversal
