@@ -3,8 +3,9 @@
 // It chooses the rt_tuning of a context for a workload by timing
 // rt_batch_render on a sample of the workload's jobs.  The search is
 // coordinate descent over a fixed grid of candidates: one knob at a time,
-// every candidate value tried with the others held at the best so far, the
-// best kept if it is at least 1% faster, two passes over the knobs or until
+// every candidate value tried with the others held at the best so far, a
+// candidate kept if it is at least 2% faster and stays so when it and the
+// incumbent are measured again, two passes over the knobs or until
 // max_trials timed trials.  Every knob leaves the films unchanged (queue
 // capacity, grid sizes, the material-sort threshold, lanes and CUDA
 // graphs), so the choice only trades speed.
@@ -12,7 +13,7 @@
 // The knobs and their candidates:
 //   graphs               0, 1
 //   volpath_wavefront    1, 0 (VolPath as a wavefront or one persistent kernel)
-//   lanes                1, 2, 4, 8 (batches of more than one job)
+//   lanes                1, 2, 4, 8 (samples of 32 jobs or more)
 //   sort_threshold       0, 2^12, 2^14, 2^16, 2^18 closest-hit rays
 //   shade blocks per SM  4, 8, 16, 24
 //   trace blocks per SM  8, 10, 12, 16
@@ -86,7 +87,9 @@ extern "C" rt_status rt_autotune(rt_ctx *ctx, rt_scene *const *scenes, const rt_
     std::vector<Knob> knobs;
     knobs.push_back({&rt_tuning::graphs, {0, 1}});
     knobs.push_back({&rt_tuning::volpath_wavefront, {1, 0}});
-    if (n > 1) knobs.push_back({&rt_tuning::lanes, {1, 2, 4, 8}});
+    // lanes pay off across many jobs: a sample of fewer than 32 cannot show
+    // it, and the caller's lane count stays
+    if (n >= 32) knobs.push_back({&rt_tuning::lanes, {1, 2, 4, 8}});
     knobs.push_back({&rt_tuning::sort_threshold, {0, 1 << 12, 1 << 14, 1 << 16, 1 << 18}});
     knobs.push_back({&rt_tuning::shade_blocks_per_sm, {4, 8, 16, 24}});
     knobs.push_back({&rt_tuning::trace_blocks_per_sm, {8, 10, 12, 16}});
@@ -102,10 +105,21 @@ extern "C" rt_status rt_autotune(rt_ctx *ctx, rt_scene *const *scenes, const rt_
                 t.*(k.field) = v;
                 double s = 0;
                 st = measure(t, s);
-                if (st == RT_OK && s < cur_s * 0.99) {
-                    cur = t;
-                    cur_s = s;
-                    changed = true;
+                if (st == RT_OK && s < cur_s * 0.98) {
+                    // confirm against a fresh measurement of both: run-to-run
+                    // noise must not move the tuning
+                    double s_inc = 0, s_new = 0;
+                    st = measure(cur, s_inc);
+                    if (st == RT_OK) st = measure(t, s_new);
+                    if (st != RT_OK) break;
+                    const double inc = std::min(cur_s, s_inc), cand = std::min(s, s_new);
+                    if (cand < inc * 0.98) {
+                        cur = t;
+                        cur_s = cand;
+                        changed = true;
+                    } else {
+                        cur_s = inc;
+                    }
                 }
             }
         }
