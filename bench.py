@@ -413,7 +413,11 @@ def _batch_jobs(n):
 
 def run_batch(args):
     """64 independent scenes: plain (one rt_render per job, one after the
-    other) against rt_batch_render on several lanes; same films."""
+    other) against rt_batch_render on several lanes and under the autotuner's
+    choice; same films.  The timed runs render into device films allocated
+    once (the tuner times the same way); `e2e` is the fastest configuration
+    again into host films (device-to-host copies and host allocation
+    included)."""
     import torch
     import raytracer_gb300 as R
     torch.cuda.init()
@@ -426,63 +430,82 @@ def run_batch(args):
     upload_s = time.time() - t0
     work = [(g, spp, dict(seed=k)) for k, (g, (_, spp)) in enumerate(zip(scs, jobs))]
     total = sum(g.width * g.height * spp for g, spp, _ in work)
+    dev = [torch.zeros((g.height, g.width, 4), dtype=torch.float32, device="cuda") for g, _, _ in work]
+    ptrs = [f.data_ptr() for f in dev]
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        fn()
+        torch.cuda.synchronize()
+        return time.perf_counter() - t
+
+    def films_now():
+        return [f.cpu().numpy().copy() for f in dev]
+
     # warm-up: every scene once at 1 spp (tile tables, wavefront buffers)
     ctx.batch_render([(g, 1, dict(seed=0)) for g, _, _ in work])
-    for g, _, _ in work[:4]:
-        g.render(1)
-    torch.cuda.synchronize()
     clocks = ClockSampler(0)
     clocks.start()
-    for g, spp, o in work:   # untimed: the context's path buffers at their largest
-        g.render(spp, **o)
-    t0 = time.perf_counter()
-    plain = [g.render(spp, **o) for g, spp, o in work]
-    plain_s = time.perf_counter() - t0
+
+    def plain_run():
+        for (g, spp, o), p in zip(work, ptrs):
+            g.render(spp, film=p, **o)
+    plain_run()   # untimed: the context's path buffers at their largest
+    plain_s = timed(plain_run)
+    plain = films_now()
     res = {}
     default_tuning = ctx.get_tuning()
     for lanes in [int(x) for x in args.lanes.split(",")]:
         ctx.set_lanes(lanes)
-        ctx.batch_render(work)   # untimed: grows the new lanes' path buffers
-        t0 = time.perf_counter()
-        films = ctx.batch_render(work)
-        dt = time.perf_counter() - t0
-        same = all(np.array_equal(a, b) for a, b in zip(films, plain))
-        res[lanes] = (dt, same)
+        ctx.batch_render(work, device_films=ptrs)   # untimed: grows the new lanes' path buffers
+        dt = timed(lambda: ctx.batch_render(work, device_films=ptrs))
+        res[lanes] = (dt, all(np.array_equal(a, b) for a, b in zip(films_now(), plain)))
     best = min(res, key=lambda k: res[k][0])
-    # the autotuner on a sample of the workload (every 4th job, at its full
-    # spp: batch sizes and path counts per job as in the workload), with the
-    # best lane count above (a 16-job sample does not tune lanes), then the
-    # whole batch under its choice
+    # the autotuner on the workload itself (as a farm tunes on its first
+    # batch and keeps the tuning for the next ones: smaller samples did not
+    # carry the 64 jobs' concurrency over the lanes), from the best lane count
+    # above, then a fresh timed run of the whole batch under its choice
     tuned = None
-    if not args.no_autotune:
-        ctx.set_tuning(**dict(default_tuning, lanes=best))
-        sample = work[::4]
-        t0 = time.perf_counter()
-        choice, sample_sps = ctx.autotune(sample, max_trials=args.tune_trials)
-        tune_s = time.perf_counter() - t0
-        ctx.batch_render(work)   # untimed: buffers and graphs of the chosen configuration
-        t0 = time.perf_counter()
-        films = ctx.batch_render(work)
-        dt = time.perf_counter() - t0
-        tuned = {"value": total / dt, "seconds": dt, "tuning": choice, "tune_seconds": tune_s,
-                 "sample_jobs": len(sample), "sample_samples_per_s": sample_sps,
-                 "films_equal_plain": all(np.array_equal(a, b) for a, b in zip(films, plain))}
-        ctx.set_tuning(**default_tuning)
-    clk = clocks.stop()
+    best_tuning = dict(default_tuning, lanes=best)
     best_s = res[best][0]
-    if tuned is not None and tuned["seconds"] < best_s:
-        best_s = tuned["seconds"]
+    if not args.no_autotune:
+        ctx.set_tuning(**best_tuning)
+        t0 = time.perf_counter()
+        choice, sample_sps = ctx.autotune(work, max_trials=args.tune_trials)
+        tune_s = time.perf_counter() - t0
+        ctx.batch_render(work, device_films=ptrs)   # untimed: buffers and graphs of the choice
+        dt = timed(lambda: ctx.batch_render(work, device_films=ptrs))
+        tuned = {"value": total / dt, "seconds": dt, "tuning": choice, "tune_seconds": tune_s,
+                 "sample_jobs": len(work), "sample_samples_per_s": sample_sps,
+                 "films_equal_plain": all(np.array_equal(a, b) for a, b in zip(films_now(), plain))}
+        if dt < best_s:
+            best_s, best_tuning = dt, choice
+    # end to end: the fastest configuration into host films
+    ctx.set_tuning(**best_tuning)
+    ctx.batch_render(work)
+    t0 = time.perf_counter()
+    host = ctx.batch_render(work)
+    e2e_s = time.perf_counter() - t0
+    e2e_same = all(np.array_equal(a, b) for a, b in zip(host, plain))
+    ctx.set_tuning(**default_tuning)
+    clk = clocks.stop()
+    d2h = int(sum(g.width * g.height * 16 for g, _, _ in work))
     line = {"metric": METRIC, "value": total / best_s, "unit": UNIT, "n_gpus": 1, "higher_is_better": True,
             "workload": "batch%d" % len(jobs), "dtype": "f32", "data": "synthetic (seeded scenes)",
             "config": {"jobs": len(jobs), "total_samples": total,
                        "triangles": int(sum(s.n_triangles for s, _ in jobs)),
                        "pixels": int(sum(g.width * g.height for g in scs)), "max_depth": 12,
+                       "films": "device (allocated once)",
                        "scene_gen_s": round(gen_s, 2), "scene_build_upload_s": round(upload_s, 2)},
             "plain": {"value": total / plain_s, "seconds": plain_s},
             "batched": {str(k): {"value": total / v[0], "seconds": v[0], "films_equal_plain": v[1]}
                         for k, v in res.items()},
-            "autotuned": tuned, "default_tuning": default_tuning,
-            "best_lanes": best, "speedup_vs_plain": plain_s / best_s, "clocks": clk}
+            "autotuned": tuned, "default_tuning": default_tuning, "best_tuning": best_tuning,
+            "best_lanes": best, "speedup_vs_plain": plain_s / best_s,
+            "e2e": {"value": total / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": d2h,
+                    "films_equal_plain": e2e_same},
+            "clocks": clk}
     print(json.dumps(line))
 
 
@@ -551,7 +574,7 @@ def main():
     ap.add_argument("--batch-jobs", type=int, default=64)
     ap.add_argument("--lanes", default="2,4,8", help="batch: lane counts to time")
     ap.add_argument("--no-autotune", action="store_true", help="batch: skip the autotuned run")
-    ap.add_argument("--tune-trials", type=int, default=24, help="batch: autotuner trial budget")
+    ap.add_argument("--tune-trials", type=int, default=20, help="batch: autotuner trial budget")
     ap.add_argument("--graphs", type=int, default=0, choices=[0, 1],
                     help="launch each wavefront batch as a CUDA graph (render and serve workloads)")
     ap.add_argument("--sort-threshold", type=int, default=0,

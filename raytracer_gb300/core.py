@@ -187,15 +187,24 @@ class Context:
             scenes[i] = sc.h
         return scenes, descs
 
-    def batch_render(self, jobs):
+    def batch_render(self, jobs, device_films=None):
         """Render independent jobs in one call (rt_batch_render).  `jobs` is
         a list of (Scene, spp, options) with the options of Scene.render
         (seed, sample_begin, block, max_depth, ...); returns the list of
-        (H, W, 4) host films, each equal to that job's Scene.render film."""
+        (H, W, 4) host films, each equal to that job's Scene.render film.
+        With `device_films` (one int device address of an H*W*4 float32
+        buffer per job) the films are written there and None is returned."""
         n = len(jobs)
         scenes, descs = self._jobs(jobs)
-        films = []
         fptr = (C.c_void_p * n)()
+        if device_films is not None:
+            if len(device_films) != n:
+                raise ValueError("one device film per job")
+            for i, f in enumerate(device_films):
+                fptr[i] = int(f)
+            _check(lib().rt_batch_render(self.h, scenes, descs, n, fptr, 1))
+            return None
+        films = []
         for i, (sc, _, _) in enumerate(jobs):
             f = np.zeros((sc.height, sc.width, 4), np.float32)
             films.append(f)
