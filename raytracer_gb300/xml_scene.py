@@ -327,13 +327,18 @@ class _Loader:
 
     def _conductor_ior(self, p):
         """IORHelper::evalConductorIOR (tools/Common.cpp:56-81): a named
-        material's spectra, else the eta and absorption colors."""
+        material's RGB eta and k (the caller's `materials`, else the
+        reference's eight names converted from its data/IOR spectra), else
+        the eta and absorption colors; an unknown name is reported and falls
+        back to the colors, as in the reference."""
+        from .conductor_ior import MATERIALS
         mat = p.get("material", "")
         if mat:
-            if mat not in self.materials:
-                raise UnsupportedScene("conductor material %r needs its eta/k: pass materials={%r: (eta, k)}"
-                                       % (mat, mat))
-            return self.materials[mat]
+            if mat in self.materials:
+                return self.materials[mat]
+            if mat in MATERIALS:
+                return MATERIALS[mat]
+            warnings.warn("material %s not found" % mat)
         return p.get("eta", (0.0, 0.0, 0.0)), p.get("absorption", (0.0, 0.0, 0.0))
 
     def phase(self, p):
@@ -587,6 +592,7 @@ def load_vol(path):
 
 def load_scene(path, materials=None):
     """Read a reference scene file.  `materials` maps conductor material
-    names (material="gold") to (eta rgb, k rgb); the reference derives them
+    names (material="gold") to (eta rgb, k rgb), overriding the reference's
+    eight names (conductor_ior.py); the reference derives them
     from spectral data files (tools/Common.cpp:56-81)."""
     return _Loader(path, materials).load()

@@ -298,3 +298,41 @@ def test_xml_two_sides_forms(built, tmp_path):
     open(tmp_path / "m.xml", "w").write(text[:first] + two + text[end:])
     with pytest.raises(UnsupportedScene):
         load_scene(str(tmp_path / "m.xml"))
+
+
+def test_conductor_material_names(built, tmp_path):
+    """material="gold" (and the other seven names of tools/Common.cpp:44-54)
+    gives the RGB eta/k the reference converts from its data/IOR spectra;
+    a caller's materials= mapping overrides; an unknown name falls back to
+    the eta and absorption colors with a warning, as in the reference."""
+    from raytracer_gb300.conductor_ior import MATERIALS
+    assert set(MATERIALS) == {"gold", "silver", "aluminium", "copper", "chromium", "iron", "nickel", "tin"}
+    s = scenes.cornell_box(8, 8)
+    s.meshes[3]["bsdf"] = s.add_bsdf(D.bsdf(D.BSDF_ROUGH_CONDUCTOR, eta=(0.5, 0.5, 0.5), k=(1, 1, 1)))
+    text = open(write_scene(s, str(tmp_path))).read()
+    i = text.index('<bsdf type="RoughConductor">') + len('<bsdf type="RoughConductor">')
+    named = text[:i] + '<string name="material" value="gold"/>' + text[i:]
+    open(tmp_path / "g.xml", "w").write(named)
+    t = load_scene(str(tmp_path / "g.xml"))
+    b = t.bsdfs[t.meshes[3]["bsdf"]]
+    assert np.allclose(b["eta"], MATERIALS["gold"][0]) and np.allclose(b["k"], MATERIALS["gold"][1])
+    t = load_scene(str(tmp_path / "g.xml"), materials={"gold": ((1, 2, 3), (4, 5, 6))})
+    assert tuple(t.bsdfs[t.meshes[3]["bsdf"]]["eta"]) == (1, 2, 3)
+    open(tmp_path / "u.xml", "w").write(named.replace('value="gold"', 'value="unobtainium"'))
+    with pytest.warns(UserWarning):
+        t = load_scene(str(tmp_path / "u.xml"))
+    assert np.allclose(t.bsdfs[t.meshes[3]["bsdf"]]["eta"], (0.5, 0.5, 0.5))
+
+
+def test_conductor_table_matches_the_reference_data():
+    """The committed table is what make_conductor_ior.py computes from the
+    reference's spectra and CIE tables (where the reference tree exists)."""
+    import os
+    from raytracer_gb300 import make_conductor_ior as M
+    from raytracer_gb300.conductor_ior import MATERIALS
+    if not os.path.isdir(M.REFERENCE_ROOT):
+        pytest.skip("reference tree not present")
+    assert M.compute() == MATERIALS
+    # gold lands where published RGB fits of Au do (eta low in red, k ~ 4, 2.4, 1.6)
+    eta, k = MATERIALS["gold"]
+    assert 0.1 < eta[0] < 0.2 and 1.3 < eta[2] < 1.6 and 3.8 < k[0] < 4.1
