@@ -11,12 +11,15 @@ the element.  Paths in the file are resolved against the file's folder
                  sizeX, sizeY, apertureRadius, focalPlane (Camera.cpp:11-14),
                  <transform> = camera to world, <filter> BoxFilter, GaussianFilter,
                  MitchellNetravaliFilter (radiusX, radiusY, alpha/omega, B/C)
-    sampler      RandomSampler: sampleNumber -> `spp` (RandomSampler.cpp:10)
+    sampler      RandomSampler, StratifiedSampler: sampleNumber -> `spp`
+                 (RandomSampler.cpp:10, StratifiedSampler.cpp:23); every path draws
+                 from its own stream
     parameters   blockSizeX, blockSizeY -> `block`, fileName -> `file_name`
                  (XMLLoader.cpp:217-259)
     medium       (top level) the camera medium (XMLLoader.cpp:96-101; the later
                  referable-medium branch of the reference is unreachable)
-    lights       EnvironmentLight: path (.hdr), toWorld, scale (EnvironmentLight.cpp:8-19)
+    lights       EnvironmentLight: path (.hdr, .exr, PNG...), toWorld, scale, gamma
+                 (EnvironmentLight.cpp:8-19)
     objects      shape Mesh (path .obj, toWorld; MeshFactory.h:39-139), Cube
                  (toWorld; Cube.cpp), Sphere (radius, toWorld; Sphere.cpp:14-15),
                  each with <bsdf>, <light type="AreaLight|MeshLight"> (radiance),
@@ -42,6 +45,23 @@ import numpy as np
 from . import desc as D
 
 F32 = np.float32
+
+
+# The reference's object factories match type names without regard to case
+# (ObjectFactoryManager::formatType, factory/ObjectFactoryManager.h:81-89):
+# "roughconductor" is RoughConductor.  _type gives the spelling used here.
+_TYPE_NAMES = ["ConstantTexture", "ImageTexture", "Diffuse", "RoughConductor", "RoughDielectric",
+               "SmoothLayeredBSDF", "LayeredBSDF", "Dielectric", "Conductor", "Mirror", "TwoSides",
+               "HGPhaseFunction", "IsotropicPhaseFunction", "Homogeneous", "Heterogeneous", "Mesh", "Cube", "Sphere",
+               "MeshLight", "AreaLight", "NoriPerspective", "BoxFilter", "GaussianFilter", "MitchellNetravaliFilter",
+               "EnvironmentLight", "RandomSampler", "StratifiedSampler", "PathTracingMIS", "VolPathTracing",
+               "GridVolume"]
+_CANON = {n.lower(): n for n in _TYPE_NAMES}
+
+
+def _type(el):
+    t = el.get("type") or ""
+    return _CANON.get(t.lower(), t)
 
 
 class UnsupportedScene(ValueError):
@@ -185,7 +205,7 @@ class _Loader:
                 else:
                     params[name] = _transform(c)
             elif tag == "texture":
-                kind = c.get("type")
+                kind = _type(c)
                 tp = self.props(c)
                 if kind == "ConstantTexture":
                     params[name] = ("texture", tp.get("albedo", (0.5, 0.5, 0.5)))   # ConstantTexture.cpp:6-10
@@ -203,9 +223,9 @@ class _Loader:
             elif tag == "medium":
                 params[name] = self.ref_medium[c.get("ref")] if c.get("ref") else self.medium(c)
             elif tag == "phase":
-                params[name] = ("phase", c.get("type"), self.props(c))
+                params[name] = ("phase", _type(c), self.props(c))
             elif tag == "volume":
-                params[name] = ("volume", c.get("type"), self.props(c))
+                params[name] = ("volume", _type(c), self.props(c))
             else:
                 warnings.warn("unknown property %s" % name)
         return params
@@ -250,7 +270,7 @@ class _Loader:
 
     # BSDFs: returns the index in the scene's BSDF table
     def bsdf(self, el, params=None):
-        kind = el.get("type")
+        kind = _type(el)
         p = self.props(el) if params is None else params
         if kind == "Diffuse":   # Diffuse.cpp:11-18
             b = D.bsdf(D.BSDF_DIFFUSE, albedo=self._tex_or(p, "albedo", (0.5, 0.5, 0.5)),
@@ -353,7 +373,7 @@ class _Loader:
         raise UnsupportedScene("phase function %s is not provided" % kind)
 
     def medium(self, el):
-        kind = el.get("type")
+        kind = _type(el)
         p = self.props(el)
         if p.get("temperature", 0.0) or p.get("scaleEmissivity", 1.0) != 1.0:
             raise UnsupportedScene("emissive media are not provided")
@@ -375,7 +395,7 @@ class _Loader:
 
     # XMLLoader::handleObject (XMLLoader.cpp:293-398)
     def shape(self, el):
-        kind = el.get("type")
+        kind = _type(el)
         bsdf, light = -1, None
         rest = []
         for c in el:
@@ -388,7 +408,7 @@ class _Loader:
                 if light is not None:
                     warnings.warn("only 1 light allowed for %s" % kind)
                     continue
-                light = (c.get("type"), self.props(c))
+                light = (_type(c), self.props(c))
             elif c.tag == "bssrdf":
                 raise UnsupportedScene("BSSRDFs are not provided")
             else:
@@ -427,7 +447,7 @@ class _Loader:
             raise UnsupportedScene("shape type %s is not provided" % kind)
 
     def camera(self, el):
-        kind = el.get("type")
+        kind = _type(el)
         if kind != "NoriPerspective":
             raise UnsupportedScene("camera type %s is not provided" % kind)
         rest = []
@@ -437,7 +457,7 @@ class _Loader:
             elif c.tag == "filter":   # ReconstructionFilter.cpp:12-18 and the filters' constructors
                 fp = self.props(c)
                 rx, ry = fp.get("radiusX", 0.5), fp.get("radiusY", 0.5)
-                kind = c.get("type")
+                kind = _type(c)
                 if kind == "BoxFilter":
                     self.filter = D.box_filter(rx, ry)
                 elif kind == "GaussianFilter":
@@ -454,18 +474,20 @@ class _Loader:
 
     def lights(self, el):
         for c in el:
-            kind = c.get("type")
+            kind = _type(c)
             p = self.props(c)
             if kind != "EnvironmentLight":
                 raise UnsupportedScene("light type %s is not provided" % kind)
-            if p.get("isProbe", False) or p.get("gamma", 0.0) not in (0.0, 1.0) or p.get("offsetU", 0.0) \
-                    or p.get("offsetV", 0.0):
-                raise UnsupportedScene("EnvironmentLight isProbe / gamma / offsets are not provided")
-            from .core import load_hdr
+            if p.get("isProbe", False) or p.get("offsetU", 0.0) or p.get("offsetV", 0.0):
+                raise UnsupportedScene("EnvironmentLight isProbe / offsets are not provided")
+            # ImageLoader::load(path, ALL, gamma) (EnvironmentLight.cpp:18):
+            # .hdr and .exr linear, 8-bit images decoded from sRGB
+            from .images import ImageError, load_image
             path = self.resolve(p.get("path", ""))
-            if not path.lower().endswith(".hdr"):
-                raise UnsupportedScene("environment maps other than Radiance .hdr are not provided")
-            rgb = load_hdr(path)
+            try:
+                rgb = load_image(path, gamma=float(p.get("gamma", 0.0)))
+            except (ImageError, OSError) as e:
+                raise UnsupportedScene("EnvironmentLight %s: %s" % (p.get("path", ""), e))
             self.s.add_env_light(rgb, scale=p.get("scale", 1.0),
                                  to_world=np.asarray(p.get("toWorld", np.eye(4)), np.float64))
 
@@ -488,11 +510,16 @@ class _Loader:
                         self.file_name = (c.text or "").strip()
                 self.block = (bx, by)
             elif key == "sampler":
-                if el.get("type") != "RandomSampler":
+                # the device draws every path from its own stream (the
+                # path-stream sampler); a StratifiedSampler's sample count is
+                # kept, its stratification is not
+                if _type(el) == "StratifiedSampler":
+                    warnings.warn("StratifiedSampler: rendered with per-path random streams")
+                elif _type(el) != "RandomSampler":
                     raise UnsupportedScene("sampler %s is not provided" % el.get("type"))
                 self.spp = int(self.props(el).get("sampleNumber", 1))
             elif key == "integrator":
-                kind = el.get("type")
+                kind = _type(el)
                 p = self.props(el)
                 ig = {"PathTracingMIS": D.INTEGRATOR_PATH_MIS, "VolPathTracing": D.INTEGRATOR_VOLPATH}.get(kind)
                 if ig is None:

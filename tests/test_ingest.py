@@ -336,3 +336,39 @@ def test_conductor_table_matches_the_reference_data():
     # gold lands where published RGB fits of Au do (eta low in red, k ~ 4, 2.4, 1.6)
     eta, k = MATERIALS["gold"]
     assert 0.1 < eta[0] < 0.2 and 1.3 < eta[2] < 1.6 and 3.8 < k[0] < 4.1
+
+
+def test_type_names_ignore_case(built, tmp_path):
+    """The reference's factories match type names without regard to case
+    (ObjectFactoryManager::formatType): a file written with lower-case type
+    names loads to the same scene."""
+    import re
+    s = scenes.cornell_smooth(16, 12)
+    text = open(write_scene(s, str(tmp_path))).read()
+    lower = re.sub(r'type="([A-Za-z]+)"', lambda m: 'type="%s"' % m.group(1).lower(), text)
+    assert lower != text
+    open(tmp_path / "lower.xml", "w").write(lower)
+    t = load_scene(str(tmp_path / "lower.xml"))
+    _same_scene(s, t)
+    fa, fb = _films_equal(s, t)
+    assert np.array_equal(fa, fb)
+
+
+def test_exr_environment_map_and_stratified_sampler(built, tmp_path):
+    """EnvironmentLight reads its image through ImageLoader (EXR linear);
+    a StratifiedSampler file loads with a warning, its sample count kept."""
+    from raytracer_gb300.exr import write_exr
+    s = scenes.displaced_icosphere(level=1, width=8, height=8, env_size=(32, 16))
+    text = open(write_scene(s, str(tmp_path), spp=6)).read()
+    env = s.lights[s.env_light]["rgb"]
+    write_exr(str(tmp_path / "sky.exr"), env)
+    i = text.index('.hdr"')
+    j = text.rindex('"', 0, i)
+    text = text[:j + 1] + "sky.exr" + text[i + 4:]
+    open(tmp_path / "e.xml", "w").write(text.replace('type="RandomSampler"', 'type="StratifiedSampler"'))
+    with pytest.warns(UserWarning):
+        t = load_scene(str(tmp_path / "e.xml"))
+    assert t.spp == 6
+    with np.errstate(over="ignore"):
+        expect = env.astype(np.float16).astype(np.float32)
+    assert np.array_equal(t.lights[t.env_light]["rgb"], expect)
