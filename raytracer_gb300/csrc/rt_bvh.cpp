@@ -44,6 +44,7 @@ struct Builder {
     std::vector<float> cen;   // 3 per triangle
     std::vector<int> order;
     int max_leaf, n_bins;
+    double c_node = 1.0;   // SAH cost of a node visit, in triangle tests
 
     // Build subtree over order[b, e); returns nodes appended into `out`
     // (local indices) with the subtree root first.
@@ -92,7 +93,7 @@ struct Builder {
         }
         double parea = box.area();
         double leaf_cost = (double)n;
-        double split_cost = parea > 0 ? 1.0 + best_cost / parea : INFINITY;
+        double split_cost = parea > 0 ? c_node + best_cost / parea : INFINITY;
         if (n <= max_leaf && (best_axis < 0 || leaf_cost <= split_cost)) {
             out[self].leaf = true; out[self].first = b; out[self].count = n;
             return;
@@ -157,7 +158,7 @@ inline void widen(const Box &b, float scale_eps, float out[6])
 
 }  // namespace
 
-void build_bvh2(const float *tv, int n, BvhImage &img, int max_leaf, int n_bins)
+void build_bvh2(const float *tv, int n, BvhImage &img, int max_leaf, int n_bins, double c_node)
 {
     img = BvhImage();
     if (n <= 0) return;
@@ -166,6 +167,7 @@ void build_bvh2(const float *tv, int n, BvhImage &img, int max_leaf, int n_bins)
     B.tv = tv;
     B.max_leaf = max_leaf;
     B.n_bins = n_bins;
+    B.c_node = c_node;
     B.tb.resize(n);
     B.cen.resize(3 * (size_t)n);
     B.order.resize(n);

@@ -46,7 +46,9 @@ struct WideBvhImage {
 // Build from triangle vertex positions (9 floats per triangle).  Boxes are
 // widened outward by a few ulps so the fused slab test never culls a node
 // that contains a hit the exact Moller-Trumbore test accepts.
-void build_bvh2(const float *tri_v, int n_tris, BvhImage &out, int max_leaf = 4, int n_bins = 32);
+// c_node: the SAH cost of visiting a node, in units of one triangle test
+void build_bvh2(const float *tri_v, int n_tris, BvhImage &out, int max_leaf = 4, int n_bins = 32,
+                double c_node = 1.0);
 
 // Binned-SAH binary tree (leaves of at most 3 triangles) collapsed into the
 // compressed 8-wide layout above, greedily opening the child of largest
