@@ -59,7 +59,11 @@ enum { RT_BSDF_DIFFUSE = 0, RT_BSDF_ROUGH_CONDUCTOR = 1,
        /* smooth (delta) BSDFs: bsdf/Dielectric.cpp, Conductor.cpp, Mirror.cpp.
         * Dielectric reads reflectance, transmittance, eta_int and eta_ext;
         * Conductor reads reflectance, eta and k; Mirror reads nothing. */
-       RT_BSDF_DIELECTRIC = 5, RT_BSDF_CONDUCTOR = 6, RT_BSDF_MIRROR = 7 };
+       RT_BSDF_DIELECTRIC = 5, RT_BSDF_CONDUCTOR = 6, RT_BSDF_MIRROR = 7,
+       /* bsdf/SheetDielectric.cpp (reflectance, transmittance, eta_int,
+        * eta_ext) and bsdf/Microfacet.cpp (albedo = kd, alpha, eta_int,
+        * eta_ext, distribution, ks = probabilitySpecular) */
+       RT_BSDF_SHEET_DIELECTRIC = 8, RT_BSDF_MICROFACET = 9 };
 /* bsdf/MicrofacetDistribution.h:9-13 name order */
 enum { RT_DIST_BECKMANN = 0, RT_DIST_PHONG = 1, RT_DIST_GGX = 2 };
 
@@ -86,10 +90,12 @@ typedef struct rt_bsdf_desc {
     int32_t two_sided;
     /* ImageTextures replacing the constants above at each hit's texture
      * coordinates: index + 1 into rt_scene_desc.textures, 0 = the constant.
-     * albedo: Diffuse; reflectance: RoughConductor, RoughDielectric,
-     * Dielectric, Conductor; transmittance: RoughDielectric, Dielectric;
+     * albedo: Diffuse, Microfacet (kd); reflectance: RoughConductor,
+     * RoughDielectric, Dielectric, Conductor, SheetDielectric; transmittance:
+     * RoughDielectric, Dielectric, SheetDielectric;
      * alpha (the texel's channel average): RoughConductor, RoughDielectric. */
     int32_t tex_albedo, tex_reflectance, tex_transmittance, tex_alpha;
+    float ks;                /* Microfacet "probabilitySpecular", default 1      */
 } rt_bsdf_desc;
 
 /* ImageTexture (texture/ImageTexture.cpp:8-70): a linear RGB image as

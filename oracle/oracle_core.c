@@ -856,6 +856,87 @@ static c3 o_mr_sample(o_bsdf_rec *r)
     return cfill(1.f);
 }
 
+/* SheetDielectric::sample (SheetDielectric.cpp:122-174): reflect with the
+ * sheet's inter-reflections fr + T^2 fr / (1 - fr^2), else straight through,
+ * typed UNKNOWN (so MIS applies to what the straight ray finds) */
+static c3 o_sd_sample(const rt_bsdf_desc *b, o_bsdf_rec *r, v2 s)
+{
+    float cosThetaI = r->wi.z;
+    float etaI = b->eta_ext, etaT = b->eta_int;
+    float relativeEta = etaI / etaT;
+    float sinThetaT = relativeEta * sqrtf(fmaxf(0.f, 1 - cosThetaI * cosThetaI));
+    float cosThetaT = sqrtf(fmaxf(0.f, 1 - sinThetaT * sinThetaT));
+    float fr = o_fresnel_dielectric(etaI, etaT, fabsf(cosThetaI), cosThetaT);
+    float T = 1.f - fr;
+    if (fr < 1.f) fr += T * T * fr / (1.f - fr * fr);
+    r->relative_eta = 1.f;
+    if (s.x <= fr) {
+        r->sampled_type = O_BSDF_DELTA_REFLECTION;
+        r->wo = o_reflect_local(r->wi);
+        r->pdf = fr;
+        return c3_from(b->reflectance);
+    }
+    r->sampled_type = O_BSDF_UNKNOWN;
+    r->wo = v3_neg(r->wi);
+    r->pdf = 1 - fr;
+    return c3_from(b->transmittance);
+}
+
+/* ===================== Microfacet (bsdf/Microfacet.cpp:62-182) ===================== */
+/* Microfacet::fresnel (:92-118): a grey dielectric Fresnel term */
+static float o_nf_fresnel(float etaExt, float etaInt, float cosThetaI)
+{
+    float etaI = etaExt, etaT = etaInt;
+    if (cosThetaI <= 0.f) { float t = etaI; etaI = etaT; etaT = t; }
+    float relativeEta = etaI / etaT;
+    float sinThetaT = relativeEta * sqrtf(fmaxf(0.f, 1 - cosThetaI * cosThetaI));
+    float cosThetaT = sqrtf(fmaxf(0.f, 1 - sinThetaT * sinThetaT));
+    if (sinThetaT >= 1.f) return 1.f;
+    return o_fresnel_dielectric(etaI, etaT, fabsf(cosThetaI), cosThetaT);
+}
+/* Microfacet::eval (:76-90) */
+static c3 o_nf_eval(const rt_bsdf_desc *b, v3 wi, v3 wo)
+{
+    float cosThetaI = wi.z, cosThetaO = wo.z;
+    if (cosThetaI <= 0.f || cosThetaO <= 0.f) return cfill(0.f);
+    v3 wh = v3_normalized(v3_add(wi, wo));
+    c3 diffusePart = c3_muls(c3_muls(c3_from(b->albedo), 1 - b->ks), O_INV_PI);
+    float F = o_nf_fresnel(b->eta_ext, b->eta_int, v3_dot(wi, wh));
+    c3 specularPart = cfill(b->ks * o_mf_D(b->distribution, wh, b->alpha) * F);
+    specularPart = c3_muls(specularPart, o_mf_G(b->distribution, wi, wo, wh, b->alpha));
+    specularPart = c3_divs(specularPart, 4 * cosThetaI * cosThetaO);
+    return c3_add(diffusePart, specularPart);
+}
+/* Microfacet::pdf (:166-182) */
+static float o_nf_pdf(const rt_bsdf_desc *b, v3 wi, v3 wo)
+{
+    float cosThetaI = wi.z, cosThetaO = wo.z;
+    v3 wh = v3_normalized(v3_add(wi, wo));
+    float cosThetaH = wh.z;
+    float alpha = o_adjusted_alpha(b->alpha, cosThetaI);
+    float Jh = 1.f / (4 * v3_dot(wh, wo));
+    return b->ks * o_mf_D(b->distribution, wh, alpha) * cosThetaH * Jh + (1 - b->ks) * cosThetaO * O_INV_PI;
+}
+/* Microfacet::sample (:120-164): the normal is drawn first, then sample.x
+ * picks the specular lobe (probability ks) or the cosine lobe */
+static c3 o_nf_sample(const rt_bsdf_desc *b, o_bsdf_rec *r, v2 s)
+{
+    if (r->wi.z <= 0.f) return cfill(0.f);
+    float alpha = o_adjusted_alpha(b->alpha, r->wi.z);
+    v3 normal = o_mf_sample_normal(b->distribution, s, alpha);
+    if (s.x <= b->ks) {
+        r->sampled_type = O_BSDF_GLOSSY_REFLECTION;
+        r->wo = o_reflect_n(r->wi, normal);
+    } else {
+        r->sampled_type = O_BSDF_DIFFUSE;
+        r->wo = o_square_to_cosine_hemisphere(s);
+    }
+    float cosThetaO = r->wo.z;
+    r->pdf = o_nf_pdf(b, r->wi, r->wo);
+    if (r->pdf == 0.f) return cfill(0.f);
+    return c3_divs(c3_muls(o_nf_eval(b, r->wi, r->wo), fabsf(cosThetaO)), r->pdf);
+}
+
 /* ===================== BSDF dispatch ===================== */
 static c3 o_bsdf_eval1(const rt_bsdf_desc *b, v3 wi, v3 wo)
 {
@@ -865,8 +946,9 @@ static c3 o_bsdf_eval1(const rt_bsdf_desc *b, v3 wi, v3 wo)
     case RT_BSDF_ROUGH_DIELECTRIC: return o_rd_eval(b, wi, wo);
     case RT_BSDF_SMOOTH_LAYERED: return o_sl_eval(b, wi, wo);
     case RT_BSDF_LAYERED: return o_ly_eval(b, wi, wo);
+    case RT_BSDF_MICROFACET: return o_nf_eval(b, wi, wo);
     }
-    return cfill(0.f);   /* Dielectric, Conductor, Mirror */
+    return cfill(0.f);   /* Dielectric, Conductor, Mirror, SheetDielectric */
 }
 static float o_bsdf_pdf1(const rt_bsdf_desc *b, v3 wi, v3 wo)
 {
@@ -876,6 +958,7 @@ static float o_bsdf_pdf1(const rt_bsdf_desc *b, v3 wi, v3 wo)
     case RT_BSDF_ROUGH_DIELECTRIC: return o_rd_pdf(b, wi, wo);
     case RT_BSDF_SMOOTH_LAYERED: return o_sl_pdf(b, wi, wo);
     case RT_BSDF_LAYERED: return o_ly_pdf(b, wi, wo);
+    case RT_BSDF_MICROFACET: return o_nf_pdf(b, wi, wo);
     }
     return 0.f;
 }
@@ -890,6 +973,8 @@ static c3 o_bsdf_sample1(const rt_bsdf_desc *b, o_bsdf_rec *r, v2 s, uint64_t au
     case RT_BSDF_DIELECTRIC: return o_dl_sample(b, r, s);
     case RT_BSDF_CONDUCTOR: return o_cd_sample(b, r);
     case RT_BSDF_MIRROR: return o_mr_sample(r);
+    case RT_BSDF_SHEET_DIELECTRIC: return o_sd_sample(b, r, s);
+    case RT_BSDF_MICROFACET: return o_nf_sample(b, r, s);
     }
     return cfill(0.f);
 }

@@ -162,7 +162,7 @@ __device__ __forceinline__ void classify_hit(const RenderParams &P, RoundCounter
     } else {
 #pragma unroll
         for (int k = 0; k < RT_NBSDF; k++) q_push(P.W.q_mat[k], &C->mat[k], slot, t == k);
-        if (P.S.has_textured) q_push(P.W.q_mixed, &C->mixed, slot, t == RT_QUEUE_MIXED);
+        if (P.S.has_mixed) q_push(P.W.q_mixed, &C->mixed, slot, t == RT_QUEUE_MIXED);
     }
     q_push(P.W.q_fin, &C->fin, slot, t < 0);
 }
@@ -796,6 +796,7 @@ __device__ __forceinline__ C3 bsdf_sample1_t(const DevBsdf &b, BsdfRec &r, V2 s,
     if (BT == 4) return ly_sample(b, r, s, aux_key);
     if (b.type == RT_BSDF_DIELECTRIC) return dl_sample(b, r, s);
     if (b.type == RT_BSDF_CONDUCTOR) return cd_sample(b, r);
+    if (b.type == RT_BSDF_SHEET_DIELECTRIC) return sd_sample(b, r, s);
     return mr_sample(r);
 }
 template <int BT>
@@ -1611,16 +1612,17 @@ static rt_status validate(const rt_scene_desc *d)
     }
     for (int b = 0; b < d->n_bsdfs; b++) {
         const rt_bsdf_desc &B = d->bsdfs[b];
-        if (B.type < 0 || B.type > RT_BSDF_MIRROR) return fail(RT_ERR_UNSUPPORTED, "BSDF type not supported");
+        if (B.type < 0 || B.type > RT_BSDF_MICROFACET) return fail(RT_ERR_UNSUPPORTED, "BSDF type not supported");
         const int32_t tx[4] = {B.tex_albedo, B.tex_reflectance, B.tex_transmittance, B.tex_alpha};
         for (int k = 0; k < 4; k++)
             if (tx[k] < 0 || tx[k] > d->n_textures) return fail(RT_ERR_INVALID, "BSDF texture index out of range");
         // the parameters each BSDF reads through a texture in the reference
         const int t = B.type;
-        const bool ok = (!B.tex_albedo || t == RT_BSDF_DIFFUSE) &&
+        const bool ok = (!B.tex_albedo || t == RT_BSDF_DIFFUSE || t == RT_BSDF_MICROFACET) &&
                         (!B.tex_reflectance || t == RT_BSDF_ROUGH_CONDUCTOR || t == RT_BSDF_ROUGH_DIELECTRIC ||
-                         t == RT_BSDF_DIELECTRIC || t == RT_BSDF_CONDUCTOR) &&
-                        (!B.tex_transmittance || t == RT_BSDF_ROUGH_DIELECTRIC || t == RT_BSDF_DIELECTRIC) &&
+                         t == RT_BSDF_DIELECTRIC || t == RT_BSDF_CONDUCTOR || t == RT_BSDF_SHEET_DIELECTRIC) &&
+                        (!B.tex_transmittance || t == RT_BSDF_ROUGH_DIELECTRIC || t == RT_BSDF_DIELECTRIC ||
+                         t == RT_BSDF_SHEET_DIELECTRIC) &&
                         (!B.tex_alpha || t == RT_BSDF_ROUGH_CONDUCTOR || t == RT_BSDF_ROUGH_DIELECTRIC);
         if (!ok) return fail(RT_ERR_UNSUPPORTED, "a texture on a parameter this BSDF type does not texture");
     }
@@ -1747,6 +1749,7 @@ rt_status rt_scene_create(rt_ctx *ctx, const rt_scene_desc *d, rt_scene **out)
         D.tex[TEX_TRANSMITTANCE] = B.tex_transmittance - 1;
         D.tex[TEX_ALPHA] = B.tex_alpha - 1;
         D.textured = (B.tex_albedo | B.tex_reflectance | B.tex_transmittance | B.tex_alpha) != 0;
+        D.ks = B.ks;
     }
     // media
     std::vector<DevMedium> media(d->n_media);
@@ -1894,7 +1897,10 @@ rt_status rt_scene_create(rt_ctx *ctx, const rt_scene_desc *d, rt_scene **out)
         S.textures = tp;
         S.n_textures = d->n_textures;
     }
-    for (const DevBsdf &b : bsdfs) S.has_textured |= b.textured;
+    for (const DevBsdf &b : bsdfs) {
+        S.has_textured |= b.textured;
+        S.has_mixed |= bsdf_queue_of(b) == RT_QUEUE_MIXED;
+    }
     if ((st = upload(sc, tri_mesh.data(), tri_mesh.size(), &ip)) != RT_OK) { rt_scene_destroy(sc); return st; }
     S.tri_mesh = ip;
     {
@@ -2676,8 +2682,8 @@ extern "C" rt_status rt_render_tile_static(rt_ctx *ctx, rt_scene *sc, const rt_r
     const DevCamera &cam = sc->S.cam;
     if (!(cam.filter == RT_FILTER_BOX && cam.frx == 0.5f && cam.fry == 0.5f))
         return fail(RT_ERR_UNSUPPORTED, "rt_render_tile_static: only the box filter of radius 0.5");
-    if (sc->S.has_textured)
-        return fail(RT_ERR_UNSUPPORTED, "rt_render_tile_static: textured BSDFs need rt_render");
+    if (sc->S.has_mixed)
+        return fail(RT_ERR_UNSUPPORTED, "rt_render_tile_static: textured and Microfacet BSDFs need rt_render");
     const int Wd = cam.width, H = cam.height;
     const int bx = rd->block_x > 0 ? rd->block_x : 32, by = rd->block_y > 0 ? rd->block_y : 32;
     if (bx > 0xffff || by > 0xffff) return fail(RT_ERR_INVALID, "block size too large");

@@ -39,6 +39,7 @@ struct DevBsdf {
     // albedo, reflectance, transmittance and alpha; textured = any of them
     int tex[4];
     int textured;
+    float ks;         // Microfacet "probabilitySpecular"
 };
 enum { TEX_ALBEDO = 0, TEX_REFLECTANCE = 1, TEX_TRANSMITTANCE = 2, TEX_ALPHA = 3 };
 
@@ -58,9 +59,10 @@ struct DevTexture {
 #define RT_QUEUE_DELTA 5
 #define RT_QUEUE_MIXED 6
 __host__ __device__ __forceinline__ int bsdf_queue(int type) { return type < RT_QUEUE_DELTA ? type : RT_QUEUE_DELTA; }
+// (Microfacet, type 9, shades from the mixed queue too)
 __host__ __device__ __forceinline__ int bsdf_queue_of(const DevBsdf &b)
 {
-    return b.textured ? RT_QUEUE_MIXED : bsdf_queue(b.type);
+    return (b.textured || b.type == 9) ? RT_QUEUE_MIXED : bsdf_queue(b.type);
 }
 
 struct DevLight {
@@ -125,7 +127,8 @@ struct DevScene {
     const float *tri_uv;        // 6 floats per triangle (uv0, uv1, uv2) or null; NaN: mesh without uvs
     const DevTexture *textures;
     int n_textures;
-    int has_textured;           // some BSDF is textured (the mixed shading queue is in use)
+    int has_textured;           // some BSDF is textured (hits carry texture coordinates)
+    int has_mixed;              // some BSDF shades from the mixed queue (bsdf_queue_of)
     const DevMesh *meshes;
     const float *mesh_cdf;
     int n_meshes;
@@ -1159,6 +1162,84 @@ __device__ __forceinline__ C3 mr_sample(BsdfRec &r)
     return cfill(1.f);
 }
 
+// SheetDielectric::sample (bsdf/SheetDielectric.cpp:122-174): reflection with
+// the thin sheet's summed inter-reflections fr + T^2 fr / (1 - fr^2), else
+// straight through (typed UNKNOWN there, not delta)
+__device__ __forceinline__ C3 sd_sample(const DevBsdf &b, BsdfRec &r, V2 s)
+{
+    float ci = r.wi.z;
+    float eI = b.eta_ext, eT = b.eta_int;
+    float rel = eI / eT;
+    float sinT = rel * sqrtf(smax(0.f, 1 - ci * ci));
+    float cT = sqrtf(smax(0.f, 1 - sinT * sinT));
+    float fr = fresnel_dielectric(eI, eT, fabsf(ci), cT);
+    float T = 1.f - fr;
+    if (fr < 1.f) fr = fr + ((T * T) * fr) / (1.f - fr * fr);
+    r.rel_eta = 1.f;
+    if (s.x <= fr) {
+        r.type = BT_DELTA_REFLECTION;
+        r.wo = v3(-r.wi.x, -r.wi.y, r.wi.z);
+        r.pdf = fr;
+        return cload(b.reflectance);
+    }
+    r.type = BT_UNKNOWN;
+    r.wo = -r.wi;
+    r.pdf = 1 - fr;
+    return cload(b.transmittance);
+}
+
+// Microfacet (bsdf/Microfacet.cpp:62-182): (1 - ks) Lambertian kd plus ks
+// times a dielectric-Fresnel microfacet lobe; its raw alpha; the sample's x
+// both picks the lobe and samples the normal
+__device__ __forceinline__ float nf_fresnel(float etaExt, float etaInt, float ci)
+{
+    float eI = etaExt, eT = etaInt;
+    if (ci <= 0.f) { float q = eI; eI = eT; eT = q; }
+    float rel = eI / eT;
+    float sinT = rel * sqrtf(smax(0.f, 1 - ci * ci));
+    float cT = sqrtf(smax(0.f, 1 - sinT * sinT));
+    if (sinT >= 1.f) return 1.f;
+    return fresnel_dielectric(eI, eT, fabsf(ci), cT);
+}
+__device__ __forceinline__ C3 nf_eval(const DevBsdf &b, V3 wi, V3 wo)
+{
+    float ci = wi.z, co = wo.z;
+    if (ci <= 0.f || co <= 0.f) return cfill(0.f);
+    V3 wh = normalized(wi + wo);
+    C3 diffuse = ((1 - b.ks) * cload(b.albedo)) * RT_INV_PI;
+    float F = nf_fresnel(b.eta_ext, b.eta_int, dot(wi, wh));
+    C3 spec = cfill((b.ks * mf_D(b.distribution, wh, b.alpha)) * F);
+    spec = spec * mf_G(b.distribution, wi, wo, wh, b.alpha);
+    spec = spec / ((4 * ci) * co);
+    return diffuse + spec;
+}
+__device__ __forceinline__ float nf_pdf(const DevBsdf &b, V3 wi, V3 wo)
+{
+    float ci = wi.z, co = wo.z;
+    V3 wh = normalized(wi + wo);
+    float ch = wh.z;
+    float alpha = adjusted_alpha(b.alpha, ci);
+    float Jh = 1.f / (4 * dot(wh, wo));
+    return (((b.ks * mf_D(b.distribution, wh, alpha)) * ch) * Jh) + (((1 - b.ks) * co) * RT_INV_PI);
+}
+__device__ __forceinline__ C3 nf_sample(const DevBsdf &b, BsdfRec &r, V2 s)
+{
+    if (r.wi.z <= 0.f) return cfill(0.f);
+    float alpha = adjusted_alpha(b.alpha, r.wi.z);
+    V3 n = mf_sample_normal(b.distribution, s, alpha);
+    if (s.x <= b.ks) {
+        r.type = BT_GLOSSY_REFLECTION;
+        r.wo = reflect_n(r.wi, n);
+    } else {
+        r.type = BT_DIFFUSE;
+        r.wo = cosine_hemisphere(s);
+    }
+    float co = r.wo.z;
+    r.pdf = nf_pdf(b, r.wi, r.wo);
+    if (r.pdf == 0.f) return cfill(0.f);
+    return (nf_eval(b, r.wi, r.wo) * fabsf(co)) / r.pdf;
+}
+
 // one BSDF type, no TwoSides wrapper
 __device__ __forceinline__ C3 bsdf_eval1(const DevBsdf &b, V3 wi, V3 wo)
 {
@@ -1168,6 +1249,7 @@ __device__ __forceinline__ C3 bsdf_eval1(const DevBsdf &b, V3 wi, V3 wo)
     case 2: return rd_eval(b, wi, wo);
     case 3: return sl_eval(b, wi, wo);
     case 4: return ly_eval(b, wi, wo);
+    case 9: return nf_eval(b, wi, wo);
     default: return cfill(0.f);
     }
 }
@@ -1179,6 +1261,7 @@ __device__ __forceinline__ float bsdf_pdf1(const DevBsdf &b, V3 wi, V3 wo)
     case 2: return rd_pdf(b, wi, wo);
     case 3: return sl_pdf(b, wi, wo);
     case 4: return ly_pdf(b, wi, wo);
+    case 9: return nf_pdf(b, wi, wo);
     default: return 0.f;
     }
 }
@@ -1192,6 +1275,8 @@ __device__ __forceinline__ C3 bsdf_sample1(const DevBsdf &b, BsdfRec &r, V2 s, u
     case 4: return ly_sample(b, r, s, aux_key);
     case 5: return dl_sample(b, r, s);
     case 6: return cd_sample(b, r);
+    case 8: return sd_sample(b, r, s);
+    case 9: return nf_sample(b, r, s);
     default: return mr_sample(r);
     }
 }

@@ -15,6 +15,7 @@ i3 = C.c_int32 * 3
 
 BSDF_DIFFUSE, BSDF_ROUGH_CONDUCTOR, BSDF_ROUGH_DIELECTRIC, BSDF_SMOOTH_LAYERED, BSDF_LAYERED = 0, 1, 2, 3, 4
 BSDF_DIELECTRIC, BSDF_CONDUCTOR, BSDF_MIRROR = 5, 6, 7
+BSDF_SHEET_DIELECTRIC, BSDF_MICROFACET = 8, 9
 DIST_BECKMANN, DIST_PHONG, DIST_GGX = 0, 1, 2
 LIGHT_AREA, LIGHT_ENV = 0, 1
 SHAPE_MESH, SHAPE_SPHERE = 0, 1
@@ -28,7 +29,8 @@ BSDF_OP_EVAL, BSDF_OP_PDF, BSDF_OP_SAMPLE = 0, 1, 2
 BSDF_TYPES = {"diffuse": BSDF_DIFFUSE, "roughconductor": BSDF_ROUGH_CONDUCTOR,
               "roughdielectric": BSDF_ROUGH_DIELECTRIC, "smoothlayeredbsdf": BSDF_SMOOTH_LAYERED,
               "layeredbsdf": BSDF_LAYERED, "dielectric": BSDF_DIELECTRIC,
-              "conductor": BSDF_CONDUCTOR, "mirror": BSDF_MIRROR}
+              "conductor": BSDF_CONDUCTOR, "mirror": BSDF_MIRROR, "sheetdielectric": BSDF_SHEET_DIELECTRIC,
+              "microfacet": BSDF_MICROFACET}
 DIST_TYPES = {"beckmann": DIST_BECKMANN, "phong": DIST_PHONG, "ggx": DIST_GGX}
 
 
@@ -39,7 +41,7 @@ class BsdfDesc(C.Structure):
                 ("thickness", C.c_float), ("absorbance", f3),
                 ("distribution_base", C.c_int32), ("alpha_base", C.c_float),
                 ("two_sided", C.c_int32), ("tex_albedo", C.c_int32), ("tex_reflectance", C.c_int32),
-                ("tex_transmittance", C.c_int32), ("tex_alpha", C.c_int32)]
+                ("tex_transmittance", C.c_int32), ("tex_alpha", C.c_int32), ("ks", C.c_float)]
 
 
 class TextureDesc(C.Structure):
@@ -170,22 +172,26 @@ def bsdf(kind, **kw):
     (Diffuse.cpp:11-18, RoughConductor.cpp:13-30, RoughDielectric.cpp:13-32,
     SmoothLayeredBSDF.cpp:12-28, LayeredBSDF.cpp:17-36: coat distribution ggx,
     alphaTop 0.01, over a default RoughConductor: beckmann, alpha 0.2,
-    eta = k = 0; Dielectric.cpp:10-17, Conductor.cpp:13-21, Mirror.cpp:7-15).
+    eta = k = 0; Dielectric.cpp:10-17, Conductor.cpp:13-21, Mirror.cpp:7-15,
+    SheetDielectric.cpp:10-17, Microfacet.cpp:11-25: kd black, alpha 0.2,
+    etaInt 1.5946, ggx, probabilitySpecular (ks) 1).
     two_sided=True wraps it in a TwoSides (TwoSides.cpp:5-15) with the same
     BSDF on both sides.  tex_albedo, tex_reflectance, tex_transmittance and
     tex_alpha name a texture of the scene (SceneData.add_texture) that
     replaces that parameter (None: the constant)."""
     layered = kind == BSDF_LAYERED
-    d = dict(type=kind, distribution=kw.get("distribution", DIST_GGX if layered else DIST_BECKMANN),
-             albedo=kw.get("albedo", (0.5, 0.5, 0.5)),
+    mf = kind == BSDF_MICROFACET
+    d = dict(type=kind, distribution=kw.get("distribution", DIST_GGX if (layered or mf) else DIST_BECKMANN),
+             albedo=kw.get("albedo", (0.0, 0.0, 0.0) if mf else (0.5, 0.5, 0.5)),
              reflectance=kw.get("reflectance", (1.0, 1.0, 1.0)),
              transmittance=kw.get("transmittance", (1.0, 1.0, 1.0)),
              eta=kw.get("eta", (0.0, 0.0, 0.0)), k=kw.get("k", (0.0, 0.0, 0.0)),
-             alpha=kw.get("alpha", 0.01 if layered else 0.2), eta_int=kw.get("eta_int", 1.5046),
+             alpha=kw.get("alpha", 0.01 if layered else 0.2), eta_int=kw.get("eta_int", 1.5946 if mf else 1.5046),
              eta_ext=kw.get("eta_ext", 1.000277), thickness=kw.get("thickness", 1.2),
              absorbance=kw.get("absorbance", (0.0, 0.0, 0.0)),
              distribution_base=kw.get("distribution_base", DIST_BECKMANN),
-             alpha_base=kw.get("alpha_base", 0.2), two_sided=bool(kw.get("two_sided", False)))
+             alpha_base=kw.get("alpha_base", 0.2), two_sided=bool(kw.get("two_sided", False)),
+             ks=float(kw.get("ks", 1.0)))
     for k in TEX_PARAMS:
         if kw.get(k) is not None:
             d[k] = int(kw[k])
@@ -202,7 +208,7 @@ def bsdf_struct(b):
                     b["eta_int"], b["eta_ext"], b["thickness"], f3(*b["absorbance"]),
                     b.get("distribution_base", DIST_BECKMANN), b.get("alpha_base", 0.2),
                     int(bool(b.get("two_sided", False))),
-                    *[0 if b.get(k) is None else int(b[k]) + 1 for k in TEX_PARAMS])
+                    *[0 if b.get(k) is None else int(b[k]) + 1 for k in TEX_PARAMS], b.get("ks", 1.0))
 
 
 class SceneData:

@@ -20,7 +20,7 @@ from .exr import write_exr
 _BSDF_NAMES = {D.BSDF_DIFFUSE: "Diffuse", D.BSDF_ROUGH_CONDUCTOR: "RoughConductor",
                D.BSDF_ROUGH_DIELECTRIC: "RoughDielectric", D.BSDF_SMOOTH_LAYERED: "SmoothLayeredBSDF",
                D.BSDF_LAYERED: "LayeredBSDF", D.BSDF_DIELECTRIC: "Dielectric", D.BSDF_CONDUCTOR: "Conductor",
-               D.BSDF_MIRROR: "Mirror"}
+               D.BSDF_MIRROR: "Mirror", D.BSDF_SHEET_DIELECTRIC: "SheetDielectric", D.BSDF_MICROFACET: "Microfacet"}
 _DIST_NAMES = {D.DIST_BECKMANN: "beckmann", D.DIST_PHONG: "phong", D.DIST_GGX: "ggx"}
 _STRATEGY_NAMES = {D.STRATEGY_ALL_LIGHTS: "all_lights", D.STRATEGY_ONE_LIGHT_UNIFORM: "one_light_uniform",
                    D.STRATEGY_ONE_LIGHT_WEIGHTED: "one_light_weighted"}
@@ -156,6 +156,20 @@ def _bsdf_xml(b, indent, tex=()):
         lines += refl_trans([refl])
     elif b["type"] == D.BSDF_MIRROR:
         pass
+    elif b["type"] == D.BSDF_SHEET_DIELECTRIC:
+        lines += ['%s  <double name="etaInt" value="%s"/>' % (pad, _f(b["eta_int"])),
+                  '%s  <double name="etaExt" value="%s"/>' % (pad, _f(b["eta_ext"]))]
+        lines += refl_trans([refl, trans])
+    elif b["type"] == D.BSDF_MICROFACET:
+        if b.get("tex_albedo") is not None:
+            lines.append(image("kd", "tex_albedo"))
+        else:
+            lines.append('%s  <color name="kd" value="%s"/>' % (pad, _c(b["albedo"])))
+        lines += ['%s  <double name="alpha" value="%s"/>' % (pad, _f(b["alpha"])),
+                  '%s  <double name="etaInt" value="%s"/>' % (pad, _f(b["eta_int"])),
+                  '%s  <double name="etaExt" value="%s"/>' % (pad, _f(b["eta_ext"])),
+                  '%s  <string name="distribution" value="%s"/>' % (pad, _DIST_NAMES[b["distribution"]]),
+                  '%s  <double name="probabilitySpecular" value="%s"/>' % (pad, _f(b.get("ks", 1.0)))]
     elif b["type"] == D.BSDF_SMOOTH_LAYERED:
         lines += ['%s  <double name="etaInt" value="%s"/>' % (pad, _f(b["eta_int"])),
                   '%s  <double name="etaExt" value="%s"/>' % (pad, _f(b["eta_ext"])),

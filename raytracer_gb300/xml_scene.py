@@ -26,7 +26,8 @@ the element.  Paths in the file are resolved against the file's folder
                  <medium name="interior|exterior">
     bsdf         Diffuse, RoughConductor, RoughDielectric, SmoothLayeredBSDF
                  (over Diffuse), LayeredBSDF (over RoughConductor), Dielectric,
-                 Conductor, Mirror, TwoSides (one "bsdf" for both sides);
+                 Conductor, Mirror, SheetDielectric, Microfacet, TwoSides (one
+                 "bsdf" for both sides);
                  top-level <bsdf id=..> and <transform id=..>
                  can be referenced with ref=".."
     media        Homogeneous (sigmaA, sigmaS, scale), Heterogeneous (albedo,
@@ -52,6 +53,7 @@ F32 = np.float32
 # "roughconductor" is RoughConductor.  _type gives the spelling used here.
 _TYPE_NAMES = ["ConstantTexture", "ImageTexture", "Diffuse", "RoughConductor", "RoughDielectric",
                "SmoothLayeredBSDF", "LayeredBSDF", "Dielectric", "Conductor", "Mirror", "TwoSides",
+               "SheetDielectric", "Microfacet",
                "HGPhaseFunction", "IsotropicPhaseFunction", "Homogeneous", "Heterogeneous", "Mesh", "Cube", "Sphere",
                "MeshLight", "AreaLight", "NoriPerspective", "BoxFilter", "GaussianFilter", "MitchellNetravaliFilter",
                "EnvironmentLight", "RandomSampler", "StratifiedSampler", "PathTracingMIS", "VolPathTracing",
@@ -333,6 +335,17 @@ class _Loader:
                        tex_reflectance=self._image(p, "reflectanceTexture"))
         elif kind == "Mirror":   # Mirror.cpp:7-15
             b = D.bsdf(D.BSDF_MIRROR)
+        elif kind == "SheetDielectric":   # SheetDielectric.cpp:10-17
+            b = D.bsdf(D.BSDF_SHEET_DIELECTRIC, eta_int=p.get("etaInt", 1.5046), eta_ext=p.get("etaExt", 1.000277),
+                       reflectance=self._tex_or(p, "reflectanceTexture", (1.0, 1.0, 1.0)),
+                       transmittance=self._tex_or(p, "transmittedTexture", (1.0, 1.0, 1.0)),
+                       tex_reflectance=self._image(p, "reflectanceTexture"),
+                       tex_transmittance=self._image(p, "transmittedTexture"))
+        elif kind == "Microfacet":   # Microfacet.cpp:11-25: kd a color or a texture, alpha a real
+            b = D.bsdf(D.BSDF_MICROFACET, albedo=self._tex_or(p, "kd", (0.0, 0.0, 0.0)),
+                       tex_albedo=self._image(p, "kd"), alpha=float(p.get("alpha", 0.2)),
+                       eta_int=p.get("etaInt", 1.5946), eta_ext=p.get("etaExt", 1.000277),
+                       distribution=_dist(p.get("distribution", "ggx")), ks=float(p.get("probabilitySpecular", 1.0)))
         elif kind == "TwoSides":   # TwoSides.cpp:5-15
             front = p.get("bsdf")
             if front is None:

@@ -140,6 +140,10 @@ BSDFS = [
            two_sided=True),
     D.bsdf(D.BSDF_DIELECTRIC, eta_int=1.5, two_sided=True),
     D.bsdf(D.BSDF_LAYERED, eta=(1.1, 0.9, 0.7), k=(3.0, 2.5, 2.0), two_sided=True),
+    D.bsdf(D.BSDF_SHEET_DIELECTRIC, eta_int=1.5, transmittance=(0.9, 0.95, 1.0)),
+    D.bsdf(D.BSDF_MICROFACET, albedo=(0.6, 0.4, 0.2), ks=0.4, alpha=0.3),
+    D.bsdf(D.BSDF_MICROFACET, albedo=(0.2, 0.5, 0.8), ks=0.7, alpha=0.15, distribution=D.DIST_BECKMANN,
+           two_sided=True),
 ]
 
 
@@ -430,6 +434,22 @@ def test_film_parity_smooth_bsdfs(ctx, rtlib, width):
     """Dielectric, Conductor and Mirror (one shared shading queue) and
     TwoSides-wrapped Diffuse and RoughConductor panels, PathTracingMIS."""
     _film_parity(ctx, rtlib, scenes.cornell_smooth(48, 40), 4, 29, max_bad=0.03)
+
+
+def _sheet_microfacet_room(w, h):
+    s = scenes.cornell_smooth(w, h)
+    s.meshes[0]["bsdf"] = s.add_bsdf(D.bsdf(D.BSDF_MICROFACET, albedo=(0.6, 0.55, 0.5), ks=0.35, alpha=0.25))
+    s.meshes[6]["bsdf"] = s.add_bsdf(D.bsdf(D.BSDF_SHEET_DIELECTRIC, eta_int=1.45, transmittance=(0.8, 0.9, 1.0)))
+    return s
+
+
+def test_film_parity_sheet_and_microfacet(ctx, rtlib):
+    """SheetDielectric (smooth queue) and Microfacet (mixed queue) walls and
+    panel, PathTracingMIS and VolPathTracing."""
+    _film_parity(ctx, rtlib, _sheet_microfacet_room(48, 40), 4, 47, max_bad=0.03)
+    s = _sheet_microfacet_room(40, 32)
+    s.integrator = dict(s.integrator, integrator=D.INTEGRATOR_VOLPATH)
+    _film_parity(ctx, rtlib, s, 3, 53, max_bad=0.05)
 
 
 def test_film_parity_smooth_bsdfs_volpath(ctx, rtlib):

@@ -372,3 +372,13 @@ def test_exr_environment_map_and_stratified_sampler(built, tmp_path):
     with np.errstate(over="ignore"):
         expect = env.astype(np.float16).astype(np.float32)
     assert np.array_equal(t.lights[t.env_light]["rgb"], expect)
+
+
+def test_xml_roundtrip_sheet_and_microfacet(built, tmp_path):
+    s = scenes.cornell_smooth(16, 12)
+    s.meshes[0]["bsdf"] = s.add_bsdf(D.bsdf(D.BSDF_MICROFACET, albedo=(0.6, 0.55, 0.5), ks=0.35, alpha=0.25))
+    s.meshes[6]["bsdf"] = s.add_bsdf(D.bsdf(D.BSDF_SHEET_DIELECTRIC, eta_int=1.45, transmittance=(0.8, 0.9, 1.0)))
+    t = load_scene(write_scene(s, str(tmp_path)))
+    _same_scene(s, t)
+    fa, fb = _films_equal(s, t)
+    assert np.array_equal(fa, fb)

@@ -235,3 +235,34 @@ def test_triangle_hit_exactness_small_scene():
     assert (h["prim"] >= 0).all()
     a = o.trace(rays, anyhit=True)
     assert (a["prim"] == 0).all()
+
+
+def test_microfacet_estimator_and_sheet_dielectric():
+    """Microfacet.cpp:120-182: the sample weight is eval |cos| / pdf and the
+    sample's pdf is pdf(); SheetDielectric.cpp:122-174: reflection with
+    probability fr + T^2 fr / (1 - fr^2), else straight through, typed
+    UNKNOWN (not delta)."""
+    rng = np.random.default_rng(9)
+    for dist in (D.DIST_GGX, D.DIST_BECKMANN):
+        b = D.bsdf(D.BSDF_MICROFACET, albedo=(0.6, 0.4, 0.2), ks=0.4, alpha=0.3, distribution=dist)
+        wi = _sphere_dirs(3000, rng)
+        r = O.bsdf_query(b, D.BSDF_OP_SAMPLE, _q(wi, u=rng.random((3000, 2))))
+        ok = (r["pdf"] > 1e-2) & (np.abs(r["value"]).sum(1) > 0)
+        assert ok.sum() > 1000
+        assert set(np.unique(r["sampled_type"][ok])) <= {4, 0x200}   # glossy or diffuse lobe
+        e = O.bsdf_query(b, D.BSDF_OP_EVAL, _q(wi[ok], r["wo"][ok]))
+        p = O.bsdf_query(b, D.BSDF_OP_PDF, _q(wi[ok], r["wo"][ok]))
+        assert np.allclose(p["pdf"], r["pdf"][ok], rtol=1e-5)
+        assert np.allclose(e["value"] * np.abs(r["wo"][ok, 2:3]) / p["pdf"][:, None], r["value"][ok], rtol=1e-4)
+    n = 1.5
+    s = D.bsdf(D.BSDF_SHEET_DIELECTRIC, eta_int=n, eta_ext=1.0, transmittance=(0.9, 0.8, 0.7))
+    fr = ((n - 1) / (n + 1)) ** 2
+    fr_sheet = fr + (1 - fr) ** 2 * fr / (1 - fr * fr)
+    wi = np.array([[0, 0, 1]] * 2 + [[0.3, 0.1, -0.9]], np.float32)
+    wi /= np.linalg.norm(wi, axis=1, keepdims=True)
+    r = O.bsdf_query(s, D.BSDF_OP_SAMPLE, _q(wi, u=np.array([[fr_sheet * 0.99, 0.5], [fr_sheet * 1.01, 0.5],
+                                                               [0.99, 0.5]], np.float32)))
+    assert r["sampled_type"][0] == 2 and np.isclose(r["pdf"][0], fr_sheet, rtol=1e-5)
+    assert r["sampled_type"][1] == 0 and np.isclose(r["pdf"][1], 1 - fr_sheet, rtol=1e-5)
+    assert np.allclose(r["wo"][1], -wi[1]) and np.allclose(r["wo"][2], -wi[2])
+    assert np.allclose(r["value"][1], [0.9, 0.8, 0.7]) and np.all(r["relative_eta"] == 1)

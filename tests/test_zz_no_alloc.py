@@ -13,7 +13,7 @@ parity tests' 1e-5 relative and, in practice, bitwise equality.
 import numpy as np
 import pytest
 
-from raytracer_gb300 import scenes
+from raytracer_gb300 import desc as D, scenes
 
 pytestmark = pytest.mark.gpu
 
@@ -75,12 +75,16 @@ def test_static_tile_render_rejects_oversize(ctx, rtlib):
 
 
 def test_static_tile_render_refuses_textured_scenes(ctx, rtlib):
-    """Textured BSDFs shade from the mixed queue, which the static scratch
-    layout does not hold: the call fails with RT_ERR_UNSUPPORTED."""
+    """Textured and Microfacet BSDFs shade from the mixed queue, which the
+    static scratch layout does not hold: the call fails with
+    RT_ERR_UNSUPPORTED."""
     torch = pytest.importorskip("torch")
-    g = rtlib.Scene(ctx, scenes.textured_room(32, 32))
-    film = torch.zeros((32, 32, 4), dtype=torch.float32, device="cuda")
-    with pytest.raises(rtlib.RtError) as e:
-        g.render_tile_static(0, 0, film.data_ptr(), 2, seed=1, block=32)
-    assert e.value.status == 5
-    g.close()
+    mf = scenes.cornell_box(32, 32)
+    mf.meshes[0]["bsdf"] = mf.add_bsdf(D.bsdf(D.BSDF_MICROFACET, albedo=(0.5, 0.5, 0.5), ks=0.3, alpha=0.2))
+    for sd in (scenes.textured_room(32, 32), mf):
+        g = rtlib.Scene(ctx, sd)
+        film = torch.zeros((32, 32, 4), dtype=torch.float32, device="cuda")
+        with pytest.raises(rtlib.RtError) as e:
+            g.render_tile_static(0, 0, film.data_ptr(), 2, seed=1, block=32)
+        assert e.value.status == 5
+        g.close()
