@@ -130,7 +130,9 @@ typedef struct rt_sphere_desc {
 } rt_sphere_desc;
 
 enum { RT_LIGHT_AREA = 0,    /* AreaLight / MeshLight bound to a shape           */
-       RT_LIGHT_ENV = 1 };   /* EnvironmentLight (lat-long map)                  */
+       RT_LIGHT_ENV = 1,     /* EnvironmentLight (lat-long map)                  */
+       RT_LIGHT_POINT = 2,   /* PointLight (light/PointLight.cpp), delta         */
+       RT_LIGHT_SPOT = 3 };  /* SpotLight (light/SpotLight.cpp), delta           */
 enum { RT_SHAPE_MESH = 0, RT_SHAPE_SPHERE = 1 };
 
 typedef struct rt_light_desc {
@@ -146,6 +148,13 @@ typedef struct rt_light_desc {
     float env_scale;         /* "scale"                                          */
     float env_to_world[16];  /* "toWorld"                                        */
     float env_to_light[16];  /* inverse of env_to_world                          */
+    /* PointLight / SpotLight: sample() returns intensity / distance^2 with pdf
+       1, and pdf() is 0 (they cannot be hit).                                  */
+    float position[3];       /* PointLight "position"; SpotLight toWorld (0,0,0) */
+    float intensity[3];      /* "intensity"                                      */
+    float spot_to_light[16]; /* SpotLight: inverse of "toWorld"                  */
+    float cos_falloff_start; /* SpotLight: cos(falloffStart), default cos(30 deg)*/
+    float cos_total_width;   /* SpotLight: cos(totalWidth), default cos(60 deg)  */
 } rt_light_desc;
 
 enum { RT_MEDIUM_HOMOGENEOUS = 0, RT_MEDIUM_HETEROGENEOUS = 1 };

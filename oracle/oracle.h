@@ -189,6 +189,7 @@ typedef struct {
 
 void o_light_sample(const o_scene *sc, int light, v3 p, v2 s, o_light_rec *out);
 float o_light_pdf(const o_scene *sc, int light, v3 p, const o_light_rec *rec);
+int o_light_is_delta(const o_scene *sc, int light);   /* Light::isDelta */
 c3 o_env_le(const o_scene *sc, int light, v3 dir);
 
 /* ---------------- ray / intersection ---------------- */

@@ -1197,6 +1197,41 @@ static float o_env_pdf(const o_scene *sc, int light, v3 to_light)
     return pdf;
 }
 
+/* ===================== delta lights ===================== */
+/* PointLight::sample (light/PointLight.cpp:20-33); SpotLight::sample and
+   SpotLight::falloff (light/SpotLight.cpp:19-44).  The spot's cosine is the z
+   of the inverse-toWorld image of -interToLight, without renormalising. */
+static void o_delta_sample(const rt_light_desc *L, v3 p, o_light_rec *out)
+{
+    v3 pos = mk3(L->position[0], L->position[1], L->position[2]);
+    out->to_light = v3_sub(pos, p);
+    out->distance = v3_norm(out->to_light);
+    float inv = 1.f / out->distance;
+    out->to_light = v3_smul(inv, out->to_light);
+    c3 I = c3_from(L->intensity);
+    if (L->type == RT_LIGHT_SPOT) {
+        v3 ld = xf_vector(L->spot_to_light, v3_neg(out->to_light));
+        float ct = ld.z, f;
+        if (ct < L->cos_total_width) f = 0.f;
+        else if (ct > L->cos_falloff_start) f = 1.f;
+        else {
+            float dl = (ct - L->cos_total_width) / (L->cos_falloff_start - L->cos_total_width);
+            f = (dl * dl) * (dl * dl);
+        }
+        I = c3_muls(I, f);
+    }
+    out->intensity = c3_muls(c3_muls(I, inv), inv);
+    out->point = pos;
+    out->normal = mk3(0.f, 0.f, 0.f);
+    out->pdf = 1.f;
+}
+
+int o_light_is_delta(const o_scene *sc, int light)
+{
+    int t = sc->d->lights[light].type;
+    return t == RT_LIGHT_POINT || t == RT_LIGHT_SPOT;
+}
+
 /* ===================== light dispatch ===================== */
 void o_light_sample(const o_scene *sc, int light, v3 p, v2 s, o_light_rec *out)
 {
@@ -1206,6 +1241,7 @@ void o_light_sample(const o_scene *sc, int light, v3 p, v2 s, o_light_rec *out)
     out->distance = 0.f;
     out->intensity = cfill(0.f);
     if (L->type == RT_LIGHT_ENV) { o_env_sample(sc, light, p, s, out); return; }
+    if (o_light_is_delta(sc, light)) { o_delta_sample(L, p, out); return; }
     v3 pt, n;
     if (L->shape_kind == RT_SHAPE_MESH) o_mesh_sample(sc, L->shape, s, &pt, &n);
     else o_sphere_sample(&sc->d->spheres[L->shape], s, &pt, &n);
@@ -1235,6 +1271,7 @@ void o_light_sample(const o_scene *sc, int light, v3 p, v2 s, o_light_rec *out)
 float o_light_pdf(const o_scene *sc, int light, v3 p, const o_light_rec *rec)
 {
     const rt_light_desc *L = &sc->d->lights[light];
+    if (o_light_is_delta(sc, light)) return 0.f;   /* PointLight / SpotLight::pdf */
     if (L->type == RT_LIGHT_ENV) return o_env_pdf(sc, light, rec->to_light);
     if (L->shape_kind == RT_SHAPE_MESH) return o_mesh_pdf(sc, L->shape, p, rec->point, rec->normal);
     return o_sphere_light_pdf(&sc->d->spheres[L->shape], p, rec->point, rec->normal);

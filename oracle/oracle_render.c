@@ -78,6 +78,11 @@ static c3 light_power(const o_scene *sc, int l)
         float R = sc->env[l].sphere_radius;
         return c3_muls(cfill(1.f), 4 * O_PI * R * R);
     }
+    if (L->type == RT_LIGHT_POINT)   /* PointLight.h power(): 4 pi I */
+        return c3_muls(c3_from(L->intensity), 4 * O_PI);
+    if (L->type == RT_LIGHT_SPOT)    /* SpotLight.h power(): 2 pi I (1 - (cosFalloffStart + cosTotalWidth) / 2) */
+        return c3_muls(c3_muls(c3_from(L->intensity), 2 * O_PI),
+                       1.f - 0.5f * (L->cos_falloff_start + L->cos_total_width));
     float area;
     if (L->shape_kind == RT_SHAPE_MESH) area = sc->mesh[L->shape].area;
     else { float r = sc->d->spheres[L->shape].radius; area = 4.f * O_PI * r * r * r; }
@@ -371,7 +376,7 @@ static c3 li_path_mis(const o_scene *sc, const rt_render_desc *rd, o_sampler *s,
                     o_bsdf_rec r;
                     r.wi = to_local(&it, li.to_light); r.wo = to_local(&it, v3_neg(ray.d));
                     float ct = fabsf(r.wi.z);
-                    float bp = o_bsdf_pdf(B, &r);
+                    float bp = o_light_is_delta(sc, l) ? 0.f : o_bsdf_pdf(B, &r);   /* PathTracingMIS.cpp:102 */
                     float w = power_heuristic(li.pdf, bp);
                     L = c3_add(L, c3_mul4(T, value, o_bsdf_eval(B, &r), ct, w));
                 }
@@ -383,7 +388,7 @@ static c3 li_path_mis(const o_scene *sc, const rt_render_desc *rd, o_sampler *s,
                 o_bsdf_rec r;
                 r.wi = to_local(&it, li.to_light); r.wo = to_local(&it, v3_neg(ray.d));
                 float ct = fabsf(r.wi.z);
-                float bp = o_bsdf_pdf(B, &r);
+                float bp = o_light_is_delta(sc, li.light) ? 0.f : o_bsdf_pdf(B, &r);   /* PathTracingMIS.cpp:136, VolPathTracing.cpp:222 */
                 float w = power_heuristic(li.pdf, bp);
                 L = c3_add(L, c3_mul4(T, value, o_bsdf_eval(B, &r), ct, w));
             }
@@ -486,7 +491,7 @@ static c3 li_volpath(const o_scene *sc, const rt_render_desc *rd, o_sampler *s, 
             memset(&li, 0, sizeof(li));
             c3 value = sample_attenuated_light(sc, it.p, s, &li, medium);
             if (!c3_iszero(value)) {
-                float pf = o_phase_eval(M, li.to_light, v3_neg(ray.d));
+                float pf = o_light_is_delta(sc, li.light) ? 0.f : o_phase_eval(M, li.to_light, v3_neg(ray.d));   /* VolPathTracing.cpp:86 */
                 float w = power_heuristic(li.pdf, pf);
                 float ev = o_phase_eval(M, li.to_light, v3_neg(ray.d));
                 L = c3_add(L, c3_muls(c3_muls(c3_mul(T, value), ev), w));
@@ -533,7 +538,7 @@ static c3 li_volpath(const o_scene *sc, const rt_render_desc *rd, o_sampler *s, 
                 o_bsdf_rec r;
                 r.wi = to_local(&it, li.to_light); r.wo = to_local(&it, v3_neg(ray.d));
                 float ct = fabsf(r.wi.z);
-                float bp = o_bsdf_pdf(B, &r);
+                float bp = o_light_is_delta(sc, li.light) ? 0.f : o_bsdf_pdf(B, &r);   /* PathTracingMIS.cpp:136, VolPathTracing.cpp:222 */
                 float w = power_heuristic(li.pdf, bp);
                 L = c3_add(L, c3_mul4(T, value, o_bsdf_eval(B, &r), ct, w));
             }

@@ -910,7 +910,8 @@ __global__ void __launch_bounds__(128, RT_SHADE_MINB) k_pt_shade(RenderParams P,
                     if (!iszero(value)) {
                         V3 wi = to_local(fr, li.to_light), wo = to_local(fr, -d);
                         float ct = fabsf(wi.z);
-                        float bp = bsdf_pdf_t<BT>(B, wi, wo);
+                        // a delta light's sample takes a zero BSDF pdf (PathTracingMIS.cpp:136)
+                        float bp = li.delta ? 0.f : bsdf_pdf_t<BT>(B, wi, wo);
                         float w = power_heuristic(li.pdf, bp);
                         C3 contrib = (((T * value) * bsdf_eval_t<BT>(B, wi, wo)) * ct) * w;
                         // The reference traces the shadow ray before it weighs the
@@ -1599,6 +1600,10 @@ static rt_status validate(const rt_scene_desc *d)
             if (L.shape_kind == RT_SHAPE_MESH ? (L.shape < 0 || L.shape >= d->n_meshes || d->meshes[L.shape].n_tris == 0)
                                               : (L.shape < 0 || L.shape >= d->n_spheres))
                 return fail(RT_ERR_INVALID, "area light without a valid shape");
+        } else if (L.type == RT_LIGHT_POINT || L.type == RT_LIGHT_SPOT) {
+            for (int i = 0; i < 3; i++)
+                if (!std::isfinite(L.position[i]) || !std::isfinite(L.intensity[i]))
+                    return fail(RT_ERR_INVALID, "point or spot light with a non-finite position or intensity");
         } else {
             return fail(RT_ERR_UNSUPPORTED, "light type not supported");
         }
@@ -1784,7 +1789,16 @@ rt_status rt_scene_create(rt_ctx *ctx, const rt_scene_desc *d, rt_scene **out)
         for (int i = 0; i < 3; i++) D.radiance[i] = L.radiance[i];
         std::memcpy(D.env_to_world, L.env_to_world, sizeof(D.env_to_world));
         std::memcpy(D.env_to_light, L.env_to_light, sizeof(D.env_to_light));
-        if (L.type == RT_LIGHT_ENV) {
+        if (L.type == RT_LIGHT_POINT || L.type == RT_LIGHT_SPOT) {
+            for (int i = 0; i < 3; i++) { D.position[i] = L.position[i]; D.intensity[i] = L.intensity[i]; }
+            std::memcpy(D.spot_to_light, L.spot_to_light, sizeof(D.spot_to_light));
+            D.cos_falloff_start = L.cos_falloff_start;
+            D.cos_total_width = L.cos_total_width;
+            // Light::power (PointLight.h, SpotLight.h) for the weighted light CDF
+            float k = 4 * RT_PI, f = 1.f;
+            if (L.type == RT_LIGHT_SPOT) { k = 2 * RT_PI; f = 1.f - 0.5f * (L.cos_falloff_start + L.cos_total_width); }
+            sc->light_power_lum[l] = h_lum((L.intensity[0] * k) * f, (L.intensity[1] * k) * f, (L.intensity[2] * k) * f);
+        } else if (L.type == RT_LIGHT_ENV) {
             int Wd = L.env_width, H = L.env_height;
             D.env_w = Wd; D.env_h = H; D.env_scale = L.env_scale;
             std::vector<float> rows((size_t)H * (Wd + 1)), weight(H);

@@ -81,6 +81,10 @@ struct DevLight {
     float env_marginal_sum;
     float env_radius;           // bounding sphere radius (EnvironmentLight::initialize)
     float env_to_world[16], env_to_light[16];
+    // PointLight / SpotLight (type 2 / 3)
+    float position[3], intensity[3];
+    float spot_to_light[16];
+    float cos_falloff_start, cos_total_width;
 };
 
 struct DevMedium {
@@ -1311,6 +1315,7 @@ struct LightRec {
     V3 point, to_light, normal;
     C3 intensity;
     float distance, pdf;
+    int delta;   // sampled from a delta light (Light::isDelta)
 };
 
 __device__ __forceinline__ void tri_verts(const DevScene &S, int tri, V3 &p0, V3 &p1, V3 &p2)
@@ -1475,9 +1480,39 @@ __device__ __forceinline__ float env_pdf(const DevLight &L, V3 to_light)
     return pdf;
 }
 
+// PointLight::sample (light/PointLight.cpp:20-33) and SpotLight::sample /
+// falloff (light/SpotLight.cpp:19-44): intensity / distance^2 towards the
+// light's position, pdf 1.  The spot's cosine is the z of the inverse-toWorld
+// image of -to_light, not renormalised, as in SpotLight::falloff.
+__device__ __forceinline__ void delta_light_sample(const DevLight &L, V3 p, LightRec &o)
+{
+    V3 pos = vload(L.position);
+    o.to_light = pos - p;
+    o.distance = norm(o.to_light);
+    float inv = 1.f / o.distance;
+    o.to_light = o.to_light * inv;
+    float f = 1.f;
+    if (L.type == 3) {
+        float ct = xf_vector(L.spot_to_light, -o.to_light).z;
+        if (ct < L.cos_total_width) f = 0.f;
+        else if (ct > L.cos_falloff_start) f = 1.f;
+        else {
+            float dl = (ct - L.cos_total_width) / (L.cos_falloff_start - L.cos_total_width);
+            f = (dl * dl) * (dl * dl);
+        }
+    }
+    C3 I = cload(L.intensity);
+    if (L.type == 3) I = I * f;
+    o.intensity = (I * inv) * inv;
+    o.point = pos;
+    o.normal = v3(0.f, 0.f, 0.f);
+    o.pdf = 1.f;
+}
+
 __device__ __forceinline__ float light_pdf(const DevScene &S, int light, V3 p, V3 point, V3 normal, V3 to_light)
 {
     const DevLight &L = S.lights[light];
+    if (L.type >= 2) return 0.f;   // PointLight / SpotLight::pdf
     if (L.type == 1) return env_pdf(L, to_light);
     if (L.shape_kind == 0) return mesh_pdf(S, L.shape, p, point, normal);
     return sphere_pdf(S.spheres[L.shape], p, point, normal);
@@ -1490,7 +1525,9 @@ __device__ __forceinline__ void light_sample(const DevScene &S, int light, V3 p,
     o.pdf = 0.f;
     o.distance = 0.f;
     o.intensity = cfill(0.f);
+    o.delta = L.type >= 2;
     if (L.type == 1) { env_sample(L, p, s, o); return; }
+    if (o.delta) { delta_light_sample(L, p, o); return; }
     V3 pt, n;
     if (L.shape_kind == 0) mesh_sample(S, L.shape, s, pt, n);
     else sphere_sample(S.spheres[L.shape], s, pt, n);

@@ -173,10 +173,11 @@ __device__ bool vol_step(const DevScene &S, VolState &st, Pcg32 &rng, int max_de
         fr.p = ray.o + t * ray.d;
         LightRec li;
         li.point = li.to_light = li.normal = v3(0, 0, 0);
-        li.intensity = cfill(0.f); li.distance = 0.f; li.pdf = 0.f;
+        li.intensity = cfill(0.f); li.distance = 0.f; li.pdf = 0.f; li.delta = 0;
         C3 value = sample_attenuated_light(S, fr.p, rng, li, medium, limit);
         if (!iszero(value)) {
-            float pf = phase_eval(M, li.to_light, -ray.d);
+            // a delta light's sample takes a zero phase pdf (VolPathTracing.cpp:86)
+            float pf = li.delta ? 0.f : phase_eval(M, li.to_light, -ray.d);
             float w = power_heuristic(li.pdf, pf);
             float ev = phase_eval(M, li.to_light, -ray.d);
             L = L + ((T * value) * ev) * w;
@@ -228,12 +229,12 @@ __device__ bool vol_step(const DevScene &S, VolState &st, Pcg32 &rng, int max_de
         if (st.emission && hl >= 0) L = L + T * area_le(S, hl, -ray.d, fr.n);
         LightRec li;
         li.point = li.to_light = li.normal = v3(0, 0, 0);
-        li.intensity = cfill(0.f); li.distance = 0.f; li.pdf = 0.f;
+        li.intensity = cfill(0.f); li.distance = 0.f; li.pdf = 0.f; li.delta = 0;
         C3 value = sample_attenuated_light(S, fr.p, rng, li, medium, limit);
         if (!iszero(value)) {
             V3 wi = to_local(fr, li.to_light), wo = to_local(fr, -ray.d);
             float ct = fabsf(wi.z);
-            float bp = vp_bsdf_pdf(B, wi, wo);
+            float bp = li.delta ? 0.f : vp_bsdf_pdf(B, wi, wo);   // VolPathTracing.cpp:222
             float w = power_heuristic(li.pdf, bp);
             L = L + (((T * value) * vp_bsdf_eval(B, wi, wo)) * ct) * w;
         }
@@ -366,7 +367,7 @@ enum { VF_FIRST = F_FIRST, VF_EMISSION = 2, VF_WAS = 4, VF_SCAT = 8, VF_NULLX = 
 __device__ __forceinline__ bool vw_light_pick(const DevScene &S, V3 p, Pcg32 &rng, LightRec &li, float &lw)
 {
     li.point = li.to_light = li.normal = v3(0, 0, 0);
-    li.intensity = cfill(0.f); li.distance = 0.f; li.pdf = 0.f;
+    li.intensity = cfill(0.f); li.distance = 0.f; li.pdf = 0.f; li.delta = 0;
     lw = 0.f;
     if (S.n_lights == 0) return false;
     V2 u = next2d(rng);
@@ -379,7 +380,7 @@ __device__ __forceinline__ void vw_store_light(const RenderParams &P, int slot, 
     P.W.v_p[slot] = f4(p, lw);
     P.W.v_li0[slot] = f4(li.to_light, li.distance);
     P.W.v_li1[slot] = f4(li.point, li.pdf);
-    P.W.v_li2[slot] = f4(li.normal, 0.f);
+    P.W.v_li2[slot] = f4(li.normal, li.delta ? 1.f : 0.f);
     P.W.v_val[slot] = f4c(li.intensity, 0.f);
 }
 __device__ __forceinline__ void vw_done(const RenderParams &P, int slot, C3 L) { P.W.out[slot] = f4c(L, 0.f); }
@@ -630,7 +631,7 @@ __global__ void __launch_bounds__(128, RT_VW_MINB_SAMPLE) k_vw_sample(RenderPara
             if (!iszero(value)) {
                 V3 to_light = xyz(P.W.v_li0[slot]);
                 float lpdf = P.W.v_li1[slot].w;
-                float pf = phase_eval(M, to_light, -ray.d);
+                float pf = P.W.v_li2[slot].w != 0.f ? 0.f : phase_eval(M, to_light, -ray.d);
                 float w = power_heuristic(lpdf, pf);
                 float ev = phase_eval(M, to_light, -ray.d);
                 L = L + ((T * value) * ev) * w;
@@ -658,7 +659,7 @@ __global__ void __launch_bounds__(128, RT_VW_MINB_SAMPLE) k_vw_sample(RenderPara
                 float lpdf = P.W.v_li1[slot].w;
                 V3 wi = to_local(fr, to_light), wo = to_local(fr, -ray.d);
                 float ct = fabsf(wi.z);
-                float bp = vp_bsdf_pdf(B, wi, wo);
+                float bp = P.W.v_li2[slot].w != 0.f ? 0.f : vp_bsdf_pdf(B, wi, wo);
                 float w = power_heuristic(lpdf, bp);
                 L = L + (((T * value) * vp_bsdf_eval(B, wi, wo)) * ct) * w;
             }

@@ -7,6 +7,7 @@ The numpy arrays stay owned by the SceneData object; the struct only points
 at them, so keep the SceneData alive while a desc is in use.
 """
 import ctypes as C
+import math
 import numpy as np
 
 f3 = C.c_float * 3
@@ -17,7 +18,7 @@ BSDF_DIFFUSE, BSDF_ROUGH_CONDUCTOR, BSDF_ROUGH_DIELECTRIC, BSDF_SMOOTH_LAYERED, 
 BSDF_DIELECTRIC, BSDF_CONDUCTOR, BSDF_MIRROR = 5, 6, 7
 BSDF_SHEET_DIELECTRIC, BSDF_MICROFACET = 8, 9
 DIST_BECKMANN, DIST_PHONG, DIST_GGX = 0, 1, 2
-LIGHT_AREA, LIGHT_ENV = 0, 1
+LIGHT_AREA, LIGHT_ENV, LIGHT_POINT, LIGHT_SPOT = 0, 1, 2, 3
 SHAPE_MESH, SHAPE_SPHERE = 0, 1
 MEDIUM_HOMOGENEOUS, MEDIUM_HETEROGENEOUS = 0, 1
 PHASE_ISOTROPIC, PHASE_HG = 0, 1
@@ -64,7 +65,9 @@ class LightDesc(C.Structure):
     _fields_ = [("type", C.c_int32), ("mesh_light", C.c_int32), ("shape_kind", C.c_int32),
                 ("shape", C.c_int32), ("radiance", f3), ("env_width", C.c_int32),
                 ("env_height", C.c_int32), ("env_rgb", C.POINTER(C.c_float)),
-                ("env_scale", C.c_float), ("env_to_world", f16), ("env_to_light", f16)]
+                ("env_scale", C.c_float), ("env_to_world", f16), ("env_to_light", f16),
+                ("position", f3), ("intensity", f3), ("spot_to_light", f16),
+                ("cos_falloff_start", C.c_float), ("cos_total_width", C.c_float)]
 
 
 class MediumDesc(C.Structure):
@@ -282,6 +285,22 @@ class SceneData:
                                 shape=shape, radiance=tuple(radiance)))
         return len(self.lights) - 1
 
+    def add_point_light(self, position, intensity):
+        """PointLight (light/PointLight.cpp:7-11): "position", "intensity"."""
+        self.lights.append(dict(type=LIGHT_POINT, position=tuple(float(x) for x in position),
+                                intensity=tuple(float(x) for x in intensity)))
+        return len(self.lights) - 1
+
+    def add_spot_light(self, to_world, intensity, falloff_start=30.0, total_width=60.0):
+        """SpotLight (light/SpotLight.cpp:8-15): "toWorld", "intensity", and the
+        "falloffStart" / "totalWidth" angles in degrees; the light sits at
+        toWorld (0,0,0) and shines along its +z."""
+        M = np.asarray(to_world, np.float64)
+        self.lights.append(dict(type=LIGHT_SPOT, to_world=M,
+                                intensity=tuple(float(x) for x in intensity),
+                                falloff_start=float(falloff_start), total_width=float(total_width)))
+        return len(self.lights) - 1
+
     def add_env_light(self, rgb, scale=1.0, to_world=IDENTITY):
         rgb = np.ascontiguousarray(rgb, dtype=np.float32)
         self.lights.append(dict(type=LIGHT_ENV, rgb=rgb, scale=scale,
@@ -348,6 +367,23 @@ class SceneData:
                 L.env_to_light = mat(inv4(l["to_world"]))
                 L.radiance = f3(0, 0, 0)
                 L.shape = -1
+            elif l["type"] in (LIGHT_POINT, LIGHT_SPOT):
+                L.shape = -1
+                L.radiance = f3(0, 0, 0)
+                L.env_to_world = mat(IDENTITY)
+                L.env_to_light = mat(IDENTITY)
+                L.intensity = f3(*l["intensity"])
+                if l["type"] == LIGHT_POINT:
+                    L.position = f3(*l["position"])
+                    L.spot_to_light = mat(IDENTITY)
+                else:
+                    # the binary32 toWorld a scene file holds, inverted in float64
+                    M = np.asarray(l["to_world"], np.float32).astype(np.float64)
+                    c = M @ np.array([0.0, 0.0, 0.0, 1.0])
+                    L.position = f3(*(c[:3] / c[3]))
+                    L.spot_to_light = mat(inv4(M))
+                    L.cos_falloff_start = math.cos(math.radians(l["falloff_start"]))
+                    L.cos_total_width = math.cos(math.radians(l["total_width"]))
             else:
                 L.mesh_light = l["mesh_light"]
                 L.shape_kind = l["shape_kind"]

@@ -262,20 +262,42 @@ def write_scene(scene, folder, spp=1, name="scene"):
             '  <sampler type="RandomSampler"><integer name="sampleNumber" value="%d"/></sampler>' % spp]
     if cam.get("medium", -1) >= 0:
         out += _medium_xml(s.media[cam["medium"]], "camera", folder, "medium%d" % cam["medium"], 2)
-    # lights are numbered in document order: the environment goes before the
-    # objects when it is light 0, after them otherwise
+    # lights are numbered in document order: shape lights with their shapes in
+    # <objects>, the others (environment, point, spot) in a <lights> block that
+    # goes before the objects when those lights come first, after them otherwise
+    free = [li for li, L in enumerate(s.lights) if L["type"] != D.LIGHT_AREA]
+    area = [li for li, L in enumerate(s.lights) if L["type"] == D.LIGHT_AREA]
+    free_first = bool(free) and (not area or max(free) < min(area))
+    if free and area and not free_first and min(free) < max(area):
+        raise ValueError("the light order (environment/point/spot lights between shape lights) "
+                         "cannot be written as one <lights> block")
     env_lines = []
-    for li, L in enumerate(s.lights):
+    for li in free:
+        L = s.lights[li]
         if L["type"] == D.LIGHT_ENV:
             hdr = "env%d.hdr" % li
             write_hdr(os.path.join(folder, hdr), L["rgb"])
-            env_lines += ["  <lights>", '    <light type="EnvironmentLight">',
+            env_lines += ['    <light type="EnvironmentLight">',
                           '      <string name="path" value="%s"/>' % hdr,
                           '      <double name="scale" value="%s"/>' % _f(L.get("scale", 1.0)),
                           '      <transform name="toWorld"><matrix value="%s"/></transform>'
                           % _matrix(L.get("to_world", np.eye(4))),
-                          "    </light>", "  </lights>"]
-    env_first = s.env_light == 0
+                          "    </light>"]
+        elif L["type"] == D.LIGHT_POINT:
+            env_lines += ['    <light type="PointLight">',
+                          '      <point name="position" value="%s"/>' % _c(L["position"]),
+                          '      <color name="intensity" value="%s"/>' % _c(L["intensity"]),
+                          "    </light>"]
+        else:
+            env_lines += ['    <light type="SpotLight">',
+                          '      <transform name="toWorld"><matrix value="%s"/></transform>' % _matrix(L["to_world"]),
+                          '      <color name="intensity" value="%s"/>' % _c(L["intensity"]),
+                          '      <double name="falloffStart" value="%s"/>' % _f(L["falloff_start"]),
+                          '      <double name="totalWidth" value="%s"/>' % _f(L["total_width"]),
+                          "    </light>"]
+    if env_lines:
+        env_lines = ["  <lights>"] + env_lines + ["  </lights>"]
+    env_first = free_first
     if env_first:
         out += env_lines
     # textures: half-float OpenEXR files, which the reference reads linearly

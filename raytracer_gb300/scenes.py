@@ -215,6 +215,27 @@ def cornell_smooth(width=128, height=128, max_depth=12):
     return s
 
 
+def cornell_delta_lights(width=96, height=96, area_light=True, spot_scale=1.0):
+    """The Cornell-box room lit by a PointLight in the upper left and a
+    SpotLight under the ceiling aimed straight down (falloff from 20 to 35
+    degrees), beside the ceiling area light unless `area_light` is False.
+    `spot_scale` scales the spot's toWorld, which narrows its cone: SpotLight
+    reads the cosine from the inverse-transformed direction without
+    renormalising it."""
+    s = cornell_box(width, height)
+    s.name = "cornell_delta_lights_%d" % width
+    if not area_light:
+        lm = len(s.meshes) - 1
+        s.meshes[lm]["light"] = -1
+        s.lights = []
+    s.add_point_light((0.25, 0.8, 0.6), (0.9, 0.8, 0.6))
+    c, sn = 0.0, 1.0   # rotation of +90 degrees about x: local +z -> world -y
+    T = np.array([[1, 0, 0, 0.7], [0, c, -sn, 0.95], [0, sn, c, 0.5], [0, 0, 0, 1]], np.float64)
+    T[:3, :3] *= spot_scale
+    s.add_spot_light(T, (1.5, 1.6, 2.0), falloff_start=20.0, total_width=35.0)
+    return s
+
+
 def texture_image(width, height, seed=0, kind="checker"):
     """A seeded test image (H, W, 3) in [0, 1], rounded to half precision (so
     that an OpenEXR copy of it is exact): "checker" squares with a colour

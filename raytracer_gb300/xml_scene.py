@@ -56,7 +56,8 @@ _TYPE_NAMES = ["ConstantTexture", "ImageTexture", "Diffuse", "RoughConductor", "
                "SheetDielectric", "Microfacet",
                "HGPhaseFunction", "IsotropicPhaseFunction", "Homogeneous", "Heterogeneous", "Mesh", "Cube", "Sphere",
                "MeshLight", "AreaLight", "NoriPerspective", "BoxFilter", "GaussianFilter", "MitchellNetravaliFilter",
-               "EnvironmentLight", "RandomSampler", "StratifiedSampler", "PathTracingMIS", "VolPathTracing",
+               "EnvironmentLight", "PointLight", "SpotLight", "RandomSampler", "StratifiedSampler",
+               "PathTracingMIS", "VolPathTracing",
                "GridVolume"]
 _CANON = {n.lower(): n for n in _TYPE_NAMES}
 
@@ -489,6 +490,14 @@ class _Loader:
         for c in el:
             kind = _type(c)
             p = self.props(c)
+            if kind == "PointLight":   # PointLight.cpp:7-11
+                self.s.add_point_light(p.get("position", (0.0, 0.0, 0.0)), p.get("intensity", (0.0, 0.0, 0.0)))
+                continue
+            if kind == "SpotLight":    # SpotLight.cpp:8-15
+                self.s.add_spot_light(np.asarray(p.get("toWorld", np.eye(4)), np.float64),
+                                      p.get("intensity", (0.0, 0.0, 0.0)),
+                                      p.get("falloffStart", 30.0), p.get("totalWidth", 60.0))
+                continue
             if kind != "EnvironmentLight":
                 raise UnsupportedScene("light type %s is not provided" % kind)
             if p.get("isProbe", False) or p.get("offsetU", 0.0) or p.get("offsetV", 0.0):

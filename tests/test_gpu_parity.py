@@ -250,6 +250,14 @@ def test_sphere_light_parity(ctx, rtlib, vol):
     _light_parity(ctx, rtlib, vol, 0, seed=2)
 
 
+@pytest.mark.parametrize("kind", [D.LIGHT_POINT, D.LIGHT_SPOT], ids=["point", "spot"])
+def test_delta_light_parity(ctx, rtlib, kind):
+    """PointLight / SpotLight::sample and ::pdf (0) through rt_light_query."""
+    s = scenes.cornell_delta_lights(16, 16, spot_scale=1.05)
+    li = [i for i, L in enumerate(s.lights) if L["type"] == kind][0]
+    _light_parity(ctx, rtlib, s, li, seed=3)
+
+
 def _medium_queries(n, rng, box_lo, box_hi):
     from raytracer_gb300.core import MEDIUM_Q
     q = np.zeros(n, MEDIUM_Q)
@@ -450,6 +458,38 @@ def test_film_parity_sheet_and_microfacet(ctx, rtlib):
     s = _sheet_microfacet_room(40, 32)
     s.integrator = dict(s.integrator, integrator=D.INTEGRATOR_VOLPATH)
     _film_parity(ctx, rtlib, s, 3, 53, max_bad=0.05)
+
+
+def test_film_parity_delta_lights(ctx, rtlib, width):
+    """PointLight and SpotLight beside the area light (uniform and weighted
+    light selection) and alone, under PathTracingMIS; their samples take MIS
+    weight 1 (PathTracingMIS.cpp:136)."""
+    s = scenes.cornell_delta_lights(40, 32, spot_scale=1.05)
+    _film_parity(ctx, rtlib, s, 4, 61, max_bad=0.03)
+    _film_parity(ctx, rtlib, s, 2, 62, max_bad=0.03, strategy=D.STRATEGY_ONE_LIGHT_WEIGHTED)
+    _film_parity(ctx, rtlib, scenes.cornell_delta_lights(32, 24, area_light=False), 4, 63, max_bad=0.03)
+
+
+def test_film_parity_delta_lights_volpath(ctx, rtlib):
+    """The same lights under VolPathTracing with a homogeneous medium in the
+    short box: attenuated shadow rays and phase-function MIS weight 1
+    (VolPathTracing.cpp:86,222), wavefront and persistent kernels."""
+    s = scenes.cornell_delta_lights(40, 32)
+    m = s.add_medium(dict(type=D.MEDIUM_HOMOGENEOUS, phase=D.PHASE_HG, g=0.3, sigma_a=(0.3, 0.6, 1.0),
+                          sigma_s=(1.5, 1.5, 1.5), scale=2.0))
+    s.meshes[4]["interior"] = m
+    s.meshes[4]["bsdf"] = -1
+    s.integrator = dict(s.integrator, integrator=D.INTEGRATOR_VOLPATH)
+    fg, _ = _film_parity(ctx, rtlib, s, 4, 67, max_bad=0.05)
+    before = ctx.get_tuning()
+    g = rtlib.Scene(ctx, s)
+    try:
+        ctx.set_tuning(volpath_wavefront=0)
+        mega = g.render(4, seed=67, block=16)
+    finally:
+        ctx.set_tuning(**before)
+    g.close()
+    assert np.array_equal(fg, mega)
 
 
 def test_film_parity_smooth_bsdfs_volpath(ctx, rtlib):
