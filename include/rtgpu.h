@@ -121,19 +121,25 @@ typedef struct rt_mesh_desc {
     int32_t exterior;        /* index into media, -1 = none                      */
 } rt_mesh_desc;
 
-/* Analytic sphere (geometricShape/Sphere.cpp), object space centred at 0. */
+/* Analytic shapes, listed in rt_scene_desc.spheres: a Sphere
+   (geometricShape/Sphere.cpp), object space centred at 0, or a Plane
+   (geometricShape/Plane.cpp), the object-space square [-1,1]^2 at z = 0 with
+   normal +z.  Hits on entry i carry prim = -i - 2.                            */
+enum { RT_ANALYTIC_SPHERE = 0, RT_ANALYTIC_PLANE = 1 };
 typedef struct rt_sphere_desc {
-    float radius;
+    float radius;            /* Sphere only                                      */
     float to_world[16];
     float to_object[16];     /* inverse of to_world                              */
     int32_t bsdf, light, interior, exterior;
+    int32_t kind;            /* RT_ANALYTIC_* (0 for a zero-filled entry: sphere) */
 } rt_sphere_desc;
 
 enum { RT_LIGHT_AREA = 0,    /* AreaLight / MeshLight bound to a shape           */
        RT_LIGHT_ENV = 1,     /* EnvironmentLight (lat-long map)                  */
        RT_LIGHT_POINT = 2,   /* PointLight (light/PointLight.cpp), delta         */
        RT_LIGHT_SPOT = 3 };  /* SpotLight (light/SpotLight.cpp), delta           */
-enum { RT_SHAPE_MESH = 0, RT_SHAPE_SPHERE = 1 };
+enum { RT_SHAPE_MESH = 0,
+       RT_SHAPE_SPHERE = 1 };  /* an entry of spheres[]: a Sphere or a Plane      */
 
 typedef struct rt_light_desc {
     int32_t type;            /* RT_LIGHT_*                                       */

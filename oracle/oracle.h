@@ -224,6 +224,8 @@ c3 o_medium_transmittance(const o_scene *sc, int m, const o_ray *ray, o_sampler 
 float o_phase_sample(const rt_medium_desc *m, v3 wi, v2 u, v3 *wo, float *pdf);
 float o_phase_eval(const rt_medium_desc *m, v3 wi, v3 wo);
 float o_sphere_light_pdf(const rt_sphere_desc *s, v3 p, v3 sampled, v3 n);
+float o_plane_area(const rt_sphere_desc *s);
+v3 o_plane_normal(const rt_sphere_desc *s);
 
 /* ---------------- public oracle API (ctypes) ---------------- */
 int32_t oracle_version(void);

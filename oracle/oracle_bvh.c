@@ -272,6 +272,10 @@ static o_box sphere_box(const rt_sphere_desc *s)
 {
     float r = s->radius;
     float mn[3] = {-r, -r, -r}, mx[3] = {r, r, r};
+    if (s->kind == RT_ANALYTIC_PLANE) {   /* Plane::getLocalBoundingBox (Plane.cpp:28-42) */
+        mn[0] = -1.f; mn[1] = -1.f; mn[2] = 0.f;
+        mx[0] = 1.f; mx[1] = 1.f; mx[2] = 0.f;
+    }
     const float cx[8][3] = {
         {mn[0], mn[1], mn[2]}, {mn[0], mn[1], mx[2]}, {mn[0], mx[1], mx[2]}, {mx[0], mx[1], mx[2]},
         {mx[0], mn[1], mn[2]}, {mx[0], mx[1], mn[2]}, {mx[0], mn[1], mx[2]}, {mn[0], mx[1], mn[2]}};
@@ -402,6 +406,21 @@ static int sphere_hit(const rt_sphere_desc *sp, const o_ray *r, float *t)
     return 0;
 }
 
+/* Plane::intersection (Plane.cpp:63-79).  A ray lying in the plane gives
+ * t = NaN, which the reference's range test lets through as a hit; here it is
+ * a miss. */
+static int plane_hit(const rt_sphere_desc *sp, const o_ray *r, float *t)
+{
+    v3 lo = xf_point(sp->to_object, r->o);
+    v3 ld = xf_vector(sp->to_object, r->d);
+    float tt = -lo.z / ld.z;
+    if (!(tt >= r->mint && tt <= r->maxt)) return 0;
+    v3 q = v3_add(lo, v3_smul(tt, ld));
+    if (q.x < -1.f || q.x > 1.f || q.y < -1.f || q.y > 1.f) return 0;
+    *t = tt;
+    return 1;
+}
+
 static int box_hit(const o_box *b, const o_ray *r)
 {
     float nearT = -O_MAX_REAL, farT = O_MAX_REAL;
@@ -431,6 +450,7 @@ static int prim_isect(const o_scene *sc, const o_bvh *b, o_pref p, const o_ray *
     float t, u = 0.f, v = 0.f;
     int hit;
     if (p.kind == P_TRI) hit = tri_hit(d, p.id, ray, &t, &u, &v);
+    else if (d->spheres[p.id].kind == RT_ANALYTIC_PLANE) hit = plane_hit(&d->spheres[p.id], ray, &t);
     else hit = sphere_hit(&d->spheres[p.id], ray, &t);
     if (!hit) return 0;
     rec->p = v3_add(ray->o, v3_smul(t, ray->d));
@@ -535,8 +555,12 @@ int o_intersect(const o_scene *sc, const o_ray *ray, o_hit *hit, int shadow)
         const rt_sphere_desc *sp = &d->spheres[-rec.prim - 2];
         hit->uv = o_sphere_uv(sp, ray, rec.t);
         hit->p = rec.p;
-        v3 nl = v3_normalized(v3_sub(xf_point(sp->to_object, rec.p), mk3(0, 0, 0)));
-        v3 n = v3_normalized(xf_normal(sp->to_object, nl));
+        v3 n;
+        if (sp->kind == RT_ANALYTIC_PLANE) n = o_plane_normal(sp);
+        else {
+            v3 nl = v3_normalized(v3_sub(xf_point(sp->to_object, rec.p), mk3(0, 0, 0)));
+            n = v3_normalized(xf_normal(sp->to_object, nl));
+        }
         hit->ng = n;
         hit->n = n;
         frame_from(n, &hit->s, &hit->tt);

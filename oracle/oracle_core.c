@@ -729,6 +729,10 @@ static c3 o_ly_sample(const rt_bsdf_desc *b, o_bsdf_rec *r, v2 s, uint64_t aux_k
 v2 o_sphere_uv(const rt_sphere_desc *sp, const o_ray *r, float t)
 {
     v3 lo = xf_point(sp->to_object, r->o), ld = xf_vector(sp->to_object, r->d);
+    if (sp->kind == RT_ANALYTIC_PLANE) {   /* Plane::intersection (Plane.cpp:75-76) */
+        v3 q = v3_add(lo, v3_smul(t, ld));
+        return mk2((q.x + 1) / 2.f, (q.y + 1) / 2.f);
+    }
     v3 n = v3_normalized(v3_add(lo, v3_smul(t, ld)));
     return mk2(o_spherical_phi(n) / (2 * O_PI), o_spherical_theta(n) / O_PI);
 }
@@ -1054,6 +1058,27 @@ static v3 o_sphere_normal(const rt_sphere_desc *s, v3 p)
     return v3_normalized(v3_sub(lp, mk3(0, 0, 0)));
 }
 static float o_sphere_area(const rt_sphere_desc *s) { return 4.f * O_PI * s->radius * s->radius * s->radius; }
+/* Plane::Plane (geometricShape/Plane.cpp:7-18): the product of the lengths of
+   the two transformed edges from the (-1,-1,0) corner */
+float o_plane_area(const rt_sphere_desc *s)
+{
+    v3 mn = xf_point(s->to_world, mk3(-1.f, -1.f, 0.f));
+    v3 s1 = v3_sub(xf_point(s->to_world, mk3(-1.f, 1.f, 0.f)), mn);
+    v3 s2 = v3_sub(xf_point(s->to_world, mk3(1.f, -1.f, 0.f)), mn);
+    return v3_norm(s1) * v3_norm(s2);
+}
+/* Plane::normal / getDifferentialGeometry (Plane.cpp:47-50,82-92): +z as a
+   normal (inverse transpose), normalised */
+v3 o_plane_normal(const rt_sphere_desc *s)
+{
+    return v3_normalized(xf_normal(s->to_object, mk3(0.f, 0.f, 1.f)));
+}
+/* Plane::sample (Plane.cpp:94-98) */
+static void o_plane_sample(const rt_sphere_desc *s, v2 u, v3 *pt, v3 *n)
+{
+    *pt = xf_point(s->to_world, mk3(1 - 2 * u.x, 1 - 2 * u.y, 0.f));
+    *n = o_plane_normal(s);
+}
 /* Sphere::sample (Sphere.cpp:146-173) */
 static void o_sphere_sample(const rt_sphere_desc *s, v2 u, v3 *pt, v3 *n)
 {
@@ -1070,6 +1095,14 @@ static void o_sphere_sample(const rt_sphere_desc *s, v2 u, v3 *pt, v3 *n)
 /* Sphere::pdf (Sphere.cpp:183-201) with the ISampledShape::pdf fallback (ISampledShape.cpp:17-40) */
 float o_sphere_light_pdf(const rt_sphere_desc *s, v3 p, v3 sampled, v3 n)
 {
+    if (s->kind == RT_ANALYTIC_PLANE) {   /* ISampledShape::pdf (ISampledShape.cpp:17-40) */
+        v3 l = v3_sub(p, sampled);
+        float dist = v3_norm(l);
+        l = v3_normalized(l);
+        float c = v3_dot(n, l);
+        if (c >= 0) return dist * dist / (o_plane_area(s) * c);
+        return 0.f;
+    }
     v3 center = xf_point(s->to_world, mk3(0.f, 0.f, 0.f));
     v3 itc = v3_sub(p, center);
     float sqd = v3_sqnorm(itc);
@@ -1244,6 +1277,7 @@ void o_light_sample(const o_scene *sc, int light, v3 p, v2 s, o_light_rec *out)
     if (o_light_is_delta(sc, light)) { o_delta_sample(L, p, out); return; }
     v3 pt, n;
     if (L->shape_kind == RT_SHAPE_MESH) o_mesh_sample(sc, L->shape, s, &pt, &n);
+    else if (sc->d->spheres[L->shape].kind == RT_ANALYTIC_PLANE) o_plane_sample(&sc->d->spheres[L->shape], s, &pt, &n);
     else o_sphere_sample(&sc->d->spheres[L->shape], s, &pt, &n);
     out->point = pt;
     out->normal = n;

@@ -85,6 +85,7 @@ static c3 light_power(const o_scene *sc, int l)
                        1.f - 0.5f * (L->cos_falloff_start + L->cos_total_width));
     float area;
     if (L->shape_kind == RT_SHAPE_MESH) area = sc->mesh[L->shape].area;
+    else if (sc->d->spheres[L->shape].kind == RT_ANALYTIC_PLANE) area = o_plane_area(&sc->d->spheres[L->shape]);
     else { float r = sc->d->spheres[L->shape].radius; area = 4.f * O_PI * r * r * r; }
     c3 p = mkc(O_PI * L->radiance[0], O_PI * L->radiance[1], O_PI * L->radiance[2]);
     return c3_muls(p, area);

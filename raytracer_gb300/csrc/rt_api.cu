@@ -422,7 +422,7 @@ __global__ void __launch_bounds__(128, RT_TRACE_MINB) k_trace(RenderParams P, in
             if (!(ANY && hprim >= 0)) {
                 for (int si = 0; si < S.n_spheres; si++) {
                     float t;
-                    if (sphere_test(S.spheres[si], v3(ox, oy, oz), v3(dx, dy, dz), tmin, hit_t, t)) {
+                    if (analytic_test(S.spheres[si], v3(ox, oy, oz), v3(dx, dy, dz), tmin, hit_t, t)) {
                         hit_t = t; hu = 0.f; hv = 0.f; hprim = -si - 2;
                         if (ANY) break;
                     }
@@ -629,7 +629,7 @@ __global__ void __launch_bounds__(128, 8) k_trace8(RenderParams P, int round)
             if (!(ANY && hprim >= 0)) {
                 for (int si = 0; si < S.n_spheres; si++) {
                     float t;
-                    if (sphere_test(S.spheres[si], v3(ox, oy, oz), v3(dx, dy, dz), tmin, hit_t, t)) {
+                    if (analytic_test(S.spheres[si], v3(ox, oy, oz), v3(dx, dy, dz), tmin, hit_t, t)) {
                         hit_t = t; hu = 0.f; hv = 0.f; hprim = -si - 2;
                         if (ANY) break;
                     }
@@ -1591,6 +1591,8 @@ static rt_status validate(const rt_scene_desc *d)
         const rt_sphere_desc &S = d->spheres[s];
         if (S.bsdf >= d->n_bsdfs || S.light >= d->n_lights || S.interior >= d->n_media || S.exterior >= d->n_media)
             return fail(RT_ERR_INVALID, "sphere references a missing component");
+        if (S.kind != RT_ANALYTIC_SPHERE && S.kind != RT_ANALYTIC_PLANE)
+            return fail(RT_ERR_INVALID, "analytic shape of unknown kind");
     }
     for (int l = 0; l < d->n_lights; l++) {
         const rt_light_desc &L = d->lights[l];
@@ -1722,8 +1724,20 @@ rt_status rt_scene_create(rt_ctx *ctx, const rt_scene_desc *d, rt_scene **out)
         std::memcpy(D.to_world, Sd.to_world, sizeof(D.to_world));
         std::memcpy(D.to_object, Sd.to_object, sizeof(D.to_object));
         D.bsdf = Sd.bsdf; D.light = Sd.light; D.interior = Sd.interior; D.exterior = Sd.exterior;
+        D.kind = Sd.kind;
+        D.area = 0.f;
         float r = Sd.radius;
         float lo[3] = {-r, -r, -r}, hi[3] = {r, r, r};
+        if (Sd.kind == RT_ANALYTIC_PLANE) {
+            // Plane::getLocalBoundingBox (Plane.cpp:28-42) and the surface area
+            // of Plane::Plane (Plane.cpp:13-17)
+            lo[0] = -1.f; lo[1] = -1.f; lo[2] = 0.f;
+            hi[0] = 1.f; hi[1] = 1.f; hi[2] = 0.f;
+            V3 mn = h_xf_point(Sd.to_world, v3(-1.f, -1.f, 0.f));
+            V3 s1 = h_xf_point(Sd.to_world, v3(-1.f, 1.f, 0.f)) - mn;
+            V3 s2 = h_xf_point(Sd.to_world, v3(1.f, -1.f, 0.f)) - mn;
+            D.area = sqrtf(dot(s1, s1)) * sqrtf(dot(s2, s2));
+        }
         const float cx[8][3] = {{lo[0], lo[1], lo[2]}, {lo[0], lo[1], hi[2]}, {lo[0], hi[1], hi[2]}, {hi[0], hi[1], hi[2]},
                                 {hi[0], lo[1], lo[2]}, {hi[0], hi[1], lo[2]}, {hi[0], lo[1], hi[2]}, {lo[0], hi[1], lo[2]}};
         for (int k = 0; k < 8; k++) {
@@ -1847,6 +1861,7 @@ rt_status rt_scene_create(rt_ctx *ctx, const rt_scene_desc *d, rt_scene **out)
         } else {
             float area;
             if (L.shape_kind == RT_SHAPE_MESH) area = meshes[L.shape].area;
+            else if (d->spheres[L.shape].kind == RT_ANALYTIC_PLANE) area = spheres[L.shape].area;
             else { float r = d->spheres[L.shape].radius; area = 4.f * RT_PI * r * r * r; }
             sc->light_power_lum[l] = h_lum(RT_PI * L.radiance[0] * area, RT_PI * L.radiance[1] * area,
                                            RT_PI * L.radiance[2] * area);

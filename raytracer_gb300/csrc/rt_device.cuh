@@ -16,11 +16,14 @@ struct DevMesh {
     float area;       // Mesh::mySurfaceArea
 };
 
+// An analytic shape: kind 0 Sphere, kind 1 Plane (RT_ANALYTIC_*)
 struct DevSphere {
     float radius;
     float to_world[16];
     float to_object[16];
     int bsdf, light, interior, exterior;
+    int kind;
+    float area;   // Plane: Plane::surfaceArea (Plane.cpp:13-17)
 };
 
 struct DevBsdf {
@@ -240,6 +243,33 @@ __device__ __forceinline__ bool sphere_test(const DevSphere &sp, V3 o, V3 d, flo
     return false;
 }
 
+// Plane::intersection (geometricShape/Plane.cpp:63-79).  A ray lying in the
+// plane gives t = NaN, which the reference's range test lets through; here it
+// is a miss.
+__device__ __forceinline__ bool plane_test(const DevSphere &sp, V3 o, V3 d, float mint, float maxt, float &t)
+{
+    V3 lo = xf_point(sp.to_object, o);
+    V3 ld = xf_vector(sp.to_object, d);
+    float tt = -lo.z / ld.z;
+    if (!(tt >= mint && tt <= maxt)) return false;
+    V3 q = lo + tt * ld;
+    if (q.x < -1.f || q.x > 1.f || q.y < -1.f || q.y > 1.f) return false;
+    t = tt;
+    return true;
+}
+__device__ __noinline__ bool plane_test_call(const DevSphere &sp, V3 o, V3 d, float mint, float maxt, float &t)
+{
+    return plane_test(sp, o, d, mint, maxt, t);
+}
+// The analytic shapes are tested one by one after the triangle BVH.  The
+// plane test is out of line, so that scenes with spheres only keep the
+// traversal kernels' registers.
+__device__ __forceinline__ bool analytic_test(const DevSphere &sp, V3 o, V3 d, float mint, float maxt, float &t)
+{
+    if (sp.kind == 1) return plane_test_call(sp, o, d, mint, maxt, t);
+    return sphere_test(sp, o, d, mint, maxt, t);
+}
+
 // Adaptive epsilon of Bvh::intersection (accelStruct/Bvh.cpp:411-413)
 __device__ __forceinline__ float adapt_mint(V3 o, float mint)
 {
@@ -341,7 +371,7 @@ __device__ __forceinline__ bool trace_ray(const DevScene &S, V3 o, V3 d, float m
     }
     for (int s = 0; s < S.n_spheres; s++) {
         float t;
-        if (sphere_test(S.spheres[s], o, d, mint, hit_t, t)) {
+        if (analytic_test(S.spheres[s], o, d, mint, hit_t, t)) {
             h.t = t; h.u = 0.f; h.v = 0.f; h.prim = -s - 2;
             found = true;
             if (ANY) return true;
@@ -388,8 +418,12 @@ __device__ __forceinline__ Frame hit_frame(const DevScene &S, const Hit &h, V3 o
     } else {
         const DevSphere &sp = S.spheres[-h.prim - 2];
         f.p = o + h.t * d;
-        V3 nl = normalized(xf_point(sp.to_object, f.p) - v3(0, 0, 0));
-        f.n = normalized(xf_normal(sp.to_object, nl));
+        if (sp.kind == 1) {   // Plane::getDifferentialGeometry (Plane.cpp:82-92)
+            f.n = normalized(xf_normal(sp.to_object, v3(0.f, 0.f, 1.f)));
+        } else {
+            V3 nl = normalized(xf_point(sp.to_object, f.p) - v3(0, 0, 0));
+            f.n = normalized(xf_normal(sp.to_object, nl));
+        }
     }
     frame_from(f.n, f.s, f.t);
     return f;
@@ -517,6 +551,10 @@ __device__ __forceinline__ V2 hit_uv(const DevScene &S, const Hit &h, V3 o, V3 d
     }
     const DevSphere &sp = S.spheres[-h.prim - 2];
     V3 lo = xf_point(sp.to_object, o), ld = xf_vector(sp.to_object, d);
+    if (sp.kind == 1) {   // Plane::intersection (Plane.cpp:75-76)
+        V3 q = lo + h.t * ld;
+        return v2((q.x + 1) / 2.f, (q.y + 1) / 2.f);
+    }
     V3 n = normalized(lo + h.t * ld);
     return v2(spherical_phi(n) / (2 * RT_PI), spherical_theta(n) / RT_PI);
 }
@@ -1370,9 +1408,24 @@ __device__ __forceinline__ void sphere_sample(const DevSphere &s, V2 u, V3 &pt, 
     n = normalized(xf_normal(s.to_object, sphere_normal(s, p)));
     pt = xf_point(s.to_world, p);
 }
-// Sphere::pdf (Sphere.cpp:183-201) with ISampledShape::pdf (ISampledShape.cpp:17-40)
+// Plane::sample (Plane.cpp:94-98)
+__device__ __forceinline__ void plane_sample(const DevSphere &s, V2 u, V3 &pt, V3 &n)
+{
+    pt = xf_point(s.to_world, v3(1 - 2 * u.x, 1 - 2 * u.y, 0.f));
+    n = normalized(xf_normal(s.to_object, v3(0.f, 0.f, 1.f)));
+}
+// Sphere::pdf (Sphere.cpp:183-201) with ISampledShape::pdf (ISampledShape.cpp:17-40);
+// a Plane has ISampledShape::pdf alone
 __device__ __forceinline__ float sphere_pdf(const DevSphere &s, V3 p, V3 sampled, V3 n)
 {
+    if (s.kind == 1) {
+        V3 l = p - sampled;
+        float dist = norm(l);
+        l = normalized(l);
+        float c = dot(n, l);
+        if (c >= 0) return dist * dist / (s.area * c);
+        return 0.f;
+    }
     V3 center = xf_point(s.to_world, v3(0.f, 0.f, 0.f));
     V3 itc = p - center;
     float sqd = sqnorm(itc);
@@ -1530,6 +1583,7 @@ __device__ __forceinline__ void light_sample(const DevScene &S, int light, V3 p,
     if (o.delta) { delta_light_sample(L, p, o); return; }
     V3 pt, n;
     if (L.shape_kind == 0) mesh_sample(S, L.shape, s, pt, n);
+    else if (S.spheres[L.shape].kind == 1) plane_sample(S.spheres[L.shape], s, pt, n);
     else sphere_sample(S.spheres[L.shape], s, pt, n);
     o.point = pt;
     o.normal = n;

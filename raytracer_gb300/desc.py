@@ -20,6 +20,7 @@ BSDF_SHEET_DIELECTRIC, BSDF_MICROFACET = 8, 9
 DIST_BECKMANN, DIST_PHONG, DIST_GGX = 0, 1, 2
 LIGHT_AREA, LIGHT_ENV, LIGHT_POINT, LIGHT_SPOT = 0, 1, 2, 3
 SHAPE_MESH, SHAPE_SPHERE = 0, 1
+ANALYTIC_SPHERE, ANALYTIC_PLANE = 0, 1
 MEDIUM_HOMOGENEOUS, MEDIUM_HETEROGENEOUS = 0, 1
 PHASE_ISOTROPIC, PHASE_HG = 0, 1
 INTEGRATOR_PATH_MIS, INTEGRATOR_VOLPATH = 0, 1
@@ -58,7 +59,7 @@ class MeshDesc(C.Structure):
 class SphereDesc(C.Structure):
     _fields_ = [("radius", C.c_float), ("to_world", f16), ("to_object", f16),
                 ("bsdf", C.c_int32), ("light", C.c_int32), ("interior", C.c_int32),
-                ("exterior", C.c_int32)]
+                ("exterior", C.c_int32), ("kind", C.c_int32)]
 
 
 class LightDesc(C.Structure):
@@ -280,6 +281,14 @@ class SceneData:
                                  bsdf=bsdf, light=light, interior=interior, exterior=exterior))
         return len(self.spheres) - 1
 
+    def add_plane(self, to_world, bsdf=-1, light=-1, interior=-1, exterior=-1):
+        """Plane (geometricShape/Plane.cpp): the square [-1,1]^2 at z = 0 of
+        its object space, normal +z, placed by "toWorld".  It joins the
+        analytic shapes (an area light on it uses SHAPE_SPHERE and this index)."""
+        self.spheres.append(dict(radius=0.0, to_world=np.asarray(to_world, np.float64), kind=ANALYTIC_PLANE,
+                                 bsdf=bsdf, light=light, interior=interior, exterior=exterior))
+        return len(self.spheres) - 1
+
     def add_area_light(self, radiance, shape_kind, shape, mesh_light=True):
         self.lights.append(dict(type=LIGHT_AREA, mesh_light=int(mesh_light), shape_kind=shape_kind,
                                 shape=shape, radiance=tuple(radiance)))
@@ -342,8 +351,11 @@ class SceneData:
 
         spheres = (SphereDesc * max(1, len(self.spheres)))()
         for i, s in enumerate(self.spheres):
-            spheres[i] = SphereDesc(s["radius"], mat(s["to_world"]), mat(inv4(s["to_world"])),
-                                    s["bsdf"], s["light"], s["interior"], s["exterior"])
+            # the binary32 toWorld a scene file holds, inverted in float64
+            tw = np.asarray(s["to_world"], np.float32).astype(np.float64)
+            spheres[i] = SphereDesc(s["radius"], mat(tw), mat(inv4(tw)),
+                                    s["bsdf"], s["light"], s["interior"], s["exterior"],
+                                    s.get("kind", ANALYTIC_SPHERE))
         D.n_spheres = len(self.spheres)
         D.spheres = C.cast(spheres, C.POINTER(SphereDesc))
 

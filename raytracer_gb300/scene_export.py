@@ -337,8 +337,12 @@ def write_scene(scene, folder, spp=1, name="scene"):
                 out += _medium_xml(s.media[m[key]], key, folder, "medium%d" % m[key], 6)
         out.append("    </shape>")
     for si, sp in enumerate(s.spheres):
-        out += ['    <shape type="Sphere">', '      <double name="radius" value="%s"/>' % _f(sp["radius"]),
-                '      <transform name="toWorld"><matrix value="%s"/></transform>' % _matrix(sp["to_world"])]
+        if sp.get("kind", D.ANALYTIC_SPHERE) == D.ANALYTIC_PLANE:
+            out += ['    <shape type="Plane">',
+                    '      <transform name="toWorld"><matrix value="%s"/></transform>' % _matrix(sp["to_world"])]
+        else:
+            out += ['    <shape type="Sphere">', '      <double name="radius" value="%s"/>' % _f(sp["radius"]),
+                    '      <transform name="toWorld"><matrix value="%s"/></transform>' % _matrix(sp["to_world"])]
         if sp["bsdf"] >= 0:
             out += _bsdf_xml(s.bsdfs[sp["bsdf"]], 6, tex)
         if sp["light"] >= 0:

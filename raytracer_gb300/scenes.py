@@ -23,6 +23,8 @@ describe:
 
 Sizes can be scaled down for tests through the keyword arguments.
 """
+import math
+
 import numpy as np
 
 from .desc import (SceneData, bsdf, camera, look_at, BSDF_DIFFUSE, BSDF_ROUGH_CONDUCTOR,
@@ -233,6 +235,47 @@ def cornell_delta_lights(width=96, height=96, area_light=True, spot_scale=1.0):
     T = np.array([[1, 0, 0, 0.7], [0, c, -sn, 0.95], [0, sn, c, 0.5], [0, 0, 0, 1]], np.float64)
     T[:3, :3] *= spot_scale
     s.add_spot_light(T, (1.5, 1.6, 2.0), falloff_start=20.0, total_width=35.0)
+    return s
+
+
+def plane_room(width=64, height=64, textured=False):
+    """A scene of Planes (geometricShape/Plane.cpp): a 3 x 3 floor plane
+    under a rotated Diffuse panel, a tilted RoughConductor plane, and a
+    0.3 x 0.3 Plane area light facing down, beside the Cornell room's tall
+    box for a triangle mesh in the same render.  With `textured` the floor's
+    albedo is a checker ImageTexture read at the plane's uv."""
+    from .desc import BSDF_ROUGH_CONDUCTOR as RC, DIST_GGX
+    s = SceneData()
+    s.name = "plane_room_%d" % width
+    grey = s.add_bsdf(bsdf(BSDF_DIFFUSE, albedo=(0.7, 0.7, 0.7)))
+    red = s.add_bsdf(bsdf(BSDF_DIFFUSE, albedo=(0.7, 0.2, 0.15)))
+    metal = s.add_bsdf(bsdf(RC, distribution=DIST_GGX, alpha=0.2, eta=AU_ETA, k=AU_K))
+    lightmat = s.add_bsdf(bsdf(BSDF_DIFFUSE, albedo=(0.78, 0.78, 0.78)))
+    if textured:
+        t = s.add_texture(texture_image(32, 32, seed=3, kind="checker"))
+        s.bsdfs[grey]["tex_albedo"] = t
+
+    def rot_x(deg):
+        a = math.radians(deg)
+        return np.array([[1, 0, 0, 0], [0, math.cos(a), -math.sin(a), 0], [0, math.sin(a), math.cos(a), 0],
+                         [0, 0, 0, 1]], np.float64)
+
+    def place(scale, deg, tr):
+        T = np.diag([scale[0], scale[1], 1.0, 1.0]) if len(scale) == 2 else np.diag(list(scale) + [1.0])
+        M = rot_x(deg) @ T
+        M[:3, 3] = tr
+        return M
+
+    s.add_plane(place((1.5, 1.5), -90.0, (0.5, 0.0, 0.5)), bsdf=grey)         # floor y = 0, normal +y
+    s.add_plane(place((0.25, 0.2), -20.0, (0.3, 0.35, 0.4)), bsdf=red)       # panel
+    s.add_plane(place((0.2, 0.3), -60.0, (0.75, 0.3, 0.3)), bsdf=metal)      # tilted metal sheet
+    li = s.add_plane(place((0.15, 0.15), 90.0, (0.5, 0.95, 0.5)), bsdf=lightmat)   # light, normal -y
+    s.spheres[li]["light"] = s.add_area_light((12.0, 11.0, 9.0), SHAPE_SPHERE, li, mesh_light=False)
+    tv, tf = _box((0.6, 0.3, 0.6), (0.2, 0.6, 0.2), 15.0)
+    s.add_mesh(tv, tf, bsdf=grey)
+    s.camera = camera(width, height, 40.0, look_at((0.5, 0.6, 2.6), (0.5, 0.3, 0.4), (0, 1, 0)))
+    s.integrator = dict(integrator=INTEGRATOR_PATH_MIS, max_depth=8, min_depth=3,
+                        strategy=STRATEGY_ONE_LIGHT_UNIFORM)
     return s
 
 

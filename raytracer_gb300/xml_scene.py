@@ -19,9 +19,11 @@ the element.  Paths in the file are resolved against the file's folder
     medium       (top level) the camera medium (XMLLoader.cpp:96-101; the later
                  referable-medium branch of the reference is unreachable)
     lights       EnvironmentLight: path (.hdr, .exr, PNG...), toWorld, scale, gamma
-                 (EnvironmentLight.cpp:8-19)
+                 (EnvironmentLight.cpp:8-19); PointLight (position, intensity);
+                 SpotLight (toWorld, intensity, falloffStart, totalWidth)
     objects      shape Mesh (path .obj, toWorld; MeshFactory.h:39-139), Cube
                  (toWorld; Cube.cpp), Sphere (radius, toWorld; Sphere.cpp:14-15),
+                 Plane (toWorld; Plane.cpp:7-18),
                  each with <bsdf>, <light type="AreaLight|MeshLight"> (radiance),
                  <medium name="interior|exterior">
     bsdf         Diffuse, RoughConductor, RoughDielectric, SmoothLayeredBSDF
@@ -55,6 +57,7 @@ _TYPE_NAMES = ["ConstantTexture", "ImageTexture", "Diffuse", "RoughConductor", "
                "SmoothLayeredBSDF", "LayeredBSDF", "Dielectric", "Conductor", "Mirror", "TwoSides",
                "SheetDielectric", "Microfacet",
                "HGPhaseFunction", "IsotropicPhaseFunction", "Homogeneous", "Heterogeneous", "Mesh", "Cube", "Sphere",
+               "Plane",
                "MeshLight", "AreaLight", "NoriPerspective", "BoxFilter", "GaussianFilter", "MitchellNetravaliFilter",
                "EnvironmentLight", "PointLight", "SpotLight", "RandomSampler", "StratifiedSampler",
                "PathTracingMIS", "VolPathTracing",
@@ -450,9 +453,13 @@ class _Loader:
                 li = self.s.add_area_light(light[1].get("radiance", (0.0, 0.0, 0.0)), D.SHAPE_MESH, mi,
                                            mesh_light=light[0] == "MeshLight")
                 self.s.meshes[mi]["light"] = li
-        elif kind == "Sphere":
-            si = self.s.add_sphere(p.get("radius", 1.0), np.asarray(to_world, np.float64), bsdf=bsdf,
-                                   interior=interior, exterior=exterior)
+        elif kind in ("Sphere", "Plane"):
+            if kind == "Sphere":
+                si = self.s.add_sphere(p.get("radius", 1.0), np.asarray(to_world, np.float64), bsdf=bsdf,
+                                       interior=interior, exterior=exterior)
+            else:   # Plane.cpp:7-18
+                si = self.s.add_plane(np.asarray(to_world, np.float64), bsdf=bsdf, interior=interior,
+                                      exterior=exterior)
             if light is not None:
                 li = self.s.add_area_light(light[1].get("radiance", (0.0, 0.0, 0.0)), D.SHAPE_SPHERE, si,
                                            mesh_light=light[0] == "MeshLight")

@@ -104,6 +104,11 @@ def test_trace_parity_spheres_and_boxes(ctx, rtlib, vol, width):
     _trace_parity(ctx, rtlib, vol, n=20000, seed=2)
 
 
+def test_trace_parity_planes(ctx, rtlib, width):
+    """Planes (Plane::intersection) beside a triangle mesh."""
+    _trace_parity(ctx, rtlib, scenes.plane_room(32, 32), seed=7)
+
+
 def test_trace_edge_cases(ctx, rtlib, cornell, width):
     g = rtlib.Scene(ctx, cornell)
     o = O.OracleScene(cornell)
@@ -256,6 +261,12 @@ def test_delta_light_parity(ctx, rtlib, kind):
     s = scenes.cornell_delta_lights(16, 16, spot_scale=1.05)
     li = [i for i, L in enumerate(s.lights) if L["type"] == kind][0]
     _light_parity(ctx, rtlib, s, li, seed=3)
+
+
+def test_plane_light_parity(ctx, rtlib):
+    """An AreaLight on a Plane: Plane::sample and ISampledShape::pdf."""
+    s = scenes.plane_room(16, 16)
+    _light_parity(ctx, rtlib, s, 0, seed=8)
 
 
 def _medium_queries(n, rng, box_lo, box_hi):
@@ -490,6 +501,17 @@ def test_film_parity_delta_lights_volpath(ctx, rtlib):
         ctx.set_tuning(**before)
     g.close()
     assert np.array_equal(fg, mega)
+
+
+def test_film_parity_planes(ctx, rtlib, width):
+    """Planes as floor, panels and area light, plain and with a texture read
+    at the plane's uv, under PathTracingMIS and VolPathTracing."""
+    plain, _ = _film_parity(ctx, rtlib, scenes.plane_room(40, 32), 4, 71, max_bad=0.03)
+    tex, _ = _film_parity(ctx, rtlib, scenes.plane_room(40, 32, textured=True), 4, 71, max_bad=0.03)
+    assert not np.array_equal(plain, tex)
+    s = scenes.plane_room(32, 24)
+    s.integrator = dict(s.integrator, integrator=D.INTEGRATOR_VOLPATH)
+    _film_parity(ctx, rtlib, s, 3, 72, max_bad=0.05)
 
 
 def test_film_parity_smooth_bsdfs_volpath(ctx, rtlib):
