@@ -55,7 +55,10 @@ def _peaks():
 
 
 class ClockSampler:
-    """nvidia-smi sampling during the timed region."""
+    """nvidia-smi sampling during the timed region.  Start it before the
+    warm-up (nvidia-smi takes a moment to print its first row) and bracket the
+    timed region with begin() / end(): only rows stamped inside it count, or,
+    for a region shorter than the sampling interval, the rows next to it."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -65,11 +68,19 @@ class ClockSampler:
         self.device = device
         self.rows = []
         self.proc = None
+        self.window = None
+
+    def begin(self):
+        self.window = [time.time(), None]
+
+    def end(self):
+        if self.window:
+            self.window[1] = time.time()
 
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -78,7 +89,7 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.rows.append([c.strip() for c in line.split(",")])
+            self.rows.append((time.time(), [c.strip() for c in line.split(",")]))
 
     def stop(self):
         if not self.proc:
@@ -91,7 +102,18 @@ class ClockSampler:
         self.t.join(timeout=2)
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for r in self.rows:
+        rows = self.rows
+        if self.window and self.window[1] is not None and rows:
+            a, b = self.window
+            inside = [r for t, r in rows if a <= t <= b + 0.06]
+            if not inside:   # a region shorter than the interval: the rows on either side
+                before = [r for t, r in rows if t < a][-1:]
+                after = [r for t, r in rows if t > b][:1]
+                inside = before + after
+            rows = inside
+        else:
+            rows = [r for _, r in rows]
+        for r in rows:
             try:
                 sm.append(float(r[1]))
                 smax.append(float(r[2]))
@@ -242,18 +264,19 @@ def run_gpu(args):
     # steps after the timed region
     ctx.set_profiling(0 if args.graphs else 1)
     ctx.set_graphs(args.graphs)
+    clocks = ClockSampler(local)
+    clocks.start()   # before the warm-up: its first rows arrive after a moment
     for _ in range(args.warmup):
         scene.render(spp, seed=7, sample_begin=sbase, film=film.data_ptr())
         pre_launches += ctx.stats()["launches"]
     barrier()
-    clocks = ClockSampler(local)
-    clocks.start()
     agg = {}
     launches = 0
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     barrier()
     torch.cuda.nvtx.range_push("timed")   # profilers can select the timed launches by this range
+    clocks.begin()
     e0.record(stream)
     for k in range(args.steps):
         scene.render(spp, seed=1000 + k, sample_begin=sbase, film=film.data_ptr())
@@ -267,6 +290,7 @@ def run_gpu(args):
     e1.record(stream)
     torch.cuda.nvtx.range_pop()
     barrier()
+    clocks.end()
     clk = clocks.stop()
     if args.graphs:
         ctx.set_graphs(0)
