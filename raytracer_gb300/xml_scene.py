@@ -53,7 +53,7 @@ F32 = np.float32
 # The reference's object factories match type names without regard to case
 # (ObjectFactoryManager::formatType, factory/ObjectFactoryManager.h:81-89):
 # "roughconductor" is RoughConductor.  _type gives the spelling used here.
-_TYPE_NAMES = ["ConstantTexture", "ImageTexture", "Diffuse", "RoughConductor", "RoughDielectric",
+_TYPE_NAMES = ["ConstantTexture", "ImageTexture", "ScaleTexture", "Diffuse", "RoughConductor", "RoughDielectric",
                "SmoothLayeredBSDF", "LayeredBSDF", "Dielectric", "Conductor", "Mirror", "TwoSides",
                "SheetDielectric", "Microfacet",
                "HGPhaseFunction", "IsotropicPhaseFunction", "Homogeneous", "Heterogeneous", "Mesh", "Cube", "Sphere",
@@ -217,6 +217,8 @@ class _Loader:
                     params[name] = ("texture", tp.get("albedo", (0.5, 0.5, 0.5)))   # ConstantTexture.cpp:6-10
                 elif kind == "ImageTexture":
                     params[name] = ("image", self.image_texture(tp))
+                elif kind == "ScaleTexture":
+                    params[name] = self.scale_texture(tp)
                 else:
                     raise UnsupportedScene("texture type %s is not provided" % kind)
             elif tag == "bsdf":
@@ -273,6 +275,29 @@ class _Loader:
             raise UnsupportedScene("ImageTexture %s: %s" % (path, e))
         self.tex_cache[key] = self.s.add_texture(rgb, scale=scale, invert_x=ix, invert_y=iy)
         return self.tex_cache[key]
+
+    def scale_texture(self, tp):
+        """ScaleTexture (texture/ScaleTexture.cpp): eval = texture.eval(uv) *
+        scale.  Over a constant it is the scaled constant; over an
+        ImageTexture it becomes a copy of that texture whose scale is the
+        product of the two (the texel is then multiplied once by the product,
+        where the reference multiplies by each in turn: at most an ulp or so
+        apart).  A negative scale is not provided: the device's textures
+        carry a non-negative scale."""
+        inner = tp.get("texture")
+        k = float(tp.get("scale", 1.0))
+        if not (isinstance(inner, tuple) and len(inner) == 2):
+            raise UnsupportedScene("ScaleTexture without a texture")
+        if k < 0:
+            raise UnsupportedScene("ScaleTexture with a negative scale is not provided")
+        if inner[0] == "texture":
+            return ("texture", tuple(float(x) * k for x in inner[1]))
+        T = self.s.textures[inner[1]]
+        key = ("scaled", inner[1], k)
+        if key not in self.tex_cache:
+            self.tex_cache[key] = self.s.add_texture(T["rgb"], scale=T["scale"] * k, invert_x=T["invert_x"],
+                                                     invert_y=T["invert_y"])
+        return ("image", self.tex_cache[key])
 
     # BSDFs: returns the index in the scene's BSDF table
     def bsdf(self, el, params=None):
