@@ -148,9 +148,42 @@ def make_scene():
                                       seed=CONFIG["seed"], env_size=CONFIG["env"], max_depth=CONFIG["max_depth"])
 
 
+def _config(data):
+    """The workload, identical in both arms' JSON lines: the scene, the
+    render and how the timed inputs relate to L2."""
+    W, H = CONFIG["width"], CONFIG["height"]
+    return {"workload": _workload_name(),
+            "integrator": "VolPathTracing" if CONFIG.get("volume") else "PathTracingMIS",
+            "triangles": data.n_triangles, "resolution": [W, H], "spp": CONFIG["spp"],
+            "max_depth": CONFIG["max_depth"], "samples_per_step": W * H * CONFIG["spp"],
+            "filter": getattr(_ARGS, "filter", "box"),
+            "parallelism": "replicas" if int(os.environ.get("WORLD_SIZE", "1")) > 1 else "single",
+            "l2": "inputs larger than L2: the scene (BVH, triangles, materials, maps) and the wavefront path "
+                  "state (about 205 bytes per path in flight) live in HBM"}
+
+
+_ARGS = None
+
+
+def _tile_sample(ntiles, n, tiles_x):
+    """n tiles spread evenly over the job grid: tiles t0 + k * stride in
+    raster order with the stride about ntiles / n and coprime with the grid
+    width, so the sample walks a diagonal lattice through every row band and
+    column (sky, sphere and ground in proportion), not the frame's centre."""
+    import math
+    n = max(1, min(n, ntiles))
+    stride = max(1, ntiles // n)
+    while stride > 1 and math.gcd(stride, tiles_x) != 1:
+        stride -= 1
+    t0 = stride // 2
+    n = min(n, (ntiles - 1 - t0) // stride + 1)
+    return t0, n, stride
+
+
 def cpu_oracle_rate(scene, target_s=15.0, threads=None):
     """Time the CPU oracle (the reference path restated in C) on a bounded
-    sample: whole 32x32 tiles at the full spp, sized for about target_s."""
+    sample: whole 32x32 tiles at the full spp, spread evenly over the frame,
+    as many as take about target_s."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle_lib as O
     threads = threads or os.cpu_count() or 1
@@ -160,17 +193,20 @@ def cpu_oracle_rate(scene, target_s=15.0, threads=None):
     W, H = scene.camera["width"], scene.camera["height"]
     tiles_x = (W + 31) // 32
     ntiles = tiles_x * ((H + 31) // 32)
-    # calibration: one tile row of the image middle
-    mid = (ntiles // 2) - tiles_x // 2
-    cal = max(1, min(threads, 8))
+    # calibration on a spread sample of one tile per thread
+    cal0, cal, cstride = _tile_sample(ntiles, max(1, min(threads, 16)), tiles_x)
     t0 = time.time()
-    o.render_tiles(CONFIG["spp"], mid, mid + cal, seed=1, threads=threads)
+    o.render_tiles_strided(CONFIG["spp"], cal0, cal, cstride, seed=1, threads=threads)
     dt = max(time.time() - t0, 1e-3)
     per_tile = dt / cal * min(threads, cal) / threads
     n = int(max(threads, min(ntiles, target_s / max(per_tile, 1e-4))))
-    n = max(1, min(n, ntiles))
-    start = max(0, ntiles // 2 - n // 2)
-    return o, start, n, build_s
+    tile0, n, stride = _tile_sample(ntiles, n, tiles_x)
+    return o, tile0, n, stride, build_s
+
+
+def _sample_desc(tile0, n, stride, ntiles, spp, threads, extra=""):
+    return ("%d of %d 32x32 tiles spread over the frame (tiles %d + %d k), %d path samples, full %d spp, "
+            "%d threads%s" % (n, ntiles, tile0, stride, n * 32 * 32 * spp, spp, threads, extra))
 
 
 def run_reference(args):
@@ -179,27 +215,25 @@ def run_reference(args):
         return
     scene = make_scene()
     threads = os.cpu_count() or 1
-    o, start, n, build_s = cpu_oracle_rate(scene, target_s=args.cpu_seconds)
+    o, tile0, n, stride, build_s = cpu_oracle_rate(scene, target_s=args.cpu_seconds)
     spp = CONFIG["spp"]
     for _ in range(max(0, min(args.warmup, 1))):
-        o.render_tiles(spp, start, start + max(1, n // 8), seed=3, threads=threads)
+        o.render_tiles_strided(spp, tile0, max(1, n // 8), stride, seed=3, threads=threads)
     times = []
     for k in range(args.steps):
         t0 = time.time()
-        o.render_tiles(spp, start, start + n, seed=4 + k, threads=threads)
+        o.render_tiles_strided(spp, tile0, n, stride, seed=4 + k, threads=threads)
         times.append(time.time() - t0)
     samples = n * 32 * 32 * spp
     value = samples * len(times) / sum(times)
     W, H = CONFIG["width"], CONFIG["height"]
-    sample_desc = "%d of %d 32x32 tiles (%d path samples) per step, full %d spp, %d threads" % (
-        n, ((W + 31) // 32) * ((H + 31) // 32), samples, spp, threads)
+    ntiles = ((W + 31) // 32) * ((H + 31) // 32)
+    sample_desc = _sample_desc(tile0, n, stride, ntiles, spp, threads, " per step")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * float(np.mean(times)),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded scene generator, no dataset)",
-            "config": {"workload": _workload_name(),
-                       "integrator": "VolPathTracing" if CONFIG.get("volume") else "PathTracingMIS",
-                       "sample": sample_desc},
+            "config": _config(scene),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample_desc},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "notes": "reference CPU path = the oracle's C restatement of the integrator with the reference's "
@@ -372,19 +406,22 @@ def run_gpu(args):
             traffic = tj[key] * rays / max(nl, 1)
         except Exception:
             traffic = None
+    dram_gbs = traffic / max(avg_launch_s, 1e-12) / 1e9 if traffic is not None else None
+    dram_frac = dram_gbs / peaks.get("hbm_gbs", 1) if dram_gbs is not None else None
+    bound = "latency/L2" if dom in ("trace_closest", "trace_any") else "latency"
     rays_per_s = (rays_c + rays_a) * world / t_local
     res = {}
     if rank == 0 and not args.small:
         try:
-            cpu_o, start, n, _ = cpu_oracle_rate(data, target_s=args.cpu_seconds)
+            cpu_o, tile0, n, stride, _ = cpu_oracle_rate(data, target_s=args.cpu_seconds)
             threads = os.cpu_count() or 1
             t0 = time.time()
-            cpu_o.render_tiles(spp, start, start + n, seed=5, threads=threads)
+            cpu_o.render_tiles_strided(spp, tile0, n, stride, seed=5, threads=threads)
             cdt = time.time() - t0
             cpu_samples = n * 32 * 32 * spp
             res["cpu_baseline"] = {"value": cpu_samples / cdt, "unit": UNIT, "cores": threads, "kind": "port",
-                                   "sample": "%d of %d 32x32 tiles at %d spp (%d path samples), %.1f s" %
-                                             (n, ((W + 31) // 32) * ((H + 31) // 32), spp, cpu_samples, cdt)}
+                                   "sample": _sample_desc(tile0, n, stride, ((W + 31) // 32) * ((H + 31) // 32),
+                                                          spp, threads, ", %.1f s" % cdt)}
         except Exception as ex:  # the baseline never blocks the GPU line
             res["cpu_baseline"] = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                                    "sample": "failed: %s" % ex}
@@ -395,24 +432,26 @@ def run_gpu(args):
                 "data": "synthetic (seeded scene generator: %s; no dataset)" % (
                     "fBm grid medium" if CONFIG.get("volume") else
                     "furnished Cornell room" if CONFIG.get("smooth") else "displaced icosphere + procedural sky"),
-                "config": {"workload": _workload_name(),
-                           "integrator": "VolPathTracing" if CONFIG.get("volume") else "PathTracingMIS",
-                           "triangles": data.n_triangles,
-                           "resolution": [W, H], "spp": spp, "bvh_width": args.bvh_width, "max_depth": CONFIG["max_depth"],
-                           "graphs": args.graphs, "sort_threshold": args.sort_threshold, "filter": args.filter,
-                           "volpath_wavefront": args.volpath_wavefront,
-                           "samples_per_step": samples_per_step, "parallelism": "replicas" if world > 1 else "single",
-                           "l2": "inputs larger than L2 (scene %.0f MB on the device, path state %.1f GB per "
-                                 "batch of %d paths)" % (info["device_bytes"] / 1e6, batch_paths * 205 / 1e9,
-                                                         batch_paths),
-                           "scene_gen_s": round(gen_s, 2), "scene_build_upload_s": round(upload_s, 2)},
+                "config": _config(data),
+                "tuning": {"bvh_width": args.bvh_width, "graphs": args.graphs,
+                           "sort_threshold": args.sort_threshold, "volpath_wavefront": args.volpath_wavefront,
+                           "wave_paths": batch_paths},
+                "setup": {"scene_device_mb": round(info["device_bytes"] / 1e6, 1),
+                          "path_state_gb_per_batch": round(batch_paths * 205 / 1e9, 2),
+                          "scene_gen_s": round(gen_s, 2), "scene_build_upload_s": round(upload_s, 2)},
                 "e2e": None if args.small else {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                                                 "d2h_bytes_per_step": d2h},
-                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                "roofline": {"bound": bound, "achieved": achieved, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
                              "frac": achieved / peaks.get("hbm_gbs", 1), "traffic": traffic,
-                             "kernel": dom, "peak_source": src,
+                             "dram_gbs": dram_gbs, "dram_frac": dram_frac,
+                             "kernel": dom, "peak_source": src, "peak_kind": "HBM copy bandwidth (of measured)",
                              "algorithmic_bytes_per_ray": per_ray, "launches": nl,
-                             "avg_launch_ms": avg_launch_s * 1000},
+                             "avg_launch_ms": avg_launch_s * 1000,
+                             "note": "frac = algorithmic bytes (node + triangle fetches, ray in, hit out) per "
+                                     "launch / launch time / HBM peak; most node fetches hit L2, so it is a "
+                                     "memory-side request rate, not DRAM throughput. dram_frac = ncu DRAM "
+                                     "bytes per launch / launch time / HBM peak. The kernel is latency-bound "
+                                     "(dependent node fetches, divergent lanes)"},
                 "mrays_per_s": rays_per_s / 1e6,
                 "kernel_ms": {k: round(v / args.steps, 3) for k, v in kern.items()},
                 "kernel_ms_source": ("kernel-by-kernel profiled steps after the graph-launched timed region"
@@ -613,6 +652,8 @@ def main():
     ap.add_argument("--target-rmse", type=float, default=0.02)
     ap.add_argument("--spp-cap", type=int, default=256)
     args = ap.parse_args()
+    global _ARGS
+    _ARGS = args
     if args.workload == "batch":
         return run_batch(args)
     if args.workload == "serve":

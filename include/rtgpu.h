@@ -433,18 +433,20 @@ rt_status rt_autotune(rt_ctx *ctx, rt_scene *const *scenes, const rt_render_desc
  * for callers that cannot allocate device memory while rendering (plugins
  * whose host application owns the device memory through its own pool under
  * a hard budget, real-time loops that forbid cudaMalloc/cudaFree after
- * start-up because they can synchronise the device, code issuing work while
- * another component captures the stream).  Renders every sample of tile
- * (tile_x, tile_y) of the block_x x block_y job grid into film_rgbw_device
- * (a device pointer to the full width*height*4 film; only the tile's pixels
- * are written), with the same results as rt_render for those pixels.
+ * start-up because they can synchronise the device).  Renders every sample
+ * of tile (tile_x, tile_y) of the block_x x block_y job grid into
+ * film_rgbw_device (a device pointer to the full width*height*4 film; only
+ * the tile's pixels are written, or added to with RT_RENDER_ACCUMULATE),
+ * with the same results as rt_render for those pixels.
  * Limits: tile pixels * spp * ~240 bytes of path state must fit the 32 MiB
  * static scratch (about 130k path samples, e.g. 32x32 at 128 spp);
- * max_depth <= 1024; at most 256 lights; larger requests return
- * RT_ERR_LIMIT.  The first call on a device looks up the scratch address
- * (cudaGetSymbolAddress) and should come before any stream capture.  All
- * calls on one device share the scratch and keep its last contents: calls
- * that overlap on the GPU (other threads or streams) race. */
+ * PathTracingMIS max_depth <= 1024; at most 256 lights; larger requests
+ * return RT_ERR_LIMIT.  The call synchronises the context's stream, so that
+ * stream must not be under stream capture (RT_ERR_UNSUPPORTED otherwise).
+ * The first call on a device looks up the scratch address
+ * (cudaGetSymbolAddress).  All calls on one device share the scratch and
+ * keep its last contents: calls that overlap on the GPU (other threads or
+ * streams) race. */
 rt_status rt_render_tile_static(rt_ctx *ctx, rt_scene *scene, const rt_render_desc *rd,
                                 int32_t tile_x, int32_t tile_y, float *film_rgbw_device);
 
@@ -498,9 +500,23 @@ rt_status rt_job_wait(rt_server *srv, rt_job_id id, int32_t timeout_ms, rt_job_i
 /* Finish running jobs, drop queued ones, release the lanes. */
 rt_status rt_server_stop(rt_server *srv);
 
-/* Trace n rays (closest hit, or any hit when anyhit != 0). */
+/* Trace n rays (closest hit, or any hit when anyhit != 0).  Returns
+ * RT_ERR_LIMIT if a traversal had to drop a subtree (a stack was full); the
+ * builder bounds the tree depth so that this does not happen. */
 rt_status rt_trace(rt_ctx *ctx, rt_scene *scene, const rt_ray *rays, int32_t n,
                    int32_t anyhit, rt_hit *hits, int32_t on_device);
+
+/* Host-only: build the device tree (width 2: binary, 8: compressed 8-wide)
+ * over n triangles (9 floats each) as rt_scene_create would, and report its
+ * deepest leaf level (root 0) and node count; the binary tree is also
+ * checked structurally (RT_ERR_INVALID if malformed).  Stands in for
+ * Bvh::build (accelStruct/Bvh.cpp:51-79), whose traversal keeps a fixed
+ * stack of 64 (Bvh.cpp:402): the builder here splits at the object median
+ * wherever the SAH tree would grow deeper than depth_cap levels (<= 0: the
+ * default 62, which rt_scene_create uses; at most 62; 2^depth_cap >= n), so
+ * the traversal stacks cannot overflow.  Needs no GPU. */
+rt_status rt_bvh_stats(const float *tri_v, int32_t n, int32_t width, int32_t depth_cap,
+                       int32_t *max_depth, int32_t *n_nodes);
 
 /* Evaluate BSDF `bsdf` of the scene for n queries (host arrays). */
 rt_status rt_bsdf_query(rt_ctx *ctx, rt_scene *scene, int32_t bsdf, int32_t op,

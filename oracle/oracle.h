@@ -235,6 +235,8 @@ int32_t oracle_scene_info(const o_scene *sc, float bounds[6], int32_t *nodes);
 int32_t oracle_render(o_scene *sc, const rt_render_desc *rd, float *film_rgbw, int32_t nthreads);
 int32_t oracle_render_tiles(o_scene *sc, const rt_render_desc *rd, int32_t tile0, int32_t tile1,
                             float *film_rgbw, int32_t nthreads);
+int32_t oracle_render_tiles_strided(o_scene *sc, const rt_render_desc *rd, int32_t tile0, int32_t count,
+                                    int32_t stride, float *film_rgbw, int32_t nthreads);
 int32_t oracle_render_paths(o_scene *sc, const rt_render_desc *rd, const int32_t *pixels,
                             const int32_t *samples, int32_t n, float *rad_out);
 int32_t oracle_trace(const o_scene *sc, const rt_ray *rays, int32_t n, int32_t anyhit, rt_hit *hits);

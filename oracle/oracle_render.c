@@ -641,7 +641,8 @@ typedef struct {
     const rt_render_desc *rd;
     float *subs;          /* one tile screen per tile of the range, (bx + 2ovx) x (by + 2ovy) */
     int ntx, nty, ovx, ovy, sw, sh;
-    int first, next, end;
+    int first, next, end;  /* tiles first + k * stride for k in [0, end - first) */
+    int stride;
     float table[1024];
     pthread_mutex_t mu;
     int64_t nan_count;
@@ -681,14 +682,15 @@ static void *job_worker(void *arg)
     int64_t nan = 0;
     for (;;) {
         pthread_mutex_lock(&J->mu);
-        int t = J->next++;
+        int k = J->next++;
         pthread_mutex_unlock(&J->mu);
-        if (t >= J->end) break;
+        if (k >= J->end) break;
+        int t = J->first + (k - J->first) * J->stride;
         int ox = (t % J->ntx) * bx, oy = (t / J->ntx) * by;
         int ex = imin(cam->width, ox + bx), ey = imin(cam->height, oy + by);
         int tw = ex - ox, th = ey - oy;
         int sw = tw + 2 * J->ovx, sh = th + 2 * J->ovy;
-        float *sub = J->subs + 4 * (size_t)J->sw * J->sh * (size_t)(t - J->first);
+        float *sub = J->subs + 4 * (size_t)J->sw * J->sh * (size_t)(k - J->first);
         memset(sub, 0, sizeof(float) * 4 * (size_t)sw * sh);
         for (int y = oy; y < ey; y++)
             for (int x = ox; x < ex; x++)
@@ -710,10 +712,37 @@ static void *job_worker(void *arg)
  * overlap border of ceil(r - 0.5) pixels; `film` receives the full screen's
  * top-left width x height block, as the reference reads it back
  * (Screen.h:52, Screen.cpp:113-122).  Pixels no tile reaches stay zero. */
+static int32_t render_tile_set(o_scene *sc, const rt_render_desc *rd, int32_t tile0, int32_t count,
+                               int32_t stride, float *film, int32_t nthreads);
+
 int32_t oracle_render_tiles(o_scene *sc, const rt_render_desc *rd, int32_t tile0, int32_t tile1,
                             float *film, int32_t nthreads)
 {
     if (!sc || !rd || !film) return RT_ERR_INVALID;
+    const rt_camera_desc *cam = &sc->d->camera;
+    int bx = rd->block_x > 0 ? rd->block_x : 32, by = rd->block_y > 0 ? rd->block_y : 32;
+    int ntiles = ((cam->width + bx - 1) / bx) * ((cam->height + by - 1) / by);
+    int first = tile0 < 0 ? 0 : tile0;
+    int end = (tile1 < 0 || tile1 > ntiles) ? ntiles : tile1;
+    return render_tile_set(sc, rd, first, end > first ? end - first : 0, 1, film, nthreads);
+}
+
+/* Render `count` tiles tile0, tile0 + stride, ... of the job grid (a sample
+ * spread over the frame), merged in tile order as oracle_render_tiles does */
+int32_t oracle_render_tiles_strided(o_scene *sc, const rt_render_desc *rd, int32_t tile0, int32_t count,
+                                    int32_t stride, float *film, int32_t nthreads)
+{
+    if (!sc || !rd || !film || tile0 < 0 || count < 0 || stride < 1) return RT_ERR_INVALID;
+    const rt_camera_desc *cam = &sc->d->camera;
+    int bx = rd->block_x > 0 ? rd->block_x : 32, by = rd->block_y > 0 ? rd->block_y : 32;
+    int ntiles = ((cam->width + bx - 1) / bx) * ((cam->height + by - 1) / by);
+    if (count > 0 && (int64_t)tile0 + (int64_t)(count - 1) * stride >= ntiles) return RT_ERR_INVALID;
+    return render_tile_set(sc, rd, tile0, count, stride, film, nthreads);
+}
+
+static int32_t render_tile_set(o_scene *sc, const rt_render_desc *rd, int32_t tile0, int32_t count,
+                               int32_t stride, float *film, int32_t nthreads)
+{
     if (sc->strategy != rd->strategy || !sc->light_cdf.cdf) build_light_cdf(sc, rd->strategy);
     const rt_camera_desc *cam = &sc->d->camera;
     int bx = rd->block_x > 0 ? rd->block_x : 32, by = rd->block_y > 0 ? rd->block_y : 32;
@@ -725,8 +754,9 @@ int32_t oracle_render_tiles(o_scene *sc, const rt_render_desc *rd, int32_t tile0
     J.ovy = (int)ceilf(cam->filter_radius[1] - 0.5f);
     J.sw = bx + 2 * J.ovx;
     J.sh = by + 2 * J.ovy;
-    J.first = J.next = tile0 < 0 ? 0 : tile0;
-    J.end = (tile1 < 0 || tile1 > J.ntx * J.nty) ? J.ntx * J.nty : tile1;
+    J.first = J.next = tile0;
+    J.end = tile0 + count;
+    J.stride = stride;
     J.nan_count = 0;
     o_filter_table(cam, J.table);
     int nt = J.end - J.first;
@@ -744,11 +774,12 @@ int32_t oracle_render_tiles(o_scene *sc, const rt_render_desc *rd, int32_t tile0
     int FW = cam->width + 2 * J.ovx, FH = cam->height + 2 * J.ovy;
     float *full = (float *)calloc(4 * (size_t)FW * FH, sizeof(float));
     if (!full) { free(J.subs); return RT_ERR_NOMEM; }
-    for (int t = J.first; t < J.end; t++) {
+    for (int k = J.first; k < J.end; k++) {
+        int t = J.first + (k - J.first) * J.stride;
         int ox = (t % J.ntx) * bx, oy = (t / J.ntx) * by;
         int tw = imin(cam->width, ox + bx) - ox, tht = imin(cam->height, oy + by) - oy;
         int sw = tw + 2 * J.ovx, sh = tht + 2 * J.ovy;
-        const float *sub = J.subs + 4 * (size_t)J.sw * J.sh * (size_t)(t - J.first);
+        const float *sub = J.subs + 4 * (size_t)J.sw * J.sh * (size_t)(k - J.first);
         for (int x = 0; x < sw; x++)
             for (int y = 0; y < sh; y++) {
                 float *dst = full + 4 * ((size_t)(oy + y) * FW + (ox + x));

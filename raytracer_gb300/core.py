@@ -109,6 +109,8 @@ def lib():
     L.rt_hdr_load.restype = C.c_int32
     L.rt_host_free.argtypes = [vp]
     L.rt_host_free.restype = None
+    L.rt_bvh_stats.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+    L.rt_bvh_stats.restype = C.c_int32
     for name in ("rt_ctx_create", "rt_ctx_destroy", "rt_ctx_set_stream", "rt_scene_create", "rt_scene_destroy",
                  "rt_scene_info", "rt_render", "rt_render_stats_get", "rt_ctx_set_profiling", "rt_ctx_set_bvh_width", "rt_ctx_set_wave_paths", "rt_ctx_set_ray_sort", "rt_ctx_set_graphs",
                  "rt_ctx_get_tuning", "rt_ctx_set_tuning", "rt_autotune",
@@ -289,11 +291,14 @@ class Scene:
         _check(lib().rt_render(self.ctx.h, self.h, C.byref(rd), C.c_void_p(int(film)), 1))
         return None
 
-    def render_tile_static(self, tile_x, tile_y, film_ptr, spp, seed=0, sample_begin=0, block=32, **over):
+    def render_tile_static(self, tile_x, tile_y, film_ptr, spp, seed=0, sample_begin=0, block=32,
+                           accumulate=False, **over):
         """Allocation-free render of one job-grid tile into a device film
-        (an int device address of a width*height*4 float32 buffer); see
-        rt_render_tile_static in include/rtgpu.h for who needs it and its limits."""
-        rd = self.data.render_desc(spp, seed=seed, sample_begin=sample_begin, block=block, **over)
+        (an int device address of a width*height*4 float32 buffer), added to
+        the tile's pixels with `accumulate`; see rt_render_tile_static in
+        include/rtgpu.h for who needs it and its limits."""
+        flags = D.RENDER_ACCUMULATE if accumulate else 0
+        rd = self.data.render_desc(spp, seed=seed, sample_begin=sample_begin, block=block, flags=flags, **over)
         _check(lib().rt_render_tile_static(self.ctx.h, self.h, C.byref(rd), int(tile_x), int(tile_y),
                                            C.c_void_p(int(film_ptr))))
 
@@ -401,6 +406,17 @@ MEDIUM_R = np.dtype([("weight", np.float32, 3), ("t", np.float32), ("scattered",
 MEDIUM_OP_SAMPLE, MEDIUM_OP_TRANSMITTANCE = 0, 1
 assert BSDF_Q.itemsize == C.sizeof(D.BsdfQ) and BSDF_R.itemsize == C.sizeof(D.BsdfR)
 assert LIGHT_Q.itemsize == C.sizeof(D.LightQ) and LIGHT_R.itemsize == C.sizeof(D.LightR)
+
+
+def bvh_stats(tri_v, width=2, depth_cap=0):
+    """Build the device tree over triangles (n, 3, 3) on the host as
+    rt_scene_create would (rt_bvh_stats, no GPU needed) and return
+    (deepest leaf level, node count); the binary tree is checked
+    structurally.  depth_cap <= 0 is the default cap of 62 levels."""
+    tv = np.ascontiguousarray(tri_v, np.float32).reshape(-1)
+    d, n = C.c_int32(), C.c_int32()
+    _check(lib().rt_bvh_stats(_p(tv), len(tv) // 9, width, depth_cap, C.byref(d), C.byref(n)))
+    return d.value, n.value
 
 
 def load_obj(path, to_world=None):

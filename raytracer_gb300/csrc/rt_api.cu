@@ -326,6 +326,7 @@ __global__ void __launch_bounds__(128, RT_TRACE_MINB) k_trace(RenderParams P, in
     float tmin = 0, hit_t = 0, hu = 0, hv = 0;
     float lx = 0, hx = 0, ly = 0, hy = 0, lz = 0, hz = 0;   // guarded plane offsets (slab_guard)
     int hprim = -1;
+    bool dropped = false;   // a push found the stack full
 
     for (;;) {
         // ---- fetch rays for lanes whose ray is finished
@@ -391,6 +392,7 @@ __global__ void __launch_bounds__(128, RT_TRACE_MINB) k_trace(RenderParams P, in
                         int far = cc.y;
                         if (c1min < c0min) { far = node; node = cc.y; }
                         if (sp < RT_STACK) SPUSH(far);
+                        else dropped = true;   // unreachable: the build bounds the depth
                     }
                 }
                 // first leaf found: postpone it and keep traversing
@@ -447,6 +449,7 @@ __global__ void __launch_bounds__(128, RT_TRACE_MINB) k_trace(RenderParams P, in
         }
     }
     if (threadIdx.x == 0 && blockIdx.x == 0) atomicAdd(&P.stats[ANY ? 1 : 0], (unsigned long long)n);
+    if (dropped && P.limit_flag) atomicExch(P.limit_flag, 1);
 #undef SPUSH
 #undef SPOP
 }
@@ -500,6 +503,7 @@ __global__ void __launch_bounds__(128, 8) k_trace8(RenderParams P, int round)
     float nx_ = 0, fx_ = 0, ny_ = 0, fy_ = 0, nz_ = 0, fz_ = 0;   // near / far plane offsets (slab_guard)
     int hprim = -1;
     bool negx = false, negy = false, negz = false;
+    bool dropped = false;   // a push found the group stack full
 
     for (;;) {
         // ---- fetch rays for lanes whose ray is finished
@@ -556,7 +560,10 @@ __global__ void __launch_bounds__(128, 8) k_trace8(RenderParams P, int round)
                     const unsigned m = meta_byte(g1, (unsigned)(__ffs(gmask) - 1) ^ oct);
                     if ((m >> 5) != 7u) break;             // a leaf comes next
                     gmask &= gmask - 1;
-                    if (gmask && sp < RT_WSTACK) stack[sp++] = (gnode << 8) | (int)gmask;
+                    if (gmask) {
+                        if (sp < RT_WSTACK) stack[sp++] = (gnode << 8) | (int)gmask;
+                        else dropped = true;   // unreachable: deeper trees are not uploaded
+                    }
                     vnode = g1.x + (int)(m & 31u);
                 }
                 if (COUNT) cnt[0]++;
@@ -654,6 +661,7 @@ __global__ void __launch_bounds__(128, 8) k_trace8(RenderParams P, int round)
         }
     }
     if (threadIdx.x == 0 && blockIdx.x == 0) atomicAdd(&P.stats[ANY ? 1 : 0], (unsigned long long)n);
+    if (dropped && P.limit_flag) atomicExch(P.limit_flag, 1);
 }
 
 // rays of the rt_trace test hook into the wavefront buffers, and back
@@ -1878,6 +1886,13 @@ rt_status rt_scene_create(rt_ctx *ctx, const rt_scene_desc *d, rt_scene **out)
     // BVH
     BvhImage img;
     build_bvh2(tri_v.data(), nt, img, RT_BVH_LEAF, RT_BVH_BINS, RT_BVH_CNODE);
+    // the traversal stacks hold a sentinel plus one entry per level; the
+    // builder bounds the depth (RT_BVH_DEPTH_CAP), so this only guards it
+    if (img.max_depth + 1 > RT_STACK) {
+        rt_scene_destroy(sc);
+        return fail(RT_ERR_LIMIT, "rt_scene_create: BVH depth " + std::to_string(img.max_depth) +
+                                      " exceeds the traversal stack (" + std::to_string(RT_STACK) + " entries)");
+    }
     const float4 *np = nullptr, *tp = nullptr;
     if ((st = upload(sc, reinterpret_cast<const float4 *>(img.nodes.data()), (size_t)img.n_nodes * 4, &np)) != RT_OK) { rt_scene_destroy(sc); return st; }
     if ((st = upload(sc, reinterpret_cast<const float4 *>(img.tri_slots.data()), (size_t)img.n_slots * 3, &tp)) != RT_OK) { rt_scene_destroy(sc); return st; }
@@ -1986,6 +2001,32 @@ rt_status rt_scene_create(rt_ctx *ctx, const rt_scene_desc *d, rt_scene **out)
     sc->n_media = d->n_media;
     for (int b = 0; b < d->n_bsdfs; b++) sc->bsdf_types |= 1 << bsdf_queue_of(bsdfs[b]);
     *out = sc;
+    return RT_OK;
+}
+
+rt_status rt_bvh_stats(const float *tri_v, int32_t n, int32_t width, int32_t depth_cap, int32_t *max_depth,
+                       int32_t *n_nodes)
+{
+    if (n < 0 || (n > 0 && !tri_v) || (width != 2 && width != 8) || depth_cap > RT_BVH_DEPTH_CAP)
+        return fail(RT_ERR_INVALID, "rt_bvh_stats: bad argument");
+    if (depth_cap <= 0) depth_cap = RT_BVH_DEPTH_CAP;
+    if (n > 0 && (int64_t(1) << std::min(depth_cap, 62)) < (int64_t)n)
+        return fail(RT_ERR_INVALID, "rt_bvh_stats: depth_cap below log2 of the triangle count");
+    int d = 0, nn = 0;
+    if (width == 2) {
+        BvhImage img;
+        build_bvh2(tri_v, n, img, RT_BVH_LEAF, RT_BVH_BINS, RT_BVH_CNODE, depth_cap);
+        std::string why;
+        int walked = 0;
+        if (!check_bvh2(img, tri_v, n, &walked, &why)) return fail(RT_ERR_INVALID, "rt_bvh_stats: malformed tree: " + why);
+        d = img.max_depth; nn = img.n_nodes;
+    } else {
+        WideBvhImage img;
+        build_wbvh8(tri_v, n, img, 32, depth_cap);
+        d = img.max_depth; nn = img.n_nodes;
+    }
+    if (max_depth) *max_depth = d;
+    if (n_nodes) *n_nodes = nn;
     return RT_OK;
 }
 
@@ -2325,6 +2366,7 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
     RenderParams P;
     std::memset(&P, 0, sizeof(P));
     P.S = sc->S;
+    P.S.limit_flag = ctx->limit_flag;
     P.S.light_cdf = ctx->light_cdf;
     P.W = ctx->W;
     P.tileorder = ctx->tileorder;
@@ -2547,10 +2589,12 @@ rt_status rt_trace(rt_ctx *ctx, rt_scene *sc, const rt_ray *rays, int32_t n, int
     RenderParams P;
     std::memset(&P, 0, sizeof(P));
     P.S = sc->S;
+    P.S.limit_flag = ctx->limit_flag;
     P.W = ctx->W;
     P.stats = ctx->stats;
     P.limit_flag = ctx->limit_flag;
     const int sm = ctx->sm_count > 0 ? ctx->sm_count : 1;
+    CK(cudaMemsetAsync(ctx->limit_flag, 0, sizeof(int), st));
     k_rays_in<<<(n + 127) / 128, 128, 0, st>>>(dr, n, P, anyhit ? 1 : 0);
     if (ctx->bvh_width == 8 && sc->wide_ok) {
         if (anyhit) k_trace8<true, false><<<sm * 12, 128, 0, st>>>(P, 0);
@@ -2565,8 +2609,14 @@ rt_status rt_trace(rt_ctx *ctx, rt_scene *sc, const rt_ray *rays, int32_t n, int
         cudaError_t e = cudaMemcpyAsync(hits, tmp_h, sizeof(rt_hit) * (size_t)n, cudaMemcpyDeviceToHost, st);
         if (e != cudaSuccess) s = fail(RT_ERR_CUDA, cudaGetErrorString(e));
     }
+    int limit = 0;
+    if (s == RT_OK) {
+        cudaError_t e = cudaMemcpyAsync(&limit, ctx->limit_flag, sizeof(int), cudaMemcpyDeviceToHost, st);
+        if (e != cudaSuccess) s = fail(RT_ERR_CUDA, cudaGetErrorString(e));
+    }
     cudaError_t e = cudaStreamSynchronize(st);
     if (s == RT_OK && e != cudaSuccess) s = fail(RT_ERR_CUDA, cudaGetErrorString(e));
+    if (s == RT_OK && limit) s = fail(RT_ERR_LIMIT, "rt_trace: a traversal stack overflowed (a subtree was skipped)");
     if (tmp_r) cudaFree(tmp_r);
     if (tmp_h) cudaFree(tmp_h);
     return s;
@@ -2705,8 +2755,15 @@ extern "C" rt_status rt_render_tile_static(rt_ctx *ctx, rt_scene *sc, const rt_r
     if (rd->integrator == RT_INTEGRATOR_PATH_MIS && rd->strategy == RT_STRATEGY_ALL_LIGHTS)
         return fail(RT_ERR_UNSUPPORTED, "rt_render_tile_static: all_lights strategy is not provided by the device path");
     if (rd->max_depth < 0 || rd->min_depth < 0) return fail(RT_ERR_INVALID, "rt_render_tile_static: negative depth");
-    if (rd->max_depth > RT_STATIC_MAX_DEPTH)
+    // PathTracingMIS keeps one round counter per bounce in the scratch;
+    // VolPathTracing runs as one persistent kernel and needs one
+    if (rd->integrator == RT_INTEGRATOR_PATH_MIS && rd->max_depth > RT_STATIC_MAX_DEPTH)
         return fail(RT_ERR_LIMIT, "rt_render_tile_static: max_depth above 1024 (the static round-counter table)");
+    // every path needs well over 64 bytes of state: a larger request cannot
+    // fit, and refusing it here keeps the size arithmetic below far from
+    // overflow
+    if (rd->spp > (int)(RT_STATIC_SCRATCH_BYTES / 64))
+        return fail(RT_ERR_LIMIT, "rt_render_tile_static: spp beyond what the static scratch can hold");
     if (sc->n_lights > RT_STATIC_MAX_LIGHTS) return fail(RT_ERR_LIMIT, "rt_render_tile_static: more than 256 lights");
     const DevCamera &cam = sc->S.cam;
     if (!(cam.filter == RT_FILTER_BOX && cam.frx == 0.5f && cam.fry == 0.5f))
@@ -2722,7 +2779,25 @@ extern "C" rt_status rt_render_tile_static(rt_ctx *ctx, rt_scene *sc, const rt_r
     const int ox = tile_x * bx, oy = tile_y * by;
     const int tw = std::min(Wd, ox + bx) - ox, th = std::min(H, oy + by) - oy;
     const int64_t npix = (int64_t)tw * th, paths = npix * rd->spp;
+    if (paths > (int64_t)(RT_STATIC_SCRATCH_BYTES / 64)) {
+        char msg[256];
+        snprintf(msg, sizeof(msg),
+                 "rt_render_tile_static: a %dx%d tile at %d spp is %lld path samples; the static scratch holds "
+                 "fewer than %u (reduce spp or the block size)", tw, th, rd->spp, (long long)paths,
+                 (unsigned)(RT_STATIC_SCRATCH_BYTES / 64));
+        return fail(RT_ERR_LIMIT, msg);
+    }
     CK(cudaSetDevice(ctx->device));
+    // The call waits on its stream (round counters, the limit flag) and
+    // copies the light CDF from host memory: neither can be recorded into a
+    // graph, so a stream under capture is refused before anything is queued.
+    {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        CK(cudaStreamIsCapturing(ctx->stream, &cs));
+        if (cs != cudaStreamCaptureStatusNone)
+            return fail(RT_ERR_UNSUPPORTED, "rt_render_tile_static: the context's stream is being captured; "
+                                            "the call synchronises its stream and must run outside a capture");
+    }
     unsigned char *base = nullptr;
     rt_status s = static_scratch(ctx->device, &base);
     if (s != RT_OK) return s;
@@ -2803,6 +2878,7 @@ extern "C" rt_status rt_render_tile_static(rt_ctx *ctx, rt_scene *sc, const rt_r
     std::memset(&Pm, 0, sizeof(Pm));
     Pm.S = sc->S;
     Pm.S.light_cdf = light_cdf;
+    Pm.S.limit_flag = limit_flag;
     Pm.W = W;
     Pm.tileorder = tileorder;
     Pm.g0 = 0;
@@ -2847,7 +2923,8 @@ extern "C" rt_status rt_render_tile_static(rt_ctx *ctx, rt_scene *sc, const rt_r
             }
         }
     }
-    k_film<<<(int)((npix + 127) / 128), 128, 0, st>>>(Pm, reinterpret_cast<float4 *>(film_rgbw_device), Wd, 0);
+    k_film<<<(int)((npix + 127) / 128), 128, 0, st>>>(Pm, reinterpret_cast<float4 *>(film_rgbw_device), Wd,
+                                                      (rd->flags & RT_RENDER_ACCUMULATE) ? 1 : 0);
     if ((s = launch_check("k_film (static)")) != RT_OK) return s;
     int limit = 0;
     CK(cudaMemcpyAsync(&limit, limit_flag, sizeof(int), cudaMemcpyDeviceToHost, st));

@@ -45,6 +45,14 @@ struct Builder {
     std::vector<int> order;
     int max_leaf, n_bins;
     double c_node = 1.0;   // SAH cost of a node visit, in triangle tests
+    int depth_cap = RT_BVH_DEPTH_CAP;
+
+    static int ceil_log2(int n)
+    {
+        int k = 0;
+        while ((int64_t(1) << k) < n) k++;
+        return k;
+    }
 
     // Build subtree over order[b, e); returns nodes appended into `out`
     // (local indices) with the subtree root first.
@@ -62,6 +70,33 @@ struct Builder {
         out[self].box = box;
         int n = e - b;
         if (n <= 1) { out[self].leaf = true; out[self].first = b; out[self].count = n; return; }
+        int mid;
+        // Depth bound.  Once depth + ceil(log2 n) reaches the cap, the subtree
+        // is split at the object median along the widest centroid axis: each
+        // child then holds at most ceil(n/2) triangles, so every leaf ends at
+        // depth <= depth_cap and the traversal stacks (one entry per level)
+        // cannot overflow.  The parent of the first capped node was below the
+        // cap with more triangles, so depth + ceil(log2 n) <= depth_cap there.
+        // SAH trees of ordinary scenes never reach it; a scene whose SAH would
+        // peel one triangle per level (sizes growing geometrically) does.
+        if (depth + ceil_log2(n) >= depth_cap) {
+            if (n <= max_leaf) { out[self].leaf = true; out[self].first = b; out[self].count = n; return; }
+            int a = 0;
+            for (int k = 1; k < 3; k++)
+                if (cb.mx[k] - cb.mn[k] > cb.mx[a] - cb.mn[a]) a = k;
+            mid = b + n / 2;
+            std::nth_element(order.data() + b, order.data() + mid, order.data() + e, [&](int x, int y) {
+                float cx = cen[3 * (size_t)x + a], cy = cen[3 * (size_t)y + a];
+                return cx < cy || (cx == cy && x < y);
+            });
+            int l = (int)out.size();
+            build(b, mid, out, depth + 1, maxd);
+            int r = (int)out.size();
+            build(mid, e, out, depth + 1, maxd);
+            out[self].child[0] = l;
+            out[self].child[1] = r;
+            return;
+        }
         // binned SAH over the centroid bounds
         int best_axis = -1, best_bin = -1;
         double best_cost = INFINITY;
@@ -98,7 +133,6 @@ struct Builder {
             out[self].leaf = true; out[self].first = b; out[self].count = n;
             return;
         }
-        int mid;
         if (best_axis < 0) {
             // all centroids coincide: split the range in the middle
             mid = b + n / 2;
@@ -158,12 +192,13 @@ inline void widen(const Box &b, float scale_eps, float out[6])
 
 }  // namespace
 
-void build_bvh2(const float *tv, int n, BvhImage &img, int max_leaf, int n_bins, double c_node)
+void build_bvh2(const float *tv, int n, BvhImage &img, int max_leaf, int n_bins, double c_node, int depth_cap)
 {
     img = BvhImage();
     if (n <= 0) return;
     max_leaf = std::max(1, std::min(max_leaf, 8));
     Builder B;
+    B.depth_cap = depth_cap;
     B.tv = tv;
     B.max_leaf = max_leaf;
     B.n_bins = n_bins;
@@ -412,7 +447,7 @@ struct Collapse {
 
 }  // namespace
 
-void build_wbvh8(const float *tv, int n, WideBvhImage &img, int n_bins)
+void build_wbvh8(const float *tv, int n, WideBvhImage &img, int n_bins, int depth_cap)
 {
     img = WideBvhImage();
     if (n <= 0) return;
@@ -420,6 +455,7 @@ void build_wbvh8(const float *tv, int n, WideBvhImage &img, int n_bins)
     B.tv = tv;
     B.max_leaf = 3;
     B.n_bins = n_bins;
+    B.depth_cap = depth_cap;
     B.tb.resize(n);
     B.cen.resize(3 * (size_t)n);
     B.order.resize(n);
@@ -445,6 +481,70 @@ void build_wbvh8(const float *tv, int n, WideBvhImage &img, int n_bins)
     Collapse cl(bn, B.order, tv, seps, img);
     cl.emit(0, 0, 0);
     img.max_depth = cl.maxd;
+}
+
+bool check_bvh2(const BvhImage &img, const float *tv, int n, int *depth, std::string *why)
+{
+    auto bad = [&](const std::string &m) { if (why) *why = m; return false; };
+    if (n <= 0) { if (depth) *depth = 0; return img.n_nodes == 0 || bad("nodes for an empty scene"); }
+    if (img.n_nodes <= 0 || img.n_slots != n) return bad("node or slot count");
+    // every triangle must lie inside the boxes of all links on its path
+    struct Item { int32_t link; int depth; int parent; };   // parent: index into boxes of the link's box
+    std::vector<float> boxes;                                 // 6 floats per visited link
+    std::vector<int> up;                                      // parent box of each box
+    std::vector<Item> todo;
+    std::vector<char> seen_slot(n, 0), seen_node(img.n_nodes, 0);
+    const float *N0 = &img.nodes[0];
+    auto push_children = [&](int node, int d, int parent) {
+        const float *o = N0 + 16 * (size_t)node;
+        int32_t l[2];
+        std::memcpy(&l[0], &o[12], 4);
+        std::memcpy(&l[1], &o[13], 4);
+        const float b[2][6] = {{o[0], o[1], o[2], o[3], o[8], o[9]}, {o[4], o[5], o[6], o[7], o[10], o[11]}};
+        for (int c = 0; c < 2; c++) {
+            if (b[c][0] > b[c][1]) continue;   // empty second child of a root leaf
+            int bi = (int)up.size();
+            boxes.insert(boxes.end(), b[c], b[c] + 6);
+            up.push_back(parent);
+            todo.push_back({l[c], d + 1, bi});
+        }
+    };
+    if (img.max_depth < 0) return bad("negative depth");
+    int maxd = 0;
+    seen_node[0] = 1;
+    push_children(0, 0, -1);
+    while (!todo.empty()) {
+        Item it = todo.back();
+        todo.pop_back();
+        if (it.link >= 0) {
+            if (it.link >= img.n_nodes || seen_node[it.link]) return bad("node linked twice or out of range");
+            seen_node[it.link] = 1;
+            push_children(it.link, it.depth, it.parent);
+            continue;
+        }
+        maxd = std::max(maxd, it.depth);
+        int v = ~it.link, first = v >> 3, cnt = (v & 7) + 1;
+        if (first < 0 || first + cnt > n) return bad("leaf range out of slots");
+        for (int k = first; k < first + cnt; k++) {
+            if (seen_slot[k]) return bad("slot in two leaves");
+            seen_slot[k] = 1;
+            int32_t id;
+            std::memcpy(&id, &img.tri_slots[12 * (size_t)k + 3], 4);
+            if (id < 0 || id >= n) return bad("slot names no triangle");
+            const float *p = tv + 9 * (size_t)id;
+            for (int b = it.parent; b >= 0; b = up[b]) {
+                const float *x = &boxes[6 * (size_t)b];
+                for (int q = 0; q < 3; q++)
+                    for (int a = 0; a < 3; a++)
+                        if (!(p[3 * q + a] >= x[2 * a] && p[3 * q + a] <= x[2 * a + 1])) return bad("triangle outside a box");
+            }
+        }
+    }
+    for (int k = 0; k < n; k++) if (!seen_slot[k]) return bad("slot in no leaf");
+    for (int k = 0; k < img.n_nodes; k++) if (!seen_node[k]) return bad("unreachable node");
+    // the root leaf case reports depth 1 here (it hangs below a synthetic node)
+    if (depth) *depth = maxd;
+    return true;
 }
 
 }  // namespace rtgpu

@@ -1,9 +1,15 @@
 // rt_bvh.h -- host-side acceleration-structure build for the device tracer.
 #pragma once
 #include <cstdint>
+#include <string>
 #include <vector>
 
 namespace rtgpu {
+
+// Deepest leaf of a built tree (root at depth 0).  The BVH2 traversals keep
+// one stack entry per level plus a sentinel in 64 entries (RT_STACK), so the
+// builder bounds the depth at 62 (see Builder::build).
+#define RT_BVH_DEPTH_CAP 62
 
 // Device BVH2 image.  Each internal node is 4 float4 (64 bytes):
 //   n0 = (c0.lo.x, c0.hi.x, c0.lo.y, c0.hi.y)
@@ -47,12 +53,20 @@ struct WideBvhImage {
 // widened outward by a few ulps so the fused slab test never culls a node
 // that contains a hit the exact Moller-Trumbore test accepts.
 // c_node: the SAH cost of visiting a node, in units of one triangle test
+// depth_cap: deepest leaf level allowed (object-median splits below it)
 void build_bvh2(const float *tri_v, int n_tris, BvhImage &out, int max_leaf = 4, int n_bins = 32,
-                double c_node = 1.0);
+                double c_node = 1.0, int depth_cap = RT_BVH_DEPTH_CAP);
 
 // Binned-SAH binary tree (leaves of at most 3 triangles) collapsed into the
 // compressed 8-wide layout above, greedily opening the child of largest
 // surface area until a node has 8 children.
-void build_wbvh8(const float *tri_v, int n_tris, WideBvhImage &out, int n_bins = 32);
+void build_wbvh8(const float *tri_v, int n_tris, WideBvhImage &out, int n_bins = 32,
+                 int depth_cap = RT_BVH_DEPTH_CAP);
+
+// Structural check of a BVH2 image against its triangles: every node reached
+// once, every triangle in exactly one leaf and inside the box of every link
+// on its path.  Reports the deepest leaf below the root node (links count as
+// levels); false with a reason otherwise.
+bool check_bvh2(const BvhImage &img, const float *tri_v, int n_tris, int *depth, std::string *why);
 
 }  // namespace rtgpu

@@ -149,6 +149,9 @@ struct DevScene {
     const DevMedium *media;
     DevCamera cam;
     float bmin[3], bmax[3];
+    // set to 1 by device code that had to cut a loop or drop work (the host
+    // turns it into RT_ERR_LIMIT); filled in per launch, null in none
+    int *limit_flag;
 };
 
 // ------------------------------------------------------------------ rays / hits
@@ -344,6 +347,7 @@ __device__ __forceinline__ bool trace_ray(const DevScene &S, V3 o, V3 d, float m
                     int nearc = cc.x, farc = cc.y;
                     if (c1min < c0min) { nearc = cc.y; farc = cc.x; }
                     if (sp < RT_STACK) stack[sp++] = farc;
+                    else if (S.limit_flag) atomicExch(S.limit_flag, 1);   // unreachable: the build bounds the depth
                     node = nearc;
                 } else {
                     node = t0 ? cc.x : cc.y;

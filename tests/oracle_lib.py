@@ -31,6 +31,8 @@ def lib():
         L.oracle_render.argtypes = [C.c_void_p, C.POINTER(D.RenderDesc), C.c_void_p, C.c_int32]
         L.oracle_render_tiles.argtypes = [C.c_void_p, C.POINTER(D.RenderDesc), C.c_int32, C.c_int32, C.c_void_p,
                                           C.c_int32]
+        L.oracle_render_tiles_strided.argtypes = [C.c_void_p, C.POINTER(D.RenderDesc), C.c_int32, C.c_int32,
+                                                  C.c_int32, C.c_void_p, C.c_int32]
         L.oracle_render_paths.argtypes = [C.c_void_p, C.POINTER(D.RenderDesc), C.c_void_p, C.c_void_p,
                                           C.c_int32, C.c_void_p]
         L.oracle_trace.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_void_p]
@@ -85,6 +87,17 @@ class OracleScene:
         film = np.zeros((H, W, 4), np.float32)
         th = threads or os.cpu_count() or 1
         rc = lib().oracle_render_tiles(self.h, C.byref(rd), tile0, tile1, _p(film), th)
+        assert rc == 0
+        return film
+
+    def render_tiles_strided(self, spp, tile0, count, stride, seed=0, threads=None, **over):
+        """Tiles tile0, tile0 + stride, ... (count of them): a sample of the
+        job grid spread over the whole frame."""
+        rd = self.scene.render_desc(spp, seed=seed, **over)
+        W, H = self.scene.camera["width"], self.scene.camera["height"]
+        film = np.zeros((H, W, 4), np.float32)
+        th = threads or os.cpu_count() or 1
+        rc = lib().oracle_render_tiles_strided(self.h, C.byref(rd), tile0, count, stride, _p(film), th)
         assert rc == 0
         return film
 

@@ -1,0 +1,78 @@
+"""The device tree's depth stays within the traversal stacks (no GPU needed).
+
+The reference's traversal keeps a fixed stack of 64 entries
+(accelStruct/Bvh.cpp:402) and would write past it on a tree deeper than
+that.  The device traversals keep a sentinel plus one entry per level in 64
+entries (RT_STACK), so the builder bounds the depth: wherever the SAH tree
+would grow past the cap it splits at the object median.  rt_bvh_stats builds
+the tree on the host exactly as rt_scene_create does, checks it structurally
+(every triangle in one leaf, inside every box on its path) and reports the
+deepest leaf.
+"""
+import numpy as np
+import pytest
+
+from raytracer_gb300 import core
+
+
+def geometric_strip(n, ratio):
+    """n triangles along +x, triangle i at x = ratio^i with size 0.1 x: the
+    SAH peels off a few of the largest per level, so the tree grows deep."""
+    x = ratio ** np.arange(n, dtype=np.float64)
+    s = 0.1 * x
+    t = np.zeros((n, 3, 3))
+    t[:, 0, 0] = x
+    t[:, 1, 0] = x + s
+    t[:, 2, 0] = x
+    t[:, 2, 1] = s
+    t[:, 2, 2] = 0.5 * s
+    return t.astype(np.float32)
+
+
+def random_soup(n, seed):
+    rng = np.random.default_rng(seed)
+    c = rng.random((n, 1, 3)) * 10.0
+    return (c + rng.normal(scale=0.05, size=(n, 3, 3))).astype(np.float32)
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from raytracer_gb300 import build
+    build.build()
+    return core.lib()
+
+
+def test_default_cap_on_deep_sah_tree(lib):
+    t = geometric_strip(60, 2.0)
+    d, nodes = core.bvh_stats(t)
+    assert 12 < d <= 62 and nodes == 59
+    d8, _ = core.bvh_stats(t, width=8)
+    assert d8 <= d
+
+
+@pytest.mark.parametrize("cap", [8, 12, 20])
+def test_reduced_cap_bounds_the_depth(lib, cap):
+    t = geometric_strip(60, 2.0)
+    free, _ = core.bvh_stats(t)
+    assert free > cap                      # the SAH tree alone is deeper
+    # capped; rt_bvh_stats has checked that every triangle is in one leaf
+    d, nodes = core.bvh_stats(t, depth_cap=cap)
+    assert d <= cap and 0 < nodes <= 59
+    d8, _ = core.bvh_stats(t, width=8, depth_cap=cap)
+    assert d8 <= cap
+
+
+def test_cap_on_a_large_soup(lib):
+    t = random_soup(20000, 3)
+    free, _ = core.bvh_stats(t)
+    d, _ = core.bvh_stats(t, depth_cap=16)   # 2^16 >= 20000 triangles
+    assert d <= 16 <= free + 16
+
+
+def test_bad_caps_are_refused(lib):
+    t = random_soup(100, 1)
+    with pytest.raises(core.RtError):
+        core.bvh_stats(t, depth_cap=5)        # 2^5 < 100 triangles
+    with pytest.raises(core.RtError):
+        core.bvh_stats(t, depth_cap=63)       # beyond the stack
+    assert core.bvh_stats(np.zeros((0, 3, 3), np.float32)) == (0, 0)

@@ -3,9 +3,8 @@
 rt_render_tile_static serves callers that cannot allocate device memory
 while they render (plugins whose host application owns the device memory
 through its own pool under a hard budget, real-time loops that forbid
-cudaMalloc/cudaFree after start-up, work issued while another component
-captures the stream).  Its path state lives in a static device array shared
-by every call.  This test renders tiles through it on two calls in a row and
+cudaMalloc/cudaFree after start-up).  Its path state lives in a static
+device array shared by every call.  This test renders tiles through it on two calls in a row and
 checks each against the same pixels of an ordinary rt_render film: the same
 kernels run on the same per-path sample streams, so the tolerance is the
 parity tests' 1e-5 relative and, in practice, bitwise equality.
@@ -88,3 +87,52 @@ def test_static_tile_render_refuses_textured_scenes(ctx, rtlib):
             g.render_tile_static(0, 0, film.data_ptr(), 2, seed=1, block=32)
         assert e.value.status == 5
         g.close()
+
+
+def test_static_tile_render_accumulates_sample_ranges(ctx, rtlib):
+    """With RT_RENDER_ACCUMULATE, samples [0, 2) and then [2, 4) rendered
+    into one tile sum to the 4-spp rt_render tile (weights exactly; rgb to
+    the parity tolerance, the two partial sums being added in another
+    order)."""
+    torch = pytest.importorskip("torch")
+    s = scenes.cornell_box(64, 48)
+    block, tile = 32, (1, 0)
+    g = rtlib.Scene(ctx, s)
+    ref = g.render(4, seed=5, block=block)
+    film = torch.zeros((48, 64, 4), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    g.render_tile_static(*tile, film.data_ptr(), 2, seed=5, sample_begin=0, block=block, accumulate=True)
+    g.render_tile_static(*tile, film.data_ptr(), 2, seed=5, sample_begin=2, block=block, accumulate=True)
+    torch.cuda.synchronize()
+    ys, xs = _tile_box(s, *tile, block)
+    a, b = film.cpu().numpy()[ys, xs], ref[ys, xs]
+    assert np.array_equal(a[..., 3], b[..., 3])
+    np.testing.assert_allclose(a[..., :3], b[..., :3], rtol=1e-5, atol=1e-6)
+    g.close()
+
+
+def test_static_tile_render_refuses_a_capturing_stream(rtlib):
+    """The call synchronises its stream, so on a stream under capture it
+    returns RT_ERR_UNSUPPORTED before it queues anything; the capture itself
+    stays valid."""
+    torch = pytest.importorskip("torch")
+    ctx2 = rtlib.Context(0)
+    stream = torch.cuda.Stream()
+    ctx2.set_stream(stream.cuda_stream)
+    s = scenes.cornell_box(32, 32)
+    g = rtlib.Scene(ctx2, s)
+    film = torch.zeros((32, 32, 4), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=stream):
+        with pytest.raises(rtlib.RtError) as e:
+            g.render_tile_static(0, 0, film.data_ptr(), 1, seed=0, block=32)
+        film.add_(1.0)
+    assert e.value.status == 5 and "captur" in str(e.value)
+    graph.replay()
+    torch.cuda.synchronize()
+    assert float(film[0, 0, 0]) == 1.0
+    g.render_tile_static(0, 0, film.data_ptr(), 1, seed=0, block=32)   # fine outside the capture
+    torch.cuda.synchronize()
+    g.close()
+    ctx2.close()
