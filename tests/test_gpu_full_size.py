@@ -1,0 +1,206 @@
+"""GPU parity at the benchmark configurations' full sizes.
+
+The miniature scenes of test_gpu_parity.py cover every code path; these
+tests run the configurations themselves:
+
+* Cornell box (10 + 12 + 12 + 2 triangles), 256x256, 16 spp, depth 8:
+  the whole film against the CPU oracle on identical per-path streams;
+* displaced icosphere, level 8 (1,310,720 triangles + a 2-triangle ground),
+  sky map, 1024x1024, 64 spp, depth 16: closest-hit and any-hit parity of
+  camera and secondary rays on the full tree (binary and 8-wide), and three
+  fixed 64x64 crops of the full-size frame against the oracle;
+* 128^3 fBm grid medium + slab + sphere light, 512x512, 128 spp, depth 64
+  (VolPathTracing): three fixed 64x64 crops against the oracle;
+* 4096-spp converged crops of both large scenes against committed 4096-spp
+  CPU renders with independent sample streams (tests/golden/make_converged.py).
+
+Tolerances are stated per test.  Ray casting: identical hit/miss, identical
+triangle index except for hits at exactly the same distance (a shared edge,
+where the reference's own answer depends on its visit order), distance and
+barycentrics within 2 ulp.  Films: weights bitwise equal; rgb per pixel
+within 1e-3 relative except for the stated fraction of pixels, where a path
+took another branch after a last-ulp difference in a transcendental
+function (CUDA's and the C library's expf/logf/sinf/powf differ by a few
+ulp).
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle_lib as O
+from raytracer_gb300 import desc as D, scenes
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LUM = np.array([0.2126, 0.7152, 0.0722])
+
+
+def _ulp_diff(a, b):
+    a = np.asarray(a, np.float32).view(np.int32).astype(np.int64)
+    b = np.asarray(b, np.float32).view(np.int32).astype(np.int64)
+    a = np.where(a < 0, np.int64(-2 ** 31) - a, a)
+    b = np.where(b < 0, np.int64(-2 ** 31) - b, b)
+    return np.abs(a - b)
+
+
+@pytest.fixture(scope="module")
+def ico_full():
+    s = scenes.displaced_icosphere()
+    return s, O.OracleScene(s)
+
+
+@pytest.fixture(scope="module")
+def vol_full():
+    s = scenes.volume_grid()
+    return s, O.OracleScene(s)
+
+
+def _width(ctx, w):
+    ctx.set_bvh_width(w)
+
+
+@pytest.mark.parametrize("w", [2, 8], ids=["bvh2", "bvh8"])
+def test_full_tree_trace_parity(ctx, rtlib, ico_full, w):
+    """131,072 camera rays plus 131,072 secondary rays leaving the camera
+    rays' hit points (uniform directions, the reference's adaptive epsilon)
+    on the 1.31M-triangle tree."""
+    s, o = ico_full
+    rng = np.random.default_rng(11)
+    W, H = s.camera["width"], s.camera["height"]
+    n = 1 << 17
+    cam = o.camera_rays(rng.random((n, 2)) * [W, H])
+    hc = o.trace(cam)
+    m = hc["prim"] >= 0
+    p = cam["o"][m] + cam["d"][m] * hc["t"][m][:, None]
+    d = rng.normal(size=(len(p), 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    sec = np.zeros(len(p), D.RAY_DTYPE)
+    sec["o"], sec["d"], sec["mint"], sec["maxt"] = p, d, 1e-4, 1e8
+    rays = np.concatenate([cam, sec])
+    g = rtlib.Scene(ctx, s)
+    _width(ctx, w)
+    try:
+        hg = g.trace(rays)
+        ag = g.trace(rays, anyhit=True)
+    finally:
+        _width(ctx, 2)
+        g.close()
+    ho = o.trace(rays)
+    ao = o.trace(rays, anyhit=True)
+    hit_g, hit_o = hg["prim"] != -1, ho["prim"] != -1
+    assert np.array_equal(hit_g, hit_o)
+    both = hit_g & hit_o
+    same = both & (hg["prim"] == ho["prim"])
+    tied = both & ~same
+    assert np.all(hg["t"][tied] == ho["t"][tied]), "another triangle at another distance"
+    ut, uu, uv = (_ulp_diff(hg[k][same], ho[k][same]).max(initial=0) for k in ("t", "u", "v"))
+    print("bvh%d: %d rays, %d hits, %d ties at equal distance, max ulp t %d u %d v %d" %
+          (w, len(rays), both.sum(), tied.sum(), ut, uu, uv))
+    assert len(rays) >= 200000 and both.sum() > 100000
+    assert ut <= 2 and uu <= 2 and uv <= 2
+    assert tied.sum() <= 1e-4 * both.sum()
+    assert np.array_equal(ag["prim"] == 0, ao["prim"] == 0)
+
+
+def _compare(fg, fo, max_bad, label):
+    assert np.array_equal(fg[..., 3], fo[..., 3]), "film weights differ"
+    a, b = fg[..., :3].astype(np.float64), fo[..., :3].astype(np.float64)
+    err = (np.abs(a - b) / np.maximum(np.abs(b), 1e-3)).max(-1)
+    bad = float(np.mean(err > 1e-3))
+    print("%s: %d pixels, bit-identical %.4f, >1e-3 rel %.4f, median rel %.1e, sum ratio %.7f" %
+          (label, err.size, np.mean(err == 0), bad, np.median(err), a.sum() / max(b.sum(), 1e-30)))
+    assert bad <= max_bad
+    return bad
+
+
+def test_full_cornell_film(ctx, rtlib):
+    """The whole 256x256, 16-spp Cornell-box film.  Measured: 0 pixels off
+    by more than 1e-3; stated tolerance 0.1%."""
+    s = scenes.cornell_box()
+    g = rtlib.Scene(ctx, s)
+    fg = g.render(16, seed=0)
+    g.close()
+    fo = O.OracleScene(s).render(16, seed=0)
+    _compare(fg, fo, 0.001, "cornell 256x256 16spp")
+
+
+def _crop_tiles(o, spp, tiles, tiles_x, seed):
+    """Oracle film of the given (tx, ty) tiles only (box filter: tiles do
+    not overlap, so the single-tile films add up exactly)."""
+    film = None
+    for tx, ty in tiles:
+        t = ty * tiles_x + tx
+        f = o.render_tiles(spp, t, t + 1, seed=seed)
+        film = f if film is None else film + f
+    return film
+
+
+def _crops(s, o, fg, crops, spp, seed, max_bad):
+    tiles_x = (s.camera["width"] + 31) // 32
+    for name, (tx, ty) in crops.items():
+        tiles = [(tx, ty), (tx + 1, ty), (tx, ty + 1), (tx + 1, ty + 1)]
+        fo = _crop_tiles(o, spp, tiles, tiles_x, seed)
+        ys, xs = slice(ty * 32, ty * 32 + 64), slice(tx * 32, tx * 32 + 64)
+        _compare(fg[ys, xs], fo[ys, xs], max_bad, "%s %s crop" % (s.name, name))
+
+
+def test_full_icosphere_crops(ctx, rtlib, ico_full):
+    """Three 64x64 crops (object centre, silhouette, horizon) of the full
+    1024x1024, 64-spp, depth-16 frame rendered on the GPU, against the oracle
+    rendering the same tiles.  Stated tolerance: 1% of pixels off by more
+    than 1e-3."""
+    s, o = ico_full
+    g = rtlib.Scene(ctx, s)
+    fg = g.render(64, seed=0)
+    g.close()
+    _crops(s, o, fg, {"centre": (15, 15), "silhouette": (7, 12), "horizon": (2, 11)}, 64, 0, 0.01)
+
+
+def test_full_volume_crops(ctx, rtlib, vol_full):
+    """Three 64x64 crops (grid centre, grid/slab edge, slab) of the full
+    512x512, 128-spp, depth-64 VolPathTracing frame against the oracle.
+    Stated tolerance: 1% of pixels off by more than 1e-3."""
+    s, o = vol_full
+    g = rtlib.Scene(ctx, s)
+    fg = g.render(128, seed=0)
+    g.close()
+    _crops(s, o, fg, {"grid": (7, 6), "edge": (4, 9), "slab": (7, 12)}, 128, 0, 0.01)
+
+
+def _luminance(film):
+    from raytracer_gb300 import post_process
+    return post_process(film).astype(np.float64) @ LUM
+
+
+@pytest.mark.parametrize("which", ["icosphere", "volume"])
+def test_converged_4096spp_crops(ctx, rtlib, ico_full, vol_full, which):
+    """A 4096-spp GPU render (its own sample streams) against 4096-spp CPU
+    renders of fixed 32x32 tiles (tests/golden/converged_4096spp.npz, seeds
+    4242 and 4343).  Per-pixel relative difference of luminance is
+    Monte-Carlo noise; the two CPU renders measure its size.  Stated
+    tolerance per crop: the GPU-vs-CPU difference at the median and at the
+    90th percentile at most 1.3x the CPU-vs-CPU difference plus 0.5%, and the
+    crop means within 3x the CPU-vs-CPU mean difference plus 0.5%."""
+    gold = np.load(os.path.join(HERE, "golden", "converged_4096spp.npz"))
+    s, _ = ico_full if which == "icosphere" else vol_full
+    g = rtlib.Scene(ctx, s)
+    fg = g.render(4096, seed=777)
+    g.close()
+    keys = sorted({k[:-2] for k in gold.files if k.startswith(which)})
+    assert keys
+    for key in keys:
+        tx, ty = (int(v) for v in key.split("_")[1:3])
+        la, lb = _luminance(gold[key + "_a"]), _luminance(gold[key + "_b"])
+        lg = _luminance(fg[ty * 32:(ty + 1) * 32, tx * 32:(tx + 1) * 32])
+        rel_gc = np.abs(lg - la) / np.maximum(la, 1e-3)
+        rel_cc = np.abs(lb - la) / np.maximum(la, 1e-3)
+        mean_gc = abs(lg.mean() / la.mean() - 1)
+        mean_cc = abs(lb.mean() / la.mean() - 1)
+        print("%s: GPU-CPU p50 %.4f p90 %.4f mean %.4f | CPU-CPU p50 %.4f p90 %.4f mean %.4f" %
+              (key, np.median(rel_gc), np.percentile(rel_gc, 90), mean_gc,
+               np.median(rel_cc), np.percentile(rel_cc, 90), mean_cc))
+        assert np.median(rel_gc) <= 1.3 * np.median(rel_cc) + 0.005
+        assert np.percentile(rel_gc, 90) <= 1.3 * np.percentile(rel_cc, 90) + 0.005
+        assert mean_gc <= 3 * mean_cc + 0.005
