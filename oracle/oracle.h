@@ -248,6 +248,14 @@ int32_t oracle_light_query(const o_scene *sc, int32_t light, const rt_light_q *q
  * drawing from the path stream (seed, pixel, sample) (rt_medium_query). */
 int32_t oracle_medium_query(const o_scene *sc, int32_t medium, int32_t op, const rt_medium_q *q, int32_t n,
                             rt_medium_r *r);
+/* pin hooks: single functions of the restatement, for comparison with the
+ * reference's own (oracle_core.c, oracle_bvh.c) */
+int32_t oracle_tri_query(const float *tri_v, const rt_ray *rays, int32_t n, rt_hit *hits);
+int32_t oracle_fresnel_query(int32_t op, const float *in, int32_t n, float *out);
+int32_t oracle_mapping_query(int32_t op, const float *u, int32_t n, float *out);
+int32_t oracle_microfacet_query(int32_t type, int32_t op, float alpha, const float *in, int32_t n, float *out);
+int32_t oracle_phase_query(float g, int32_t op, const float *in, int32_t n, float *out);
+int32_t oracle_env_sphere(const o_scene *sc, int32_t light, float *out4);
 void oracle_pcg_stream(uint64_t initstate, uint64_t initseq, int32_t n, uint32_t *out);
 void oracle_cdf_sample_reuse(const float *pdfs, int32_t n, const float *u, int32_t m,
                              int32_t *index, float *u_out, float *pdf_out, float *sum_out);

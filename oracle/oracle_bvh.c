@@ -365,10 +365,8 @@ o_bvh *o_bvh_build_scene(const o_scene *sc)
 typedef struct { float t, u, v; int prim; v3 p; } o_rec;
 
 /* Triangle::intersection (Triangle.cpp:46-88) */
-static int tri_hit(const rt_scene_desc *d, int tri, const o_ray *r, float *t, float *u, float *v)
+static int tri_hit_p(v3 p0, v3 p1, v3 p2, const o_ray *r, float *t, float *u, float *v)
 {
-    v3 p0, p1, p2;
-    tri_verts(d, tri, &p0, &p1, &p2);
     v3 e1 = v3_sub(p1, p0), e2 = v3_sub(p2, p0), s = v3_sub(r->o, p0);
     v3 s1 = v3_cross(r->d, e2), s2 = v3_cross(s, e1);
     float det = v3_dot(s1, e1);
@@ -382,6 +380,35 @@ static int tri_hit(const rt_scene_desc *d, int tri, const o_ray *r, float *t, fl
     if (tt < r->mint || tt > r->maxt) return 0;
     *t = tt; *u = b1; *v = b2;
     return 1;
+}
+static int tri_hit(const rt_scene_desc *d, int tri, const o_ray *r, float *t, float *u, float *v)
+{
+    v3 p0, p1, p2;
+    tri_verts(d, tri, &p0, &p1, &p2);
+    return tri_hit_p(p0, p1, p2, r, t, u, v);
+}
+
+/* Pin hook: Triangle::intersection of each ray against the triangle tri_v
+ * (9 floats), with the ray's own [mint, maxt] (no adaptive epsilon: that is
+ * the BVH's, Bvh.cpp:411-413).  hits: t, u, v, prim 0 on a hit, -1 else. */
+int32_t oracle_tri_query(const float *tri_v, const rt_ray *rays, int32_t n, rt_hit *hits)
+{
+    v3 p0 = mk3(tri_v[0], tri_v[1], tri_v[2]), p1 = mk3(tri_v[3], tri_v[4], tri_v[5]);
+    v3 p2 = mk3(tri_v[6], tri_v[7], tri_v[8]);
+    for (int i = 0; i < n; i++) {
+        o_ray r;
+        r.o = mk3(rays[i].o[0], rays[i].o[1], rays[i].o[2]);
+        r.d = mk3(rays[i].d[0], rays[i].d[1], rays[i].d[2]);
+        r.mint = rays[i].mint;
+        r.maxt = rays[i].maxt;
+        float t = 0, u = 0, v = 0;
+        memset(&hits[i], 0, sizeof(hits[i]));
+        hits[i].prim = -1;
+        if (tri_hit_p(p0, p1, p2, &r, &t, &u, &v)) {
+            hits[i].t = t; hits[i].u = u; hits[i].v = v; hits[i].prim = 0;
+        }
+    }
+    return RT_OK;
 }
 
 /* Sphere::intersection (Sphere.cpp:38-111) */

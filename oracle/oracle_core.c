@@ -1532,3 +1532,92 @@ c3 o_medium_transmittance(const o_scene *sc, int mi, const o_ray *ray, o_sampler
     if (m->type == RT_MEDIUM_HETEROGENEOUS) return o_hetero_tr(sc, mi, ray, s);
     return o_homog_tr(m, ray->mint, ray->maxt);
 }
+
+/* ===================== pin hooks =====================
+ * Direct entry points over the restated Fresnel, warp, microfacet and phase
+ * functions, so that each can be compared one to one with the reference's
+ * own function on the same inputs (tests/test_oracle_pins.py).  Test
+ * infrastructure, like the rest of this file. */
+
+/* op 0: fresnelConductor for one channel (Fresnel.h:30-49), in (eta, k, cosI);
+ * op 1: fresnelDielectric (Fresnel.h:51-63), in (etaI, etaT, cosI, cosT);
+ * op 2: estimateDielectric (Fresnel.h:83-114), in (etaExt, etaInt, cosI),
+ *       out (reflectance, etaI, etaT, relativeEta, cosThetaT).
+ * Each query reads 4 floats and writes 5. */
+int32_t oracle_fresnel_query(int32_t op, const float *in, int32_t n, float *out)
+{
+    for (int i = 0; i < n; i++) {
+        const float *a = in + 4 * i;
+        float *o = out + 5 * i;
+        o[0] = o[1] = o[2] = o[3] = o[4] = 0.f;
+        if (op == 0) o[0] = o_fresnel_conductor1(a[0], a[1], a[2]);
+        else if (op == 1) o[0] = o_fresnel_dielectric(a[0], a[1], a[2], a[3]);
+        else if (op == 2) {
+            float f = o_estimate_dielectric(a[0], a[1], a[2], &o[1], &o[2], &o[3], &o[4]);
+            o[0] = f;
+        } else return RT_ERR_INVALID;
+    }
+    return RT_OK;
+}
+
+/* Warps of core/Mapping.h for 2-D samples u (2 floats each), 3 floats out:
+ * op 0 squareToConcentricDisk (x, y, 0), 1 squareToCosineWeightedHemisphere,
+ * 2 squareToTriangle (barycentrics), 3 squareToUniformSphere. */
+int32_t oracle_mapping_query(int32_t op, const float *u, int32_t n, float *out)
+{
+    for (int i = 0; i < n; i++) {
+        v2 s = mk2(u[2 * i], u[2 * i + 1]);
+        v3 r;
+        if (op == 0) { v2 d = o_square_to_concentric_disk(s); r = mk3(d.x, d.y, 0.f); }
+        else if (op == 1) r = o_square_to_cosine_hemisphere(s);
+        else if (op == 2) r = o_square_to_triangle(s);
+        else if (op == 3) r = o_square_to_uniform_sphere(s);
+        else return RT_ERR_INVALID;
+        out[3 * i] = r.x; out[3 * i + 1] = r.y; out[3 * i + 2] = r.z;
+    }
+    return RT_OK;
+}
+
+/* MicrofacetDistribution (bsdf/MicrofacetDistribution.cpp) of `type` at
+ * `alpha`, 9 floats in and 3 out per query: op 0 D(wh) (in wh), op 1
+ * G(wi, wo, wh) (in wi, wo, wh), op 2 sampleNormal(u) (in u). */
+int32_t oracle_microfacet_query(int32_t type, int32_t op, float alpha, const float *in, int32_t n, float *out)
+{
+    for (int i = 0; i < n; i++) {
+        const float *a = in + 9 * i;
+        float *o = out + 3 * i;
+        o[0] = o[1] = o[2] = 0.f;
+        if (op == 0) o[0] = o_mf_D(type, mk3(a[0], a[1], a[2]), alpha);
+        else if (op == 1) o[0] = o_mf_G(type, mk3(a[0], a[1], a[2]), mk3(a[3], a[4], a[5]), mk3(a[6], a[7], a[8]), alpha);
+        else if (op == 2) {
+            v3 m = o_mf_sample_normal(type, mk2(a[0], a[1]), alpha);
+            o[0] = m.x; o[1] = m.y; o[2] = m.z;
+        } else return RT_ERR_INVALID;
+    }
+    return RT_OK;
+}
+
+/* Henyey-Greenstein phase function (medium/HGPhaseFunction.cpp) with
+ * asymmetry g, 6 floats in and 5 out per query: op 0 eval (in wi, wo; out
+ * value), op 1 sample (in wi, u; out wo, pdf, weight). */
+int32_t oracle_phase_query(float g, int32_t op, const float *in, int32_t n, float *out)
+{
+    rt_medium_desc m;
+    memset(&m, 0, sizeof(m));
+    m.phase = RT_PHASE_HG;
+    m.g = g;
+    for (int i = 0; i < n; i++) {
+        const float *a = in + 6 * i;
+        float *o = out + 5 * i;
+        o[0] = o[1] = o[2] = o[3] = o[4] = 0.f;
+        v3 wi = mk3(a[0], a[1], a[2]);
+        if (op == 0) o[0] = o_phase_eval(&m, wi, mk3(a[3], a[4], a[5]));
+        else if (op == 1) {
+            v3 wo;
+            float pdf;
+            float w = o_phase_sample(&m, wi, mk2(a[3], a[4]), &wo, &pdf);
+            o[0] = wo.x; o[1] = wo.y; o[2] = wo.z; o[3] = pdf; o[4] = w;
+        } else return RT_ERR_INVALID;
+    }
+    return RT_OK;
+}

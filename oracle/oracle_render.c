@@ -268,6 +268,17 @@ o_scene *oracle_scene_create(const rt_scene_desc *d, int32_t strategy)
     return sc;
 }
 
+/* Pin hook: the bounding sphere (centre, radius) that
+ * EnvironmentLight::initialize (EnvironmentLight.cpp:256-262) gives light
+ * `light` from the scene box. */
+int32_t oracle_env_sphere(const o_scene *sc, int32_t light, float *out4)
+{
+    if (light < 0 || light >= sc->d->n_lights || sc->d->lights[light].type != RT_LIGHT_ENV) return RT_ERR_INVALID;
+    const o_env_rt *E = &sc->env[light];
+    out4[0] = E->center.x; out4[1] = E->center.y; out4[2] = E->center.z; out4[3] = E->sphere_radius;
+    return RT_OK;
+}
+
 void oracle_scene_destroy(o_scene *sc)
 {
     if (!sc) return;

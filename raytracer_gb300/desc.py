@@ -205,6 +205,30 @@ def bsdf(kind, **kw):
 TEX_PARAMS = ("tex_albedo", "tex_reflectance", "tex_transmittance", "tex_alpha")
 
 
+def medium_struct(m, keep):
+    """rt_medium_desc of a medium dict (its density grid, if any, appended to
+    `keep`, which must outlive the struct)."""
+    M = MediumDesc()
+    M.type = m["type"]
+    M.phase = m.get("phase", PHASE_ISOTROPIC)
+    M.g = m.get("g", -0.8)
+    M.sigma_a = f3(*m.get("sigma_a", (0.15, 0.15, 0.15)))
+    M.sigma_s = f3(*m.get("sigma_s", (0.15, 0.15, 0.15)))
+    M.scale = m.get("scale", 1.0)
+    M.albedo = f3(*m.get("albedo", (0.0, 0.0, 0.0)))
+    dens = m.get("density")
+    if dens is not None:
+        dens = np.ascontiguousarray(dens, np.float32)
+        keep.append(dens)
+        M.res = i3(dens.shape[2], dens.shape[1], dens.shape[0])
+        M.density = _fp(dens)
+        M.grid_min = f3(*m.get("grid_min", (0, 0, 0)))
+        M.grid_max = f3(*m.get("grid_max", (1, 1, 1)))
+    M.to_world = mat(m.get("to_world", IDENTITY))
+    M.centered = int(m.get("centered", 1))
+    return M
+
+
 def bsdf_struct(b):
     """rt_bsdf_desc of a bsdf() dict."""
     return BsdfDesc(b["type"], b["distribution"], f3(*b["albedo"]), f3(*b["reflectance"]),
@@ -410,24 +434,7 @@ class SceneData:
 
         ms = (MediumDesc * max(1, len(self.media)))()
         for i, m in enumerate(self.media):
-            M = MediumDesc()
-            M.type = m["type"]
-            M.phase = m.get("phase", PHASE_ISOTROPIC)
-            M.g = m.get("g", -0.8)
-            M.sigma_a = f3(*m.get("sigma_a", (0.15, 0.15, 0.15)))
-            M.sigma_s = f3(*m.get("sigma_s", (0.15, 0.15, 0.15)))
-            M.scale = m.get("scale", 1.0)
-            M.albedo = f3(*m.get("albedo", (0.0, 0.0, 0.0)))
-            dens = m.get("density")
-            if dens is not None:
-                keep.append(dens)
-                M.res = i3(dens.shape[2], dens.shape[1], dens.shape[0])
-                M.density = _fp(dens)
-                M.grid_min = f3(*m.get("grid_min", (0, 0, 0)))
-                M.grid_max = f3(*m.get("grid_max", (1, 1, 1)))
-            M.to_world = mat(m.get("to_world", IDENTITY))
-            M.centered = int(m.get("centered", 1))
-            ms[i] = M
+            ms[i] = medium_struct(m, keep)
         D.n_media = len(self.media)
         D.media = C.cast(ms, C.POINTER(MediumDesc))
 

@@ -104,10 +104,7 @@ def spectrum_to_rgb(lam, val, cie):
     return tuple(float(max(F(0), F(c))) for c in (r, g, b))
 
 
-REFERENCE_ROOT = "/root/reference/RaytracerNew2"
-
-
-def compute(ref_root=REFERENCE_ROOT):
+def compute(ref_root):
     """{name: (eta rgb, k rgb)} from the reference tree."""
     src = open(os.path.join(ref_root, "src", "core", "Color.cpp"), encoding="latin-1").read()
     cie = (_table(src, "CIE_lambda"), _table(src, "CIE_X"), _table(src, "CIE_Y"), _table(src, "CIE_Z"))
@@ -134,4 +131,8 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else REFERENCE_ROOT)
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("RT_REFERENCE_ROOT")
+    if not root or not os.path.isdir(os.path.join(root, "data", "IOR")):
+        raise SystemExit("usage: make_conductor_ior.py <reference>/RaytracerNew2 "
+                         "(or set RT_REFERENCE_ROOT): the directory holding src/ and data/IOR/")
+    main(root)

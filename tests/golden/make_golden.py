@@ -1,13 +1,21 @@
 """Generate the golden fixtures that pin the CPU oracle to the reference.
 
-The reference's own tools/Rng.h (PCG32) and core/CDF.{h,cpp} are compiled in
-place by oracle/build_oracle.py (libref_pin.so); this script runs them on
-seeded inputs and writes small JSON fixtures next to itself:
+oracle/build_oracle.py compiles the reference's own sources in place:
+tools/Rng.h (PCG32) and core/CDF.{h,cpp} into libref_pin.so, and the
+hot-path sources (triangle test, warps, Fresnel, microfacet distributions,
+Diffuse / RoughConductor / RoughDielectric / SmoothLayeredBSDF, mesh, sphere
+and environment lights, HG phase function, homogeneous and grid media) into
+libref_hot.so.  This script runs them on seeded inputs and writes the
+fixtures next to itself:
 
 * pcg32_ref.json  -- raw 32-bit outputs and mantissa floats of Rng streams
 * cdf_ref.json    -- CDF::sampleAndReuse / CDF::sample on seeded pdf lists
+* ref_hot.npz     -- the queries of tests/pin_cases.py with the reference's
+                     answers
 
-Run from the repository root:  python tests/golden/make_golden.py
+Run from the repository root, naming the reference's RaytracerNew2/src:
+    python tests/golden/make_golden.py <reference>/RaytracerNew2/src
+(or set RT_REFERENCE_SRC).
 """
 import ctypes as C
 import json
@@ -21,11 +29,14 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 import build_oracle  # noqa: E402
 
+PIN_QUERIES = 1024   # queries per family in ref_hot.npz
+
 
 def main():
-    path = build_oracle.build_ref_pin(force=True)
-    if path is None:
-        raise SystemExit("reference sources not present; fixtures cannot be regenerated here")
+    ref = sys.argv[1] if len(sys.argv) > 1 else None
+    if build_oracle.reference_src(ref) is None:
+        raise SystemExit("name the reference's RaytracerNew2/src directory (argument or RT_REFERENCE_SRC)")
+    path = build_oracle.build_ref_pin(force=True, ref_src=ref)
     L = C.CDLL(path)
     L.ref_pcg_stream.argtypes = [C.c_uint64, C.c_uint64, C.c_int, C.c_void_p]
     L.ref_pcg_reals.argtypes = [C.c_uint64, C.c_uint64, C.c_int, C.c_void_p]
@@ -75,6 +86,15 @@ def main():
     json.dump(dict(source="RaytracerNew2/src/core/CDF.h + CDF.cpp compiled in place", cases=cases),
               open(os.path.join(HERE, "cdf_ref.json"), "w"))
     print("wrote", os.path.join(HERE, "pcg32_ref.json"), os.path.join(HERE, "cdf_ref.json"))
+    hot = build_oracle.build_ref_hot(force=True, ref_src=ref)
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    sys.path.insert(0, ROOT)
+    import pin_cases
+    inp = pin_cases.inputs(n=PIN_QUERIES)
+    out = pin_cases.run(C.CDLL(hot), inp)
+    np.savez_compressed(os.path.join(HERE, "ref_hot.npz"),
+                        **{"in_" + k: v for k, v in inp.items()}, **{"out_" + k: v for k, v in out.items()})
+    print("wrote", os.path.join(HERE, "ref_hot.npz"))
 
 
 if __name__ == "__main__":
