@@ -7,7 +7,8 @@ infrastructure only).
   compiled in place with oracle/ref_shim.h force-included, into oracle/_ref/.
 * libref_hot.so -- the reference's own hot-path sources (triangle test,
   BSDFs, Fresnel, warps, microfacet distributions, lights, media, phase
-  function; REF_HOT_SOURCES below) compiled in place against the
+  function, and for whole renders the integrators, the scene with its BVH
+  and the camera; REF_HOT_SOURCES below) compiled in place against the
   project-written Eigen-subset shim and registry stand-ins in
   oracle/ref_include/, with the C entry points of oracle/ref_hot.cpp, into
   oracle/_ref/.
@@ -29,7 +30,10 @@ reference each time) with exactly these rewrites, each asserted to match:
                        nested-name-specifier lose the `typename`; parameter
                        packs passed as `(args)` are expanded `(args...)`.
 None of them changes arithmetic.  Standard headers that MSVC's headers
-pull in transitively (cassert, cstring, vector, unistd.h) are force-included.  GCC's -I- makes every include (also a
+pull in transitively (cassert, cstring, vector, functional,
+condition_variable, thread, mutex, unistd.h) are
+force-included, and Scene.cpp's `#include <Eigen\\StdVector>` (a Windows
+path separator) reaches a generated one-line header of that literal name.  GCC's -I- makes every include (also a
 sibling include such as "Color.h") resolve to those copies and to the
 stand-ins first; all other reference files are read where they lie.
 """
@@ -64,10 +68,20 @@ REF_HOT_SOURCES = [
     "core/Fresnel.cpp", "core/Intersection.cpp", "core/Mapping.cpp", "core/Parameters.cpp", "core/Ray.cpp",
     "core/RaytracerObject.cpp", "core/Transform.cpp",
     "sampler/Sampler.cpp",
-    "tools/Common.cpp", "tools/Logger.cpp", "tools/Filesystem.cpp",
+    "tools/Common.cpp", "tools/Logger.cpp", "tools/Filesystem.cpp", "tools/Timer.cpp",
+    # whole-path renders: the integrators, the scene and its BVH, the camera
+    "integrator/Integrator.cpp", "integrator/PathTracingMIS.cpp", "integrator/VolPathTracing.cpp",
+    "integrator/DirectLightingMIS.cpp",
+    "accelStruct/Bvh.cpp", "core/Scene.cpp", "core/Primitive.cpp",
+    "camera/Camera.cpp", "camera/NoriPerspective.cpp",
+    "core/Screen.cpp", "core/Job.cpp", "core/SampleJob.cpp", "core/JobManager.cpp",
+    "filter/ReconstructionFilter.cpp", "filter/BoxFilter.cpp", "filter/GaussianFilter.cpp",
+    "filter/MitchellNetravaliFilter.cpp",
+    "thread/TaskSet.cpp", "thread/ThreadPool.cpp", "thread/Barrier.cpp",
 ]
 REF_CXXFLAGS = ["-std=c++17", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-fpermissive", "-w",
-                "-include", "cassert", "-include", "cstring", "-include", "vector", "-include", "unistd.h"]
+                "-include", "cassert", "-include", "cstring", "-include", "vector", "-include", "functional", "-include", "condition_variable",
+                "-include", "thread", "-include", "mutex", "-include", "unistd.h"]
 
 
 def _run(cmd):
@@ -145,7 +159,9 @@ def normalise_headers(src, dest):
                      "WithSmartPtr.h make_shared")
     smart = smart.replace("return new Derived(args);", "return new Derived(args...);")
     smart = smart.replace("return new const Derived(args);", "return new const Derived(args...);")
-    for rel, text in (("core/Color.h", color), ("tools/WithSmartPtr.h", smart)):
+    # core/Scene.cpp:11 includes <Eigen\StdVector>: a file of that literal name
+    files = [("core/Color.h", color), ("tools/WithSmartPtr.h", smart), ("Eigen\\StdVector", "#include <Eigen/StdVector>\n")]
+    for rel, text in files:
         p = os.path.join(dest, rel)
         os.makedirs(os.path.dirname(p), exist_ok=True)
         with open(p, "w", encoding="latin-1") as f:
@@ -174,7 +190,7 @@ def ref_hot_includes(src):
     norm = os.path.join(REF_OUT, "include")
     quote = [SHIM, os.path.join(SHIM, "factory"), norm, os.path.join(norm, "core"), os.path.join(norm, "tools")]
     subdirs = sorted(d for d in os.listdir(src) if os.path.isdir(os.path.join(src, d)))
-    angle = [SHIM, src] + [os.path.join(src, d) for d in subdirs] + _std_quote_dirs()
+    angle = [SHIM, norm, src] + [os.path.join(src, d) for d in subdirs] + _std_quote_dirs()
     flags = []
     for d in quote:
         flags += ["-I", d]

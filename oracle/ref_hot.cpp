@@ -11,12 +11,24 @@
  * TEST INFRASTRUCTURE ONLY: nothing in the library links this.
  *
  * Objects are built directly from Parameters, as the reference's factories
- * would build them from a scene file.  Two pieces of the reference that read
+ * would build them from a scene file.  ref_scene_create assembles a whole
+ * reference Scene from an rt_scene_desc (the description the GPU path and
+ * the CPU oracle take) the way MeshFactory / GeometricShapeFactory and the
+ * scene loader do, and ref_render_paths runs the reference's own
+ * integrator (PathTracingMIS::li or VolPathTracing::li) on per-path sample
+ * streams, as SampleJob::run does.  Two pieces of the reference that read
  * files are fed from memory instead: ImageLoader::load (the environment map,
  * defined below) and the GridVolume's .vol file (written to a temporary file
  * in the reference's own format).
  */
+#include "accelStruct/Bvh.h"
 #include "bsdf/Diffuse.h"
+#include "camera/NoriPerspective.h"
+#include "core/Primitive.h"
+#include "core/Scene.h"
+#include "core/XMLLoader.h"
+#include "integrator/PathTracingMIS.h"
+#include "integrator/VolPathTracing.h"
 #include "bsdf/MicrofacetDistribution.h"
 #include "bsdf/RoughConductor.h"
 #include "bsdf/RoughDielectric.h"
@@ -148,6 +160,70 @@ public:
     }
 };
 
+// The grid of a heterogeneous medium in the .vol layout the reference reads
+// (GridVolume.cpp:22-59), in a temporary file; "" on failure.
+std::string write_grid(const rt_medium_desc *m)
+{
+    char tmpl[] = "/tmp/rt_pin_grid_XXXXXX";
+    int fd = mkstemp(tmpl);
+    if (fd < 0) return "";
+    FILE *f = fdopen(fd, "wb");
+    const char hdr[4] = {'V', 'O', 'L', 3};
+    int32_t type = 1, channels = 1;
+    fwrite(hdr, 1, 4, f);
+    fwrite(&type, 4, 1, f);
+    fwrite(m->res, 4, 3, f);
+    fwrite(&channels, 4, 1, f);
+    fwrite(m->grid_min, 4, 3, f);
+    fwrite(m->grid_max, 4, 3, f);
+    const char skipped[4] = {0, 0, 0, 0};   // GridVolume.cpp:51-54 skips 4 bytes before the data
+    fwrite(skipped, 1, 4, f);
+    fwrite(m->density, 4, (size_t)m->res[0] * m->res[1] * m->res[2], f);
+    fclose(f);
+    return tmpl;
+}
+
+// Medium of an rt_medium_desc (its phase function: HG or isotropic).
+Medium::ptr make_medium(const rt_medium_desc *m, std::string &grid_path)
+{
+    Parameters p;
+    if (m->phase == RT_PHASE_HG) {
+        Parameters hp;
+        hp.addReal("g", m->g);
+        p.addPhaseFunction("phaseFunction", PhaseFunction::ptr(new HGPhaseFunction(hp)));
+    }
+    if (m->type == RT_MEDIUM_HOMOGENEOUS) {
+        p.addColor("sigmaA", C3(m->sigma_a));
+        p.addColor("sigmaS", C3(m->sigma_s));
+        p.addReal("scale", m->scale);
+        return Medium::ptr(new Homogeneous(p));
+    }
+    grid_path = write_grid(m);
+    if (grid_path.empty()) return Medium::ptr();
+    Parameters vp;
+    vp.addString("path", grid_path);
+    p.addVolume("volume", Volume::ptr(new GridVolume(vp)));
+    p.addColor("albedo", C3(m->albedo));
+    p.addReal("scale", m->scale);
+    p.addBool("centered", m->centered != 0);
+    p.addTransform("toWorld", xform(m->to_world));
+    return Medium::ptr(new Heterogeneous(p));
+}
+
+// NoriPerspective with the two matrices of an rt_camera_desc (the sample ->
+// camera and camera -> world transforms its constructor and the scene
+// loader would compute).
+class PinCamera : public NoriPerspective {
+public:
+    PinCamera(const Parameters &p, const rt_camera_desc &c) : NoriPerspective(p)
+    {
+        real v[16];
+        for (int i = 0; i < 16; i++) v[i] = c.sample_to_camera[i];
+        mySampleToCamera = Transform(v);
+        myWorldTransform = xform(c.camera_to_world);
+    }
+};
+
 void fill_light(rt_light_r &r, Light &L, const Point3d &p, const LightSamplingInfos &li)
 {
     memset(&r, 0, sizeof(r));
@@ -161,6 +237,15 @@ void fill_light(rt_light_r &r, Light &L, const Point3d &p, const LightSamplingIn
 }
 
 }  // namespace
+
+// Scene-file loader stand-in: Scene::loadScene (core/Scene.cpp:63-70) names
+// it, but the pins assemble scenes from descriptions (ref_scene_create) and
+// never load a file.
+namespace xml {
+XMLLoader::XMLLoader() {}
+XMLLoader::~XMLLoader() {}
+bool XMLLoader::loadScene(Scene &, const std::string &) { return false; }
+}  // namespace xml
 
 // ImageLoader::load stand-in: the image the caller put in g_next_image.
 std::shared_ptr<Array2D<Color3>> ImageLoader::load(const std::string &, Channel, real, real)
@@ -397,24 +482,8 @@ int32_t ref_medium_query(const rt_medium_desc *m, const float *owner_min, const 
         p.addReal("scale", m->scale);
         med = Medium::ptr(new Homogeneous(p));
     } else {
-        // the grid in the .vol layout the reference reads (GridVolume.cpp:22-59)
-        char tmpl[] = "/tmp/rt_pin_grid_XXXXXX";
-        int fd = mkstemp(tmpl);
-        if (fd < 0) return RT_ERR_INVALID;
-        FILE *f = fdopen(fd, "wb");
-        const char hdr[4] = {'V', 'O', 'L', 3};
-        int32_t type = 1, channels = 1;
-        fwrite(hdr, 1, 4, f);
-        fwrite(&type, 4, 1, f);
-        fwrite(m->res, 4, 3, f);
-        fwrite(&channels, 4, 1, f);
-        fwrite(m->grid_min, 4, 3, f);
-        fwrite(m->grid_max, 4, 3, f);
-        const char skipped[4] = {0, 0, 0, 0};   // GridVolume.cpp:52-54 skips 4 bytes before the data
-        fwrite(skipped, 1, 4, f);
-        fwrite(m->density, 4, (size_t)m->res[0] * m->res[1] * m->res[2], f);
-        fclose(f);
-        path = tmpl;
+        path = write_grid(m);
+        if (path.empty()) return RT_ERR_INVALID;
         Parameters vp;
         vp.addString("path", path);
         Volume::ptr vol(new GridVolume(vp));
@@ -442,6 +511,200 @@ int32_t ref_medium_query(const rt_medium_desc *m, const float *owner_min, const 
         }
     }
     if (!path.empty()) unlink(path.c_str());
+    return RT_OK;
+}
+
+/* ------------------------------------------------------------------ whole renders */
+struct ref_scene {
+    Scene scene;
+    std::shared_ptr<Camera> camera;
+    std::vector<std::string> grids;
+    int width = 0, height = 0;
+    ~ref_scene()
+    {
+        for (auto &g : grids) unlink(g.c_str());
+    }
+};
+
+/* A reference Scene assembled from an rt_scene_desc: BSDFs (Diffuse,
+ * RoughConductor, RoughDielectric, SmoothLayeredBSDF), media, area, mesh and
+ * environment lights in the description's order, one Mesh (Triangles under a
+ * per-mesh Bvh, MeshFactory.h:39-139) per mesh, Spheres
+ * (GeometricShapeFactory.h), the camera, and the integrator of `rd`; then
+ * Scene::initialize (the reference's own BVH build, light and integrator
+ * initialisation).  Returns null for a description with parts the pin build
+ * does not assemble (textures, planes, point and spot lights, the smooth
+ * BSDFs). */
+ref_scene *ref_scene_create(const rt_scene_desc *d, const rt_render_desc *rd)
+{
+    if (d->n_textures > 0) return nullptr;
+    std::unique_ptr<ref_scene> R(new ref_scene());
+    std::vector<BSDF::ptr> bsdfs;
+    for (int i = 0; i < d->n_bsdfs; i++) {
+        if (d->bsdfs[i].two_sided) return nullptr;
+        bsdfs.push_back(make_bsdf(&d->bsdfs[i]));
+        if (!bsdfs.back()) return nullptr;
+    }
+    std::vector<Medium::ptr> media;
+    for (int i = 0; i < d->n_media; i++) {
+        std::string g;
+        media.push_back(make_medium(&d->media[i], g));
+        if (!g.empty()) R->grids.push_back(g);
+        if (!media.back()) return nullptr;
+    }
+    std::vector<Light::ptr> lights;
+    for (int i = 0; i < d->n_lights; i++) {
+        const rt_light_desc &L = d->lights[i];
+        Parameters p;
+        if (L.type == RT_LIGHT_AREA) {
+            p.addColor("radiance", C3(L.radiance));
+            if (L.mesh_light) lights.push_back(Light::ptr(new MeshLight(p)));
+            else lights.push_back(Light::ptr(new AreaLight(p)));
+        } else if (L.type == RT_LIGHT_ENV) {
+            auto img = std::make_shared<Array2D<Color3>>(L.env_width, L.env_height);
+            for (int y = 0; y < L.env_height; y++)
+                for (int x = 0; x < L.env_width; x++) {
+                    const float *c = L.env_rgb + 3 * ((size_t)y * L.env_width + x);
+                    (*img)(x, y) = Color3(c[0], c[1], c[2]);
+                }
+            g_next_image = img;
+            p.addString("path", "in-memory");
+            p.addReal("scale", L.env_scale);
+            p.addTransform("toWorld", xform(L.env_to_world));
+            lights.push_back(Light::ptr(new EnvironmentLight(p)));
+            g_next_image.reset();
+        } else {
+            return nullptr;
+        }
+    }
+    auto med = [&](int i) { return i >= 0 ? media[i] : Medium::ptr(); };
+    auto bsdf = [&](int i) { return i >= 0 ? bsdfs[i] : BSDF::ptr(); };
+    for (int m = 0; m < d->n_meshes; m++) {
+        const rt_mesh_desc &M = d->meshes[m];
+        if (M.n_tris == 0) continue;
+        // the mesh's own vertex list, in order of first use
+        std::vector<Point3d, Eigen::aligned_allocator<Point3d>> verts;
+        std::vector<Normal3d, Eigen::aligned_allocator<Normal3d>> normals;
+        std::vector<Point2d, Eigen::aligned_allocator<Point2d>> uvs;
+        std::vector<int> idx;
+        std::map<int, int> remap;
+        bool has_n = d->normals != nullptr, has_uv = d->uvs != nullptr;
+        for (int t = M.first_tri; t < M.first_tri + M.n_tris; t++)
+            for (int k = 0; k < 3; k++) {
+                int v = d->indices[3 * t + k];
+                if (has_n && std::isnan(d->normals[3 * v])) has_n = false;
+                if (has_uv && std::isnan(d->uvs[2 * v])) has_uv = false;
+            }
+        for (int t = M.first_tri; t < M.first_tri + M.n_tris; t++)
+            for (int k = 0; k < 3; k++) {
+                int v = d->indices[3 * t + k];
+                auto it = remap.find(v);
+                if (it == remap.end()) {
+                    it = remap.emplace(v, (int)verts.size()).first;
+                    verts.push_back(P3(d->vertices + 3 * v));
+                    if (has_n) normals.push_back(Normal3d(d->normals[3 * v], d->normals[3 * v + 1], d->normals[3 * v + 2]));
+                    if (has_uv) uvs.push_back(Point2d(d->uvs[2 * v], d->uvs[2 * v + 1]));
+                }
+                idx.push_back(it->second);
+            }
+        Mesh::ptr mesh(new Mesh("", verts, normals, uvs, idx));
+        Light::ptr light = M.light >= 0 ? lights[M.light] : Light::ptr();
+        if (light) ((AreaLight *)light.get())->setShape(mesh);
+        std::vector<IPrimitive::ptr> tris;
+        for (unsigned i = 0; i < idx.size(); i += 3) {
+            GeometricShape::ptr shape(new Triangle(Parameters(), mesh, (int)i));
+            IPrimitive::ptr prim(std::make_shared<SimplePrimitive>(shape, bsdf(M.bsdf), BSSRDF::ptr(), med(M.interior),
+                                                                   med(M.exterior)));
+            if (light) {
+                mesh->addLightTriangle(shape);
+                prim->addLight(light);
+            }
+            tris.push_back(prim);
+        }
+        mesh->initialize();
+        IPrimitive::ptr prim = std::make_shared<Bvh>(tris);
+        if (light) prim->addLight(light);
+        if (M.interior >= 0) media[M.interior]->setOwnerBBox(prim->getWorldBoundingBox());
+        if (M.exterior >= 0) media[M.exterior]->setOwnerBBox(prim->getWorldBoundingBox());
+        R->scene.addPrimitive(prim);
+    }
+    for (int i = 0; i < d->n_spheres; i++) {
+        const rt_sphere_desc &S = d->spheres[i];
+        if (S.kind != RT_ANALYTIC_SPHERE) return nullptr;
+        Parameters sp;
+        sp.addReal("radius", S.radius);
+        sp.addTransform("toWorld", xform(S.to_world));
+        GeometricShape::ptr shape(new Sphere(sp));
+        IPrimitive::ptr prim(std::make_shared<SimplePrimitive>(shape, bsdf(S.bsdf), BSSRDF::ptr(), med(S.interior),
+                                                               med(S.exterior)));
+        if (S.light >= 0) {
+            ((AreaLight *)lights[S.light].get())->setShape(std::dynamic_pointer_cast<ISampledShape>(shape));
+            prim->addLight(lights[S.light]);
+        }
+        if (S.interior >= 0) media[S.interior]->setOwnerBBox(prim->getWorldBoundingBox());
+        if (S.exterior >= 0) media[S.exterior]->setOwnerBBox(prim->getWorldBoundingBox());
+        R->scene.addPrimitive(prim);
+    }
+    for (int i = 0; i < d->n_lights; i++) {
+        R->scene.addLight(lights[i]);
+        if (d->lights[i].type == RT_LIGHT_ENV) R->scene.setEnvironementLight(lights[i]);
+    }
+    const rt_camera_desc &c = d->camera;
+    if (c.filter != RT_FILTER_BOX || c.filter_radius[0] != 0.5f || c.filter_radius[1] != 0.5f) return nullptr;
+    Parameters cp;
+    cp.addInt("sizeX", c.width);
+    cp.addInt("sizeY", c.height);
+    cp.addReal("nearClip", c.near_clip);
+    cp.addReal("farClip", c.far_clip);
+    cp.addReal("apertureRadius", c.aperture_radius);
+    cp.addReal("focalPlane", c.focal_plane);
+    R->camera = std::make_shared<PinCamera>(cp, c);
+    R->scene.setCamera(R->camera);
+    if (c.medium >= 0) R->scene.setCameraMedium(media[c.medium]);
+    Parameters ip;
+    ip.addInt("maxDepth", rd->max_depth);
+    ip.addInt("minDepth", rd->min_depth);
+    ip.addString("strategy", rd->strategy == RT_STRATEGY_ONE_LIGHT_WEIGHTED ? "one_light_weighted"
+                             : rd->strategy == RT_STRATEGY_ALL_LIGHTS     ? "all_lights"
+                                                                           : "one_light_uniform");
+    if (rd->integrator == RT_INTEGRATOR_VOLPATH) R->scene.addIntegrator(Integrator::ptr(new VolPathTracing(ip)));
+    else R->scene.addIntegrator(Integrator::ptr(new PathTracingMIS(ip)));
+    R->scene.initialize();
+    R->width = c.width;
+    R->height = c.height;
+    return R.release();
+}
+
+void ref_scene_destroy(ref_scene *s) { delete s; }
+
+/* Radiance of path samples (pixel y * width + x, sample index) as
+ * SampleJob::run computes them (core/SampleJob.cpp:46-61): the sampler on
+ * the path's stream, the 2-D pixel jitter, a lens sample when the camera has
+ * an aperture, Camera::getRay, Integrator::li.  rad: 3 floats per path;
+ * jit: the sample's film position (2 floats per path), may be null. */
+int32_t ref_render_paths(ref_scene *s, uint64_t seed, const int32_t *pixels, const int32_t *samples, int32_t n,
+                         float *rad, float *jit)
+{
+    std::shared_ptr<PathStreamSampler> sampler(new PathStreamSampler());
+    Integrator *integ = s->scene.getIntegrator().get();
+    for (int i = 0; i < n; i++) {
+        int x = pixels[i] % s->width, y = pixels[i] / s->width;
+        sampler->seed(mix64((seed << 32) ^ (uint64_t)(uint32_t)pixels[i]), (uint64_t)(uint32_t)samples[i]);
+        Point2d sample = sampler->getNextSample2D();
+        real xx = (real)x + sample.x();
+        real yy = (real)y + sample.y();
+        Point2d lens;
+        if (s->camera->needsDoFSample()) lens = sampler->getNextSample2D();
+        Ray ray = s->camera->getRay(xx, yy, lens);
+        Color col = integ->li(s->scene, sampler, ray);
+        rad[3 * i] = col(0);
+        rad[3 * i + 1] = col(1);
+        rad[3 * i + 2] = col(2);
+        if (jit) {
+            jit[2 * i] = xx;
+            jit[2 * i + 1] = yy;
+        }
+    }
     return RT_OK;
 }
 

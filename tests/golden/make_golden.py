@@ -5,13 +5,18 @@ tools/Rng.h (PCG32) and core/CDF.{h,cpp} into libref_pin.so, and the
 hot-path sources (triangle test, warps, Fresnel, microfacet distributions,
 Diffuse / RoughConductor / RoughDielectric / SmoothLayeredBSDF, mesh, sphere
 and environment lights, HG phase function, homogeneous and grid media) into
-libref_hot.so.  This script runs them on seeded inputs and writes the
+libref_hot.so, together with the integrators, the scene and its BVH and
+the camera.  This script runs them on seeded inputs and writes the
 fixtures next to itself:
 
 * pcg32_ref.json  -- raw 32-bit outputs and mantissa floats of Rng streams
 * cdf_ref.json    -- CDF::sampleAndReuse / CDF::sample on seeded pdf lists
 * ref_hot.npz     -- the queries of tests/pin_cases.py with the reference's
                      answers
+* ref_paths.npz   -- the radiance of every path sample of small renders of
+                     the three configurations' scene families, computed by
+                     the reference's own PathTracingMIS::li /
+                     VolPathTracing::li over its own BVH
 
 Run from the repository root, naming the reference's RaytracerNew2/src:
     python tests/golden/make_golden.py <reference>/RaytracerNew2/src
@@ -95,6 +100,13 @@ def main():
     np.savez_compressed(os.path.join(HERE, "ref_hot.npz"),
                         **{"in_" + k: v for k, v in inp.items()}, **{"out_" + k: v for k, v in out.items()})
     print("wrote", os.path.join(HERE, "ref_hot.npz"))
+    films = {}
+    for name, scene, spp in pin_cases.film_scenes():
+        pix, smp = pin_cases.all_paths(scene, spp)
+        films[name + "_rad"] = pin_cases.reference_paths(C.CDLL(hot), scene, pix, smp, seed=0)
+        films[name + "_digest"] = np.array(pin_cases.scene_digest(scene))
+    np.savez_compressed(os.path.join(HERE, "ref_paths.npz"), **films)
+    print("wrote", os.path.join(HERE, "ref_paths.npz"))
 
 
 if __name__ == "__main__":

@@ -359,3 +359,54 @@ def run(side, inp):
                 out["medium_%s_%s" % (name, tag)] = osc.medium_query(mid, op, mq)
         osc.close()
     return out
+
+
+# ---------------------------------------------------------------- whole paths
+def film_scenes():
+    """Scenes whose every path sample the reference's own integrator renders
+    for the film pins: the configurations' scene families at small sizes."""
+    return [("cornell_64x64_4spp", scenes.cornell_box(64, 64), 4),
+            ("icosphere_l5_48x48_2spp", scenes.displaced_icosphere(level=5, width=48, height=48, env_size=(128, 64)), 2),
+            ("volume_res32_40x32_2spp", scenes.volume_grid(40, 32, res=32), 2)]
+
+
+def scene_digest(s):
+    """A checksum of a scene's geometry, maps and grids (the fixture records
+    it, so a changed generator is reported as such)."""
+    import hashlib
+    h = hashlib.sha256()
+    h.update(np.ascontiguousarray(s.vertices, np.float32).tobytes())
+    h.update(np.ascontiguousarray(s.indices, np.int32).tobytes())
+    for l in s.lights:
+        if "rgb" in l:
+            h.update(np.ascontiguousarray(l["rgb"], np.float32).tobytes())
+    for m in s.media:
+        if m.get("density") is not None:
+            h.update(np.ascontiguousarray(m["density"], np.float32).tobytes())
+    return h.hexdigest()
+
+
+def all_paths(s, spp):
+    W, H = s.camera["width"], s.camera["height"]
+    pix = np.repeat(np.arange(W * H, dtype=np.int32), spp)
+    smp = np.tile(np.arange(spp, dtype=np.int32), W * H)
+    return pix, smp
+
+
+def reference_paths(L, s, pix, smp, seed=0):
+    """Per-path radiance of the reference's own integrator (ref_render_paths)."""
+    L.ref_scene_create.restype = C.c_void_p
+    L.ref_scene_create.argtypes = [C.POINTER(D.SceneDesc), C.POINTER(D.RenderDesc)]
+    L.ref_render_paths.argtypes = [C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]
+    L.ref_render_paths.restype = C.c_int32
+    L.ref_scene_destroy.argtypes = [C.c_void_p]
+    d = s.desc()
+    rd = s.render_desc(1, seed=seed)
+    h = L.ref_scene_create(C.byref(d), C.byref(rd))
+    assert h, "scene has parts the reference pin build does not assemble"
+    pix = np.ascontiguousarray(pix, np.int32)
+    smp = np.ascontiguousarray(smp, np.int32)
+    rad = np.zeros((len(pix), 3), np.float32)
+    assert L.ref_render_paths(h, seed, _p(pix), _p(smp), len(pix), _p(rad), None) == 0
+    L.ref_scene_destroy(h)
+    return rad

@@ -156,6 +156,52 @@ def test_reference_hot_path_agrees_live():
         _compare_family(key, ref[key], mine[key])
 
 
+PATHS = os.path.join(GOLDEN, "ref_paths.npz")
+
+
+@pytest.mark.parametrize("case", [0, 1, 2], ids=["cornell", "icosphere", "volume"])
+def test_oracle_paths_match_reference_integrator(case):
+    """Every path sample of small renders of the three configurations' scene
+    families, against the reference's own PathTracingMIS::li /
+    VolPathTracing::li over its own BVH (ref_paths.npz).  Stated tolerance:
+    per-path radiance within 1e-5 relative for every path.  Measured:
+    bit-identical."""
+    import pin_cases
+    name, scene, spp = pin_cases.film_scenes()[case]
+    gold = np.load(PATHS)
+    assert str(gold[name + "_digest"]) == pin_cases.scene_digest(scene), \
+        "the scene generator changed: regenerate tests/golden/ref_paths.npz"
+    pix, smp = pin_cases.all_paths(scene, spp)
+    ref = gold[name + "_rad"]
+    mine = O.OracleScene(scene).render_paths(pix, smp, seed=0)
+    same = np.all(ref == mine, axis=1)
+    rel = np.abs(ref - mine) / np.maximum(np.maximum(np.abs(ref), np.abs(mine)), 1e-30)
+    print("%s: %d paths, %.4f bit-identical, max rel %.2e" % (name, len(pix), same.mean(), rel.max()))
+    assert np.all(same[:, None] | (rel <= 1e-5))
+
+
+def test_oracle_paths_match_reference_integrator_live():
+    """Where the reference pin library was built on this machine: larger
+    renders (the Cornell box at its full 256x256, a level-6 icosphere, a 64^3
+    grid), path by path."""
+    import ctypes as C
+    import pin_cases
+    path = os.path.join(O.ROOT, "oracle", "_ref", "libref_hot.so")
+    if not os.path.exists(path):
+        pytest.skip("reference pin library not built on this machine")
+    L = C.CDLL(path)
+    for scene, spp in [(scenes.cornell_box(256, 256), 1),
+                       (scenes.displaced_icosphere(level=6, width=64, height=64, env_size=(256, 128)), 2),
+                       (scenes.volume_grid(64, 48, res=64), 2)]:
+        pix, smp = pin_cases.all_paths(scene, spp)
+        ref = pin_cases.reference_paths(L, scene, pix, smp, seed=3)
+        mine = O.OracleScene(scene).render_paths(pix, smp, seed=3)
+        same = np.all(ref == mine, axis=1)
+        rel = np.abs(ref - mine) / np.maximum(np.maximum(np.abs(ref), np.abs(mine)), 1e-30)
+        print("%s: %d paths, %.4f bit-identical" % (scene.name, len(pix), same.mean()))
+        assert np.all(same[:, None] | (rel <= 1e-5))
+
+
 def test_oracle_render_is_thread_count_independent():
     s = scenes.cornell_box(40, 24)
     o = O.OracleScene(s)
