@@ -415,6 +415,11 @@ typedef struct rt_tuning {
     int32_t volpath_wavefront;   /* VolPathTracing as a wavefront of kernels
                                     over queues (1, the default) or as one
                                     persistent kernel per path (0)            */
+    int32_t batch_wavefront;     /* rt_batch_render: the PathTracingMIS jobs
+                                    (box filter) in one wavefront whose path
+                                    slots span their scenes, batches of up to
+                                    wave_paths (1, the default), or every job
+                                    as its own render on the lanes (0)        */
 } rt_tuning;
 rt_status rt_ctx_get_tuning(rt_ctx *ctx, rt_tuning *out);
 rt_status rt_ctx_set_tuning(rt_ctx *ctx, const rt_tuning *t);
@@ -452,14 +457,21 @@ rt_status rt_render_tile_static(rt_ctx *ctx, rt_scene *scene, const rt_render_de
 
 /* Batched rendering: n independent jobs (scenes[i] rendered with descs[i]
  * into films[i], each width*height*4 floats on the host or, with
- * on_device = 1, on the device), largest job first, on up to
- * rt_ctx_set_lanes() worker lanes of the context's device (one stream,
- * wavefront buffers and host thread each).  Each film equals what
- * rt_render writes for that job alone.  Returns after every job has
- * finished; on failures the other jobs still run and the first error is
- * returned.  rt_render_stats_get then reports the sums over the jobs, with
- * kernel_ms the wall time of the batch.  The reference renders one scene per
- * process (core/main.cpp:439-447); this call replaces a loop of such runs. */
+ * on_device = 1, on the device).  With rt_tuning.batch_wavefront (the
+ * default), the PathTracingMIS jobs with the box filter of radius 0.5 that
+ * share max_depth and min_depth run together as one wavefront: every batch
+ * of up to wave_paths path slots holds whole tiles of several jobs, each
+ * path carries its job's scene, and one launch per kernel per bounce serves
+ * all of them.  Other jobs (VolPathTracing, other filters) run meanwhile as
+ * one rt_render each, largest first, on up to rt_ctx_set_lanes() worker
+ * lanes of the context's device (one stream, wavefront buffers and host
+ * thread each).  Each film equals what rt_render writes for that job alone.
+ * Returns after every job has finished; on failures the other jobs still
+ * run and the first error is returned.  rt_render_stats_get then reports
+ * the sums over the jobs, with kernel_ms the wall time of the batch.  The
+ * reference renders one scene per process (core/main.cpp:439-447) and cuts
+ * a frame into tile jobs (core/Scene.cpp:83-95); this call replaces a loop
+ * of such runs. */
 rt_status rt_batch_render(rt_ctx *ctx, rt_scene *const *scenes, const rt_render_desc *descs,
                           int32_t n, float *const *films, int32_t on_device);
 /* Worker lanes of rt_batch_render: 1..16, default 4. */

@@ -38,7 +38,7 @@ class Tuning(C.Structure):
     """rt_tuning: launch shapes, queue capacities and scheduling choices."""
     _fields_ = [("wave_paths", C.c_int32), ("lane_wave_paths", C.c_int32), ("trace_blocks_per_sm", C.c_int32),
                 ("shade_blocks_per_sm", C.c_int32), ("sort_threshold", C.c_int32), ("lanes", C.c_int32),
-                ("graphs", C.c_int32), ("volpath_wavefront", C.c_int32)]
+                ("graphs", C.c_int32), ("volpath_wavefront", C.c_int32), ("batch_wavefront", C.c_int32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -108,6 +108,11 @@ struct RenderParams {
     // rounds with fewer closest-hit rays than this are not sorted by
     // material: their hits go to one queue shaded by k_pt_shade<RT_QUEUE_MIXED>
     int sort_threshold;
+    // multi-scene batches: the scene table (one entry per job, indexed by
+    // W.sid), the batch's work items and their count; null otherwise
+    const DevScene *scenes;
+    const MultiItem *items;
+    int n_items;
 };
 
 __device__ __forceinline__ int cur_round(const RenderParams &P, int round)
@@ -149,20 +154,70 @@ __global__ void k_camera(RenderParams P)
     }
 }
 
+// Camera rays of a multi-scene batch: the work item of each slot (binary
+// search over the items' first slots), then exactly what k_camera does for
+// that item's job: its camera, tile order and seed.  The slot's scene-table
+// index is recorded for the kernels that follow.
+__device__ __forceinline__ int item_of_slot(const MultiItem *items, int n_items, int slot)
+{
+    int lo = 0, hi = n_items - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (items[mid].path0 <= slot) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+__global__ void k_camera_multi(RenderParams P)
+{
+    for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < P.n_paths; slot += gridDim.x * blockDim.x) {
+        const MultiItem &it = P.items[item_of_slot(P.items, P.n_items, slot)];
+        const DevCamera &cam = P.scenes[it.job].cam;
+        const int local = slot - it.path0;
+        const int q = local % it.npix;
+        const int s = local / it.npix;
+        int4 to = it.tileorder[it.g0 + q];
+        int x = to.x, y = to.y;
+        int lx = to.z & 0xffff, ly = to.z >> 16, tw = to.w & 0xffff, th = to.w >> 16;
+        Pcg32 rng;
+        path_stream_seed(rng, it.seed, (uint32_t)(y * cam.width + x), (uint32_t)(it.sample_begin + s));
+        V2 j = next2d(rng);
+        float xx = (float)x + j.x, yy = (float)y + j.y;
+        V2 lens = v2(0.f, 0.f);
+        if (cam.aperture_radius > 0.f) lens = next2d(rng);
+        Ray r = camera_ray(cam, xx, yy, lens);
+        uint8_t code = splat_code(xx, yy, x - lx, y - ly, lx, ly, tw, th);
+        P.W.splat[slot] = code;
+        if (code != 0x55) P.W.pix_irregular[it.pix0 + q] = 1;
+        P.W.sid[slot] = it.job;
+        P.W.rng[slot] = rng;
+        P.W.ray_o[slot] = f4(r.o, r.mint);
+        P.W.ray_d[slot] = f4(r.d, r.maxt);
+        P.W.tp[slot] = make_float4(1.f, 1.f, 1.f, 1.f);
+        P.W.rad[slot] = make_float4(0.f, 0.f, 0.f, __int_as_float(0));
+        P.W.flags[slot] = F_FIRST;
+        P.W.q_closest[slot] = slot;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        P.W.cnt[0].closest = P.n_paths;
+        P.W.cnt[0].shadow = 0;
+    }
+}
+
 // Sort a traced path by what its ray hit: the shading queue of the hit
 // surface's BSDF type, or the finish queue for a miss or a surface without a
 // BSDF.  Called by the lanes that just finished a closest-hit ray.
 // `n` is the round's closest-hit ray count: below P.sort_threshold the hits
 // are not sorted by material (one queue, one generic shading kernel).
-__device__ __forceinline__ void classify_hit(const RenderParams &P, RoundCounters *C, int slot, int prim, int n)
+__device__ __forceinline__ void classify_hit(const RenderParams &P, const DevScene &S, RoundCounters *C, int slot,
+                                             int prim, int n)
 {
-    const int t = prim == -1 ? -1 : prim_type(P.S, prim);
+    const int t = prim == -1 ? -1 : prim_type(S, prim);
     if (n < P.sort_threshold) {
         q_push(P.W.q_mixed, &C->mixed, slot, t >= 0);
     } else {
 #pragma unroll
         for (int k = 0; k < RT_NBSDF; k++) q_push(P.W.q_mat[k], &C->mat[k], slot, t == k);
-        if (P.S.has_mixed) q_push(P.W.q_mixed, &C->mixed, slot, t == RT_QUEUE_MIXED);
+        if (S.has_mixed) q_push(P.W.q_mixed, &C->mixed, slot, t == RT_QUEUE_MIXED);
     }
     q_push(P.W.q_fin, &C->fin, slot, t < 0);
 }
@@ -284,11 +339,15 @@ __global__ void k_sort_copy(RenderParams P, int round, int shadow)
 #ifndef RT_BVH_CNODE
 #define RT_BVH_CNODE 1.0
 #endif
-template <bool ANY, bool COUNT>
+// MULTI: a multi-scene batch; each ray traverses the tree of its path's
+// scene (P.scenes[W.sid[slot]]), held per lane
+template <bool ANY, bool COUNT, bool MULTI = false>
 __global__ void __launch_bounds__(128, RT_TRACE_MINB) k_trace(RenderParams P, int round)
 {
     round = cur_round(P, round);
     const DevScene S = P.S;
+    const DevScene *ms = nullptr;                 // MULTI: the lane's scene
+    const float4 *mnodes = nullptr, *mtris = nullptr;
     RoundCounters *C = &P.W.cnt[round];
     const int n = ANY ? C->shadow : C->closest;
     int *wc = ANY ? &C->wc_shadow : &C->wc_closest;
@@ -344,6 +403,11 @@ __global__ void __launch_bounds__(128, RT_TRACE_MINB) k_trace(RenderParams P, in
             has_ray = q < n;
             if (has_ray) {
                 slot = queue[q];
+                if (MULTI) {
+                    ms = &P.scenes[P.W.sid[slot]];
+                    mnodes = ms->nodes;
+                    mtris = ms->tri_slots;
+                }
                 float4 o4 = ANY ? P.W.sh_o[slot] : P.W.ray_o[slot];
                 float4 d4 = ANY ? P.W.sh_d[slot] : P.W.ray_d[slot];
                 ox = o4.x; oy = o4.y; oz = o4.z; dx = d4.x; dy = d4.y; dz = d4.z;
@@ -361,7 +425,7 @@ __global__ void __launch_bounds__(128, RT_TRACE_MINB) k_trace(RenderParams P, in
                 sp = 0;
                 SPUSH(RT_SENT);
                 leaf = 0;
-                node = (S.n_nodes > 0 && !(hit_t < tmin)) ? 0 : RT_SENT;
+                node = ((MULTI ? ms->n_nodes : S.n_nodes) > 0 && !(hit_t < tmin)) ? 0 : RT_SENT;
             }
         }
         if (!__any_sync(0xffffffffu, has_ray)) break;
@@ -370,7 +434,7 @@ __global__ void __launch_bounds__(128, RT_TRACE_MINB) k_trace(RenderParams P, in
         while (node != RT_SENT) {
             while ((unsigned)node < (unsigned)RT_SENT) {
                 if (COUNT) cnt[0]++;
-                const float4 *N = S.nodes + 4 * (size_t)node;
+                const float4 *N = (MULTI ? mnodes : S.nodes) + 4 * (size_t)node;
                 float4 n0 = __ldg(N), n1 = __ldg(N + 1), n2 = __ldg(N + 2);
                 int4 cc = __ldg(reinterpret_cast<const int4 *>(N + 3));
                 float c0lox = __fmaf_rn(n0.x, idx, lx), c0hix = __fmaf_rn(n0.y, idx, hx);
@@ -405,7 +469,7 @@ __global__ void __launch_bounds__(128, RT_TRACE_MINB) k_trace(RenderParams P, in
                 int first = v >> 3, cl = (v & 7) + 1;
                 for (int i = 0; i < cl; i++) {
                     if (COUNT) cnt[1]++;
-                    const float4 *T = S.tri_slots + 3 * (size_t)(first + i);
+                    const float4 *T = (MULTI ? mtris : S.tri_slots) + 3 * (size_t)(first + i);
                     float4 a = __ldg(T), b = __ldg(T + 1), c = __ldg(T + 2);
                     float t, u, w;
                     if (mt_test(a, b, c, v3(ox, oy, oz), v3(dx, dy, dz), tmin, hit_t, t, u, w)) {
@@ -422,9 +486,11 @@ __global__ void __launch_bounds__(128, RT_TRACE_MINB) k_trace(RenderParams P, in
         // ---- finished rays: analytic spheres, then store
         if (node == RT_SENT && has_ray) {
             if (!(ANY && hprim >= 0)) {
-                for (int si = 0; si < S.n_spheres; si++) {
+                const int nsph = MULTI ? ms->n_spheres : S.n_spheres;
+                const DevSphere *sph = MULTI ? ms->spheres : S.spheres;
+                for (int si = 0; si < nsph; si++) {
                     float t;
-                    if (analytic_test(S.spheres[si], v3(ox, oy, oz), v3(dx, dy, dz), tmin, hit_t, t)) {
+                    if (analytic_test(sph[si], v3(ox, oy, oz), v3(dx, dy, dz), tmin, hit_t, t)) {
                         hit_t = t; hu = 0.f; hv = 0.f; hprim = -si - 2;
                         if (ANY) break;
                     }
@@ -433,7 +499,8 @@ __global__ void __launch_bounds__(128, RT_TRACE_MINB) k_trace(RenderParams P, in
             if (ANY) P.W.occl[slot] = hprim != -1 ? 1 : 0;
             else {
                 P.W.hit[slot] = make_float4(hit_t, hu, hv, __int_as_float(hprim));
-                classify_hit(P, C, slot, hprim, n);
+                if (MULTI) classify_hit(P, *ms, C, slot, hprim, n);
+                else classify_hit(P, S, C, slot, hprim, n);
             }
             has_ray = false;
         }
@@ -645,7 +712,7 @@ __global__ void __launch_bounds__(128, 8) k_trace8(RenderParams P, int round)
             if (ANY) P.W.occl[slot] = hprim != -1 ? 1 : 0;
             else {
                 P.W.hit[slot] = make_float4(hit_t, hu, hv, __int_as_float(hprim));
-                classify_hit(P, C, slot, hprim, n);
+                classify_hit(P, S, C, slot, hprim, n);
             }
             has_ray = false;
         }
@@ -714,55 +781,61 @@ __global__ void k_hits_out(RenderParams P, int n, int anyhit, rt_hit *hits)
 //                     then shades the new vertex: emission at depth 0
 //                     (:73-74), light sample (:121-153), BSDF sample (:156-168),
 //                     emitting the shadow ray and the next closest-hit ray.
+__device__ __forceinline__ void pt_finish_path(const RenderParams &P, const DevScene &S, int slot)
+{
+    const int env = S.env_light;
+    int flags = P.W.flags[slot];
+    C3 L = rgb(P.W.rad[slot]);
+    if (flags & F_FIRST) {
+        // camera ray: the environment if it missed; a surface without a
+        // BSDF ends the path (PathTracingMIS.cpp:60-70)
+        float4 hv = P.W.hit[slot];
+        if (__float_as_int(hv.w) == -1 && env >= 0) L = L + env_le(S.lights[env], xyz(P.W.ray_d[slot]));
+    } else {
+        if ((flags & F_NEE) && !P.W.occl[slot]) L = L + rgb(P.W.nee[slot]);
+        if (!(flags & F_END)) {
+            float4 hv = P.W.hit[slot];
+            Hit h; h.t = hv.x; h.u = hv.y; h.v = hv.z; h.prim = __float_as_int(hv.w);
+            float4 ro = P.W.ray_o[slot], rd = P.W.ray_d[slot];
+            V3 o = xyz(ro), d = xyz(rd);
+            int caught = -1;
+            C3 Le = cfill(0.f);
+            V3 pt = v3(0, 0, 0), nn = v3(0, 0, 0);
+            if (h.prim != -1) {
+                int nl = prim_light(S, h.prim);
+                if (nl >= 0) {
+                    Frame fr = hit_frame(S, h, o, d);
+                    pt = fr.p; nn = fr.n;
+                    caught = nl;
+                    Le = area_le(S, nl, -d, fr.n);
+                }
+            } else if (env >= 0) {
+                caught = env;
+                Le = env_le(S.lights[env], d);
+            }
+            if (caught >= 0) {
+                C3 T = rgb(P.W.tp[slot]);
+                float4 bsv = P.W.bs[slot];
+                float pl = (flags & F_DELTA) ? 0.f : light_pdf(S, caught, o, pt, nn, d);
+                float w = power_heuristic(bsv.w, pl);
+                L = L + ((T * Le) * rgb(bsv)) * w;
+            }
+        }
+    }
+    P.W.out[slot] = f4c(L, 0.f);
+    P.W.flags[slot] = (flags & ~(F_FIRST | F_NEE)) | F_DONE;
+}
+// MULTI: a multi-scene batch, each path read against its own scene
+template <bool MULTI = false>
 __global__ void __launch_bounds__(128) k_pt_finish(RenderParams P, int round)
 {
     round = cur_round(P, round);
-    const DevScene &S = P.S;
     RoundCounters *C = &P.W.cnt[round];
     const int nf = C->fin, n = nf + C->end;
-    const int env = S.env_light;
     for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
         const int slot = idx < nf ? P.W.q_fin[idx] : P.W.q_end[idx - nf];
-        int flags = P.W.flags[slot];
-        C3 L = rgb(P.W.rad[slot]);
-        if (flags & F_FIRST) {
-            // camera ray: the environment if it missed; a surface without a
-            // BSDF ends the path (PathTracingMIS.cpp:60-70)
-            float4 hv = P.W.hit[slot];
-            if (__float_as_int(hv.w) == -1 && env >= 0) L = L + env_le(S.lights[env], xyz(P.W.ray_d[slot]));
-        } else {
-            if ((flags & F_NEE) && !P.W.occl[slot]) L = L + rgb(P.W.nee[slot]);
-            if (!(flags & F_END)) {
-                float4 hv = P.W.hit[slot];
-                Hit h; h.t = hv.x; h.u = hv.y; h.v = hv.z; h.prim = __float_as_int(hv.w);
-                float4 ro = P.W.ray_o[slot], rd = P.W.ray_d[slot];
-                V3 o = xyz(ro), d = xyz(rd);
-                int caught = -1;
-                C3 Le = cfill(0.f);
-                V3 pt = v3(0, 0, 0), nn = v3(0, 0, 0);
-                if (h.prim != -1) {
-                    int nl = prim_light(S, h.prim);
-                    if (nl >= 0) {
-                        Frame fr = hit_frame(S, h, o, d);
-                        pt = fr.p; nn = fr.n;
-                        caught = nl;
-                        Le = area_le(S, nl, -d, fr.n);
-                    }
-                } else if (env >= 0) {
-                    caught = env;
-                    Le = env_le(S.lights[env], d);
-                }
-                if (caught >= 0) {
-                    C3 T = rgb(P.W.tp[slot]);
-                    float4 bsv = P.W.bs[slot];
-                    float pl = (flags & F_DELTA) ? 0.f : light_pdf(S, caught, o, pt, nn, d);
-                    float w = power_heuristic(bsv.w, pl);
-                    L = L + ((T * Le) * rgb(bsv)) * w;
-                }
-            }
-        }
-        P.W.out[slot] = f4c(L, 0.f);
-        P.W.flags[slot] = (flags & ~(F_FIRST | F_NEE)) | F_DONE;
+        if (MULTI) pt_finish_path(P, P.scenes[P.W.sid[slot]], slot);
+        else pt_finish_path(P, P.S, slot);
     }
 }
 
@@ -828,10 +901,135 @@ __device__ __forceinline__ C3 bsdf_sample_t(const DevBsdf &b, BsdfRec &r, V2 s, 
 #define RT_SHADE_GRID 16
 #endif
 template <int BT>
+__device__ __forceinline__ void pt_shade_path(const RenderParams &P, const DevScene &S, int slot, bool &push_end,
+                                              bool &push_closest, bool &push_shadow)
+{
+    Pcg32 rng = P.W.rng[slot];
+    float4 tpv = P.W.tp[slot];
+    C3 T = rgb(tpv);
+    float eta = tpv.w;
+    float4 radv = P.W.rad[slot];
+    C3 L = rgb(radv);
+    int depth = __float_as_int(radv.w);
+    int flags = P.W.flags[slot];
+    float4 ro = P.W.ray_o[slot], rd = P.W.ray_d[slot];
+    V3 o = xyz(ro), d = xyz(rd);
+    float4 hv = P.W.hit[slot];
+    Hit h; h.t = hv.x; h.u = hv.y; h.v = hv.z; h.prim = __float_as_int(hv.w);
+    Frame fr = hit_frame(S, h, o, d);
+    // the mixed queue's BSDF is a copy with its textures applied at
+    // the hit; the sorted queues read the scene's (untextured) BSDF
+    DevBsdf Bl;
+    if (BT == RT_QUEUE_MIXED) {
+        Bl = S.bsdfs[prim_bsdf(S, h.prim)];
+        if (Bl.textured) tex_apply(S, Bl, hit_uv(S, h, o, d));
+    }
+    const DevBsdf &B = BT == RT_QUEUE_MIXED ? Bl : S.bsdfs[prim_bsdf(S, h.prim)];
+    bool done = false;
+    // finish the previous vertex (its light sample and the emission
+    // its BSDF-sampled ray found), update throughput, roulette
+    if (flags & F_FIRST) {
+        flags &= ~F_FIRST;
+        if (depth >= P.max_depth) done = true;
+    } else {
+        if ((flags & F_NEE) && !P.W.occl[slot]) L = L + rgb(P.W.nee[slot]);
+        flags &= ~F_NEE;
+        float4 bsv = P.W.bs[slot];
+        C3 f = rgb(bsv);
+        int nl = prim_light(S, h.prim);
+        if (nl >= 0) {
+            C3 Le = area_le(S, nl, -d, fr.n);
+            float pl = (flags & F_DELTA) ? 0.f : light_pdf(S, nl, o, fr.p, fr.n, d);
+            float w = power_heuristic(bsv.w, pl);
+            L = L + ((T * Le) * f) * w;
+        }
+        T = T * f;
+        eta *= P.W.rel_eta[slot];
+        if (depth >= P.min_depth) {
+            float stop = smin(0.95f, lum(T) * eta * eta);
+            if (next1d(rng) < stop) T = T / stop;
+            else done = true;
+        }
+        if (!done) {
+            depth++;
+            if (depth >= P.max_depth) done = true;
+        }
+    }
+    if (done) {
+        P.W.out[slot] = f4c(L, 0.f);
+        P.W.flags[slot] = flags | F_DONE;
+        P.W.rng[slot] = rng;
+    } else {
+    // emission of a light hit by the camera ray (PathTracingMIS.cpp:73-74)
+    if (depth == 0) {
+        int hl = prim_light(S, h.prim);
+        if (hl >= 0) L = L + T * area_le(S, hl, -d, fr.n);
+    }
+    // light sampling (Integrator::sampleLightDirect, Integrator.cpp:176-218)
+    V2 s = next2d(rng);
+    if (S.n_lights > 0) {
+        float lw;
+        int li_idx = cdf_sample_reuse(S.light_cdf, S.n_lights + 1, s.x, lw);
+        LightRec li;
+        light_sample(S, li_idx, fr.p, s, li);
+        if (li.pdf > 0 && lum(li.intensity) > 0) {
+            C3 value = (li.intensity / li.pdf) / lw;
+            li.pdf *= lw;
+            if (!iszero(value)) {
+                V3 wi = to_local(fr, li.to_light), wo = to_local(fr, -d);
+                float ct = fabsf(wi.z);
+                // a delta light's sample takes a zero BSDF pdf (PathTracingMIS.cpp:136)
+                float bp = li.delta ? 0.f : bsdf_pdf_t<BT>(B, wi, wo);
+                float w = power_heuristic(li.pdf, bp);
+                C3 contrib = (((T * value) * bsdf_eval_t<BT>(B, wi, wo)) * ct) * w;
+                // The reference traces the shadow ray before it weighs the
+                // sample by the BSDF (Integrator.cpp:176-218); the ray draws
+                // no random numbers, so when the weighted contribution is
+                // exactly zero (e.g. a light direction below an opaque
+                // surface) its outcome cannot change L and it is not traced.
+                if (contrib.r != 0.f || contrib.g != 0.f || contrib.b != 0.f) {
+                    P.W.nee[slot] = f4c(contrib, 0.f);
+                    P.W.sh_o[slot] = f4(fr.p, RT_EPSILON);
+                    P.W.sh_d[slot] = f4(li.to_light, li.distance - RT_EPSILON);
+                    flags |= F_NEE;
+                    push_shadow = true;
+                }
+            }
+        }
+    }
+    // BSDF sampling
+    BsdfRec r;
+    r.wi = to_local(fr, -d); r.wo = v3(0, 0, 0);
+    r.type = BT_ALL; r.rel_eta = 1.f; r.pdf = -1.f;
+    V2 u = next2d(rng);
+    C3 f = bsdf_sample_t<BT>(B, r, u, rng.state);
+    if (iszero(f)) {
+        if (flags & F_NEE) {
+            flags |= F_END;   // the light sample still needs its shadow ray
+            push_end = true;
+        } else {
+            flags |= F_DONE;
+            P.W.out[slot] = f4c(L, 0.f);
+        }
+    } else {
+        P.W.ray_o[slot] = f4(fr.p, RT_EPSILON);
+        P.W.ray_d[slot] = f4(to_world(fr, r.wo), RT_MAX_REAL);
+        P.W.bs[slot] = f4c(f, r.pdf);
+        P.W.rel_eta[slot] = r.rel_eta;
+        if (r.type & BT_DELTA) flags |= F_DELTA; else flags &= ~F_DELTA;
+        push_closest = true;
+    }
+    P.W.rad[slot] = f4c(L, __int_as_float(depth));
+    P.W.tp[slot] = f4c(T, eta);
+    P.W.rng[slot] = rng;
+    P.W.flags[slot] = flags;
+    }
+}
+// MULTI: a multi-scene batch, each path shaded against its own scene
+template <int BT, bool MULTI = false>
 __global__ void __launch_bounds__(128, RT_SHADE_MINB) k_pt_shade(RenderParams P, int round)
 {
     round = cur_round(P, round);
-    const DevScene &S = P.S;
     RoundCounters *C = &P.W.cnt[round];
     RoundCounters *Cout = &P.W.cnt[round + 1];
     const int n = BT == RT_QUEUE_MIXED ? C->mixed : C->mat[BT];
@@ -844,126 +1042,8 @@ __global__ void __launch_bounds__(128, RT_SHADE_MINB) k_pt_shade(RenderParams P,
         int slot = valid ? qin[idx] : 0;
         bool push_end = false, push_closest = false, push_shadow = false;
         if (valid) {
-            Pcg32 rng = P.W.rng[slot];
-            float4 tpv = P.W.tp[slot];
-            C3 T = rgb(tpv);
-            float eta = tpv.w;
-            float4 radv = P.W.rad[slot];
-            C3 L = rgb(radv);
-            int depth = __float_as_int(radv.w);
-            int flags = P.W.flags[slot];
-            float4 ro = P.W.ray_o[slot], rd = P.W.ray_d[slot];
-            V3 o = xyz(ro), d = xyz(rd);
-            float4 hv = P.W.hit[slot];
-            Hit h; h.t = hv.x; h.u = hv.y; h.v = hv.z; h.prim = __float_as_int(hv.w);
-            Frame fr = hit_frame(S, h, o, d);
-            // the mixed queue's BSDF is a copy with its textures applied at
-            // the hit; the sorted queues read the scene's (untextured) BSDF
-            DevBsdf Bl;
-            if (BT == RT_QUEUE_MIXED) {
-                Bl = S.bsdfs[prim_bsdf(S, h.prim)];
-                if (Bl.textured) tex_apply(S, Bl, hit_uv(S, h, o, d));
-            }
-            const DevBsdf &B = BT == RT_QUEUE_MIXED ? Bl : S.bsdfs[prim_bsdf(S, h.prim)];
-            bool done = false;
-            // finish the previous vertex (its light sample and the emission
-            // its BSDF-sampled ray found), update throughput, roulette
-            if (flags & F_FIRST) {
-                flags &= ~F_FIRST;
-                if (depth >= P.max_depth) done = true;
-            } else {
-                if ((flags & F_NEE) && !P.W.occl[slot]) L = L + rgb(P.W.nee[slot]);
-                flags &= ~F_NEE;
-                float4 bsv = P.W.bs[slot];
-                C3 f = rgb(bsv);
-                int nl = prim_light(S, h.prim);
-                if (nl >= 0) {
-                    C3 Le = area_le(S, nl, -d, fr.n);
-                    float pl = (flags & F_DELTA) ? 0.f : light_pdf(S, nl, o, fr.p, fr.n, d);
-                    float w = power_heuristic(bsv.w, pl);
-                    L = L + ((T * Le) * f) * w;
-                }
-                T = T * f;
-                eta *= P.W.rel_eta[slot];
-                if (depth >= P.min_depth) {
-                    float stop = smin(0.95f, lum(T) * eta * eta);
-                    if (next1d(rng) < stop) T = T / stop;
-                    else done = true;
-                }
-                if (!done) {
-                    depth++;
-                    if (depth >= P.max_depth) done = true;
-                }
-            }
-            if (done) {
-                P.W.out[slot] = f4c(L, 0.f);
-                P.W.flags[slot] = flags | F_DONE;
-                P.W.rng[slot] = rng;
-            } else {
-            // emission of a light hit by the camera ray (PathTracingMIS.cpp:73-74)
-            if (depth == 0) {
-                int hl = prim_light(S, h.prim);
-                if (hl >= 0) L = L + T * area_le(S, hl, -d, fr.n);
-            }
-            // light sampling (Integrator::sampleLightDirect, Integrator.cpp:176-218)
-            V2 s = next2d(rng);
-            if (S.n_lights > 0) {
-                float lw;
-                int li_idx = cdf_sample_reuse(S.light_cdf, S.n_lights + 1, s.x, lw);
-                LightRec li;
-                light_sample(S, li_idx, fr.p, s, li);
-                if (li.pdf > 0 && lum(li.intensity) > 0) {
-                    C3 value = (li.intensity / li.pdf) / lw;
-                    li.pdf *= lw;
-                    if (!iszero(value)) {
-                        V3 wi = to_local(fr, li.to_light), wo = to_local(fr, -d);
-                        float ct = fabsf(wi.z);
-                        // a delta light's sample takes a zero BSDF pdf (PathTracingMIS.cpp:136)
-                        float bp = li.delta ? 0.f : bsdf_pdf_t<BT>(B, wi, wo);
-                        float w = power_heuristic(li.pdf, bp);
-                        C3 contrib = (((T * value) * bsdf_eval_t<BT>(B, wi, wo)) * ct) * w;
-                        // The reference traces the shadow ray before it weighs the
-                        // sample by the BSDF (Integrator.cpp:176-218); the ray draws
-                        // no random numbers, so when the weighted contribution is
-                        // exactly zero (e.g. a light direction below an opaque
-                        // surface) its outcome cannot change L and it is not traced.
-                        if (contrib.r != 0.f || contrib.g != 0.f || contrib.b != 0.f) {
-                            P.W.nee[slot] = f4c(contrib, 0.f);
-                            P.W.sh_o[slot] = f4(fr.p, RT_EPSILON);
-                            P.W.sh_d[slot] = f4(li.to_light, li.distance - RT_EPSILON);
-                            flags |= F_NEE;
-                            push_shadow = true;
-                        }
-                    }
-                }
-            }
-            // BSDF sampling
-            BsdfRec r;
-            r.wi = to_local(fr, -d); r.wo = v3(0, 0, 0);
-            r.type = BT_ALL; r.rel_eta = 1.f; r.pdf = -1.f;
-            V2 u = next2d(rng);
-            C3 f = bsdf_sample_t<BT>(B, r, u, rng.state);
-            if (iszero(f)) {
-                if (flags & F_NEE) {
-                    flags |= F_END;   // the light sample still needs its shadow ray
-                    push_end = true;
-                } else {
-                    flags |= F_DONE;
-                    P.W.out[slot] = f4c(L, 0.f);
-                }
-            } else {
-                P.W.ray_o[slot] = f4(fr.p, RT_EPSILON);
-                P.W.ray_d[slot] = f4(to_world(fr, r.wo), RT_MAX_REAL);
-                P.W.bs[slot] = f4c(f, r.pdf);
-                P.W.rel_eta[slot] = r.rel_eta;
-                if (r.type & BT_DELTA) flags |= F_DELTA; else flags &= ~F_DELTA;
-                push_closest = true;
-            }
-            P.W.rad[slot] = f4c(L, __int_as_float(depth));
-            P.W.tp[slot] = f4c(T, eta);
-            P.W.rng[slot] = rng;
-            P.W.flags[slot] = flags;
-            }
+            if (MULTI) pt_shade_path<BT>(P, P.scenes[P.W.sid[slot]], slot, push_end, push_closest, push_shadow);
+            else pt_shade_path<BT>(P, P.S, slot, push_end, push_closest, push_shadow);
         }
         q_push(P.W.q_end, &Cout->end, slot, push_end);
         q_push(P.W.q_closest, &Cout->closest, slot, push_closest);
@@ -1018,6 +1098,51 @@ __global__ void k_film(RenderParams P, float4 *film, int width, int accumulate)
     }
     float4 *px = &film[(size_t)to.y * width + to.x];
     if (accumulate) {
+        float4 o = *px;
+        *px = make_float4(o.x + r, o.y + g, o.z + b, o.w + w);
+    } else {
+        *px = make_float4(0.f + r, 0.f + g, 0.f + b, 0.f + w);
+    }
+    if (nan) atomicAdd(&P.stats[2], (unsigned long long)nan);
+}
+
+// k_film for a multi-scene batch: one thread per batch pixel of any item,
+// reduced in the same order into the item's job film.  A pixel's neighbours
+// lie in its own tile, so in its own item.
+__global__ void k_film_multi(RenderParams P)
+{
+    int gq = blockIdx.x * blockDim.x + threadIdx.x;
+    if (gq >= P.npix) return;
+    int lo = 0, hi = P.n_items - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (P.items[mid].pix0 <= gq) lo = mid; else hi = mid - 1;
+    }
+    const MultiItem &it = P.items[lo];
+    const int q = gq - it.pix0;
+    int4 to = it.tileorder[it.g0 + q];
+    int lx = to.z & 0xffff, ly = to.z >> 16, tw = to.w & 0xffff, th = to.w >> 16;
+    float r = 0.f, g = 0.f, b = 0.f, w = 0.f;
+    int nan = 0;
+    for (int dy = -1; dy <= 1; dy++) {
+        for (int dx = -1; dx <= 1; dx++) {
+            int sx = lx + dx, sy = ly + dy;
+            if (sx < 0 || sy < 0 || sx >= tw || sy >= th) continue;
+            int qs = q + dy * tw + dx;
+            bool self = (dx == 0 && dy == 0);
+            if (!self && !P.W.pix_irregular[it.pix0 + qs]) continue;
+            for (int s = 0; s < it.spp; s++) {
+                int slot = it.path0 + s * it.npix + qs;
+                uint8_t code = P.W.splat[slot];
+                if (!splat_covers(code, -dx, -dy)) continue;
+                float4 L = P.W.out[slot];
+                if (isnan(L.x) || isnan(L.y) || isnan(L.z)) { if (self) nan++; continue; }
+                r += L.x * 1.f; g += L.y * 1.f; b += L.z * 1.f; w += 1.f;
+            }
+        }
+    }
+    float4 *px = &it.film[(size_t)to.y * it.width + to.x];
+    if (it.accumulate) {
         float4 o = *px;
         *px = make_float4(o.x + r, o.y + g, o.z + b, o.w + w);
     } else {
@@ -1218,6 +1343,7 @@ struct rt_ctx {
     int shade_bpsm = RT_SHADE_GRID;   // finish and shading kernels: blocks per SM
     int sort_threshold = 0;     // rounds with fewer closest-hit rays shade unsorted
     int volpath_wave = 1;       // VolPathTracing as the wavefront (0: the megakernel)
+    int batch_wave = 1;         // rt_batch_render: eligible jobs in one multi-scene wavefront
     std::vector<cudaEvent_t> ev_pool;
     std::vector<int> ev_kind;   // kernel kind per recorded pair
     size_t ev_used = 0;
@@ -1239,6 +1365,16 @@ struct rt_ctx {
     };
     std::vector<GraphEntry> gcache;
     int64_t graph_builds = 0, graph_hits = 0;
+    // multi-scene batches (rt_internal_render_multi): scene table, work
+    // items, concatenated tile orders and light CDFs (grown on demand)
+    DevScene *m_scenes = nullptr;
+    size_t m_scenes_n = 0;
+    MultiItem *m_items = nullptr;
+    size_t m_items_n = 0;
+    int4 *m_order = nullptr;
+    size_t m_order_n = 0;
+    float *m_cdf = nullptr;
+    size_t m_cdf_n = 0;
 };
 
 static void graph_cache_clear(rt_ctx *c)
@@ -1504,6 +1640,10 @@ rt_status rt_ctx_destroy(rt_ctx *c)
     if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
     cudaFree(c->tileorder);
     cudaFree(c->work);
+    cudaFree(c->m_scenes);
+    cudaFree(c->m_items);
+    cudaFree(c->m_order);
+    cudaFree(c->m_cdf);
     cudaFree(c->limit_flag);
     cudaFree(c->stats);
     cudaFree(c->light_cdf);
@@ -2098,6 +2238,7 @@ static rt_status ensure_wave(rt_ctx *c, int capacity, int max_rounds)
     for (int t = 0; t < RT_NBSDF; t++) ok &= alloc((void **)&W.q_mat[t], P * sizeof(int));
     ok &= alloc((void **)&W.q_mixed, P * sizeof(int));
     ok &= alloc((void **)&W.cnt, (size_t)(max_rounds + 2) * sizeof(RoundCounters));
+    ok &= alloc((void **)&W.sid, P * sizeof(int));
     ok &= alloc((void **)&W.sort_keys, P * sizeof(unsigned));
     ok &= alloc((void **)&W.sort_tmp, P * sizeof(int));
     ok &= alloc((void **)&W.sort_hist, (size_t)RT_SORT_BINS * sizeof(unsigned));
@@ -2560,6 +2701,285 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
     return RT_OK;
 }
 
+}  // extern "C"
+
+// Grow a device buffer of a context to hold at least `count` elements.
+template <typename T>
+static rt_status grow_buf(T *&buf, size_t &have, size_t count, const char *what)
+{
+    if (have >= count && buf) return RT_OK;
+    cudaFree(buf);
+    buf = nullptr;
+    have = 0;
+    size_t n = std::max<size_t>(count, 16);
+    if (cudaMalloc(&buf, n * sizeof(T)) != cudaSuccess) return fail(RT_ERR_NOMEM, std::string(what) + " allocation failed");
+    have = n;
+    return RT_OK;
+}
+
+// Many PathTracingMIS jobs (scene, render desc, device film) in one
+// wavefront: the path slots of a batch belong to several jobs, each path
+// carries its job's scene-table index, and every kernel reads the path's own
+// scene.  A job's tiles are cut into work items of whole tiles with all
+// their samples; items of all jobs are packed into batches of at most
+// ctx->wave_paths paths.  Each path computes exactly what it computes in
+// rt_render, and each pixel's samples are reduced in order within one
+// batch, so every film equals rt_render's for that job alone.  All jobs
+// share max_depth and min_depth; each has its own seed, sample range,
+// light-selection strategy, block size and film.
+rt_status rt_internal_render_multi(rt_ctx *ctx, rt_scene *const *scenes, const rt_render_desc *descs, int n,
+                                   float *const *films, int32_t on_device)
+{
+    if (!ctx || n <= 0 || !scenes || !descs || !films) return fail(RT_ERR_INVALID, "render_multi: bad argument");
+    const int max_depth = descs[0].max_depth, min_depth = descs[0].min_depth;
+    for (int j = 0; j < n; j++) {
+        const rt_render_desc &rd = descs[j];
+        if (!scenes[j] || !films[j]) return fail(RT_ERR_INVALID, "render_multi: null scene or film");
+        if (rd.spp <= 0 || rd.sample_begin < 0) return fail(RT_ERR_INVALID, "render_multi: bad sample range");
+        if (rd.integrator != RT_INTEGRATOR_PATH_MIS || rd.strategy == RT_STRATEGY_ALL_LIGHTS)
+            return fail(RT_ERR_UNSUPPORTED, "render_multi: PathTracingMIS jobs only (one light per vertex)");
+        if (rd.max_depth != max_depth || rd.min_depth != min_depth)
+            return fail(RT_ERR_UNSUPPORTED, "render_multi: jobs must share max_depth and min_depth");
+        if (rd.max_depth < 0 || rd.min_depth < 0 || rd.max_depth > (1 << 16))
+            return fail(RT_ERR_INVALID, "render_multi: bad depth");
+        if (rd.flags & ~RT_RENDER_ACCUMULATE) return fail(RT_ERR_INVALID, "render_multi: unknown flags");
+        const DevCamera &cam = scenes[j]->S.cam;
+        if (!(cam.filter == RT_FILTER_BOX && cam.frx == 0.5f && cam.fry == 0.5f))
+            return fail(RT_ERR_UNSUPPORTED, "render_multi: box filter of radius 0.5 only");
+        const int bx = rd.block_x > 0 ? rd.block_x : 32, by = rd.block_y > 0 ? rd.block_y : 32;
+        if (bx > 0xffff || by > 0xffff) return fail(RT_ERR_INVALID, "block size too large");
+        if ((int64_t)bx * by * rd.spp > ctx->wave_paths)
+            return fail(RT_ERR_LIMIT, "render_multi: one tile's samples exceed the path capacity");
+    }
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    const int cap = ctx->wave_paths;
+    // per job: tile order (Scene.cpp:83-95 job grid) and light-selection CDF
+    std::vector<int4> orders;
+    std::vector<size_t> order_off(n);
+    std::vector<std::vector<int>> tile_start(n);
+    std::vector<float> cdfs;
+    std::vector<size_t> cdf_off(n);
+    for (int j = 0; j < n; j++) {
+        const rt_render_desc &rd = descs[j];
+        const DevCamera &cam = scenes[j]->S.cam;
+        const int Wd = cam.width, H = cam.height;
+        const int bx = rd.block_x > 0 ? rd.block_x : 32, by = rd.block_y > 0 ? rd.block_y : 32;
+        const int tiles_x = (Wd + bx - 1) / bx, tiles_y = (H + by - 1) / by;
+        order_off[j] = orders.size();
+        tile_start[j].assign(tiles_x * tiles_y + 1, 0);
+        int g = 0;
+        for (int ty = 0; ty < tiles_y; ty++)
+            for (int tx = 0; tx < tiles_x; tx++) {
+                tile_start[j][ty * tiles_x + tx] = g;
+                int ox = tx * bx, oy = ty * by;
+                int tw = std::min(Wd, ox + bx) - ox, th = std::min(H, oy + by) - oy;
+                for (int y = 0; y < th; y++)
+                    for (int x = 0; x < tw; x++, g++) orders.push_back(make_int4(ox + x, oy + y, x | (y << 16), tw | (th << 16)));
+            }
+        tile_start[j][tiles_x * tiles_y] = g;
+        HCdf c;
+        rt_scene *sc = scenes[j];
+        float pu = (float)1. / (float)sc->n_lights;
+        for (int l = 0; l < sc->n_lights; l++)
+            c.add(rd.strategy == RT_STRATEGY_ONE_LIGHT_WEIGHTED ? sc->light_power_lum[l] : pu);
+        c.normalize();
+        cdf_off[j] = cdfs.size();
+        cdfs.insert(cdfs.end(), c.c.begin(), c.c.end());
+        while (cdfs.size() % 16) cdfs.push_back(0.f);
+    }
+    rt_status s;
+    if ((s = grow_buf(ctx->m_order, ctx->m_order_n, orders.size(), "tile order")) != RT_OK) return s;
+    if ((s = grow_buf(ctx->m_cdf, ctx->m_cdf_n, cdfs.size(), "light CDF")) != RT_OK) return s;
+    if ((s = grow_buf(ctx->m_scenes, ctx->m_scenes_n, (size_t)n, "scene table")) != RT_OK) return s;
+    CK(cudaMemcpyAsync(ctx->m_order, orders.data(), orders.size() * sizeof(int4), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(ctx->m_cdf, cdfs.data(), cdfs.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+    std::vector<DevScene> table(n);
+    int types = ctx->sort_threshold > 0 ? 1 << RT_QUEUE_MIXED : 0;
+    for (int j = 0; j < n; j++) {
+        table[j] = scenes[j]->S;
+        table[j].light_cdf = ctx->m_cdf + cdf_off[j];
+        table[j].limit_flag = ctx->limit_flag;
+        types |= scenes[j]->bsdf_types;
+    }
+    CK(cudaMemcpyAsync(ctx->m_scenes, table.data(), (size_t)n * sizeof(DevScene), cudaMemcpyHostToDevice, st));
+    // device films: the caller's, or staging films for host memory
+    std::vector<float4 *> dfilm(n, nullptr);
+    std::vector<void *> staging;
+    auto release = [&]() { for (void *p : staging) cudaFree(p); };
+    for (int j = 0; j < n; j++) {
+        if (on_device) { dfilm[j] = reinterpret_cast<float4 *>(films[j]); continue; }
+        const size_t npix = (size_t)scenes[j]->S.cam.width * scenes[j]->S.cam.height;
+        void *p = nullptr;
+        if (cudaMalloc(&p, npix * sizeof(float4)) != cudaSuccess) { release(); return fail(RT_ERR_NOMEM, "film allocation failed"); }
+        staging.push_back(p);
+        dfilm[j] = (float4 *)p;
+        if (descs[j].flags & RT_RENDER_ACCUMULATE) {
+            cudaError_t e = cudaMemcpyAsync(p, films[j], npix * sizeof(float4), cudaMemcpyHostToDevice, st);
+            if (e != cudaSuccess) { release(); return fail(RT_ERR_CUDA, cudaGetErrorString(e)); }
+        }
+    }
+    // work items: per job, runs of whole tiles of at most `cap` paths
+    struct Item { MultiItem m; int paths; };
+    std::vector<Item> items;
+    for (int j = 0; j < n; j++) {
+        const rt_render_desc &rd = descs[j];
+        const int bx = rd.block_x > 0 ? rd.block_x : 32, by = rd.block_y > 0 ? rd.block_y : 32;
+        const int ntiles = (int)tile_start[j].size() - 1;
+        const int per = std::max(1, cap / std::max(1, bx * by * rd.spp));
+        for (int t0 = 0; t0 < ntiles; t0 += per) {
+            int t1 = std::min(ntiles, t0 + per);
+            Item it;
+            std::memset(&it.m, 0, sizeof(it.m));
+            it.m.job = j;
+            it.m.npix = tile_start[j][t1] - tile_start[j][t0];
+            it.m.spp = rd.spp;
+            it.m.sample_begin = rd.sample_begin;
+            it.m.g0 = tile_start[j][t0];
+            it.m.width = scenes[j]->S.cam.width;
+            it.m.accumulate = (rd.flags & RT_RENDER_ACCUMULATE) ? 1 : 0;
+            it.m.tileorder = ctx->m_order + order_off[j];
+            it.m.film = dfilm[j];
+            it.m.seed = rd.seed;
+            it.paths = it.m.npix * rd.spp;
+            items.push_back(it);
+        }
+    }
+    // batches: items in job order, each batch up to `cap` paths
+    std::vector<std::vector<MultiItem>> batches;
+    std::vector<int> batch_paths, batch_pix;
+    int capacity = 0;
+    for (size_t i = 0; i < items.size();) {
+        std::vector<MultiItem> b;
+        int paths = 0, pix = 0;
+        while (i < items.size() && (b.empty() || paths + items[i].paths <= cap)) {
+            MultiItem m = items[i].m;
+            m.path0 = paths;
+            m.pix0 = pix;
+            paths += items[i].paths;
+            pix += m.npix;
+            b.push_back(m);
+            i++;
+        }
+        capacity = std::max(capacity, paths);
+        batches.push_back(std::move(b));
+        batch_paths.push_back(paths);
+        batch_pix.push_back(pix);
+    }
+    const int max_rounds = max_depth + 3;
+    if ((s = ensure_wave(ctx, capacity, max_rounds)) != RT_OK) { release(); return s; }
+    size_t max_items = 0;
+    for (auto &b : batches) max_items = std::max(max_items, b.size());
+    if ((s = grow_buf(ctx->m_items, ctx->m_items_n, max_items, "work items")) != RT_OK) { release(); return s; }
+    CK(cudaMemsetAsync(ctx->stats, 0, sizeof(unsigned long long) * 8, st));
+    CK(cudaMemsetAsync(ctx->limit_flag, 0, sizeof(int), st));
+    RenderParams P;
+    std::memset(&P, 0, sizeof(P));
+    P.S = scenes[0]->S;
+    P.W = ctx->W;
+    P.max_depth = max_depth;
+    P.min_depth = min_depth;
+    P.limit_flag = ctx->limit_flag;
+    P.stats = ctx->stats;
+    P.sort_threshold = ctx->sort_threshold;
+    P.scenes = ctx->m_scenes;
+    P.items = ctx->m_items;
+    const int sm = ctx->sm_count > 0 ? ctx->sm_count : 1;
+    const int trace_blocks = sm * ctx->trace_bpsm, shade_blocks = sm * ctx->shade_bpsm;
+    int64_t launches = 0, rounds_run = 0, total_paths = 0;
+    ctx->ev_used = 0;
+    CK(cudaEventRecord(ctx->ev0, st));
+    for (size_t bi = 0; bi < batches.size(); bi++) {
+        const std::vector<MultiItem> &b = batches[bi];
+        CK(cudaMemcpyAsync(ctx->m_items, b.data(), b.size() * sizeof(MultiItem), cudaMemcpyHostToDevice, st));
+        P.n_items = (int)b.size();
+        P.n_paths = batch_paths[bi];
+        P.npix = batch_pix[bi];
+        total_paths += P.n_paths;
+        CK(cudaMemsetAsync(ctx->W.pix_irregular, 0, (size_t)P.npix, st));
+        CK(cudaMemsetAsync(ctx->W.cnt, 0, sizeof(RoundCounters) * (size_t)(max_rounds + 2), st));
+        prof_begin(ctx, K_CAMERA);
+        k_camera_multi<<<std::min((P.n_paths + 255) / 256, sm * 16), 256, 0, st>>>(P);
+        prof_end(ctx);
+        launches++;
+        if ((s = launch_check("k_camera_multi")) != RT_OK) { release(); return s; }
+        for (int r = 0; r < max_rounds; r++) {
+            prof_begin(ctx, K_TRACE_C);
+            k_trace<false, false, true><<<trace_blocks, 128, 0, st>>>(P, r);
+            prof_end(ctx);
+            prof_begin(ctx, K_TRACE_A);
+            k_trace<true, false, true><<<trace_blocks, 128, 0, st>>>(P, r);
+            prof_end(ctx);
+            prof_begin(ctx, K_RESOLVE);
+            k_pt_finish<true><<<shade_blocks, 128, 0, st>>>(P, r);
+            prof_end(ctx);
+            prof_begin(ctx, K_SHADE);
+            if (types & 1) k_pt_shade<0, true><<<shade_blocks, 128, 0, st>>>(P, r);
+            if (types & 2) k_pt_shade<1, true><<<shade_blocks, 128, 0, st>>>(P, r);
+            if (types & 4) k_pt_shade<2, true><<<shade_blocks, 128, 0, st>>>(P, r);
+            if (types & 8) k_pt_shade<3, true><<<shade_blocks, 128, 0, st>>>(P, r);
+            if (types & 16) k_pt_shade<4, true><<<shade_blocks, 128, 0, st>>>(P, r);
+            if (types & 32) k_pt_shade<5, true><<<shade_blocks, 128, 0, st>>>(P, r);
+            if (types & (1 << RT_QUEUE_MIXED)) k_pt_shade<RT_QUEUE_MIXED, true><<<shade_blocks, 128, 0, st>>>(P, r);
+            prof_end(ctx);
+            launches += 3 + __builtin_popcount(types);
+            rounds_run++;
+            if ((s = launch_check("multi-scene round")) != RT_OK) { release(); return s; }
+            if ((r & 3) == 3 && r + 1 < max_rounds) {
+                RoundCounters nc;
+                CK(cudaMemcpyAsync(&nc, &ctx->W.cnt[r + 1], sizeof(nc), cudaMemcpyDeviceToHost, st));
+                CK(cudaStreamSynchronize(st));
+                if (nc.closest == 0 && nc.end == 0) break;
+            }
+        }
+        prof_begin(ctx, K_FILM);
+        k_film_multi<<<(P.npix + 127) / 128, 128, 0, st>>>(P);
+        prof_end(ctx);
+        launches++;
+        if ((s = launch_check("k_film_multi")) != RT_OK) { release(); return s; }
+    }
+    CK(cudaEventRecord(ctx->ev1, st));
+    for (int j = 0; j < n && !on_device; j++) {
+        const size_t npix = (size_t)scenes[j]->S.cam.width * scenes[j]->S.cam.height;
+        cudaError_t e = cudaMemcpyAsync(films[j], dfilm[j], npix * sizeof(float4), cudaMemcpyDeviceToHost, st);
+        if (e != cudaSuccess) { release(); return fail(RT_ERR_CUDA, cudaGetErrorString(e)); }
+    }
+    unsigned long long stats[8];
+    int limit = 0;
+    CK(cudaMemcpyAsync(stats, ctx->stats, sizeof(stats), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&limit, ctx->limit_flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    release();
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    std::memset(&ctx->last, 0, sizeof(ctx->last));
+    ctx->last.kernel_ms = ms;
+    double kt[K_KINDS] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (size_t i = 0; i < ctx->ev_used; i++) {
+        float e = 0.f;
+        cudaEventElapsedTime(&e, ctx->ev_pool[2 * i], ctx->ev_pool[2 * i + 1]);
+        kt[ctx->ev_kind[i]] += e;
+    }
+    ctx->last.camera_ms = kt[K_CAMERA];
+    ctx->last.trace_closest_ms = kt[K_TRACE_C];
+    ctx->last.trace_any_ms = kt[K_TRACE_A];
+    ctx->last.shade_ms = kt[K_SHADE] + kt[K_RESOLVE];
+    ctx->last.resolve_ms = kt[K_RESOLVE];
+    ctx->last.film_ms = kt[K_FILM];
+    ctx->last.trace_closest_launches = rounds_run;
+    ctx->last.trace_any_launches = rounds_run;
+    ctx->last.paths = total_paths;
+    ctx->last.closest_rays = (int64_t)stats[0];
+    ctx->last.shadow_rays = (int64_t)stats[1];
+    ctx->last.nan_samples = (int64_t)stats[2];
+    ctx->last.launches = launches;
+    ctx->last.limit_hits = limit;
+    if (limit) return fail(RT_ERR_LIMIT, "a device loop reached its iteration cap");
+    return RT_OK;
+}
+
+extern "C" {
+
 rt_status rt_render_stats_get(const rt_ctx *ctx, rt_render_stats *out)
 {
     if (!ctx || !out) return fail(RT_ERR_INVALID, "null argument");
@@ -2941,6 +3361,16 @@ int rt_internal_device(const rt_ctx *c) { return c->device; }
 int rt_internal_bvh_width(const rt_ctx *c) { return c->bvh_width; }
 int rt_internal_graphs(const rt_ctx *c) { return c->graphs; }
 int rt_internal_volpath_wave(const rt_ctx *c) { return c->volpath_wave; }
+int rt_internal_batch_wave(const rt_ctx *c) { return c->batch_wave; }
+void rt_internal_set_batch_wave(rt_ctx *c, int on) { c->batch_wave = on ? 1 : 0; }
+bool rt_internal_multi_ok(const rt_scene *sc, const rt_render_desc *rd)
+{
+    const DevCamera &cam = sc->S.cam;
+    return rd->integrator == RT_INTEGRATOR_PATH_MIS && rd->strategy != RT_STRATEGY_ALL_LIGHTS && rd->spp > 0 &&
+           rd->sample_begin >= 0 && rd->max_depth >= 0 && rd->min_depth >= 0 && rd->max_depth <= (1 << 16) &&
+           !(rd->flags & ~RT_RENDER_ACCUMULATE) && cam.filter == RT_FILTER_BOX && cam.frx == 0.5f &&
+           cam.fry == 0.5f;
+}
 void rt_internal_set_volpath_wave(rt_ctx *c, int on) { c->volpath_wave = on ? 1 : 0; }
 void rt_internal_get_shape(const rt_ctx *c, int *wave_paths, int *trace_bpsm, int *shade_bpsm, int *sort_threshold)
 {

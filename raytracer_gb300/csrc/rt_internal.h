@@ -21,6 +21,11 @@ RT_HIDDEN void rt_internal_get_shape(const rt_ctx *c, int *wave_paths, int *trac
                                      int *sort_threshold);
 RT_HIDDEN rt_status rt_internal_set_shape(rt_ctx *c, int trace_bpsm, int shade_bpsm, int sort_threshold);
 RT_HIDDEN int rt_internal_volpath_wave(const rt_ctx *c);
+RT_HIDDEN int rt_internal_batch_wave(const rt_ctx *c);
+RT_HIDDEN void rt_internal_set_batch_wave(rt_ctx *c, int on);
+// a job rt_internal_render_multi can take: PathTracingMIS, one light per
+// vertex, the box filter of radius 0.5
+RT_HIDDEN bool rt_internal_multi_ok(const rt_scene *sc, const rt_render_desc *rd);
 RT_HIDDEN void rt_internal_set_volpath_wave(rt_ctx *c, int on);
 RT_HIDDEN void *rt_internal_stream(const rt_ctx *c);
 RT_HIDDEN rt_lane_pool *&rt_internal_pool(rt_ctx *c);
@@ -31,5 +36,10 @@ RT_HIDDEN void rt_internal_film_size(const rt_scene *sc, int *w, int *h);
 RT_HIDDEN rt_status rt_internal_film_sqdiff(rt_ctx *c, const float *a, const float *b, size_t npix, double *mean_sq);
 // dst += src for two device films, queued on the context's stream
 RT_HIDDEN rt_status rt_internal_film_add(rt_ctx *c, float *dst, const float *src, size_t npix);
+
+// many PathTracingMIS jobs in one wavefront (rt_api.cu): films as
+// rt_render writes them for each job alone; jobs share max/min depth
+RT_HIDDEN rt_status rt_internal_render_multi(rt_ctx *ctx, rt_scene *const *scenes, const rt_render_desc *descs, int n,
+                                             float *const *films, int32_t on_device);
 
 RT_HIDDEN void rt_lane_pool_destroy(rt_lane_pool *p);   // rt_serve.cpp

@@ -51,6 +51,7 @@ struct Wave {
     int *sort_tmp;
     unsigned *sort_hist;
     RoundCounters *cnt;
+    int *sid;          // multi-scene batches: scene-table index of the path's job
     int capacity;
     int max_rounds;
     // VolPathTracing wavefront (allocated only for it, vw_capacity paths)
@@ -61,6 +62,26 @@ struct Wave {
     float4 *v_li2;     // light sample: normal at the point
     float4 *v_val;     // light sample intensity, then the attenuated light-sample value
     int vw_capacity;
+};
+
+// One work item of a multi-scene batch (rt_internal_render_multi): whole
+// tiles of one job with every sample of their pixels.  The batch's path
+// slots are the items' slots one after another; within an item, slot
+// path0 + s * npix + q is sample s of the item's pixel q, as in a
+// single-scene batch.
+struct MultiItem {
+    int job;             // scene-table index
+    int path0;           // first path slot of the item
+    int pix0;            // first batch pixel of the item (film threads, pix_irregular)
+    int npix;            // pixels of the item's tiles
+    int spp, sample_begin;
+    int g0;              // first entry of the item's tiles in its job's tile order
+    int width;           // film width of the job
+    int accumulate;      // add to the film instead of writing it
+    int pad;
+    const int4 *tileorder;   // the job's tile-order table
+    float4 *film;            // the job's film (device memory)
+    uint64_t seed;
 };
 
 // batch geometry: tiles [tile0, tile0 + ntiles) of the reference job grid

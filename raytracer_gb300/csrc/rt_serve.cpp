@@ -162,6 +162,7 @@ extern "C" rt_status rt_ctx_get_tuning(rt_ctx *ctx, rt_tuning *out)
     out->lanes = pool->want;
     out->graphs = rt_internal_graphs(ctx);
     out->volpath_wavefront = rt_internal_volpath_wave(ctx);
+    out->batch_wavefront = rt_internal_batch_wave(ctx);
     return RT_OK;
 }
 
@@ -173,12 +174,15 @@ extern "C" rt_status rt_ctx_set_tuning(rt_ctx *ctx, const rt_tuning *t)
     if (t->graphs != 0 && t->graphs != 1) return rt_internal_error(RT_ERR_INVALID, "tuning: graphs must be 0 or 1");
     if (t->volpath_wavefront != 0 && t->volpath_wavefront != 1)
         return rt_internal_error(RT_ERR_INVALID, "tuning: volpath_wavefront must be 0 or 1");
+    if (t->batch_wavefront != 0 && t->batch_wavefront != 1)
+        return rt_internal_error(RT_ERR_INVALID, "tuning: batch_wavefront must be 0 or 1");
     rt_status s = rt_ctx_set_wave_paths(ctx, t->wave_paths);
     if (s == RT_OK) s = rt_internal_set_shape(ctx, t->trace_blocks_per_sm, t->shade_blocks_per_sm, t->sort_threshold);
     if (s == RT_OK) s = rt_ctx_set_lanes(ctx, t->lanes);
     if (s != RT_OK) return s;
     rt_ctx_set_graphs(ctx, t->graphs);
     rt_internal_set_volpath_wave(ctx, t->volpath_wavefront);
+    rt_internal_set_batch_wave(ctx, t->batch_wavefront);
     pool_of(ctx)->set.wave_paths = t->lane_wave_paths;
     return RT_OK;
 }
@@ -197,30 +201,51 @@ extern "C" rt_status rt_batch_render(rt_ctx *ctx, rt_scene *const *scenes, const
     // films) completes before the lanes start on their own streams
     if (cudaStreamSynchronize((cudaStream_t)rt_internal_stream(ctx)) != cudaSuccess)
         return rt_internal_error(RT_ERR_CUDA, "rt_batch_render: stream synchronize failed");
+    // with batch_wavefront: the eligible jobs in one multi-scene wavefront
+    // per (max_depth, min_depth) group on the calling context, the rest on
+    // the lanes at the same time
+    std::vector<int> lane_jobs;
+    std::vector<std::vector<int>> groups;
+    for (int i = 0; i < n; i++) {
+        if (!rt_internal_batch_wave(ctx) || !rt_internal_multi_ok(scenes[i], &descs[i])) {
+            lane_jobs.push_back(i);
+            continue;
+        }
+        bool placed = false;
+        for (auto &g : groups)
+            if (descs[g[0]].max_depth == descs[i].max_depth && descs[g[0]].min_depth == descs[i].min_depth) {
+                g.push_back(i);
+                placed = true;
+                break;
+            }
+        if (!placed) groups.push_back({i});
+    }
     rt_lane_pool *pool = pool_of(ctx);
-    const int k = std::min(pool->want, n);
-    rt_status s = pool->set.grow(k, ctx);
-    if (s != RT_OK) return s;
+    const int nl = (int)lane_jobs.size();
+    const int k = std::min(pool->want, nl);
+    if (k > 0) {
+        rt_status s = pool->set.grow(k, ctx);
+        if (s != RT_OK) return s;
+    }
     // largest job first, so that the long ones do not start last
-    std::vector<int> order(n);
+    std::vector<int> order(lane_jobs);
     std::vector<double> work(n);
     for (int i = 0; i < n; i++) {
         int w = 0, h = 0;
         rt_internal_film_size(scenes[i], &w, &h);
         work[i] = (double)w * h * std::max(1, descs[i].spp) * std::max(1, std::min(descs[i].max_depth, 64));
-        order[i] = i;
     }
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return work[a] > work[b]; });
     std::atomic<int> next(0);
     FirstError err;
-    std::vector<rt_render_stats> lane_stats(k);
+    std::vector<rt_render_stats> lane_stats(std::max(k, 1));
     const double t0 = now_ms();
     auto worker = [&](int li) {
         rt_ctx *lane = pool->set.lanes[li];
         std::memset(&lane_stats[li], 0, sizeof(rt_render_stats));
         for (;;) {
             int j = next.fetch_add(1);
-            if (j >= n) break;
+            if (j >= nl) break;
             int i = order[j];
             rt_status st = rt_render(lane, scenes[i], &descs[i], films[i], on_device);
             if (st != RT_OK) { err.set(st); continue; }
@@ -229,16 +254,30 @@ extern "C" rt_status rt_batch_render(rt_ctx *ctx, rt_scene *const *scenes, const
             add_stats(lane_stats[li], one);
         }
     };
-    if (k == 1) {
-        worker(0);
-    } else {
-        std::vector<std::thread> th;
-        for (int li = 0; li < k; li++) th.emplace_back(worker, li);
-        for (auto &t : th) t.join();
+    std::vector<std::thread> th;
+    for (int li = 0; li < k; li++) th.emplace_back(worker, li);
+    rt_render_stats multi_stats;
+    std::memset(&multi_stats, 0, sizeof(multi_stats));
+    for (auto &g : groups) {
+        std::vector<rt_scene *> gs;
+        std::vector<rt_render_desc> gd;
+        std::vector<float *> gf;
+        for (int i : g) {
+            gs.push_back(scenes[i]);
+            gd.push_back(descs[i]);
+            gf.push_back(films[i]);
+        }
+        rt_status st = rt_internal_render_multi(ctx, gs.data(), gd.data(), (int)g.size(), gf.data(), on_device);
+        if (st != RT_OK) { err.set(st); continue; }
+        rt_render_stats one;
+        rt_render_stats_get(ctx, &one);
+        add_stats(multi_stats, one);
     }
+    for (auto &t : th) t.join();
     rt_render_stats tot;
     std::memset(&tot, 0, sizeof(tot));
-    for (auto &ls : lane_stats) add_stats(tot, ls);
+    for (int li = 0; li < k; li++) add_stats(tot, lane_stats[li]);
+    add_stats(tot, multi_stats);
     tot.kernel_ms = (float)(now_ms() - t0);   // wall time of the whole batch
     rt_internal_set_stats(ctx, tot);
     if (err.status != RT_OK) return rt_internal_error(err.status, err.msg.c_str());

@@ -7,17 +7,21 @@
 // candidate kept if it is at least 2% faster and stays so when it and the
 // incumbent are measured again, two passes over the knobs or until
 // max_trials timed trials.  Every knob leaves the films unchanged (queue
-// capacity, grid sizes, the material-sort threshold, lanes and CUDA
-// graphs), so the choice only trades speed.
+// capacity, grid sizes, the material-sort threshold, lanes, the multi-scene
+// wavefront and CUDA graphs), so the choice only trades speed.
 //
 // The knobs and their candidates:
+//   batch_wavefront      1, 0 (jobs in one multi-scene wavefront, or lanes;
+//                        samples of more than one job)
 //   graphs               0, 1
 //   volpath_wavefront    1, 0 (VolPath as a wavefront or one persistent kernel)
 //   lanes                1, 2, 4, 8 (samples of 32 jobs or more)
 //   sort_threshold       0, 2^12, 2^14, 2^16, 2^18 closest-hit rays
 //   shade blocks per SM  4, 8, 16, 24
 //   trace blocks per SM  8, 10, 12, 16
-//   wave paths           2^20, 2^22, 2^24, 2^26 (lanes: up to 2^25)
+//   wave paths           2^20, 2^22, 2^24, 2^26 (a single render's and the
+//                        multi-scene wavefront's batch capacity)
+//   lane wave paths      2^20, 2^22, 2^24, 2^25 (samples of more than one job)
 #include <algorithm>
 #include <chrono>
 #include <cstring>
@@ -85,6 +89,7 @@ extern "C" rt_status rt_autotune(rt_ctx *ctx, rt_scene *const *scenes, const rt_
     };
     if (st == RT_OK) st = measure(cur, cur_s);
     std::vector<Knob> knobs;
+    if (n > 1) knobs.push_back({&rt_tuning::batch_wavefront, {1, 0}});
     knobs.push_back({&rt_tuning::graphs, {0, 1}});
     knobs.push_back({&rt_tuning::volpath_wavefront, {1, 0}});
     // lanes pay off across many jobs: a sample of fewer than 32 cannot show
@@ -94,7 +99,7 @@ extern "C" rt_status rt_autotune(rt_ctx *ctx, rt_scene *const *scenes, const rt_
     knobs.push_back({&rt_tuning::shade_blocks_per_sm, {4, 8, 16, 24}});
     knobs.push_back({&rt_tuning::trace_blocks_per_sm, {8, 10, 12, 16}});
     if (n > 1) knobs.push_back({&rt_tuning::lane_wave_paths, {1 << 20, 1 << 22, 1 << 24, 1 << 25}});
-    else knobs.push_back({&rt_tuning::wave_paths, {1 << 20, 1 << 22, 1 << 24, 1 << 26}});
+    knobs.push_back({&rt_tuning::wave_paths, {1 << 20, 1 << 22, 1 << 24, 1 << 26}});
     for (int pass = 0; pass < 2 && st == RT_OK && trials < max_trials; pass++) {
         bool changed = false;
         for (const Knob &k : knobs) {

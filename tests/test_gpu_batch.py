@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 import raytracer_gb300 as R
-from raytracer_gb300 import scenes
+from raytracer_gb300 import desc as D, scenes
 
 pytestmark = pytest.mark.gpu
 
@@ -47,6 +47,48 @@ def test_batch_matches_individual_renders(ctx, job_scenes):
     for a, b in zip(films1, films[:2]):
         assert np.array_equal(a, b)
     ctx.set_lanes(4)
+
+
+def test_one_wavefront_equals_lanes(ctx, job_scenes):
+    """rt_tuning.batch_wavefront = 1 runs the PathTracingMIS jobs of a batch
+    in one multi-scene wavefront (path slots of several scenes in each
+    launch); = 0 runs every job as its own rt_render on the lanes.  The films
+    are identical, also when a small wave capacity cuts the jobs into work
+    items over several batches, with accumulation into device films."""
+    torch = pytest.importorskip("torch")
+    jobs = [(job_scenes[n], spp, opt) for n, spp, opt in JOBS]
+    ctx.set_tuning(batch_wavefront=0)
+    try:
+        lanes = ctx.batch_render(jobs)
+    finally:
+        ctx.set_tuning(batch_wavefront=1)
+    one = ctx.batch_render(jobs)
+    st = ctx.stats()
+    for (n, _, _), a, b in zip(JOBS, lanes, one):
+        assert np.array_equal(a, b), n
+    assert st["paths"] == sum(job_scenes[n].width * job_scenes[n].height * spp for n, spp, _ in JOBS)
+    wave = ctx.get_tuning()["wave_paths"]
+    ctx.set_wave_paths(1 << 16)   # 65,536 paths: several batches, jobs split into tile runs
+    try:
+        small = ctx.batch_render(jobs)
+        for (n, _, _), a, b in zip(JOBS, lanes, small):
+            assert np.array_equal(a, b), n
+        # accumulation into device films: samples [0, 2) then [2, 4)
+        big = [(job_scenes["cornell"], 2, dict(seed=5)), (job_scenes["ico"], 2, dict(seed=6))]
+        dev = [torch.zeros((g.height, g.width, 4), dtype=torch.float32, device="cuda") for g, _, _ in big]
+        ptrs = [f.data_ptr() for f in dev]
+        torch.cuda.synchronize()
+        ctx.batch_render(big, device_films=ptrs)
+        second = [(g, spp, dict(opt, sample_begin=2, flags=D.RENDER_ACCUMULATE)) for g, spp, opt in big]
+        ctx.batch_render(second, device_films=ptrs)
+        torch.cuda.synchronize()
+        for (g, _, opt), f in zip(big, dev):
+            ref = g.render(4, seed=opt["seed"])
+            got = f.cpu().numpy()
+            assert np.array_equal(got[..., 3], ref[..., 3])
+            np.testing.assert_allclose(got[..., :3], ref[..., :3], rtol=1e-5, atol=1e-6)
+    finally:
+        ctx.set_wave_paths(wave)
 
 
 def test_batch_with_graphs_matches_individual_renders(ctx, job_scenes):
