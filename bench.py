@@ -476,8 +476,9 @@ def _batch_jobs(n):
 
 def run_batch(args):
     """64 independent scenes: plain (one rt_render per job, one after the
-    other) against rt_batch_render on several lanes and under the autotuner's
-    choice; same films.  The timed runs render into device films allocated
+    other) against rt_batch_render as one wavefront spanning the scenes, on
+    several lanes (a render per job each), and under the autotuner's choice;
+    same films.  The timed runs render into device films allocated
     once (the tuner times the same way); `e2e` is the fastest configuration
     again into host films (device-to-host copies and host allocation
     included)."""
@@ -519,19 +520,29 @@ def run_batch(args):
     plain = films_now()
     res = {}
     default_tuning = ctx.get_tuning()
+    # every job as its own rt_render on 2, 4, 8 worker lanes
+    ctx.set_tuning(batch_wavefront=0)
     for lanes in [int(x) for x in args.lanes.split(",")]:
         ctx.set_lanes(lanes)
         ctx.batch_render(work, device_films=ptrs)   # untimed: grows the new lanes' path buffers
         dt = timed(lambda: ctx.batch_render(work, device_films=ptrs))
         res[lanes] = (dt, all(np.array_equal(a, b) for a, b in zip(films_now(), plain)))
     best = min(res, key=lambda k: res[k][0])
+    best_tuning = dict(default_tuning, lanes=best, batch_wavefront=0)
+    best_s = res[best][0]
+    # all jobs in one wavefront: each launch's path slots span the scenes
+    ctx.set_tuning(**dict(default_tuning, batch_wavefront=1))
+    ctx.batch_render(work, device_films=ptrs)   # untimed: path buffers at the batch capacity
+    wave_s = timed(lambda: ctx.batch_render(work, device_films=ptrs))
+    wave_st = ctx.stats()
+    one_wave = {"value": total / wave_s, "seconds": wave_s, "launches": wave_st["launches"],
+                "films_equal_plain": all(np.array_equal(a, b) for a, b in zip(films_now(), plain))}
+    if wave_s < best_s:
+        best_s, best_tuning = wave_s, dict(default_tuning, batch_wavefront=1)
     # the autotuner on the workload itself (as a farm tunes on its first
-    # batch and keeps the tuning for the next ones: smaller samples did not
-    # carry the 64 jobs' concurrency over the lanes), from the best lane count
+    # batch and keeps the tuning for the next ones), from the best form
     # above, then a fresh timed run of the whole batch under its choice
     tuned = None
-    best_tuning = dict(default_tuning, lanes=best)
-    best_s = res[best][0]
     if not args.no_autotune:
         ctx.set_tuning(**best_tuning)
         t0 = time.perf_counter()
@@ -564,6 +575,7 @@ def run_batch(args):
             "plain": {"value": total / plain_s, "seconds": plain_s},
             "batched": {str(k): {"value": total / v[0], "seconds": v[0], "films_equal_plain": v[1]}
                         for k, v in res.items()},
+            "one_wavefront": one_wave,
             "autotuned": tuned, "default_tuning": default_tuning, "best_tuning": best_tuning,
             "best_lanes": best, "speedup_vs_plain": plain_s / best_s,
             "e2e": {"value": total / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": d2h,

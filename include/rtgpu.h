@@ -477,15 +477,29 @@ rt_status rt_batch_render(rt_ctx *ctx, rt_scene *const *scenes, const rt_render_
 /* Worker lanes of rt_batch_render: 1..16, default 4. */
 rt_status rt_ctx_set_lanes(rt_ctx *ctx, int32_t lanes);
 
-/* Served rendering: a job queue drained by worker lanes (one stream,
- * wavefront buffers and host thread each) on the context's device.  No
- * counterpart in the reference, which renders one scene per process. */
+/* Served rendering, with continuous batching.  No counterpart in the
+ * reference, which renders one scene per process.  PathTracingMIS jobs with
+ * the box filter (rt_render's requirements for one multi-scene wavefront)
+ * are admitted from the queue, in order, while the device budget allows:
+ * a job holds its scene's device bytes (rt_scene_info) and its films (one,
+ * or three for a progressive job) until it finishes, and the wavefront's
+ * and lanes' path state count from the start.  A scheduler thread then runs
+ * steps: each renders the next chunk of every admitted job together in one
+ * wavefront (jobs that arrive meanwhile join at the next step), updates the
+ * progressive estimates and retires finished jobs.  Other jobs run on worker
+ * lanes (one stream, wavefront buffers and host thread each) under the same
+ * budget. */
 typedef struct rt_server rt_server;
 typedef int64_t rt_job_id;
 typedef struct rt_server_opts {
-    int32_t lanes;                /* concurrent jobs, 1..16 (0: 4)                  */
+    int32_t lanes;                /* lanes for jobs the wavefront cannot take,
+                                     1..16 (0: 4)                                   */
     int32_t max_queue;            /* queued jobs before submit fails (0: 4096)      */
-    int64_t device_budget_bytes;  /* film memory of running jobs, 0 = unlimited    */
+    int64_t device_budget_bytes;  /* device memory of path state, admitted jobs'
+                                     scenes and films; 0 = unlimited               */
+    int32_t lanes_only;           /* 0: continuous batching in one wavefront (the
+                                     default); 1: every job on a lane               */
+    int32_t pad;
 } rt_server_opts;
 enum { RT_JOB_QUEUED = 0, RT_JOB_RUNNING = 1, RT_JOB_DONE = 2, RT_JOB_FAILED = 3 };
 typedef struct rt_job_info {
@@ -496,8 +510,9 @@ typedef struct rt_job_info {
     char error[128];              /* RT_JOB_FAILED: rt_last_error of the job        */
 } rt_job_info;
 rt_status rt_server_start(rt_ctx *ctx, const rt_server_opts *opts, rt_server **out);
-/* Queue a render of `scene` (which must outlive the job).  target_rmse <= 0:
- * render desc->spp samples, the film equals rt_render's.  target_rmse > 0:
+/* Queue a render of `scene` (which must outlive the job).  A job whose
+ * scene and films alone exceed the budget is refused (RT_ERR_LIMIT).
+ * target_rmse <= 0: render desc->spp samples, the film equals rt_render's.  target_rmse > 0:
  * render progressively from desc->sample_begin, at most desc->spp samples,
  * until the RMSE of the film's pixel means (rgb / weight, over pixels and
  * channels) estimated from two half films falls to target_rmse. */

@@ -12,9 +12,12 @@
 //                    first, on `lanes` worker contexts: one CUDA stream,
 //                    wavefront buffers and host thread each.  Every film is
 //                    the one rt_render produces for that job alone.
-//   rt_server_*      a job queue served by the same kind of lanes.  A job
-//                    either renders its sample count in one call or, with a
-//                    target RMSE, renders progressively into two films of
+//   rt_server_*      continuous batching: PathTracingMIS jobs are admitted
+//                    by a device-memory budget and rendered chunk by chunk,
+//                    all resident jobs' chunks together in one multi-scene
+//                    wavefront per step; other jobs run on lanes.  A job
+//                    either renders its sample count in one chunk or, with
+//                    a target RMSE, renders progressively into two films of
 //                    interleaved sample ranges until the RMSE estimated
 //                    from their difference meets the target.
 #include <cuda_runtime_api.h>
@@ -295,13 +298,19 @@ struct Job {
     rt_render_desc desc;
     float target = 0.f;
     int w = 0, h = 0;
-    int64_t bytes = 0;
+    int64_t bytes = 0;       // device bytes held while resident: scene + films
     int state = RT_JOB_QUEUED;
     int spp_done = 0;
     float rmse = -1.f;
     double t_submit = 0, t_start = 0, t_end = 0;
     std::vector<float> film;
     std::string error;
+    // continuous batching: device films (progressive: A and B, plain: A),
+    // the next chunk size and the estimate so far
+    bool batched = false;
+    float *A = nullptr, *B = nullptr;
+    int k = 0;
+    double est = -1.0;
 };
 
 }  // namespace
@@ -312,12 +321,17 @@ struct rt_server {
     std::vector<std::thread> threads;
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
-    std::deque<Job *> queue;
+    std::deque<Job *> queue;        // waiting for a lane (jobs the wavefront cannot take)
+    std::deque<Job *> bqueue;       // waiting for admission to the wavefront
+    std::vector<Job *> resident;    // admitted to the wavefront, owned by the scheduler
     std::unordered_map<rt_job_id, Job *> jobs;
     bool stopping = false;
     rt_job_id next_id = 1;
     int max_queue = 4096;
-    int64_t budget = 0, in_flight = 0;
+    int64_t budget = 0, in_flight = 0, fixed = 0;
+    bool wavefront = true;
+    rt_ctx *sched = nullptr;        // the wavefront's context
+    std::thread scheduler;
 };
 
 // One job on one lane.  Plain jobs are a single rt_render.  Progressive
@@ -326,6 +340,15 @@ struct rt_server {
 // the same image; with equal counts the error of their average is
 // |A - B| / 2 per pixel in expectation, and the next chunk is sized from
 // the ratio of that estimate to the target.
+static int next_chunk(const Job *J, int done, double est)
+{
+    const int cap = std::max(2, J->desc.spp);
+    double need = done * (est / J->target) * (est / J->target) * 1.1;
+    int nk = (int)std::ceil((need - done) * 0.5);
+    return std::max(1, std::min(nk, (cap - done) / 2));
+}
+static int first_chunk(const Job *J) { return std::max(1, std::min(std::max(2, J->desc.spp) / 2, 4)); }
+
 static rt_status run_job(rt_ctx *lane, Job *J)
 {
     const size_t npix = (size_t)J->w * J->h;
@@ -345,7 +368,7 @@ static rt_status run_job(rt_ctx *lane, Job *J)
     if (cudaMemsetAsync(A, 0, npix * 16, st) != cudaSuccess || cudaMemsetAsync(B, 0, npix * 16, st) != cudaSuccess)
         s = rt_internal_error(RT_ERR_CUDA, "server: film clear failed");
     const int cap = std::max(2, J->desc.spp);
-    int done = 0, k = std::max(1, std::min(cap / 2, 4));
+    int done = 0, k = first_chunk(J);
     double est = -1.0;
     while (s == RT_OK) {
         rt_render_desc d = J->desc;
@@ -360,9 +383,7 @@ static rt_status run_job(rt_ctx *lane, Job *J)
         if ((s = rt_internal_film_sqdiff(lane, A, B, npix, &msq)) != RT_OK) break;
         est = std::sqrt(msq) * 0.5;
         if (est <= J->target || cap - done < 2) break;
-        double need = done * (est / J->target) * (est / J->target) * 1.1;
-        int nk = (int)std::ceil((need - done) * 0.5);
-        k = std::max(1, std::min(nk, (cap - done) / 2));
+        k = next_chunk(J, done, est);
     }
     if (s == RT_OK) s = rt_internal_film_add(lane, A, B, npix);
     if (s == RT_OK && cudaMemcpyAsync(J->film.data(), A, npix * 16, cudaMemcpyDeviceToHost, st) != cudaSuccess)
@@ -376,6 +397,11 @@ static rt_status run_job(rt_ctx *lane, Job *J)
     return s;
 }
 
+static bool admit_ok(const rt_server *S, const Job *J)
+{
+    return S->budget <= 0 || S->in_flight == 0 || S->fixed + S->in_flight + J->bytes <= S->budget;
+}
+
 static void serve(rt_server *S, int li)
 {
     rt_ctx *lane = S->set.lanes[li];
@@ -387,8 +413,7 @@ static void serve(rt_server *S, int li)
             S->cv_work.wait(g, [&] {
                 if (S->stopping) return true;
                 if (S->queue.empty()) return false;
-                Job *f = S->queue.front();
-                return S->budget <= 0 || S->in_flight == 0 || S->in_flight + f->bytes <= S->budget;
+                return admit_ok(S, S->queue.front());
             });
             if (S->stopping) return;
             J = S->queue.front();
@@ -410,25 +435,166 @@ static void serve(rt_server *S, int li)
     }
 }
 
+// The wavefront's scheduler: continuous batching.  Every step admits the
+// queued jobs that fit the device budget (their scene and films stay
+// resident until they finish), then renders the next chunk of every
+// resident job in one multi-scene wavefront per (max_depth, min_depth)
+// group: a plain job all its samples into its film, a progressive job k
+// samples into film A and the next k into film B (accumulating).  After the
+// step each progressive job re-estimates its RMSE from |A - B| and sizes its
+// next chunk, exactly as on a lane; a job whose estimate meets its target
+// or whose samples are spent leaves with A + B.  A job's chunks depend on
+// its own films only, so its film is the same alone and in any mix.
+static void finish_batched(rt_server *S, Job *J, rt_status s)
+{
+    const size_t npix = (size_t)J->w * J->h;
+    cudaStream_t st = (cudaStream_t)rt_internal_stream(S->sched);
+    if (s == RT_OK && J->target > 0.f) s = rt_internal_film_add(S->sched, J->A, J->B, npix);
+    if (s == RT_OK) {
+        J->film.assign(npix * 4, 0.f);
+        if (cudaMemcpyAsync(J->film.data(), J->A, npix * 16, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess)
+            s = rt_internal_error(RT_ERR_CUDA, "server: film copy failed");
+    }
+    cudaFree(J->A);
+    cudaFree(J->B);
+    J->A = J->B = nullptr;
+    std::lock_guard<std::mutex> g(S->mu);
+    J->t_end = now_ms();
+    J->state = s == RT_OK ? RT_JOB_DONE : RT_JOB_FAILED;
+    if (s != RT_OK) J->error = rt_last_error();
+    S->in_flight -= J->bytes;
+}
+
+static void schedule(rt_server *S)
+{
+    cudaSetDevice(S->set.device);
+    cudaStream_t st = (cudaStream_t)rt_internal_stream(S->sched);
+    for (;;) {
+        std::vector<Job *> fresh;
+        {
+            std::unique_lock<std::mutex> g(S->mu);
+            S->cv_work.wait(g, [&] { return S->stopping || !S->resident.empty() || !S->bqueue.empty(); });
+            if (S->stopping) return;
+            while (!S->bqueue.empty() && admit_ok(S, S->bqueue.front())) {
+                Job *J = S->bqueue.front();
+                S->bqueue.pop_front();
+                J->state = RT_JOB_RUNNING;
+                J->t_start = now_ms();
+                S->in_flight += J->bytes;
+                fresh.push_back(J);
+            }
+        }
+        for (Job *J : fresh) {
+            const size_t npix = (size_t)J->w * J->h;
+            rt_status s = RT_OK;
+            if (cudaMalloc((void **)&J->A, npix * 16) != cudaSuccess ||
+                (J->target > 0.f && cudaMalloc((void **)&J->B, npix * 16) != cudaSuccess))
+                s = rt_internal_error(RT_ERR_NOMEM, "server: film allocation failed");
+            if (s == RT_OK && (cudaMemsetAsync(J->A, 0, npix * 16, st) != cudaSuccess ||
+                               (J->B && cudaMemsetAsync(J->B, 0, npix * 16, st) != cudaSuccess)))
+                s = rt_internal_error(RT_ERR_CUDA, "server: film clear failed");
+            if (s != RT_OK) { finish_batched(S, J, s); S->cv_done.notify_all(); continue; }
+            J->k = J->target > 0.f ? first_chunk(J) : J->desc.spp;
+            S->resident.push_back(J);
+        }
+        if (S->resident.empty()) continue;
+        // one step: the next chunk of every resident job
+        std::vector<std::vector<int>> groups;
+        for (int i = 0; i < (int)S->resident.size(); i++) {
+            const rt_render_desc &d = S->resident[i]->desc;
+            bool placed = false;
+            for (auto &gr : groups)
+                if (S->resident[gr[0]]->desc.max_depth == d.max_depth &&
+                    S->resident[gr[0]]->desc.min_depth == d.min_depth) { gr.push_back(i); placed = true; break; }
+            if (!placed) groups.push_back({i});
+        }
+        std::vector<rt_status> result(S->resident.size(), RT_OK);
+        for (auto &gr : groups) {
+            std::vector<rt_scene *> sc;
+            std::vector<rt_render_desc> ds;
+            std::vector<float *> fs;
+            for (int i : gr) {
+                Job *J = S->resident[i];
+                rt_render_desc d = J->desc;
+                if (J->target > 0.f) {
+                    d.flags |= RT_RENDER_ACCUMULATE;
+                    d.spp = J->k;
+                    d.sample_begin = J->desc.sample_begin + J->spp_done;
+                    sc.push_back(J->scene); ds.push_back(d); fs.push_back(J->A);
+                    d.sample_begin += J->k;
+                    sc.push_back(J->scene); ds.push_back(d); fs.push_back(J->B);
+                } else {
+                    sc.push_back(J->scene); ds.push_back(d); fs.push_back(J->A);
+                }
+            }
+            rt_status s = rt_internal_render_multi(S->sched, sc.data(), ds.data(), (int)sc.size(), fs.data(), 1);
+            for (int i : gr) result[i] = s;
+        }
+        std::vector<Job *> keep;
+        for (size_t i = 0; i < S->resident.size(); i++) {
+            Job *J = S->resident[i];
+            rt_status s = result[i];
+            bool done = s != RT_OK;
+            if (s == RT_OK && J->target > 0.f) {
+                J->spp_done += 2 * J->k;
+                double msq = 0.0;
+                s = rt_internal_film_sqdiff(S->sched, J->A, J->B, (size_t)J->w * J->h, &msq);
+                J->est = std::sqrt(msq) * 0.5;
+                J->rmse = (float)J->est;
+                const int cap = std::max(2, J->desc.spp);
+                if (s != RT_OK || J->est <= J->target || cap - J->spp_done < 2) done = true;
+                else J->k = next_chunk(J, J->spp_done, J->est);
+            } else if (s == RT_OK) {
+                J->spp_done = J->desc.spp;
+                done = true;
+            }
+            if (done) {
+                finish_batched(S, J, s);
+                S->cv_done.notify_all();
+                S->cv_work.notify_all();
+            } else {
+                keep.push_back(J);
+            }
+        }
+        S->resident.swap(keep);
+    }
+}
+
 extern "C" rt_status rt_server_start(rt_ctx *ctx, const rt_server_opts *opts, rt_server **out)
 {
     if (!ctx || !out) return rt_internal_error(RT_ERR_INVALID, "rt_server_start: null argument");
     *out = nullptr;
     int lanes = opts && opts->lanes > 0 ? opts->lanes : 4;
     if (lanes > 16) return rt_internal_error(RT_ERR_INVALID, "rt_server_start: lanes must be in 1..16");
+    if (opts && opts->lanes_only != 0 && opts->lanes_only != 1)
+        return rt_internal_error(RT_ERR_INVALID, "rt_server_start: lanes_only must be 0 or 1");
     rt_server *S = new rt_server();
     S->parent = ctx;
     S->set.device = rt_internal_device(ctx);
     S->max_queue = opts && opts->max_queue > 0 ? opts->max_queue : 4096;
     S->budget = opts ? opts->device_budget_bytes : 0;
+    S->wavefront = !opts || opts->lanes_only == 0;
     S->set.wave_paths = pool_of(ctx)->set.wave_paths;
     rt_status s = S->set.grow(lanes, ctx);
+    if (s == RT_OK && S->wavefront) {
+        s = rt_ctx_create(S->set.device, &S->sched);
+        int wave = 0, tb = 0, sb = 0, thr = 0;
+        rt_internal_get_shape(ctx, &wave, &tb, &sb, &thr);
+        if (s == RT_OK) s = rt_ctx_set_wave_paths(S->sched, wave);
+        if (s == RT_OK) s = rt_internal_set_shape(S->sched, tb, sb, thr);
+        // the wavefront's path state (about 240 bytes per path at its
+        // capacity) and the lanes' count against the budget from the start
+        S->fixed = (int64_t)240 * wave + (int64_t)240 * S->set.wave_paths * lanes;
+    }
     if (s != RT_OK) {
+        if (S->sched) rt_ctx_destroy(S->sched);
         S->set.clear();
         delete S;
         return s;
     }
     for (int li = 0; li < lanes; li++) S->threads.emplace_back(serve, S, li);
+    if (S->wavefront) S->scheduler = std::thread(schedule, S);
     *out = S;
     return RT_OK;
 }
@@ -445,23 +611,28 @@ extern "C" rt_status rt_job_submit(rt_server *S, rt_scene *scene, const rt_rende
     J->desc = *desc;
     J->target = target_rmse;
     rt_internal_film_size(scene, &J->w, &J->h);
-    J->bytes = (int64_t)J->w * J->h * 16 * (target_rmse > 0.f ? 3 : 1);
+    int64_t scene_bytes = 0;
+    float bounds[6];
+    rt_scene_info(scene, bounds, &scene_bytes, nullptr);
+    J->bytes = scene_bytes + (int64_t)J->w * J->h * 16 * (target_rmse > 0.f ? 3 : 1);
+    J->batched = S->wavefront && rt_internal_multi_ok(scene, desc);
     std::lock_guard<std::mutex> g(S->mu);
     if (S->stopping) { delete J; return rt_internal_error(RT_ERR_INVALID, "rt_job_submit: server is stopping"); }
-    if (S->budget > 0 && J->bytes > S->budget) {
+    if (S->budget > 0 && S->fixed + J->bytes > S->budget) {
         delete J;
-        return rt_internal_error(RT_ERR_LIMIT, "rt_job_submit: job film exceeds the device budget");
+        return rt_internal_error(RT_ERR_LIMIT, "rt_job_submit: the job's scene and films exceed the device budget");
     }
-    if ((int)S->queue.size() >= S->max_queue) {
+    if ((int)(S->queue.size() + S->bqueue.size()) >= S->max_queue) {
         delete J;
         return rt_internal_error(RT_ERR_LIMIT, "rt_job_submit: queue full");
     }
     J->id = S->next_id++;
     J->t_submit = now_ms();
     S->jobs[J->id] = J;
-    S->queue.push_back(J);
+    if (J->batched) S->bqueue.push_back(J);
+    else S->queue.push_back(J);
     *id = J->id;
-    S->cv_work.notify_one();
+    S->cv_work.notify_all();
     return RT_OK;
 }
 
@@ -519,10 +690,18 @@ extern "C" rt_status rt_server_stop(rt_server *S)
     }
     S->cv_work.notify_all();
     for (auto &t : S->threads) t.join();
-    // running jobs have finished; queued ones are dropped
+    if (S->scheduler.joinable()) S->scheduler.join();
+    // lanes finish their running jobs; the wavefront stops between steps;
+    // queued and resident jobs are dropped
+    for (Job *J : S->resident) {
+        cudaFree(J->A);
+        cudaFree(J->B);
+    }
+    S->resident.clear();
     for (auto &kv : S->jobs) delete kv.second;
     S->jobs.clear();
     S->set.clear();
+    if (S->sched) rt_ctx_destroy(S->sched);
     delete S;
     return RT_OK;
 }

@@ -158,8 +158,57 @@ def test_server_progressive_meets_target(ctx, job_scenes):
     assert abs(film[..., 3].mean() - info["spp_done"]) <= 0.01 * info["spp_done"]
 
 
+def test_server_progressive_same_alone_and_in_mix(ctx, job_scenes):
+    """Continuous batching: a progressive job sizes its chunks from its own
+    films only, so whatever else shares its steps, it renders the same sample
+    ranges and its film is the same bit for bit.  The mix: two other
+    progressive jobs, plain jobs of three scenes and a VolPath job (on a
+    lane), all submitted together."""
+    g = job_scenes["cornell"]
+    alone_srv = R.Server(ctx, lanes=1)
+    jid = alone_srv.submit(g, 512, target_rmse=0.05, seed=21)
+    alone_info, alone = alone_srv.wait(jid)
+    alone_srv.stop()
+    srv = R.Server(ctx, lanes=2)
+    others = [srv.submit(job_scenes["ico"], 256, target_rmse=0.04, seed=3),
+              srv.submit(job_scenes["ragged"], 3, seed=4, block=8),
+              srv.submit(job_scenes["vol"], 2, seed=5)]
+    jid = srv.submit(g, 512, target_rmse=0.05, seed=21)
+    others += [srv.submit(job_scenes["ico"], 2, seed=7), srv.submit(job_scenes["cornell"], 128, target_rmse=0.08, seed=9)]
+    info, mixed = srv.wait(jid)
+    for o in others:
+        oi, _ = srv.wait(o)
+        assert oi["state"] == R.JOB_DONE, oi
+    srv.stop()
+    print("progressive alone: %d spp, estimate %.4f; in the mix: %d spp, estimate %.4f" %
+          (alone_info["spp_done"], alone_info["rmse_estimate"], info["spp_done"], info["rmse_estimate"]))
+    assert info["spp_done"] == alone_info["spp_done"]
+    assert info["rmse_estimate"] == alone_info["rmse_estimate"]
+    assert np.array_equal(mixed, alone)
+
+
+def test_server_budget_admits_in_order(ctx, job_scenes):
+    """With a device budget that holds the path state and one job's scene and
+    films at a time, jobs are admitted one by one, in order, and every film
+    still equals rt_render's."""
+    g = job_scenes["ico"]
+    nbytes = g.info()["device_bytes"] + g.width * g.height * 16
+    # the lanes' and the wavefront's path state, then room for one job
+    t = ctx.get_tuning()
+    fixed = 240 * t["wave_paths"] + 240 * t["lane_wave_paths"] * 1
+    srv = R.Server(ctx, lanes=1, device_budget_bytes=fixed + nbytes + 1024)
+    jobs = [(g, 2, dict(seed=s)) for s in range(4)]
+    ids = [srv.submit(sc, spp, **o) for sc, spp, o in jobs]
+    for jid, (sc, spp, o) in zip(ids, jobs):
+        info, film = srv.wait(jid)
+        assert info["state"] == R.JOB_DONE
+        assert np.array_equal(film, sc.render(spp, **o))
+    srv.stop()
+
+
 def test_server_queue_states_and_stop(ctx, job_scenes):
-    srv = R.Server(ctx, lanes=1, max_queue=3)
+    """The queue bound and stop on the lanes (every job on a lane)."""
+    srv = R.Server(ctx, lanes=1, max_queue=3, lanes_only=True)
     g = job_scenes["ico"]
     ids = [srv.submit(g, 8, seed=i) for i in range(3)]
     with pytest.raises(R.RtError) as e:   # the queue holds at most 3 (one may already run)
@@ -171,7 +220,7 @@ def test_server_queue_states_and_stop(ctx, job_scenes):
     info, film = srv.wait(ids[0])
     assert info["state"] == R.JOB_DONE and film is not None
     srv.stop()   # drops what is still queued without hanging
-    budget = R.Server(ctx, lanes=1, device_budget_bytes=1024)
+    budget = R.Server(ctx, lanes=1, device_budget_bytes=1024)   # smaller than any job
     with pytest.raises(R.RtError) as e:
         budget.submit(g, 1)
     assert e.value.status == 3
