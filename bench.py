@@ -242,6 +242,69 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def batched_block(ctx_factory, n_jobs=64):
+    """The 64-scene batch (its jobs' scenes, resolutions and sample counts
+    from the batch distribution), rendered into device films allocated once:
+    one rt_render per job one after the other (plain) against rt_batch_render
+    as one multi-scene wavefront.  Films compared bit for bit."""
+    import torch
+    import raytracer_gb300 as R
+    t0 = time.time()
+    jobs = _batch_jobs(n_jobs)
+    ctx = ctx_factory()
+    scs = [R.Scene(ctx, s) for s, _ in jobs]
+    prep = time.time() - t0
+    work = [(g, spp, dict(seed=k)) for k, (g, (_, spp)) in enumerate(zip(scs, jobs))]
+    total = sum(g.width * g.height * spp for g, spp, _ in work)
+    dev = [torch.zeros((g.height, g.width, 4), dtype=torch.float32, device="cuda") for g, _, _ in work]
+    ptrs = [f.data_ptr() for f in dev]
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        fn()
+        torch.cuda.synchronize()
+        return time.perf_counter() - t
+
+    def plain_run():
+        for (g, spp, o), p in zip(work, ptrs):
+            g.render(spp, film=p, **o)
+    plain_run()
+    plain_s = min(timed(plain_run), timed(plain_run))
+    plain = [f.cpu().numpy().copy() for f in dev]
+    ctx.set_tuning(batch_wavefront=1)
+    ctx.batch_render(work, device_films=ptrs)
+    wave_s = min(timed(lambda: ctx.batch_render(work, device_films=ptrs)) for _ in range(2))
+    same = all(np.array_equal(f.cpu().numpy(), p) for f, p in zip(dev, plain))
+    for g in scs:
+        g.close()
+    ctx.close()
+    return {"jobs": len(work), "total_samples": total, "plain_samples_per_s": total / plain_s,
+            "batched_samples_per_s": total / wave_s, "speedup": plain_s / wave_s, "films_equal": same,
+            "form": "one multi-scene wavefront (rt_batch_render, batch_wavefront=1) vs one rt_render per job",
+            "prep_s": round(prep, 1)}
+
+
+def served_block(ctx_factory, rate=20.0, n_jobs=40, pool_pt=8, target=0.02, cap=256):
+    """Served jobs at one Poisson arrival rate: continuous batching against
+    one job at a time, same arrivals, p50/p99 latency to completion and the
+    true RMSE of the finished films against 4096-spp GPU renders."""
+    ctx = ctx_factory()
+    pool, refs = _serve_pool(ctx, pool_pt, 2)
+    rng = np.random.default_rng(7)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n_jobs))
+    picks = [(int(pool_pt + rng.integers(2)) if rng.random() < 0.2 else int(rng.integers(pool_pt)), j)
+             for j in range(n_jobs)]
+    res = {"rate_jobs_per_s": rate, "jobs": n_jobs, "target_rmse": target, "spp_cap": cap,
+           "pool": "%d scenes of the batch distribution + 2 grid-medium scenes, 4096-spp references" % pool_pt}
+    for form in ("plain", "batched"):
+        res[form] = _serve_run(ctx, pool, refs, picks, arrivals, form, target, cap, 4)
+    for g in pool:
+        g.close()
+    ctx.close()
+    return res
+
+
 def run_gpu(args):
     import torch
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -411,6 +474,19 @@ def run_gpu(args):
     bound = "latency/L2" if dom in ("trace_closest", "trace_any") else "latency"
     rays_per_s = (rays_c + rays_a) * world / t_local
     res = {}
+    if rank == 0 and not args.small and args.forms and not CONFIG.get("volume") and not CONFIG.get("smooth"):
+        # the batched and served forms on the same GPU, after the timed region
+        scene.close()
+        del film
+        torch.cuda.empty_cache()
+        try:
+            res["batched"] = batched_block(lambda: R.Context(local))
+        except Exception as ex:
+            res["batched"] = {"failed": str(ex)}
+        try:
+            res["served"] = served_block(lambda: R.Context(local))
+        except Exception as ex:
+            res["served"] = {"failed": str(ex)}
     if rank == 0 and not args.small:
         try:
             cpu_o, tile0, n, stride, _ = cpu_oracle_rate(data, target_s=args.cpu_seconds)
@@ -584,49 +660,85 @@ def run_batch(args):
     print(json.dumps(line))
 
 
-def run_serve(args):
-    """Poisson job arrivals served by rt_server (several lanes) and by a
-    one-lane server (plain, one job after another), same arrival trace,
-    each job rendered progressively to a target RMSE."""
-    import torch
+def _serve_pool(ctx, n_pt, n_vol, ref_spp=4096):
+    """The served stream's scene pool: n_pt scenes of the 64-scene batch
+    distribution (seeded displaced icospheres, 1e3-5e5 triangles, 128^2 to
+    1024^2, the sky map) and n_vol 256x256 grid-medium scenes, each with its
+    ref_spp-sample GPU render as the RMSE reference."""
     import raytracer_gb300 as R
     from raytracer_gb300 import scenes
+    env, _ = scenes.sky_env(1024, 512)
+    pool = []
+    for k in range(n_pt):
+        s, _ = scenes.batch_job(1000 + k, env)
+        pool.append(R.Scene(ctx, s))
+    for k in range(n_vol):
+        pool.append(R.Scene(ctx, scenes.volume_grid(256, 256, res=128, seed=k)))
+    refs = [R.post_process(g.render(ref_spp, seed=999)) for g in pool]
+    return pool, refs
+
+
+def _serve_run(ctx, pool, refs, picks, arrivals, form, target, cap, lanes):
+    """Submit the jobs at their arrival times to a server of the given form;
+    per job: latency to completion (queue + run), samples rendered and the
+    true RMSE of its film against the pool scene's reference."""
+    import raytracer_gb300 as R
+    srv = R.Server(ctx, lanes=1 if form == "plain" else lanes, lanes_only=form != "batched")
+    t0 = time.perf_counter()
+    ids = []
+    for (pi, seed), ta in zip(picks, arrivals):
+        dt = ta - (time.perf_counter() - t0)
+        if dt > 0:
+            time.sleep(dt)
+        g = pool[pi]
+        jcap = 64 if g.data.integrator["integrator"] == 1 else cap
+        ids.append(srv.submit(g, jcap, target_rmse=target, seed=seed))
+    lat, samples, rmse = [], 0, []
+    for j, (pi, _) in zip(ids, picks):
+        info, film = srv.wait(j)
+        lat.append(info["queue_ms"] + info["run_ms"])
+        g = pool[pi]
+        samples += g.width * g.height * info["spp_done"]
+        rmse.append(float(np.sqrt(np.mean((R.post_process(film) - refs[pi]) ** 2))))
+    wall = time.perf_counter() - t0
+    srv.stop()
+    rmse = np.array(rmse)
+    return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "jobs_per_s": len(ids) / wall, "samples_per_s": samples / wall,
+            "true_rmse_p50": float(np.median(rmse)), "true_rmse_p90": float(np.percentile(rmse, 90)),
+            "met_target_frac": float(np.mean(rmse <= target * 1.25))}
+
+
+def run_serve(args):
+    """Open-loop Poisson arrivals at each rate, the same trace for three
+    server forms: plain (one job at a time), lanes (every job a render of
+    its own on 4 lanes) and batched (continuous batching: the chunks of all
+    admitted jobs in one multi-scene wavefront per step).  Jobs render
+    progressively to a target RMSE; latency is submission to completion,
+    and each finished film's true RMSE is measured against its scene's
+    4096-spp GPU render."""
+    import torch
+    import raytracer_gb300 as R
     torch.cuda.init()
-    jobs = _batch_jobs(args.batch_jobs)
-    vols = [scenes.volume_grid(256, 256, res=128, seed=k) for k in range(2)]
     ctx = R.Context(0)
-    pt = [R.Scene(ctx, s) for s, _ in jobs]
-    vo = [R.Scene(ctx, s) for s in vols]
-    ctx.batch_render([(g, 1, dict(seed=0)) for g in pt + vo])
+    t0 = time.time()
+    pool, refs = _serve_pool(ctx, args.serve_pool, max(1, args.serve_pool // 6))
+    prep_s = time.time() - t0
+    n_pt = args.serve_pool
     out = {"metric": "job latency", "unit": "ms", "workload": "serve", "higher_is_better": False,
            "target_rmse": args.target_rmse, "spp_cap": args.spp_cap, "jobs_per_rate": args.serve_jobs,
+           "pool": {"path_mis_scenes": n_pt, "volume_scenes": len(pool) - n_pt, "reference_spp": 4096,
+                    "prep_s": round(prep_s, 1)},
            "rates": {}}
+    forms = [f for f in args.serve_forms.split(",")]
     for lam in [float(x) for x in args.rates.split(",")]:
         rng = np.random.default_rng(int(lam * 10))
         arrivals = np.cumsum(rng.exponential(1.0 / lam, args.serve_jobs))
-        picks = [(vo[rng.integers(len(vo))], 64) if rng.random() < 0.2 else (pt[rng.integers(len(pt))], args.spp_cap)
-                 for _ in range(args.serve_jobs)]
-        rec = {}
-        for name, lanes in (("plain", 1), ("served", args.serve_lanes)):
-            ctx.set_graphs(args.graphs if name == "served" else 0)
-            srv = R.Server(ctx, lanes=lanes)
-            t0 = time.perf_counter()
-            ids = []
-            for (g, cap), ta in zip(picks, arrivals):
-                dt = ta - (time.perf_counter() - t0)
-                if dt > 0:
-                    time.sleep(dt)
-                ids.append(srv.submit(g, cap, target_rmse=args.target_rmse, seed=len(ids)))
-            lat, spp = [], []
-            for j in ids:
-                info, _ = srv.wait(j)
-                lat.append(info["queue_ms"] + info["run_ms"])
-                spp.append(info["spp_done"])
-            wall = time.perf_counter() - t0
-            srv.stop()
-            rec[name] = {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-                         "jobs_per_s": len(ids) / wall, "mean_spp": float(np.mean(spp))}
-        out["rates"][str(lam)] = rec
+        picks = [(int(n_pt + rng.integers(len(pool) - n_pt)) if rng.random() < 0.2 else int(rng.integers(n_pt)), j)
+                 for j in range(args.serve_jobs)]
+        out["rates"][str(lam)] = {f: _serve_run(ctx, pool, refs, picks, arrivals, f, args.target_rmse, args.spp_cap,
+                                                args.serve_lanes) for f in forms}
+        print(json.dumps({"rate": lam, **out["rates"][str(lam)]}), file=sys.stderr, flush=True)
     print(json.dumps(out))
 
 
@@ -637,6 +749,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--forms", type=int, default=1, choices=[0, 1],
+                    help="add the batched (64 scenes) and served (one arrival rate) blocks to the line")
     ap.add_argument("--small", action="store_true",
                     help="profiler case: same scene at 512x512, 8 spp, no CPU baseline, no e2e")
     ap.add_argument("--bvh-width", type=int, default=2, choices=[2, 8],
@@ -658,8 +772,10 @@ def main():
                     help="VolPathTracing as a wavefront of kernels (1) or one persistent kernel (0)")
     ap.add_argument("--filter", default="box", choices=["box", "gaussian", "mitchell"],
                     help="reconstruction filter of the rendered scene (box: radius 0.5)")
-    ap.add_argument("--rates", default="5,20,100", help="serve: arrival rates (jobs/s)")
-    ap.add_argument("--serve-jobs", type=int, default=24, help="serve: jobs per arrival rate")
+    ap.add_argument("--rates", default="5,10,20,50,100,200", help="serve: arrival rates (jobs/s)")
+    ap.add_argument("--serve-jobs", type=int, default=100, help="serve: jobs per arrival rate")
+    ap.add_argument("--serve-pool", type=int, default=24, help="serve: scenes of the batch distribution in the pool")
+    ap.add_argument("--serve-forms", default="plain,lanes,batched", help="serve: server forms to time")
     ap.add_argument("--serve-lanes", type=int, default=4)
     ap.add_argument("--target-rmse", type=float, default=0.02)
     ap.add_argument("--spp-cap", type=int, default=256)

@@ -373,6 +373,14 @@ rt_status rt_scene_info(const rt_scene *scene, float bounds[6], int64_t *device_
 rt_status rt_render(rt_ctx *ctx, rt_scene *scene, const rt_render_desc *rd,
                     float *film_rgbw, int32_t on_device);
 rt_status rt_render_stats_get(const rt_ctx *ctx, rt_render_stats *out);
+/* Radiance (3 floats each) of n path samples: pixel index y * width + x and
+ * absolute sample index, drawn from the same per-path streams and traced
+ * through the same kernels as rt_render.  Stands in for Integrator::li
+ * (integrator/Integrator.h:68) called per sample by SampleJob::run
+ * (core/SampleJob.cpp:46-61): a plugin's li() issues a 1-path launch of the
+ * sample it is asked for.  Not a film: nothing is reduced or splatted. */
+rt_status rt_render_paths(rt_ctx *ctx, rt_scene *scene, const rt_render_desc *rd,
+                          const int32_t *pixels, const int32_t *samples, int32_t n, float *rgb);
 /* Profiling level of later renders: 0 off, 1 per-kernel CUDA-event timing,
  * 2 timing plus BVH traversal counters (slower; for roofline accounting). */
 rt_status rt_ctx_set_profiling(rt_ctx *ctx, int32_t level);

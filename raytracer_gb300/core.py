@@ -90,6 +90,8 @@ def lib():
     L.rt_autotune.argtypes = [vp, C.POINTER(C.c_void_p), C.POINTER(D.RenderDesc), C.c_int32, C.c_int32,
                               C.POINTER(Tuning), C.POINTER(C.c_double)]
     L.rt_trace.argtypes = [vp, vp, vp, C.c_int32, C.c_int32, vp, C.c_int32]
+    L.rt_render_paths.argtypes = [vp, vp, C.POINTER(D.RenderDesc), vp, vp, C.c_int32, vp]
+    L.rt_render_paths.restype = C.c_int32
     L.rt_render_tile_static.argtypes = [vp, vp, C.POINTER(D.RenderDesc), C.c_int32, C.c_int32, vp]
     L.rt_render_tile_static.restype = C.c_int32
     L.rt_bsdf_query.argtypes = [vp, vp, C.c_int32, C.c_int32, vp, C.c_int32, vp]
@@ -302,6 +304,16 @@ class Scene:
         rd = self.data.render_desc(spp, seed=seed, sample_begin=sample_begin, block=block, flags=flags, **over)
         _check(lib().rt_render_tile_static(self.ctx.h, self.h, C.byref(rd), int(tile_x), int(tile_y),
                                            C.c_void_p(int(film_ptr))))
+
+    def render_paths(self, pixels, samples, seed=0, **over):
+        """Radiance (n, 3) of the path samples (pixel index, sample index)
+        through the device kernels (rt_render_paths)."""
+        rd = self.data.render_desc(1, seed=seed, **over)
+        px = np.ascontiguousarray(pixels, np.int32)
+        sm = np.ascontiguousarray(samples, np.int32)
+        out = np.zeros((len(px), 3), np.float32)
+        _check(lib().rt_render_paths(self.ctx.h, self.h, C.byref(rd), _p(px), _p(sm), len(px), _p(out)))
+        return out
 
     def trace(self, rays, anyhit=False):
         rays = np.ascontiguousarray(rays, D.RAY_DTYPE)

@@ -113,6 +113,9 @@ struct RenderParams {
     const DevScene *scenes;
     const MultiItem *items;
     int n_items;
+    // rt_render_paths: slot i renders (pixel path_list[i].x, absolute sample
+    // index path_list[i].y) and is not reduced into a film; null otherwise
+    const int2 *path_list;
 };
 
 __device__ __forceinline__ int cur_round(const RenderParams &P, int round)
@@ -125,21 +128,32 @@ __global__ void k_camera(RenderParams P)
 {
     const DevCamera &cam = P.S.cam;
     for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < P.n_paths; slot += gridDim.x * blockDim.x) {
-        int q = slot % P.npix;
-        int s = slot / P.npix;
-        int4 to = P.tileorder[P.g0 + q];
-        int x = to.x, y = to.y;
-        int lx = to.z & 0xffff, ly = to.z >> 16, tw = to.w & 0xffff, th = to.w >> 16;
+        int q = 0, x, y, lx = 0, ly = 0, tw = 1, th = 1, smp;
+        if (P.path_list) {
+            const int2 pl = P.path_list[slot];
+            x = pl.x % cam.width;
+            y = pl.x / cam.width;
+            smp = pl.y;
+        } else {
+            q = slot % P.npix;
+            int s = slot / P.npix;
+            int4 to = P.tileorder[P.g0 + q];
+            x = to.x; y = to.y;
+            lx = to.z & 0xffff; ly = to.z >> 16; tw = to.w & 0xffff; th = to.w >> 16;
+            smp = P.sample_begin + s;
+        }
         Pcg32 rng;
-        path_stream_seed(rng, P.seed, (uint32_t)(y * cam.width + x), (uint32_t)(P.sample_begin + s));
+        path_stream_seed(rng, P.seed, (uint32_t)(y * cam.width + x), (uint32_t)smp);
         V2 j = next2d(rng);
         float xx = (float)x + j.x, yy = (float)y + j.y;
         V2 lens = v2(0.f, 0.f);
         if (cam.aperture_radius > 0.f) lens = next2d(rng);
         Ray r = camera_ray(cam, xx, yy, lens);
-        uint8_t code = splat_code(xx, yy, x - lx, y - ly, lx, ly, tw, th);
-        P.W.splat[slot] = code;
-        if (code != 0x55) P.W.pix_irregular[q] = 1;
+        if (!P.path_list) {
+            uint8_t code = splat_code(xx, yy, x - lx, y - ly, lx, ly, tw, th);
+            P.W.splat[slot] = code;
+            if (code != 0x55) P.W.pix_irregular[q] = 1;
+        }
         P.W.rng[slot] = rng;
         P.W.ray_o[slot] = f4(r.o, r.mint);
         P.W.ray_d[slot] = f4(r.d, r.maxt);
@@ -2979,6 +2993,132 @@ rt_status rt_internal_render_multi(rt_ctx *ctx, rt_scene *const *scenes, const r
 }
 
 extern "C" {
+
+rt_status rt_render_paths(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, const int32_t *pixels,
+                          const int32_t *samples, int32_t n, float *rgb)
+{
+    if (!ctx || !sc || !rd || n < 0 || (n > 0 && (!pixels || !samples || !rgb)))
+        return fail(RT_ERR_INVALID, "rt_render_paths: bad argument");
+    if (n == 0) return RT_OK;
+    if (rd->integrator != RT_INTEGRATOR_PATH_MIS && rd->integrator != RT_INTEGRATOR_VOLPATH)
+        return fail(RT_ERR_UNSUPPORTED, "rt_render_paths: unknown integrator");
+    if (rd->integrator == RT_INTEGRATOR_PATH_MIS && rd->strategy == RT_STRATEGY_ALL_LIGHTS)
+        return fail(RT_ERR_UNSUPPORTED, "rt_render_paths: all_lights strategy is not provided by the device path");
+    if (rd->max_depth < 0 || rd->min_depth < 0 || rd->max_depth > (1 << 16))
+        return fail(RT_ERR_INVALID, "rt_render_paths: bad depth");
+    const DevCamera &cam = sc->S.cam;
+    const int64_t npix = (int64_t)cam.width * cam.height;
+    std::vector<int2> list(n);
+    for (int i = 0; i < n; i++) {
+        if (pixels[i] < 0 || pixels[i] >= npix || samples[i] < 0)
+            return fail(RT_ERR_INVALID, "rt_render_paths: pixel or sample index out of range");
+        list[i] = make_int2(pixels[i], samples[i]);
+    }
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    HCdf c;
+    {
+        float pu = (float)1. / (float)sc->n_lights;
+        for (int l = 0; l < sc->n_lights; l++)
+            c.add(rd->strategy == RT_STRATEGY_ONE_LIGHT_WEIGHTED ? sc->light_power_lum[l] : pu);
+        c.normalize();
+    }
+    const bool vw = rd->integrator == RT_INTEGRATOR_VOLPATH && ctx->volpath_wave;
+    const int max_rounds = rd->integrator == RT_INTEGRATOR_PATH_MIS ? rd->max_depth + 3 : vw ? (1 << 16) + 2 : 1;
+    rt_status s = ensure_wave(ctx, n, max_rounds);
+    if (s != RT_OK) return s;
+    if (vw && (s = ensure_vw(ctx, n)) != RT_OK) return s;
+    // the list and the light CDF in one temporary buffer
+    void *tmp = nullptr;
+    const size_t list_bytes = (size_t)n * sizeof(int2), cdf_off = (list_bytes + 255) & ~(size_t)255;
+    CK(cudaMalloc(&tmp, cdf_off + c.c.size() * sizeof(float)));
+    std::vector<float4> out(n);
+    auto run = [&]() -> rt_status {
+        CK(cudaMemcpyAsync(tmp, list.data(), list_bytes, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync((char *)tmp + cdf_off, c.c.data(), c.c.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+        CK(cudaMemsetAsync(ctx->limit_flag, 0, sizeof(int), st));
+        CK(cudaMemsetAsync(ctx->W.cnt, 0, sizeof(RoundCounters) * (size_t)(max_rounds + 2), st));
+        RenderParams P;
+        std::memset(&P, 0, sizeof(P));
+        P.S = sc->S;
+        P.S.limit_flag = ctx->limit_flag;
+        P.S.light_cdf = (const float *)((char *)tmp + cdf_off);
+        P.W = ctx->W;
+        P.seed = rd->seed;
+        P.max_depth = rd->max_depth;
+        P.min_depth = rd->min_depth;
+        P.limit_flag = ctx->limit_flag;
+        P.stats = ctx->stats;
+        P.n_paths = n;
+        P.npix = n;
+        P.sort_threshold = ctx->sort_threshold;
+        P.path_list = (const int2 *)tmp;
+        const int sm = ctx->sm_count > 0 ? ctx->sm_count : 1;
+        rt_status e;
+        k_camera<<<std::min((n + 255) / 256, sm * 16), 256, 0, st>>>(P);
+        if ((e = launch_check("k_camera (paths)")) != RT_OK) return e;
+        if (vw) {
+            for (int r = 0; r < max_rounds; r++) {
+                k_vw_trace<<<sm * RT_VW_MINB_TRACE, 128, 0, st>>>(P, r);
+                k_vw_step<<<sm * RT_VW_MINB_STEP, 128, 0, st>>>(P, r);
+                k_vw_shadow<<<sm * RT_VW_MINB_SHADOW, 128, 0, st>>>(P, r);
+                k_vw_sample<<<sm * RT_VW_MINB_SAMPLE, 128, 0, st>>>(P, r);
+                k_vw_trsamp<<<sm * RT_VW_MINB_TRSAMP, 128, 0, st>>>(P, r);
+                k_vw_finish<<<sm * RT_VW_MINB_FINISH, 128, 0, st>>>(P, r);
+                if ((e = launch_check("VolPath round (paths)")) != RT_OK) return e;
+                int nq = 0;
+                CK(cudaMemcpyAsync(&nq, &ctx->W.cnt[r + 1].closest, sizeof(int), cudaMemcpyDeviceToHost, st));
+                CK(cudaStreamSynchronize(st));
+                if (nq == 0) break;
+            }
+        } else if (rd->integrator == RT_INTEGRATOR_VOLPATH) {
+            CK(cudaMemsetAsync(ctx->work, 0, sizeof(int), st));
+            k_volpath<<<sm * RT_VOLPATH_GRID, 128, 0, st>>>(P, ctx->work);
+            if ((e = launch_check("k_volpath (paths)")) != RT_OK) return e;
+        } else {
+            const int types = sc->bsdf_types | (P.sort_threshold > 0 ? 1 << RT_QUEUE_MIXED : 0);
+            const int tb = sm * ctx->trace_bpsm, sb = sm * ctx->shade_bpsm;
+            const bool w8 = ctx->bvh_width == 8 && sc->wide_ok;
+            for (int r = 0; r < max_rounds; r++) {
+                if (w8) {
+                    k_trace8<false, false><<<tb, 128, 0, st>>>(P, r);
+                    k_trace8<true, false><<<tb, 128, 0, st>>>(P, r);
+                } else {
+                    k_trace<false, false><<<tb, 128, 0, st>>>(P, r);
+                    k_trace<true, false><<<tb, 128, 0, st>>>(P, r);
+                }
+                k_pt_finish<<<sb, 128, 0, st>>>(P, r);
+                if (types & 1) k_pt_shade<0><<<sb, 128, 0, st>>>(P, r);
+                if (types & 2) k_pt_shade<1><<<sb, 128, 0, st>>>(P, r);
+                if (types & 4) k_pt_shade<2><<<sb, 128, 0, st>>>(P, r);
+                if (types & 8) k_pt_shade<3><<<sb, 128, 0, st>>>(P, r);
+                if (types & 16) k_pt_shade<4><<<sb, 128, 0, st>>>(P, r);
+                if (types & 32) k_pt_shade<5><<<sb, 128, 0, st>>>(P, r);
+                if (types & (1 << RT_QUEUE_MIXED)) k_pt_shade<RT_QUEUE_MIXED><<<sb, 128, 0, st>>>(P, r);
+                if ((e = launch_check("pt round (paths)")) != RT_OK) return e;
+                RoundCounters nc;
+                CK(cudaMemcpyAsync(&nc, &ctx->W.cnt[r + 1], sizeof(nc), cudaMemcpyDeviceToHost, st));
+                CK(cudaStreamSynchronize(st));
+                if (nc.closest == 0 && nc.end == 0) break;
+            }
+        }
+        CK(cudaMemcpyAsync(out.data(), ctx->W.out, (size_t)n * sizeof(float4), cudaMemcpyDeviceToHost, st));
+        int limit = 0;
+        CK(cudaMemcpyAsync(&limit, ctx->limit_flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (limit) return fail(RT_ERR_LIMIT, "a device loop reached its iteration cap");
+        return RT_OK;
+    };
+    s = run();
+    cudaFree(tmp);
+    if (s != RT_OK) return s;
+    for (int i = 0; i < n; i++) {
+        rgb[3 * i] = out[i].x;
+        rgb[3 * i + 1] = out[i].y;
+        rgb[3 * i + 2] = out[i].z;
+    }
+    return RT_OK;
+}
 
 rt_status rt_render_stats_get(const rt_ctx *ctx, rt_render_stats *out)
 {
