@@ -41,6 +41,7 @@ WORKLOAD = "displaced_icosphere_1310720tri_1024x1024_64spp_depth16_sky1024x512"
 METRIC = "path samples/s"
 UNIT = "samples/s"
 S_NODE = {8: 80,   # bytes per compressed 8-wide node fetch (origin, exponents, links, 8 quantised boxes)
+          4: 112,  # bytes per 4-wide node fetch (four child boxes + links; the 16-byte pad is not read)
           2: 64}   # bytes per BVH2 node fetch (two child boxes + links)
 S_TRI = 36         # bytes per triangle test (three float3 vertices)
 S_RAY_IN = 32      # origin, direction, tmin, tmax
@@ -753,7 +754,7 @@ def main():
                     help="add the batched (64 scenes) and served (one arrival rate) blocks to the line")
     ap.add_argument("--small", action="store_true",
                     help="profiler case: same scene at 512x512, 8 spp, no CPU baseline, no e2e")
-    ap.add_argument("--bvh-width", type=int, default=2, choices=[2, 8],
+    ap.add_argument("--bvh-width", type=int, default=2, choices=[2, 4, 8],
                     help="traversal tree: binary BVH (default) or compressed 8-wide BVH")
     ap.add_argument("--workload", default="icosphere", choices=["icosphere", "volume", "smooth", "batch", "serve"],
                     help="icosphere: the headline single-scene render; batch: 64 scenes, plain vs "

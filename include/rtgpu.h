@@ -384,9 +384,11 @@ rt_status rt_render_paths(rt_ctx *ctx, rt_scene *scene, const rt_render_desc *rd
 /* Profiling level of later renders: 0 off, 1 per-kernel CUDA-event timing,
  * 2 timing plus BVH traversal counters (slower; for roofline accounting). */
 rt_status rt_ctx_set_profiling(rt_ctx *ctx, int32_t level);
-/* Tree used by later renders and rt_trace: 2 (binary BVH, the default) or 8
- * (compressed 8-wide BVH); both report the same closest hits (a tie at equal
- * distance may name another triangle) and the same occlusion. */
+/* Tree used by later renders and rt_trace: 2 (binary BVH, the default), 4
+ * (4-wide BVH collapsed from the binary one, same boxes) or 8 (compressed
+ * 8-wide BVH); all report the same closest hits (a tie at equal distance may
+ * name another triangle) and the same occlusion.  Stands in for the
+ * reference's binary traversal, Bvh::intersection (accelStruct/Bvh.cpp:392-481). */
 rt_status rt_ctx_set_bvh_width(rt_ctx *ctx, int32_t width);
 /* Paths per wavefront batch of later renders (whole tiles x all samples are
  * batched up to this count): 2^16..2^26.  Device memory for path state is
@@ -541,10 +543,11 @@ rt_status rt_server_stop(rt_server *srv);
 rt_status rt_trace(rt_ctx *ctx, rt_scene *scene, const rt_ray *rays, int32_t n,
                    int32_t anyhit, rt_hit *hits, int32_t on_device);
 
-/* Host-only: build the device tree (width 2: binary, 8: compressed 8-wide)
- * over n triangles (9 floats each) as rt_scene_create would, and report its
- * deepest leaf level (root 0) and node count; the binary tree is also
- * checked structurally (RT_ERR_INVALID if malformed).  Stands in for
+/* Host-only: build the device tree (width 2: binary, 4: 4-wide collapsed
+ * from the binary one, 8: compressed 8-wide) over n triangles (9 floats
+ * each) as rt_scene_create would, and report its deepest level (root 0) and
+ * node count; the binary and 4-wide trees are also checked structurally
+ * (RT_ERR_INVALID if malformed).  Stands in for
  * Bvh::build (accelStruct/Bvh.cpp:51-79), whose traversal keeps a fixed
  * stack of 64 (Bvh.cpp:402): the builder here splits at the object median
  * wherever the SAH tree would grow deeper than depth_cap levels (<= 0: the

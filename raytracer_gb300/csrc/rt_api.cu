@@ -37,6 +37,17 @@ static rt_status fail(rt_status st, const std::string &msg)
     g_err = msg;
     return st;
 }
+// RT_ERR_LIMIT message naming the caps whose bits a render read back
+static std::string limit_message(int bits)
+{
+    std::string m = "a device loop reached its iteration cap:";
+    if (bits & RT_LIM_STACK2) m += " BVH2 traversal stack;";
+    if (bits & RT_LIM_STACK4) m += " 4-wide traversal stack;";
+    if (bits & RT_LIM_STACK8) m += " 8-wide group stack;";
+    if (bits & RT_LIM_VOLPATH) m += " VolPathTracing loop cap;";
+    if (bits & RT_LIM_LINK) m += " BVH child link outside the node array;";
+    return m;
+}
 #define CK(call)                                                                       \
     do {                                                                               \
         cudaError_t e_ = (call);                                                       \
@@ -400,6 +411,7 @@ __global__ void __launch_bounds__(128, RT_TRACE_MINB) k_trace(RenderParams P, in
     float lx = 0, hx = 0, ly = 0, hy = 0, lz = 0, hz = 0;   // guarded plane offsets (slab_guard)
     int hprim = -1;
     bool dropped = false;   // a push found the stack full
+    bool bad_link = false;  // a child link outside the node array
 
     for (;;) {
         // ---- fetch rays for lanes whose ray is finished
@@ -447,6 +459,7 @@ __global__ void __launch_bounds__(128, RT_TRACE_MINB) k_trace(RenderParams P, in
         // ---- traversal
         while (node != RT_SENT) {
             while ((unsigned)node < (unsigned)RT_SENT) {
+                if (node >= (MULTI ? ms->n_nodes : S.n_nodes)) { bad_link = true; node = RT_SENT; leaf = 0; break; }
                 if (COUNT) cnt[0]++;
                 const float4 *N = (MULTI ? mnodes : S.nodes) + 4 * (size_t)node;
                 float4 n0 = __ldg(N), n1 = __ldg(N + 1), n2 = __ldg(N + 2);
@@ -530,9 +543,200 @@ __global__ void __launch_bounds__(128, RT_TRACE_MINB) k_trace(RenderParams P, in
         }
     }
     if (threadIdx.x == 0 && blockIdx.x == 0) atomicAdd(&P.stats[ANY ? 1 : 0], (unsigned long long)n);
-    if (dropped && P.limit_flag) atomicExch(P.limit_flag, 1);
+    if (dropped && P.limit_flag) atomicOr(P.limit_flag, RT_LIM_STACK2);
+    if (bad_link && P.limit_flag) atomicOr(P.limit_flag, RT_LIM_LINK);
 #undef SPUSH
 #undef SPOP
+}
+
+// ---------------------------------------------------------------- 4-wide traversal
+// Persistent traversal of the 4-wide BVH (rt_bvh.h), built like k_trace:
+// while-while node and leaf phases, postponed leaves, lanes that finish a
+// ray take the next one from the queue.  A node visit tests its four child
+// boxes with the BVH2's fused slab test and guards, sorts the hit children
+// by entry distance (4-key network on (distance bits | slot)), descends into
+// the nearest and pushes the others far to near.  Half as many dependent
+// node fetches per ray as the binary tree, for about twice the arithmetic
+// per fetch.  The boxes are the BVH2's, so the same triangles are tested
+// against the same rays: closest hits and occlusion equal the BVH2's (a tie
+// at exactly equal distance may name another triangle).
+#ifndef RT_STACK4
+#define RT_STACK4 96
+#endif
+#ifndef RT_TRACE4_MINB
+#define RT_TRACE4_MINB 8
+#endif
+
+// Key of child `slot` of a 4-wide node: its near and far planes per axis
+// (chosen by the ray's direction signs) through the BVH2's guarded slab
+// test.  A hit child's key orders by entry distance; a miss sorts last.
+__device__ __forceinline__ unsigned box4_key(float xn, float xf, float yn, float yf, float zn, float zf, unsigned slot,
+                                             float idx, float idy, float idz, float nx, float fx, float ny, float fy,
+                                             float nz, float fz, float tmin, float tmax)
+{
+    const float tn = rt_max3(__fmaf_rn(xn, idx, nx), __fmaf_rn(yn, idy, ny), fmaxf(__fmaf_rn(zn, idz, nz), tmin));
+    const float tf = rt_min3(__fmaf_rn(xf, idx, fx), __fmaf_rn(yf, idy, fy), fminf(__fmaf_rn(zf, idz, fz), tmax));
+    return tn <= tf ? ((__float_as_uint(tn) & ~3u) | slot) : 0xffffffffu;
+}
+
+__device__ __forceinline__ int link4(const int4 &cc, unsigned key)
+{
+    const unsigned s = key & 3u;
+    return s == 0 ? cc.x : s == 1 ? cc.y : s == 2 ? cc.z : cc.w;
+}
+
+template <bool ANY, bool COUNT>
+__global__ void __launch_bounds__(128, RT_TRACE4_MINB) k_trace4(RenderParams P, int round)
+{
+    round = cur_round(P, round);
+    const DevScene S = P.S;
+    RoundCounters *C = &P.W.cnt[round];
+    const int n = ANY ? C->shadow : C->closest;
+    int *wc = ANY ? &C->wc_shadow : &C->wc_closest;
+    const int *queue = ANY ? P.W.q_shadow : P.W.q_closest;
+    const int lane = threadIdx.x & 31;
+    int cnt[2] = {0, 0};
+
+    int stack[RT_STACK4];
+    int sp = 0;
+    int node = RT_SENT, leaf = 0;
+    int slot = -1;
+    bool has_ray = false;
+    float ox = 0, oy = 0, oz = 0, dx = 0, dy = 0, dz = 0, idx = 0, idy = 0, idz = 0;
+    float tmin = 0, hit_t = 0, hu = 0, hv = 0;
+    float nx = 0, fx = 0, ny = 0, fy = 0, nz = 0, fz = 0;   // near / far plane offsets (slab_guard)
+    int sx = 0, sy = 0, sz = 0;                             // 1: the axis's near plane is the box's upper one
+    int hprim = -1;
+    bool dropped = false;   // a push found the stack full
+    bool bad_link = false;  // a child link outside the node array
+
+    for (;;) {
+        // ---- fetch rays for lanes whose ray is finished
+        const bool terminated = (node == RT_SENT);
+        const unsigned mterm = __ballot_sync(0xffffffffu, terminated);
+        const int nterm = __popc(mterm);
+        int base = 0;
+        if (nterm) {
+            const int leader = __ffs(mterm) - 1;
+            if (lane == leader) base = atomicAdd(wc, nterm);
+            base = __shfl_sync(0xffffffffu, base, leader);
+        }
+        if (terminated) {
+            int q = base + __popc(mterm & ((1u << lane) - 1));
+            has_ray = q < n;
+            if (has_ray) {
+                slot = queue[q];
+                float4 o4 = ANY ? P.W.sh_o[slot] : P.W.ray_o[slot];
+                float4 d4 = ANY ? P.W.sh_d[slot] : P.W.ray_d[slot];
+                ox = o4.x; oy = o4.y; oz = o4.z; dx = d4.x; dy = d4.y; dz = d4.z;
+                tmin = adapt_mint(v3(ox, oy, oz), o4.w);
+                hit_t = d4.w;
+                hprim = -1;
+                const float eps = 1e-20f;
+                idx = 1.0f / (fabsf(dx) > eps ? dx : copysignf(eps, dx));
+                idy = 1.0f / (fabsf(dy) > eps ? dy : copysignf(eps, dy));
+                idz = 1.0f / (fabsf(dz) > eps ? dz : copysignf(eps, dz));
+                const float oox = ox * idx, ooy = oy * idy, ooz = oz * idz;
+                nx = -(oox + slab_guard(oox)); fx = -(oox - slab_guard(oox));
+                ny = -(ooy + slab_guard(ooy)); fy = -(ooy - slab_guard(ooy));
+                nz = -(ooz + slab_guard(ooz)); fz = -(ooz - slab_guard(ooz));
+                sx = idx < 0.f; sy = idy < 0.f; sz = idz < 0.f;
+                sp = 0;
+                stack[sp++] = RT_SENT;
+                leaf = 0;
+                node = (S.n_nodes4 > 0 && !(hit_t < tmin)) ? 0 : RT_SENT;
+            }
+        }
+        if (!__any_sync(0xffffffffu, has_ray)) break;
+
+        // ---- traversal
+        while (node != RT_SENT) {
+            while ((unsigned)node < (unsigned)RT_SENT) {
+                if (node >= S.n_nodes4) { bad_link = true; node = RT_SENT; leaf = 0; break; }
+                if (COUNT) cnt[0]++;
+                const float4 *N = S.nodes4 + 8 * (size_t)node;
+                // near / far plane rows of each axis by the ray's direction sign
+                const float4 xn = __ldg(N + sx), xf = __ldg(N + 1 - sx);
+                const float4 yn = __ldg(N + 2 + sy), yf = __ldg(N + 3 - sy);
+                const float4 zn = __ldg(N + 4 + sz), zf = __ldg(N + 5 - sz);
+                const int4 cc = __ldg(reinterpret_cast<const int4 *>(N + 6));
+                unsigned k0 = box4_key(xn.x, xf.x, yn.x, yf.x, zn.x, zf.x, 0u, idx, idy, idz, nx, fx, ny, fy, nz, fz, tmin, hit_t);
+                unsigned k1 = box4_key(xn.y, xf.y, yn.y, yf.y, zn.y, zf.y, 1u, idx, idy, idz, nx, fx, ny, fy, nz, fz, tmin, hit_t);
+                unsigned k2 = box4_key(xn.z, xf.z, yn.z, yf.z, zn.z, zf.z, 2u, idx, idy, idz, nx, fx, ny, fy, nz, fz, tmin, hit_t);
+                unsigned k3 = box4_key(xn.w, xf.w, yn.w, yf.w, zn.w, zf.w, 3u, idx, idy, idz, nx, fx, ny, fy, nz, fz, tmin, hit_t);
+#define RT_CSWAP(a, b)                  \
+    do {                                \
+        const unsigned t_ = umin(a, b); \
+        b = umax(a, b);                 \
+        a = t_;                         \
+    } while (0)
+                RT_CSWAP(k0, k1); RT_CSWAP(k2, k3); RT_CSWAP(k0, k2); RT_CSWAP(k1, k3); RT_CSWAP(k1, k2);
+#undef RT_CSWAP
+                if (k0 == 0xffffffffu) {
+                    node = stack[--sp];
+                } else {
+                    // push the farther hits, farthest first
+                    if (k3 != 0xffffffffu) { if (sp < RT_STACK4) stack[sp++] = link4(cc, k3); else dropped = true; }
+                    if (k2 != 0xffffffffu) { if (sp < RT_STACK4) stack[sp++] = link4(cc, k2); else dropped = true; }
+                    if (k1 != 0xffffffffu) { if (sp < RT_STACK4) stack[sp++] = link4(cc, k1); else dropped = true; }
+                    node = link4(cc, k0);
+                }
+                // first leaf found: postpone it and keep traversing
+                if (node < 0 && leaf >= 0) { leaf = node; node = stack[--sp]; }
+                if (!__any_sync(__activemask(), leaf >= 0)) break;
+            }
+            // ---- postponed leaves
+            while (leaf < 0) {
+                int v = ~leaf;
+                int first = v >> 3, cl = (v & 7) + 1;
+                for (int i = 0; i < cl; i++) {
+                    if (COUNT) cnt[1]++;
+                    const float4 *T = S.tri_slots + 3 * (size_t)(first + i);
+                    float4 a = __ldg(T), b = __ldg(T + 1), c = __ldg(T + 2);
+                    float t, u, w;
+                    if (mt_test(a, b, c, v3(ox, oy, oz), v3(dx, dy, dz), tmin, hit_t, t, u, w)) {
+                        hit_t = t; hu = u; hv = w; hprim = __float_as_int(a.w);
+                        if (ANY) { node = RT_SENT; break; }
+                    }
+                }
+                if (ANY && node == RT_SENT && hprim >= 0) { leaf = 0; break; }
+                leaf = node;
+                if (node < 0) node = stack[--sp];
+            }
+            if (__popc(__activemask()) < RT_FETCH_THRESHOLD) break;
+        }
+        // ---- finished rays: analytic spheres, then store
+        if (node == RT_SENT && has_ray) {
+            if (!(ANY && hprim >= 0)) {
+                for (int si = 0; si < S.n_spheres; si++) {
+                    float t;
+                    if (analytic_test(S.spheres[si], v3(ox, oy, oz), v3(dx, dy, dz), tmin, hit_t, t)) {
+                        hit_t = t; hu = 0.f; hv = 0.f; hprim = -si - 2;
+                        if (ANY) break;
+                    }
+                }
+            }
+            if (ANY) P.W.occl[slot] = hprim != -1 ? 1 : 0;
+            else {
+                P.W.hit[slot] = make_float4(hit_t, hu, hv, __int_as_float(hprim));
+                classify_hit(P, S, C, slot, hprim, n);
+            }
+            has_ray = false;
+        }
+    }
+    if (COUNT) {
+        for (int off = 16; off > 0; off >>= 1) {
+            cnt[0] += __shfl_down_sync(0xffffffffu, cnt[0], off);
+            cnt[1] += __shfl_down_sync(0xffffffffu, cnt[1], off);
+        }
+        if (lane == 0) {
+            atomicAdd(&P.stats[ANY ? 5 : 3], (unsigned long long)cnt[0]);
+            atomicAdd(&P.stats[ANY ? 6 : 4], (unsigned long long)cnt[1]);
+        }
+    }
+    if (threadIdx.x == 0 && blockIdx.x == 0) atomicAdd(&P.stats[ANY ? 1 : 0], (unsigned long long)n);
+    if (dropped && P.limit_flag) atomicOr(P.limit_flag, RT_LIM_STACK4);
+    if (bad_link && P.limit_flag) atomicOr(P.limit_flag, RT_LIM_LINK);
 }
 
 // ---------------------------------------------------------------- 8-wide traversal
@@ -742,7 +946,7 @@ __global__ void __launch_bounds__(128, 8) k_trace8(RenderParams P, int round)
         }
     }
     if (threadIdx.x == 0 && blockIdx.x == 0) atomicAdd(&P.stats[ANY ? 1 : 0], (unsigned long long)n);
-    if (dropped && P.limit_flag) atomicExch(P.limit_flag, 1);
+    if (dropped && P.limit_flag) atomicOr(P.limit_flag, RT_LIM_STACK8);
 }
 
 // rays of the rt_trace test hook into the wavefront buffers, and back
@@ -1349,7 +1553,7 @@ struct rt_ctx {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     rt_render_stats last;
     int profiling = 0;
-    int bvh_width = 2;          // traversal used by renders and rt_trace: 2 or 8
+    int bvh_width = 2;          // traversal used by renders and rt_trace: 2, 4 or 8
     int wave_paths = 1 << 26;   // target paths per wavefront batch (about 14 GB of path state)
     int ray_sort = 0;           // reorder secondary and shadow rays before tracing
     // launch shapes and the material-sort threshold (rt_ctx_set_tuning)
@@ -1433,10 +1637,30 @@ struct rt_scene {
     int bsdf_types = 0;   // bit q set when some BSDF uses shading queue q (bsdf_queue)
     int wide_depth = 0;
     bool wide_ok = false;  // the 8-wide BVH is uploaded (or the scene has no triangles)
+    bool w4_ok = false;    // the 4-wide BVH is uploaded (or the scene has no triangles)
     std::vector<float> light_power_lum;  // per light, for the weighted strategy
     std::vector<DevLight> lights_host;
     DevLight *lights_dev = nullptr;
 };
+
+// Traversal of a scene under the context's tree width (rt_ctx_set_bvh_width):
+// the 8- or 4-wide tree where the scene has it uploaded, else the binary one.
+static int trace_width(const rt_ctx *ctx, const rt_scene *sc);
+// One closest-hit (any = false) or shadow-ray (any = true) traversal launch
+// of round r; count adds the node / triangle fetch counters.
+static void launch_trace(int width, const RenderParams &P, int r, bool any, bool count, int blocks, cudaStream_t st)
+{
+    if (width == 8) {
+        if (any) { if (count) k_trace8<true, true><<<blocks, 128, 0, st>>>(P, r); else k_trace8<true, false><<<blocks, 128, 0, st>>>(P, r); }
+        else { if (count) k_trace8<false, true><<<blocks, 128, 0, st>>>(P, r); else k_trace8<false, false><<<blocks, 128, 0, st>>>(P, r); }
+    } else if (width == 4) {
+        if (any) { if (count) k_trace4<true, true><<<blocks, 128, 0, st>>>(P, r); else k_trace4<true, false><<<blocks, 128, 0, st>>>(P, r); }
+        else { if (count) k_trace4<false, true><<<blocks, 128, 0, st>>>(P, r); else k_trace4<false, false><<<blocks, 128, 0, st>>>(P, r); }
+    } else {
+        if (any) { if (count) k_trace<true, true><<<blocks, 128, 0, st>>>(P, r); else k_trace<true, false><<<blocks, 128, 0, st>>>(P, r); }
+        else { if (count) k_trace<false, true><<<blocks, 128, 0, st>>>(P, r); else k_trace<false, false><<<blocks, 128, 0, st>>>(P, r); }
+    }
+}
 
 template <typename T>
 static rt_status upload(rt_scene *sc, const T *host, size_t count, const T **dev)
@@ -1681,7 +1905,7 @@ rt_status rt_ctx_set_profiling(rt_ctx *c, int32_t level)
 rt_status rt_ctx_set_bvh_width(rt_ctx *c, int32_t width)
 {
     if (!c) return fail(RT_ERR_INVALID, "null ctx");
-    if (width != 2 && width != 8) return fail(RT_ERR_INVALID, "BVH width must be 2 or 8");
+    if (width != 2 && width != 4 && width != 8) return fail(RT_ERR_INVALID, "BVH width must be 2, 4 or 8");
     c->bvh_width = width;
     return RT_OK;
 }
@@ -2052,6 +2276,17 @@ rt_status rt_scene_create(rt_ctx *ctx, const rt_scene_desc *d, rt_scene **out)
     if ((st = upload(sc, reinterpret_cast<const float4 *>(img.tri_slots.data()), (size_t)img.n_slots * 3, &tp)) != RT_OK) { rt_scene_destroy(sc); return st; }
     S.nodes = np; S.tri_slots = tp; S.n_nodes = img.n_nodes;
     {
+        // the 4-wide traversal pushes up to three children per level; a tree
+        // too deep for its stack is not uploaded and renders use the BVH2
+        Bvh4Image w4;
+        build_bvh4(img, w4);
+        if (nt > 0 && 3 * (w4.max_depth + 1) + 1 > RT_STACK4) w4 = Bvh4Image();
+        const float4 *n4 = nullptr;
+        if ((st = upload(sc, reinterpret_cast<const float4 *>(w4.nodes.data()), (size_t)w4.n_nodes * 8, &n4)) != RT_OK) { rt_scene_destroy(sc); return st; }
+        S.nodes4 = n4; S.n_nodes4 = w4.n_nodes;
+        sc->w4_ok = nt == 0 || w4.n_nodes > 0;
+    }
+    {
         WideBvhImage wimg;
         build_wbvh8(tri_v.data(), nt, wimg, 32);
         // the group stack holds one entry per level and node indices < 2^23;
@@ -2161,7 +2396,7 @@ rt_status rt_scene_create(rt_ctx *ctx, const rt_scene_desc *d, rt_scene **out)
 rt_status rt_bvh_stats(const float *tri_v, int32_t n, int32_t width, int32_t depth_cap, int32_t *max_depth,
                        int32_t *n_nodes)
 {
-    if (n < 0 || (n > 0 && !tri_v) || (width != 2 && width != 8) || depth_cap > RT_BVH_DEPTH_CAP)
+    if (n < 0 || (n > 0 && !tri_v) || (width != 2 && width != 4 && width != 8) || depth_cap > RT_BVH_DEPTH_CAP)
         return fail(RT_ERR_INVALID, "rt_bvh_stats: bad argument");
     if (depth_cap <= 0) depth_cap = RT_BVH_DEPTH_CAP;
     if (n > 0 && (int64_t(1) << std::min(depth_cap, 62)) < (int64_t)n)
@@ -2174,6 +2409,16 @@ rt_status rt_bvh_stats(const float *tri_v, int32_t n, int32_t width, int32_t dep
         int walked = 0;
         if (!check_bvh2(img, tri_v, n, &walked, &why)) return fail(RT_ERR_INVALID, "rt_bvh_stats: malformed tree: " + why);
         d = img.max_depth; nn = img.n_nodes;
+    } else if (width == 4) {
+        BvhImage img;
+        build_bvh2(tri_v, n, img, RT_BVH_LEAF, RT_BVH_BINS, RT_BVH_CNODE, depth_cap);
+        std::string why;
+        int walked = 0;
+        if (!check_bvh2(img, tri_v, n, &walked, &why)) return fail(RT_ERR_INVALID, "rt_bvh_stats: malformed tree: " + why);
+        Bvh4Image w4;
+        build_bvh4(img, w4);
+        if (!check_bvh4(w4, img, &why)) return fail(RT_ERR_INVALID, "rt_bvh_stats: malformed 4-wide tree: " + why);
+        d = w4.max_depth; nn = w4.n_nodes;
     } else {
         WideBvhImage img;
         build_wbvh8(tri_v, n, img, 32, depth_cap);
@@ -2300,19 +2545,19 @@ static rt_status pt_batch_graph(rt_ctx *ctx, rt_scene *sc, const RenderParams &P
     const int sm = ctx->sm_count > 0 ? ctx->sm_count : 1;
     const int cam_blocks = std::min((P.n_paths + 255) / 256, sm * 16);
     const int trace_blocks = sm * ctx->trace_bpsm, shade_blocks = sm * ctx->shade_bpsm;
-    const bool w8 = ctx->bvh_width == 8 && sc->wide_ok;
+    const int width = trace_width(ctx, sc);
     const int types = sc->bsdf_types | (P.sort_threshold > 0 ? 1 << RT_QUEUE_MIXED : 0);
     const size_t npix_all = (size_t)Wd * sc->S.cam.height;
     struct Tail {
         const void *film;
         int box, accumulate, wd, t0, t1, tiles_x, bx, by, max_rounds, round_buf, cam_blocks, trace_blocks,
-            shade_blocks, w8, types, vw;
+            shade_blocks, width, types, vw;
     } tail;
     std::memset(&tail, 0, sizeof(tail));
     tail.film = film; tail.box = box_film; tail.accumulate = accumulate; tail.wd = Wd; tail.t0 = t0; tail.t1 = t1;
     tail.tiles_x = tiles_x; tail.bx = bx; tail.by = by; tail.max_rounds = max_rounds; tail.round_buf = round_buf;
     tail.cam_blocks = cam_blocks; tail.trace_blocks = trace_blocks; tail.shade_blocks = shade_blocks;
-    tail.w8 = w8; tail.types = types; tail.vw = vw;
+    tail.width = width; tail.types = types; tail.vw = vw;
     std::vector<unsigned char> key(sizeof(RenderParams) + sizeof(Tail));
     std::memcpy(key.data(), &P, sizeof(RenderParams));
     std::memcpy(key.data() + sizeof(RenderParams), &tail, sizeof(Tail));
@@ -2367,13 +2612,8 @@ static rt_status pt_batch_graph(rt_ctx *ctx, rt_scene *sc, const RenderParams &P
                 k_vw_trsamp<<<sm * RT_VW_MINB_TRSAMP, 128, 0, bs>>>(P, 0);
                 k_vw_finish<<<sm * RT_VW_MINB_FINISH, 128, 0, bs>>>(P, 0);
             } else {
-                if (w8) {
-                    k_trace8<false, false><<<trace_blocks, 128, 0, bs>>>(P, 0);
-                    k_trace8<true, false><<<trace_blocks, 128, 0, bs>>>(P, 0);
-                } else {
-                    k_trace<false, false><<<trace_blocks, 128, 0, bs>>>(P, 0);
-                    k_trace<true, false><<<trace_blocks, 128, 0, bs>>>(P, 0);
-                }
+                launch_trace(width, P, 0, false, false, trace_blocks, bs);
+                launch_trace(width, P, 0, true, false, trace_blocks, bs);
                 k_pt_finish<<<shade_blocks, 128, 0, bs>>>(P, 0);
                 if (types & 1) k_pt_shade<0><<<shade_blocks, 128, 0, bs>>>(P, 0);
                 if (types & 2) k_pt_shade<1><<<shade_blocks, 128, 0, bs>>>(P, 0);
@@ -2604,7 +2844,8 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
             int shade_blocks = sm * ctx->shade_bpsm;
             for (int r = 0; r < max_rounds; r++) {
                 int ri = r;
-                const bool cnt2 = ctx->profiling >= 2, w8 = ctx->bvh_width == 8 && sc->wide_ok;
+                const bool cnt2 = ctx->profiling >= 2;
+                const int width = trace_width(ctx, sc);
                 if (ctx->ray_sort && ri > 0) {
                     prof_begin(ctx, K_SORT);
                     if ((s = sort_rays(ctx, P, ri, 0, launches)) != RT_OK) return s;
@@ -2612,22 +2853,10 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
                     prof_end(ctx);
                 }
                 prof_begin(ctx, K_TRACE_C);
-                if (w8) {
-                    if (cnt2) k_trace8<false, true><<<trace_blocks, 128, 0, st>>>(P, ri);
-                    else k_trace8<false, false><<<trace_blocks, 128, 0, st>>>(P, ri);
-                } else {
-                    if (cnt2) k_trace<false, true><<<trace_blocks, 128, 0, st>>>(P, ri);
-                    else k_trace<false, false><<<trace_blocks, 128, 0, st>>>(P, ri);
-                }
+                launch_trace(width, P, ri, false, cnt2, trace_blocks, st);
                 prof_end(ctx);
                 prof_begin(ctx, K_TRACE_A);
-                if (w8) {
-                    if (cnt2) k_trace8<true, true><<<trace_blocks, 128, 0, st>>>(P, ri);
-                    else k_trace8<true, false><<<trace_blocks, 128, 0, st>>>(P, ri);
-                } else {
-                    if (cnt2) k_trace<true, true><<<trace_blocks, 128, 0, st>>>(P, ri);
-                    else k_trace<true, false><<<trace_blocks, 128, 0, st>>>(P, ri);
-                }
+                launch_trace(width, P, ri, true, cnt2, trace_blocks, st);
                 prof_end(ctx);
                 prof_begin(ctx, K_RESOLVE);
                 k_pt_finish<<<shade_blocks, 128, 0, st>>>(P, ri);
@@ -2711,7 +2940,7 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
     }
     ctx->last.launches = launches;
     ctx->last.limit_hits = limit;
-    if (limit) return fail(RT_ERR_LIMIT, "a device loop reached its iteration cap");
+    if (limit) return fail(RT_ERR_LIMIT, limit_message(limit));
     return RT_OK;
 }
 
@@ -2988,7 +3217,7 @@ rt_status rt_internal_render_multi(rt_ctx *ctx, rt_scene *const *scenes, const r
     ctx->last.nan_samples = (int64_t)stats[2];
     ctx->last.launches = launches;
     ctx->last.limit_hits = limit;
-    if (limit) return fail(RT_ERR_LIMIT, "a device loop reached its iteration cap");
+    if (limit) return fail(RT_ERR_LIMIT, limit_message(limit));
     return RT_OK;
 }
 
@@ -3078,15 +3307,10 @@ rt_status rt_render_paths(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, c
         } else {
             const int types = sc->bsdf_types | (P.sort_threshold > 0 ? 1 << RT_QUEUE_MIXED : 0);
             const int tb = sm * ctx->trace_bpsm, sb = sm * ctx->shade_bpsm;
-            const bool w8 = ctx->bvh_width == 8 && sc->wide_ok;
+            const int width = trace_width(ctx, sc);
             for (int r = 0; r < max_rounds; r++) {
-                if (w8) {
-                    k_trace8<false, false><<<tb, 128, 0, st>>>(P, r);
-                    k_trace8<true, false><<<tb, 128, 0, st>>>(P, r);
-                } else {
-                    k_trace<false, false><<<tb, 128, 0, st>>>(P, r);
-                    k_trace<true, false><<<tb, 128, 0, st>>>(P, r);
-                }
+                launch_trace(width, P, r, false, false, tb, st);
+                launch_trace(width, P, r, true, false, tb, st);
                 k_pt_finish<<<sb, 128, 0, st>>>(P, r);
                 if (types & 1) k_pt_shade<0><<<sb, 128, 0, st>>>(P, r);
                 if (types & 2) k_pt_shade<1><<<sb, 128, 0, st>>>(P, r);
@@ -3106,7 +3330,7 @@ rt_status rt_render_paths(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, c
         int limit = 0;
         CK(cudaMemcpyAsync(&limit, ctx->limit_flag, sizeof(int), cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
-        if (limit) return fail(RT_ERR_LIMIT, "a device loop reached its iteration cap");
+        if (limit) return fail(RT_ERR_LIMIT, limit_message(limit));
         return RT_OK;
     };
     s = run();
@@ -3156,13 +3380,7 @@ rt_status rt_trace(rt_ctx *ctx, rt_scene *sc, const rt_ray *rays, int32_t n, int
     const int sm = ctx->sm_count > 0 ? ctx->sm_count : 1;
     CK(cudaMemsetAsync(ctx->limit_flag, 0, sizeof(int), st));
     k_rays_in<<<(n + 127) / 128, 128, 0, st>>>(dr, n, P, anyhit ? 1 : 0);
-    if (ctx->bvh_width == 8 && sc->wide_ok) {
-        if (anyhit) k_trace8<true, false><<<sm * 12, 128, 0, st>>>(P, 0);
-        else k_trace8<false, false><<<sm * 12, 128, 0, st>>>(P, 0);
-    } else {
-        if (anyhit) k_trace<true, false><<<sm * 12, 128, 0, st>>>(P, 0);
-        else k_trace<false, false><<<sm * 12, 128, 0, st>>>(P, 0);
-    }
+    launch_trace(trace_width(ctx, sc), P, 0, anyhit != 0, false, sm * 12, st);
     k_hits_out<<<(n + 127) / 128, 128, 0, st>>>(P, n, anyhit ? 1 : 0, dh);
     s = launch_check("rt_trace kernels");
     if (s == RT_OK && !on_device) {
@@ -3176,7 +3394,7 @@ rt_status rt_trace(rt_ctx *ctx, rt_scene *sc, const rt_ray *rays, int32_t n, int
     }
     cudaError_t e = cudaStreamSynchronize(st);
     if (s == RT_OK && e != cudaSuccess) s = fail(RT_ERR_CUDA, cudaGetErrorString(e));
-    if (s == RT_OK && limit) s = fail(RT_ERR_LIMIT, "rt_trace: a traversal stack overflowed (a subtree was skipped)");
+    if (s == RT_OK && limit) s = fail(RT_ERR_LIMIT, "rt_trace: " + limit_message(limit));
     if (tmp_r) cudaFree(tmp_r);
     if (tmp_h) cudaFree(tmp_h);
     return s;
@@ -3460,13 +3678,8 @@ extern "C" rt_status rt_render_tile_static(rt_ctx *ctx, rt_scene *sc, const rt_r
     } else {
         const int blocks = sm * 8;
         for (int r = 0; r < rounds; r++) {
-            if (ctx->bvh_width == 8 && sc->wide_ok) {
-                k_trace8<false, false><<<sm * 12, 128, 0, st>>>(Pm, r);
-                k_trace8<true, false><<<sm * 12, 128, 0, st>>>(Pm, r);
-            } else {
-                k_trace<false, false><<<sm * 12, 128, 0, st>>>(Pm, r);
-                k_trace<true, false><<<sm * 12, 128, 0, st>>>(Pm, r);
-            }
+            launch_trace(trace_width(ctx, sc), Pm, r, false, false, sm * 12, st);
+            launch_trace(trace_width(ctx, sc), Pm, r, true, false, sm * 12, st);
             k_pt_finish<<<blocks, 128, 0, st>>>(Pm, r);
             if (sc->bsdf_types & 1) k_pt_shade<0><<<blocks, 128, 0, st>>>(Pm, r);
             if (sc->bsdf_types & 2) k_pt_shade<1><<<blocks, 128, 0, st>>>(Pm, r);
@@ -3489,7 +3702,7 @@ extern "C" rt_status rt_render_tile_static(rt_ctx *ctx, rt_scene *sc, const rt_r
     int limit = 0;
     CK(cudaMemcpyAsync(&limit, limit_flag, sizeof(int), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    if (limit) return fail(RT_ERR_LIMIT, "a device loop reached its iteration cap");
+    if (limit) return fail(RT_ERR_LIMIT, limit_message(limit));
     return RT_OK;
 }
 
@@ -3499,6 +3712,12 @@ extern "C" rt_status rt_render_tile_static(rt_ctx *ctx, rt_scene *sc, const rt_r
 rt_status rt_internal_error(rt_status st, const char *msg) { return fail(st, msg ? msg : ""); }
 int rt_internal_device(const rt_ctx *c) { return c->device; }
 int rt_internal_bvh_width(const rt_ctx *c) { return c->bvh_width; }
+static int trace_width(const rt_ctx *ctx, const rt_scene *sc)
+{
+    if (ctx->bvh_width == 8 && sc->wide_ok) return 8;
+    if (ctx->bvh_width == 4 && sc->w4_ok) return 4;
+    return 2;
+}
 int rt_internal_graphs(const rt_ctx *c) { return c->graphs; }
 int rt_internal_volpath_wave(const rt_ctx *c) { return c->volpath_wave; }
 int rt_internal_batch_wave(const rt_ctx *c) { return c->batch_wave; }

@@ -9,6 +9,7 @@
 #include "rt_bvh.h"
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstring>
 #include <thread>
@@ -481,6 +482,126 @@ void build_wbvh8(const float *tv, int n, WideBvhImage &img, int n_bins, int dept
     Collapse cl(bn, B.order, tv, seps, img);
     cl.emit(0, 0, 0);
     img.max_depth = cl.maxd;
+}
+
+void build_bvh4(const BvhImage &b2, Bvh4Image &out)
+{
+    out = Bvh4Image();
+    if (b2.n_nodes <= 0) return;
+    // one child entry of a binary node: its box (the six widened planes as
+    // stored) and its link
+    struct Entry { float pl[6]; int32_t link; double area; };
+    auto entry = [&](int node, int k, Entry &e) -> bool {
+        const float *o = &b2.nodes[16 * (size_t)node];
+        if (k == 0) { e.pl[0] = o[0]; e.pl[1] = o[1]; e.pl[2] = o[2]; e.pl[3] = o[3]; e.pl[4] = o[8]; e.pl[5] = o[9]; }
+        else { e.pl[0] = o[4]; e.pl[1] = o[5]; e.pl[2] = o[6]; e.pl[3] = o[7]; e.pl[4] = o[10]; e.pl[5] = o[11]; }
+        std::memcpy(&e.link, &o[12 + k], 4);
+        // the empty second child of a root leaf: an inverted box
+        if (!(e.pl[0] <= e.pl[1])) return false;
+        double dx = (double)e.pl[1] - e.pl[0], dy = (double)e.pl[3] - e.pl[2], dz = (double)e.pl[5] - e.pl[4];
+        e.area = 2.0 * (dx * dy + dy * dz + dz * dx);
+        return true;
+    };
+    // breadth-first: a queue of (binary node, 4-wide node index, depth)
+    struct Work { int node, wi, depth; };
+    std::vector<Work> q;
+    q.push_back({0, 0, 0});
+    out.n_nodes = 1;
+    out.nodes.assign(32, INFINITY);
+    for (size_t h = 0; h < q.size(); h++) {
+        const Work w = q[h];
+        out.max_depth = std::max(out.max_depth, w.depth);
+        Entry ch[4];
+        int nc = 0;
+        for (int k = 0; k < 2; k++)
+            if (entry(w.node, k, ch[nc])) nc++;
+        while (nc < 4) {
+            int best = -1;
+            for (int i = 0; i < nc; i++)
+                if (ch[i].link >= 0 && (best < 0 || ch[i].area > ch[best].area)) best = i;
+            if (best < 0) break;
+            const int nb = ch[best].link;
+            Entry a, b;
+            bool ha = entry(nb, 0, a), hb = entry(nb, 1, b);
+            if (ha && hb) { ch[best] = a; ch[nc++] = b; }
+            else if (ha) ch[best] = a;
+            else if (hb) ch[best] = b;
+            else { ch[best] = ch[--nc]; }
+        }
+        float *o = &out.nodes[32 * (size_t)w.wi];
+        for (int i = 0; i < 4; i++) {
+            int32_t link = 0x7fffffff;
+            if (i < nc) {
+                for (int pl = 0; pl < 6; pl++) o[4 * pl + i] = ch[i].pl[pl];
+                link = ch[i].link;
+                if (link >= 0) {
+                    const int wi = out.n_nodes++;
+                    out.nodes.resize(32 * (size_t)out.n_nodes, INFINITY);
+                    o = &out.nodes[32 * (size_t)w.wi];   // the resize may move the array
+                    q.push_back({link, wi, w.depth + 1});
+                    link = wi;
+                }
+            }
+            std::memcpy(&o[24 + i], &link, 4);
+        }
+        for (int i = 28; i < 32; i++) o[i] = 0.f;
+    }
+}
+
+bool check_bvh4(const Bvh4Image &w, const BvhImage &b2, std::string *why)
+{
+    auto bad = [&](const std::string &m) { if (why) *why = m; return false; };
+    if (b2.n_nodes == 0) return w.n_nodes == 0 ? true : bad("nodes without a binary tree");
+    // every leaf entry of the binary tree: its link and six planes
+    std::vector<std::pair<int32_t, std::array<float, 6>>> leaves;
+    for (int nd = 0; nd < b2.n_nodes; nd++)
+        for (int k = 0; k < 2; k++) {
+            const float *o = &b2.nodes[16 * (size_t)nd];
+            std::array<float, 6> pl;
+            if (k == 0) pl = {o[0], o[1], o[2], o[3], o[8], o[9]};
+            else pl = {o[4], o[5], o[6], o[7], o[10], o[11]};
+            if (!(pl[0] <= pl[1])) continue;
+            int32_t link;
+            std::memcpy(&link, &o[12 + k], 4);
+            if (link < 0) leaves.push_back({link, pl});
+        }
+    std::sort(leaves.begin(), leaves.end(), [](const auto &a, const auto &b) { return a.first < b.first; });
+    std::vector<int32_t> seen_leaves;
+    std::vector<char> seen(w.n_nodes, 0);
+    std::vector<int> stack{0};
+    seen[0] = 1;
+    while (!stack.empty()) {
+        const int nd = stack.back();
+        stack.pop_back();
+        const float *o = &w.nodes[32 * (size_t)nd];
+        for (int i = 0; i < 4; i++) {
+            int32_t link;
+            std::memcpy(&link, &o[24 + i], 4);
+            std::array<float, 6> pl = {o[i], o[4 + i], o[8 + i], o[12 + i], o[16 + i], o[20 + i]};
+            if (link == 0x7fffffff) {
+                for (float v : pl) if (!(v == INFINITY)) return bad("unused slot with a finite plane");
+                continue;
+            }
+            if (link >= 0) {
+                if (link >= w.n_nodes || seen[link]) return bad("internal link out of range or shared");
+                seen[link] = 1;
+                stack.push_back(link);
+                continue;
+            }
+            auto it = std::lower_bound(leaves.begin(), leaves.end(), link,
+                                       [](const auto &a, int32_t l) { return a.first < l; });
+            if (it == leaves.end() || it->first != link) return bad("leaf not in the binary tree");
+            if (it->second != pl) return bad("leaf box differs from the binary tree's");
+            seen_leaves.push_back(link);
+        }
+    }
+    for (int nd = 0; nd < w.n_nodes; nd++)
+        if (!seen[nd]) return bad("unreachable node");
+    std::sort(seen_leaves.begin(), seen_leaves.end());
+    if (seen_leaves.size() != leaves.size()) return bad("leaf count differs from the binary tree's");
+    for (size_t i = 0; i < leaves.size(); i++)
+        if (seen_leaves[i] != leaves[i].first) return bad("a leaf is reached twice or never");
+    return true;
 }
 
 bool check_bvh2(const BvhImage &img, const float *tv, int n, int *depth, std::string *why)

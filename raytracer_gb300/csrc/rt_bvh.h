@@ -30,6 +30,29 @@ struct BvhImage {
     double sah_cost = 0.0;
 };
 
+// 4-wide BVH collapsed from a BVH2 image; it shares the BVH2's triangle
+// slots and leaf encoding.  Each node is 8 float4 (128 bytes, one cache
+// line), one plane of the four child boxes per float4:
+//   xlo[4], xhi[4], ylo[4], yhi[4], zlo[4], zhi[4], link[4] (int32), pad
+// link >= 0: internal node; < 0: leaf as in the BVH2.  An unused slot has
+// every plane at +inf, a box no ray can enter whatever its direction.  The
+// child boxes are the BVH2's (already widened), so the 4-wide traversal
+// culls exactly what the BVH2's would.
+struct Bvh4Image {
+    std::vector<float> nodes;      // 32 floats per node
+    int n_nodes = 0;
+    int max_depth = 0;             // deepest node level below the root
+};
+
+// Collapse a BVH2 image: every 4-wide node takes the two children of a
+// binary node and opens the internal child of largest surface area until it
+// has four children (or only leaves).
+void build_bvh4(const BvhImage &b2, Bvh4Image &out);
+// Structural check of a 4-wide image against the BVH2 it was collapsed
+// from: every node reached once, every BVH2 leaf reached exactly once with
+// the BVH2's box, unused slots all +inf.
+bool check_bvh4(const Bvh4Image &w, const BvhImage &b2, std::string *why);
+
 // Compressed 8-wide BVH.  Each node is 5 float4 (80 bytes):
 //   w0 = (px, py, pz, bits: ex | ey << 8 | ez << 16)      grid origin, exponents
 //   w1 = (child_base, tri_base, meta[0..3], meta[4..7])   as int32 / packed bytes

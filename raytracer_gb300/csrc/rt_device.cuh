@@ -122,6 +122,10 @@ struct DevScene {
     const float4 *nodes;
     const float4 *tri_slots;    // 3 float4 per leaf slot: (p0, id), (e1, 0), (e2, 0)
     int n_nodes;
+    // 4-wide BVH collapsed from the BVH2 (128-byte nodes, see rt_bvh.h); its
+    // leaves are the BVH2's triangle slots
+    const float4 *nodes4;
+    int n_nodes4;
     // compressed 8-wide BVH (80-byte nodes, see rt_bvh.h) and its triangle slots
     const float4 *wnodes;
     const float4 *wtri;
@@ -203,6 +207,15 @@ __device__ __forceinline__ bool ref_box_hit(const float *bmin, const float *bmax
 // |det| < 1e-8 (double compare in Triangle.cpp:66) <=> |det| <= float32(1e-8)
 #define RT_DET_EPS 9.99999993922529e-09f
 #define RT_STACK 64
+// Bits of the limit flag a render reads back: which device cap tripped
+// (the host names them in the RT_ERR_LIMIT message).
+enum {
+    RT_LIM_STACK2 = 1,     // BVH2 traversal stack full (the build bounds the depth)
+    RT_LIM_STACK4 = 2,     // 4-wide traversal stack full (deeper trees are not uploaded)
+    RT_LIM_STACK8 = 4,     // 8-wide group stack full (deeper trees are not uploaded)
+    RT_LIM_VOLPATH = 8,    // a VolPathTracing loop cap (boundaries, tracking steps, iterations)
+    RT_LIM_LINK = 16,      // a BVH child link outside the node array (a corrupted tree)
+};
 
 // Triangle::intersection (geometricShape/Triangle.cpp:46-88), exact order
 __device__ __forceinline__ bool mt_test(float4 a, float4 b, float4 c, V3 o, V3 d, float mint, float maxt,
@@ -293,8 +306,34 @@ __device__ __forceinline__ float slab_guard(float oo) { return fabsf(oo) * 4.768
 
 // Leaf encoding of BVH2 child links: c >= 0 internal node index; c < 0 leaf
 // with v = ~c, first slot = v >> 3, count = (v & 7) + 1.
-__device__ __forceinline__ float rt_min4(float a, float b, float c, float d) { return fminf(fminf(a, b), fminf(c, d)); }
-__device__ __forceinline__ float rt_max4(float a, float b, float c, float d) { return fmaxf(fmaxf(a, b), fmaxf(c, d)); }
+// Three-input min / max (sm_100 and later: min.f32 / max.f32 with three
+// sources; NaN inputs are ignored as by fminf / fmaxf).  RT_MNMX3=0 builds
+// them from two-input operations.
+#ifndef RT_MNMX3
+#define RT_MNMX3 1
+#endif
+__device__ __forceinline__ float rt_min3(float a, float b, float c)
+{
+#if RT_MNMX3
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+#else
+    return fminf(fminf(a, b), c);
+#endif
+}
+__device__ __forceinline__ float rt_max3(float a, float b, float c)
+{
+#if RT_MNMX3
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+#else
+    return fmaxf(fmaxf(a, b), c);
+#endif
+}
+__device__ __forceinline__ float rt_min4(float a, float b, float c, float d) { return rt_min3(a, b, fminf(c, d)); }
+__device__ __forceinline__ float rt_max4(float a, float b, float c, float d) { return rt_max3(a, b, fmaxf(c, d)); }
 
 // Closest / any hit through the BVH2 plus the analytic spheres.  With
 // COUNT, nodes fetched and triangle slots tested are added to cnt[0], cnt[1]
@@ -347,7 +386,7 @@ __device__ __forceinline__ bool trace_ray(const DevScene &S, V3 o, V3 d, float m
                     int nearc = cc.x, farc = cc.y;
                     if (c1min < c0min) { nearc = cc.y; farc = cc.x; }
                     if (sp < RT_STACK) stack[sp++] = farc;
-                    else if (S.limit_flag) atomicExch(S.limit_flag, 1);   // unreachable: the build bounds the depth
+                    else if (S.limit_flag) atomicOr(S.limit_flag, RT_LIM_STACK2);   // unreachable: the build bounds the depth
                     node = nearc;
                 } else {
                     node = t0 ? cc.x : cc.y;

@@ -206,11 +206,18 @@ extern "C" rt_status rt_batch_render(rt_ctx *ctx, rt_scene *const *scenes, const
         return rt_internal_error(RT_ERR_CUDA, "rt_batch_render: stream synchronize failed");
     // with batch_wavefront: the eligible jobs in one multi-scene wavefront
     // per (max_depth, min_depth) group on the calling context, the rest on
-    // the lanes at the same time
+    // the lanes at the same time.  A job of at least a quarter of the
+    // wavefront capacity fills the device by itself: it renders alone on a
+    // lane, with the single-scene kernels (no per-path scene lookups).
+    int wave_paths = 0, tb = 0, sb = 0, thr = 0;
+    rt_internal_get_shape(ctx, &wave_paths, &tb, &sb, &thr);
     std::vector<int> lane_jobs;
     std::vector<std::vector<int>> groups;
     for (int i = 0; i < n; i++) {
-        if (!rt_internal_batch_wave(ctx) || !rt_internal_multi_ok(scenes[i], &descs[i])) {
+        int fw = 0, fh = 0;
+        rt_internal_film_size(scenes[i], &fw, &fh);
+        const bool alone = (double)fw * fh * std::max(1, descs[i].spp) >= 0.25 * wave_paths;
+        if (!rt_internal_batch_wave(ctx) || alone || !rt_internal_multi_ok(scenes[i], &descs[i])) {
             lane_jobs.push_back(i);
             continue;
         }

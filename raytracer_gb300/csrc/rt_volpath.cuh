@@ -328,7 +328,7 @@ __global__ void __launch_bounds__(128, RT_VOLPATH_MINB) k_volpath(RenderParams P
             active = false;
         }
     }
-    if (limit) atomicExch(P.limit_flag, 1);
+    if (limit) atomicOr(P.limit_flag, RT_LIM_VOLPATH);
 }
 
 // ---------------------------------------------------------------- VolPathTracing wavefront
@@ -580,7 +580,7 @@ __global__ void __launch_bounds__(128, RT_VW_MINB_STEP) k_vw_step(RenderParams P
         q_push(P.W.q_mat[1], &C->mat[1], slot, push_sample);
         q_push(P.W.q_closest, &Cn->closest, slot, push_trace);
     }
-    if (limit) atomicExch(P.limit_flag, 1);
+    if (limit) atomicOr(P.limit_flag, RT_LIM_VOLPATH);
 }
 
 __global__ void __launch_bounds__(128, RT_VW_MINB_SHADOW) k_vw_shadow(RenderParams P, int round)
@@ -604,7 +604,7 @@ __global__ void __launch_bounds__(128, RT_VW_MINB_SHADOW) k_vw_shadow(RenderPara
         P.W.flags[slot] |= VF_HASVAL;
         q_push(P.W.q_mat[1], &C->mat[1], slot, true);
     }
-    if (limit) atomicExch(P.limit_flag, 1);
+    if (limit) atomicOr(P.limit_flag, RT_LIM_VOLPATH);
 }
 
 __global__ void __launch_bounds__(128, RT_VW_MINB_SAMPLE) k_vw_sample(RenderParams P, int round)
@@ -720,7 +720,7 @@ __global__ void __launch_bounds__(128, RT_VW_MINB_TRSAMP) k_vw_trsamp(RenderPara
         P.W.flags[slot] = flags;
         q_push(P.W.q_mat[3], &C->mat[3], slot, true);
     }
-    if (limit) atomicExch(P.limit_flag, 1);
+    if (limit) atomicOr(P.limit_flag, RT_LIM_VOLPATH);
 }
 
 __global__ void __launch_bounds__(128, RT_VW_MINB_FINISH) k_vw_finish(RenderParams P, int round)

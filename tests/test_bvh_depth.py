@@ -76,3 +76,19 @@ def test_bad_caps_are_refused(lib):
     with pytest.raises(core.RtError):
         core.bvh_stats(t, depth_cap=63)       # beyond the stack
     assert core.bvh_stats(np.zeros((0, 3, 3), np.float32)) == (0, 0)
+
+
+@pytest.mark.parametrize("tris", ["strip", "soup"])
+def test_four_wide_collapse(lib, tris):
+    """The 4-wide tree collapsed from the binary one: rt_bvh_stats checks that
+    every binary leaf is reached exactly once, with the binary tree's box, and
+    that unused slots cannot be entered; it is no deeper and has fewer nodes."""
+    t = geometric_strip(60, 2.0) if tris == "strip" else random_soup(20000, 3)
+    d2, n2 = core.bvh_stats(t)
+    d4, n4 = core.bvh_stats(t, width=4)
+    assert d4 <= d2 and 0 < n4 < n2
+    if tris == "soup":
+        assert d4 <= (d2 + 1) // 2 + 2      # two binary levels per 4-wide level, give or take
+    cap = 12 if tris == "strip" else 16
+    d4c, _ = core.bvh_stats(t, width=4, depth_cap=cap)
+    assert d4c <= cap

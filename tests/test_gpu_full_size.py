@@ -61,7 +61,7 @@ def _width(ctx, w):
     ctx.set_bvh_width(w)
 
 
-@pytest.mark.parametrize("w", [2, 8], ids=["bvh2", "bvh8"])
+@pytest.mark.parametrize("w", [2, 4, 8], ids=["bvh2", "bvh4", "bvh8"])
 def test_full_tree_trace_parity(ctx, rtlib, ico_full, w):
     """131,072 camera rays plus 131,072 secondary rays leaving the camera
     rays' hit points (uniform directions, the reference's adaptive epsilon)

@@ -84,9 +84,9 @@ def _trace_parity(ctx, rtlib, scene, n=20000, seed=0):
     o.close()
 
 
-@pytest.fixture(params=[2, 8], ids=["bvh2", "bvh8"])
+@pytest.fixture(params=[2, 4, 8], ids=["bvh2", "bvh4", "bvh8"])
 def width(request, ctx):
-    """Runs a test once per traversal tree (binary and compressed 8-wide)."""
+    """Runs a test once per traversal tree (binary, 4-wide, compressed 8-wide)."""
     ctx.set_bvh_width(request.param)
     yield request.param
     ctx.set_bvh_width(2)
