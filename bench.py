@@ -286,17 +286,19 @@ def batched_block(ctx_factory, n_jobs=64):
             "prep_s": round(prep, 1)}
 
 
-def served_block(ctx_factory, rate=20.0, n_jobs=40, pool_pt=8, target=0.02, cap=256):
+def served_block(ctx_factory, rate=5.0, n_jobs=30, pool_pt=8, target=0.02, cap=4096):
     """Served jobs at one Poisson arrival rate: continuous batching against
-    one job at a time, same arrivals, p50/p99 latency to completion and the
-    true RMSE of the finished films against 4096-spp GPU renders."""
+    one job at a time, same arrivals, p50/p99 latency to completion (time to
+    target) and the true RMSE of the finished films against 4096-spp GPU
+    renders, on the displayed image (pixel means clipped to [0, 1])."""
     ctx = ctx_factory()
     pool, refs = _serve_pool(ctx, pool_pt, 2)
     rng = np.random.default_rng(7)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, n_jobs))
     picks = [(int(pool_pt + rng.integers(2)) if rng.random() < 0.2 else int(rng.integers(pool_pt)), j)
              for j in range(n_jobs)]
-    res = {"rate_jobs_per_s": rate, "jobs": n_jobs, "target_rmse": target, "spp_cap": cap,
+    res = {"rate_jobs_per_s": rate, "jobs": n_jobs, "target_rmse": target, "rmse_space": "display ([0, 1] clipped)",
+           "spp_cap": cap,
            "pool": "%d scenes of the batch distribution + 2 grid-medium scenes, 4096-spp references" % pool_pt}
     for form in ("plain", "batched"):
         res[form] = _serve_run(ctx, pool, refs, picks, arrivals, form, target, cap, 4)
@@ -684,30 +686,36 @@ def _serve_run(ctx, pool, refs, picks, arrivals, form, target, cap, lanes):
     per job: latency to completion (queue + run), samples rendered and the
     true RMSE of its film against the pool scene's reference."""
     import raytracer_gb300 as R
-    srv = R.Server(ctx, lanes=1 if form == "plain" else lanes, lanes_only=form != "batched")
+    srv = R.Server(ctx, lanes=1 if form == "plain" else lanes, lanes_only=form != "batched", rmse_display=True)
     t0 = time.perf_counter()
     ids = []
     for (pi, seed), ta in zip(picks, arrivals):
         dt = ta - (time.perf_counter() - t0)
         if dt > 0:
             time.sleep(dt)
-        g = pool[pi]
-        jcap = 64 if g.data.integrator["integrator"] == 1 else cap
-        ids.append(srv.submit(g, jcap, target_rmse=target, seed=seed))
-    lat, samples, rmse = [], 0, []
+        ids.append(srv.submit(pool[pi], cap, target_rmse=target, seed=seed))
+    lat, samples, rmse, rmse_lin, spp = [], 0, [], [], []
     for j, (pi, _) in zip(ids, picks):
         info, film = srv.wait(j)
         lat.append(info["queue_ms"] + info["run_ms"])
         g = pool[pi]
         samples += g.width * g.height * info["spp_done"]
-        rmse.append(float(np.sqrt(np.mean((R.post_process(film) - refs[pi]) ** 2))))
+        spp.append(info["spp_done"])
+        img = R.post_process(film)
+        rmse.append(float(np.sqrt(np.mean((np.clip(img, 0, 1) - np.clip(refs[pi], 0, 1)) ** 2))))
+        rmse_lin.append(float(np.sqrt(np.mean((img - refs[pi]) ** 2))))
     wall = time.perf_counter() - t0
     srv.stop()
     rmse = np.array(rmse)
+    # the reference renders carry noise of their own (about 0.01 on the
+    # displayed image), so a film that meets the target measures up to
+    # sqrt(0.02^2 + 0.01^2) against them: 1.25x the target is the bar
     return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
             "jobs_per_s": len(ids) / wall, "samples_per_s": samples / wall,
+            "spp_p50": float(np.median(spp)), "spp_max": int(np.max(spp)),
             "true_rmse_p50": float(np.median(rmse)), "true_rmse_p90": float(np.percentile(rmse, 90)),
-            "met_target_frac": float(np.mean(rmse <= target * 1.25))}
+            "met_target_frac": float(np.mean(rmse <= target * 1.25)),
+            "linear_rmse_p50": float(np.median(rmse_lin))}
 
 
 def run_serve(args):
@@ -779,7 +787,7 @@ def main():
     ap.add_argument("--serve-forms", default="plain,lanes,batched", help="serve: server forms to time")
     ap.add_argument("--serve-lanes", type=int, default=4)
     ap.add_argument("--target-rmse", type=float, default=0.02)
-    ap.add_argument("--spp-cap", type=int, default=256)
+    ap.add_argument("--spp-cap", type=int, default=4096)
     args = ap.parse_args()
     global _ARGS
     _ARGS = args

@@ -509,7 +509,9 @@ typedef struct rt_server_opts {
                                      scenes and films; 0 = unlimited               */
     int32_t lanes_only;           /* 0: continuous batching in one wavefront (the
                                      default); 1: every job on a lane               */
-    int32_t pad;
+    int32_t rmse_display;         /* 0: target RMSE over the pixel means (linear
+                                     radiance); 1: over the pixel means clipped to
+                                     [0, 1] per channel, the range a display shows */
 } rt_server_opts;
 enum { RT_JOB_QUEUED = 0, RT_JOB_RUNNING = 1, RT_JOB_DONE = 2, RT_JOB_FAILED = 3 };
 typedef struct rt_job_info {

@@ -24,7 +24,7 @@ _STATUS = {1: "RT_ERR_INVALID", 2: "RT_ERR_CUDA", 3: "RT_ERR_LIMIT", 4: "RT_ERR_
 
 class ServerOpts(C.Structure):
     _fields_ = [("lanes", C.c_int32), ("max_queue", C.c_int32), ("device_budget_bytes", C.c_int64),
-                ("lanes_only", C.c_int32), ("pad", C.c_int32)]
+                ("lanes_only", C.c_int32), ("rmse_display", C.c_int32)]
 
 
 class JobInfo(C.Structure):
@@ -345,13 +345,16 @@ class Scene:
 class Server:
     """A render job queue on one device (rt_server_start ... rt_server_stop)."""
 
-    def __init__(self, ctx, lanes=4, max_queue=0, device_budget_bytes=0, lanes_only=False):
+    def __init__(self, ctx, lanes=4, max_queue=0, device_budget_bytes=0, lanes_only=False, rmse_display=False):
         """lanes_only=False: continuous batching of PathTracingMIS jobs in
-        one wavefront (other jobs on the lanes); True: every job on a lane."""
+        one wavefront (other jobs on the lanes); True: every job on a lane.
+        rmse_display=True: target RMSEs are over the pixel means clipped to
+        [0, 1] (the displayed image) instead of the linear radiance."""
         self.ctx = ctx
         self.h = C.c_void_p()
         self._scenes = {}
-        o = ServerOpts(int(lanes), int(max_queue), int(device_budget_bytes), int(bool(lanes_only)), 0)
+        o = ServerOpts(int(lanes), int(max_queue), int(device_budget_bytes), int(bool(lanes_only)),
+                       int(bool(rmse_display)))
         _check(lib().rt_server_start(ctx.h, C.byref(o), C.byref(self.h)))
 
     def submit(self, scene, spp, target_rmse=0.0, seed=0, sample_begin=0, block=32, **over):

@@ -3757,16 +3757,21 @@ void rt_internal_film_size(const rt_scene *sc, int *w, int *h)
 }
 
 // partial sums of (a.rgb/a.w - b.rgb/b.w)^2 over pixels with weight in both
-__global__ void k_film_sqdiff(const float4 *a, const float4 *b, size_t npix, double *partial)
+__device__ __forceinline__ double film_mean(float v, float w, int clip)
+{
+    const double m = (double)v / w;
+    return clip ? fmin(fmax(m, 0.0), 1.0) : m;
+}
+__global__ void k_film_sqdiff(const float4 *a, const float4 *b, size_t npix, int clip, double *partial)
 {
     __shared__ double sh[256];
     double acc = 0.0;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < npix; i += (size_t)gridDim.x * blockDim.x) {
         float4 x = a[i], y = b[i];
         if (x.w > 0.f && y.w > 0.f) {
-            double dr = (double)x.x / x.w - (double)y.x / y.w;
-            double dg = (double)x.y / x.w - (double)y.y / y.w;
-            double db = (double)x.z / x.w - (double)y.z / y.w;
+            double dr = film_mean(x.x, x.w, clip) - film_mean(y.x, y.w, clip);
+            double dg = film_mean(x.y, x.w, clip) - film_mean(y.y, y.w, clip);
+            double db = film_mean(x.z, x.w, clip) - film_mean(y.z, y.w, clip);
             acc += dr * dr + dg * dg + db * db;
         }
     }
@@ -3787,14 +3792,15 @@ __global__ void k_film_add(float4 *dst, const float4 *src, size_t npix)
     }
 }
 
-rt_status rt_internal_film_sqdiff(rt_ctx *c, const float *a, const float *b, size_t npix, double *mean_sq)
+rt_status rt_internal_film_sqdiff(rt_ctx *c, const float *a, const float *b, size_t npix, int clip,
+                                  double *mean_sq)
 {
     CK(cudaSetDevice(c->device));
     const int blocks = 256;
     double *part = nullptr;
     CK(cudaMalloc(&part, blocks * sizeof(double)));
     k_film_sqdiff<<<blocks, 256, 0, c->stream>>>(reinterpret_cast<const float4 *>(a), reinterpret_cast<const float4 *>(b),
-                                                  npix, part);
+                                                  npix, clip, part);
     double h[blocks];
     cudaError_t e = cudaMemcpyAsync(h, part, sizeof(h), cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);

@@ -32,8 +32,10 @@ RT_HIDDEN rt_lane_pool *&rt_internal_pool(rt_ctx *c);
 RT_HIDDEN void rt_internal_set_stats(rt_ctx *c, const rt_render_stats &s);
 RT_HIDDEN void rt_internal_film_size(const rt_scene *sc, int *w, int *h);
 // mean over pixels and channels of (a.rgb / a.w - b.rgb / b.w)^2 for two
-// device films (pixels with zero weight in either are skipped); synchronous
-RT_HIDDEN rt_status rt_internal_film_sqdiff(rt_ctx *c, const float *a, const float *b, size_t npix, double *mean_sq);
+// device films (pixels with zero weight in either are skipped); with clip,
+// each mean is clipped to [0, 1] first; synchronous
+RT_HIDDEN rt_status rt_internal_film_sqdiff(rt_ctx *c, const float *a, const float *b, size_t npix, int clip,
+                                            double *mean_sq);
 // dst += src for two device films, queued on the context's stream
 RT_HIDDEN rt_status rt_internal_film_add(rt_ctx *c, float *dst, const float *src, size_t npix);
 

@@ -304,6 +304,7 @@ struct Job {
     rt_scene *scene = nullptr;
     rt_render_desc desc;
     float target = 0.f;
+    int clip = 0;            // target RMSE over pixel means clipped to [0, 1] (rt_server_opts.rmse_display)
     int w = 0, h = 0;
     int64_t bytes = 0;       // device bytes held while resident: scene + films
     int state = RT_JOB_QUEUED;
@@ -337,6 +338,7 @@ struct rt_server {
     int max_queue = 4096;
     int64_t budget = 0, in_flight = 0, fixed = 0;
     bool wavefront = true;
+    int rmse_display = 0;          // rt_server_opts.rmse_display
     rt_ctx *sched = nullptr;        // the wavefront's context
     std::thread scheduler;
 };
@@ -387,7 +389,7 @@ static rt_status run_job(rt_ctx *lane, Job *J)
         if ((s = rt_render(lane, J->scene, &d, B, 1)) != RT_OK) break;
         done += 2 * k;
         double msq = 0.0;
-        if ((s = rt_internal_film_sqdiff(lane, A, B, npix, &msq)) != RT_OK) break;
+        if ((s = rt_internal_film_sqdiff(lane, A, B, npix, J->clip, &msq)) != RT_OK) break;
         est = std::sqrt(msq) * 0.5;
         if (est <= J->target || cap - done < 2) break;
         k = next_chunk(J, done, est);
@@ -546,7 +548,7 @@ static void schedule(rt_server *S)
             if (s == RT_OK && J->target > 0.f) {
                 J->spp_done += 2 * J->k;
                 double msq = 0.0;
-                s = rt_internal_film_sqdiff(S->sched, J->A, J->B, (size_t)J->w * J->h, &msq);
+                s = rt_internal_film_sqdiff(S->sched, J->A, J->B, (size_t)J->w * J->h, J->clip, &msq);
                 J->est = std::sqrt(msq) * 0.5;
                 J->rmse = (float)J->est;
                 const int cap = std::max(2, J->desc.spp);
@@ -576,12 +578,15 @@ extern "C" rt_status rt_server_start(rt_ctx *ctx, const rt_server_opts *opts, rt
     if (lanes > 16) return rt_internal_error(RT_ERR_INVALID, "rt_server_start: lanes must be in 1..16");
     if (opts && opts->lanes_only != 0 && opts->lanes_only != 1)
         return rt_internal_error(RT_ERR_INVALID, "rt_server_start: lanes_only must be 0 or 1");
+    if (opts && opts->rmse_display != 0 && opts->rmse_display != 1)
+        return rt_internal_error(RT_ERR_INVALID, "rt_server_start: rmse_display must be 0 or 1");
     rt_server *S = new rt_server();
     S->parent = ctx;
     S->set.device = rt_internal_device(ctx);
     S->max_queue = opts && opts->max_queue > 0 ? opts->max_queue : 4096;
     S->budget = opts ? opts->device_budget_bytes : 0;
     S->wavefront = !opts || opts->lanes_only == 0;
+    S->rmse_display = opts ? opts->rmse_display : 0;
     S->set.wave_paths = pool_of(ctx)->set.wave_paths;
     rt_status s = S->set.grow(lanes, ctx);
     if (s == RT_OK && S->wavefront) {
@@ -617,6 +622,7 @@ extern "C" rt_status rt_job_submit(rt_server *S, rt_scene *scene, const rt_rende
     J->scene = scene;
     J->desc = *desc;
     J->target = target_rmse;
+    J->clip = S->rmse_display;
     rt_internal_film_size(scene, &J->w, &J->h);
     int64_t scene_bytes = 0;
     float bounds[6];

@@ -158,6 +158,29 @@ def test_server_progressive_meets_target(ctx, job_scenes):
     assert abs(film[..., 3].mean() - info["spp_done"]) <= 0.01 * info["spp_done"]
 
 
+@pytest.mark.parametrize("lanes_only", [False, True], ids=["wavefront", "lanes"])
+def test_server_progressive_display_rmse(ctx, job_scenes, lanes_only):
+    """rmse_display: the target is on the displayed image (pixel means
+    clipped to [0, 1]).  The icosphere under the sky has bright sun
+    highlights whose linear error stays far above the target for thousands
+    of samples; on the displayed image the job stops well before its cap,
+    and the measured error against a 4096-sample render (which carries noise
+    of its own) is close to the target."""
+    g = job_scenes["ico"]
+    ref = np.clip(R.post_process(g.render(4096, seed=100)), 0, 1)
+    srv = R.Server(ctx, lanes=2, lanes_only=lanes_only, rmse_display=True)
+    target = 0.03
+    jid = srv.submit(g, 4096, target_rmse=target, seed=11)
+    info, film = srv.wait(jid)
+    srv.stop()
+    assert info["state"] == R.JOB_DONE
+    true_rmse = float(np.sqrt(np.mean((np.clip(R.post_process(film), 0, 1) - ref) ** 2)))
+    print("display rmse: spp %d, estimate %.4f, measured %.4f" % (info["spp_done"], info["rmse_estimate"], true_rmse))
+    assert info["rmse_estimate"] <= target
+    assert 4 <= info["spp_done"] < 4096
+    assert true_rmse < 1.5 * target
+
+
 def test_server_progressive_same_alone_and_in_mix(ctx, job_scenes):
     """Continuous batching: a progressive job sizes its chunks from its own
     films only, so whatever else shares its steps, it renders the same sample
