@@ -45,7 +45,6 @@ static std::string limit_message(int bits)
     if (bits & RT_LIM_STACK4) m += " 4-wide traversal stack;";
     if (bits & RT_LIM_STACK8) m += " 8-wide group stack;";
     if (bits & RT_LIM_VOLPATH) m += " VolPathTracing loop cap;";
-    if (bits & RT_LIM_LINK) m += " BVH child link outside the node array;";
     return m;
 }
 #define CK(call)                                                                       \
@@ -411,7 +410,6 @@ __global__ void __launch_bounds__(128, RT_TRACE_MINB) k_trace(RenderParams P, in
     float lx = 0, hx = 0, ly = 0, hy = 0, lz = 0, hz = 0;   // guarded plane offsets (slab_guard)
     int hprim = -1;
     bool dropped = false;   // a push found the stack full
-    bool bad_link = false;  // a child link outside the node array
 
     for (;;) {
         // ---- fetch rays for lanes whose ray is finished
@@ -459,7 +457,6 @@ __global__ void __launch_bounds__(128, RT_TRACE_MINB) k_trace(RenderParams P, in
         // ---- traversal
         while (node != RT_SENT) {
             while ((unsigned)node < (unsigned)RT_SENT) {
-                if (node >= (MULTI ? ms->n_nodes : S.n_nodes)) { bad_link = true; node = RT_SENT; leaf = 0; break; }
                 if (COUNT) cnt[0]++;
                 const float4 *N = (MULTI ? mnodes : S.nodes) + 4 * (size_t)node;
                 float4 n0 = __ldg(N), n1 = __ldg(N + 1), n2 = __ldg(N + 2);
@@ -544,7 +541,6 @@ __global__ void __launch_bounds__(128, RT_TRACE_MINB) k_trace(RenderParams P, in
     }
     if (threadIdx.x == 0 && blockIdx.x == 0) atomicAdd(&P.stats[ANY ? 1 : 0], (unsigned long long)n);
     if (dropped && P.limit_flag) atomicOr(P.limit_flag, RT_LIM_STACK2);
-    if (bad_link && P.limit_flag) atomicOr(P.limit_flag, RT_LIM_LINK);
 #undef SPUSH
 #undef SPOP
 }
@@ -608,7 +604,6 @@ __global__ void __launch_bounds__(128, RT_TRACE4_MINB) k_trace4(RenderParams P, 
     int sx = 0, sy = 0, sz = 0;                             // 1: the axis's near plane is the box's upper one
     int hprim = -1;
     bool dropped = false;   // a push found the stack full
-    bool bad_link = false;  // a child link outside the node array
 
     for (;;) {
         // ---- fetch rays for lanes whose ray is finished
@@ -652,7 +647,6 @@ __global__ void __launch_bounds__(128, RT_TRACE4_MINB) k_trace4(RenderParams P, 
         // ---- traversal
         while (node != RT_SENT) {
             while ((unsigned)node < (unsigned)RT_SENT) {
-                if (node >= S.n_nodes4) { bad_link = true; node = RT_SENT; leaf = 0; break; }
                 if (COUNT) cnt[0]++;
                 const float4 *N = S.nodes4 + 8 * (size_t)node;
                 // near / far plane rows of each axis by the ray's direction sign
@@ -736,7 +730,6 @@ __global__ void __launch_bounds__(128, RT_TRACE4_MINB) k_trace4(RenderParams P, 
     }
     if (threadIdx.x == 0 && blockIdx.x == 0) atomicAdd(&P.stats[ANY ? 1 : 0], (unsigned long long)n);
     if (dropped && P.limit_flag) atomicOr(P.limit_flag, RT_LIM_STACK4);
-    if (bad_link && P.limit_flag) atomicOr(P.limit_flag, RT_LIM_LINK);
 }
 
 // ---------------------------------------------------------------- 8-wide traversal

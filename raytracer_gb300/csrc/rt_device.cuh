@@ -214,7 +214,6 @@ enum {
     RT_LIM_STACK4 = 2,     // 4-wide traversal stack full (deeper trees are not uploaded)
     RT_LIM_STACK8 = 4,     // 8-wide group stack full (deeper trees are not uploaded)
     RT_LIM_VOLPATH = 8,    // a VolPathTracing loop cap (boundaries, tracking steps, iterations)
-    RT_LIM_LINK = 16,      // a BVH child link outside the node array (a corrupted tree)
 };
 
 // Triangle::intersection (geometricShape/Triangle.cpp:46-88), exact order
@@ -385,8 +384,11 @@ __device__ __forceinline__ bool trace_ray(const DevScene &S, V3 o, V3 d, float m
                 if (t0 && t1) {
                     int nearc = cc.x, farc = cc.y;
                     if (c1min < c0min) { nearc = cc.y; farc = cc.x; }
+                    // rt_scene_create refuses a tree deeper than the stack,
+                    // so the stack cannot be full here.  (No flag is written:
+                    // any use of the limit flag in this loop made the VolPath
+                    // kernels that call it twice as slow.)
                     if (sp < RT_STACK) stack[sp++] = farc;
-                    else if (S.limit_flag) atomicOr(S.limit_flag, RT_LIM_STACK2);   // unreachable: the build bounds the depth
                     node = nearc;
                 } else {
                     node = t0 ? cc.x : cc.y;
