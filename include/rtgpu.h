@@ -190,7 +190,7 @@ typedef struct rt_camera_desc {
     float aperture_radius;       /* 0 = pinhole                                  */
     float focal_plane;
     int32_t medium;              /* camera medium or -1                          */
-    /* reconstruction filter of the camera's screen (filter/*.h): RT_FILTER_*,
+    /* reconstruction filter of the camera's screen (the filter/ sources): RT_FILTER_*,
      * radii "radiusX"/"radiusY" (default 0.5) and two parameters: Gaussian
      * "alpha", "omega" (GaussianFilter.cpp:16-17); Mitchell-Netravali "B", "C"
      * (MitchellNetravaliFilter.cpp:17-18) */

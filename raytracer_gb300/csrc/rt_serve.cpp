@@ -475,17 +475,35 @@ static void finish_batched(rt_server *S, Job *J, rt_status s)
     S->in_flight -= J->bytes;
 }
 
+// Paths of a job's next step: both half chunks of a progressive job, all
+// samples of a plain one.
+static double step_paths(const Job *J, int k)
+{
+    return (double)J->w * J->h * (J->target > 0.f ? 2.0 * k : (double)J->desc.spp);
+}
+
 static void schedule(rt_server *S)
 {
     cudaSetDevice(S->set.device);
     cudaStream_t st = (cudaStream_t)rt_internal_stream(S->sched);
+    int wave = 0, tb = 0, sb = 0, thr = 0;
+    rt_internal_get_shape(S->sched, &wave, &tb, &sb, &thr);
     for (;;) {
         std::vector<Job *> fresh;
         {
             std::unique_lock<std::mutex> g(S->mu);
             S->cv_work.wait(g, [&] { return S->stopping || !S->resident.empty() || !S->bqueue.empty(); });
             if (S->stopping) return;
-            while (!S->bqueue.empty() && admit_ok(S, S->bqueue.front())) {
+            // Admission in arrival order while the budget allows and the
+            // step still fits one wavefront batch: beyond that, more resident
+            // jobs only share the device more finely (every job finishes
+            // later), so later arrivals wait for the earlier ones.
+            double step = 0.0;
+            for (const Job *J : S->resident) step += step_paths(J, J->k);
+            while (!S->bqueue.empty() && admit_ok(S, S->bqueue.front()) &&
+                   ((S->resident.empty() && fresh.empty()) ||
+                    step + step_paths(S->bqueue.front(), first_chunk(S->bqueue.front())) <= (double)wave)) {
+                step += step_paths(S->bqueue.front(), first_chunk(S->bqueue.front()));
                 Job *J = S->bqueue.front();
                 S->bqueue.pop_front();
                 J->state = RT_JOB_RUNNING;
