@@ -238,8 +238,9 @@ def run_reference(args):
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample_desc},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "notes": "reference CPU path = the oracle's C restatement of the integrator with the reference's "
-                     "two-level SAH BVH (the reference itself needs Eigen/SFML/OpenEXR/OpenVDB, absent here); "
-                     "oracle scene build %.1f s not timed" % build_s}
+                     "two-level SAH BVH, whose per-path radiance is bit-identical to the reference's own "
+                     "PathTracingMIS compiled from its sources (pin tests); those sources are not on this "
+                     "machine, so the restatement is what runs; oracle scene build %.1f s not timed" % build_s}
     print(json.dumps(line))
 
 
