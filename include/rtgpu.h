@@ -545,6 +545,33 @@ rt_status rt_server_stop(rt_server *srv);
 rt_status rt_trace(rt_ctx *ctx, rt_scene *scene, const rt_ray *rays, int32_t n,
                    int32_t anyhit, rt_hit *hits, int32_t on_device);
 
+/* A binary BVH built by the caller, as topology: node i is internal when
+ * count == 0 (children left, right), else a leaf over prims[first, first +
+ * count) (indices of the scene's triangles, the order of rt_scene_desc's
+ * indices).  Node 0 is the root; every node is reached once and every
+ * triangle is in exactly one leaf. */
+typedef struct rt_bvh_node {
+    int32_t left, right, first, count;
+} rt_bvh_node;
+/* rt_scene_create with the caller's tree instead of the library's SAH build:
+ * the device traverses the reference's own tree.  Stands in for Bvh::build
+ * and Bvh::flatten (accelStruct/Bvh.cpp:51-79, 587-607) over the primitives
+ * MeshFactory and Scene::initialize arrange in two levels
+ * (factory/MeshFactory.h:123, core/Scene.cpp:117): the plugin flattens the
+ * top-level tree with every mesh leaf replaced by that mesh's tree (analytic
+ * spheres and planes are left out: they are tested after the tree).  Boxes
+ * are recomputed from the triangles and widened as the library's own build
+ * widens them; leaves of more than 8 triangles are split in halves of their
+ * range; a tree deeper than 62 levels is refused (RT_ERR_INVALID), as is a
+ * malformed one.  The 4-wide tree is collapsed from this one. */
+rt_status rt_scene_create_bvh(rt_ctx *ctx, const rt_scene_desc *desc, const rt_bvh_node *nodes, int32_t n_nodes,
+                              const int32_t *prims, int32_t n_prims, rt_scene **out);
+/* Host-only check of such a tree over n triangles (9 floats each): the
+ * device image rt_scene_create_bvh would upload, checked structurally; its
+ * depth and internal node count.  Needs no GPU. */
+rt_status rt_bvh_import_check(const float *tri_v, int32_t n, const rt_bvh_node *nodes, int32_t n_nodes,
+                              const int32_t *prims, int32_t n_prims, int32_t *max_depth, int32_t *n_device_nodes);
+
 /* Host-only: build the device tree (width 2: binary, 4: 4-wide collapsed
  * from the binary one, 8: compressed 8-wide) over n triangles (9 floats
  * each) as rt_scene_create would, and report its deepest level (root 0) and

@@ -209,6 +209,8 @@ typedef struct {
 } o_hit;
 
 o_bvh *o_bvh_build_scene(const o_scene *sc);
+int32_t oracle_export_bvh(const o_scene *sc, rt_bvh_node *nodes, int32_t cap_nodes, int32_t *prims,
+                          int32_t cap_prims, int32_t *n_nodes, int32_t *n_prims);
 void o_bvh_free(o_bvh *b);
 int o_intersect(const o_scene *sc, const o_ray *ray, o_hit *hit, int shadow);
 int o_bvh_node_count(const o_bvh *b);

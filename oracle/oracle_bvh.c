@@ -361,6 +361,92 @@ o_bvh *o_bvh_build_scene(const o_scene *sc)
     return t;
 }
 
+/* ---------------- export (test infrastructure for rt_scene_create_bvh) ----
+ * The two-level tree of o_bvh_build_scene as one binary tree over the
+ * scene's triangles, the form a plugin hands to rt_scene_create_bvh: every
+ * top-level mesh leaf replaced by that mesh's tree, spheres and planes left
+ * out (the device tests them after the tree), a top-level leaf of several
+ * meshes joined into a chain.  Nodes are numbered in post-order and the root
+ * is then swapped to index 0. */
+typedef struct { rt_bvh_node *nodes; int n, cap; int32_t *prims; int np, capp; int err; } o_exp;
+
+static int exp_new(o_exp *E)
+{
+    if (E->n >= E->cap) { E->err = 1; return -1; }
+    int k = E->n++;
+    E->nodes[k].left = E->nodes[k].right = -1;
+    E->nodes[k].first = E->nodes[k].count = 0;
+    return k;
+}
+static int exp_join(o_exp *E, int l, int r)
+{
+    if (l < 0) return r;
+    if (r < 0) return l;
+    int k = exp_new(E);
+    if (k < 0) return -1;
+    E->nodes[k].left = l;
+    E->nodes[k].right = r;
+    return k;
+}
+static int exp_mesh(o_exp *E, const o_bvh *b, int i)
+{
+    const o_lnode *ln = &b->nodes[i];
+    if (ln->right < 0) {   /* leaf */
+        if (ln->count <= 0) return -1;
+        int k = exp_new(E);
+        if (k < 0) return -1;
+        E->nodes[k].first = E->np;
+        E->nodes[k].count = ln->count;
+        for (int j = 0; j < ln->count; j++) {
+            if (E->np >= E->capp) { E->err = 1; return -1; }
+            E->prims[E->np++] = b->prims[ln->first + j].id;
+        }
+        return k;
+    }
+    int l = exp_mesh(E, b, i + 1);
+    int r = exp_mesh(E, b, ln->right);
+    return exp_join(E, l, r);
+}
+static int exp_top(o_exp *E, const o_bvh *t, int i)
+{
+    const o_lnode *ln = &t->nodes[i];
+    if (ln->right < 0) {
+        int acc = -1;
+        for (int j = 0; j < ln->count; j++) {
+            o_pref p = t->prims[ln->first + j];
+            if (p.kind != P_MESH) continue;
+            const o_bvh *s = t->sub[p.id];
+            if (s && s->n_nodes > 0) acc = exp_join(E, acc, exp_mesh(E, s, 0));
+        }
+        return acc;
+    }
+    int l = exp_top(E, t, i + 1);
+    int r = exp_top(E, t, ln->right);
+    return exp_join(E, l, r);
+}
+int32_t oracle_export_bvh(const o_scene *sc, rt_bvh_node *nodes, int32_t cap_nodes, int32_t *prims, int32_t cap_prims,
+                          int32_t *n_nodes, int32_t *n_prims)
+{
+    o_exp E = {nodes, 0, cap_nodes, prims, 0, cap_prims, 0};
+    int root = (sc->top && sc->top->n_nodes > 0) ? exp_top(&E, sc->top, 0) : -1;
+    if (E.err) return 1;
+    if (root > 0) {
+        rt_bvh_node tmp = E.nodes[0];
+        E.nodes[0] = E.nodes[root];
+        E.nodes[root] = tmp;
+        for (int k = 0; k < E.n; k++) {
+            if (E.nodes[k].count != 0) continue;
+            if (E.nodes[k].left == 0) E.nodes[k].left = root;
+            else if (E.nodes[k].left == root) E.nodes[k].left = 0;
+            if (E.nodes[k].right == 0) E.nodes[k].right = root;
+            else if (E.nodes[k].right == root) E.nodes[k].right = 0;
+        }
+    }
+    *n_nodes = E.n;
+    *n_prims = E.np;
+    return 0;
+}
+
 /* ---------------- intersection ---------------- */
 typedef struct { float t, u, v; int prim; v3 p; } o_rec;
 

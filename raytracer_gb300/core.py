@@ -114,6 +114,11 @@ def lib():
     L.rt_host_free.restype = None
     L.rt_bvh_stats.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
     L.rt_bvh_stats.restype = C.c_int32
+    L.rt_scene_create_bvh.argtypes = [vp, C.POINTER(D.SceneDesc), vp, C.c_int32, vp, C.c_int32, C.POINTER(vp)]
+    L.rt_scene_create_bvh.restype = C.c_int32
+    L.rt_bvh_import_check.argtypes = [vp, C.c_int32, vp, C.c_int32, vp, C.c_int32, C.POINTER(C.c_int32),
+                                      C.POINTER(C.c_int32)]
+    L.rt_bvh_import_check.restype = C.c_int32
     for name in ("rt_ctx_create", "rt_ctx_destroy", "rt_ctx_set_stream", "rt_scene_create", "rt_scene_destroy",
                  "rt_scene_info", "rt_render", "rt_render_stats_get", "rt_ctx_set_profiling", "rt_ctx_set_bvh_width", "rt_ctx_set_wave_paths", "rt_ctx_set_ray_sort", "rt_ctx_set_graphs",
                  "rt_ctx_get_tuning", "rt_ctx_set_tuning", "rt_autotune",
@@ -251,12 +256,21 @@ class Context:
 class Scene:
     """A SceneData flattened and uploaded to the device (rt_scene)."""
 
-    def __init__(self, ctx, scene):
+    def __init__(self, ctx, scene, bvh=None):
+        """bvh: optional (nodes, prims) of a binary tree built elsewhere
+        (rt_scene_create_bvh): nodes (n, 4) int32 rows (left, right, first,
+        count), prims the triangle index of every leaf slot."""
         self.ctx = ctx
         self.data = scene
         self._desc = scene.desc()
         self.h = C.c_void_p()
-        _check(lib().rt_scene_create(ctx.h, C.byref(self._desc), C.byref(self.h)))
+        if bvh is None:
+            _check(lib().rt_scene_create(ctx.h, C.byref(self._desc), C.byref(self.h)))
+        else:
+            nodes = np.ascontiguousarray(bvh[0], np.int32).reshape(-1, 4)
+            prims = np.ascontiguousarray(bvh[1], np.int32).reshape(-1)
+            _check(lib().rt_scene_create_bvh(ctx.h, C.byref(self._desc), _p(nodes), len(nodes), _p(prims), len(prims),
+                                             C.byref(self.h)))
         self.width = scene.camera["width"]
         self.height = scene.camera["height"]
 
@@ -434,6 +448,19 @@ def bvh_stats(tri_v, width=2, depth_cap=0):
     tv = np.ascontiguousarray(tri_v, np.float32).reshape(-1)
     d, n = C.c_int32(), C.c_int32()
     _check(lib().rt_bvh_stats(_p(tv), len(tv) // 9, width, depth_cap, C.byref(d), C.byref(n)))
+    return d.value, n.value
+
+
+def bvh_import_check(tri_v, nodes, prims):
+    """The device image rt_scene_create_bvh would upload for a tree built
+    elsewhere (rt_bvh_import_check, no GPU needed): (depth, internal nodes);
+    raises RtError if the tree is malformed."""
+    tv = np.ascontiguousarray(tri_v, np.float32).reshape(-1)
+    nodes = np.ascontiguousarray(nodes, np.int32).reshape(-1, 4)
+    prims = np.ascontiguousarray(prims, np.int32).reshape(-1)
+    d, n = C.c_int32(), C.c_int32()
+    _check(lib().rt_bvh_import_check(_p(tv), len(tv) // 9, _p(nodes), len(nodes), _p(prims), len(prims),
+                                     C.byref(d), C.byref(n)))
     return d.value, n.value
 
 

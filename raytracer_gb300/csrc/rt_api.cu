@@ -2029,7 +2029,16 @@ static rt_status validate(const rt_scene_desc *d)
     return RT_OK;
 }
 
-rt_status rt_scene_create(rt_ctx *ctx, const rt_scene_desc *d, rt_scene **out)
+// a caller-built binary tree (rt_scene_create_bvh)
+struct ExtTree {
+    const rt_bvh_node *nodes;
+    int n_nodes;
+    const int32_t *prims;
+    int n_prims;
+};
+static_assert(sizeof(rt_bvh_node) == sizeof(ExtNode), "rt_bvh_node and ExtNode share one layout");
+
+static rt_status scene_create(rt_ctx *ctx, const rt_scene_desc *d, const ExtTree *ext, rt_scene **out)
 {
     if (!ctx || !out) return fail(RT_ERR_INVALID, "rt_scene_create: null argument");
     *out = nullptr;
@@ -2256,9 +2265,19 @@ rt_status rt_scene_create(rt_ctx *ctx, const rt_scene_desc *d, rt_scene **out)
     }
     // BVH
     BvhImage img;
-    build_bvh2(tri_v.data(), nt, img, RT_BVH_LEAF, RT_BVH_BINS, RT_BVH_CNODE);
+    if (ext) {
+        std::string why;
+        if (!import_bvh2(tri_v.data(), nt, reinterpret_cast<const ExtNode *>(ext->nodes), ext->n_nodes, ext->prims,
+                         ext->n_prims, img, &why)) {
+            rt_scene_destroy(sc);
+            return fail(RT_ERR_INVALID, "rt_scene_create_bvh: " + why);
+        }
+    } else {
+        build_bvh2(tri_v.data(), nt, img, RT_BVH_LEAF, RT_BVH_BINS, RT_BVH_CNODE);
+    }
     // the traversal stacks hold a sentinel plus one entry per level; the
-    // builder bounds the depth (RT_BVH_DEPTH_CAP), so this only guards it
+    // builder (and the import) bound the depth (RT_BVH_DEPTH_CAP), so this
+    // only guards it
     if (img.max_depth + 1 > RT_STACK) {
         rt_scene_destroy(sc);
         return fail(RT_ERR_LIMIT, "rt_scene_create: BVH depth " + std::to_string(img.max_depth) +
@@ -2383,6 +2402,37 @@ rt_status rt_scene_create(rt_ctx *ctx, const rt_scene_desc *d, rt_scene **out)
     sc->n_media = d->n_media;
     for (int b = 0; b < d->n_bsdfs; b++) sc->bsdf_types |= 1 << bsdf_queue_of(bsdfs[b]);
     *out = sc;
+    return RT_OK;
+}
+
+rt_status rt_scene_create(rt_ctx *ctx, const rt_scene_desc *d, rt_scene **out)
+{
+    return scene_create(ctx, d, nullptr, out);
+}
+
+rt_status rt_scene_create_bvh(rt_ctx *ctx, const rt_scene_desc *d, const rt_bvh_node *nodes, int32_t n_nodes,
+                              const int32_t *prims, int32_t n_prims, rt_scene **out)
+{
+    if (n_nodes < 0 || n_prims < 0 || (n_nodes > 0 && !nodes) || (n_prims > 0 && !prims))
+        return fail(RT_ERR_INVALID, "rt_scene_create_bvh: bad tree arguments");
+    ExtTree t{nodes, n_nodes, prims, n_prims};
+    return scene_create(ctx, d, &t, out);
+}
+
+rt_status rt_bvh_import_check(const float *tri_v, int32_t n, const rt_bvh_node *nodes, int32_t n_nodes,
+                              const int32_t *prims, int32_t n_prims, int32_t *max_depth, int32_t *n_device_nodes)
+{
+    if (n < 0 || (n > 0 && !tri_v) || n_nodes < 0 || n_prims < 0 || (n_nodes > 0 && !nodes) || (n_prims > 0 && !prims))
+        return fail(RT_ERR_INVALID, "rt_bvh_import_check: bad argument");
+    BvhImage img;
+    std::string why;
+    if (!import_bvh2(tri_v, n, reinterpret_cast<const ExtNode *>(nodes), n_nodes, prims, n_prims, img, &why))
+        return fail(RT_ERR_INVALID, "rt_bvh_import_check: " + why);
+    int walked = 0;
+    if (n > 0 && !check_bvh2(img, tri_v, n, &walked, &why))
+        return fail(RT_ERR_INVALID, "rt_bvh_import_check: malformed image: " + why);
+    if (max_depth) *max_depth = img.max_depth;
+    if (n_device_nodes) *n_device_nodes = img.n_nodes;
     return RT_OK;
 }
 

@@ -193,40 +193,15 @@ inline void widen(const Box &b, float scale_eps, float out[6])
 
 }  // namespace
 
-void build_bvh2(const float *tv, int n, BvhImage &img, int max_leaf, int n_bins, double c_node, int depth_cap)
+// The device image of a built tree: internal nodes in build order (a root
+// leaf gets a synthetic parent with an empty second child), triangle slots
+// in leaf order, boxes widened.
+static void write_image(const float *tv, int n, const std::vector<BuildNode> &bn, const std::vector<int> &order,
+                        float seps, int maxd, BvhImage &img)
 {
-    img = BvhImage();
-    if (n <= 0) return;
-    max_leaf = std::max(1, std::min(max_leaf, 8));
-    Builder B;
-    B.depth_cap = depth_cap;
-    B.tv = tv;
-    B.max_leaf = max_leaf;
-    B.n_bins = n_bins;
-    B.c_node = c_node;
-    B.tb.resize(n);
-    B.cen.resize(3 * (size_t)n);
-    B.order.resize(n);
-    Box scene; scene.reset();
-    for (int t = 0; t < n; t++) {
-        Box b; b.reset();
-        for (int k = 0; k < 3; k++) b.grow(tv + 9 * (size_t)t + 3 * k);
-        B.tb[t] = b;
-        scene.grow(b);
-        for (int a = 0; a < 3; a++) B.cen[3 * (size_t)t + a] = 0.5f * (b.mn[a] + b.mx[a]);
-        B.order[t] = t;
-    }
-    float sext = 0.f;
-    for (int a = 0; a < 3; a++) sext = std::max(sext, scene.mx[a] - scene.mn[a]);
-    float seps = std::max(sext * 1e-7f, 1e-30f);
-    std::vector<BuildNode> bn;
-    bn.reserve(2 * (size_t)n / std::max(1, max_leaf) + 16);
-    int maxd = 0;
-    B.build(0, n, bn, 0, maxd);
-    // leaves larger than 8 cannot be encoded: split them (only happens for
-    // n > max_leaf with identical centroids, handled by the mid split above)
-    // Map build nodes -> device internal nodes.  A root leaf gets a
-    // synthetic internal parent with an empty second child.
+    // Leaves hold at most 8 triangles (a link encodes count - 1 in 3 bits);
+    // both builders guarantee it.  Build nodes map to device internal nodes;
+    // a root leaf gets a synthetic internal parent with an empty second child.
     std::vector<int> dev_index(bn.size(), -1);
     int n_int = 0;
     for (size_t i = 0; i < bn.size(); i++) if (!bn[i].leaf) dev_index[i] = n_int++;
@@ -237,7 +212,7 @@ void build_bvh2(const float *tv, int n, BvhImage &img, int max_leaf, int n_bins,
     img.n_slots = n;
     img.tri_slots.assign(12 * (size_t)n, 0.f);
     for (int s = 0; s < n; s++) {
-        int t = B.order[s];
+        int t = order[s];
         const float *p = tv + 9 * (size_t)t;
         float *o = &img.tri_slots[12 * (size_t)s];
         int32_t id = t;
@@ -278,6 +253,39 @@ void build_bvh2(const float *tv, int n, BvhImage &img, int max_leaf, int n_bins,
     }
     img.max_depth = maxd;
     img.sah_cost = sah;
+}
+
+void build_bvh2(const float *tv, int n, BvhImage &img, int max_leaf, int n_bins, double c_node, int depth_cap)
+{
+    img = BvhImage();
+    if (n <= 0) return;
+    max_leaf = std::max(1, std::min(max_leaf, 8));
+    Builder B;
+    B.depth_cap = depth_cap;
+    B.tv = tv;
+    B.max_leaf = max_leaf;
+    B.n_bins = n_bins;
+    B.c_node = c_node;
+    B.tb.resize(n);
+    B.cen.resize(3 * (size_t)n);
+    B.order.resize(n);
+    Box scene; scene.reset();
+    for (int t = 0; t < n; t++) {
+        Box b; b.reset();
+        for (int k = 0; k < 3; k++) b.grow(tv + 9 * (size_t)t + 3 * k);
+        B.tb[t] = b;
+        scene.grow(b);
+        for (int a = 0; a < 3; a++) B.cen[3 * (size_t)t + a] = 0.5f * (b.mn[a] + b.mx[a]);
+        B.order[t] = t;
+    }
+    float sext = 0.f;
+    for (int a = 0; a < 3; a++) sext = std::max(sext, scene.mx[a] - scene.mn[a]);
+    float seps = std::max(sext * 1e-7f, 1e-30f);
+    std::vector<BuildNode> bn;
+    bn.reserve(2 * (size_t)n / std::max(1, max_leaf) + 16);
+    int maxd = 0;
+    B.build(0, n, bn, 0, maxd);
+    write_image(tv, n, bn, B.order, seps, maxd, img);
 }
 
 namespace {
@@ -546,6 +554,101 @@ void build_bvh4(const BvhImage &b2, Bvh4Image &out)
         }
         for (int i = 28; i < 32; i++) o[i] = 0.f;
     }
+}
+
+bool import_bvh2(const float *tv, int n, const ExtNode *nodes, int n_nodes, const int32_t *prims, int n_prims,
+                 BvhImage &img, std::string *why, int depth_cap)
+{
+    img = BvhImage();
+    auto bad = [&](const std::string &m) { if (why) *why = m; return false; };
+    if (n <= 0) return n_nodes == 0 ? true : bad("a tree for a scene without triangles");
+    if (n_nodes <= 0 || !nodes) return bad("no nodes");
+    if (n_prims != n || !prims) return bad("the leaves must list every triangle once");
+    // Walk the tree (explicit stack): every node once, leaves in depth-first
+    // order, every triangle once.  A leaf of more than 8 triangles becomes a
+    // balanced subtree over halves of its range.
+    struct Item { int node; int first, count; int depth; int parent; int side; };
+    std::vector<char> seen(n_nodes, 0), tri_seen(n, 0);
+    std::vector<BuildNode> bn;          // the tree as build_bvh2 would produce it
+    std::vector<int> order;             // triangle per slot
+    order.reserve(n);
+    std::vector<Item> todo;
+    todo.push_back({0, 0, 0, 0, -1, 0});
+    int maxd = 0;
+    while (!todo.empty()) {
+        Item it = todo.back();
+        todo.pop_back();
+        int first = it.first, count = it.count;
+        bool split_leaf = it.node < 0;   // a half of an oversized leaf
+        if (!split_leaf) {
+            if (it.node >= n_nodes) return bad("child index out of range");
+            if (seen[it.node]) return bad("a node is reached twice");
+            seen[it.node] = 1;
+            const ExtNode &e = nodes[it.node];
+            if (e.count < 0) return bad("negative leaf size");
+            if (e.count == 0) {
+                if (e.left < 0 || e.right < 0 || e.left >= n_nodes || e.right >= n_nodes)
+                    return bad("internal node with a missing child");
+                const int self = (int)bn.size();
+                bn.emplace_back();
+                if (it.parent >= 0) bn[it.parent].child[it.side] = self;
+                maxd = std::max(maxd, it.depth);
+                // right first on the stack, so the left subtree is laid out first
+                todo.push_back({e.right, 0, 0, it.depth + 1, self, 1});
+                todo.push_back({e.left, 0, 0, it.depth + 1, self, 0});
+                continue;
+            }
+            if (e.first < 0 || (int64_t)e.first + e.count > n_prims) return bad("leaf range outside the triangle list");
+            first = e.first;
+            count = e.count;
+        }
+        if (count > 8) {
+            const int self = (int)bn.size();
+            bn.emplace_back();
+            if (it.parent >= 0) bn[it.parent].child[it.side] = self;
+            maxd = std::max(maxd, it.depth);
+            const int h = count / 2;
+            todo.push_back({-1, first + h, count - h, it.depth + 1, self, 1});
+            todo.push_back({-1, first, h, it.depth + 1, self, 0});
+            continue;
+        }
+        const int self = (int)bn.size();
+        bn.emplace_back();
+        if (it.parent >= 0) bn[it.parent].child[it.side] = self;
+        maxd = std::max(maxd, it.depth);
+        BuildNode &L = bn[self];
+        L.leaf = true;
+        L.first = (int)order.size();
+        L.count = count;
+        for (int k = 0; k < count; k++) {
+            const int t = prims[first + k];
+            if (t < 0 || t >= n) return bad("triangle index out of range");
+            if (tri_seen[t]) return bad("a triangle is in two leaves");
+            tri_seen[t] = 1;
+            order.push_back(t);
+        }
+    }
+    if ((int)order.size() != n) return bad("some triangles are in no leaf");
+    if (maxd > depth_cap) return bad("deeper than the traversal stacks allow (" + std::to_string(maxd) + " levels)");
+    // boxes bottom-up: children come after their parent in bn
+    Box scene; scene.reset();
+    for (int i = (int)bn.size() - 1; i >= 0; i--) {
+        BuildNode &b = bn[i];
+        b.box.reset();
+        if (b.leaf) {
+            for (int k = 0; k < b.count; k++)
+                for (int c = 0; c < 3; c++) b.box.grow(tv + 9 * (size_t)order[b.first + k] + 3 * c);
+        } else {
+            b.box.grow(bn[b.child[0]].box);
+            b.box.grow(bn[b.child[1]].box);
+        }
+    }
+    scene = bn[0].box;
+    float sext = 0.f;
+    for (int a = 0; a < 3; a++) sext = std::max(sext, scene.mx[a] - scene.mn[a]);
+    const float seps = std::max(sext * 1e-7f, 1e-30f);
+    write_image(tv, n, bn, order, seps, maxd, img);
+    return true;
 }
 
 bool check_bvh4(const Bvh4Image &w, const BvhImage &b2, std::string *why)

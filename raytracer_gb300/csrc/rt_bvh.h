@@ -53,6 +53,20 @@ void build_bvh4(const BvhImage &b2, Bvh4Image &out);
 // the BVH2's box, unused slots all +inf.
 bool check_bvh4(const Bvh4Image &w, const BvhImage &b2, std::string *why);
 
+// A binary tree built elsewhere (the reference's SAH BVH, flattened to one
+// tree over the scene's triangles), as topology only: node i is internal
+// when count == 0 (children left and right), else a leaf over
+// prims[first, first + count) (triangle indices).  Node 0 is the root.
+struct ExtNode { int32_t left, right, first, count; };
+
+// The BVH2 image of such a tree: every node reached once, every triangle in
+// exactly one leaf; boxes are recomputed from the triangles (and widened as
+// build_bvh2 widens them), and leaves of more than 8 triangles are split in
+// halves of their range.  False with a reason when the tree is malformed or
+// deeper than depth_cap.
+bool import_bvh2(const float *tri_v, int n_tris, const ExtNode *nodes, int n_nodes, const int32_t *prims,
+                 int n_prims, BvhImage &out, std::string *why, int depth_cap = RT_BVH_DEPTH_CAP);
+
 // Compressed 8-wide BVH.  Each node is 5 float4 (80 bytes):
 //   w0 = (px, py, pz, bits: ex | ey << 8 | ez << 16)      grid origin, exponents
 //   w1 = (child_base, tri_base, meta[0..3], meta[4..7])   as int32 / packed bytes

@@ -36,6 +36,9 @@ def lib():
         L.oracle_render_paths.argtypes = [C.c_void_p, C.POINTER(D.RenderDesc), C.c_void_p, C.c_void_p,
                                           C.c_int32, C.c_void_p]
         L.oracle_trace.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_void_p]
+        L.oracle_export_bvh.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32,
+                                        C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+        L.oracle_export_bvh.restype = C.c_int32
         L.oracle_bsdf_query.argtypes = [C.POINTER(D.BsdfDesc), C.c_int32, C.c_void_p, C.c_int32, C.c_void_p]
         L.oracle_light_query.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p]
         L.oracle_medium_query.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p]
@@ -71,6 +74,18 @@ class OracleScene:
 
     def __del__(self):
         self.close()
+
+    def export_bvh(self):
+        """The reference's two-level tree as one binary tree over the scene's
+        triangles (nodes (n, 4) int32 left, right, first, count; prims), the
+        form rt_scene_create_bvh takes."""
+        nt = int(self.desc.n_triangles)
+        nodes = np.zeros((max(1, 2 * nt), 4), np.int32)
+        prims = np.zeros(max(1, nt), np.int32)
+        nn, npr = C.c_int32(), C.c_int32()
+        rc = lib().oracle_export_bvh(self.h, _p(nodes), len(nodes), _p(prims), len(prims), C.byref(nn), C.byref(npr))
+        assert rc == 0
+        return nodes[:nn.value].copy(), prims[:npr.value].copy()
 
     def render(self, spp, seed=0, sample_begin=0, threads=None, **over):
         rd = self.scene.render_desc(spp, seed=seed, sample_begin=sample_begin, **over)

@@ -92,3 +92,36 @@ def test_four_wide_collapse(lib, tris):
     cap = 12 if tris == "strip" else 16
     d4c, _ = core.bvh_stats(t, width=4, depth_cap=cap)
     assert d4c <= cap
+
+
+def test_reference_tree_import():
+    """rt_scene_create_bvh takes the reference's own tree: the oracle builds
+    the reference's two-level SAH BVH (Bvh.cpp, MeshFactory + Scene), flattens
+    it into one binary tree over the triangles, and the library's host import
+    turns it into the device image (rt_bvh_import_check checks every triangle
+    in one leaf and inside every box on its path)."""
+    import oracle_lib as O
+    from raytracer_gb300 import scenes
+    for s in (scenes.cornell_box(32, 32), scenes.displaced_icosphere(level=4, width=32, height=32, env_size=(64, 32))):
+        o = O.OracleScene(s)
+        nodes, prims = o.export_bvh()
+        tri = np.asarray(s.vertices, np.float32).reshape(-1, 3)[np.asarray(s.indices).reshape(-1, 3)]
+        assert sorted(prims.tolist()) == list(range(len(tri)))
+        d, n = core.bvh_import_check(tri, nodes, prims)
+        counts = nodes[:, 3]
+        leaves = int(np.count_nonzero(counts))
+        # leaves of more than 8 triangles are split in halves of their range
+        extra = int(sum(int(np.ceil(c / 8.0)) - 1 for c in counts if c > 8))
+        assert n >= len(nodes) - leaves + extra and 0 < d < 62
+        # malformed trees are refused
+        bad = nodes.copy()
+        bad[0, 0] = bad[0, 1]
+        with pytest.raises(core.RtError):
+            core.bvh_import_check(tri, bad, prims)
+        with pytest.raises(core.RtError):
+            core.bvh_import_check(tri, nodes, prims[:-1])
+        dup = prims.copy()
+        dup[0] = dup[1]
+        with pytest.raises(core.RtError):
+            core.bvh_import_check(tri, nodes, dup)
+        o.close()

@@ -61,11 +61,13 @@ def _width(ctx, w):
     ctx.set_bvh_width(w)
 
 
+@pytest.mark.parametrize("tree", ["library", "reference"])
 @pytest.mark.parametrize("w", [2, 4, 8], ids=["bvh2", "bvh4", "bvh8"])
-def test_full_tree_trace_parity(ctx, rtlib, ico_full, w):
+def test_full_tree_trace_parity(ctx, rtlib, ico_full, w, tree):
     """131,072 camera rays plus 131,072 secondary rays leaving the camera
     rays' hit points (uniform directions, the reference's adaptive epsilon)
-    on the 1.31M-triangle tree."""
+    on the 1.31M-triangle tree: the library's own SAH build, or the
+    reference's two-level tree through rt_scene_create_bvh."""
     s, o = ico_full
     rng = np.random.default_rng(11)
     W, H = s.camera["width"], s.camera["height"]
@@ -79,7 +81,7 @@ def test_full_tree_trace_parity(ctx, rtlib, ico_full, w):
     sec = np.zeros(len(p), D.RAY_DTYPE)
     sec["o"], sec["d"], sec["mint"], sec["maxt"] = p, d, 1e-4, 1e8
     rays = np.concatenate([cam, sec])
-    g = rtlib.Scene(ctx, s)
+    g = rtlib.Scene(ctx, s, bvh=o.export_bvh() if tree == "reference" else None)
     _width(ctx, w)
     try:
         hg = g.trace(rays)
@@ -96,8 +98,8 @@ def test_full_tree_trace_parity(ctx, rtlib, ico_full, w):
     tied = both & ~same
     assert np.all(hg["t"][tied] == ho["t"][tied]), "another triangle at another distance"
     ut, uu, uv = (_ulp_diff(hg[k][same], ho[k][same]).max(initial=0) for k in ("t", "u", "v"))
-    print("bvh%d: %d rays, %d hits, %d ties at equal distance, max ulp t %d u %d v %d" %
-          (w, len(rays), both.sum(), tied.sum(), ut, uu, uv))
+    print("bvh%d (%s tree): %d rays, %d hits, %d ties at equal distance, max ulp t %d u %d v %d" %
+          (w, tree, len(rays), both.sum(), tied.sum(), ut, uu, uv))
     assert len(rays) >= 200000 and both.sum() > 100000
     assert ut <= 2 and uu <= 2 and uv <= 2
     assert tied.sum() <= 1e-4 * both.sum()

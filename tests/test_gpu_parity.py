@@ -55,13 +55,13 @@ def vol():
     return scenes.volume_grid(40, 32, res=32)
 
 
-def _trace_parity(ctx, rtlib, scene, n=20000, seed=0):
+def _trace_parity(ctx, rtlib, scene, n=20000, seed=0, reference_tree=False):
     rng = np.random.default_rng(seed)
     rays = _random_rays(scene, n, rng)
     o = O.OracleScene(scene)
     cam = o.camera_rays(rng.random((n // 4, 2)) * [scene.camera["width"], scene.camera["height"]])
     rays = np.concatenate([rays, cam])
-    g = rtlib.Scene(ctx, scene)
+    g = rtlib.Scene(ctx, scene, bvh=o.export_bvh() if reference_tree else None)
     hg = g.trace(rays)
     ho = o.trace(rays)
     hit_g, hit_o = hg["prim"] != -1, ho["prim"] != -1
@@ -102,6 +102,34 @@ def test_trace_parity_icosphere(ctx, rtlib, ico, width):
 
 def test_trace_parity_spheres_and_boxes(ctx, rtlib, vol, width):
     _trace_parity(ctx, rtlib, vol, n=20000, seed=2)
+
+
+@pytest.mark.parametrize("which", ["cornell", "icosphere", "spheres_and_boxes"])
+def test_trace_parity_reference_tree(ctx, rtlib, cornell, ico, vol, width, which):
+    """The reference's own two-level SAH tree (built by the oracle as
+    Bvh.cpp builds it, flattened to one binary tree over the triangles) as
+    the device tree through rt_scene_create_bvh, under every traversal width
+    (the 4-wide tree collapses it; the 8-wide one is the library's own)."""
+    _trace_parity(ctx, rtlib, {"cornell": cornell, "icosphere": ico, "spheres_and_boxes": vol}[which],
+                  reference_tree=True)
+
+
+def test_film_parity_reference_tree(ctx, rtlib, cornell, ico):
+    """Films over the reference's own tree: the same as the oracle's."""
+    for s, spp, seed in ((cornell, 4, 11), (ico, 2, 3)):
+        o = O.OracleScene(s)
+        g = rtlib.Scene(ctx, s, bvh=o.export_bvh())
+        fg = g.render(spp, seed=seed, block=16)
+        fo = o.render(spp, seed=seed, block=16)
+        assert np.array_equal(fg[..., 3], fo[..., 3])
+        err = (np.abs(fg[..., :3].astype(np.float64) - fo[..., :3]) / np.maximum(np.abs(fo[..., :3]), 1e-3)).max(-1)
+        bad = float(np.mean(err > 1e-3))
+        print("%s over the reference tree: exact %.4f, >1e-3 %.4f" % (s.name, np.mean(err == 0), bad))
+        assert bad <= 0.002   # the library's own tree measures 0
+        ref = rtlib.Scene(ctx, s).render(spp, seed=seed, block=16)
+        assert np.array_equal(fg[..., 3], ref[..., 3])
+        g.close()
+        o.close()
 
 
 def test_trace_parity_planes(ctx, rtlib, width):
