@@ -545,6 +545,23 @@ rt_status rt_server_stop(rt_server *srv);
 rt_status rt_trace(rt_ctx *ctx, rt_scene *scene, const rt_ray *rays, int32_t n,
                    int32_t anyhit, rt_hit *hits, int32_t on_device);
 
+/* Move a resident scene's triangles: `vertices` holds new positions for all
+ * of the scene's vertices (3 floats each, the count and order of
+ * rt_scene_desc.vertices; `normals` likewise, required when and only when
+ * the scene has vertex normals), in host memory or, with on_device = 1, in
+ * device memory.  On the device, the triangle arrays are rewritten and the
+ * binary tree's boxes are recomputed bottom-up over its unchanged topology
+ * (widened as the build widens them), then the 4-wide tree's; the
+ * compressed 8-wide tree is dropped (renders at width 8 use the binary
+ * one).  Closest hits and occlusion afterwards equal those of a scene built
+ * from the new positions (a tie at equal distance may name another
+ * triangle); traversal slows as the positions drift from the ones the tree
+ * was built for.  Refused (RT_ERR_UNSUPPORTED) for scenes with an emissive
+ * mesh or a mesh bounding a grid medium, whose light CDFs or medium boxes
+ * would change.  Stands in for rebuilding the scene: the reference rebuilds
+ * every BVH per scene load (core/Scene.cpp:115-138). */
+rt_status rt_scene_refit(rt_ctx *ctx, rt_scene *scene, const float *vertices, const float *normals,
+                         int32_t on_device);
 /* A binary BVH built by the caller, as topology: node i is internal when
  * count == 0 (children left, right), else a leaf over prims[first, first +
  * count) (indices of the scene's triangles, the order of rt_scene_desc's

@@ -119,6 +119,8 @@ def lib():
     L.rt_bvh_import_check.argtypes = [vp, C.c_int32, vp, C.c_int32, vp, C.c_int32, C.POINTER(C.c_int32),
                                       C.POINTER(C.c_int32)]
     L.rt_bvh_import_check.restype = C.c_int32
+    L.rt_scene_refit.argtypes = [vp, vp, vp, vp, C.c_int32]
+    L.rt_scene_refit.restype = C.c_int32
     for name in ("rt_ctx_create", "rt_ctx_destroy", "rt_ctx_set_stream", "rt_scene_create", "rt_scene_destroy",
                  "rt_scene_info", "rt_render", "rt_render_stats_get", "rt_ctx_set_profiling", "rt_ctx_set_bvh_width", "rt_ctx_set_wave_paths", "rt_ctx_set_ray_sort", "rt_ctx_set_graphs",
                  "rt_ctx_get_tuning", "rt_ctx_set_tuning", "rt_autotune",
@@ -284,6 +286,17 @@ class Scene:
             self.close()
         except Exception:
             pass
+
+    def refit(self, vertices, normals=None):
+        """Move the scene's vertices (n, 3) (rt_scene_refit): host arrays, or
+        torch CUDA tensors for device memory."""
+        if hasattr(vertices, "data_ptr"):
+            _check(lib().rt_scene_refit(self.ctx.h, self.h, C.c_void_p(vertices.data_ptr()),
+                                        C.c_void_p(normals.data_ptr()) if normals is not None else None, 1))
+            return
+        v = np.ascontiguousarray(vertices, np.float32).reshape(-1)
+        n = np.ascontiguousarray(normals, np.float32).reshape(-1) if normals is not None else None
+        _check(lib().rt_scene_refit(self.ctx.h, self.h, _p(v), _p(n) if n is not None else None, 0))
 
     def info(self):
         b = np.zeros(6, np.float32)

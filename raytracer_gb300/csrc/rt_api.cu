@@ -1427,6 +1427,114 @@ __global__ void k_film_wide(RenderParams P, float4 *film, int t0, int t1, int ti
 }
 
 // ---------------------------------------------------------------- standalone queries
+// ---------------------------------------------------------------- scene refit
+// rt_scene_refit: new vertex positions into the triangle arrays, then the
+// binary tree's boxes bottom-up over its unchanged topology, widened as the
+// host build widens them, then the 4-wide tree's copies of them.
+__global__ void k_refit_tris(const float *vtx, const float *nrm, const int32_t *idx, int nt, float *tri_v, float *tri_n)
+{
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += gridDim.x * blockDim.x)
+        for (int k = 0; k < 3; k++) {
+            const size_t v = (size_t)idx[3 * (size_t)t + k];
+            for (int a = 0; a < 3; a++) {
+                tri_v[9 * (size_t)t + 3 * k + a] = vtx[3 * v + a];
+                if (tri_n) tri_n[9 * (size_t)t + 3 * k + a] = nrm[3 * v + a];
+            }
+        }
+}
+// triangle slots (p0 and id, e1 = p1 - p0, e2 = p2 - p0) from the new vertices
+__global__ void k_refit_slots(float4 *slots, int n_slots, const float *tri_v)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_slots; i += gridDim.x * blockDim.x) {
+        const float4 a = slots[3 * (size_t)i];
+        const float *P = tri_v + 9 * (size_t)__float_as_int(a.w);
+        slots[3 * (size_t)i] = make_float4(P[0], P[1], P[2], a.w);
+        slots[3 * (size_t)i + 1] = make_float4(P[3] - P[0], P[4] - P[1], P[5] - P[2], 0.f);
+        slots[3 * (size_t)i + 2] = make_float4(P[6] - P[0], P[7] - P[1], P[8] - P[2], 0.f);
+    }
+}
+// one level of internal nodes: the exact boxes of both children (a leaf's
+// triangles, or an internal child's two boxes from the deeper level) into
+// boxes[12 * node]: child 0 then child 1, each (min xyz, max xyz)
+__global__ void k_refit_level(const float4 *nodes, const float4 *slots, const float *tri_v, const int32_t *order,
+                              int begin, int end, float *boxes)
+{
+    for (int i = begin + blockIdx.x * blockDim.x + threadIdx.x; i < end; i += gridDim.x * blockDim.x) {
+        const int nd = order[i];
+        const float4 n1 = nodes[4 * (size_t)nd + 1];
+        const int4 cc = reinterpret_cast<const int4 *>(nodes)[4 * (size_t)nd + 3];
+        for (int k = 0; k < 2; k++) {
+            float b[6] = {RT_MAX_REAL, RT_MAX_REAL, RT_MAX_REAL, -RT_MAX_REAL, -RT_MAX_REAL, -RT_MAX_REAL};
+            const int link = k ? cc.y : cc.x;
+            // the empty second child of a root leaf (an inverted box) stays empty
+            const bool empty = k == 1 && !(n1.x <= n1.y);
+            if (empty) {
+                b[0] = b[1] = b[2] = INFINITY;
+                b[3] = b[4] = b[5] = -INFINITY;
+            } else if (link < 0) {
+                const int v = ~link, first = v >> 3, cnt = (v & 7) + 1;
+                for (int j = 0; j < cnt; j++) {
+                    const float *P = tri_v + 9 * (size_t)__float_as_int(slots[3 * (size_t)(first + j)].w);
+                    for (int c = 0; c < 3; c++)
+                        for (int a = 0; a < 3; a++) {
+                            b[a] = fminf(b[a], P[3 * c + a]);
+                            b[3 + a] = fmaxf(b[3 + a], P[3 * c + a]);
+                        }
+                }
+            } else {
+                const float *cb = boxes + 12 * (size_t)link;
+                for (int a = 0; a < 3; a++) {
+                    b[a] = fminf(cb[a], cb[6 + a]);
+                    b[3 + a] = fmaxf(cb[3 + a], cb[9 + a]);
+                }
+            }
+            for (int a = 0; a < 6; a++) boxes[12 * (size_t)nd + 6 * k + a] = b[a];
+        }
+    }
+}
+// every node's two child boxes widened (pad = extent 1e-6 + magnitude 1.2e-6
+// + 1e-7 of the scene's largest extent, as the host build pads) into the node
+__global__ void k_refit_widen(float4 *nodes, int n_nodes, const float *boxes)
+{
+    float sext = 0.f;
+    for (int a = 0; a < 3; a++) {
+        float mn = boxes[a], mx = boxes[3 + a];
+        if (boxes[6] <= boxes[9]) { mn = fminf(mn, boxes[6 + a]); mx = fmaxf(mx, boxes[9 + a]); }
+        sext = fmaxf(sext, mx - mn);
+    }
+    const float seps = fmaxf(sext * 1e-7f, 1e-30f);
+    for (int nd = blockIdx.x * blockDim.x + threadIdx.x; nd < n_nodes; nd += gridDim.x * blockDim.x) {
+        float w[2][6];
+        for (int k = 0; k < 2; k++) {
+            const float *b = boxes + 12 * (size_t)nd + 6 * k;
+            for (int a = 0; a < 3; a++) {
+                if (!(b[0] <= b[3])) { w[k][2 * a] = INFINITY; w[k][2 * a + 1] = -INFINITY; continue; }
+                const float ext = b[3 + a] - b[a];
+                const float m = fmaxf(fabsf(b[a]), fabsf(b[3 + a]));
+                const float pad = ext * 1e-6f + m * 1.2e-6f + seps;
+                w[k][2 * a] = b[a] - pad;
+                w[k][2 * a + 1] = b[3 + a] + pad;
+            }
+        }
+        nodes[4 * (size_t)nd] = make_float4(w[0][0], w[0][1], w[0][2], w[0][3]);
+        nodes[4 * (size_t)nd + 1] = make_float4(w[1][0], w[1][1], w[1][2], w[1][3]);
+        nodes[4 * (size_t)nd + 2] = make_float4(w[0][4], w[0][5], w[1][4], w[1][5]);
+    }
+}
+// the 4-wide tree's child planes: copies of the binary tree's (src[slot])
+__global__ void k_refit_bvh4(float *nodes4, int n4, const int32_t *src, const float4 *nodes2)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 4 * n4; i += gridDim.x * blockDim.x) {
+        const int s = src[i];
+        if (s < 0) continue;
+        const int nd = s >> 1, k = s & 1, slot = i & 3;
+        const float4 a = nodes2[4 * (size_t)nd + k], z = nodes2[4 * (size_t)nd + 2];
+        const float pl[6] = {a.x, a.y, a.z, a.w, k ? z.z : z.x, k ? z.w : z.y};
+        float *o = nodes4 + 32 * (size_t)(i >> 2);
+        for (int p = 0; p < 6; p++) o[4 * p + slot] = pl[p];
+    }
+}
+
 __global__ void k_trace_rays(DevScene S, const rt_ray *rays, int n, int any, rt_hit *hits)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1634,6 +1742,19 @@ struct rt_scene {
     std::vector<float> light_power_lum;  // per light, for the weighted strategy
     std::vector<DevLight> lights_host;
     DevLight *lights_dev = nullptr;
+    // rt_scene_refit: the vertex count and device indices, the binary tree's
+    // internal nodes deepest level first (level_off[l] .. level_off[l+1]),
+    // the 4-wide tree's slot sources, scratch for exact boxes; refit_why is
+    // empty when the scene can be refitted
+    int n_vertices = 0, n_tris = 0;
+    bool has_normals = false;
+    const int32_t *indices_dev = nullptr;
+    const int32_t *refit_order = nullptr;
+    std::vector<int> level_off;
+    const int32_t *bvh4_src = nullptr;
+    float *refit_boxes = nullptr;
+    std::string refit_why;
+    float sph_bounds[6] = {RT_MAX_REAL, RT_MAX_REAL, RT_MAX_REAL, -RT_MAX_REAL, -RT_MAX_REAL, -RT_MAX_REAL};
 };
 
 // Traversal of a scene under the context's tree width (rt_ctx_set_bvh_width):
@@ -1942,6 +2063,7 @@ rt_status rt_scene_destroy(rt_scene *sc)
 {
     if (!sc) return RT_OK;
     for (void *p : sc->allocs) cudaFree(p);
+    cudaFree(sc->refit_boxes);
     delete sc;
     return RT_OK;
 }
@@ -2132,6 +2254,11 @@ static rt_status scene_create(rt_ctx *ctx, const rt_scene_desc *d, const ExtTree
             V3 p = h_xf_point(Sd.to_world, v3(cx[k][0], cx[k][1], cx[k][2]));
             bmin[0] = h_smin(bmin[0], p.x); bmin[1] = h_smin(bmin[1], p.y); bmin[2] = h_smin(bmin[2], p.z);
             bmax[0] = h_smax(bmax[0], p.x); bmax[1] = h_smax(bmax[1], p.y); bmax[2] = h_smax(bmax[2], p.z);
+            const float pc[3] = {p.x, p.y, p.z};
+            for (int a = 0; a < 3; a++) {
+                sc->sph_bounds[a] = h_smin(sc->sph_bounds[a], pc[a]);
+                sc->sph_bounds[3 + a] = h_smax(sc->sph_bounds[3 + a], pc[a]);
+            }
         }
     }
     for (int i = 0; i < 3; i++) { sc->bounds[i] = bmin[i]; sc->bounds[3 + i] = bmax[i]; S.bmin[i] = bmin[i]; S.bmax[i] = bmax[i]; }
@@ -2287,6 +2414,44 @@ static rt_status scene_create(rt_ctx *ctx, const rt_scene_desc *d, const ExtTree
     if ((st = upload(sc, reinterpret_cast<const float4 *>(img.nodes.data()), (size_t)img.n_nodes * 4, &np)) != RT_OK) { rt_scene_destroy(sc); return st; }
     if ((st = upload(sc, reinterpret_cast<const float4 *>(img.tri_slots.data()), (size_t)img.n_slots * 3, &tp)) != RT_OK) { rt_scene_destroy(sc); return st; }
     S.nodes = np; S.tri_slots = tp; S.n_nodes = img.n_nodes;
+    if (nt > 0) {
+        // refit data: internal nodes by depth (children before parents when
+        // taken deepest level first), the indices, what refit cannot redo
+        std::vector<int> depth(img.n_nodes, 0), order;
+        std::vector<std::vector<int>> by_level(1, std::vector<int>{0});
+        for (size_t l = 0; l < by_level.size(); l++)
+            for (int nd : by_level[l])
+                for (int k = 0; k < 2; k++) {
+                    int32_t link;
+                    std::memcpy(&link, &img.nodes[16 * (size_t)nd + 12 + k], 4);
+                    if (link < 0 || link == nd) continue;
+                    if (l + 1 >= by_level.size()) by_level.emplace_back();
+                    by_level[l + 1].push_back(link);
+                }
+        sc->level_off.assign(1, 0);
+        for (size_t l = by_level.size(); l-- > 0;) {
+            order.insert(order.end(), by_level[l].begin(), by_level[l].end());
+            sc->level_off.push_back((int)order.size());
+        }
+        if ((st = upload(sc, order.data(), order.size(), &sc->refit_order)) != RT_OK) { rt_scene_destroy(sc); return st; }
+        if ((st = upload(sc, d->indices, 3 * (size_t)nt, &sc->indices_dev)) != RT_OK) { rt_scene_destroy(sc); return st; }
+        sc->n_vertices = d->n_vertices;
+        sc->n_tris = nt;
+        sc->has_normals = d->normals != nullptr;
+        for (int m = 0; m < d->n_meshes && sc->refit_why.empty(); m++) {
+            const rt_mesh_desc &M = d->meshes[m];
+            if (M.n_tris == 0) continue;
+            if (M.light >= 0) sc->refit_why = "an emissive mesh (its area CDF would change)";
+            const bool owner = (M.interior >= 0 && d->media[M.interior].type == RT_MEDIUM_HETEROGENEOUS) ||
+                               (M.exterior >= 0 && d->media[M.exterior].type == RT_MEDIUM_HETEROGENEOUS);
+            if (owner) sc->refit_why = "a mesh that bounds a grid medium (the medium's box would change)";
+        }
+        if (sc->refit_why.empty())
+            for (int l = 0; l < d->n_lights; l++)
+                if (d->lights[l].type != RT_LIGHT_ENV && d->lights[l].type != RT_LIGHT_POINT &&
+                    d->lights[l].type != RT_LIGHT_SPOT && d->lights[l].shape_kind == RT_SHAPE_MESH)
+                    sc->refit_why = "a mesh light";
+    }
     {
         // the 4-wide traversal pushes up to three children per level; a tree
         // too deep for its stack is not uploaded and renders use the BVH2
@@ -2296,6 +2461,7 @@ static rt_status scene_create(rt_ctx *ctx, const rt_scene_desc *d, const ExtTree
         const float4 *n4 = nullptr;
         if ((st = upload(sc, reinterpret_cast<const float4 *>(w4.nodes.data()), (size_t)w4.n_nodes * 8, &n4)) != RT_OK) { rt_scene_destroy(sc); return st; }
         S.nodes4 = n4; S.n_nodes4 = w4.n_nodes;
+        if ((st = upload(sc, w4.src.data(), w4.src.size(), &sc->bvh4_src)) != RT_OK) { rt_scene_destroy(sc); return st; }
         sc->w4_ok = nt == 0 || w4.n_nodes > 0;
     }
     {
@@ -2469,6 +2635,73 @@ rt_status rt_bvh_stats(const float *tri_v, int32_t n, int32_t width, int32_t dep
     }
     if (max_depth) *max_depth = d;
     if (n_nodes) *n_nodes = nn;
+    return RT_OK;
+}
+
+static rt_status launch_check(const char *what);
+
+rt_status rt_scene_refit(rt_ctx *ctx, rt_scene *sc, const float *vertices, const float *normals, int32_t on_device)
+{
+    if (!ctx || !sc || !vertices) return fail(RT_ERR_INVALID, "rt_scene_refit: null argument");
+    if (sc->ctx != ctx) return fail(RT_ERR_INVALID, "rt_scene_refit: the scene belongs to another context");
+    if (!sc->indices_dev || sc->n_tris == 0) return RT_OK;   // no triangles: nothing to refit
+    if (!sc->refit_why.empty()) return fail(RT_ERR_UNSUPPORTED, "rt_scene_refit: the scene has " + sc->refit_why);
+    if ((normals != nullptr) != sc->has_normals)
+        return fail(RT_ERR_INVALID, sc->has_normals ? "rt_scene_refit: the scene has vertex normals: pass new ones"
+                                                    : "rt_scene_refit: the scene has no vertex normals");
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    const size_t nv = (size_t)sc->n_vertices;
+    const int n_tris = sc->n_tris;
+    // the new positions (and normals) on the device
+    const float *vd = vertices, *nd_ = normals;
+    void *tmp = nullptr;
+    if (!on_device) {
+        CK(cudaMalloc(&tmp, 3 * nv * sizeof(float) * (normals ? 2 : 1)));
+        CK(cudaMemcpyAsync(tmp, vertices, 3 * nv * sizeof(float), cudaMemcpyHostToDevice, st));
+        vd = (const float *)tmp;
+        if (normals) {
+            CK(cudaMemcpyAsync((float *)tmp + 3 * nv, normals, 3 * nv * sizeof(float), cudaMemcpyHostToDevice, st));
+            nd_ = (const float *)tmp + 3 * nv;
+        }
+    }
+    rt_status s = RT_OK;
+    if (!sc->refit_boxes && cudaMalloc((void **)&sc->refit_boxes, 12 * sizeof(float) * (size_t)sc->S.n_nodes) != cudaSuccess) {
+        cudaFree(tmp);
+        return fail(RT_ERR_NOMEM, "rt_scene_refit: box scratch allocation failed");
+    }
+    const int sm = ctx->sm_count > 0 ? ctx->sm_count : 1;
+    auto grid = [&](int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)sm * 16)); };
+    k_refit_tris<<<grid(n_tris), 256, 0, st>>>(vd, nd_, sc->indices_dev, n_tris, const_cast<float *>(sc->S.tri_v),
+                                               const_cast<float *>(sc->S.tri_n));
+    k_refit_slots<<<grid(n_tris), 256, 0, st>>>(const_cast<float4 *>(sc->S.tri_slots), n_tris, sc->S.tri_v);
+    for (size_t l = 0; l + 1 < sc->level_off.size(); l++) {
+        const int b = sc->level_off[l], e = sc->level_off[l + 1];
+        k_refit_level<<<grid(e - b), 256, 0, st>>>(sc->S.nodes, sc->S.tri_slots, sc->S.tri_v, sc->refit_order, b, e,
+                                                    sc->refit_boxes);
+    }
+    k_refit_widen<<<grid(sc->S.n_nodes), 256, 0, st>>>(const_cast<float4 *>(sc->S.nodes), sc->S.n_nodes, sc->refit_boxes);
+    if (sc->S.n_nodes4 > 0)
+        k_refit_bvh4<<<grid(4 * (int64_t)sc->S.n_nodes4), 256, 0, st>>>(const_cast<float *>(reinterpret_cast<const float *>(sc->S.nodes4)),
+                                                                        sc->S.n_nodes4, sc->bvh4_src, sc->S.nodes);
+    if ((s = launch_check("refit kernels")) != RT_OK) { cudaFree(tmp); return s; }
+    // the scene box: the tree's root box and the analytic shapes'
+    float root[12];
+    cudaError_t e = cudaMemcpyAsync(root, sc->refit_boxes, sizeof(root), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(tmp);
+    if (e != cudaSuccess) return fail(RT_ERR_CUDA, std::string("rt_scene_refit: ") + cudaGetErrorString(e));
+    for (int a = 0; a < 3; a++) {
+        float mn = root[a], mx = root[3 + a];
+        if (root[6] <= root[9]) { mn = std::min(mn, root[6 + a]); mx = std::max(mx, root[9 + a]); }
+        mn = std::min(mn, sc->sph_bounds[a]);
+        mx = std::max(mx, sc->sph_bounds[3 + a]);
+        sc->bounds[a] = sc->S.bmin[a] = mn;
+        sc->bounds[3 + a] = sc->S.bmax[a] = mx;
+    }
+    // the compressed 8-wide tree is not refitted: renders at width 8 use the binary tree
+    sc->S.n_wnodes = 0;
+    sc->wide_ok = false;
     return RT_OK;
 }
 

@@ -498,12 +498,13 @@ void build_bvh4(const BvhImage &b2, Bvh4Image &out)
     if (b2.n_nodes <= 0) return;
     // one child entry of a binary node: its box (the six widened planes as
     // stored) and its link
-    struct Entry { float pl[6]; int32_t link; double area; };
+    struct Entry { float pl[6]; int32_t link; double area; int32_t src; };
     auto entry = [&](int node, int k, Entry &e) -> bool {
         const float *o = &b2.nodes[16 * (size_t)node];
         if (k == 0) { e.pl[0] = o[0]; e.pl[1] = o[1]; e.pl[2] = o[2]; e.pl[3] = o[3]; e.pl[4] = o[8]; e.pl[5] = o[9]; }
         else { e.pl[0] = o[4]; e.pl[1] = o[5]; e.pl[2] = o[6]; e.pl[3] = o[7]; e.pl[4] = o[10]; e.pl[5] = o[11]; }
         std::memcpy(&e.link, &o[12 + k], 4);
+        e.src = 2 * node + k;
         // the empty second child of a root leaf: an inverted box
         if (!(e.pl[0] <= e.pl[1])) return false;
         double dx = (double)e.pl[1] - e.pl[0], dy = (double)e.pl[3] - e.pl[2], dz = (double)e.pl[5] - e.pl[4];
@@ -516,6 +517,7 @@ void build_bvh4(const BvhImage &b2, Bvh4Image &out)
     q.push_back({0, 0, 0});
     out.n_nodes = 1;
     out.nodes.assign(32, INFINITY);
+    out.src.assign(4, -1);
     for (size_t h = 0; h < q.size(); h++) {
         const Work w = q[h];
         out.max_depth = std::max(out.max_depth, w.depth);
@@ -541,10 +543,12 @@ void build_bvh4(const BvhImage &b2, Bvh4Image &out)
             int32_t link = 0x7fffffff;
             if (i < nc) {
                 for (int pl = 0; pl < 6; pl++) o[4 * pl + i] = ch[i].pl[pl];
+                out.src[4 * (size_t)w.wi + i] = ch[i].src;
                 link = ch[i].link;
                 if (link >= 0) {
                     const int wi = out.n_nodes++;
                     out.nodes.resize(32 * (size_t)out.n_nodes, INFINITY);
+                    out.src.resize(4 * (size_t)out.n_nodes, -1);
                     o = &out.nodes[32 * (size_t)w.wi];   // the resize may move the array
                     q.push_back({link, wi, w.depth + 1});
                     link = wi;

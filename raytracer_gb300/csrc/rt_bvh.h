@@ -40,6 +40,7 @@ struct BvhImage {
 // culls exactly what the BVH2's would.
 struct Bvh4Image {
     std::vector<float> nodes;      // 32 floats per node
+    std::vector<int32_t> src;      // per node and slot: the BVH2 child it copies (node * 2 + child), -1 unused
     int n_nodes = 0;
     int max_depth = 0;             // deepest node level below the root
 };
