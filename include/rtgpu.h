@@ -390,6 +390,16 @@ rt_status rt_ctx_set_profiling(rt_ctx *ctx, int32_t level);
  * name another triangle) and the same occlusion.  Stands in for the
  * reference's binary traversal, Bvh::intersection (accelStruct/Bvh.cpp:392-481). */
 rt_status rt_ctx_set_bvh_width(rt_ctx *ctx, int32_t width);
+/* Builder of the binary tree for scenes created later on this context:
+ * RT_BUILDER_HOST_SAH (the default: binned SAH on the host, plus the 4- and
+ * 8-wide trees) or RT_BUILDER_DEVICE (a linear BVH over Morton codes built on
+ * the device in milliseconds, one triangle per leaf, no wide trees, slower
+ * to traverse; for scenes that arrive with the job, as in serving).  A
+ * device tree deeper than the traversal stack falls back to the host build.
+ * Both give the same closest hits (a tie at equal distance may name another
+ * triangle).  Stands in for Bvh::build (accelStruct/Bvh.cpp:51-79). */
+enum { RT_BUILDER_HOST_SAH = 0, RT_BUILDER_DEVICE = 1 };
+rt_status rt_ctx_set_bvh_builder(rt_ctx *ctx, int32_t builder);
 /* Paths per wavefront batch of later renders (whole tiles x all samples are
  * batched up to this count): 2^16..2^26.  Device memory for path state is
  * about 240 bytes per path. */

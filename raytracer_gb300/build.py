@@ -23,7 +23,8 @@ NVCC = os.environ.get("NVCC", "nvcc")
 
 CUDA_SOURCES = ["rt_api.cu"]
 HOST_SOURCES = ["rt_bvh.cpp", "rt_serve.cpp", "rt_io.cpp", "rt_tune.cpp"]
-HEADERS = ["rt_math.cuh", "rt_device.cuh", "rt_kernels.cuh", "rt_volpath.cuh", "rt_bvh.h", "rt_internal.h"]
+HEADERS = ["rt_math.cuh", "rt_device.cuh", "rt_kernels.cuh", "rt_volpath.cuh", "rt_lbvh.cuh", "rt_bvh.h",
+           "rt_internal.h"]
 
 
 def _cuda_include():

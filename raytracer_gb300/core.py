@@ -119,6 +119,8 @@ def lib():
     L.rt_bvh_import_check.argtypes = [vp, C.c_int32, vp, C.c_int32, vp, C.c_int32, C.POINTER(C.c_int32),
                                       C.POINTER(C.c_int32)]
     L.rt_bvh_import_check.restype = C.c_int32
+    L.rt_ctx_set_bvh_builder.argtypes = [vp, C.c_int32]
+    L.rt_ctx_set_bvh_builder.restype = C.c_int32
     L.rt_scene_refit.argtypes = [vp, vp, vp, vp, C.c_int32]
     L.rt_scene_refit.restype = C.c_int32
     for name in ("rt_ctx_create", "rt_ctx_destroy", "rt_ctx_set_stream", "rt_scene_create", "rt_scene_destroy",
@@ -165,6 +167,11 @@ class Context:
     def set_profiling(self, level):
         """0 off, 1 per-kernel event timing, 2 timing + traversal counters."""
         _check(lib().rt_ctx_set_profiling(self.h, int(level)))
+
+    def set_bvh_builder(self, device):
+        """Trees of scenes created later: built on the device (True, a
+        Morton-code linear BVH in milliseconds) or on the host (binned SAH)."""
+        _check(lib().rt_ctx_set_bvh_builder(self.h, 1 if device else 0))
 
     def set_bvh_width(self, width):
         """Traversal tree for later renders and traces: 2 (default) or 8."""

@@ -1535,6 +1535,8 @@ __global__ void k_refit_bvh4(float *nodes4, int n4, const int32_t *src, const fl
     }
 }
 
+#include "rt_lbvh.cuh"
+
 __global__ void k_trace_rays(DevScene S, const rt_ray *rays, int n, int any, rt_hit *hits)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1655,6 +1657,7 @@ struct rt_ctx {
     rt_render_stats last;
     int profiling = 0;
     int bvh_width = 2;          // traversal used by renders and rt_trace: 2, 4 or 8
+    int bvh_builder = 0;        // scenes created later: RT_BUILDER_HOST_SAH or RT_BUILDER_DEVICE
     int wave_paths = 1 << 26;   // target paths per wavefront batch (about 14 GB of path state)
     int ray_sort = 0;           // reorder secondary and shadow rays before tracing
     // launch shapes and the material-sort threshold (rt_ctx_set_tuning)
@@ -2024,6 +2027,15 @@ rt_status rt_ctx_set_bvh_width(rt_ctx *c, int32_t width)
     return RT_OK;
 }
 
+rt_status rt_ctx_set_bvh_builder(rt_ctx *c, int32_t builder)
+{
+    if (!c) return fail(RT_ERR_INVALID, "null ctx");
+    if (builder != RT_BUILDER_HOST_SAH && builder != RT_BUILDER_DEVICE)
+        return fail(RT_ERR_INVALID, "BVH builder must be RT_BUILDER_HOST_SAH or RT_BUILDER_DEVICE");
+    c->bvh_builder = builder;
+    return RT_OK;
+}
+
 rt_status rt_ctx_set_wave_paths(rt_ctx *c, int32_t paths)
 {
     if (!c) return fail(RT_ERR_INVALID, "null ctx");
@@ -2149,6 +2161,83 @@ static rt_status validate(const rt_scene_desc *d)
         if (!(d->camera.filter_radius[k] > 0.f) || d->camera.filter_radius[k] > 16.f)
             return fail(RT_ERR_INVALID, "filter radius must be in (0, 16]");
     return RT_OK;
+}
+
+static rt_status launch_check(const char *what);
+
+// The binary tree built on the device (rt_lbvh.cuh) over the scene's
+// triangles, already on the device in S.tri_v: the node image and the
+// triangle slots, in memory the scene owns.  RT_ERR_LIMIT when the tree is
+// deeper than the traversal stacks (the caller then builds on the host).
+static rt_status device_tree(rt_ctx *ctx, rt_scene *sc, int nt)
+{
+    DevScene &S = sc->S;
+    cudaStream_t st = ctx->stream;
+    const int sm = ctx->sm_count > 0 ? ctx->sm_count : 1;
+    auto grid = [&](int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)sm * 32)); };
+    const int tiles = (nt + RT_RSORT_TILE - 1) / RT_RSORT_TILE;
+    // temporaries in one allocation: codes and ids twice, digit counts,
+    // parents, arrival counters, exact boxes, the depth
+    const size_t n = (size_t)nt;
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t o = off; off = (off + bytes + 255) & ~(size_t)255; return o; };
+    const size_t o_code0 = take(4 * n), o_code1 = take(4 * n), o_id0 = take(4 * n), o_id1 = take(4 * n);
+    const size_t o_hist = take(4 * 256 * (size_t)tiles), o_ipar = take(4 * n), o_lpar = take(4 * n);
+    const size_t o_arr = take(4 * n), o_box = take(48 * n), o_depth = take(4);
+    char *tmp = nullptr;
+    if (cudaMalloc((void **)&tmp, off) != cudaSuccess) return fail(RT_ERR_NOMEM, "device tree: scratch allocation failed");
+    unsigned *code[2] = {(unsigned *)(tmp + o_code0), (unsigned *)(tmp + o_code1)};
+    int *id[2] = {(int *)(tmp + o_id0), (int *)(tmp + o_id1)};
+    int *hist = (int *)(tmp + o_hist), *ipar = (int *)(tmp + o_ipar), *lpar = (int *)(tmp + o_lpar);
+    int *arr = (int *)(tmp + o_arr), *depth = (int *)(tmp + o_depth);
+    float *boxes = (float *)(tmp + o_box);
+    float4 *nodes = nullptr, *slots = nullptr;
+    rt_status s = RT_OK;
+    auto done = [&](rt_status r) { cudaFree(tmp); return r; };
+    if (cudaMalloc((void **)&nodes, sizeof(float4) * 4 * (n - 1)) != cudaSuccess) return done(fail(RT_ERR_NOMEM, "device tree: node allocation failed"));
+    sc->allocs.push_back(nodes);
+    if (cudaMalloc((void **)&slots, sizeof(float4) * 3 * n) != cudaSuccess) return done(fail(RT_ERR_NOMEM, "device tree: slot allocation failed"));
+    sc->allocs.push_back(slots);
+    sc->bytes += (int64_t)(sizeof(float4) * (4 * (n - 1) + 3 * n));
+    // Morton codes over the scene box
+    float scale[3];
+    for (int a = 0; a < 3; a++) {
+        const float ext = sc->bounds[3 + a] - sc->bounds[a];
+        scale[a] = ext > 0.f ? 1024.f / ext : 0.f;
+    }
+    k_lbvh_codes<<<grid(nt), 256, 0, st>>>(S.tri_v, nt, sc->bounds[0], sc->bounds[1], sc->bounds[2], scale[0], scale[1],
+                                          scale[2], code[0], id[0]);
+    int cur = 0;
+    for (int shift = 0; shift < 30; shift += 8) {
+        k_rsort_hist<<<tiles, RT_RSORT_THREADS, 0, st>>>(code[cur], nt, shift, tiles, hist);
+        k_rsort_scan<<<1, 1024, 0, st>>>(hist, 256 * tiles);
+        k_rsort_scatter<<<tiles, RT_RSORT_THREADS, 0, st>>>(code[cur], id[cur], nt, shift, tiles, hist, code[1 - cur],
+                                                            id[1 - cur]);
+        cur = 1 - cur;
+    }
+    k_lbvh_nodes<<<grid(nt - 1), 256, 0, st>>>(code[cur], nt, nodes, ipar, lpar);
+    if (cudaMemsetAsync(arr, 0, 4 * n, st) != cudaSuccess || cudaMemsetAsync(depth, 0, 4, st) != cudaSuccess)
+        return done(fail(RT_ERR_CUDA, "device tree: memset failed"));
+    k_lbvh_boxes<<<grid(nt), 256, 0, st>>>(S.tri_v, id[cur], nt, ipar, lpar, arr, boxes, depth);
+    k_refit_widen<<<grid(nt - 1), 256, 0, st>>>(nodes, nt - 1, boxes);
+    k_lbvh_slots<<<grid(nt), 256, 0, st>>>(S.tri_v, id[cur], nt, slots);
+    if ((s = launch_check("device tree kernels")) != RT_OK) return done(s);
+    int maxd = 0;
+    if (cudaMemcpyAsync(&maxd, depth, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess)
+        return done(fail(RT_ERR_CUDA, "device tree: readback failed"));
+    if (maxd + 1 > RT_STACK) {
+        // too deep for the stacks: give the memory back; the caller builds on the host
+        sc->allocs.pop_back();
+        sc->allocs.pop_back();
+        cudaFree(nodes);
+        cudaFree(slots);
+        sc->bytes -= (int64_t)(sizeof(float4) * (4 * (n - 1) + 3 * n));
+        return done(fail(RT_ERR_LIMIT, "device tree: deeper than the traversal stack"));
+    }
+    S.nodes = nodes;
+    S.tri_slots = slots;
+    S.n_nodes = nt - 1;
+    return done(RT_OK);
 }
 
 // a caller-built binary tree (rt_scene_create_bvh)
@@ -2390,7 +2479,23 @@ static rt_status scene_create(rt_ctx *ctx, const rt_scene_desc *d, const ExtTree
         if ((st = upload(sc, M.density, (size_t)M.res[0] * M.res[1] * M.res[2], &dp)) != RT_OK) { rt_scene_destroy(sc); return st; }
         media[m].density = dp;
     }
-    // BVH
+    const float *fp;
+    const int *ip;
+    if ((st = upload(sc, tri_v.data(), tri_v.size(), &fp)) != RT_OK) { rt_scene_destroy(sc); return st; }
+    S.tri_v = fp;
+    // BVH: built on the device when the context asks for it (a tree too deep
+    // for the stacks falls back to the host build), else on the host
+    bool dev_tree = false;
+    if (!ext && ctx->bvh_builder == RT_BUILDER_DEVICE && nt >= 2 && nt < (1 << 28)) {
+        if ((st = device_tree(ctx, sc, nt)) == RT_OK) dev_tree = true;
+        else if (st != RT_ERR_LIMIT) { rt_scene_destroy(sc); return st; }
+    }
+    if (dev_tree) {
+        // one triangle per leaf; no wide trees, no refit table
+        S.n_nodes4 = 0; sc->w4_ok = false;
+        S.n_wnodes = 0; sc->wide_ok = false;
+        sc->refit_why = "a tree built on the device";
+    } else {
     BvhImage img;
     if (ext) {
         std::string why;
@@ -2477,10 +2582,7 @@ static rt_status scene_create(rt_ctx *ctx, const rt_scene_desc *d, const ExtTree
         sc->wide_depth = wimg.max_depth;
         sc->wide_ok = nt == 0 || wimg.n_nodes > 0;
     }
-    const float *fp;
-    const int *ip;
-    if ((st = upload(sc, tri_v.data(), tri_v.size(), &fp)) != RT_OK) { rt_scene_destroy(sc); return st; }
-    S.tri_v = fp;
+    }   // host-built tree
     if (!tri_n.empty()) { if ((st = upload(sc, tri_n.data(), tri_n.size(), &fp)) != RT_OK) { rt_scene_destroy(sc); return st; } S.tri_n = fp; }
     if (!tri_uv.empty()) { if ((st = upload(sc, tri_uv.data(), tri_uv.size(), &fp)) != RT_OK) { rt_scene_destroy(sc); return st; } S.tri_uv = fp; }
     // textures: all texels in one buffer, one DevTexture each

@@ -61,7 +61,7 @@ def _width(ctx, w):
     ctx.set_bvh_width(w)
 
 
-@pytest.mark.parametrize("tree", ["library", "reference"])
+@pytest.mark.parametrize("tree", ["library", "reference", "device"])
 @pytest.mark.parametrize("w", [2, 4, 8], ids=["bvh2", "bvh4", "bvh8"])
 def test_full_tree_trace_parity(ctx, rtlib, ico_full, w, tree):
     """131,072 camera rays plus 131,072 secondary rays leaving the camera
@@ -81,7 +81,11 @@ def test_full_tree_trace_parity(ctx, rtlib, ico_full, w, tree):
     sec = np.zeros(len(p), D.RAY_DTYPE)
     sec["o"], sec["d"], sec["mint"], sec["maxt"] = p, d, 1e-4, 1e8
     rays = np.concatenate([cam, sec])
-    g = rtlib.Scene(ctx, s, bvh=o.export_bvh() if tree == "reference" else None)
+    ctx.set_bvh_builder(tree == "device")
+    try:
+        g = rtlib.Scene(ctx, s, bvh=o.export_bvh() if tree == "reference" else None)
+    finally:
+        ctx.set_bvh_builder(False)
     _width(ctx, w)
     try:
         hg = g.trace(rays)

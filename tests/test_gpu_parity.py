@@ -55,13 +55,17 @@ def vol():
     return scenes.volume_grid(40, 32, res=32)
 
 
-def _trace_parity(ctx, rtlib, scene, n=20000, seed=0, reference_tree=False):
+def _trace_parity(ctx, rtlib, scene, n=20000, seed=0, reference_tree=False, device_tree=False):
     rng = np.random.default_rng(seed)
     rays = _random_rays(scene, n, rng)
     o = O.OracleScene(scene)
     cam = o.camera_rays(rng.random((n // 4, 2)) * [scene.camera["width"], scene.camera["height"]])
     rays = np.concatenate([rays, cam])
-    g = rtlib.Scene(ctx, scene, bvh=o.export_bvh() if reference_tree else None)
+    ctx.set_bvh_builder(device_tree)
+    try:
+        g = rtlib.Scene(ctx, scene, bvh=o.export_bvh() if reference_tree else None)
+    finally:
+        ctx.set_bvh_builder(False)
     hg = g.trace(rays)
     ho = o.trace(rays)
     hit_g, hit_o = hg["prim"] != -1, ho["prim"] != -1
@@ -112,6 +116,33 @@ def test_trace_parity_reference_tree(ctx, rtlib, cornell, ico, vol, width, which
     (the 4-wide tree collapses it; the 8-wide one is the library's own)."""
     _trace_parity(ctx, rtlib, {"cornell": cornell, "icosphere": ico, "spheres_and_boxes": vol}[which],
                   reference_tree=True)
+
+
+@pytest.mark.parametrize("which", ["cornell", "icosphere", "spheres_and_boxes"])
+def test_trace_parity_device_tree(ctx, rtlib, cornell, ico, vol, which):
+    """The linear BVH built on the device (rt_ctx_set_bvh_builder)."""
+    _trace_parity(ctx, rtlib, {"cornell": cornell, "icosphere": ico, "spheres_and_boxes": vol}[which],
+                  device_tree=True)
+
+
+def test_film_parity_device_tree(ctx, rtlib, ico):
+    """Films over the device-built tree: the oracle's, and the same weights
+    as over the host-built tree."""
+    o = O.OracleScene(ico)
+    ctx.set_bvh_builder(True)
+    try:
+        g = rtlib.Scene(ctx, ico)
+    finally:
+        ctx.set_bvh_builder(False)
+    fg = g.render(2, seed=3, block=16)
+    fo = o.render(2, seed=3, block=16)
+    assert np.array_equal(fg[..., 3], fo[..., 3])
+    err = (np.abs(fg[..., :3].astype(np.float64) - fo[..., :3]) / np.maximum(np.abs(fo[..., :3]), 1e-3)).max(-1)
+    print("device tree film: exact %.4f, >1e-3 %.4f" % (np.mean(err == 0), np.mean(err > 1e-3)))
+    assert float(np.mean(err > 1e-3)) <= 0.002
+    assert rtlib.lib().rt_ctx_set_bvh_builder(ctx.h, 7) != 0   # neither builder: refused
+    g.close()
+    o.close()
 
 
 def test_film_parity_reference_tree(ctx, rtlib, cornell, ico):
