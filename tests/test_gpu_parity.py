@@ -411,6 +411,13 @@ def test_film_parity_volume(ctx, rtlib, vol):
     _film_parity(ctx, rtlib, vol, 2, 4, max_bad=0.002)   # measured 0
 
 
+def test_film_parity_stacked_media(ctx, rtlib):
+    """Transmittance rays through five stacked media (many null-boundary
+    segments, zero transmittance between segments, blocked light samples)
+    against the oracle."""
+    _film_parity(ctx, rtlib, _stacked_media(), 4, 13, max_bad=0.002)
+
+
 @pytest.mark.parametrize("flt", [D.gaussian_filter(1.5, 1.5), D.mitchell_filter(2.0, 1.0), D.box_filter(1.0, 0.5)],
                          ids=["gauss1.5", "mitchell2x1", "box1x0.5"])
 def test_film_parity_filters(ctx, rtlib, flt):
@@ -630,6 +637,44 @@ def test_texture_validation(ctx, rtlib):
     assert e.value.status == 5
 
 
+def _stacked_media(width=40, height=32):
+    """Five media boxes stacked under a sphere light: grid, dense
+    homogeneous, grid, thin homogeneous, grid.  Light-sample and sampled rays
+    from the lower boxes cross up to five medium segments with null
+    boundaries between them; the dense layer (sigma_t 90 over 0.2) drives a
+    ray's transmittance to zero (isZero) between segments, which ends the
+    transmittance loops early; a diffuse block on one side blocks some light
+    samples and ends some sampled rays on a surface."""
+    s = D.SceneData()
+    s.name = "stacked_media"
+    for k, y in enumerate((0.1, 0.35, 0.6, 0.85, 1.1)):
+        if k % 2 == 0:
+            m = s.add_medium(dict(type=D.MEDIUM_HETEROGENEOUS, phase=D.PHASE_HG, g=0.2, scale=8.0 + 4 * k,
+                                  albedo=(0.8, 0.85, 0.9), density=scenes.density_grid(8, seed=k),
+                                  grid_min=(0, 0, 0), grid_max=(1, 1, 1), centered=1))
+        elif k == 1:
+            m = s.add_medium(dict(type=D.MEDIUM_HOMOGENEOUS, phase=D.PHASE_ISOTROPIC, sigma_a=(10.0, 10.0, 10.0),
+                                  sigma_s=(80.0, 80.0, 80.0), scale=1.0))
+        else:
+            m = s.add_medium(dict(type=D.MEDIUM_HOMOGENEOUS, phase=D.PHASE_ISOTROPIC, sigma_a=(0.3, 0.6, 0.9),
+                                  sigma_s=(1.0, 1.0, 1.0), scale=1.0))
+        v, f = scenes._box((0.0, y, 0.0), (1.0, 0.2, 1.0))
+        s.add_mesh(v, f, bsdf=-1, interior=m)
+    wall = s.add_bsdf(D.bsdf(D.BSDF_DIFFUSE, albedo=(0.6, 0.5, 0.4)))
+    v, f = scenes._box((0.75, 0.6, 0.0), (0.3, 1.2, 1.0))
+    s.add_mesh(v, f, bsdf=wall)
+    lm = s.add_bsdf(D.bsdf(D.BSDF_DIFFUSE, albedo=(0.0, 0.0, 0.0)))
+    T = np.eye(4)
+    T[:3, 3] = (-0.2, 2.0, 0.1)
+    sp = s.add_sphere(0.25, T, bsdf=lm)
+    li = s.add_area_light((40.0, 40.0, 40.0), D.SHAPE_SPHERE, sp, mesh_light=False)
+    s.spheres[sp]["light"] = li
+    s.camera = D.camera(width, height, 40.0, D.look_at((0.3, 0.7, 3.0), (0.0, 0.6, 0.0), (0, 1, 0)))
+    s.integrator = dict(integrator=D.INTEGRATOR_VOLPATH, max_depth=32, min_depth=3,
+                        strategy=D.STRATEGY_ONE_LIGHT_UNIFORM)
+    return s
+
+
 def _volpath_cases():
     smooth = scenes.cornell_smooth(40, 32)
     m = smooth.add_medium(dict(type=D.MEDIUM_HOMOGENEOUS, phase=D.PHASE_HG, g=0.4, sigma_a=(0.5, 1.0, 2.0),
@@ -644,10 +689,11 @@ def _volpath_cases():
     fog.camera["medium"] = fm
     fog.integrator = dict(fog.integrator, integrator=D.INTEGRATOR_VOLPATH)
     return {"grid": (scenes.volume_grid(48, 40, res=16), 3), "smooth": (smooth, 3), "textured": (tex, 2),
-            "fog": (fog, 3), "two_batches": (scenes.volume_grid(80, 60, res=16), 16)}
+            "fog": (fog, 3), "two_batches": (scenes.volume_grid(80, 60, res=16), 16),
+            "stacked": (_stacked_media(), 4)}
 
 
-@pytest.mark.parametrize("case", ["grid", "smooth", "textured", "fog", "two_batches"])
+@pytest.mark.parametrize("case", ["grid", "smooth", "textured", "fog", "two_batches", "stacked"])
 def test_volpath_wavefront_equals_megakernel(ctx, rtlib, case):
     """VolPathTracing as six kernels over queues (one vol_step per round),
     launched kernel by kernel or as a graph, gives the persistent
