@@ -160,7 +160,7 @@ def _config(data):
             "filter": getattr(_ARGS, "filter", "box"),
             "parallelism": "replicas" if int(os.environ.get("WORLD_SIZE", "1")) > 1 else "single",
             "l2": "inputs larger than L2: the scene (BVH, triangles, materials, maps) and the wavefront path "
-                  "state (about 205 bytes per path in flight) live in HBM"}
+                  "state (246 bytes per path in flight, 342 for VolPathTracing) live in HBM"}
 
 
 _ARGS = None
@@ -299,7 +299,7 @@ def served_block(ctx_factory, rate=5.0, n_jobs=30, pool_pt=8, target=0.02, cap=4
     picks = [(int(pool_pt + rng.integers(2)) if rng.random() < 0.2 else int(rng.integers(pool_pt)), j)
              for j in range(n_jobs)]
     res = {"rate_jobs_per_s": rate, "jobs": n_jobs, "target_rmse": target, "rmse_space": "display ([0, 1] clipped)",
-           "spp_cap": cap,
+           "spp_cap": cap, "device_budget_gb": SERVE_BUDGET / 1e9,
            "pool": "%d scenes of the batch distribution + 2 grid-medium scenes, 4096-spp references" % pool_pt}
     for form in ("plain", "batched"):
         res[form] = _serve_run(ctx, pool, refs, picks, arrivals, form, target, cap, 4)
@@ -682,12 +682,16 @@ def _serve_pool(ctx, n_pt, n_vol, ref_spp=4096):
     return pool, refs
 
 
+SERVE_BUDGET = 150 * 10 ** 9   # device bytes a server may hold for admitted jobs (scenes, films, path state)
+
+
 def _serve_run(ctx, pool, refs, picks, arrivals, form, target, cap, lanes):
     """Submit the jobs at their arrival times to a server of the given form;
     per job: latency to completion (queue + run), samples rendered and the
     true RMSE of its film against the pool scene's reference."""
     import raytracer_gb300 as R
-    srv = R.Server(ctx, lanes=1 if form == "plain" else lanes, lanes_only=form != "batched", rmse_display=True)
+    srv = R.Server(ctx, lanes=1 if form == "plain" else lanes, lanes_only=form != "batched", rmse_display=True,
+                   device_budget_bytes=SERVE_BUDGET)
     t0 = time.perf_counter()
     ids = []
     for (pi, seed), ta in zip(picks, arrivals):
@@ -737,6 +741,7 @@ def run_serve(args):
     n_pt = args.serve_pool
     out = {"metric": "job latency", "unit": "ms", "workload": "serve", "higher_is_better": False,
            "target_rmse": args.target_rmse, "spp_cap": args.spp_cap, "jobs_per_rate": args.serve_jobs,
+           "device_budget_gb": SERVE_BUDGET / 1e9,
            "pool": {"path_mis_scenes": n_pt, "volume_scenes": len(pool) - n_pt, "reference_spp": 4096,
                     "prep_s": round(prep_s, 1)},
            "rates": {}}

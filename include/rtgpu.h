@@ -515,7 +515,9 @@ typedef struct rt_server_opts {
     int32_t lanes;                /* lanes for jobs the wavefront cannot take,
                                      1..16 (0: 4)                                   */
     int32_t max_queue;            /* queued jobs before submit fails (0: 4096)      */
-    int64_t device_budget_bytes;  /* device memory of path state, admitted jobs'
+    int64_t device_budget_bytes;  /* device memory of path state (the wavefront's
+                                     slots and every lane's, at
+                                     rt_path_state_bytes each), admitted jobs'
                                      scenes and films; 0 = unlimited               */
     int32_t lanes_only;           /* 0: continuous batching in one wavefront (the
                                      default); 1: every job on a lane               */
@@ -532,6 +534,12 @@ typedef struct rt_job_info {
     char error[128];              /* RT_JOB_FAILED: rt_last_error of the job        */
 } rt_job_info;
 rt_status rt_server_start(rt_ctx *ctx, const rt_server_opts *opts, rt_server **out);
+/* Device bytes of wavefront path state per path slot for an integrator
+ * (RT_INTEGRATOR_*): the per-slot part of a render's working memory, and
+ * what a server counts against its budget per slot (lanes at the
+ * VolPathTracing figure, since a lane may take either kind of job).  0 for
+ * an unknown integrator. */
+int64_t rt_path_state_bytes(int32_t integrator);
 /* Queue a render of `scene` (which must outlive the job).  A job whose
  * scene and films alone exceed the budget is refused (RT_ERR_LIMIT).
  * target_rmse <= 0: render desc->spp samples, the film equals rt_render's.  target_rmse > 0:

@@ -123,6 +123,8 @@ def lib():
     L.rt_ctx_set_bvh_builder.restype = C.c_int32
     L.rt_scene_refit.argtypes = [vp, vp, vp, vp, C.c_int32]
     L.rt_scene_refit.restype = C.c_int32
+    L.rt_path_state_bytes.argtypes = [C.c_int32]
+    L.rt_path_state_bytes.restype = C.c_int64
     for name in ("rt_ctx_create", "rt_ctx_destroy", "rt_ctx_set_stream", "rt_scene_create", "rt_scene_destroy",
                  "rt_scene_info", "rt_render", "rt_render_stats_get", "rt_ctx_set_profiling", "rt_ctx_set_bvh_width", "rt_ctx_set_wave_paths", "rt_ctx_set_ray_sort", "rt_ctx_set_graphs",
                  "rt_ctx_get_tuning", "rt_ctx_set_tuning", "rt_autotune",
@@ -458,6 +460,13 @@ MEDIUM_R = np.dtype([("weight", np.float32, 3), ("t", np.float32), ("scattered",
 MEDIUM_OP_SAMPLE, MEDIUM_OP_TRANSMITTANCE = 0, 1
 assert BSDF_Q.itemsize == C.sizeof(D.BsdfQ) and BSDF_R.itemsize == C.sizeof(D.BsdfR)
 assert LIGHT_Q.itemsize == C.sizeof(D.LightQ) and LIGHT_R.itemsize == C.sizeof(D.LightR)
+
+
+def path_state_bytes(integrator=0):
+    """Device bytes of wavefront path state per path slot for an integrator
+    (0: PathTracingMIS, 1: VolPathTracing), as a server counts them against
+    its budget."""
+    return int(lib().rt_path_state_bytes(int(integrator)))
 
 
 def bvh_stats(tri_v, width=2, depth_cap=0):

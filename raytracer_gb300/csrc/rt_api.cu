@@ -2839,6 +2839,20 @@ static rt_status ensure_vw(rt_ctx *c, int capacity)
     return RT_OK;
 }
 
+// the per-slot allocations of ensure_wave and (VolPathTracing) ensure_vw
+extern "C" int64_t rt_path_state_bytes(int32_t integrator)
+{
+    if (integrator != RT_INTEGRATOR_PATH_MIS && integrator != RT_INTEGRATOR_VOLPATH) return 0;
+    const bool volpath = integrator == RT_INTEGRATOR_VOLPATH;
+    const int64_t wave = sizeof(Pcg32) +
+                         10 * sizeof(float4) +                 // tp rad ray_o ray_d hit bs nee sh_o sh_d out
+                         3 * sizeof(int) +                     // rel_eta flags occl
+                         2 +                                   // splat pix_irregular
+                         (4 + RT_NBSDF + 1) * sizeof(int) +    // fin end closest shadow, material, mixed queues
+                         3 * sizeof(int);                      // sid, sort keys and scratch
+    return wave + (volpath ? 6 * (int64_t)sizeof(float4) : 0);   // v_seg v_p v_li0 v_li1 v_li2 v_val
+}
+
 static rt_status ensure_wave(rt_ctx *c, int capacity, int max_rounds)
 {
     if (c->capacity >= capacity && c->W.max_rounds >= max_rounds) return RT_OK;

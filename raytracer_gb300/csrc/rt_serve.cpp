@@ -47,7 +47,7 @@ double now_ms()
 struct LaneSet {
     int device = 0;
     // lanes overlap several renders; smaller batches than a lone render's
-    // bound their memory (about 240 bytes per path each)
+    // bound their memory (rt_path_state_bytes per path each)
     int wave_paths = 1 << 24;
     std::vector<rt_ctx *> lanes;
 
@@ -613,10 +613,12 @@ extern "C" rt_status rt_server_start(rt_ctx *ctx, const rt_server_opts *opts, rt
         rt_internal_get_shape(ctx, &wave, &tb, &sb, &thr);
         if (s == RT_OK) s = rt_ctx_set_wave_paths(S->sched, wave);
         if (s == RT_OK) s = rt_internal_set_shape(S->sched, tb, sb, thr);
-        // the wavefront's path state (about 240 bytes per path at its
-        // capacity) and the lanes' count against the budget from the start
-        S->fixed = (int64_t)240 * wave + (int64_t)240 * S->set.wave_paths * lanes;
+        // the wavefront's path state at its capacity (PathTracingMIS jobs)
+        // counts against the budget from the start
+        S->fixed = rt_path_state_bytes(RT_INTEGRATOR_PATH_MIS) * wave;
     }
+    // and so does the lanes' (any job: VolPathTracing's state included)
+    S->fixed += rt_path_state_bytes(RT_INTEGRATOR_VOLPATH) * S->set.wave_paths * lanes;
     if (s != RT_OK) {
         if (S->sched) rt_ctx_destroy(S->sched);
         S->set.clear();

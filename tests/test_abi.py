@@ -16,7 +16,7 @@ HEADER = os.path.join(ROOT, "include", "rtgpu.h")
 
 def _declared_functions():
     src = open(HEADER).read()
-    return sorted(set(re.findall(r"^\s*(?:rt_status|int32_t|uint64_t|const char \*)\s*(rt_\w+)\s*\(", src, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:rt_status|int32_t|int64_t|uint64_t|const char \*)\s*(rt_\w+)\s*\(", src, re.M)))
 
 
 @pytest.fixture(scope="module")
@@ -31,6 +31,17 @@ def test_library_exports_every_declared_symbol(built):
     lib = C.CDLL(built)
     missing = [n for n in names if not hasattr(lib, n)]
     assert not missing, missing
+
+
+def test_path_state_bytes(built):
+    """The per-slot path state a server counts against its budget: the
+    wavefront arrays of a PathTracingMIS render, plus the VolPath
+    wavefront's six float4 arrays; 0 for an unknown integrator."""
+    import raytracer_gb300 as R
+    pt, vp = R.path_state_bytes(0), R.path_state_bytes(1)
+    assert pt == 16 + 10 * 16 + 3 * 4 + 2 + 11 * 4 + 3 * 4
+    assert vp == pt + 6 * 16
+    assert R.path_state_bytes(7) == 0
 
 
 def test_struct_layout_matches_header(tmp_path):

@@ -216,9 +216,9 @@ def test_server_budget_admits_in_order(ctx, job_scenes):
     still equals rt_render's."""
     g = job_scenes["ico"]
     nbytes = g.info()["device_bytes"] + g.width * g.height * 16
-    # the lanes' and the wavefront's path state, then room for one job
+    # the wavefront's and the lane's path state, then room for one job
     t = ctx.get_tuning()
-    fixed = 240 * t["wave_paths"] + 240 * t["lane_wave_paths"] * 1
+    fixed = R.path_state_bytes(0) * t["wave_paths"] + R.path_state_bytes(1) * t["lane_wave_paths"] * 1
     srv = R.Server(ctx, lanes=1, device_budget_bytes=fixed + nbytes + 1024)
     jobs = [(g, 2, dict(seed=s)) for s in range(4)]
     ids = [srv.submit(sc, spp, **o) for sc, spp, o in jobs]
