@@ -3938,8 +3938,6 @@ extern "C" rt_status rt_render_tile_static(rt_ctx *ctx, rt_scene *sc, const rt_r
     const DevCamera &cam = sc->S.cam;
     if (!(cam.filter == RT_FILTER_BOX && cam.frx == 0.5f && cam.fry == 0.5f))
         return fail(RT_ERR_UNSUPPORTED, "rt_render_tile_static: only the box filter of radius 0.5");
-    if (sc->S.has_mixed)
-        return fail(RT_ERR_UNSUPPORTED, "rt_render_tile_static: textured and Microfacet BSDFs need rt_render");
     const int Wd = cam.width, H = cam.height;
     const int bx = rd->block_x > 0 ? rd->block_x : 32, by = rd->block_y > 0 ? rd->block_y : 32;
     if (bx > 0xffff || by > 0xffff) return fail(RT_ERR_INVALID, "block size too large");
@@ -4003,6 +4001,8 @@ extern "C" rt_status rt_render_tile_static(rt_ctx *ctx, rt_scene *sc, const rt_r
     W.q_closest = (int *)take(P * sizeof(int));
     W.q_shadow = (int *)take(P * sizeof(int));
     for (int t = 0; t < RT_NBSDF; t++) W.q_mat[t] = (int *)take(P * sizeof(int));
+    // textured and Microfacet BSDFs shade from the mixed queue
+    if (sc->S.has_mixed) W.q_mixed = (int *)take(P * sizeof(int));
     W.cnt = (RoundCounters *)take((size_t)(rounds + 2) * sizeof(RoundCounters));
     W.capacity = (int)P;
     W.max_rounds = rounds;
@@ -4079,6 +4079,7 @@ extern "C" rt_status rt_render_tile_static(rt_ctx *ctx, rt_scene *sc, const rt_r
             if (sc->bsdf_types & 8) k_pt_shade<3><<<blocks, 128, 0, st>>>(Pm, r);
             if (sc->bsdf_types & 16) k_pt_shade<4><<<blocks, 128, 0, st>>>(Pm, r);
             if (sc->bsdf_types & 32) k_pt_shade<5><<<blocks, 128, 0, st>>>(Pm, r);
+            if (sc->bsdf_types & (1 << RT_QUEUE_MIXED)) k_pt_shade<RT_QUEUE_MIXED><<<blocks, 128, 0, st>>>(Pm, r);
             if ((s = launch_check("pt round (static)")) != RT_OK) return s;
             if ((r & 3) == 3 && r + 1 < rounds) {
                 RoundCounters nc;

@@ -73,20 +73,35 @@ def test_static_tile_render_rejects_oversize(ctx, rtlib):
     g.close()
 
 
-def test_static_tile_render_refuses_textured_scenes(ctx, rtlib):
+@pytest.mark.parametrize("which", ["textured", "microfacet", "textured_volpath"])
+def test_static_tile_render_mixed_queue_scenes(ctx, rtlib, which):
     """Textured and Microfacet BSDFs shade from the mixed queue, which the
-    static scratch layout does not hold: the call fails with
-    RT_ERR_UNSUPPORTED."""
+    static scratch holds for scenes that have such BSDFs: the tiles equal
+    rt_render's (VolPathTracing applies the textures in its kernel)."""
     torch = pytest.importorskip("torch")
-    mf = scenes.cornell_box(32, 32)
-    mf.meshes[0]["bsdf"] = mf.add_bsdf(D.bsdf(D.BSDF_MICROFACET, albedo=(0.5, 0.5, 0.5), ks=0.3, alpha=0.2))
-    for sd in (scenes.textured_room(32, 32), mf):
-        g = rtlib.Scene(ctx, sd)
-        film = torch.zeros((32, 32, 4), dtype=torch.float32, device="cuda")
-        with pytest.raises(rtlib.RtError) as e:
-            g.render_tile_static(0, 0, film.data_ptr(), 2, seed=1, block=32)
-        assert e.value.status == 5
-        g.close()
+    if which == "microfacet":
+        s = scenes.cornell_box(64, 48)
+        s.meshes[0]["bsdf"] = s.add_bsdf(D.bsdf(D.BSDF_MICROFACET, albedo=(0.5, 0.5, 0.5), ks=0.3, alpha=0.2))
+    else:
+        s = scenes.textured_room(64, 48)
+        if which == "textured_volpath":
+            s.integrator = dict(s.integrator, integrator=D.INTEGRATOR_VOLPATH)
+    block, spp, tiles = 32, 2, [(0, 0), (1, 1)]
+    g = rtlib.Scene(ctx, s)
+    ref = g.render(spp, seed=1, block=block)
+    film = torch.zeros((48, 64, 4), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    for tx, ty in tiles:
+        g.render_tile_static(tx, ty, film.data_ptr(), spp, seed=1, block=block)
+    torch.cuda.synchronize()
+    out = film.cpu().numpy()
+    for tx, ty in tiles:
+        ys, xs = _tile_box(s, tx, ty, block)
+        a, b = out[ys, xs], ref[ys, xs]
+        assert np.array_equal(a[..., 3], b[..., 3])
+        np.testing.assert_allclose(a[..., :3], b[..., :3], rtol=1e-5, atol=1e-7)
+        print("%s tile (%d,%d): bitwise equal %s" % (which, tx, ty, np.array_equal(a, b)))
+    g.close()
 
 
 def test_static_tile_render_accumulates_sample_ranges(ctx, rtlib):
