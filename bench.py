@@ -412,13 +412,14 @@ def run_gpu(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         t_local = float(t.item())
     value = samples_per_step * args.steps * world / t_local
-    # end to end through the C ABI with a host film
+    # end to end through the C ABI with a host film: one page-locked buffer
+    # that every step's film is copied into, as a host render loop reuses
     ctx.set_profiling(0)
-    host_film = None
+    host_film = torch.empty((H, W, 4), dtype=torch.float32, pin_memory=True).numpy()
     barrier()
     t0 = time.perf_counter()
     for k in range(0 if args.small else args.steps):
-        host_film = scene.render(spp, seed=2000 + k, sample_begin=sbase)
+        scene.render(spp, seed=2000 + k, sample_begin=sbase, out=host_film)
     barrier()
     e2e_s = max(time.perf_counter() - t0, 1e-9)
     e2e_value = samples_per_step * args.steps * world / e2e_s
