@@ -356,7 +356,8 @@ __global__ void __launch_bounds__(128, RT_VOLPATH_MINB) k_volpath(RenderParams P
 // rebuilt from the hit, the origin of the ray segment that found it and the
 // path's direction (hit_frame), which is what the megakernel holds.  Queue
 // counts live in the round's RoundCounters: trace = closest, step = mat[0],
-// shadow = shadow, sample = mat[1], trsamp = mat[2], finish = mat[3]; the
+// shadow = shadow, sample = mat[1] (medium vertices) and mat[4] (surface
+// vertices), trsamp = mat[2], finish = mat[3]; the
 // next round's trace queue is the next counters' closest.
 enum { VF_FIRST = F_FIRST, VF_EMISSION = 2, VF_WAS = 4, VF_SCAT = 8, VF_NULLX = 16, VF_DELTA = 32, VF_NEWM = 64,
        VF_HASVAL = 128, VF_GUARD_SHIFT = 8 };
@@ -576,8 +577,10 @@ __global__ void __launch_bounds__(128, RT_VW_MINB_STEP) k_vw_step(RenderParams P
                 P.W.flags[slot] = (flags & ((1 << VF_GUARD_SHIFT) - 1)) | (guard << VF_GUARD_SHIFT);
             }
         }
+        const bool scat = (flags & VF_SCAT) != 0;
         q_push(P.W.q_shadow, &C->shadow, slot, push_shadow);
-        q_push(P.W.q_mat[1], &C->mat[1], slot, push_sample);
+        q_push(P.W.q_mat[1], &C->mat[1], slot, push_sample && scat);
+        q_push(P.W.q_mat[4], &C->mat[4], slot, push_sample && !scat);
         q_push(P.W.q_closest, &Cn->closest, slot, push_trace);
     }
     if (limit) atomicOr(P.limit_flag, RT_LIM_VOLPATH);
@@ -601,18 +604,24 @@ __global__ void __launch_bounds__(128, RT_VW_MINB_SHADOW) k_vw_shadow(RenderPara
         P.W.v_li1[slot] = make_float4(l1.x, l1.y, l1.z, pdf);
         P.W.v_val[slot] = f4c(value, 0.f);
         P.W.rng[slot] = rng;
-        P.W.flags[slot] |= VF_HASVAL;
-        q_push(P.W.q_mat[1], &C->mat[1], slot, true);
+        const int flags = P.W.flags[slot] | VF_HASVAL;
+        P.W.flags[slot] = flags;
+        q_push(P.W.q_mat[1], &C->mat[1], slot, (flags & VF_SCAT) != 0);
+        q_push(P.W.q_mat[4], &C->mat[4], slot, (flags & VF_SCAT) == 0);
     }
     if (limit) atomicOr(P.limit_flag, RT_LIM_VOLPATH);
 }
 
+// SCAT: the paths whose vertex is a scatter point in a medium (sample queue
+// mat[1]); otherwise those on a surface (mat[4]).  Split so that the
+// frequent medium vertices run in a kernel without the BSDF code.
+template <bool SCAT>
 __global__ void __launch_bounds__(128, RT_VW_MINB_SAMPLE) k_vw_sample(RenderParams P, int round)
 {
     round = cur_round(P, round);
     const DevScene &S = P.S;
     RoundCounters *C = &P.W.cnt[round];
-    VW_LOOP(C->mat[1], P.W.q_mat[1])
+    VW_LOOP(C->mat[SCAT ? 1 : 4], P.W.q_mat[SCAT ? 1 : 4])
     {
         const int slot = qin_[i_];
         int flags = P.W.flags[slot];
@@ -626,7 +635,7 @@ __global__ void __launch_bounds__(128, RT_VW_MINB_SAMPLE) k_vw_sample(RenderPara
         const bool hasval = flags & VF_HASVAL;
         C3 value = hasval ? rgb(P.W.v_val[slot]) : cfill(0.f);
         bool push = true;
-        if (flags & VF_SCAT) {
+        if (SCAT) {
             const DevMedium &M = S.media[medium];
             if (!iszero(value)) {
                 V3 to_light = xyz(P.W.v_li0[slot]);
