@@ -336,29 +336,31 @@ __global__ void __launch_bounds__(128, RT_VOLPATH_MINB) k_volpath(RenderParams P
 // over a queue of paths in HBM.  One round runs one vol_step of every live
 // path (a bounce, or a null-boundary crossing, which the reference also
 // runs as one pass of its loop):
-//   k_vw_trace   [trace queue]   closest hit of the path's ray (the trace that
-//                                ends vol_step / vol_start / a null crossing)
-//   k_vw_step    [step queue]    depth and guard, delta tracking through the
-//                                medium, then either the scatter point or the
-//                                surface (emission, null boundary, env miss),
-//                                and the light pick and sample of
-//                                sampleAttenuatedLightDirect
-//   k_vw_shadow  [shadow queue]  the light sample's transmittance
-//                                (evalTransmittance: traces through null
-//                                boundaries, ratio tracking in media)
-//   k_vw_sample  [sample queue]  the light sample's MIS contribution, the
-//                                phase or BSDF sample and the new ray
-//   k_vw_trsamp  [trsamp queue]  evalTransmittanceFromSampledBSDF along it
-//   k_vw_finish  [finish queue]  emission MIS of what the sampled ray found,
-//                                throughput, Russian roulette
+//   k_vw_trace_step [trace queue]  closest hit of the path's ray (the trace
+//                                  that ends vol_step / vol_start / a null
+//                                  crossing), then depth and guard, delta
+//                                  tracking through the medium, then either
+//                                  the scatter point or the surface
+//                                  (emission, null boundary, env miss), and
+//                                  the light pick and sample of
+//                                  sampleAttenuatedLightDirect
+//   k_vw_shadow  [shadow queue]    the light sample's transmittance
+//                                  (evalTransmittance: traces through null
+//                                  boundaries, ratio tracking in media)
+//   k_vw_sample  [sample queues]   the light sample's MIS contribution, the
+//                                  phase or BSDF sample and the new ray
+//   k_vw_trsamp  [trsamp queue]    evalTransmittanceFromSampledBSDF along it
+//   k_vw_finish  [finish queue]    emission MIS of what the sampled ray
+//                                  found, throughput, Russian roulette
 // Each path's draws come in the order of one uninterrupted vol_step, so a
 // path's radiance is the megakernel's.  The hit frame is not stored: it is
 // rebuilt from the hit, the origin of the ray segment that found it and the
 // path's direction (hit_frame), which is what the megakernel holds.  Queue
-// counts live in the round's RoundCounters: trace = closest, step = mat[0],
-// shadow = shadow, sample = mat[1] (medium vertices) and mat[4] (surface
-// vertices), trsamp = mat[2], finish = mat[3]; the
-// next round's trace queue is the next counters' closest.
+// counts live in the round's RoundCounters: trace = closest (queue
+// q_closest in even rounds, q_mat[0] in odd ones), shadow = shadow, sample =
+// mat[1] (medium vertices) and mat[4] (surface vertices), trsamp = mat[2],
+// finish = mat[3]; the next round's trace queue is the next counters'
+// closest.
 enum { VF_FIRST = F_FIRST, VF_EMISSION = 2, VF_WAS = 4, VF_SCAT = 8, VF_NULLX = 16, VF_DELTA = 32, VF_NEWM = 64,
        VF_HASVAL = 128, VF_GUARD_SHIFT = 8 };
 
@@ -422,9 +424,6 @@ __device__ __noinline__ C3 vw_tr_sampled(const DevScene &S, Ray ray, Pcg32 &rng,
 #ifndef RT_VW_MINB
 #define RT_VW_MINB 8
 #endif
-#ifndef RT_VW_MINB_TRACE
-#define RT_VW_MINB_TRACE RT_VW_MINB
-#endif
 #ifndef RT_VW_MINB_STEP
 #define RT_VW_MINB_STEP RT_VW_MINB
 #endif
@@ -445,60 +444,62 @@ __device__ __noinline__ C3 vw_tr_sampled(const DevScene &S, Ray ray, Pcg32 &rng,
     const int *qin_ = (QUEUE);                                                                     \
     for (int i_ = blockIdx.x * blockDim.x + threadIdx.x; i_ < n_; i_ += gridDim.x * blockDim.x)
 
-__global__ void __launch_bounds__(128, RT_VW_MINB_TRACE) k_vw_trace(RenderParams P, int round)
+// The trace queue of a round: rounds alternate between two arrays, since
+// the kernel that reads round r's queue also appends to round r + 1's.
+__device__ __forceinline__ int *vw_trace_queue(const RenderParams &P, int round)
 {
-    round = cur_round(P, round);
-    const DevScene &S = P.S;
-    RoundCounters *C = &P.W.cnt[round];
-    VW_LOOP(C->closest, P.W.q_closest)
-    {
-        const int slot = qin_[i_];
-        int flags = P.W.flags[slot];
-        float4 ro = P.W.ray_o[slot], rd = P.W.ray_d[slot];
-        float4 seg;
-        Hit h;
-        if (flags & VF_FIRST) {
-            // vol_start: no hit yet, the camera medium
-            h.t = RT_MAX_REAL; h.u = h.v = 0.f; h.prim = -1;
-            seg = make_float4(0.f, 0.f, 0.f, __int_as_float(S.cam.medium));
-            flags = VF_EMISSION;
-        } else {
-            float4 hv = P.W.hit[slot];
-            h.t = hv.x; h.u = hv.y; h.v = hv.z; h.prim = __float_as_int(hv.w);
-            seg = P.W.v_seg[slot];
-            if (!(flags & VF_NULLX)) {   // the trace that ends a bounce
-                flags &= ~VF_EMISSION;
-                float4 rad = P.W.rad[slot];
-                rad.w = __int_as_float(__float_as_int(rad.w) + 1);
-                P.W.rad[slot] = rad;
-            }
-        }
-        Hit nh;
-        const bool was = vp_trace(S, xyz(ro), xyz(rd), ro.w, rd.w, nh);
-        if (was) {
-            h = nh;
-            seg = make_float4(ro.x, ro.y, ro.z, seg.w);
-        }
-        flags = (flags & ~(VF_NULLX | VF_WAS)) | (was ? VF_WAS : 0);
-        P.W.hit[slot] = make_float4(h.t, h.u, h.v, __int_as_float(h.prim));
-        P.W.v_seg[slot] = seg;
-        P.W.flags[slot] = flags;
-        q_push(P.W.q_mat[0], &C->mat[0], slot, true);
-    }
+    return (round & 1) ? P.W.q_mat[0] : P.W.q_closest;
 }
 
-__global__ void __launch_bounds__(128, RT_VW_MINB_STEP) k_vw_step(RenderParams P, int round)
+// k_vw_trace_step: the closest hit of the path's ray (the trace that ends
+// vol_step, vol_start or a null crossing), then the step over that hit:
+// depth and guard, delta tracking through the medium, then the scatter point
+// or the surface (emission, null boundary, env miss), and the light pick and
+// sample of sampleAttenuatedLightDirect.  The trace's hit, segment origin,
+// flags and depth stay in registers for the step; the hit is stored for the
+// kernels after it.
+__global__ void __launch_bounds__(128, RT_VW_MINB_STEP) k_vw_trace_step(RenderParams P, int round)
 {
     round = cur_round(P, round);
     const DevScene &S = P.S;
     RoundCounters *C = &P.W.cnt[round];
     RoundCounters *Cn = &P.W.cnt[round + 1];
+    int *next_q = vw_trace_queue(P, round + 1);
     int limit = 0;
-    VW_LOOP(C->mat[0], P.W.q_mat[0])
+    VW_LOOP(C->closest, vw_trace_queue(P, round))
     {
         const int slot = qin_[i_];
+        // ---- the trace (k_vw_trace)
         int flags = P.W.flags[slot];
-        float4 radv = P.W.rad[slot], tpv = P.W.tp[slot];
+        const float4 ro = P.W.ray_o[slot], rd = P.W.ray_d[slot];
+        float4 radv = P.W.rad[slot];
+        float4 seg;
+        Hit h;
+        if (flags & VF_FIRST) {
+            h.t = RT_MAX_REAL; h.u = h.v = 0.f; h.prim = -1;
+            seg = make_float4(0.f, 0.f, 0.f, __int_as_float(S.cam.medium));
+            flags = VF_EMISSION;
+        } else {
+            const float4 hv = P.W.hit[slot];
+            h.t = hv.x; h.u = hv.y; h.v = hv.z; h.prim = __float_as_int(hv.w);
+            seg = P.W.v_seg[slot];
+            if (!(flags & VF_NULLX)) {   // the trace that ends a bounce
+                flags &= ~VF_EMISSION;
+                radv.w = __int_as_float(__float_as_int(radv.w) + 1);
+            }
+        }
+        {
+            Hit nh;
+            const bool was = vp_trace(S, xyz(ro), xyz(rd), ro.w, rd.w, nh);
+            if (was) {
+                h = nh;
+                seg = make_float4(ro.x, ro.y, ro.z, seg.w);
+            }
+            flags = (flags & ~(VF_NULLX | VF_WAS)) | (was ? VF_WAS : 0);
+        }
+        P.W.hit[slot] = make_float4(h.t, h.u, h.v, __int_as_float(h.prim));
+        // ---- the step (k_vw_step)
+        const float4 tpv = P.W.tp[slot];
         C3 L = rgb(radv), T = rgb(tpv);
         const int depth = __float_as_int(radv.w);
         bool push_shadow = false, push_sample = false, push_trace = false;
@@ -510,11 +511,7 @@ __global__ void __launch_bounds__(128, RT_VW_MINB_STEP) k_vw_step(RenderParams P
             vw_done(P, slot, L);
         } else {
             Pcg32 rng = P.W.rng[slot];
-            float4 ro = P.W.ray_o[slot], rd = P.W.ray_d[slot];
             Ray ray = make_ray(xyz(ro), xyz(rd), ro.w, rd.w);
-            float4 hv = P.W.hit[slot];
-            Hit h; h.t = hv.x; h.u = hv.y; h.v = hv.z; h.prim = __float_as_int(hv.w);
-            float4 seg = P.W.v_seg[slot];
             int medium = __float_as_int(seg.w);
             float t = 0.f;
             C3 wm = cfill(0.f), em = cfill(0.f);
@@ -581,7 +578,7 @@ __global__ void __launch_bounds__(128, RT_VW_MINB_STEP) k_vw_step(RenderParams P
         q_push(P.W.q_shadow, &C->shadow, slot, push_shadow);
         q_push(P.W.q_mat[1], &C->mat[1], slot, push_sample && scat);
         q_push(P.W.q_mat[4], &C->mat[4], slot, push_sample && !scat);
-        q_push(P.W.q_closest, &Cn->closest, slot, push_trace);
+        q_push(next_q, &Cn->closest, slot, push_trace);
     }
     if (limit) atomicOr(P.limit_flag, RT_LIM_VOLPATH);
 }
@@ -811,7 +808,7 @@ __global__ void __launch_bounds__(128, RT_VW_MINB_FINISH) k_vw_finish(RenderPara
             P.W.rad[slot] = f4c(L, radv.w);
             P.W.tp[slot] = f4c(T, eta);
         }
-        q_push(P.W.q_closest, &Cn->closest, slot, !done);
+        q_push(vw_trace_queue(P, round + 1), &Cn->closest, slot, !done);
     }
 }
 
