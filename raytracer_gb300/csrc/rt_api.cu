@@ -2925,7 +2925,7 @@ static rt_status launch_check(const char *what)
 // One wavefront batch as a CUDA graph: reset the batch's counters and the
 // device round index, camera rays, then a conditional WHILE node whose body
 // is one round (PathTracingMIS: closest-hit trace, shadow trace, finish,
-// shading; VolPath: its six kernels; then k_round_next), then the film
+// shading; VolPath: its five kernels; then k_round_next), then the film
 // reduction.  The graph is built once
 // per distinct set of launch parameters and kept; the conditional handle it
 // owns is only ever set by its own k_round_next.
@@ -3001,8 +3001,7 @@ static rt_status pt_batch_graph(rt_ctx *ctx, rt_scene *sc, const RenderParams &P
                 k_vw_shadow<<<sm * RT_VW_MINB_SHADOW, 128, 0, bs>>>(P, 0);
                 k_vw_sample<true><<<sm * RT_VW_MINB_SAMPLE, 128, 0, bs>>>(P, 0);
                 k_vw_sample<false><<<sm * RT_VW_MINB_SAMPLE, 128, 0, bs>>>(P, 0);
-                k_vw_trsamp<<<sm * RT_VW_MINB_TRSAMP, 128, 0, bs>>>(P, 0);
-                k_vw_finish<<<sm * RT_VW_MINB_FINISH, 128, 0, bs>>>(P, 0);
+                k_vw_trsamp_finish<<<sm * RT_VW_MINB_TRSAMP, 128, 0, bs>>>(P, 0);
             } else {
                 launch_trace(width, P, 0, false, false, trace_blocks, bs);
                 launch_trace(width, P, 0, true, false, trace_blocks, bs);
@@ -3205,16 +3204,15 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
         launches++;
         if ((s = launch_check("k_camera")) != RT_OK) return s;
         if (rd->integrator == RT_INTEGRATOR_VOLPATH && ctx->volpath_wave) {
-            // one round = one vol_step of every live path (six kernels)
+            // one round = one vol_step of every live path (five kernels)
             prof_begin(ctx, K_VOLPATH);
             for (int r = 0; r < max_rounds; r++) {
                 k_vw_trace_step<<<sm * RT_VW_MINB_STEP, 128, 0, st>>>(P, r);
                 k_vw_shadow<<<sm * RT_VW_MINB_SHADOW, 128, 0, st>>>(P, r);
                 k_vw_sample<true><<<sm * RT_VW_MINB_SAMPLE, 128, 0, st>>>(P, r);
                 k_vw_sample<false><<<sm * RT_VW_MINB_SAMPLE, 128, 0, st>>>(P, r);
-                k_vw_trsamp<<<sm * RT_VW_MINB_TRSAMP, 128, 0, st>>>(P, r);
-                k_vw_finish<<<sm * RT_VW_MINB_FINISH, 128, 0, st>>>(P, r);
-                launches += 6;
+                k_vw_trsamp_finish<<<sm * RT_VW_MINB_TRSAMP, 128, 0, st>>>(P, r);
+                launches += 5;
                 if ((s = launch_check("VolPath round")) != RT_OK) return s;
                 if ((r & 3) == 3 && r + 1 < max_rounds) {
                     int nq = 0;
@@ -3684,8 +3682,7 @@ rt_status rt_render_paths(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, c
                 k_vw_shadow<<<sm * RT_VW_MINB_SHADOW, 128, 0, st>>>(P, r);
                 k_vw_sample<true><<<sm * RT_VW_MINB_SAMPLE, 128, 0, st>>>(P, r);
                 k_vw_sample<false><<<sm * RT_VW_MINB_SAMPLE, 128, 0, st>>>(P, r);
-                k_vw_trsamp<<<sm * RT_VW_MINB_TRSAMP, 128, 0, st>>>(P, r);
-                k_vw_finish<<<sm * RT_VW_MINB_FINISH, 128, 0, st>>>(P, r);
+                k_vw_trsamp_finish<<<sm * RT_VW_MINB_TRSAMP, 128, 0, st>>>(P, r);
                 if ((e = launch_check("VolPath round (paths)")) != RT_OK) return e;
                 int nq = 0;
                 CK(cudaMemcpyAsync(&nq, &ctx->W.cnt[r + 1].closest, sizeof(int), cudaMemcpyDeviceToHost, st));

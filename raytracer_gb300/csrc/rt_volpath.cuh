@@ -349,18 +349,18 @@ __global__ void __launch_bounds__(128, RT_VOLPATH_MINB) k_volpath(RenderParams P
 //                                  boundaries, ratio tracking in media)
 //   k_vw_sample  [sample queues]   the light sample's MIS contribution, the
 //                                  phase or BSDF sample and the new ray
-//   k_vw_trsamp  [trsamp queue]    evalTransmittanceFromSampledBSDF along it
-//   k_vw_finish  [finish queue]    emission MIS of what the sampled ray
-//                                  found, throughput, Russian roulette
+//   k_vw_trsamp_finish [trsamp queue]  evalTransmittanceFromSampledBSDF
+//                                  along it, then emission MIS of what the
+//                                  sampled ray found, throughput, Russian
+//                                  roulette
 // Each path's draws come in the order of one uninterrupted vol_step, so a
 // path's radiance is the megakernel's.  The hit frame is not stored: it is
 // rebuilt from the hit, the origin of the ray segment that found it and the
 // path's direction (hit_frame), which is what the megakernel holds.  Queue
 // counts live in the round's RoundCounters: trace = closest (queue
 // q_closest in even rounds, q_mat[0] in odd ones), shadow = shadow, sample =
-// mat[1] (medium vertices) and mat[4] (surface vertices), trsamp = mat[2],
-// finish = mat[3]; the next round's trace queue is the next counters'
-// closest.
+// mat[1] (medium vertices) and mat[4] (surface vertices), trsamp = mat[2];
+// the next round's trace queue is the next counters' closest.
 enum { VF_FIRST = F_FIRST, VF_EMISSION = 2, VF_WAS = 4, VF_SCAT = 8, VF_NULLX = 16, VF_DELTA = 32, VF_NEWM = 64,
        VF_HASVAL = 128, VF_GUARD_SHIFT = 8 };
 
@@ -435,9 +435,6 @@ __device__ __noinline__ C3 vw_tr_sampled(const DevScene &S, Ray ray, Pcg32 &rng,
 #endif
 #ifndef RT_VW_MINB_TRSAMP
 #define RT_VW_MINB_TRSAMP RT_VW_MINB
-#endif
-#ifndef RT_VW_MINB_FINISH
-#define RT_VW_MINB_FINISH RT_VW_MINB
 #endif
 #define VW_LOOP(COUNT, QUEUE)                                                                      \
     const int n_ = (COUNT);                                                                        \
@@ -698,59 +695,41 @@ __global__ void __launch_bounds__(128, RT_VW_MINB_SAMPLE) k_vw_sample(RenderPara
     }
 }
 
-__global__ void __launch_bounds__(128, RT_VW_MINB_TRSAMP) k_vw_trsamp(RenderParams P, int round)
+// k_vw_trsamp_finish: evalTransmittanceFromSampledBSDF along the sampled ray,
+// then the end of the pass: emission MIS of what the ray found, throughput,
+// Russian roulette.  The transmittance, hit, segment origin and flags stay in
+// registers between the two; survivors go to the next round's trace queue.
+__global__ void __launch_bounds__(128, RT_VW_MINB_TRSAMP) k_vw_trsamp_finish(RenderParams P, int round)
 {
     round = cur_round(P, round);
     const DevScene &S = P.S;
     RoundCounters *C = &P.W.cnt[round];
+    RoundCounters *Cn = &P.W.cnt[round + 1];
+    int *next_q = vw_trace_queue(P, round + 1);
     int limit = 0;
     VW_LOOP(C->mat[2], P.W.q_mat[2])
     {
         const int slot = qin_[i_];
         int flags = P.W.flags[slot];
         Pcg32 rng = P.W.rng[slot];
-        float4 ro = P.W.ray_o[slot], rd = P.W.ray_d[slot];
-        float4 hv = P.W.hit[slot];
+        const float4 ro = P.W.ray_o[slot], rd = P.W.ray_d[slot];
+        const float4 hv = P.W.hit[slot];
         Hit h; h.t = hv.x; h.u = hv.y; h.v = hv.z; h.prim = __float_as_int(hv.w);
         float4 seg = P.W.v_seg[slot];
         V3 so = xyz(seg);
         bool was;
         int newm = -1;
-        C3 tr = vw_tr_sampled(S, make_ray(xyz(ro), xyz(rd), ro.w, rd.w), rng, __float_as_int(seg.w), h, so, was, newm,
-                              limit);
-        P.W.nee[slot] = f4c(tr, 0.f);
-        P.W.hit[slot] = make_float4(h.t, h.u, h.v, __int_as_float(h.prim));
-        P.W.v_seg[slot] = make_float4(so.x, so.y, so.z, seg.w);
-        P.W.rng[slot] = rng;
+        const C3 tr = vw_tr_sampled(S, make_ray(xyz(ro), xyz(rd), ro.w, rd.w), rng, __float_as_int(seg.w), h, so,
+                                    was, newm, limit);
         flags = (flags & ~(VF_WAS | VF_NEWM)) | (was ? VF_WAS : 0) | (newm >= 0 ? VF_NEWM : 0);
-        P.W.flags[slot] = flags;
-        q_push(P.W.q_mat[3], &C->mat[3], slot, true);
-    }
-    if (limit) atomicOr(P.limit_flag, RT_LIM_VOLPATH);
-}
-
-__global__ void __launch_bounds__(128, RT_VW_MINB_FINISH) k_vw_finish(RenderParams P, int round)
-{
-    round = cur_round(P, round);
-    const DevScene &S = P.S;
-    RoundCounters *C = &P.W.cnt[round];
-    RoundCounters *Cn = &P.W.cnt[round + 1];
-    VW_LOOP(C->mat[3], P.W.q_mat[3])
-    {
-        const int slot = qin_[i_];
-        const int flags = P.W.flags[slot];
-        float4 radv = P.W.rad[slot], tpv = P.W.tp[slot];
+        seg = make_float4(so.x, so.y, so.z, seg.w);
+        // ---- the end of the pass (emission MIS, throughput, roulette)
+        const float4 radv = P.W.rad[slot], tpv = P.W.tp[slot];
         C3 L = rgb(radv), T = rgb(tpv);
         float eta = tpv.w;
         const int depth = __float_as_int(radv.w);
-        float4 rd = P.W.ray_d[slot];
         const V3 d = xyz(rd);
-        float4 bsv = P.W.bs[slot];
-        C3 tr = rgb(P.W.nee[slot]);
-        const bool was = flags & VF_WAS;
-        float4 hv = P.W.hit[slot];
-        Hit h; h.t = hv.x; h.u = hv.y; h.v = hv.z; h.prim = __float_as_int(hv.w);
-        float4 seg = P.W.v_seg[slot];
+        const float4 bsv = P.W.bs[slot];
         const int medium = __float_as_int(seg.w);
         bool done = false;
         if (flags & VF_SCAT) {
@@ -796,19 +775,22 @@ __global__ void __launch_bounds__(128, RT_VW_MINB_FINISH) k_vw_finish(RenderPara
             }
         }
         if (!done && depth >= P.min_depth) {
-            Pcg32 rng = P.W.rng[slot];
             float stop = smin(0.95f, cmax(T) * eta * eta);
             if (next1d(rng) < stop) T = T / stop;
             else done = true;
-            P.W.rng[slot] = rng;
         }
         if (done) {
             vw_done(P, slot, L);
         } else {
+            P.W.rng[slot] = rng;
+            P.W.hit[slot] = make_float4(h.t, h.u, h.v, __int_as_float(h.prim));
+            P.W.v_seg[slot] = seg;
+            P.W.flags[slot] = flags;
             P.W.rad[slot] = f4c(L, radv.w);
             P.W.tp[slot] = f4c(T, eta);
         }
-        q_push(vw_trace_queue(P, round + 1), &Cn->closest, slot, !done);
+        q_push(next_q, &Cn->closest, slot, !done);
     }
+    if (limit) atomicOr(P.limit_flag, RT_LIM_VOLPATH);
 }
 
