@@ -2999,7 +2999,7 @@ static rt_status pt_batch_graph(rt_ctx *ctx, rt_scene *sc, const RenderParams &P
                 // counters' closest, which k_round_next tests)
                 k_vw_trace_step<<<sm * RT_VW_MINB_STEP, 128, 0, bs>>>(P, 0);
                 k_vw_shadow<<<sm * RT_VW_MINB_SHADOW, 128, 0, bs>>>(P, 0);
-                k_vw_sample<true><<<sm * RT_VW_MINB_SAMPLE, 128, 0, bs>>>(P, 0);
+                k_vw_scatter<<<sm * RT_VW_MINB_TRSAMP, 128, 0, bs>>>(P, 0);
                 k_vw_sample<false><<<sm * RT_VW_MINB_SAMPLE, 128, 0, bs>>>(P, 0);
                 k_vw_trsamp_finish<<<sm * RT_VW_MINB_TRSAMP, 128, 0, bs>>>(P, 0);
             } else {
@@ -3209,7 +3209,7 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
             for (int r = 0; r < max_rounds; r++) {
                 k_vw_trace_step<<<sm * RT_VW_MINB_STEP, 128, 0, st>>>(P, r);
                 k_vw_shadow<<<sm * RT_VW_MINB_SHADOW, 128, 0, st>>>(P, r);
-                k_vw_sample<true><<<sm * RT_VW_MINB_SAMPLE, 128, 0, st>>>(P, r);
+                k_vw_scatter<<<sm * RT_VW_MINB_TRSAMP, 128, 0, st>>>(P, r);
                 k_vw_sample<false><<<sm * RT_VW_MINB_SAMPLE, 128, 0, st>>>(P, r);
                 k_vw_trsamp_finish<<<sm * RT_VW_MINB_TRSAMP, 128, 0, st>>>(P, r);
                 launches += 5;
@@ -3323,7 +3323,7 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
     if (graph_batches) {
         // camera and film per batch, the rounds' kernels and k_round_next
         const int64_t rounds = (int64_t)stats[7];
-        const int per_round = vw ? 6 + 1 : 3 + __builtin_popcount(types) + 1;
+        const int per_round = vw ? 5 + 1 : 3 + __builtin_popcount(types) + 1;
         launches += 2 * (int64_t)graph_batches + rounds * per_round;
         trace_c_launches += rounds;
         trace_a_launches += rounds;
@@ -3680,7 +3680,7 @@ rt_status rt_render_paths(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, c
             for (int r = 0; r < max_rounds; r++) {
                 k_vw_trace_step<<<sm * RT_VW_MINB_STEP, 128, 0, st>>>(P, r);
                 k_vw_shadow<<<sm * RT_VW_MINB_SHADOW, 128, 0, st>>>(P, r);
-                k_vw_sample<true><<<sm * RT_VW_MINB_SAMPLE, 128, 0, st>>>(P, r);
+                k_vw_scatter<<<sm * RT_VW_MINB_TRSAMP, 128, 0, st>>>(P, r);
                 k_vw_sample<false><<<sm * RT_VW_MINB_SAMPLE, 128, 0, st>>>(P, r);
                 k_vw_trsamp_finish<<<sm * RT_VW_MINB_TRSAMP, 128, 0, st>>>(P, r);
                 if ((e = launch_check("VolPath round (paths)")) != RT_OK) return e;

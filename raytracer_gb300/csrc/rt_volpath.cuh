@@ -347,12 +347,16 @@ __global__ void __launch_bounds__(128, RT_VOLPATH_MINB) k_volpath(RenderParams P
 //   k_vw_shadow  [shadow queue]    the light sample's transmittance
 //                                  (evalTransmittance: traces through null
 //                                  boundaries, ratio tracking in media)
-//   k_vw_sample  [sample queues]   the light sample's MIS contribution, the
-//                                  phase or BSDF sample and the new ray
+//   k_vw_sample<false> [surface sample queue]  the light sample's MIS
+//                                  contribution, the BSDF sample and the new
+//                                  ray
 //   k_vw_trsamp_finish [trsamp queue]  evalTransmittanceFromSampledBSDF
 //                                  along it, then emission MIS of what the
 //                                  sampled ray found, throughput, Russian
 //                                  roulette
+//   k_vw_scatter [medium sample queue]  the same three steps for scatter
+//                                  points in media (phase function), in
+//                                  one kernel
 // Each path's draws come in the order of one uninterrupted vol_step, so a
 // path's radiance is the megakernel's.  The hit frame is not stored: it is
 // rebuilt from the hit, the origin of the ray segment that found it and the
@@ -607,8 +611,10 @@ __global__ void __launch_bounds__(128, RT_VW_MINB_SHADOW) k_vw_shadow(RenderPara
 }
 
 // SCAT: the paths whose vertex is a scatter point in a medium (sample queue
-// mat[1]); otherwise those on a surface (mat[4]).  Split so that the
-// frequent medium vertices run in a kernel without the BSDF code.
+// mat[1]); otherwise those on a surface (mat[4]).  The wavefront runs the
+// medium vertices through k_vw_scatter instead, which continues into the
+// sampled ray's transmittance in registers; k_vw_sample<true> is the same
+// step as a kernel of its own.
 template <bool SCAT>
 __global__ void __launch_bounds__(128, RT_VW_MINB_SAMPLE) k_vw_sample(RenderParams P, int round)
 {
@@ -695,10 +701,86 @@ __global__ void __launch_bounds__(128, RT_VW_MINB_SAMPLE) k_vw_sample(RenderPara
     }
 }
 
-// k_vw_trsamp_finish: evalTransmittanceFromSampledBSDF along the sampled ray,
-// then the end of the pass: emission MIS of what the ray found, throughput,
-// Russian roulette.  The transmittance, hit, segment origin and flags stay in
-// registers between the two; survivors go to the next round's trace queue.
+// The end of a pass once the sampled ray's transmittance is known: emission
+// MIS of what the ray found, throughput, Russian roulette
+// (VolPathTracing.cpp:300-367).  ro, rd: the sampled ray; h, seg, was,
+// flags: what evalTransmittanceFromSampledBSDF reported; L: the radiance with
+// this vertex's light-sample MIS.  Survivors go to the next round's trace
+// queue with their sampled ray.
+__device__ __forceinline__ void vw_finish_one(const RenderParams &P, const DevScene &S, RoundCounters *Cn,
+                                              int *next_q, int slot, int flags, Pcg32 rng, float4 ro, float4 rd,
+                                              float4 seg, const Hit &h, bool was, C3 tr, C3 L, int depth,
+                                              float4 tpv, float4 bsv)
+{
+    C3 T = rgb(tpv);
+    float eta = tpv.w;
+    const V3 d = xyz(rd);
+    const int medium = __float_as_int(seg.w);
+    bool done = false;
+    if (flags & VF_SCAT) {
+        T = T * rgb(bsv);
+        if (was) {
+            int hl = prim_light(S, h.prim);
+            if (hl >= 0) {
+                Frame fr = vp_frame(S, h, xyz(seg), d);
+                C3 Le = area_le(S, hl, -d, fr.n);
+                float pl = vp_light_pdf(S, hl, fr.p, xyz(P.W.v_li1[slot]), xyz(P.W.v_li2[slot]),
+                                        xyz(P.W.v_li0[slot]));
+                float w = power_heuristic(bsv.w, pl);
+                L = L + ((T * Le) * tr) * w;
+            }
+        }
+    } else {
+        const C3 f = rgb(bsv);
+        int caught = -1;
+        bool isenv = false;
+        C3 Le = cfill(0.f);
+        Frame fr;
+        fr.p = fr.n = v3(0, 0, 0);
+        if (was) {
+            int nl = prim_light(S, h.prim);
+            if (nl >= 0) {
+                caught = nl;
+                fr = vp_frame(S, h, xyz(seg), d);
+                Le = area_le(S, nl, -d, fr.n);
+            }
+        } else if (!(flags & VF_NEWM)) {
+            // a miss: the environment (its pdf depends on the direction only)
+            if (S.env_light >= 0) { caught = S.env_light; isenv = true; Le = env_le(S.lights[S.env_light], d); }
+        }
+        if (caught >= 0) {
+            float pl = (flags & VF_DELTA) ? 0.f : vp_light_pdf(S, caught, xyz(P.W.v_p[slot]), fr.p, fr.n, d);
+            float w = power_heuristic(bsv.w, pl);
+            L = L + (((T * Le) * f) * tr) * w;
+            if (isenv && medium < 0) done = true;
+        }
+        if (!done) {
+            T = T * f;
+            eta *= P.W.rel_eta[slot];
+        }
+    }
+    if (!done && depth >= P.min_depth) {
+        float stop = smin(0.95f, cmax(T) * eta * eta);
+        if (next1d(rng) < stop) T = T / stop;
+        else done = true;
+    }
+    if (done) {
+        vw_done(P, slot, L);
+    } else {
+        P.W.rng[slot] = rng;
+        P.W.ray_o[slot] = ro;
+        P.W.ray_d[slot] = rd;
+        P.W.hit[slot] = make_float4(h.t, h.u, h.v, __int_as_float(h.prim));
+        P.W.v_seg[slot] = seg;
+        P.W.flags[slot] = flags;
+        P.W.rad[slot] = f4c(L, __int_as_float(depth));
+        P.W.tp[slot] = f4c(T, eta);
+    }
+    q_push(next_q, &Cn->closest, slot, !done);
+}
+
+// k_vw_trsamp_finish: evalTransmittanceFromSampledBSDF along the ray that
+// k_vw_sample<false> sampled at a surface vertex, then vw_finish_one
 __global__ void __launch_bounds__(128, RT_VW_MINB_TRSAMP) k_vw_trsamp_finish(RenderParams P, int round)
 {
     round = cur_round(P, round);
@@ -723,74 +805,65 @@ __global__ void __launch_bounds__(128, RT_VW_MINB_TRSAMP) k_vw_trsamp_finish(Ren
                                     was, newm, limit);
         flags = (flags & ~(VF_WAS | VF_NEWM)) | (was ? VF_WAS : 0) | (newm >= 0 ? VF_NEWM : 0);
         seg = make_float4(so.x, so.y, so.z, seg.w);
-        // ---- the end of the pass (emission MIS, throughput, roulette)
-        const float4 radv = P.W.rad[slot], tpv = P.W.tp[slot];
-        C3 L = rgb(radv), T = rgb(tpv);
-        float eta = tpv.w;
-        const int depth = __float_as_int(radv.w);
-        const V3 d = xyz(rd);
-        const float4 bsv = P.W.bs[slot];
-        const int medium = __float_as_int(seg.w);
-        bool done = false;
-        if (flags & VF_SCAT) {
-            T = T * rgb(bsv);
-            if (was) {
-                int hl = prim_light(S, h.prim);
-                if (hl >= 0) {
-                    Frame fr = vp_frame(S, h, xyz(seg), d);
-                    C3 Le = area_le(S, hl, -d, fr.n);
-                    float pl = vp_light_pdf(S, hl, fr.p, xyz(P.W.v_li1[slot]), xyz(P.W.v_li2[slot]),
-                                            xyz(P.W.v_li0[slot]));
-                    float w = power_heuristic(bsv.w, pl);
-                    L = L + ((T * Le) * tr) * w;
-                }
-            }
-        } else {
-            const C3 f = rgb(bsv);
-            int caught = -1;
-            bool isenv = false;
-            C3 Le = cfill(0.f);
-            Frame fr;
-            fr.p = fr.n = v3(0, 0, 0);
-            if (was) {
-                int nl = prim_light(S, h.prim);
-                if (nl >= 0) {
-                    caught = nl;
-                    fr = vp_frame(S, h, xyz(seg), d);
-                    Le = area_le(S, nl, -d, fr.n);
-                }
-            } else if (!(flags & VF_NEWM)) {
-                // a miss: the environment (its pdf depends on the direction only)
-                if (S.env_light >= 0) { caught = S.env_light; isenv = true; Le = env_le(S.lights[S.env_light], d); }
-            }
-            if (caught >= 0) {
-                float pl = (flags & VF_DELTA) ? 0.f : vp_light_pdf(S, caught, xyz(P.W.v_p[slot]), fr.p, fr.n, d);
-                float w = power_heuristic(bsv.w, pl);
-                L = L + (((T * Le) * f) * tr) * w;
-                if (isenv && medium < 0) done = true;
-            }
-            if (!done) {
-                T = T * f;
-                eta *= P.W.rel_eta[slot];
-            }
-        }
-        if (!done && depth >= P.min_depth) {
-            float stop = smin(0.95f, cmax(T) * eta * eta);
-            if (next1d(rng) < stop) T = T / stop;
-            else done = true;
-        }
-        if (done) {
-            vw_done(P, slot, L);
-        } else {
-            P.W.rng[slot] = rng;
-            P.W.hit[slot] = make_float4(h.t, h.u, h.v, __int_as_float(h.prim));
-            P.W.v_seg[slot] = seg;
-            P.W.flags[slot] = flags;
-            P.W.rad[slot] = f4c(L, radv.w);
-            P.W.tp[slot] = f4c(T, eta);
-        }
-        q_push(next_q, &Cn->closest, slot, !done);
+        const float4 radv = P.W.rad[slot];
+        vw_finish_one(P, S, Cn, next_q, slot, flags, rng, ro, rd, seg, h, was, tr, rgb(radv),
+                      __float_as_int(radv.w), P.W.tp[slot], P.W.bs[slot]);
     }
     if (limit) atomicOr(P.limit_flag, RT_LIM_VOLPATH);
 }
 
+// k_vw_scatter: a scatter point in a medium (sample queue mat[1]) through the
+// rest of its pass in one kernel: the phase sample and the new ray
+// (k_vw_sample's medium branch), the transmittance along it, then the light
+// sample's MIS with the phase function (no draws, so its place after the
+// transmittance leaves the path's stream as it was) and vw_finish_one
+__global__ void __launch_bounds__(128, RT_VW_MINB_TRSAMP) k_vw_scatter(RenderParams P, int round)
+{
+    round = cur_round(P, round);
+    const DevScene &S = P.S;
+    RoundCounters *C = &P.W.cnt[round];
+    RoundCounters *Cn = &P.W.cnt[round + 1];
+    int *next_q = vw_trace_queue(P, round + 1);
+    int limit = 0;
+    VW_LOOP(C->mat[1], P.W.q_mat[1])
+    {
+        const int slot = qin_[i_];
+        int flags = P.W.flags[slot];
+        Pcg32 rng = P.W.rng[slot];
+        float4 seg = P.W.v_seg[slot];
+        const int medium = __float_as_int(seg.w);
+        float4 rd = P.W.ray_d[slot];
+        V3 wo;
+        float pfpdf;
+        const float pfw = phase_sample(S.media[medium], -xyz(rd), next2d(rng), wo, pfpdf);
+        const float4 ro = f4(xyz(P.W.v_p[slot]), 0.f);
+        rd = f4(wo, rd.w);
+        const float4 hv = P.W.hit[slot];
+        Hit h; h.t = hv.x; h.u = hv.y; h.v = hv.z; h.prim = __float_as_int(hv.w);
+        V3 so = xyz(seg);
+        bool was;
+        int newm = -1;
+        const C3 tr = vw_tr_sampled(S, make_ray(xyz(ro), wo, 0.f, rd.w), rng, medium, h, so, was, newm, limit);
+        flags = (flags & ~(VF_WAS | VF_NEWM)) | (was ? VF_WAS : 0) | (newm >= 0 ? VF_NEWM : 0);
+        seg = make_float4(so.x, so.y, so.z, seg.w);
+        // the light sample's MIS at the scatter point (k_vw_sample)
+        const float4 radv = P.W.rad[slot], tpv = P.W.tp[slot];
+        C3 L = rgb(radv);
+        if (flags & VF_HASVAL) {
+            const C3 value = rgb(P.W.v_val[slot]);
+            if (!iszero(value)) {
+                const DevMedium &M = S.media[medium];
+                const V3 din = xyz(P.W.ray_d[slot]);
+                const V3 to_light = xyz(P.W.v_li0[slot]);
+                const float lpdf = P.W.v_li1[slot].w;
+                const float pf = P.W.v_li2[slot].w != 0.f ? 0.f : phase_eval(M, to_light, -din);
+                const float w = power_heuristic(lpdf, pf);
+                const float ev = phase_eval(M, to_light, -din);
+                L = L + ((rgb(tpv) * value) * ev) * w;
+            }
+        }
+        vw_finish_one(P, S, Cn, next_q, slot, flags, rng, ro, rd, seg, h, was, tr, L, __float_as_int(radv.w), tpv,
+                      f4c(cfill(pfw), pfpdf));
+    }
+    if (limit) atomicOr(P.limit_flag, RT_LIM_VOLPATH);
+}
