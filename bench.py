@@ -239,8 +239,9 @@ def run_reference(args):
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "notes": "reference CPU path = the oracle's C restatement of the integrator with the reference's "
                      "two-level SAH BVH, whose per-path radiance is bit-identical to the reference's own "
-                     "PathTracingMIS compiled from its sources (pin tests); those sources are not on this "
-                     "machine, so the restatement is what runs; oracle scene build %.1f s not timed" % build_s}
+                     "PathTracingMIS compiled from its sources (pin tests); the GPU machine has no copy of "
+                     "those sources, so the restatement is what runs everywhere; oracle scene build %.1f s "
+                     "not timed" % build_s}
     print(json.dumps(line))
 
 
