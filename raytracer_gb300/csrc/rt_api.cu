@@ -3000,7 +3000,7 @@ static rt_status pt_batch_graph(rt_ctx *ctx, rt_scene *sc, const RenderParams &P
                 k_vw_trace_step<<<sm * RT_VW_MINB_STEP, 128, 0, bs>>>(P, 0);
                 k_vw_shadow<<<sm * RT_VW_MINB_SHADOW, 128, 0, bs>>>(P, 0);
                 k_vw_scatter<<<sm * RT_VW_MINB_TRSAMP, 128, 0, bs>>>(P, 0);
-                k_vw_sample<false><<<sm * RT_VW_MINB_SAMPLE, 128, 0, bs>>>(P, 0);
+                k_vw_sample_surface<<<sm * RT_VW_MINB_SAMPLE, 128, 0, bs>>>(P, 0);
                 k_vw_trsamp_finish<<<sm * RT_VW_MINB_TRSAMP, 128, 0, bs>>>(P, 0);
             } else {
                 launch_trace(width, P, 0, false, false, trace_blocks, bs);
@@ -3210,7 +3210,7 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
                 k_vw_trace_step<<<sm * RT_VW_MINB_STEP, 128, 0, st>>>(P, r);
                 k_vw_shadow<<<sm * RT_VW_MINB_SHADOW, 128, 0, st>>>(P, r);
                 k_vw_scatter<<<sm * RT_VW_MINB_TRSAMP, 128, 0, st>>>(P, r);
-                k_vw_sample<false><<<sm * RT_VW_MINB_SAMPLE, 128, 0, st>>>(P, r);
+                k_vw_sample_surface<<<sm * RT_VW_MINB_SAMPLE, 128, 0, st>>>(P, r);
                 k_vw_trsamp_finish<<<sm * RT_VW_MINB_TRSAMP, 128, 0, st>>>(P, r);
                 launches += 5;
                 if ((s = launch_check("VolPath round")) != RT_OK) return s;
@@ -3681,7 +3681,7 @@ rt_status rt_render_paths(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, c
                 k_vw_trace_step<<<sm * RT_VW_MINB_STEP, 128, 0, st>>>(P, r);
                 k_vw_shadow<<<sm * RT_VW_MINB_SHADOW, 128, 0, st>>>(P, r);
                 k_vw_scatter<<<sm * RT_VW_MINB_TRSAMP, 128, 0, st>>>(P, r);
-                k_vw_sample<false><<<sm * RT_VW_MINB_SAMPLE, 128, 0, st>>>(P, r);
+                k_vw_sample_surface<<<sm * RT_VW_MINB_SAMPLE, 128, 0, st>>>(P, r);
                 k_vw_trsamp_finish<<<sm * RT_VW_MINB_TRSAMP, 128, 0, st>>>(P, r);
                 if ((e = launch_check("VolPath round (paths)")) != RT_OK) return e;
                 int nq = 0;

@@ -347,7 +347,7 @@ __global__ void __launch_bounds__(128, RT_VOLPATH_MINB) k_volpath(RenderParams P
 //   k_vw_shadow  [shadow queue]    the light sample's transmittance
 //                                  (evalTransmittance: traces through null
 //                                  boundaries, ratio tracking in media)
-//   k_vw_sample<false> [surface sample queue]  the light sample's MIS
+//   k_vw_sample_surface [surface sample queue]  the light sample's MIS
 //                                  contribution, the BSDF sample and the new
 //                                  ray
 //   k_vw_trsamp_finish [trsamp queue]  evalTransmittanceFromSampledBSDF
@@ -610,18 +610,16 @@ __global__ void __launch_bounds__(128, RT_VW_MINB_SHADOW) k_vw_shadow(RenderPara
     if (limit) atomicOr(P.limit_flag, RT_LIM_VOLPATH);
 }
 
-// SCAT: the paths whose vertex is a scatter point in a medium (sample queue
-// mat[1]); otherwise those on a surface (mat[4]).  The wavefront runs the
-// medium vertices through k_vw_scatter instead, which continues into the
-// sampled ray's transmittance in registers; k_vw_sample<true> is the same
-// step as a kernel of its own.
-template <bool SCAT>
-__global__ void __launch_bounds__(128, RT_VW_MINB_SAMPLE) k_vw_sample(RenderParams P, int round)
+// k_vw_sample_surface: the paths whose vertex is on a surface (sample queue
+// mat[4]): the light sample's MIS with the BSDF (textures applied), the BSDF
+// sample and the new ray.  Scatter points in media (mat[1]) go through
+// k_vw_scatter, which continues into the sampled ray's transmittance.
+__global__ void __launch_bounds__(128, RT_VW_MINB_SAMPLE) k_vw_sample_surface(RenderParams P, int round)
 {
     round = cur_round(P, round);
     const DevScene &S = P.S;
     RoundCounters *C = &P.W.cnt[round];
-    VW_LOOP(C->mat[SCAT ? 1 : 4], P.W.q_mat[SCAT ? 1 : 4])
+    VW_LOOP(C->mat[4], P.W.q_mat[4])
     {
         const int slot = qin_[i_];
         int flags = P.W.flags[slot];
@@ -635,23 +633,7 @@ __global__ void __launch_bounds__(128, RT_VW_MINB_SAMPLE) k_vw_sample(RenderPara
         const bool hasval = flags & VF_HASVAL;
         C3 value = hasval ? rgb(P.W.v_val[slot]) : cfill(0.f);
         bool push = true;
-        if (SCAT) {
-            const DevMedium &M = S.media[medium];
-            if (!iszero(value)) {
-                V3 to_light = xyz(P.W.v_li0[slot]);
-                float lpdf = P.W.v_li1[slot].w;
-                float pf = P.W.v_li2[slot].w != 0.f ? 0.f : phase_eval(M, to_light, -ray.d);
-                float w = power_heuristic(lpdf, pf);
-                float ev = phase_eval(M, to_light, -ray.d);
-                L = L + ((T * value) * ev) * w;
-            }
-            V3 wo;
-            float pfpdf;
-            float pfw = phase_sample(M, -ray.d, next2d(rng), wo, pfpdf);
-            V3 p = xyz(P.W.v_p[slot]);
-            ray = make_ray(p, wo, 0.f, ray.maxt);
-            P.W.bs[slot] = f4c(cfill(pfw), pfpdf);
-        } else {
+        {
             float4 hv = P.W.hit[slot];
             Hit h; h.t = hv.x; h.u = hv.y; h.v = hv.z; h.prim = __float_as_int(hv.w);
             Frame fr = vp_frame(S, h, xyz(seg), ray.d);
@@ -780,7 +762,7 @@ __device__ __forceinline__ void vw_finish_one(const RenderParams &P, const DevSc
 }
 
 // k_vw_trsamp_finish: evalTransmittanceFromSampledBSDF along the ray that
-// k_vw_sample<false> sampled at a surface vertex, then vw_finish_one
+// k_vw_sample_surface sampled at a surface vertex, then vw_finish_one
 __global__ void __launch_bounds__(128, RT_VW_MINB_TRSAMP) k_vw_trsamp_finish(RenderParams P, int round)
 {
     round = cur_round(P, round);
@@ -814,7 +796,7 @@ __global__ void __launch_bounds__(128, RT_VW_MINB_TRSAMP) k_vw_trsamp_finish(Ren
 
 // k_vw_scatter: a scatter point in a medium (sample queue mat[1]) through the
 // rest of its pass in one kernel: the phase sample and the new ray
-// (k_vw_sample's medium branch), the transmittance along it, then the light
+// (the phase function's), the transmittance along it, then the light
 // sample's MIS with the phase function (no draws, so its place after the
 // transmittance leaves the path's stream as it was) and vw_finish_one
 __global__ void __launch_bounds__(128, RT_VW_MINB_TRSAMP) k_vw_scatter(RenderParams P, int round)
@@ -846,7 +828,7 @@ __global__ void __launch_bounds__(128, RT_VW_MINB_TRSAMP) k_vw_scatter(RenderPar
         const C3 tr = vw_tr_sampled(S, make_ray(xyz(ro), wo, 0.f, rd.w), rng, medium, h, so, was, newm, limit);
         flags = (flags & ~(VF_WAS | VF_NEWM)) | (was ? VF_WAS : 0) | (newm >= 0 ? VF_NEWM : 0);
         seg = make_float4(so.x, so.y, so.z, seg.w);
-        // the light sample's MIS at the scatter point (k_vw_sample)
+        // the light sample's MIS at the scatter point
         const float4 radv = P.W.rad[slot], tpv = P.W.tp[slot];
         C3 L = rgb(radv);
         if (flags & VF_HASVAL) {
