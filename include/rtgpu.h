@@ -232,7 +232,9 @@ typedef struct rt_scene_desc {
 /* Render description                                                  */
 /* ------------------------------------------------------------------ */
 enum { RT_INTEGRATOR_PATH_MIS = 0, RT_INTEGRATOR_VOLPATH = 1 };
-/* integrator/Integrator.h:11-15 strategy names */
+/* integrator/Integrator.h:11-15 strategy names.  ALL_LIGHTS: PathTracingMIS
+ * samples every light at every vertex (PathTracingMIS.cpp:80-117);
+ * VolPathTracing then selects one light uniformly, as the reference does. */
 enum { RT_STRATEGY_ALL_LIGHTS = 0, RT_STRATEGY_ONE_LIGHT_UNIFORM = 1,
        RT_STRATEGY_ONE_LIGHT_WEIGHTED = 2 };
 

@@ -118,6 +118,10 @@ struct RenderParams {
     // rounds with fewer closest-hit rays than this are not sorted by
     // material: their hits go to one queue shaded by k_pt_shade<RT_QUEUE_MIXED>
     int sort_threshold;
+    // PathTracingMIS with the all-lights strategy: every light sampled at
+    // every vertex, its shadow ray traced in the shading kernel (the
+    // k_pt_shade<..., ALL> kernels)
+    int all_lights;
     // multi-scene batches: the scene table (one entry per job, indexed by
     // W.sid), the batch's work items and their count; null otherwise
     const DevScene *scenes;
@@ -1111,7 +1115,38 @@ __device__ __forceinline__ C3 bsdf_sample_t(const DevBsdf &b, BsdfRec &r, V2 s, 
 #ifndef RT_SHADE_GRID
 #define RT_SHADE_GRID 16
 #endif
+// The all-lights strategy of PathTracingMIS::li (PathTracingMIS.cpp:80-117):
+// one sample of every light in turn, each with its own shadow ray (traced
+// here, any hit through the binary tree and the analytic shapes, as
+// Integrator::sampleOneLight does) and its MIS weight against the BSDF,
+// added to L in light order.  Out of line so that the shading kernels'
+// registers on the one-light path stay as they are.
 template <int BT>
+__device__ __noinline__ C3 pt_all_lights(const DevScene &S, const DevBsdf &B, const Frame &fr, V3 d, C3 T, C3 L,
+                                         Pcg32 &rng)
+{
+    for (int l = 0; l < S.n_lights; l++) {
+        const V2 s = next2d(rng);
+        LightRec li;
+        light_sample(S, l, fr.p, s, li);
+        C3 value = cfill(0.f);
+        if (li.pdf > 0 && lum(li.intensity) > 0) {
+            Hit sh;
+            if (!trace_ray<true>(S, fr.p, li.to_light, RT_EPSILON, li.distance - RT_EPSILON, sh))
+                value = li.intensity / li.pdf;
+        }
+        if (!iszero(value)) {
+            V3 wi = to_local(fr, li.to_light), wo = to_local(fr, -d);
+            float ct = fabsf(wi.z);
+            float bp = li.delta ? 0.f : bsdf_pdf_t<BT>(B, wi, wo);
+            float w = power_heuristic(li.pdf, bp);
+            L = L + (((T * value) * bsdf_eval_t<BT>(B, wi, wo)) * ct) * w;
+        }
+    }
+    return L;
+}
+
+template <int BT, bool ALL = false>
 __device__ __forceinline__ void pt_shade_path(const RenderParams &P, const DevScene &S, int slot, bool &push_end,
                                               bool &push_closest, bool &push_shadow)
 {
@@ -1177,6 +1212,9 @@ __device__ __forceinline__ void pt_shade_path(const RenderParams &P, const DevSc
         if (hl >= 0) L = L + T * area_le(S, hl, -d, fr.n);
     }
     // light sampling (Integrator::sampleLightDirect, Integrator.cpp:176-218)
+    if (ALL) {
+        L = pt_all_lights<BT>(S, B, fr, d, T, L, rng);
+    } else {
     V2 s = next2d(rng);
     if (S.n_lights > 0) {
         float lw;
@@ -1208,6 +1246,7 @@ __device__ __forceinline__ void pt_shade_path(const RenderParams &P, const DevSc
             }
         }
     }
+    }
     // BSDF sampling
     BsdfRec r;
     r.wi = to_local(fr, -d); r.wo = v3(0, 0, 0);
@@ -1236,8 +1275,10 @@ __device__ __forceinline__ void pt_shade_path(const RenderParams &P, const DevSc
     P.W.flags[slot] = flags;
     }
 }
-// MULTI: a multi-scene batch, each path shaded against its own scene
-template <int BT, bool MULTI = false>
+// MULTI: a multi-scene batch, each path shaded against its own scene.
+// ALL: the all-lights strategy (its own instantiations, so that the
+// one-light kernels are compiled as without it)
+template <int BT, bool MULTI = false, bool ALL = false>
 __global__ void __launch_bounds__(128, RT_SHADE_MINB) k_pt_shade(RenderParams P, int round)
 {
     round = cur_round(P, round);
@@ -1253,12 +1294,35 @@ __global__ void __launch_bounds__(128, RT_SHADE_MINB) k_pt_shade(RenderParams P,
         int slot = valid ? qin[idx] : 0;
         bool push_end = false, push_closest = false, push_shadow = false;
         if (valid) {
-            if (MULTI) pt_shade_path<BT>(P, P.scenes[P.W.sid[slot]], slot, push_end, push_closest, push_shadow);
-            else pt_shade_path<BT>(P, P.S, slot, push_end, push_closest, push_shadow);
+            if (MULTI) pt_shade_path<BT, ALL>(P, P.scenes[P.W.sid[slot]], slot, push_end, push_closest, push_shadow);
+            else pt_shade_path<BT, ALL>(P, P.S, slot, push_end, push_closest, push_shadow);
         }
         q_push(P.W.q_end, &Cout->end, slot, push_end);
         q_push(P.W.q_closest, &Cout->closest, slot, push_closest);
         q_push(P.W.q_shadow, &Cout->shadow, slot, push_shadow);
+    }
+}
+
+// The shading kernels of one round for the shading queues in `types` (bit
+// q: queue q in use), the all-lights instantiations for that strategy
+static void launch_shades(int types, const RenderParams &P, int r, int blocks, cudaStream_t st)
+{
+    if (P.all_lights) {
+        if (types & 1) k_pt_shade<0, false, true><<<blocks, 128, 0, st>>>(P, r);
+        if (types & 2) k_pt_shade<1, false, true><<<blocks, 128, 0, st>>>(P, r);
+        if (types & 4) k_pt_shade<2, false, true><<<blocks, 128, 0, st>>>(P, r);
+        if (types & 8) k_pt_shade<3, false, true><<<blocks, 128, 0, st>>>(P, r);
+        if (types & 16) k_pt_shade<4, false, true><<<blocks, 128, 0, st>>>(P, r);
+        if (types & 32) k_pt_shade<5, false, true><<<blocks, 128, 0, st>>>(P, r);
+        if (types & (1 << RT_QUEUE_MIXED)) k_pt_shade<RT_QUEUE_MIXED, false, true><<<blocks, 128, 0, st>>>(P, r);
+    } else {
+        if (types & 1) k_pt_shade<0><<<blocks, 128, 0, st>>>(P, r);
+        if (types & 2) k_pt_shade<1><<<blocks, 128, 0, st>>>(P, r);
+        if (types & 4) k_pt_shade<2><<<blocks, 128, 0, st>>>(P, r);
+        if (types & 8) k_pt_shade<3><<<blocks, 128, 0, st>>>(P, r);
+        if (types & 16) k_pt_shade<4><<<blocks, 128, 0, st>>>(P, r);
+        if (types & 32) k_pt_shade<5><<<blocks, 128, 0, st>>>(P, r);
+        if (types & (1 << RT_QUEUE_MIXED)) k_pt_shade<RT_QUEUE_MIXED><<<blocks, 128, 0, st>>>(P, r);
     }
 }
 
@@ -3006,13 +3070,7 @@ static rt_status pt_batch_graph(rt_ctx *ctx, rt_scene *sc, const RenderParams &P
                 launch_trace(width, P, 0, false, false, trace_blocks, bs);
                 launch_trace(width, P, 0, true, false, trace_blocks, bs);
                 k_pt_finish<<<shade_blocks, 128, 0, bs>>>(P, 0);
-                if (types & 1) k_pt_shade<0><<<shade_blocks, 128, 0, bs>>>(P, 0);
-                if (types & 2) k_pt_shade<1><<<shade_blocks, 128, 0, bs>>>(P, 0);
-                if (types & 4) k_pt_shade<2><<<shade_blocks, 128, 0, bs>>>(P, 0);
-                if (types & 8) k_pt_shade<3><<<shade_blocks, 128, 0, bs>>>(P, 0);
-                if (types & 16) k_pt_shade<4><<<shade_blocks, 128, 0, bs>>>(P, 0);
-                if (types & 32) k_pt_shade<5><<<shade_blocks, 128, 0, bs>>>(P, 0);
-                if (types & 64) k_pt_shade<RT_QUEUE_MIXED><<<shade_blocks, 128, 0, bs>>>(P, 0);
+                launch_shades(types, P, 0, shade_blocks, bs);
             }
             k_round_next<<<1, 1, 0, bs>>>(P, loop, max_rounds);
             if (bad(cudaGetLastError(), "round kernels")) break;
@@ -3055,8 +3113,6 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
     if (rd->spp <= 0 || rd->sample_begin < 0) return fail(RT_ERR_INVALID, "rt_render: bad sample range");
     if (rd->integrator != RT_INTEGRATOR_PATH_MIS && rd->integrator != RT_INTEGRATOR_VOLPATH)
         return fail(RT_ERR_UNSUPPORTED, "rt_render: unknown integrator");
-    if (rd->integrator == RT_INTEGRATOR_PATH_MIS && rd->strategy == RT_STRATEGY_ALL_LIGHTS)
-        return fail(RT_ERR_UNSUPPORTED, "rt_render: all_lights strategy is not provided by the device path");
     if (rd->max_depth < 0 || rd->min_depth < 0) return fail(RT_ERR_INVALID, "rt_render: negative depth");
     if (rd->flags & ~RT_RENDER_ACCUMULATE) return fail(RT_ERR_INVALID, "rt_render: unknown flags");
     const int accumulate = (rd->flags & RT_RENDER_ACCUMULATE) ? 1 : 0;
@@ -3164,6 +3220,7 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
     P.spp = rd->spp;
     P.sample_begin = rd->sample_begin;
     P.sort_threshold = ctx->sort_threshold;
+    P.all_lights = rd->integrator == RT_INTEGRATOR_PATH_MIS && rd->strategy == RT_STRATEGY_ALL_LIGHTS;
     // shading queues in use: the scene's (textured BSDFs in the mixed one),
     // and the mixed one for bounces below the sort threshold
     const int types = sc->bsdf_types | (P.sort_threshold > 0 ? 1 << RT_QUEUE_MIXED : 0);
@@ -3252,13 +3309,7 @@ rt_status rt_render(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, float *
                 k_pt_finish<<<shade_blocks, 128, 0, st>>>(P, ri);
                 prof_end(ctx);
                 prof_begin(ctx, K_SHADE);
-                if (sc->bsdf_types & 1) k_pt_shade<0><<<shade_blocks, 128, 0, st>>>(P, ri);
-                if (sc->bsdf_types & 2) k_pt_shade<1><<<shade_blocks, 128, 0, st>>>(P, ri);
-                if (sc->bsdf_types & 4) k_pt_shade<2><<<shade_blocks, 128, 0, st>>>(P, ri);
-                if (sc->bsdf_types & 8) k_pt_shade<3><<<shade_blocks, 128, 0, st>>>(P, ri);
-                if (sc->bsdf_types & 16) k_pt_shade<4><<<shade_blocks, 128, 0, st>>>(P, ri);
-                if (sc->bsdf_types & 32) k_pt_shade<5><<<shade_blocks, 128, 0, st>>>(P, ri);
-                if (types & (1 << RT_QUEUE_MIXED)) k_pt_shade<RT_QUEUE_MIXED><<<shade_blocks, 128, 0, st>>>(P, ri);
+                launch_shades(types, P, ri, shade_blocks, st);
                 prof_end(ctx);
                 launches += 3 + __builtin_popcount(types);
                 trace_c_launches++;
@@ -3621,8 +3672,6 @@ rt_status rt_render_paths(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, c
     if (n == 0) return RT_OK;
     if (rd->integrator != RT_INTEGRATOR_PATH_MIS && rd->integrator != RT_INTEGRATOR_VOLPATH)
         return fail(RT_ERR_UNSUPPORTED, "rt_render_paths: unknown integrator");
-    if (rd->integrator == RT_INTEGRATOR_PATH_MIS && rd->strategy == RT_STRATEGY_ALL_LIGHTS)
-        return fail(RT_ERR_UNSUPPORTED, "rt_render_paths: all_lights strategy is not provided by the device path");
     if (rd->max_depth < 0 || rd->min_depth < 0 || rd->max_depth > (1 << 16))
         return fail(RT_ERR_INVALID, "rt_render_paths: bad depth");
     const DevCamera &cam = sc->S.cam;
@@ -3671,6 +3720,7 @@ rt_status rt_render_paths(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, c
         P.n_paths = n;
         P.npix = n;
         P.sort_threshold = ctx->sort_threshold;
+        P.all_lights = rd->integrator == RT_INTEGRATOR_PATH_MIS && rd->strategy == RT_STRATEGY_ALL_LIGHTS;
         P.path_list = (const int2 *)tmp;
         const int sm = ctx->sm_count > 0 ? ctx->sm_count : 1;
         rt_status e;
@@ -3701,13 +3751,7 @@ rt_status rt_render_paths(rt_ctx *ctx, rt_scene *sc, const rt_render_desc *rd, c
                 launch_trace(width, P, r, false, false, tb, st);
                 launch_trace(width, P, r, true, false, tb, st);
                 k_pt_finish<<<sb, 128, 0, st>>>(P, r);
-                if (types & 1) k_pt_shade<0><<<sb, 128, 0, st>>>(P, r);
-                if (types & 2) k_pt_shade<1><<<sb, 128, 0, st>>>(P, r);
-                if (types & 4) k_pt_shade<2><<<sb, 128, 0, st>>>(P, r);
-                if (types & 8) k_pt_shade<3><<<sb, 128, 0, st>>>(P, r);
-                if (types & 16) k_pt_shade<4><<<sb, 128, 0, st>>>(P, r);
-                if (types & 32) k_pt_shade<5><<<sb, 128, 0, st>>>(P, r);
-                if (types & (1 << RT_QUEUE_MIXED)) k_pt_shade<RT_QUEUE_MIXED><<<sb, 128, 0, st>>>(P, r);
+                launch_shades(types, P, r, sb, st);
                 if ((e = launch_check("pt round (paths)")) != RT_OK) return e;
                 RoundCounters nc;
                 CK(cudaMemcpyAsync(&nc, &ctx->W.cnt[r + 1], sizeof(nc), cudaMemcpyDeviceToHost, st));
@@ -3919,8 +3963,6 @@ extern "C" rt_status rt_render_tile_static(rt_ctx *ctx, rt_scene *sc, const rt_r
     if (rd->spp <= 0 || rd->sample_begin < 0) return fail(RT_ERR_INVALID, "rt_render_tile_static: bad sample range");
     if (rd->integrator != RT_INTEGRATOR_PATH_MIS && rd->integrator != RT_INTEGRATOR_VOLPATH)
         return fail(RT_ERR_UNSUPPORTED, "rt_render_tile_static: unknown integrator");
-    if (rd->integrator == RT_INTEGRATOR_PATH_MIS && rd->strategy == RT_STRATEGY_ALL_LIGHTS)
-        return fail(RT_ERR_UNSUPPORTED, "rt_render_tile_static: all_lights strategy is not provided by the device path");
     if (rd->max_depth < 0 || rd->min_depth < 0) return fail(RT_ERR_INVALID, "rt_render_tile_static: negative depth");
     // PathTracingMIS keeps one round counter per bounce in the scratch;
     // VolPathTracing runs as one persistent kernel and needs one
@@ -4055,6 +4097,7 @@ extern "C" rt_status rt_render_tile_static(rt_ctx *ctx, rt_scene *sc, const rt_r
     Pm.n_paths = (int)paths;
     Pm.seed = rd->seed;
     Pm.max_depth = rd->max_depth;
+    Pm.all_lights = rd->integrator == RT_INTEGRATOR_PATH_MIS && rd->strategy == RT_STRATEGY_ALL_LIGHTS;
     Pm.min_depth = rd->min_depth;
     Pm.limit_flag = limit_flag;
     Pm.stats = stats;
@@ -4070,13 +4113,7 @@ extern "C" rt_status rt_render_tile_static(rt_ctx *ctx, rt_scene *sc, const rt_r
             launch_trace(trace_width(ctx, sc), Pm, r, false, false, sm * 12, st);
             launch_trace(trace_width(ctx, sc), Pm, r, true, false, sm * 12, st);
             k_pt_finish<<<blocks, 128, 0, st>>>(Pm, r);
-            if (sc->bsdf_types & 1) k_pt_shade<0><<<blocks, 128, 0, st>>>(Pm, r);
-            if (sc->bsdf_types & 2) k_pt_shade<1><<<blocks, 128, 0, st>>>(Pm, r);
-            if (sc->bsdf_types & 4) k_pt_shade<2><<<blocks, 128, 0, st>>>(Pm, r);
-            if (sc->bsdf_types & 8) k_pt_shade<3><<<blocks, 128, 0, st>>>(Pm, r);
-            if (sc->bsdf_types & 16) k_pt_shade<4><<<blocks, 128, 0, st>>>(Pm, r);
-            if (sc->bsdf_types & 32) k_pt_shade<5><<<blocks, 128, 0, st>>>(Pm, r);
-            if (sc->bsdf_types & (1 << RT_QUEUE_MIXED)) k_pt_shade<RT_QUEUE_MIXED><<<blocks, 128, 0, st>>>(Pm, r);
+            launch_shades(sc->bsdf_types, Pm, r, blocks, st);
             if ((s = launch_check("pt round (static)")) != RT_OK) return s;
             if ((r & 3) == 3 && r + 1 < rounds) {
                 RoundCounters nc;

@@ -411,6 +411,71 @@ def test_film_parity_volume(ctx, rtlib, vol):
     _film_parity(ctx, rtlib, vol, 2, 4, max_bad=0.002)   # measured 0
 
 
+def _all_lights_scene(width=48, height=40):
+    """The Cornell room with its area light, a point light, a spot light and
+    a sphere area light (lights on a mesh, on an analytic shape and delta
+    lights), a rough gold sphere among the boxes, under the all-lights
+    strategy."""
+    s = scenes.cornell_delta_lights(width, height)
+    gold = s.add_bsdf(D.bsdf(D.BSDF_ROUGH_CONDUCTOR, distribution=D.DIST_GGX, alpha=0.2,
+                             eta=scenes.AU_ETA, k=scenes.AU_K))
+    T = np.eye(4)
+    T[:3, 3] = (0.3, 0.12, 0.3)
+    s.add_sphere(0.12, T, bsdf=gold)
+    lm = s.add_bsdf(D.bsdf(D.BSDF_DIFFUSE, albedo=(0.0, 0.0, 0.0)))
+    T = np.eye(4)
+    T[:3, 3] = (0.75, 0.6, 0.25)
+    sp = s.add_sphere(0.06, T, bsdf=lm)
+    li = s.add_area_light((6.0, 5.0, 4.0), D.SHAPE_SPHERE, sp, mesh_light=False)
+    s.spheres[sp]["light"] = li
+    s.integrator = dict(s.integrator, strategy=D.STRATEGY_ALL_LIGHTS)
+    return s
+
+
+def test_film_parity_all_lights(ctx, rtlib):
+    """PathTracingMIS's all-lights strategy (PathTracingMIS.cpp:80-117):
+    every light sampled at every vertex, each with its own shadow ray and MIS
+    weight, against the oracle; also with graph launches."""
+    s = _all_lights_scene()
+    assert len(s.lights) == 4
+    fg, _ = _film_parity(ctx, rtlib, s, 4, 29, max_bad=0.002)
+    g = rtlib.Scene(ctx, s)
+    before = ctx.get_tuning()
+    try:
+        ctx.set_tuning(graphs=1)
+        assert np.array_equal(g.render(4, seed=29, block=16), fg)
+    finally:
+        ctx.set_tuning(**before)
+        g.close()
+
+
+def test_all_lights_strategy_tiles_and_volpath(ctx, rtlib):
+    """The all-lights strategy through the allocation-free tile render equals
+    the film's (per-path radiance: test_gpu_paths.py); VolPathTracing
+    takes the strategy as the reference does (uniform light selection, one
+    light per vertex), so its film equals the one-light-uniform film."""
+    torch = pytest.importorskip("torch")
+    s = _all_lights_scene(32, 32)
+    g = rtlib.Scene(ctx, s)
+    ref = g.render(2, seed=5, block=16)
+    film = torch.zeros((32, 32, 4), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    g.render_tile_static(1, 0, film.data_ptr(), 2, seed=5, block=16)
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(film.cpu().numpy()[0:16, 16:32], ref[0:16, 16:32], rtol=1e-5, atol=1e-7)
+    g.close()
+    v = _all_lights_scene(24, 24)
+    v.integrator = dict(v.integrator, integrator=D.INTEGRATOR_VOLPATH)
+    gv = rtlib.Scene(ctx, v)
+    a = gv.render(2, seed=3)
+    v.integrator = dict(v.integrator, strategy=D.STRATEGY_ONE_LIGHT_UNIFORM)
+    gv.close()
+    gv = rtlib.Scene(ctx, v)
+    b = gv.render(2, seed=3)
+    gv.close()
+    assert np.array_equal(a, b)
+
+
 def test_film_parity_stacked_media(ctx, rtlib):
     """Transmittance rays through five stacked media (many null-boundary
     segments, zero transmittance between segments, blocked light samples)

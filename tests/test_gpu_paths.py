@@ -19,8 +19,10 @@ pytestmark = pytest.mark.gpu
 
 
 def _cases():
+    from test_gpu_parity import _all_lights_scene
     return {
         "cornell": (scenes.cornell_box(48, 40), 4),
+        "all_lights": (_all_lights_scene(), 2),
         "icosphere_env": (scenes.displaced_icosphere(level=4, width=40, height=40, env_size=(128, 64)), 2),
         "volume": (scenes.volume_grid(40, 32, res=32), 2),
     }
@@ -31,7 +33,7 @@ def _rel(a, b):
     return (np.abs(a - b) / np.maximum(np.abs(b), 1e-3)).max(-1)
 
 
-@pytest.mark.parametrize("name", ["cornell", "icosphere_env", "volume"])
+@pytest.mark.parametrize("name", ["cornell", "all_lights", "icosphere_env", "volume"])
 def test_paths_match_oracle(ctx, rtlib, name):
     s, spp = _cases()[name]
     W, H = s.camera["width"], s.camera["height"]
