@@ -121,3 +121,27 @@ def test_xml_roundtrip_delta_lights(built, tmp_path):
     u = load_scene(str(tmp_path / "c.xml"))
     spot = [L for L in u.lights if L["type"] == D.LIGHT_SPOT][0]
     assert spot["falloff_start"] == 30.0 and spot["total_width"] == 60.0
+
+
+def test_all_lights_with_one_light_equals_one_light_uniform(built):
+    """With a single light, the all-lights loop (PathTracingMIS.cpp:80-117)
+    draws the same 2-D sample and takes the same pdf as one-light-uniform
+    selection (a one-entry light CDF maps u to itself with weight 1), so the
+    oracle's films are identical; with several lights the two strategies
+    differ but converge to the same image."""
+    s = scenes.cornell_box(24, 20)
+    assert len(s.lights) == 1
+    o = O.OracleScene(s)
+    a = o.render(4, seed=3, strategy=D.STRATEGY_ALL_LIGHTS)
+    b = o.render(4, seed=3, strategy=D.STRATEGY_ONE_LIGHT_UNIFORM)
+    o.close()
+    assert np.array_equal(a, b)
+    m = scenes.cornell_delta_lights(16, 16)
+    assert len(m.lights) == 3
+    o = O.OracleScene(m)
+    a = o.render(64, seed=1, strategy=D.STRATEGY_ALL_LIGHTS)
+    b = o.render(64, seed=1, strategy=D.STRATEGY_ONE_LIGHT_UNIFORM)
+    o.close()
+    assert not np.array_equal(a, b)
+    ma, mb = a[..., :3].sum() / a[..., 3].sum(), b[..., :3].sum() / b[..., 3].sum()
+    assert abs(ma / mb - 1) < 0.05
